@@ -1,0 +1,176 @@
+/*
+ * rdxg.h -- C ABI of the GB300 MOMFBD per-patch solver core.
+ *
+ * A drop-in for the per-patch work of redux's momfbd::Solver
+ * (include/redux/momfbd/solver.hpp:86-179 in ISP-SST/redux): the caller (the job/worker
+ * layer, unchanged) hands over the static job data that redux keeps in GlobalData (modes,
+ * pupil, supports, constraint null space) once, then batches of patches (the float32
+ * image cutouts of PatchData), and receives the mode coefficients, metric histories and
+ * per-patch reports that Solver::run stores back into PatchData.
+ *
+ * Plain pointers and sizes only; every function returns an rdxg_status and never throws.
+ * All host pointers are read or written synchronously before the call returns unless the
+ * function says otherwise.  One handle per host thread; each handle owns one CUDA stream.
+ */
+#ifndef RDXG_H
+#define RDXG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    RDXG_OK = 0,
+    RDXG_ERR_ARG = 1,          /* bad argument or shape */
+    RDXG_ERR_UNSUPPORTED = 2,  /* size not supported by the compiled kernels */
+    RDXG_ERR_CUDA = 3,         /* CUDA runtime error (message in rdxg_last_error) */
+    RDXG_ERR_STATE = 4,        /* call out of order (e.g. solve before set_patches) */
+    RDXG_ERR_NONFINITE = 5,    /* non-finite metric or gradient */
+    RDXG_ERR_NOMEM = 6
+} rdxg_status;
+
+typedef enum { RDXG_FP32 = 0, RDXG_FP64 = 1 } rdxg_precision;
+
+/* gradient methods: the reference's analytic gradient (Vogel weights), the exact
+ * derivative of the metric, and the reference's one-sided finite differences */
+typedef enum { RDXG_GRAD_VOGEL = 0, RDXG_GRAD_EXACT = 1, RDXG_GRAD_FD = 2 } rdxg_grad_method;
+
+typedef struct rdxg_solver rdxg_solver;
+
+/* Geometry of a job: sizes that redux derives in MomfbdJob/Object::initProcessing. */
+typedef struct {
+    int32_t otf_size;      /* N = 2 * pupil_pixels (Solver::otfSize) */
+    int32_t pupil_pixels;  /* n (job.pupilPixels) */
+    int32_t patch_size;    /* image size; must equal otf_size */
+    int32_t n_modes;       /* M */
+    int32_t n_objects;
+    int32_t n_images;      /* I: all images of all objects/channels of one patch */
+    int32_t n_channels;    /* C: all channels of all objects */
+    int32_t tilt_x;        /* index of the x-tilt mode (ModeSet::tiltMode.x), -1 if none */
+    int32_t tilt_y;
+    int32_t n_free;        /* columns of the null-space map (Constraints::nFreeParameters) */
+    int32_t cutout_size;   /* image cutout size incl. the max-local-shift margins */
+    int32_t max_patches;   /* batch capacity */
+    int32_t precision;     /* rdxg_precision */
+    int32_t device;        /* CUDA device ordinal */
+} rdxg_geometry;
+
+/* Static inputs (host pointers, copied by rdxg_create). */
+typedef struct {
+    const double* modes;          /* [M][n][n], already scaled by 1/lambda (GlobalData::get) */
+    const double* pupil;          /* [n][n] Pupil */
+    int32_t n_pupil_support;
+    const int32_t* pupil_support; /* Pupil::pupilSupport, indices into n*n */
+    int32_t n_otf_support;
+    const int32_t* otf_support;   /* Pupil::otfSupport, indices into the centred N*N OTF */
+    const int32_t* image_object;  /* [I] object of each image (images of an object contiguous) */
+    const int32_t* image_channel; /* [I] global channel index of each image */
+    const double* phi_fixed;      /* [C][n][n] Channel::phi_fixed (diversity) */
+    const double* object_weight;  /* [nObj] Object::weight */
+    const double* object_grad_step; /* [nObj] GRADDIFF_STEP * wavelength (SubImage::grad_step) */
+    const double* window;         /* [ps][ps] Solver::window */
+    const double* noise_window;   /* [ps][ps] Solver::noiseWindow */
+    int64_t ns_nnz;               /* Constraints::ns_entries: alpha[row] += val * beta[col] */
+    const int32_t* ns_rows;
+    const int32_t* ns_cols;
+    const double* ns_vals;
+    const double* tilt_jacobian;  /* [2][2] ModeSet::J_T_xy (alpha -> pixel shift), or NULL */
+} rdxg_static;
+
+/* Solver settings (GlobalCfg fields read by Solver::run, config.hpp:196-228). */
+typedef struct {
+    int32_t mode_start;        /* MODE_START */
+    int32_t mode_step;         /* MODE_STEP */
+    int32_t max_iterations;    /* MAX_ITER */
+    int32_t min_iterations;    /* MIN_ITER */
+    int32_t target_iterations; /* N_DONE_ITER */
+    int32_t fd_first;          /* 1: first gradient by finite differences (the reference) */
+    int32_t max_metrics;       /* capacity of the per-patch metric history */
+    int32_t check_every;       /* rounds between host checks for completion (0: 8) */
+    double ftol;               /* FTOL */
+    double eps;                /* EPS */
+} rdxg_solve_params;
+
+/* Per-patch outcome (what Solver::run logs and stores in PatchData). */
+typedef struct {
+    double initial_metric;
+    double final_metric;       /* PatchData::finalMetric */
+    int32_t iterations;        /* total CG iterations */
+    int32_t status;            /* 0 ok, 1 gave up after too many failures */
+    int32_t n_f_evals;         /* metric evaluations */
+    int32_t n_df_evals;        /* gradient evaluations */
+    int32_t fail_count;
+    int32_t n_metrics;         /* entries of the metric history (PatchData::metrics) */
+} rdxg_patch_report;
+
+int rdxg_version(void);
+
+/* Replaces Solver::Solver + Solver::init (solver.cpp:63-181). */
+int rdxg_create(const rdxg_geometry* geometry, const rdxg_static* statics, rdxg_solver** out);
+int rdxg_destroy(rdxg_solver* h);
+const char* rdxg_last_error(const rdxg_solver* h);
+
+/* Work on a caller-provided CUDA stream (cudaStream_t); NULL restores the handle's own. */
+int rdxg_set_stream(rdxg_solver* h, void* cuda_stream);
+
+/* Loads a batch of patches: Channel::initPatch + Solver::shiftAndInit(alpha_offset, true)
+ * (channel.cpp:846-953, solver.cpp:583-605, subimage.cpp:155-209).
+ * cutouts: [P][I][cutout][cutout] float32 (PatchData channel images);
+ * residual_alpha: [P][I][2] (y, x) channel residual tilt coefficients or NULL;
+ * fixed_gamma: [P][nObj] regularisation overriding the noise-derived one, or NULL. */
+int rdxg_set_patches(rdxg_solver* h, int32_t n_patches, const float* cutouts,
+                     const double* residual_alpha, const double* fixed_gamma);
+
+/* Same, with the cutouts already in device memory (no host copy). */
+int rdxg_set_patches_device(rdxg_solver* h, int32_t n_patches, const float* d_cutouts,
+                            const double* residual_alpha, const double* fixed_gamma);
+
+/* Metric of every patch at alpha [P][I][M] (Solver::applyAlpha + Solver::metric,
+ * solver.cpp:219-225, 763-817).  metric: [P]. */
+int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric);
+
+/* Gradient in alpha space [P][I][M] at alpha (Solver::my_df without the constraint map,
+ * solver.cpp:228-234, 860-894); enabled: [M] flags or NULL (all); metric: [P] or NULL. */
+int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, int32_t method,
+                  double* grad, double* metric);
+
+/* Full per-patch solve (Solver::run, solver.cpp:330-580) for every loaded patch.
+ * alpha_out: [P][I][M]; reports: [P]; metrics: [P][max_metrics] or NULL. */
+int rdxg_solve(rdxg_solver* h, const rdxg_solve_params* params, double* alpha_out,
+               rdxg_patch_report* reports, double* metrics);
+
+/* Same, leaving the results on the device; rdxg_fetch_results copies them out. */
+int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* params);
+int rdxg_fetch_results(rdxg_solver* h, double* alpha_out, rdxg_patch_report* reports,
+                       double* metrics);
+
+/* Number of kernel launches issued by the last rdxg_solve / rdxg_solve_async. */
+int64_t rdxg_last_launch_count(const rdxg_solver* h);
+
+/* Debug copies of device state (host buffers sized by the caller):
+ * which = 0 D [P][I][N][N] complex, 1 OTF [P][I][N][N] complex, 2 gamma [P][nObj],
+ *         3 image stats [P][I][3] (mean, stddev, noise), 4 object O [P][nObj][N][N] complex,
+ *         5 shifts [P][I][2] int32.  Complex values are float pairs in FP32 mode and
+ *         double pairs in FP64 mode. */
+int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes);
+
+/* Host drop-in for redux's conjugate_rdx minimiser with the Solver::run stage loop
+ * (conjugate_gradient.cpp:128-256, helpers.cpp:58-215, solver.cpp:425-537) driving
+ * caller-supplied callbacks.  n_modes stages the enabled-mode count exactly as Solver::run;
+ * df receives the number of enabled modes.  Writes x (n_free), the metric history and a
+ * report.  Used for host-side validation of the device state machine. */
+typedef double (*rdxg_f_fn)(const double* x, void* user);
+typedef void (*rdxg_df_fn)(const double* x, int32_t method, int32_t mode_count, double* g, void* user);
+typedef void (*rdxg_shift_fn)(const double* x, void* user);
+int rdxg_cg_minimize(int32_t n_free, int32_t n_modes, const rdxg_solve_params* params,
+                     double grad_scale, rdxg_f_fn f, rdxg_df_fn df, rdxg_shift_fn shift,
+                     void* user, double* x_out, rdxg_patch_report* report, double* metrics);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RDXG_H */

@@ -1,0 +1,245 @@
+"""ctypes front-end of the FP64 CPU oracle (oracle.c).
+
+TEST INFRASTRUCTURE ONLY: the checker for the GPU solver.  Only tests/, the smoke
+check in __graft_entry__ and bench.py's CPU-baseline leg may use it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+
+
+class Geom(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in (
+        "otf_size", "pupil_pixels", "patch_size", "n_modes", "n_objects", "n_images",
+        "n_channels", "tilt_x", "tilt_y", "n_free", "cutout_size", "pad")]
+
+
+class Cfg(C.Structure):
+    _fields_ = [("n_initial_modes", C.c_int32), ("n_mode_increment", C.c_int32),
+                ("max_iterations", C.c_int32), ("min_iterations", C.c_int32),
+                ("target_iterations", C.c_int32), ("fd_first", C.c_int32),
+                ("ftol", C.c_double), ("eps", C.c_double), ("brent_tol", C.c_double)]
+
+
+class Report(C.Structure):
+    _fields_ = [("initial_metric", C.c_double), ("final_metric", C.c_double),
+                ("iterations", C.c_int32), ("status", C.c_int32), ("n_f_evals", C.c_int32),
+                ("n_df_evals", C.c_int32), ("fail_count", C.c_int32), ("n_metrics", C.c_int32)]
+
+
+def build():
+    """Compile liboracle.so in place (gcc, optional OpenMP)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(os.path.join(_HERE, "oracle.c")):
+            build()
+        L = C.CDLL(path)
+        L.orc_fft2.argtypes = [f64p, C.c_int, C.c_int, C.c_int]
+        L.orc_reorder.argtypes = [f64p, C.c_int, C.c_int, C.c_int]
+        L.orc_autocorrelate.argtypes = [f64p, C.c_int, C.c_int, C.c_int]
+        L.orc_create.restype = C.c_void_p
+        L.orc_create.argtypes = [C.POINTER(Geom), f64p, f64p, C.c_int, i32p, C.c_int, i32p,
+                                 i32p, i32p, f64p, f64p, f64p, f64p, f64p,
+                                 C.c_long, i32p, i32p, f64p, C.c_void_p]
+        L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_set_threads.argtypes = [C.c_void_p, C.c_int]
+        L.orc_set_images.argtypes = [C.c_void_p, f32p, f64p, C.c_void_p]
+        L.orc_metric.restype = C.c_double
+        L.orc_metric.argtypes = [C.c_void_p, f64p]
+        L.orc_gradient.restype = C.c_double
+        L.orc_gradient.argtypes = [C.c_void_p, f64p, C.c_void_p, C.c_int, f64p]
+        L.orc_solve.restype = C.c_int
+        L.orc_solve.argtypes = [C.c_void_p, C.POINTER(Cfg), f64p, C.POINTER(Report),
+                                C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+        for nm in ("orc_get_D", "orc_get_otf", "orc_get_pf", "orc_get_ftsum", "orc_get_gamma",
+                   "orc_get_otfnorm"):
+            getattr(L, nm).argtypes = [C.c_void_p, f64p]
+        L.orc_get_pq.argtypes = [C.c_void_p, f64p, f64p]
+        L.orc_get_stats.argtypes = [C.c_void_p, f64p, f64p, f64p]
+        L.orc_get_shifts.argtypes = [C.c_void_p, i32p, f64p]
+        L.orc_shift.argtypes = [C.c_void_p, f64p]
+        L.orc_cons_apply.argtypes = [C.c_void_p, f64p, f64p]
+        L.orc_cons_reverse_add.argtypes = [C.c_void_p, f64p, f64p, f64p]
+        _LIB = L
+    return _LIB
+
+
+def fft2(a: np.ndarray, sign: int = -1) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    buf = a.view(np.float64).copy()
+    lib().orc_fft2(buf, a.shape[0], a.shape[1], sign)
+    return buf.view(np.complex128).reshape(a.shape)
+
+
+def reorder(a: np.ndarray) -> np.ndarray:
+    if np.iscomplexobj(a):
+        buf = np.ascontiguousarray(a, np.complex128).view(np.float64).copy()
+        lib().orc_reorder(buf, a.shape[0], a.shape[1], 1)
+        return buf.view(np.complex128).reshape(a.shape)
+    buf = np.ascontiguousarray(a, np.float64).copy()
+    lib().orc_reorder(buf, a.shape[0], a.shape[1], 0)
+    return buf
+
+
+def autocorrelate(a: np.ndarray, center: bool = False) -> np.ndarray:
+    buf = np.ascontiguousarray(a, np.float64).copy()
+    lib().orc_autocorrelate(buf, a.shape[0], a.shape[1], int(center))
+    return buf
+
+
+def default_cfg(max_iterations=50, n_initial_modes=None, n_modes=None, min_iterations=None,
+                ftol=0.0, eps=1e-10, target_iterations=3, n_mode_increment=5, fd_first=1):
+    """Solver settings; ``max_iterations`` fixed iterations with FTOL = 0 by default."""
+    if n_initial_modes is None:
+        n_initial_modes = n_modes
+    return Cfg(n_initial_modes=n_initial_modes, n_mode_increment=n_mode_increment,
+               max_iterations=max_iterations,
+               min_iterations=max_iterations if min_iterations is None else min_iterations,
+               target_iterations=target_iterations, fd_first=fd_first, ftol=ftol, eps=eps,
+               brent_tol=0.1)
+
+
+class OraclePatch:
+    """One patch of a job in the FP64 oracle."""
+
+    def __init__(self, job, threads: int = 1):
+        L = lib()
+        self.job = job
+        g = Geom(otf_size=job.otf_size, pupil_pixels=job.pupil_pixels, patch_size=job.patch_size,
+                 n_modes=job.n_modes, n_objects=job.n_objects, n_images=job.n_images,
+                 n_channels=job.n_channels, tilt_x=job.tilt_x, tilt_y=job.tilt_y,
+                 n_free=job.nullspace.n_free, cutout_size=job.cutout_size, pad=0)
+        self._keep = []
+        sup = job.support
+
+        def c(a, dt):
+            a = np.ascontiguousarray(a, dt)
+            self._keep.append(a)
+            return a
+
+        J = c(job.J_T_xy.ravel(), np.float64)
+        self.h = L.orc_create(C.byref(g), c(job.modes, np.float64), c(job.pupil, np.float64),
+                              int(sup.pupil_support.size), c(sup.pupil_support, np.int32),
+                              int(sup.otf_support.size), c(sup.otf_support, np.int32),
+                              c(job.img_object, np.int32), c(job.img_channel, np.int32),
+                              c(job.phi_fixed, np.float64), c(job.obj_weight, np.float64),
+                              c(job.obj_grad_step, np.float64), c(job.window, np.float64),
+                              c(job.noise_window, np.float64), int(job.nullspace.vals.size),
+                              c(job.nullspace.rows, np.int32), c(job.nullspace.cols, np.int32),
+                              c(job.nullspace.vals, np.float64), J.ctypes.data)
+        L.orc_set_threads(self.h, threads)
+        self.N, self.n = job.otf_size, job.pupil_pixels
+        self.I, self.M, self.nObj = job.n_images, job.n_modes, job.n_objects
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def set_images(self, cutouts, residual_alpha=None, fixed_gamma=None):
+        cut = np.ascontiguousarray(cutouts, np.float32)
+        ra = np.ascontiguousarray(residual_alpha if residual_alpha is not None
+                                  else np.zeros((self.I, 2)), np.float64)
+        fg = None
+        if fixed_gamma is not None:
+            fg = np.ascontiguousarray(fixed_gamma, np.float64)
+            self._fg = fg
+        lib().orc_set_images(self.h, cut, ra, fg.ctypes.data if fg is not None else None)
+
+    def metric(self, alpha) -> float:
+        return lib().orc_metric(self.h, np.ascontiguousarray(alpha, np.float64).ravel())
+
+    def gradient(self, alpha, method="vogel", enabled=None):
+        g = np.zeros(self.I * self.M)
+        en = None
+        if enabled is not None:
+            en = np.ascontiguousarray(enabled, np.uint8)
+        f = lib().orc_gradient(self.h, np.ascontiguousarray(alpha, np.float64).ravel(),
+                               en.ctypes.data if en is not None else None,
+                               2 if method == "vogel" else 1, g)
+        return f, g.reshape(self.I, self.M)
+
+    def solve(self, cfg, log_evals=False, cap=200000):
+        alpha = np.zeros(self.I * self.M)
+        rep = Report()
+        metrics = np.zeros(100000)
+        ev = np.zeros(2 * cap) if log_evals else None
+        lib().orc_solve(self.h, C.byref(cfg), alpha, C.byref(rep), metrics.ctypes.data, metrics.size,
+                        ev.ctypes.data if ev is not None else None, cap if log_evals else 0)
+        out = dict(alpha=alpha.reshape(self.I, self.M), report=rep,
+                   metrics=metrics[:rep.n_metrics].copy())
+        if log_evals:
+            out["evals"] = ev.reshape(-1, 2)
+        return out
+
+    def _get(self, name, shape, cplx=False):
+        n = int(np.prod(shape)) * (2 if cplx else 1)
+        buf = np.zeros(n)
+        getattr(lib(), name)(self.h, buf)
+        return (buf.view(np.complex128) if cplx else buf).reshape(shape)
+
+    def D(self):
+        return self._get("orc_get_D", (self.I, self.N, self.N), True)
+
+    def otf(self):
+        return self._get("orc_get_otf", (self.I, self.N, self.N), True)
+
+    def pf(self):
+        return self._get("orc_get_pf", (self.I, self.n, self.n), True)
+
+    def ftsum(self):
+        return self._get("orc_get_ftsum", (self.nObj, self.N, self.N))
+
+    def gamma(self):
+        return self._get("orc_get_gamma", (self.nObj,))
+
+    def otfnorm(self):
+        return self._get("orc_get_otfnorm", (self.job.n_channels,))
+
+    def pq(self):
+        P = np.zeros(self.nObj * self.N * self.N * 2)
+        Q = np.zeros(self.nObj * self.N * self.N)
+        lib().orc_get_pq(self.h, P, Q)
+        return P.view(np.complex128).reshape(self.nObj, self.N, self.N), Q.reshape(self.nObj, self.N, self.N)
+
+    def cons_reverse_add(self, beta, offset):
+        out = np.zeros(self.I * self.M)
+        lib().orc_cons_reverse_add(self.h, np.ascontiguousarray(beta, np.float64),
+                                   np.ascontiguousarray(offset, np.float64).ravel(), out)
+        return out
+
+    def cons_apply(self, galpha):
+        out = np.zeros(self.job.nullspace.n_free)
+        lib().orc_cons_apply(self.h, np.ascontiguousarray(galpha, np.float64).ravel(), out)
+        return out
+
+    def shift(self, alpha):
+        lib().orc_shift(self.h, np.ascontiguousarray(alpha, np.float64).ravel())
+
+    def shifts(self):
+        s = np.zeros(2 * self.I, np.int32)
+        t = np.zeros(2 * self.I)
+        lib().orc_get_shifts(self.h, s, t)
+        return s.reshape(self.I, 2), t.reshape(self.I, 2)
+
+    def stats(self):
+        m, s, n = np.zeros(self.I), np.zeros(self.I), np.zeros(self.I)
+        lib().orc_get_stats(self.h, m, s, n)
+        return m, s, n

@@ -1,0 +1,1356 @@
+/*
+ * oracle.c -- FP64 CPU restatement of redux's per-patch MOMFBD solver.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU solver in
+ * redux_gb300: only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg may load it.  The product never links, imports or calls it.
+ *
+ * It restates, in plain C99 and double precision, the reference code of the
+ * MOMFBD hot path (paths relative to the ISP-SST/redux tree):
+ *   src/lib/momfbd/subimage.cpp    getWindowedImg 106-150, initialize 155-209,
+ *                                  addPQ 226-234, metricChange 261-278,
+ *                                  gradientFiniteDifference 281-292,
+ *                                  gradientVogel 312-326, calcVogelWeight 348-390,
+ *                                  adjustShifts 444-480, addToPhi/calcPhi 509-544,
+ *                                  calcOTF 567-583, calcPFOTF 586-612
+ *   src/lib/momfbd/object.cpp      initPQ 459, addRegGamma 465, addToFT 471,
+ *                                  addDiffToFT 482, addToPQ 508, calcHelpers 531,
+ *                                  calcMetric 597-615, reInitialize 885-904
+ *   src/lib/momfbd/solver.cpp      run 330-580, applyBeta 662, metric 763-817,
+ *                                  calcPQ 820-857, gradient 860-902
+ *   src/lib/momfbd/channel.cpp     initPatch (phi_channel, otfNormalization) 846-953
+ *   include/redux/momfbd/constraints.hpp  apply/reverse/reverseAndAdd 128-159
+ *   src/lib/util/gsl/conjugate_gradient.cpp  conjugate_rdx_set 72-86,
+ *                                  take_step/value_at 106-123, iterate 128-256
+ *   src/lib/math/helpers.cpp       bracket 58-129, brent 133-215
+ *   src/lib/image/fouriertransform.cpp  noise 448-495; fouriertransform.hpp
+ *                                  reorderInto 112-171, autocorrelate 281-286
+ *
+ * Third-party arithmetic: the reference transforms with FFTW3 (unpinned
+ * version; fftw_plan_dft_2d, FFTW_MEASURE).  FFTW computes the plain DFT
+ * X[k] = sum_x x[x] exp(-2 pi i k.x/N) (forward) and the unnormalised inverse
+ * with exp(+...); this file implements the same DFT with its own mixed-radix
+ * recursive FFT, pinned by the known-answer tests of
+ * testsuite/image/fourier.cpp restated in tests/test_oracle_fft.py.
+ *
+ * Parity status: the FFT/autocorrelation/reorder conventions are pinned by the
+ * reference's known-answer tests.  The reference has no tests for the metric,
+ * gradient, CG or line search, and it cannot be built here (Boost, FFTW3, GSL
+ * and OpenCV are absent), so those parts are "parity unpinned": they follow the
+ * cited source line by line and are cross-checked against an independent
+ * numpy restatement (oracle/np_oracle.py) and against finite differences.
+ */
+#include <complex.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef double complex cplx;
+
+/* ------------------------------------------------------------------------- */
+/* FFT: recursive mixed-radix decimation in time (any length).               */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+    int n;
+    int nfac;
+    int fac[40];
+    cplx* tw_fwd; /* exp(-2 pi i k / n), k < n */
+    cplx* tw_bwd; /* exp(+2 pi i k / n) */
+} fft_plan;
+
+static void plan_init(fft_plan* p, int n) {
+    p->n = n;
+    p->nfac = 0;
+    int m = n;
+    /* radix-4 first (fewer stages), then 2, 3, 5, ..., any prime */
+    while (m % 4 == 0) { p->fac[p->nfac++] = 4; m /= 4; }
+    while (m % 2 == 0) { p->fac[p->nfac++] = 2; m /= 2; }
+    for (int f = 3; m > 1; f += 2) {
+        while (m % f == 0) { p->fac[p->nfac++] = f; m /= f; }
+    }
+    p->tw_fwd = (cplx*)malloc(sizeof(cplx) * (size_t)n);
+    p->tw_bwd = (cplx*)malloc(sizeof(cplx) * (size_t)n);
+    for (int k = 0; k < n; ++k) {
+        double a = 2.0 * M_PI * (double)k / (double)n;
+        p->tw_fwd[k] = cos(a) - I * sin(a);
+        p->tw_bwd[k] = cos(a) + I * sin(a);
+    }
+}
+
+static void plan_free(fft_plan* p) {
+    free(p->tw_fwd);
+    free(p->tw_bwd);
+    p->tw_fwd = p->tw_bwd = NULL;
+}
+
+/* out[0..L) = DFT_L of in[q*istride]; fi = index into p->fac; L = prod fac[fi..] */
+static void fft_rec(const fft_plan* p, const cplx* tw, cplx* out, const cplx* in, long istride,
+                    int fi, long L, long fstride) {
+    int r = p->fac[fi];
+    long m = L / r;
+    if (m == 1) {
+        for (int q = 0; q < r; ++q) out[q] = in[q * istride];
+    } else {
+        for (int q = 0; q < r; ++q)
+            fft_rec(p, tw, out + q * m, in + q * istride, istride * r, fi + 1, m, fstride * r);
+    }
+    const int N = p->n;
+    cplx t[64];
+    cplx* tt = (r <= 64) ? t : (cplx*)malloc(sizeof(cplx) * (size_t)r);
+    for (long k = 0; k < m; ++k) {
+        for (int q = 0; q < r; ++q) {
+            long e = ((long)q * k * fstride) % N;
+            tt[q] = out[q * m + k] * tw[e];
+        }
+        if (r == 2) {
+            out[k] = tt[0] + tt[1];
+            out[k + m] = tt[0] - tt[1];
+        } else if (r == 4) {
+            /* w = exp(sign 2 pi i / 4): sign taken from tw[N/4] */
+            cplx w = tw[N / 4];
+            cplx a0 = tt[0] + tt[2], a1 = tt[0] - tt[2];
+            cplx b0 = tt[1] + tt[3], b1 = (tt[1] - tt[3]) * w;
+            out[k] = a0 + b0;
+            out[k + m] = a1 + b1;
+            out[k + 2 * m] = a0 - b0;
+            out[k + 3 * m] = a1 - b1;
+        } else {
+            long step = N / r;
+            for (int u = 0; u < r; ++u) {
+                cplx s = 0;
+                for (int q = 0; q < r; ++q) s += tt[q] * tw[((long)q * u * step) % N];
+                out[k + u * m] = s;
+            }
+        }
+    }
+    if (tt != t) free(tt);
+}
+
+/* in-place 1-D transform of x[0..n) with stride; sign<0 forward (FFTW_FORWARD) */
+static void fft1(const fft_plan* p, cplx* x, long stride, int sign, cplx* work, cplx* work2) {
+    const int n = p->n;
+    for (int i = 0; i < n; ++i) work[i] = x[i * stride];
+    fft_rec(p, sign < 0 ? p->tw_fwd : p->tw_bwd, work2, work, 1, 0, n, 1);
+    for (int i = 0; i < n; ++i) x[i * stride] = work2[i];
+}
+
+/* unnormalised 2-D transform of a ny x nx row-major array */
+static void fft2(const fft_plan* py, const fft_plan* px, cplx* a, int sign, cplx* work) {
+    const int ny = py->n, nx = px->n;
+    int mx = ny > nx ? ny : nx;
+    cplx* w1 = work;
+    cplx* w2 = work + mx;
+    for (int y = 0; y < ny; ++y) fft1(px, a + (long)y * nx, 1, sign, w1, w2);
+    for (int x = 0; x < nx; ++x) fft1(py, a + x, nx, sign, w1, w2);
+}
+
+/* reorderInto for even and odd sizes, same size in/out (fouriertransform.hpp:112-171,
+ * center=false, outSize==inSize): a quadrant swap, i.e. fftshift for even sizes. */
+static void reorder_c(cplx* a, int ny, int nx, cplx* buf) {
+    const int midY = ny / 2, midX = nx / 2, oddY = ny % 2, oddX = nx % 2;
+    /* out[(y + ny - midY - oddY) % ny][(x + nx - midX - oddX) % nx] = in[y][x] for the
+     * quadrant layout used by reorderInto: the lower block is one pixel larger for odd sizes. */
+    for (int y = 0; y < ny; ++y) {
+        int oy = (y + midY) % ny;  /* in row y goes to out row (y + midY) mod ny */
+        for (int x = 0; x < nx; ++x) {
+            int ox = (x + midX) % nx;
+            buf[(long)oy * nx + ox] = a[(long)y * nx + x];
+        }
+    }
+    (void)oddY; (void)oddX;
+    memcpy(a, buf, sizeof(cplx) * (size_t)ny * nx);
+}
+
+static void reorder_d(double* a, int ny, int nx, double* buf) {
+    const int midY = ny / 2, midX = nx / 2;
+    for (int y = 0; y < ny; ++y) {
+        int oy = (y + midY) % ny;
+        for (int x = 0; x < nx; ++x) {
+            int ox = (x + midX) % nx;
+            buf[(long)oy * nx + ox] = a[(long)y * nx + x];
+        }
+    }
+    memcpy(a, buf, sizeof(double) * (size_t)ny * nx);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Exported FFT helpers, used by the known-answer tests.                     */
+/* ------------------------------------------------------------------------- */
+
+/* data: interleaved complex, ny x nx; sign -1 forward, +1 backward (unnormalised) */
+void orc_fft2(double* data, int ny, int nx, int sign) {
+    fft_plan py, px;
+    plan_init(&py, ny);
+    plan_init(&px, nx);
+    int mx = ny > nx ? ny : nx;
+    cplx* work = (cplx*)malloc(sizeof(cplx) * 2 * (size_t)mx);
+    fft2(&py, &px, (cplx*)data, sign, work);
+    free(work);
+    plan_free(&py);
+    plan_free(&px);
+}
+
+void orc_reorder(double* data, int ny, int nx, int is_complex) {
+    if (is_complex) {
+        cplx* buf = (cplx*)malloc(sizeof(cplx) * (size_t)ny * nx);
+        reorder_c((cplx*)data, ny, nx, buf);
+        free(buf);
+    } else {
+        double* buf = (double*)malloc(sizeof(double) * (size_t)ny * nx);
+        reorder_d(data, ny, nx, buf);
+        free(buf);
+    }
+}
+
+/* FourierTransform::autocorrelate(in, out, center) (fouriertransform.hpp:281-286) for
+ * real input: ft (FULLCOMPLEX) -> |.|^2 -> ift normalised by 1/(ny*nx) -> real part ->
+ * optional reorder. */
+void orc_autocorrelate(double* data, int ny, int nx, int center) {
+    long np = (long)ny * nx;
+    cplx* c = (cplx*)malloc(sizeof(cplx) * (size_t)np);
+    for (long i = 0; i < np; ++i) c[i] = data[i];
+    orc_fft2((double*)c, ny, nx, -1);
+    for (long i = 0; i < np; ++i) c[i] = creal(c[i]) * creal(c[i]) + cimag(c[i]) * cimag(c[i]);
+    orc_fft2((double*)c, ny, nx, +1);
+    for (long i = 0; i < np; ++i) data[i] = creal(c[i]) / (double)np;
+    if (center) orc_reorder(data, ny, nx, 0);
+    free(c);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Patch model.                                                              */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+    int32_t otf_size;     /* N = 2 * pupil_pixels */
+    int32_t pupil_pixels; /* n */
+    int32_t patch_size;   /* image size, <= N */
+    int32_t n_modes;      /* M */
+    int32_t n_objects;
+    int32_t n_images;     /* I, all objects and channels */
+    int32_t n_channels;   /* C, all objects */
+    int32_t tilt_x, tilt_y;  /* mode indices of the tilts, -1 if absent */
+    int32_t n_free;       /* columns of the null-space map */
+    int32_t cutout_size;  /* size of the image cutouts incl. shift margins */
+    int32_t pad;
+} orc_geom;
+
+typedef struct {
+    int32_t n_initial_modes;   /* MODE_START */
+    int32_t n_mode_increment;  /* MODE_STEP */
+    int32_t max_iterations;    /* MAX_ITER */
+    int32_t min_iterations;    /* MIN_ITER */
+    int32_t target_iterations; /* N_DONE_ITER */
+    int32_t fd_first;          /* 1: first gradient evaluations by finite differences (as the reference) */
+    double ftol;               /* FTOL */
+    double eps;                /* EPS */
+    double brent_tol;          /* 0.1 in conjugate_gradient.cpp:231 */
+} orc_cfg;
+
+typedef struct {
+    double initial_metric;
+    double final_metric;
+    int32_t iterations;
+    int32_t status;   /* 0 ok, 1 gave up (failCount > maxFails) */
+    int32_t n_f_evals;
+    int32_t n_df_evals;
+    int32_t fail_count;
+    int32_t n_metrics;
+} orc_report;
+
+typedef struct {
+    cplx* otf;   /* N*N, centred (work / current OTF) */
+    cplx* pf;    /* n*n */
+    cplx* tmpc;  /* N*N */
+    cplx* tmpc2; /* N*N */
+    cplx* tmpc3; /* N*N */
+    double* tmpd;  /* max(N,cs)^2 */
+    double* tmpd2; /* max(N,cs)^2 */
+    double* phi;   /* n*n */
+    double* vogel; /* n*n */
+    cplx* work;    /* 2*N */
+} img_scratch;
+
+typedef struct {
+    orc_geom g;
+    int N, n, ps, M, nObj, nImg, nCh, cs, margin;
+    long N2, n2;
+    /* static */
+    double* modes;      /* M*n2 */
+    double* pupil;      /* n2 */
+    double area;
+    int nPupSup; int32_t* pupSup; int32_t* pupInOtf;
+    int nOtfSup; int32_t* otfSup;
+    int32_t* imgObj; int32_t* imgCh;
+    int32_t* objImgCount;
+    double* phiFixed;   /* nCh*n2 */
+    double* objWeight;  /* nObj */
+    double* objGradStep;/* nObj: graddiff_step * wavelength */
+    double* window; double* noiseWindow;  /* ps*ps */
+    double J_T_xy[2][2], J_xy_T[2][2];
+    int have_jacobian;
+    /* constraints (ns_entries): alpha[row] += val * beta[col] */
+    int nPar, nFree; long nnz; int32_t* nsRow; int32_t* nsCol; double* nsVal;
+    /* per patch */
+    float* cutouts;     /* nImg * cs * cs */
+    double* phiChannel; /* nImg * n2 */
+    double* otfNorm;    /* nCh */
+    int32_t* curShift;  /* nImg*2: (y,x) */
+    double* curTiltOffset; /* nImg*2: (y,x) currentTiltOffset */
+    double* statMean; double* statStd; double* statNoise; /* nImg */
+    cplx* D;            /* nImg*N2 centred image FT */
+    double* ftSum;      /* nObj*N2 */
+    double* regGamma;   /* nObj */
+    int fixed_gamma;
+    double* fixedGamma;
+    /* object work */
+    cplx* P; double* Q; cplx* PQ; double* PS; double* QS; /* nObj*N2 */
+    double* objMetric;
+    /* image state */
+    cplx* OTF;          /* nImg*N2 */
+    cplx* PF;           /* nImg*n2 */
+    double* PHI;        /* nImg*n2 */
+    /* solver vectors */
+    double* alpha; double* alphaOffset; double* gradAlpha; /* nPar */
+    uint8_t* enabled;
+    fft_plan planN, planPS;
+    img_scratch* scr;   /* per image */
+    int nthreads;
+    int64_t n_f, n_df;
+} orc_patch;
+
+static void* xcalloc(size_t n, size_t s) {
+    void* p = calloc(n ? n : 1, s);
+    if (!p) { fprintf(stderr, "oracle: out of memory\n"); abort(); }
+    return p;
+}
+
+void orc_destroy(orc_patch* p);
+
+/* pupInOtf is derived here from pupSup exactly as Pupil::generateSupport (pupil.cpp:245-262). */
+orc_patch* orc_create(const orc_geom* g, const double* modes, const double* pupil,
+                      int nPupSup, const int32_t* pupSup, int nOtfSup, const int32_t* otfSup,
+                      const int32_t* imgObj, const int32_t* imgCh, const double* phiFixed,
+                      const double* objWeight, const double* objGradStep,
+                      const double* window, const double* noiseWindow,
+                      long nnz, const int32_t* nsRow, const int32_t* nsCol, const double* nsVal,
+                      const double* J_T_xy /* 4 or NULL */) {
+    orc_patch* p = (orc_patch*)xcalloc(1, sizeof(orc_patch));
+    p->g = *g;
+    p->N = g->otf_size; p->n = g->pupil_pixels; p->ps = g->patch_size; p->M = g->n_modes;
+    p->nObj = g->n_objects; p->nImg = g->n_images; p->nCh = g->n_channels;
+    p->cs = g->cutout_size > 0 ? g->cutout_size : g->patch_size;
+    p->margin = (p->cs - p->ps) / 2;
+    p->N2 = (long)p->N * p->N; p->n2 = (long)p->n * p->n;
+    const long N2 = p->N2, n2 = p->n2;
+    p->modes = (double*)xcalloc((size_t)p->M * n2, sizeof(double));
+    memcpy(p->modes, modes, sizeof(double) * (size_t)p->M * n2);
+    p->pupil = (double*)xcalloc((size_t)n2, sizeof(double));
+    memcpy(p->pupil, pupil, sizeof(double) * (size_t)n2);
+    p->nPupSup = nPupSup;
+    p->pupSup = (int32_t*)xcalloc((size_t)nPupSup, sizeof(int32_t));
+    p->pupInOtf = (int32_t*)xcalloc((size_t)nPupSup, sizeof(int32_t));
+    p->area = 0;
+    for (int i = 0; i < nPupSup; ++i) {
+        int32_t c = pupSup[i];
+        p->pupSup[i] = c;
+        p->pupInOtf[i] = (c / p->n) * p->N + (c % p->n) + (p->n / 2) + (p->n / 2) * p->N;
+        p->area += pupil[c];
+    }
+    p->nOtfSup = nOtfSup;
+    p->otfSup = (int32_t*)xcalloc((size_t)nOtfSup, sizeof(int32_t));
+    memcpy(p->otfSup, otfSup, sizeof(int32_t) * (size_t)nOtfSup);
+    p->imgObj = (int32_t*)xcalloc((size_t)p->nImg, sizeof(int32_t));
+    p->imgCh = (int32_t*)xcalloc((size_t)p->nImg, sizeof(int32_t));
+    memcpy(p->imgObj, imgObj, sizeof(int32_t) * (size_t)p->nImg);
+    memcpy(p->imgCh, imgCh, sizeof(int32_t) * (size_t)p->nImg);
+    p->objImgCount = (int32_t*)xcalloc((size_t)p->nObj, sizeof(int32_t));
+    for (int i = 0; i < p->nImg; ++i) p->objImgCount[imgObj[i]]++;
+    p->phiFixed = (double*)xcalloc((size_t)p->nCh * n2, sizeof(double));
+    memcpy(p->phiFixed, phiFixed, sizeof(double) * (size_t)p->nCh * n2);
+    p->objWeight = (double*)xcalloc((size_t)p->nObj, sizeof(double));
+    memcpy(p->objWeight, objWeight, sizeof(double) * (size_t)p->nObj);
+    p->objGradStep = (double*)xcalloc((size_t)p->nObj, sizeof(double));
+    memcpy(p->objGradStep, objGradStep, sizeof(double) * (size_t)p->nObj);
+    long ps2 = (long)p->ps * p->ps;
+    p->window = (double*)xcalloc((size_t)ps2, sizeof(double));
+    p->noiseWindow = (double*)xcalloc((size_t)ps2, sizeof(double));
+    memcpy(p->window, window, sizeof(double) * (size_t)ps2);
+    memcpy(p->noiseWindow, noiseWindow, sizeof(double) * (size_t)ps2);
+    if (J_T_xy) {
+        p->have_jacobian = 1;
+        p->J_T_xy[0][0] = J_T_xy[0]; p->J_T_xy[0][1] = J_T_xy[1];
+        p->J_T_xy[1][0] = J_T_xy[2]; p->J_T_xy[1][1] = J_T_xy[3];
+        /* invert_2x2 */
+        double det = p->J_T_xy[0][0] * p->J_T_xy[1][1] - p->J_T_xy[0][1] * p->J_T_xy[1][0];
+        p->J_xy_T[0][0] = p->J_T_xy[1][1] / det;
+        p->J_xy_T[0][1] = -p->J_T_xy[0][1] / det;
+        p->J_xy_T[1][0] = -p->J_T_xy[1][0] / det;
+        p->J_xy_T[1][1] = p->J_T_xy[0][0] / det;
+    }
+    p->nPar = p->nImg * p->M;
+    p->nFree = g->n_free;
+    p->nnz = nnz;
+    p->nsRow = (int32_t*)xcalloc((size_t)nnz, sizeof(int32_t));
+    p->nsCol = (int32_t*)xcalloc((size_t)nnz, sizeof(int32_t));
+    p->nsVal = (double*)xcalloc((size_t)nnz, sizeof(double));
+    memcpy(p->nsRow, nsRow, sizeof(int32_t) * (size_t)nnz);
+    memcpy(p->nsCol, nsCol, sizeof(int32_t) * (size_t)nnz);
+    memcpy(p->nsVal, nsVal, sizeof(double) * (size_t)nnz);
+
+    p->cutouts = (float*)xcalloc((size_t)p->nImg * p->cs * p->cs, sizeof(float));
+    p->phiChannel = (double*)xcalloc((size_t)p->nImg * n2, sizeof(double));
+    p->otfNorm = (double*)xcalloc((size_t)p->nCh, sizeof(double));
+    p->curShift = (int32_t*)xcalloc((size_t)p->nImg * 2, sizeof(int32_t));
+    p->curTiltOffset = (double*)xcalloc((size_t)p->nImg * 2, sizeof(double));
+    p->statMean = (double*)xcalloc((size_t)p->nImg, sizeof(double));
+    p->statStd = (double*)xcalloc((size_t)p->nImg, sizeof(double));
+    p->statNoise = (double*)xcalloc((size_t)p->nImg, sizeof(double));
+    p->D = (cplx*)xcalloc((size_t)p->nImg * N2, sizeof(cplx));
+    p->ftSum = (double*)xcalloc((size_t)p->nObj * N2, sizeof(double));
+    p->regGamma = (double*)xcalloc((size_t)p->nObj, sizeof(double));
+    p->fixedGamma = (double*)xcalloc((size_t)p->nObj, sizeof(double));
+    p->P = (cplx*)xcalloc((size_t)p->nObj * N2, sizeof(cplx));
+    p->Q = (double*)xcalloc((size_t)p->nObj * N2, sizeof(double));
+    p->PQ = (cplx*)xcalloc((size_t)p->nObj * N2, sizeof(cplx));
+    p->PS = (double*)xcalloc((size_t)p->nObj * N2, sizeof(double));
+    p->QS = (double*)xcalloc((size_t)p->nObj * N2, sizeof(double));
+    p->objMetric = (double*)xcalloc((size_t)p->nObj, sizeof(double));
+    p->OTF = (cplx*)xcalloc((size_t)p->nImg * N2, sizeof(cplx));
+    p->PF = (cplx*)xcalloc((size_t)p->nImg * n2, sizeof(cplx));
+    p->PHI = (double*)xcalloc((size_t)p->nImg * n2, sizeof(double));
+    p->alpha = (double*)xcalloc((size_t)p->nPar, sizeof(double));
+    p->alphaOffset = (double*)xcalloc((size_t)p->nPar, sizeof(double));
+    p->gradAlpha = (double*)xcalloc((size_t)p->nPar, sizeof(double));
+    p->enabled = (uint8_t*)xcalloc((size_t)p->M, 1);
+    plan_init(&p->planN, p->N);
+    plan_init(&p->planPS, p->ps);
+    long big = N2 > (long)p->cs * p->cs ? N2 : (long)p->cs * p->cs;
+    p->scr = (img_scratch*)xcalloc((size_t)p->nImg, sizeof(img_scratch));
+    for (int i = 0; i < p->nImg; ++i) {
+        img_scratch* s = &p->scr[i];
+        s->otf = (cplx*)xcalloc((size_t)N2, sizeof(cplx));
+        s->pf = (cplx*)xcalloc((size_t)n2, sizeof(cplx));
+        s->tmpc = (cplx*)xcalloc((size_t)big, sizeof(cplx));
+        s->tmpc2 = (cplx*)xcalloc((size_t)big, sizeof(cplx));
+        s->tmpc3 = (cplx*)xcalloc((size_t)big, sizeof(cplx));
+        s->tmpd = (double*)xcalloc((size_t)big, sizeof(double));
+        s->tmpd2 = (double*)xcalloc((size_t)big, sizeof(double));
+        s->phi = (double*)xcalloc((size_t)n2, sizeof(double));
+        s->vogel = (double*)xcalloc((size_t)n2, sizeof(double));
+        int mx = p->N > p->cs ? p->N : p->cs;
+        s->work = (cplx*)xcalloc((size_t)4 * mx, sizeof(cplx));
+    }
+    p->nthreads = 1;
+    return p;
+}
+
+void orc_destroy(orc_patch* p) {
+    if (!p) return;
+    for (int i = 0; i < p->nImg; ++i) {
+        img_scratch* s = &p->scr[i];
+        free(s->otf); free(s->pf); free(s->tmpc); free(s->tmpc2); free(s->tmpc3);
+        free(s->tmpd); free(s->tmpd2); free(s->phi); free(s->vogel); free(s->work);
+    }
+    free(p->scr);
+    plan_free(&p->planN); plan_free(&p->planPS);
+    free(p->modes); free(p->pupil); free(p->pupSup); free(p->pupInOtf); free(p->otfSup);
+    free(p->imgObj); free(p->imgCh); free(p->objImgCount); free(p->phiFixed);
+    free(p->objWeight); free(p->objGradStep); free(p->window); free(p->noiseWindow);
+    free(p->nsRow); free(p->nsCol); free(p->nsVal);
+    free(p->cutouts); free(p->phiChannel); free(p->otfNorm); free(p->curShift);
+    free(p->curTiltOffset); free(p->statMean); free(p->statStd); free(p->statNoise);
+    free(p->D); free(p->ftSum); free(p->regGamma); free(p->fixedGamma);
+    free(p->P); free(p->Q); free(p->PQ); free(p->PS); free(p->QS); free(p->objMetric);
+    free(p->OTF); free(p->PF); free(p->PHI);
+    free(p->alpha); free(p->alphaOffset); free(p->gradAlpha); free(p->enabled);
+    free(p);
+}
+
+void orc_set_threads(orc_patch* p, int n) { p->nthreads = n > 0 ? n : 1; }
+
+/* ---------------- autocorrelation of an N x N complex array (in place) --------------- */
+/* FourierTransform::autocorrelate(inout, center=true), fouriertransform.hpp:281-286 */
+static void autocorr_inplace(orc_patch* p, cplx* a, img_scratch* s) {
+    const long N2 = p->N2;
+    fft2(&p->planN, &p->planN, a, -1, s->work);
+    for (long i = 0; i < N2; ++i) a[i] = creal(a[i]) * creal(a[i]) + cimag(a[i]) * cimag(a[i]);
+    fft2(&p->planN, &p->planN, a, +1, s->work);
+    const double nrm = 1.0 / (double)N2;
+    for (long i = 0; i < N2; ++i) a[i] *= nrm;
+    reorder_c(a, p->N, p->N, s->tmpc3);
+}
+
+/* SubImage::calcPFOTF (subimage.cpp:586-612) for image j, phase phi */
+static void calc_pf_otf(orc_patch* p, int j, double otfNorm, const double* phi, cplx* pf, cplx* otf,
+                        img_scratch* s) {
+    memset(pf, 0, sizeof(cplx) * (size_t)p->n2);
+    memset(otf, 0, sizeof(cplx) * (size_t)p->N2);
+    for (int i = 0; i < p->nPupSup; ++i) {
+        int32_t a = p->pupSup[i];
+        double A = p->pupil[a];
+        pf[a] = A * cos(phi[a]) + I * (A * sin(phi[a]));   /* std::polar(A, phi) */
+        otf[p->pupInOtf[i]] = otfNorm * pf[a];
+    }
+    (void)j;
+    autocorr_inplace(p, otf, s);
+}
+
+/* SubImage::calcOTF(otf, phi) (subimage.cpp:567-583) */
+static void calc_otf(orc_patch* p, double otfNorm, const double* phi, cplx* otf, img_scratch* s) {
+    memset(otf, 0, sizeof(cplx) * (size_t)p->N2);
+    for (int i = 0; i < p->nPupSup; ++i) {
+        int32_t a = p->pupSup[i];
+        double A = p->pupil[a] * otfNorm;
+        otf[p->pupInOtf[i]] = A * cos(phi[a]) + I * (A * sin(phi[a]));
+    }
+    autocorr_inplace(p, otf, s);
+}
+
+/* SubImage::calcPhi / addToPhi (subimage.cpp:509-544) */
+static void calc_phi(orc_patch* p, int j, const double* a, double* phi) {
+    const long n2 = p->n2;
+    memcpy(phi, p->phiChannel + (long)j * n2, sizeof(double) * (size_t)n2);
+    for (int m = 0; m < p->M; ++m) {
+        double al = a[m];
+        if (m == p->g.tilt_x) al += p->curTiltOffset[2 * j + 1];
+        else if (m == p->g.tilt_y) al += p->curTiltOffset[2 * j + 0];
+        if (fabs(al) > 0.0) {
+            const double* mp = p->modes + (long)m * n2;
+            for (long i = 0; i < n2; ++i) phi[i] = phi[i] + al * mp[i];
+        }
+    }
+}
+
+/* Channel::initPatch otfNormalization (channel.cpp:941-952) */
+static void compute_otf_norms(orc_patch* p) {
+    img_scratch* s = &p->scr[0];
+    double* zero = (double*)xcalloc((size_t)p->n2, sizeof(double));
+    for (int c = 0; c < p->nCh; ++c) {
+        calc_pf_otf(p, 0, 1.0, zero, s->pf, s->otf, s);
+        double mx = 0;
+        for (long i = 0; i < p->N2; ++i) { double v = cabs(s->otf[i]); if (v > mx) mx = v; }
+        p->otfNorm[c] = 1.0 / sqrt(mx);
+    }
+    free(zero);
+}
+
+/* ---------------- image initialisation (SubImage::initialize) ---------------- */
+
+/* FourierTransform::noise(-1,-1) for a FULLCOMPLEX, un-reordered ps x ps transform
+ * (fouriertransform.cpp:448-495) */
+static double ft_noise(const cplx* ft, int ny, int nx) {
+    int mask = (ny > nx ? ny : nx) / 6 + 1;
+    double limits = (double)ny * nx / 4.0;
+    int endX = nx - mask + 1, endY = ny - mask + 1;
+    double np = 0; long cnt = 0;
+    for (int x = mask; x < endX; ++x) {
+        double xx = (double)(x < nx - x ? x : nx - x);
+        xx *= xx;
+        for (int y = mask; y < endY; ++y) {
+            double yy = (double)(y < ny - y ? y : ny - y);
+            if (xx + yy * yy < limits) continue;
+            const cplx v = ft[(long)y * nx + x];
+            np += creal(v) * creal(v) + cimag(v) * cimag(v);
+            cnt++;
+        }
+    }
+    if (cnt) np = sqrt(np / ((double)cnt * ny * nx));
+    return np;
+}
+
+/* mean and stddev as ArrayStats ST_VALUES|ST_RMS (arraystats.cpp:60-80) */
+static void img_stats(const double* x, long n, double* mean, double* stddev) {
+    double s = 0, s2 = 0;
+    for (long i = 0; i < n; ++i) { s += x[i]; s2 += x[i] * x[i]; }
+    double m = s / n, r = s2 / n;
+    *mean = m;
+    *stddev = sqrt(r - m * m);
+}
+
+/* SubImage::initialize(o, doReset) (subimage.cpp:155-209) with getWindowedImg (106-150);
+ * returns the contribution rg to reg_gamma when doReset. */
+static void init_image(orc_patch* p, int j, int doReset, double* rg_out, cplx* oldFT) {
+    img_scratch* s = &p->scr[j];
+    const int ps = p->ps, N = p->N, cs = p->cs;
+    const long ps2 = (long)ps * ps;
+    double* img = s->tmpd;
+    /* the view: patch-size window at (margin + shift) inside the cutout */
+    const int oy = p->margin + p->curShift[2 * j + 0];
+    const int ox = p->margin + p->curShift[2 * j + 1];
+    const float* cut = p->cutouts + (long)j * cs * cs;
+    for (int y = 0; y < ps; ++y)
+        for (int x = 0; x < ps; ++x) img[(long)y * ps + x] = (double)cut[(long)(oy + y) * cs + ox + x];
+    double avg, sd;
+    img_stats(img, ps2, &avg, &sd);
+    for (long i = 0; i < ps2; ++i) img[i] = (img[i] - avg) * p->window[i] + avg;
+    double mean, stddev;
+    img_stats(img, ps2, &mean, &stddev);
+    p->statMean[j] = mean;
+    p->statStd[j] = stddev;
+    cplx* D = p->D + (long)j * p->N2;
+    if (oldFT) memcpy(oldFT, D, sizeof(cplx) * (size_t)p->N2);
+    if (doReset) {
+        cplx* c = s->tmpc;
+        for (long i = 0; i < ps2; ++i) c[i] = (img[i] - mean) * p->noiseWindow[i];
+        fft2(&p->planPS, &p->planPS, c, -1, s->work);
+        double noise = ft_noise(c, ps, ps);  /* noiseFudge = 1 */
+        p->statNoise[j] = noise;
+        *rg_out = noise / stddev;
+    }
+    cplx* c2 = s->tmpc2;
+    if (ps != N) {
+        int off = (N - ps) / 2;
+        for (long i = 0; i < p->N2; ++i) c2[i] = mean;
+        for (int y = 0; y < ps; ++y)
+            for (int x = 0; x < ps; ++x) c2[(long)(off + y) * N + off + x] = img[(long)y * ps + x];
+    } else {
+        for (long i = 0; i < p->N2; ++i) c2[i] = img[i];
+    }
+    fft2(&p->planN, &p->planN, c2, -1, s->work);
+    reorder_c(c2, N, N, s->tmpc3);   /* REORDER_FT */
+    memcpy(D, c2, sizeof(cplx) * (size_t)p->N2);
+}
+
+/* Load the cutouts of one patch and initialise everything that Channel::initPatch,
+ * Object::initPatch and Solver::shiftAndInit(alpha_offset, true) set up.
+ * residual_alpha: per image (y, x) channel residual tilt coefficient (residualAlpha in
+ * channel.cpp:906-939); the channel phase is phi_fixed - residual_alpha * Z_tilt. */
+void orc_set_images(orc_patch* p, const float* cutouts, const double* residual_alpha,
+                    const double* fixed_gamma /* nObj or NULL */) {
+    const long n2 = p->n2;
+    memcpy(p->cutouts, cutouts, sizeof(float) * (size_t)p->nImg * p->cs * p->cs);
+    for (int j = 0; j < p->nImg; ++j) {
+        double* pc = p->phiChannel + (long)j * n2;
+        memcpy(pc, p->phiFixed + (long)p->imgCh[j] * n2, sizeof(double) * (size_t)n2);
+        if (residual_alpha) {
+            double ry = residual_alpha[2 * j + 0], rx = residual_alpha[2 * j + 1];
+            if (p->g.tilt_x >= 0 && fabs(rx) > 0) {
+                const double* mp = p->modes + (long)p->g.tilt_x * n2;
+                double res = -rx;
+                for (long i = 0; i < n2; ++i) pc[i] = pc[i] + res * mp[i];
+            }
+            if (p->g.tilt_y >= 0 && fabs(ry) > 0) {
+                const double* mp = p->modes + (long)p->g.tilt_y * n2;
+                double res = -ry;
+                for (long i = 0; i < n2; ++i) pc[i] = pc[i] + res * mp[i];
+            }
+        }
+        p->curShift[2 * j] = p->curShift[2 * j + 1] = 0;
+        p->curTiltOffset[2 * j] = p->curTiltOffset[2 * j + 1] = 0;
+    }
+    compute_otf_norms(p);
+    p->fixed_gamma = fixed_gamma != NULL;
+    if (fixed_gamma) memcpy(p->fixedGamma, fixed_gamma, sizeof(double) * (size_t)p->nObj);
+    /* shiftAndInit(alpha_offset = 0, doReset = true): no shift, full initialisation */
+    memset(p->ftSum, 0, sizeof(double) * (size_t)p->nObj * p->N2);
+    memset(p->regGamma, 0, sizeof(double) * (size_t)p->nObj);
+    double* rg = (double*)xcalloc((size_t)p->nImg, sizeof(double));
+#pragma omp parallel for schedule(dynamic, 1) num_threads(p->nthreads)
+    for (int j = 0; j < p->nImg; ++j) init_image(p, j, 1, &rg[j], NULL);
+    for (int j = 0; j < p->nImg; ++j) {
+        int o = p->imgObj[j];
+        p->regGamma[o] += 0.10 * rg[j] / p->objImgCount[o];   /* Object::addRegGamma */
+        const cplx* D = p->D + (long)j * p->N2;
+        double* fs = p->ftSum + (long)o * p->N2;
+        for (long i = 0; i < p->N2; ++i) fs[i] += creal(D[i]) * creal(D[i]) + cimag(D[i]) * cimag(D[i]);
+    }
+    if (p->fixed_gamma) memcpy(p->regGamma, p->fixedGamma, sizeof(double) * (size_t)p->nObj);
+    free(rg);
+}
+
+/* ---------------- forward: applyAlpha + metric ---------------- */
+
+static void apply_alpha(orc_patch* p, const double* alpha) {
+#pragma omp parallel for schedule(dynamic, 1) num_threads(p->nthreads)
+    for (int j = 0; j < p->nImg; ++j) {
+        img_scratch* s = &p->scr[j];
+        double* phi = p->PHI + (long)j * p->n2;
+        calc_phi(p, j, alpha + (long)j * p->M, phi);
+        calc_pf_otf(p, j, p->otfNorm[p->imgCh[j]], phi, p->PF + (long)j * p->n2,
+                    p->OTF + (long)j * p->N2, s);
+    }
+}
+
+/* Object::initPQ + addPQ over all images (Solver::metric / calcPQ) */
+static void calc_pq(orc_patch* p) {
+    const long N2 = p->N2;
+    for (int o = 0; o < p->nObj; ++o) {
+        cplx* P = p->P + (long)o * N2;
+        double* Q = p->Q + (long)o * N2;
+        for (long i = 0; i < N2; ++i) { P[i] = 0; Q[i] = p->regGamma[o]; }
+    }
+#pragma omp parallel for schedule(static) num_threads(p->nthreads)
+    for (int k = 0; k < p->nOtfSup; ++k) {
+        const int32_t u = p->otfSup[k];
+        for (int j = 0; j < p->nImg; ++j) {
+            const int o = p->imgObj[j];
+            const cplx S = p->OTF[(long)j * N2 + u];
+            const cplx Dv = p->D[(long)j * N2 + u];
+            p->Q[(long)o * N2 + u] += creal(S) * creal(S) + cimag(S) * cimag(S);
+            p->P[(long)o * N2 + u] += conj(Dv) * S;
+        }
+    }
+}
+
+/* Object::calcHelpers (object.cpp:531-550) */
+static void calc_helpers(orc_patch* p) {
+    const long N2 = p->N2;
+    for (int o = 0; o < p->nObj; ++o) {
+        cplx* P = p->P + (long)o * N2; double* Q = p->Q + (long)o * N2;
+        cplx* PQ = p->PQ + (long)o * N2; double* PS = p->PS + (long)o * N2; double* QS = p->QS + (long)o * N2;
+        memset(PQ, 0, sizeof(cplx) * (size_t)N2);
+        memset(PS, 0, sizeof(double) * (size_t)N2);
+        memset(QS, 0, sizeof(double) * (size_t)N2);
+        for (int k = 0; k < p->nOtfSup; ++k) {
+            const int32_t u = p->otfSup[k];
+            PQ[u] = P[u] * Q[u];
+            PS[u] = creal(P[u]) * creal(P[u]) + cimag(P[u]) * cimag(P[u]);
+            QS[u] = Q[u] * Q[u];
+        }
+    }
+}
+
+/* Object::calcMetric (object.cpp:597-615); Solver::metric sums weight * currentMetric */
+static double calc_metric(orc_patch* p) {
+    const long N2 = p->N2;
+    double sum = 0;
+    for (int o = 0; o < p->nObj; ++o) {
+        if (p->objWeight[o] == 0.0) { p->objMetric[o] = 0; continue; }
+        const double* fs = p->ftSum + (long)o * N2;
+        const cplx* P = p->P + (long)o * N2;
+        const double* Q = p->Q + (long)o * N2;
+        double m = 0;
+        for (int k = 0; k < p->nOtfSup; ++k) {
+            const int32_t u = p->otfSup[k];
+            m += (fs[u] - (creal(P[u]) * creal(P[u]) + cimag(P[u]) * cimag(P[u])) / Q[u]);
+        }
+        m /= ((double)p->ps * p->ps);
+        p->objMetric[o] = m;
+        sum += p->objWeight[o] * m;
+    }
+    return sum;
+}
+
+double orc_metric(orc_patch* p, const double* alpha) {
+    apply_alpha(p, alpha);
+    calc_pq(p);
+    p->n_f++;
+    return calc_metric(p);
+}
+
+/* ---------------- gradients ---------------- */
+
+/* SubImage::calcVogelWeight (subimage.cpp:348-390), writes s->vogel */
+static void calc_vogel_weight(orc_patch* p, int j, img_scratch* s) {
+    const int N = p->N, n = p->n;
+    const long N2 = p->N2;
+    const int o = p->imgObj[j];
+    const cplx* otf = p->OTF + (long)j * N2;
+    const cplx* ft = p->D + (long)j * N2;
+    const cplx* pf = p->PF + (long)j * p->n2;
+    const cplx* pq = p->PQ + (long)o * N2;
+    const double* psv = p->PS + (long)o * N2;
+    const double* qs = p->QS + (long)o * N2;
+    cplx* tmp = s->tmpc;   /* tmp->OTF */
+    cplx* hj = s->tmpc2;
+    cplx* gl = s->otf;     /* tmp->C (N2) */
+    memset(tmp, 0, sizeof(cplx) * (size_t)N2);
+    /* reorderInto(pf, n, n, tmp, N, N): quadrants of pf into the corners of tmp */
+    {
+        const int mid = n / 2;
+        for (int y = 0; y < n; ++y) {
+            int oy = (y < mid) ? (N - mid + y) : (y - mid);
+            for (int x = 0; x < n; ++x) {
+                int ox = (x < mid) ? (N - mid + x) : (x - mid);
+                tmp[(long)oy * N + ox] = pf[(long)y * n + x];
+            }
+        }
+    }
+    /* hj = ift(tmp) normalised by 1/N^2 */
+    memcpy(hj, tmp, sizeof(cplx) * (size_t)N2);
+    fft2(&p->planN, &p->planN, hj, +1, s->work);
+    for (long i = 0; i < N2; ++i) hj[i] /= (double)N2;
+    memset(tmp, 0, sizeof(cplx) * (size_t)N2);
+    for (int k = 0; k < p->nOtfSup; ++k) {
+        const int32_t u = p->otfSup[k];
+        tmp[u] = (pq[u] * ft[u] - psv[u] * otf[u]) / qs[u];
+    }
+    reorder_c(tmp, N, N, s->tmpc3);
+    memcpy(gl, tmp, sizeof(cplx) * (size_t)N2);
+    fft2(&p->planN, &p->planN, gl, +1, s->work);
+    for (long i = 0; i < N2; ++i) gl[i] /= (double)N2;
+    for (long i = 0; i < N2; ++i) gl[i] = hj[i] * creal(gl[i]);
+    fft2(&p->planN, &p->planN, gl, -1, s->work);
+    reorder_c(gl, N, N, s->tmpc3);
+    for (int i = 0; i < p->nPupSup; ++i) {
+        int32_t a = p->pupSup[i];
+        s->vogel[a] = cimag(conj(pf[a]) * gl[p->pupInOtf[i]]) * p->pupil[a];
+    }
+}
+
+/* SubImage::gradientVogel (subimage.cpp:312-326), already multiplied by weight */
+static double gradient_vogel(orc_patch* p, int j, int m, img_scratch* s) {
+    const int o = p->imgObj[j];
+    if (p->objWeight[o] == 0) return 0;
+    const double* mp = p->modes + (long)m * p->n2;
+    const double scale = -2.0 * p->area / (double)p->N2;
+    double ret = 0;
+    for (int i = 0; i < p->nPupSup; ++i) {
+        int32_t a = p->pupSup[i];
+        ret += scale * s->vogel[a] * mp[a];
+    }
+    return ret * p->objWeight[o];
+}
+
+/* SubImage::metricChange (subimage.cpp:261-278) */
+static double metric_change(orc_patch* p, int j, const cplx* newOTF) {
+    const int o = p->imgObj[j];
+    const long N2 = p->N2;
+    const cplx* oldOTF = p->OTF + (long)j * N2;
+    const cplx* P = p->P + (long)o * N2;
+    const cplx* ft = p->D + (long)j * N2;
+    const double* Q = p->Q + (long)o * N2;
+    double dl = 0;
+    for (int k = 0; k < p->nOtfSup; ++k) {
+        const int32_t u = p->otfSup[k];
+        cplx dsj = newOTF[u] - oldOTF[u];
+        cplx dp = conj(ft[u]) * dsj;
+        double dq = 2.0 * (creal(oldOTF[u]) * creal(dsj) + cimag(oldOTF[u]) * cimag(dsj)) +
+                    (creal(dsj) * creal(dsj) + cimag(dsj) * cimag(dsj));
+        double dn = 2.0 * (creal(dp) * creal(P[u]) + cimag(dp) * cimag(P[u])) +
+                    (creal(dp) * creal(dp) + cimag(dp) * cimag(dp));
+        double pn = creal(P[u]) * creal(P[u]) + cimag(P[u]) * cimag(P[u]);
+        dl -= (Q[u] * dn - dq * pn) / (Q[u] * (Q[u] + dq));
+    }
+    return dl / (double)N2;
+}
+
+/* SubImage::gradientFiniteDifference (subimage.cpp:281-292) */
+static double gradient_fd(orc_patch* p, int j, int m, img_scratch* s) {
+    const int o = p->imgObj[j];
+    if (p->objWeight[o] == 0) return 0;
+    const double h = p->objGradStep[o];
+    double* tphi = s->phi;
+    memcpy(tphi, p->PHI + (long)j * p->n2, sizeof(double) * (size_t)p->n2);
+    const double* mp = p->modes + (long)m * p->n2;
+    for (long i = 0; i < p->n2; ++i) tphi[i] = tphi[i] + h * mp[i];
+    calc_otf(p, p->otfNorm[p->imgCh[j]], tphi, s->tmpc, s);
+    return metric_change(p, j, s->tmpc) / h * p->objWeight[o];
+}
+
+/* Solver::gradient (solver.cpp:860-894): per image, per enabled mode.
+ * method 1 = finite differences, 2 = Vogel.  grad is in alpha space (nPar). */
+static void gradient_alpha(orc_patch* p, int method, double* g) {
+    memset(g, 0, sizeof(double) * (size_t)p->nPar);   /* REG_ALPHA = 0 */
+#pragma omp parallel for schedule(dynamic, 1) num_threads(p->nthreads)
+    for (int j = 0; j < p->nImg; ++j) {
+        img_scratch* s = &p->scr[j];
+        const int o = p->imgObj[j];
+        if (method == 2) calc_vogel_weight(p, j, s);
+        for (int m = 0; m < p->M; ++m) {
+            if (!p->enabled[m]) continue;
+            double v = (method == 2) ? gradient_vogel(p, j, m, s) : gradient_fd(p, j, m, s);
+            g[(long)j * p->M + m] = p->objWeight[o] * v;
+        }
+    }
+}
+
+/* my_df in alpha space: applyAlpha, calcPQ (with helpers), gradient.
+ * enabled: M flags (NULL = all); returns the metric at alpha as a by-product. */
+double orc_gradient(orc_patch* p, const double* alpha, const uint8_t* enabled, int method,
+                    double* grad) {
+    for (int m = 0; m < p->M; ++m) p->enabled[m] = enabled ? enabled[m] : 1;
+    apply_alpha(p, alpha);
+    calc_pq(p);
+    calc_helpers(p);
+    gradient_alpha(p, method, grad);
+    p->n_df++;
+    return calc_metric(p);
+}
+
+/* ---------------- constraints ---------------- */
+
+/* Constraints::apply: out[col] = sum val * in[row] (constraints.hpp:128-133) */
+static void cons_apply(const orc_patch* p, const double* in, double* out) {
+    memset(out, 0, sizeof(double) * (size_t)p->nFree);
+    for (long e = 0; e < p->nnz; ++e) out[p->nsCol[e]] += p->nsVal[e] * in[p->nsRow[e]];
+}
+
+/* Constraints::reverseAndAdd: out = offset + N in (constraints.hpp:141-146) */
+static void cons_reverse_add(const orc_patch* p, const double* in, const double* offset, double* out) {
+    memcpy(out, offset, sizeof(double) * (size_t)p->nPar);
+    for (long e = 0; e < p->nnz; ++e) out[p->nsRow[e]] += p->nsVal[e] * in[p->nsCol[e]];
+}
+
+void orc_cons_apply(const orc_patch* p, const double* in, double* out) { cons_apply(p, in, out); }
+void orc_cons_reverse_add(const orc_patch* p, const double* in, const double* off, double* out) {
+    cons_reverse_add(p, in, off, out);
+}
+
+/* ---------------- the solver (Solver::run with conjugate_rdx) ---------------- */
+
+typedef struct {
+    orc_patch* p;
+    int gradMethod;   /* 1 FD, 2 Vogel */
+    double* beta_tmp;
+    double* metrics; int nMetrics; int capMetrics;
+    int logEvals; double* evalLog; int nEval; int capEval; /* (kind, step, f) */
+} solver_ctx;
+
+/* my_f: applyBeta + metric */
+static double my_f(solver_ctx* c, const double* b) {
+    orc_patch* p = c->p;
+    cons_reverse_add(p, b, p->alphaOffset, p->alpha);
+    double f = orc_metric(p, p->alpha);
+    return f;
+}
+
+/* my_df: applyBeta + calcPQ + gradient; grad in beta space */
+static void my_df(solver_ctx* c, const double* b, double* df) {
+    orc_patch* p = c->p;
+    cons_reverse_add(p, b, p->alphaOffset, p->alpha);
+    apply_alpha(p, p->alpha);
+    calc_pq(p);
+    calc_helpers(p);
+    gradient_alpha(p, c->gradMethod, p->gradAlpha);
+    cons_apply(p, p->gradAlpha, df);
+    p->n_df++;
+}
+
+/* my_fdf: applyBeta, metric, gradient with the helpers left from the last calcPQ
+ * (solver.cpp:237-243).  The gradient it leaves is overwritten by the first statement
+ * of conjugate_rdx_iterate before anything reads it, so only f is needed here. */
+static double my_fdf(solver_ctx* c, const double* b, double* df) {
+    double f = my_f(c, b);
+    (void)df;
+    return f;
+}
+
+typedef struct {
+    int n;
+    int iter;
+    double step, tol, pnorm, g0norm;
+    double *x1, *p, *g0, *dx;
+} cg_state;
+
+/* value_at (conjugate_gradient.cpp:115-118): f(x - step*lambda*p) */
+static double value_at(solver_ctx* c, cg_state* st, const double* x, double step, double lambda) {
+    for (int i = 0; i < st->n; ++i) {
+        st->dx[i] = 0.0 + (-step * lambda) * st->p[i];   /* take_step */
+        st->x1[i] = x[i] + 1.0 * st->dx[i];
+    }
+    double f = my_f(c, st->x1);
+    if (c->logEvals) {
+        if (c->nEval + 1 > c->capEval) {
+            c->capEval = c->capEval ? 2 * c->capEval : 1024;
+            c->evalLog = (double*)realloc(c->evalLog, sizeof(double) * 2 * (size_t)c->capEval);
+        }
+        c->evalLog[2 * c->nEval] = step;
+        c->evalLog[2 * c->nEval + 1] = f;
+        c->nEval++;
+    }
+    return f;
+}
+
+#define SIGNX(a, b) ((b) >= 0.0 ? fabs(a) : -fabs(a))
+#define TINY 1.0E-32
+static const double GOLD = 1.6180339887498949025257;  /* (1+sqrt(5))/2 */
+
+/* redux::math::bracket (helpers.cpp:58-129), limit = 100 */
+static void bracket(solver_ctx* c, cg_state* st, const double* x, double lambda, double* a, double* b,
+                    double* mid, double* fa, double* fb, double* fmid) {
+    const int limit = 100;
+    double u, fu, ulim;
+    if (*fb > *fa) {
+        double t = *a; *a = *b; *b = t;
+        t = *fa; *fa = *fb; *fb = t;
+    }
+    *mid = *b + GOLD * (*b - *a);
+    *fmid = value_at(c, st, x, *mid, lambda);
+    while (*fb > *fmid) {
+        double r = (*b - *a) * (*fb - *fmid);
+        double q = (*b - *mid) * (*fb - *fa);
+        double mx = fabs(q - r) > TINY ? fabs(q - r) : TINY;
+        u = (*b) - ((*b - *mid) * q - (*b - *a) * r) / (2.0 * SIGNX(mx, q - r));
+        ulim = *b + limit * (*mid - *b);
+        if ((*b - u) * (u - *mid) > 0.0) {
+            fu = value_at(c, st, x, u, lambda);
+            if (fu < *fmid) {
+                *a = *b; *b = u; *fa = *fb; *fb = fu;
+                break;
+            } else if (fu > *fb) {
+                *mid = u; *fmid = fu;
+                break;
+            }
+            u = *mid + GOLD * (*mid - *b);
+            fu = value_at(c, st, x, u, lambda);
+        } else if ((*mid - u) * (u - ulim) > 0.0) {
+            fu = value_at(c, st, x, u, lambda);
+            if (fu < *fmid) {
+                /* SHFT(b, mid, u, mid + GOLD*(mid-b)); SHFT(fb, fmid, fu, f(u)) */
+                *b = *mid; *mid = u; u = *mid + GOLD * (*mid - *b);
+                *fb = *fmid; *fmid = fu; fu = value_at(c, st, x, u, lambda);
+            }
+        } else if ((*mid - ulim) * (ulim - u) >= 0.0) {
+            u = ulim;
+            fu = value_at(c, st, x, u, lambda);
+        } else {
+            u = *mid + GOLD * (*mid - *b);
+            fu = value_at(c, st, x, u, lambda);
+        }
+        *a = *b; *b = *mid; *mid = u;
+        *fa = *fb; *fb = *fmid; *fmid = fu;
+    }
+    if (*a > *b) { double t = *a; *a = *b; *b = t; t = *fa; *fa = *fb; *fb = t; }
+    if (*mid > *b) { double t = *mid; *mid = *b; *b = t; t = *fmid; *fmid = *fb; *fb = t; }
+    if (*mid < *a) { double t = *mid; *mid = *a; *a = t; t = *fmid; *fmid = *fa; *fa = t; }
+}
+
+/* redux::math::brent (helpers.cpp:133-215), limit = 100 */
+static void brent(solver_ctx* c, cg_state* st, const double* xv, double lambda, double ax, double bx,
+                  double* x, double* fx, double tol) {
+    const int limit = 100;
+    const double CGOLD = 2.0 - GOLD;
+    double a = ax < bx ? ax : bx;
+    double b = ax > bx ? ax : bx;
+    double u, v, w;
+    u = v = w = *x;
+    double fu, fv, fw;
+    fu = fv = fw = *fx = value_at(c, st, xv, *x, lambda);
+    double d = 0.0, e = 0.0;
+    for (int iter = 1; iter <= limit; ++iter) {
+        double xm = 0.5 * (a + b);
+        double tol1 = tol * fabs(*x) + TINY;
+        double tol2 = 2.0 * tol1;
+        if (fabs(*x - xm) <= (tol2 - 0.5 * (b - a))) return;
+        if (fabs(e) > tol1) {
+            double r = (*x - w) * (*fx - fv);
+            double q = (*x - v) * (*fx - fw);
+            double pp = (*x - v) * q - (*x - w) * r;
+            q = 2.0 * (q - r);
+            if (q > 0.0) pp = -pp;
+            q = fabs(q);
+            double etemp = e;
+            e = d;
+            if (fabs(pp) >= fabs(0.5 * q * etemp) || pp <= q * (a - *x) || pp >= q * (b - *x)) {
+                e = (*x >= xm ? a - *x : b - *x);
+                d = CGOLD * e;
+            } else {
+                d = pp / q;
+                u = *x + d;
+                if (u - a < tol2 || b - u < tol2) d = SIGNX(tol1, xm - *x);
+            }
+        } else {
+            e = (*x >= xm ? a - *x : b - *x);
+            d = CGOLD * e;
+        }
+        if (fabs(d) < tol1) d *= (tol1 / fabs(d));
+        u = ((fabs(d) >= tol1) ? *x + d : *x + SIGNX(tol1, d));
+        fu = value_at(c, st, xv, u, lambda);
+        if (fu <= *fx) {
+            if (u >= *x) a = *x; else b = *x;
+            v = w; w = *x; *x = u;
+            fv = fw; fw = *fx; *fx = fu;
+        } else {
+            if (u < *x) a = u; else b = u;
+            if (fu <= fw || w == *x) {
+                v = w; w = u; fv = fw; fw = fu;
+            } else if (fu <= fv || v == *x || v == w) {
+                v = u; fv = fu;
+            }
+        }
+    }
+    fprintf(stderr, "Error in brent: too many iterations!\n");
+}
+
+#define RDX_SUCCESS 0
+#define RDX_ENOPROG 27
+#define RDX_FAILURE (-1)
+
+/* gsl_blas_dnrm2: the scaled sum of squares of the reference BLAS dnrm2 */
+static double dnrm2(const double* v, int n) {
+    double scale = 0.0, ssq = 1.0;
+    if (n == 1) return fabs(v[0]);
+    for (int i = 0; i < n; ++i) {
+        if (v[i] != 0.0) {
+            double ax = fabs(v[i]);
+            if (scale < ax) { ssq = 1.0 + ssq * (scale / ax) * (scale / ax); scale = ax; }
+            else ssq += (ax / scale) * (ax / scale);
+        }
+    }
+    return scale * sqrt(ssq);
+}
+
+/* conjugate_rdx_iterate (conjugate_gradient.cpp:128-256) */
+static int cg_iterate(solver_ctx* c, cg_state* st, double* x, double* f, double* gradient, double* dx) {
+    const int n = st->n;
+    my_df(c, x, gradient);
+    double pnorm = st->pnorm;
+    double g0norm = st->g0norm;
+    double g1norm = dnrm2(gradient, n);
+    double pg;
+    if (st->iter++ == 0) {
+        memcpy(st->p, gradient, sizeof(double) * (size_t)n);
+        pnorm = st->pnorm = g1norm;
+        pg = g1norm * g1norm;
+    } else {
+        if (g0norm == 0.0) {
+            memset(dx, 0, sizeof(double) * (size_t)n);
+            return RDX_ENOPROG;
+        }
+        double g0g1 = 0;
+        for (int i = 0; i < n; ++i) {
+            double tmp = st->g0[i] - gradient[i];
+            g0g1 += tmp * gradient[i];
+            st->g0[i] = tmp;
+        }
+        double beta = g0g1 / (g0norm * g0norm);
+        for (int i = 0; i < n; ++i) st->p[i] = gradient[i] - beta * st->p[i];
+        pnorm = st->pnorm = dnrm2(st->p, n);
+        pg = 0;
+        for (int i = 0; i < n; ++i) pg += st->p[i] * gradient[i];
+    }
+    double lambda = (pg >= 0.0) ? +1.0 / pnorm : -1.0 / pnorm;
+    if (pnorm == 0.0) {
+        memset(dx, 0, sizeof(double) * (size_t)n);
+        return RDX_ENOPROG;
+    }
+    double fa = *f, fb, fc;
+    double stepa = 0.0, stepb, stepc = 1E-21 / lambda;
+    fc = value_at(c, st, x, stepc, lambda);
+    bracket(c, st, x, lambda, &stepa, &stepc, &stepb, &fa, &fc, &fb);
+    brent(c, st, x, lambda, stepa, stepc, &stepb, &fb, c->p ? 0.1 : 0.1);
+    for (int i = 0; i < n; ++i) {
+        dx[i] = 0.0 + (-stepb * lambda) * st->p[i];
+        st->x1[i] = x[i] + 1.0 * dx[i];
+    }
+    memcpy(x, st->x1, sizeof(double) * (size_t)n);
+    *f = fb;
+    st->step = 0.5 * (fabs(stepb) > 2.0E-9 ? fabs(stepb) : 2.0E-9);
+    st->g0norm = g1norm;
+    memcpy(st->g0, gradient, sizeof(double) * (size_t)n);
+    st->iter = st->iter % n;
+    return RDX_SUCCESS;
+}
+
+static void push_metric(solver_ctx* c, double v) {
+    if (c->nMetrics + 1 > c->capMetrics) {
+        c->capMetrics = c->capMetrics ? 2 * c->capMetrics : 256;
+        c->metrics = (double*)realloc(c->metrics, sizeof(double) * (size_t)c->capMetrics);
+    }
+    c->metrics[c->nMetrics++] = v;
+}
+
+/* SubImage::adjustShifts (subimage.cpp:444-480); returns 1 if the image was shifted */
+static int adjust_shifts(orc_patch* p, int j, const double* a) {
+    if (!p->have_jacobian || p->g.tilt_x < 0 || p->g.tilt_y < 0) return 0;
+    const double ay = a[p->g.tilt_y] + p->curTiltOffset[2 * j + 0];
+    const double ax = a[p->g.tilt_x] + p->curTiltOffset[2 * j + 1];
+    /* alphaToShift: (y, x) = (ax J[1][0] + ay J[1][1], ax J[0][0] + ay J[0][1]) */
+    double sy = ax * p->J_T_xy[1][0] + ay * p->J_T_xy[1][1];
+    double sx = ax * p->J_T_xy[0][0] + ay * p->J_T_xy[0][1];
+    int ty = -(int)lround(sy), tx = -(int)lround(sx);
+    int act[2] = {0, 0};
+    int want[2] = {ty, tx};
+    for (int d = 0; d < 2; ++d) {
+        int nsh = want[d];
+        if (!nsh) continue;
+        int first = p->margin + p->curShift[2 * j + d];
+        int last = first + p->ps - 1;
+        if (nsh + first < 0) nsh = -first;
+        if (abs(nsh + last) >= p->cs) nsh = p->cs - last - 1;
+        act[d] = nsh;
+    }
+    if (act[0] || act[1]) {
+        p->curShift[2 * j + 0] += act[0];
+        p->curShift[2 * j + 1] += act[1];
+        /* shiftToAlpha */
+        double dy = act[1] * p->J_xy_T[1][0] + act[0] * p->J_xy_T[1][1];
+        double dxv = act[1] * p->J_xy_T[0][0] + act[0] * p->J_xy_T[0][1];
+        p->curTiltOffset[2 * j + 0] += dy;
+        p->curTiltOffset[2 * j + 1] += dxv;
+        return 1;
+    }
+    return 0;
+}
+
+/* Solver::shiftAndInit(a, false) + Object::reInitialize (object.cpp:885-904) */
+static void shift_and_init(orc_patch* p, const double* a) {
+    int* shifted = (int*)xcalloc((size_t)p->nObj, sizeof(int));
+    for (int j = 0; j < p->nImg; ++j)
+        if (adjust_shifts(p, j, a + (long)j * p->M)) shifted[p->imgObj[j]] = 1;
+    for (int o = 0; o < p->nObj; ++o) {
+        if (!shifted[o]) continue;
+        for (int j = 0; j < p->nImg; ++j) {
+            if (p->imgObj[j] != o) continue;
+            cplx* oldFT = p->scr[j].tmpc3;   /* reused after init_image's reorder */
+            cplx* keep = (cplx*)xcalloc((size_t)p->N2, sizeof(cplx));
+            init_image(p, j, 0, NULL, keep);
+            (void)oldFT;
+            const cplx* D = p->D + (long)j * p->N2;
+            double* fs = p->ftSum + (long)o * p->N2;
+            for (long i = 0; i < p->N2; ++i)      /* Object::addDiffToFT */
+                fs[i] += (creal(D[i]) * creal(D[i]) + cimag(D[i]) * cimag(D[i])) -
+                         (creal(keep[i]) * creal(keep[i]) + cimag(keep[i]) * cimag(keep[i]));
+            free(keep);
+        }
+    }
+    free(shifted);
+}
+
+/* Solver::run (solver.cpp:330-580) with GETSTEP = conjugate_gradient.
+ * alpha_out: nPar; metrics_out: optional buffer of cap_metrics entries;
+ * eval_log: optional (step, f) pairs of every line-search evaluation. */
+int orc_solve(orc_patch* p, const orc_cfg* cfg, double* alpha_out, orc_report* rep,
+              double* metrics_out, int cap_metrics, double* eval_log, int cap_eval) {
+    const int nFree = p->nFree, nPar = p->nPar, M = p->M;
+    solver_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.p = p;
+    c.gradMethod = cfg->fd_first ? 1 : 2;
+    c.logEvals = eval_log != NULL;
+    p->n_f = p->n_df = 0;
+    memset(p->alpha, 0, sizeof(double) * (size_t)nPar);
+    memset(p->gradAlpha, 0, sizeof(double) * (size_t)nPar);
+    memset(p->alphaOffset, 0, sizeof(double) * (size_t)nPar);
+    cg_state st;
+    memset(&st, 0, sizeof(st));
+    st.n = nFree;
+    st.x1 = (double*)xcalloc((size_t)nFree, sizeof(double));
+    st.p = (double*)xcalloc((size_t)nFree, sizeof(double));
+    st.g0 = (double*)xcalloc((size_t)nFree, sizeof(double));
+    st.dx = (double*)xcalloc((size_t)nFree, sizeof(double));
+    double* x = (double*)xcalloc((size_t)nFree, sizeof(double));
+    double* gradient = (double*)xcalloc((size_t)nFree, sizeof(double));
+    double* dx = (double*)xcalloc((size_t)nFree, sizeof(double));
+    double* beta_init = (double*)xcalloc((size_t)nFree, sizeof(double));
+    memset(p->enabled, 0, (size_t)M);
+    double sf = 0;
+    double previousMetric = 0, thisMetric = 0, gradNorm = 0;
+    double tol = 1.0E-1;
+    int failCount = 0, totalIterations = 0, maxIterations = 10, maxFails = 3;
+    int status = 0;
+    /* loadInit: alpha_offset = 0 (no init file); shiftAndInit(alpha_offset, true) was done
+     * by orc_set_images. */
+    double initialMetric = my_f(&c, beta_init);
+    push_metric(&c, initialMetric);
+    const double nTotalPixels = (double)p->nImg * p->ps * p->ps;
+    const double gradScale = 1.0 / (nTotalPixels * nTotalPixels);
+    int exitLoop = 0;
+    for (int modeCount = cfg->n_initial_modes; !exitLoop; modeCount += cfg->n_mode_increment) {
+        if (modeCount > M) modeCount = M;
+        for (int m = 0; m < modeCount; ++m) p->enabled[m] = 1;
+        if (modeCount == M || cfg->max_iterations == 0) {
+            exitLoop = 1;
+            tol = cfg->ftol;
+            maxIterations = cfg->max_iterations;
+        }
+        /* gsl_multimin_fdfminimizer_set -> conjugate_rdx_set */
+        memcpy(x, beta_init, sizeof(double) * (size_t)nFree);
+        memset(dx, 0, sizeof(double) * (size_t)nFree);
+        st.iter = 0;
+        sf = my_fdf(&c, x, gradient);
+        int iter = 0, successCount = 0, done = 0;
+        while ((!done || iter < cfg->min_iterations) && iter < maxIterations) {
+            iter++;
+            status = cg_iterate(&c, &st, x, &sf, gradient, dx);
+            if (failCount > maxFails) {
+                status = RDX_FAILURE;
+                exitLoop = 1;
+                done = 1;
+                break;
+            }
+            c.gradMethod = 2;   /* switch to Vogel after the first iteration */
+            if (status == RDX_ENOPROG) { failCount++; break; }
+            thisMetric = sf;
+            if (!isfinite(thisMetric)) { failCount++; break; }
+            push_metric(&c, thisMetric);
+            gradNorm = dnrm2(gradient, nFree) * gradScale;
+            if (!isfinite(gradNorm)) { failCount++; break; }
+            if (gradNorm < cfg->ftol) { exitLoop = 1; done = 1; break; }
+            if (iter > 1) {
+                double rc = 2.0 * fabs(thisMetric - previousMetric) /
+                            (fabs(thisMetric) + fabs(previousMetric) + cfg->eps);
+                if (rc < tol) {
+                    if (++successCount >= cfg->target_iterations) { successCount = 0; done = 1; }
+                } else {
+                    successCount = 0;
+                }
+            }
+            previousMetric = thisMetric;
+        }
+        thisMetric = my_f(&c, x);
+        totalIterations += iter;
+        if (!exitLoop) {
+            shift_and_init(p, p->alpha);
+            memcpy(p->alphaOffset, p->alpha, sizeof(double) * (size_t)nPar);
+        }
+    }
+    memcpy(alpha_out, p->alpha, sizeof(double) * (size_t)nPar);
+    if (rep) {
+        rep->initial_metric = initialMetric;
+        rep->final_metric = thisMetric;
+        rep->iterations = totalIterations;
+        rep->status = (status == RDX_FAILURE) ? 1 : 0;
+        rep->n_f_evals = (int32_t)p->n_f;
+        rep->n_df_evals = (int32_t)p->n_df;
+        rep->fail_count = failCount;
+        rep->n_metrics = c.nMetrics;
+    }
+    if (metrics_out) {
+        int nm = c.nMetrics < cap_metrics ? c.nMetrics : cap_metrics;
+        memcpy(metrics_out, c.metrics, sizeof(double) * (size_t)nm);
+    }
+    if (eval_log) {
+        int ne = c.nEval < cap_eval ? c.nEval : cap_eval;
+        memcpy(eval_log, c.evalLog, sizeof(double) * 2 * (size_t)ne);
+    }
+    free(c.metrics); free(c.evalLog);
+    free(st.x1); free(st.p); free(st.g0); free(st.dx);
+    free(x); free(gradient); free(dx); free(beta_init);
+    return status == RDX_FAILURE ? 1 : 0;
+}
+
+/* ---------------- accessors for tests ---------------- */
+
+void orc_get_D(const orc_patch* p, double* out) {
+    memcpy(out, p->D, sizeof(cplx) * (size_t)p->nImg * p->N2);
+}
+void orc_get_otf(const orc_patch* p, double* out) {
+    memcpy(out, p->OTF, sizeof(cplx) * (size_t)p->nImg * p->N2);
+}
+void orc_get_pf(const orc_patch* p, double* out) {
+    memcpy(out, p->PF, sizeof(cplx) * (size_t)p->nImg * p->n2);
+}
+void orc_get_pq(const orc_patch* p, double* P, double* Q) {
+    memcpy(P, p->P, sizeof(cplx) * (size_t)p->nObj * p->N2);
+    memcpy(Q, p->Q, sizeof(double) * (size_t)p->nObj * p->N2);
+}
+void orc_get_ftsum(const orc_patch* p, double* out) {
+    memcpy(out, p->ftSum, sizeof(double) * (size_t)p->nObj * p->N2);
+}
+void orc_get_gamma(const orc_patch* p, double* out) {
+    memcpy(out, p->regGamma, sizeof(double) * (size_t)p->nObj);
+}
+void orc_get_otfnorm(const orc_patch* p, double* out) {
+    memcpy(out, p->otfNorm, sizeof(double) * (size_t)p->nCh);
+}
+void orc_get_stats(const orc_patch* p, double* mean, double* stddev, double* noise) {
+    memcpy(mean, p->statMean, sizeof(double) * (size_t)p->nImg);
+    memcpy(stddev, p->statStd, sizeof(double) * (size_t)p->nImg);
+    memcpy(noise, p->statNoise, sizeof(double) * (size_t)p->nImg);
+}
+void orc_get_shifts(const orc_patch* p, int32_t* shift, double* tiltoff) {
+    memcpy(shift, p->curShift, sizeof(int32_t) * 2 * (size_t)p->nImg);
+    memcpy(tiltoff, p->curTiltOffset, sizeof(double) * 2 * (size_t)p->nImg);
+}
+
+/* Solver::shiftAndInit(alpha, false) for an external driver */
+void orc_shift(orc_patch* p, const double* alpha) { shift_and_init(p, alpha); }

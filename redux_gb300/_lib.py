@@ -1,0 +1,92 @@
+"""ctypes declarations of the C ABI in include/rdxg.h (libredux_gb300.so)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libredux_gb300.so")
+
+RDXG_OK, RDXG_ERR_ARG, RDXG_ERR_UNSUPPORTED, RDXG_ERR_CUDA, RDXG_ERR_STATE, RDXG_ERR_NONFINITE, RDXG_ERR_NOMEM = range(7)
+RDXG_FP32, RDXG_FP64 = 0, 1
+RDXG_GRAD_VOGEL, RDXG_GRAD_EXACT, RDXG_GRAD_FD = 0, 1, 2
+
+EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "rdxg_set_stream",
+            "rdxg_set_patches", "rdxg_set_patches_device", "rdxg_metric", "rdxg_gradient",
+            "rdxg_solve", "rdxg_solve_async", "rdxg_fetch_results", "rdxg_last_launch_count",
+            "rdxg_debug_copy", "rdxg_cg_minimize")
+
+
+class Geometry(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in (
+        "otf_size", "pupil_pixels", "patch_size", "n_modes", "n_objects", "n_images", "n_channels",
+        "tilt_x", "tilt_y", "n_free", "cutout_size", "max_patches", "precision", "device")]
+
+
+class Static(C.Structure):
+    _fields_ = [("modes", C.c_void_p), ("pupil", C.c_void_p),
+                ("n_pupil_support", C.c_int32), ("pupil_support", C.c_void_p),
+                ("n_otf_support", C.c_int32), ("otf_support", C.c_void_p),
+                ("image_object", C.c_void_p), ("image_channel", C.c_void_p),
+                ("phi_fixed", C.c_void_p), ("object_weight", C.c_void_p),
+                ("object_grad_step", C.c_void_p), ("window", C.c_void_p), ("noise_window", C.c_void_p),
+                ("ns_nnz", C.c_int64), ("ns_rows", C.c_void_p), ("ns_cols", C.c_void_p),
+                ("ns_vals", C.c_void_p), ("tilt_jacobian", C.c_void_p)]
+
+
+class SolveParams(C.Structure):
+    _fields_ = [("mode_start", C.c_int32), ("mode_step", C.c_int32), ("max_iterations", C.c_int32),
+                ("min_iterations", C.c_int32), ("target_iterations", C.c_int32), ("fd_first", C.c_int32),
+                ("max_metrics", C.c_int32), ("check_every", C.c_int32), ("ftol", C.c_double),
+                ("eps", C.c_double)]
+
+
+class PatchReport(C.Structure):
+    _fields_ = [("initial_metric", C.c_double), ("final_metric", C.c_double), ("iterations", C.c_int32),
+                ("status", C.c_int32), ("n_f_evals", C.c_int32), ("n_df_evals", C.c_int32),
+                ("fail_count", C.c_int32), ("n_metrics", C.c_int32)]
+
+
+F_FN = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_void_p)
+DF_FN = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.c_int32, C.c_int32, C.POINTER(C.c_double), C.c_void_p)
+SHIFT_FN = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.c_void_p)
+
+_LIB = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads the library; raises if it has not been built (there is no fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run redux_gb300.build.build() first "
+                           "(the solver has no CPU fallback)")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.rdxg_version.restype = C.c_int
+    L.rdxg_create.argtypes = [C.POINTER(Geometry), C.POINTER(Static), C.POINTER(vp)]
+    L.rdxg_destroy.argtypes = [vp]
+    L.rdxg_last_error.restype = C.c_char_p
+    L.rdxg_last_error.argtypes = [vp]
+    L.rdxg_set_stream.argtypes = [vp, vp]
+    L.rdxg_set_patches.argtypes = [vp, C.c_int32, vp, vp, vp]
+    L.rdxg_set_patches_device.argtypes = [vp, C.c_int32, vp, vp, vp]
+    L.rdxg_metric.argtypes = [vp, vp, vp]
+    L.rdxg_gradient.argtypes = [vp, vp, vp, C.c_int32, vp, vp]
+    L.rdxg_solve.argtypes = [vp, C.POINTER(SolveParams), vp, vp, vp]
+    L.rdxg_solve_async.argtypes = [vp, C.POINTER(SolveParams)]
+    L.rdxg_fetch_results.argtypes = [vp, vp, vp, vp]
+    L.rdxg_last_launch_count.restype = C.c_int64
+    L.rdxg_last_launch_count.argtypes = [vp]
+    L.rdxg_debug_copy.argtypes = [vp, C.c_int32, vp, C.c_size_t]
+    L.rdxg_cg_minimize.argtypes = [C.c_int32, C.c_int32, C.POINTER(SolveParams), C.c_double, F_FN, DF_FN,
+                                   SHIFT_FN, vp, vp, C.POINTER(PatchReport), vp]
+    _LIB = L
+    return L
+
+
+def ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)

@@ -1,0 +1,663 @@
+// C ABI of the batched MOMFBD solver core (include/rdxg.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/rdxg.h"
+#include "rdxg_launch.h"
+
+using namespace rdxg;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct rdxg_solver {
+    rdxg_geometry geo{};
+    int N = 0, n = 0, ps = 0, cs = 0, margin = 0, M = 0, I = 0, nObj = 0, C = 0, nPar = 0, nFree = 0;
+    int Pmax = 0, P = 0, nTiles = 0;
+    bool fp64 = false;
+    cudaStream_t own = nullptr, stream = nullptr;
+    std::string err;
+    std::vector<void*> allocs;
+    // host copies
+    std::vector<int32_t> imgObj, imgCh, objFirst, objCount;
+    std::vector<double> objWeight, gradStep;
+    double J[2][2] = {{0, 0}, {0, 0}}, Jinv[2][2] = {{0, 0}, {0, 0}};
+    bool haveJ = false;
+    double area = 0;
+    // device static
+    void *dZ = nullptr, *dA = nullptr, *dPhi = nullptr, *dOtfNorm = nullptr, *dTw = nullptr;
+    uint8_t* dMask = nullptr;
+    int32_t *dImgObj = nullptr, *dImgCh = nullptr, *dObjFirst = nullptr, *dObjCount = nullptr;
+    double *dObjW = nullptr, *dGradStep = nullptr, *dWin = nullptr, *dNWin = nullptr;
+    int32_t *dRowPtr = nullptr, *dRowCol = nullptr, *dColPtr = nullptr, *dColRow = nullptr;
+    double *dRowVal = nullptr, *dColVal = nullptr;
+    // device per patch
+    float* dCut = nullptr;
+    const float* dCutExt = nullptr;   // caller-owned device cutouts
+    int32_t* dShift = nullptr;
+    double *dMean = nullptr, *dStd = nullptr, *dNoise = nullptr, *dRg = nullptr;
+    void *dAlphaEff = nullptr, *dD = nullptr, *dS = nullptr, *dX = nullptr, *dPF = nullptr, *dO = nullptr, *dQt = nullptr;
+    double *dGamma = nullptr, *dPartial = nullptr, *dGalpha = nullptr;
+    int32_t *dReq = nullptr, *dGm = nullptr, *dMc = nullptr;
+    uint8_t* dReinit = nullptr;
+    double *dCurTilt = nullptr, *dResAlpha = nullptr;
+    // solver state
+    CgState* dStates = nullptr;
+    double *dVec = nullptr, *dMetrics = nullptr, *dAlpha = nullptr, *dAlphaOff = nullptr;
+    int32_t* dActive = nullptr;
+    int32_t* hActive = nullptr;   // pinned
+    int maxMetrics = 0;
+    bool loaded = false, dirty = false;
+    std::vector<double> hResAlpha, hFixedGamma;
+    bool haveFixedGamma = false;
+    int64_t launches = 0;
+    rdxg_solve_params lastParams{};
+};
+
+namespace {
+
+#define CK(h, call)                                                                            \
+    do {                                                                                       \
+        cudaError_t _e = (call);                                                               \
+        if (_e != cudaSuccess) {                                                               \
+            (h)->err = std::string(#call) + ": " + cudaGetErrorString(_e);                     \
+            return RDXG_ERR_CUDA;                                                              \
+        }                                                                                      \
+    } while (0)
+
+#define CKL(h)                                                                                 \
+    do {                                                                                       \
+        cudaError_t _e = cudaGetLastError();                                                   \
+        if (_e != cudaSuccess) {                                                               \
+            (h)->err = std::string("kernel launch: ") + cudaGetErrorString(_e);               \
+            return RDXG_ERR_CUDA;                                                              \
+        }                                                                                      \
+    } while (0)
+
+int dalloc(rdxg_solver* h, void** p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        h->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return RDXG_ERR_NOMEM;
+    }
+    h->allocs.push_back(*p);
+    return RDXG_OK;
+}
+
+template <typename P>
+int dalloc_t(rdxg_solver* h, P** p, size_t count) {
+    void* v = nullptr;
+    int r = dalloc(h, &v, count * sizeof(P));
+    *p = static_cast<P*>(v);
+    return r;
+}
+
+template <typename T>
+int upload(rdxg_solver* h, void** dst, const std::vector<T>& v) {
+    int r = dalloc(h, dst, v.size() * sizeof(T));
+    if (r) return r;
+    CK(h, cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return RDXG_OK;
+}
+
+bool supported_N(int N) { return N == 32 || N == 64 || N == 88 || N == 128; }
+
+// dispatch on (precision, N)
+template <typename F>
+void with_size(int N, bool fp64, F&& f) {
+#define RDXG_CASE(NN)                                                  \
+    case NN:                                                           \
+        if (fp64) f(Launcher<double, NN>{}, double{}); else f(Launcher<float, NN>{}, float{}); \
+        break;
+    switch (N) {
+        RDXG_CASE(32)
+        RDXG_CASE(64)
+        RDXG_CASE(88)
+        RDXG_CASE(128)
+        default: break;
+    }
+#undef RDXG_CASE
+}
+
+template <typename T>
+KParams<T> make_kparams(rdxg_solver* h) {
+    KParams<T> k{};
+    k.P = h->P; k.I = h->I; k.M = h->M; k.nObj = h->nObj; k.N = h->N; k.n = h->n;
+    k.ps = h->ps; k.cs = h->cs; k.margin = h->margin; k.nTiles = h->nTiles;
+    k.Z = (const T*)h->dZ; k.A = (const T*)h->dA; k.phiFixed = (const T*)h->dPhi;
+    k.otfNorm = (const T*)h->dOtfNorm; k.otfMask = h->dMask;
+    k.imgObj = h->dImgObj; k.imgCh = h->dImgCh; k.objFirst = h->dObjFirst; k.objCount = h->dObjCount;
+    k.objWeight = h->dObjW; k.objGradStep = h->dGradStep; k.window = h->dWin; k.noiseWindow = h->dNWin;
+    k.tw = (const cx<T>*)h->dTw; k.area = h->area; k.tiltX = h->geo.tilt_x; k.tiltY = h->geo.tilt_y;
+    k.cutouts = h->dCutExt ? h->dCutExt : h->dCut;
+    k.shift = h->dShift; k.statMean = h->dMean; k.statStd = h->dStd; k.statNoise = h->dNoise; k.rg = h->dRg;
+    k.alphaEff = (const T*)h->dAlphaEff;
+    k.D = (cx<T>*)h->dD; k.S = (cx<T>*)h->dS; k.X = (cx<T>*)h->dX; k.PF = (cx<T>*)h->dPF;
+    k.O = (cx<T>*)h->dO; k.Qt = (T*)h->dQt;
+    k.gamma = h->dGamma; k.partial = h->dPartial; k.galpha = h->dGalpha;
+    k.req = h->dReq; k.gmethod = h->dGm; k.modeCount = h->dMc; k.reinit = h->dReinit;
+    return k;
+}
+
+template <typename T>
+CgArgs<T> make_cgargs(rdxg_solver* h, const CgParams& prm) {
+    CgArgs<T> a{};
+    a.prm = prm;
+    a.P = h->P; a.I = h->I; a.M = h->M; a.nObj = h->nObj; a.nPar = h->nPar; a.nTiles = h->nTiles; a.ps = h->ps;
+    a.states = h->dStates; a.vec = h->dVec; a.metrics = h->dMetrics; a.alpha = h->dAlpha; a.alphaOff = h->dAlphaOff;
+    a.galpha = h->dGalpha; a.partial = h->dPartial; a.objWeight = h->dObjW;
+    a.rowPtr = h->dRowPtr; a.rowCol = h->dRowCol; a.rowVal = h->dRowVal;
+    a.colPtr = h->dColPtr; a.colRow = h->dColRow; a.colVal = h->dColVal;
+    a.curTilt = h->dCurTilt; a.resAlpha = h->dResAlpha; a.tiltX = h->geo.tilt_x; a.tiltY = h->geo.tilt_y;
+    a.alphaEff = (T*)h->dAlphaEff; a.req = h->dReq; a.gmethod = h->dGm; a.modeCount = h->dMc; a.active = h->dActive;
+    return a;
+}
+
+template <typename T>
+int create_static(rdxg_solver* h, const rdxg_static* s) {
+    const int n = h->n, N = h->N, M = h->M, C = h->C;
+    const size_t n2 = (size_t)n * n, N2 = (size_t)N * N;
+    std::vector<T> Z(M * n2), A(n2, (T)0), phi(C * n2), cn(C);
+    for (size_t i = 0; i < M * n2; ++i) Z[i] = (T)s->modes[i];
+    double a2 = 0, area = 0;
+    for (int k = 0; k < s->n_pupil_support; ++k) {
+        const int q = s->pupil_support[k];
+        if (q < 0 || (size_t)q >= n2) { h->err = "pupil_support index out of range"; return RDXG_ERR_ARG; }
+        A[q] = (T)s->pupil[q];
+        a2 += s->pupil[q] * s->pupil[q];
+        area += s->pupil[q];
+    }
+    h->area = area;
+    // Channel::initPatch: otfNormalization = 1/sqrt(max |OTF(phi = 0)|); the maximum is the
+    // zero lag of the pupil autocorrelation, sum A^2 over the pupil support.
+    for (int c = 0; c < C; ++c) cn[c] = (T)(1.0 / std::sqrt(a2));
+    for (size_t i = 0; i < C * n2; ++i) phi[i] = (T)s->phi_fixed[i];
+    std::vector<uint8_t> mask(N2, 0);
+    for (int k = 0; k < s->n_otf_support; ++k) {
+        const int u = s->otf_support[k];
+        if (u < 0 || (size_t)u >= N2) { h->err = "otf_support index out of range"; return RDXG_ERR_ARG; }
+        mask[u] = 1;
+    }
+    std::vector<cx<T>> tw(N);
+    for (int k = 0; k < N; ++k) {
+        const double ang = 2.0 * M_PI * (double)k / (double)N;
+        tw[k].x = (T)std::cos(ang);
+        tw[k].y = (T)(-std::sin(ang));
+    }
+    int r;
+    if ((r = upload(h, &h->dZ, Z)) || (r = upload(h, &h->dA, A)) || (r = upload(h, &h->dPhi, phi)) ||
+        (r = upload(h, &h->dOtfNorm, cn)) || (r = upload(h, &h->dTw, tw)))
+        return r;
+    void* v;
+    if ((r = upload(h, &v, mask))) return r;
+    h->dMask = (uint8_t*)v;
+    return RDXG_OK;
+}
+
+template <typename T>
+int alloc_patch_buffers(rdxg_solver* h) {
+    const size_t P = h->Pmax, I = h->I, N2 = (size_t)h->N * h->N, n2 = (size_t)h->n * h->n;
+    const size_t G = P * I, PO = P * h->nObj;
+    int r;
+    if ((r = dalloc_t(h, &h->dCut, G * h->cs * h->cs)) || (r = dalloc_t(h, &h->dShift, G * 2)) ||
+        (r = dalloc_t(h, &h->dMean, G)) || (r = dalloc_t(h, &h->dStd, G)) || (r = dalloc_t(h, &h->dNoise, G)) ||
+        (r = dalloc_t(h, &h->dRg, G)) || (r = dalloc(h, &h->dAlphaEff, G * h->M * sizeof(T))) ||
+        (r = dalloc(h, &h->dD, G * N2 * sizeof(cx<T>))) || (r = dalloc(h, &h->dS, G * N2 * sizeof(cx<T>))) ||
+        (r = dalloc(h, &h->dX, G * N2 * sizeof(cx<T>))) || (r = dalloc(h, &h->dPF, G * n2 * sizeof(cx<T>))) ||
+        (r = dalloc(h, &h->dO, PO * N2 * sizeof(cx<T>))) || (r = dalloc(h, &h->dQt, PO * N2 * sizeof(T))) ||
+        (r = dalloc_t(h, &h->dGamma, PO)) || (r = dalloc_t(h, &h->dPartial, PO * h->nTiles)) ||
+        (r = dalloc_t(h, &h->dGalpha, G * h->M)) || (r = dalloc_t(h, &h->dReq, P)) ||
+        (r = dalloc_t(h, &h->dGm, P)) || (r = dalloc_t(h, &h->dMc, P)) || (r = dalloc_t(h, &h->dReinit, G)) ||
+        (r = dalloc_t(h, &h->dCurTilt, G * 2)) || (r = dalloc_t(h, &h->dResAlpha, G * 2)) ||
+        (r = dalloc_t(h, &h->dStates, P)) || (r = dalloc_t(h, &h->dVec, P * 5 * h->nFree)) ||
+        (r = dalloc_t(h, &h->dAlpha, P * h->nPar)) || (r = dalloc_t(h, &h->dAlphaOff, P * h->nPar)) ||
+        (r = dalloc_t(h, &h->dActive, 1)))
+        return r;
+    CK(h, cudaMallocHost((void**)&h->hActive, sizeof(int32_t)));
+    CK(h, cudaMemset(h->dReinit, 0, G));
+    return RDXG_OK;
+}
+
+int build_nullspace(rdxg_solver* h, const rdxg_static* s) {
+    const int nPar = h->nPar, nF = h->nFree;
+    std::vector<int32_t> rc(nPar + 1, 0), cc(nF + 1, 0);
+    for (int64_t e = 0; e < s->ns_nnz; ++e) {
+        const int r = s->ns_rows[e], c = s->ns_cols[e];
+        if (r < 0 || r >= nPar || c < 0 || c >= nF) { h->err = "null-space entry out of range"; return RDXG_ERR_ARG; }
+        rc[r + 1]++;
+        cc[c + 1]++;
+    }
+    for (int i = 0; i < nPar; ++i) rc[i + 1] += rc[i];
+    for (int i = 0; i < nF; ++i) cc[i + 1] += cc[i];
+    std::vector<int32_t> rcol(s->ns_nnz), crow(s->ns_nnz), rfill(rc.begin(), rc.end() - 1), cfill(cc.begin(), cc.end() - 1);
+    std::vector<double> rval(s->ns_nnz), cval(s->ns_nnz);
+    for (int64_t e = 0; e < s->ns_nnz; ++e) {
+        const int r = s->ns_rows[e], c = s->ns_cols[e];
+        rcol[rfill[r]] = c; rval[rfill[r]++] = s->ns_vals[e];
+        crow[cfill[c]] = r; cval[cfill[c]++] = s->ns_vals[e];
+    }
+    int r;
+    void* v;
+    if ((r = upload(h, &v, rc))) return r;
+    h->dRowPtr = (int32_t*)v;
+    if ((r = upload(h, &v, rcol))) return r;
+    h->dRowCol = (int32_t*)v;
+    if ((r = upload(h, &v, rval))) return r;
+    h->dRowVal = (double*)v;
+    if ((r = upload(h, &v, cc))) return r;
+    h->dColPtr = (int32_t*)v;
+    if ((r = upload(h, &v, crow))) return r;
+    h->dColRow = (int32_t*)v;
+    if ((r = upload(h, &v, cval))) return r;
+    h->dColVal = (double*)v;
+    return RDXG_OK;
+}
+
+// (re)initialise the loaded patches: shifts 0, full image preparation, gamma
+int prepare_patches(rdxg_solver* h) {
+    const size_t G = (size_t)h->P * h->I;
+    CK(h, cudaMemsetAsync(h->dShift, 0, G * 2 * sizeof(int32_t), h->stream));
+    CK(h, cudaMemsetAsync(h->dCurTilt, 0, G * 2 * sizeof(double), h->stream));
+    CK(h, cudaMemcpyAsync(h->dResAlpha, h->hResAlpha.data(), G * 2 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    int rc = RDXG_OK;
+    with_size(h->N, h->fp64, [&](auto L, auto t) {
+        using T = decltype(t);
+        KParams<T> kp = make_kparams<T>(h);
+        decltype(L)::prep(kp, 1, (int)G, h->stream);
+    });
+    h->launches++;
+    CKL(h);
+    std::vector<double> rg(G);
+    CK(h, cudaMemcpyAsync(rg.data(), h->dRg, G * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    // Object::addRegGamma (object.cpp:465-468): reg_gamma = sum_j 0.1 rg_j / nObjectImages
+    std::vector<double> gam((size_t)h->P * h->nObj, 0.0);
+    for (int p = 0; p < h->P; ++p) {
+        for (int j = 0; j < h->I; ++j) {
+            const int o = h->imgObj[j];
+            gam[(size_t)p * h->nObj + o] += 0.10 * rg[(size_t)p * h->I + j] / h->objCount[o];
+        }
+    }
+    if (h->haveFixedGamma) gam = h->hFixedGamma;
+    for (double g : gam) {
+        if (!std::isfinite(g)) { h->err = "non-finite regularisation (image with zero variance?)"; rc = RDXG_ERR_NONFINITE; }
+    }
+    CK(h, cudaMemcpyAsync(h->dGamma, gam.data(), gam.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->dirty = false;
+    return rc;
+}
+
+int set_patches_common(rdxg_solver* h, int32_t P, const double* residual_alpha, const double* fixed_gamma) {
+    if (P < 1 || P > h->Pmax) { h->err = "n_patches out of range"; return RDXG_ERR_ARG; }
+    h->P = P;
+    const size_t G = (size_t)P * h->I;
+    h->hResAlpha.assign(G * 2, 0.0);
+    if (residual_alpha) std::memcpy(h->hResAlpha.data(), residual_alpha, G * 2 * sizeof(double));
+    h->haveFixedGamma = fixed_gamma != nullptr;
+    if (fixed_gamma) h->hFixedGamma.assign(fixed_gamma, fixed_gamma + (size_t)P * h->nObj);
+    int r = prepare_patches(h);
+    h->loaded = (r == RDXG_OK);
+    return r;
+}
+
+// alpha_eff on the host for single evaluations
+template <typename T>
+int upload_alpha(rdxg_solver* h, const double* alpha) {
+    const size_t G = (size_t)h->P * h->I;
+    std::vector<double> curTilt(G * 2);
+    CK(h, cudaMemcpyAsync(curTilt.data(), h->dCurTilt, G * 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    std::vector<T> ae(G * h->M);
+    for (size_t g = 0; g < G; ++g) {
+        for (int m = 0; m < h->M; ++m) {
+            double v = alpha[g * h->M + m];
+            if (m == h->geo.tilt_x) v += curTilt[g * 2 + 1] - h->hResAlpha[g * 2 + 1];
+            else if (m == h->geo.tilt_y) v += curTilt[g * 2 + 0] - h->hResAlpha[g * 2 + 0];
+            ae[g * h->M + m] = (T)v;
+        }
+    }
+    CK(h, cudaMemcpyAsync(h->dAlphaEff, ae.data(), ae.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return RDXG_OK;
+}
+
+int metric_from_partials(rdxg_solver* h, double* metric) {
+    const size_t PO = (size_t)h->P * h->nObj;
+    std::vector<double> part(PO * h->nTiles);
+    CK(h, cudaMemcpyAsync(part.data(), h->dPartial, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int p = 0; p < h->P; ++p) {
+        double sum = 0;
+        for (int o = 0; o < h->nObj; ++o) {
+            if (h->objWeight[o] == 0.0) continue;
+            double m = 0;
+            for (int t = 0; t < h->nTiles; ++t) m += part[((size_t)p * h->nObj + o) * h->nTiles + t];
+            sum += h->objWeight[o] * (m / ((double)h->ps * h->ps));
+        }
+        metric[p] = sum;
+    }
+    return RDXG_OK;
+}
+
+int set_requests(rdxg_solver* h, int req, int gm, int mc) {
+    std::vector<int32_t> a(h->P, req), b(h->P, gm), c(h->P, mc);
+    CK(h, cudaMemcpyAsync(h->dReq, a.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->dGm, b.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->dMc, c.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return RDXG_OK;
+}
+
+CgParams make_cg_params(rdxg_solver* h, const rdxg_solve_params* s) {
+    CgParams prm{};
+    prm.n_free = h->nFree;
+    prm.n_modes = h->M;
+    prm.mode_start = s->mode_start > 0 ? s->mode_start : 1;
+    prm.mode_step = s->mode_step > 0 ? s->mode_step : 1;
+    prm.max_iterations = s->max_iterations;
+    prm.min_iterations = s->min_iterations;
+    prm.target_iterations = s->target_iterations;
+    prm.fd_first = s->fd_first;
+    prm.max_fails = 3;
+    prm.max_metrics = s->max_metrics > 0 ? s->max_metrics : 1;
+    prm.ftol = s->ftol;
+    prm.eps = s->eps;
+    const double nTotalPixels = (double)h->I * h->ps * h->ps;
+    prm.grad_scale = 1.0 / (nTotalPixels * nTotalPixels);
+    prm.brent_tol = 0.1;
+    prm.init_step = 1E-21;
+    return prm;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rdxg_version(void) { return 100; }
+
+const char* rdxg_last_error(const rdxg_solver* h) { return h ? h->err.c_str() : "null handle"; }
+
+int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out) {
+    if (!g || !s || !out) return RDXG_ERR_ARG;
+    *out = nullptr;
+    rdxg_solver* h = new rdxg_solver();
+    h->geo = *g;
+    h->N = g->otf_size; h->n = g->pupil_pixels; h->ps = g->patch_size; h->M = g->n_modes;
+    h->I = g->n_images; h->nObj = g->n_objects; h->C = g->n_channels; h->nFree = g->n_free;
+    h->cs = g->cutout_size > 0 ? g->cutout_size : g->patch_size;
+    h->margin = (h->cs - h->ps) / 2;
+    h->nPar = h->I * h->M;
+    h->Pmax = g->max_patches;
+    h->fp64 = g->precision == RDXG_FP64;
+    auto fail = [&](int code, const char* msg) {
+        if (msg) h->err = msg;
+        *out = h;          // hand the handle back so the caller can read the message
+        return code;
+    };
+    if (h->N != 2 * h->n) return fail(RDXG_ERR_ARG, "otf_size must be 2 * pupil_pixels");
+    if (!supported_N(h->N)) return fail(RDXG_ERR_UNSUPPORTED, "otf_size not compiled (supported: 32, 64, 88, 128)");
+    if (h->ps != h->N) return fail(RDXG_ERR_UNSUPPORTED, "patch_size must equal otf_size");
+    if (h->cs < h->ps || ((h->cs - h->ps) & 1)) return fail(RDXG_ERR_ARG, "bad cutout_size");
+    if (h->M < 1 || h->I < 1 || h->nObj < 1 || h->nObj > 64 || h->C < 1 || h->Pmax < 1 || h->nFree < 1)
+        return fail(RDXG_ERR_ARG, "bad geometry");
+    h->imgObj.assign(s->image_object, s->image_object + h->I);
+    h->imgCh.assign(s->image_channel, s->image_channel + h->I);
+    h->objFirst.assign(h->nObj, -1);
+    h->objCount.assign(h->nObj, 0);
+    for (int j = 0; j < h->I; ++j) {
+        const int o = h->imgObj[j];
+        if (o < 0 || o >= h->nObj || h->imgCh[j] < 0 || h->imgCh[j] >= h->C) return fail(RDXG_ERR_ARG, "bad image map");
+        if (h->objFirst[o] < 0) h->objFirst[o] = j;
+        if (h->objFirst[o] + h->objCount[o] != j) return fail(RDXG_ERR_ARG, "images of an object must be contiguous");
+        h->objCount[o]++;
+    }
+    for (int o = 0; o < h->nObj; ++o)
+        if (h->objCount[o] == 0) return fail(RDXG_ERR_ARG, "object without images");
+    h->objWeight.assign(s->object_weight, s->object_weight + h->nObj);
+    h->gradStep.assign(s->object_grad_step, s->object_grad_step + h->nObj);
+    if (s->tilt_jacobian) {
+        h->haveJ = true;
+        h->J[0][0] = s->tilt_jacobian[0]; h->J[0][1] = s->tilt_jacobian[1];
+        h->J[1][0] = s->tilt_jacobian[2]; h->J[1][1] = s->tilt_jacobian[3];
+        const double det = h->J[0][0] * h->J[1][1] - h->J[0][1] * h->J[1][0];
+        h->Jinv[0][0] = h->J[1][1] / det; h->Jinv[0][1] = -h->J[0][1] / det;
+        h->Jinv[1][0] = -h->J[1][0] / det; h->Jinv[1][1] = h->J[0][0] / det;
+    }
+    h->nTiles = (h->N * h->N + kAccumThreads - 1) / kAccumThreads;
+    cudaError_t e = cudaSetDevice(g->device);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); *out = h; return RDXG_ERR_CUDA; }
+    e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); *out = h; return RDXG_ERR_CUDA; }
+    h->stream = h->own;
+    int r = h->fp64 ? create_static<double>(h, s) : create_static<float>(h, s);
+    if (!r) r = build_nullspace(h, s);
+    if (!r) r = h->fp64 ? alloc_patch_buffers<double>(h) : alloc_patch_buffers<float>(h);
+    std::vector<double> win(s->window, s->window + (size_t)h->ps * h->ps), nwin(s->noise_window, s->noise_window + (size_t)h->ps * h->ps);
+    std::vector<int32_t> of(h->objFirst), oc(h->objCount);
+    void* v;
+    if (!r) { r = upload(h, &v, win); h->dWin = (double*)v; }
+    if (!r) { r = upload(h, &v, nwin); h->dNWin = (double*)v; }
+    if (!r) { r = upload(h, &v, h->imgObj); h->dImgObj = (int32_t*)v; }
+    if (!r) { r = upload(h, &v, h->imgCh); h->dImgCh = (int32_t*)v; }
+    if (!r) { r = upload(h, &v, of); h->dObjFirst = (int32_t*)v; }
+    if (!r) { r = upload(h, &v, oc); h->dObjCount = (int32_t*)v; }
+    if (!r) { r = upload(h, &v, h->objWeight); h->dObjW = (double*)v; }
+    if (!r) { r = upload(h, &v, h->gradStep); h->dGradStep = (double*)v; }
+    if (!r) {
+        cudaError_t se = cudaSuccess;
+        with_size(h->N, h->fp64, [&](auto L, auto) { se = decltype(L)::setup(h->M); });
+        if (se != cudaSuccess) { h->err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(se); r = RDXG_ERR_CUDA; }
+    }
+    *out = h;
+    return r;
+}
+
+int rdxg_destroy(rdxg_solver* h) {
+    if (!h) return RDXG_OK;
+    for (void* p : h->allocs) cudaFree(p);
+    if (h->hActive) cudaFreeHost(h->hActive);
+    if (h->own) cudaStreamDestroy(h->own);
+    delete h;
+    return RDXG_OK;
+}
+
+int rdxg_set_stream(rdxg_solver* h, void* st) {
+    if (!h) return RDXG_ERR_ARG;
+    h->stream = st ? (cudaStream_t)st : h->own;
+    return RDXG_OK;
+}
+
+int rdxg_set_patches(rdxg_solver* h, int32_t P, const float* cut, const double* ra, const double* fg) {
+    if (!h || !cut) return RDXG_ERR_ARG;
+    if (P < 1 || P > h->Pmax) { h->err = "n_patches out of range"; return RDXG_ERR_ARG; }
+    h->dCutExt = nullptr;
+    CK(h, cudaMemcpyAsync(h->dCut, cut, (size_t)P * h->I * h->cs * h->cs * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    return set_patches_common(h, P, ra, fg);
+}
+
+int rdxg_set_patches_device(rdxg_solver* h, int32_t P, const float* dcut, const double* ra, const double* fg) {
+    if (!h || !dcut) return RDXG_ERR_ARG;
+    h->dCutExt = dcut;
+    return set_patches_common(h, P, ra, fg);
+}
+
+int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric) {
+    if (!h || !alpha || !metric) return RDXG_ERR_ARG;
+    if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
+    int r = h->fp64 ? upload_alpha<double>(h, alpha) : upload_alpha<float>(h, alpha);
+    if (r) return r;
+    if ((r = set_requests(h, REQ_F, GM_VOGEL, h->M))) return r;
+    with_size(h->N, h->fp64, [&](auto L, auto t) {
+        using T = decltype(t);
+        KParams<T> kp = make_kparams<T>(h);
+        decltype(L)::forward(kp, h->P * h->I, h->stream);
+        launch_accum<T>(kp, h->P * h->nObj, h->stream);
+    });
+    CKL(h);
+    return metric_from_partials(h, metric);
+}
+
+int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, int32_t method, double* grad,
+                  double* metric) {
+    if (!h || !alpha || !grad) return RDXG_ERR_ARG;
+    if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
+    if (method != RDXG_GRAD_VOGEL && method != RDXG_GRAD_EXACT && method != RDXG_GRAD_FD) return RDXG_ERR_ARG;
+    int r = h->fp64 ? upload_alpha<double>(h, alpha) : upload_alpha<float>(h, alpha);
+    if (r) return r;
+    const int gm = method == RDXG_GRAD_FD ? GM_FD : GM_VOGEL;
+    if ((r = set_requests(h, REQ_DF, gm, h->M))) return r;
+    with_size(h->N, h->fp64, [&](auto L, auto t) {
+        using T = decltype(t);
+        KParams<T> kp = make_kparams<T>(h);
+        decltype(L)::forward(kp, h->P * h->I, h->stream);
+        launch_accum<T>(kp, h->P * h->nObj, h->stream);
+        if (method == RDXG_GRAD_FD) decltype(L)::fd(kp, h->P * h->I, h->M, h->stream);
+        else decltype(L)::adjoint(kp, h->P * h->I, method == RDXG_GRAD_EXACT ? GK_EXACT : GK_VOGEL, h->stream);
+    });
+    CKL(h);
+    const size_t G = (size_t)h->P * h->I;
+    CK(h, cudaMemcpyAsync(grad, h->dGalpha, G * h->M * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (enabled)
+        for (size_t g = 0; g < G; ++g)
+            for (int m = 0; m < h->M; ++m)
+                if (!enabled[m]) grad[g * h->M + m] = 0.0;
+    if (metric) return metric_from_partials(h, metric);
+    return RDXG_OK;
+}
+
+int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
+    if (!h || !s) return RDXG_ERR_ARG;
+    if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
+    int r;
+    if (h->dirty && (r = prepare_patches(h))) return r;
+    h->dirty = true;
+    h->launches = 0;
+    h->lastParams = *s;
+    const CgParams prm = make_cg_params(h, s);
+    if (prm.max_metrics != h->maxMetrics) {
+        if (h->dMetrics) {
+            for (auto it = h->allocs.begin(); it != h->allocs.end(); ++it)
+                if (*it == h->dMetrics) { cudaFree(*it); h->allocs.erase(it); break; }
+            h->dMetrics = nullptr;
+        }
+        if ((r = dalloc_t(h, &h->dMetrics, (size_t)h->Pmax * prm.max_metrics))) return r;
+        h->maxMetrics = prm.max_metrics;
+    }
+    const int P = h->P;
+    CK(h, cudaMemsetAsync(h->dStates, 0, P * sizeof(CgState), h->stream));
+    CK(h, cudaMemsetAsync(h->dVec, 0, (size_t)P * 5 * h->nFree * sizeof(double), h->stream));
+    CK(h, cudaMemsetAsync(h->dAlphaOff, 0, (size_t)P * h->nPar * sizeof(double), h->stream));
+    CK(h, cudaMemsetAsync(h->dAlpha, 0, (size_t)P * h->nPar * sizeof(double), h->stream));
+    const int check = s->check_every > 0 ? s->check_every : 8;
+    ShiftArgs sa{};
+    sa.P = P; sa.I = h->I; sa.M = h->M; sa.nObj = h->nObj; sa.ps = h->ps; sa.cs = h->cs; sa.margin = h->margin;
+    sa.tiltX = h->haveJ ? h->geo.tilt_x : -1; sa.tiltY = h->haveJ ? h->geo.tilt_y : -1;
+    sa.req = h->dReq; sa.alpha = h->dAlpha; sa.tiltOff = h->dCurTilt; sa.shift = h->dShift;
+    sa.reinit = h->dReinit; sa.imgObj = h->dImgObj;
+    std::memcpy(sa.J, h->J, sizeof(sa.J));
+    std::memcpy(sa.Jinv, h->Jinv, sizeof(sa.Jinv));
+    const int G = P * h->I;
+    for (long round = 0;; ++round) {
+        CK(h, cudaMemsetAsync(h->dActive, 0, sizeof(int32_t), h->stream));
+        with_size(h->N, h->fp64, [&](auto L, auto t) {
+            using T = decltype(t);
+            KParams<T> kp = make_kparams<T>(h);
+            CgArgs<T> ca = make_cgargs<T>(h, prm);
+            launch_cg<T>(ca, P, h->stream);
+            launch_shift(sa, P, h->stream);
+            decltype(L)::prep(kp, 0, G, h->stream);
+            decltype(L)::forward(kp, G, h->stream);
+            launch_accum<T>(kp, P * h->nObj, h->stream);
+            decltype(L)::adjoint(kp, G, GK_VOGEL, h->stream);
+            // all patches reach their first gradient together (round 2 of the first stage);
+            // later gradients use the analytic method
+            if (prm.fd_first && round == 2) { decltype(L)::fd(kp, G, h->M, h->stream); h->launches++; }
+        });
+        h->launches += 6;
+        CKL(h);
+        if ((round + 1) % check == 0) {
+            CK(h, cudaMemcpyAsync(h->hActive, h->dActive, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+            CK(h, cudaStreamSynchronize(h->stream));
+            if (*h->hActive == 0) break;
+        }
+        if (round > 2000000L) { h->err = "solver did not terminate"; return RDXG_ERR_STATE; }
+    }
+    return RDXG_OK;
+}
+
+int rdxg_fetch_results(rdxg_solver* h, double* alpha_out, rdxg_patch_report* reports, double* metrics) {
+    if (!h) return RDXG_ERR_ARG;
+    const int P = h->P;
+    if (alpha_out)
+        CK(h, cudaMemcpyAsync(alpha_out, h->dAlpha, (size_t)P * h->nPar * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    std::vector<CgState> st(P);
+    CK(h, cudaMemcpyAsync(st.data(), h->dStates, P * sizeof(CgState), cudaMemcpyDeviceToHost, h->stream));
+    if (metrics && h->dMetrics)
+        CK(h, cudaMemcpyAsync(metrics, h->dMetrics, (size_t)P * h->maxMetrics * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (reports) {
+        for (int p = 0; p < P; ++p) {
+            rdxg_patch_report& r = reports[p];
+            r.initial_metric = st[p].initial_metric;
+            r.final_metric = st[p].this_metric;
+            r.iterations = st[p].total_iterations;
+            r.status = st[p].status == ST_FAILURE ? 1 : 0;
+            r.n_f_evals = st[p].n_f;
+            r.n_df_evals = st[p].n_df;
+            r.fail_count = st[p].fail_count;
+            r.n_metrics = st[p].n_metrics;
+        }
+    }
+    return RDXG_OK;
+}
+
+int rdxg_solve(rdxg_solver* h, const rdxg_solve_params* s, double* alpha_out, rdxg_patch_report* reports,
+               double* metrics) {
+    int r = rdxg_solve_async(h, s);
+    if (r) return r;
+    return rdxg_fetch_results(h, alpha_out, reports, metrics);
+}
+
+int64_t rdxg_last_launch_count(const rdxg_solver* h) { return h ? h->launches : 0; }
+
+int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes) {
+    if (!h || !out) return RDXG_ERR_ARG;
+    const size_t G = (size_t)h->P * h->I, N2 = (size_t)h->N * h->N, PO = (size_t)h->P * h->nObj;
+    const size_t cxs = h->fp64 ? 16 : 8;
+    CK(h, cudaStreamSynchronize(h->stream));
+    switch (which) {
+        case 0: if (bytes < G * N2 * cxs) return RDXG_ERR_ARG; CK(h, cudaMemcpy(out, h->dD, G * N2 * cxs, cudaMemcpyDeviceToHost)); break;
+        case 1: if (bytes < G * N2 * cxs) return RDXG_ERR_ARG; CK(h, cudaMemcpy(out, h->dS, G * N2 * cxs, cudaMemcpyDeviceToHost)); break;
+        case 2: if (bytes < PO * 8) return RDXG_ERR_ARG; CK(h, cudaMemcpy(out, h->dGamma, PO * 8, cudaMemcpyDeviceToHost)); break;
+        case 3: {
+            if (bytes < G * 3 * 8) return RDXG_ERR_ARG;
+            std::vector<double> a(G), b(G), c(G);
+            CK(h, cudaMemcpy(a.data(), h->dMean, G * 8, cudaMemcpyDeviceToHost));
+            CK(h, cudaMemcpy(b.data(), h->dStd, G * 8, cudaMemcpyDeviceToHost));
+            CK(h, cudaMemcpy(c.data(), h->dNoise, G * 8, cudaMemcpyDeviceToHost));
+            double* o = (double*)out;
+            for (size_t g = 0; g < G; ++g) { o[3 * g] = a[g]; o[3 * g + 1] = b[g]; o[3 * g + 2] = c[g]; }
+            break;
+        }
+        case 4: if (bytes < PO * N2 * cxs) return RDXG_ERR_ARG; CK(h, cudaMemcpy(out, h->dO, PO * N2 * cxs, cudaMemcpyDeviceToHost)); break;
+        case 5: if (bytes < G * 2 * 4) return RDXG_ERR_ARG; CK(h, cudaMemcpy(out, h->dShift, G * 8, cudaMemcpyDeviceToHost)); break;
+        default: return RDXG_ERR_ARG;
+    }
+    return RDXG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,217 @@
+// Device side of the per-patch optimiser: one thread block per patch runs the state
+// machine of cg_machine.h (scalar logic replicated in every thread, vector operations
+// block-parallel, all sums in double in a fixed order), maps the point of the next
+// evaluation through the null-space map (Constraints::reverseAndAdd,
+// constraints.hpp:141-146) and the gradient back (Constraints::apply, 128-133), and
+// performs the integer image re-shifts between mode stages (SubImage::adjustShifts,
+// subimage.cpp:444-480).
+#pragma once
+
+#include "cg_machine.h"
+#include "rdxg_kernels.cuh"
+
+namespace rdxg {
+
+template <int THREADS>
+struct DevVec {
+    int n;
+    double* red;
+    __device__ void copy(double* d, const double* s) {
+        for (int i = threadIdx.x; i < n; i += THREADS) d[i] = s[i];
+        __syncthreads();
+    }
+    __device__ void zero(double* d) {
+        for (int i = threadIdx.x; i < n; i += THREADS) d[i] = 0.0;
+        __syncthreads();
+    }
+    __device__ double nrm2(const double* v) {
+        double a = 0;
+        for (int i = threadIdx.x; i < n; i += THREADS) a += v[i] * v[i];
+        return sqrt(block_sum<THREADS>(a, red));
+    }
+    __device__ double dot(const double* x, const double* y) {
+        double a = 0;
+        for (int i = threadIdx.x; i < n; i += THREADS) a += x[i] * y[i];
+        return block_sum<THREADS>(a, red);
+    }
+    __device__ double pr_update(double* g0, const double* g) {
+        double a = 0;
+        for (int i = threadIdx.x; i < n; i += THREADS) {
+            const double t = g0[i] - g[i];
+            a += t * g[i];
+            g0[i] = t;
+        }
+        return block_sum<THREADS>(a, red);
+    }
+    __device__ void dir_update(double* p, const double* g, double beta) {
+        for (int i = threadIdx.x; i < n; i += THREADS) p[i] = g[i] - beta * p[i];
+        __syncthreads();
+    }
+    __device__ void step(double* x1, const double* x, const double* p, double s) {
+        for (int i = threadIdx.x; i < n; i += THREADS) x1[i] = x[i] + s * p[i];
+        __syncthreads();
+    }
+};
+
+template <typename T>
+struct CgArgs {
+    CgParams prm;
+    int32_t P, I, M, nObj, nPar, nTiles, ps;
+    CgState* states;        // [P]
+    double* vec;            // [P][5][nFree]: x, p, g, g0, x1
+    double* metrics;        // [P][max_metrics]
+    double* alpha;          // [P][nPar]
+    double* alphaOff;       // [P][nPar]
+    const double* galpha;   // [P][nPar]
+    const double* partial;  // [P][nObj][nTiles]
+    const double* objWeight;
+    // null-space map, by parameter row and by free column
+    const int32_t* rowPtr; const int32_t* rowCol; const double* rowVal;
+    const int32_t* colPtr; const int32_t* colRow; const double* colVal;
+    const double* curTilt;  // [P][I][2] (y, x): currentTiltOffset of each image
+    const double* resAlpha; // [P][I][2] (y, x): channel residual tilt (phi_channel term)
+    int32_t tiltX, tiltY;
+    T* alphaEff;            // [P][I][M]
+    int32_t* req;
+    int32_t* gmethod;
+    int32_t* modeCount;
+    int32_t* active;
+};
+
+// alpha = offset + N x1; alpha_eff = alpha + currentTiltOffset - residual for the tilt modes
+// (the residual is what Channel::initPatch adds to phi_channel, channel.cpp:916-939)
+template <typename T, int THREADS>
+__device__ void map_point(const CgArgs<T>& a, int p, const double* x1) {
+    const double* off = a.alphaOff + (size_t)p * a.nPar;
+    double* al = a.alpha + (size_t)p * a.nPar;
+    T* ae = a.alphaEff + (size_t)p * a.nPar;
+    for (int r = threadIdx.x; r < a.nPar; r += THREADS) {
+        double v = off[r];
+        for (int e = a.rowPtr[r]; e < a.rowPtr[r + 1]; ++e) v += a.rowVal[e] * x1[a.rowCol[e]];
+        al[r] = v;
+        const int j = r / a.M, m = r % a.M;
+        double ve = v;
+        const size_t b = ((size_t)p * a.I + j) * 2;
+        if (m == a.tiltX) ve += a.curTilt[b + 1] - a.resAlpha[b + 1];
+        else if (m == a.tiltY) ve += a.curTilt[b + 0] - a.resAlpha[b + 0];
+        ae[r] = (T)ve;
+    }
+    __syncthreads();
+}
+
+template <typename T, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
+    const int p = blockIdx.x;
+    __shared__ double red[33];
+    __shared__ double fsh;
+    CgState st = a.states[p];
+    const int nF = a.prm.n_free;
+    double* x = a.vec + (size_t)p * 5 * nF;
+    double* pv = x + nF;
+    double* g = pv + nF;
+    double* g0 = g + nF;
+    double* x1 = g0 + nF;
+    if (st.pc == PC_DONE) {
+        if (threadIdx.x == 0) a.req[p] = REQ_DONE;
+        return;
+    }
+    double f = 0;
+    if (st.req == REQ_F) {
+        if (threadIdx.x == 0) {
+            double sum = 0;
+            for (int o = 0; o < a.nObj; ++o) {
+                const double w = a.objWeight[o];
+                if (w == 0.0) continue;
+                double m = 0;
+                const double* pp = a.partial + ((size_t)p * a.nObj + o) * a.nTiles;
+                for (int t = 0; t < a.nTiles; ++t) m += pp[t];
+                sum += w * (m / ((double)a.ps * a.ps));
+            }
+            fsh = sum;
+        }
+        __syncthreads();
+        f = fsh;
+    } else if (st.req == REQ_DF) {
+        const double* ga = a.galpha + (size_t)p * a.nPar;
+        for (int c = threadIdx.x; c < nF; c += THREADS) {
+            double v = 0;
+            for (int e = a.colPtr[c]; e < a.colPtr[c + 1]; ++e) v += a.colVal[e] * ga[a.colRow[e]];
+            g[c] = v;
+        }
+        __syncthreads();
+    } else if (st.req == REQ_SHIFT) {
+        double* off = a.alphaOff + (size_t)p * a.nPar;
+        const double* al = a.alpha + (size_t)p * a.nPar;
+        for (int r = threadIdx.x; r < a.nPar; r += THREADS) off[r] = al[r];
+        __syncthreads();
+    }
+    DevVec<THREADS> V{nF, red};
+    Machine<DevVec<THREADS>> mc(a.prm, st, V, x, pv, g, g0, x1, a.metrics + (size_t)p * a.prm.max_metrics);
+    const int rq = mc.advance(f);
+    if (rq == REQ_F || rq == REQ_DF || rq == REQ_SHIFT) map_point<T, THREADS>(a, p, x1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a.states[p] = st;
+        a.req[p] = rq;
+        a.gmethod[p] = st.grad_method;
+        a.modeCount[p] = st.mode_count;
+        if (rq != REQ_DONE) atomicAdd(a.active, 1);
+    }
+}
+
+// adjustShifts for every image of patches that requested a re-shift; marks the images of
+// every object that has a shifted image for re-initialisation (Object::reInitialize).
+struct ShiftArgs {
+    int32_t P, I, M, nObj, ps, cs, margin, tiltX, tiltY;
+    const int32_t* req;
+    const double* alpha;     // [P][I*M]
+    double* tiltOff;         // [P][I][2] currentTiltOffset (y, x)
+    int32_t* shift;          // [P][I][2]
+    uint8_t* reinit;         // [P][I]
+    const int32_t* imgObj;
+    double J[2][2], Jinv[2][2];
+};
+
+template <int UNUSED = 0>
+__global__ void k_shift(ShiftArgs a) {
+    const int p = blockIdx.x;
+    if (a.req[p] != REQ_SHIFT) {
+        for (int j = threadIdx.x; j < a.I; j += blockDim.x) a.reinit[(size_t)p * a.I + j] = 0;
+        return;
+    }
+    __shared__ int objShifted[64];
+    for (int o = threadIdx.x; o < a.nObj; o += blockDim.x) objShifted[o] = 0;
+    __syncthreads();
+    for (int j = threadIdx.x; j < a.I; j += blockDim.x) {
+        const size_t gi = (size_t)p * a.I + j;
+        const double* al = a.alpha + gi * a.M;
+        if (a.tiltX < 0 || a.tiltY < 0) continue;
+        const double ay = al[a.tiltY] + a.tiltOff[gi * 2 + 0];
+        const double ax = al[a.tiltX] + a.tiltOff[gi * 2 + 1];
+        const double sy = ax * a.J[1][0] + ay * a.J[1][1];
+        const double sx = ax * a.J[0][0] + ay * a.J[0][1];
+        const int want[2] = {-(int)llround(sy), -(int)llround(sx)};
+        int act[2] = {0, 0};
+        for (int d = 0; d < 2; ++d) {
+            int nsh = want[d];
+            if (!nsh) continue;
+            const int first = a.margin + a.shift[gi * 2 + d];
+            const int last = first + a.ps - 1;
+            if (nsh + first < 0) nsh = -first;
+            if (abs(nsh + last) >= a.cs) nsh = a.cs - last - 1;
+            act[d] = nsh;
+        }
+        if (act[0] || act[1]) {
+            a.shift[gi * 2 + 0] += act[0];
+            a.shift[gi * 2 + 1] += act[1];
+            a.tiltOff[gi * 2 + 0] += act[1] * a.Jinv[1][0] + act[0] * a.Jinv[1][1];
+            a.tiltOff[gi * 2 + 1] += act[1] * a.Jinv[0][0] + act[0] * a.Jinv[0][1];
+            atomicExch(&objShifted[a.imgObj[j]], 1);
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < a.I; j += blockDim.x)
+        a.reinit[(size_t)p * a.I + j] = objShifted[a.imgObj[j]] ? 1 : 0;
+}
+
+}  // namespace rdxg

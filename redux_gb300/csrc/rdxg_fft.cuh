@@ -1,0 +1,250 @@
+// Shared-memory 2-D FFT for one N x N complex tile per thread block.
+//
+// Stockham auto-sort, one radix per stage, register-staged in place: every thread loads
+// the inputs of its butterflies, the block synchronises, every thread writes its outputs.
+// Rows are padded to LDS = N + 1 elements so that the row pass (lanes on consecutive
+// rows) and the column pass (lanes on consecutive columns) are both free of shared-memory
+// bank conflicts for 8-byte elements.
+//
+// Convention (as FFTW): forward DIR = -1 computes X[k] = sum_x x[x] exp(-2 pi i k.x / N),
+// inverse DIR = +1 the same with exp(+...), both unnormalised.
+//
+// Two-stage plans N = R1 * R2 (R2 may be odd: the radix-11 pass is what makes N = 88 work
+// without padding, which would change the image transform).  Twiddles come from a per-N
+// table tw[k] = exp(-2 pi i k / N) in shared memory, built on the host in double precision.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft_tables.h"
+
+namespace rdxg {
+
+template <typename T> struct CxT;
+template <> struct CxT<float> { using type = float2; };
+template <> struct CxT<double> { using type = double2; };
+template <typename T> using cx = typename CxT<T>::type;
+
+template <typename T> __device__ __forceinline__ cx<T> mkc(T r, T i) { cx<T> c; c.x = r; c.y = i; return c; }
+template <typename T> __device__ __forceinline__ cx<T> cadd(cx<T> a, cx<T> b) { return mkc<T>(a.x + b.x, a.y + b.y); }
+template <typename T> __device__ __forceinline__ cx<T> csub(cx<T> a, cx<T> b) { return mkc<T>(a.x - b.x, a.y - b.y); }
+template <typename T> __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) {
+    return mkc<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename T> __device__ __forceinline__ cx<T> cmulc(cx<T> a, cx<T> b) {
+    return mkc<T>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <typename T> __device__ __forceinline__ cx<T> cscale(cx<T> a, T s) { return mkc<T>(a.x * s, a.y * s); }
+template <typename T> __device__ __forceinline__ T cnorm(cx<T> a) { return a.x * a.x + a.y * a.y; }
+// multiply by i*s (s = +-1)
+template <int S, typename T> __device__ __forceinline__ cx<T> mul_is(cx<T> a) {
+    return S > 0 ? mkc<T>(-a.y, a.x) : mkc<T>(a.y, -a.x);
+}
+
+template <typename T> __device__ __forceinline__ T tab_cos(int R, int k);
+template <typename T> __device__ __forceinline__ T tab_sin(int R, int k);
+
+#define RDXG_TAB(R)                                                                                   \
+    template <typename T> struct Tab##R;                                                              \
+    template <> struct Tab##R<float> {                                                                \
+        __device__ static __forceinline__ float c(int k) { return kCos##R##f[k]; }                    \
+        __device__ static __forceinline__ float s(int k) { return kSin##R##f[k]; }                    \
+    };                                                                                                \
+    template <> struct Tab##R<double> {                                                               \
+        __device__ static __forceinline__ double c(int k) { return kCos##R##d[k]; }                   \
+        __device__ static __forceinline__ double s(int k) { return kSin##R##d[k]; }                   \
+    };
+RDXG_TAB(3)
+RDXG_TAB(5)
+RDXG_TAB(7)
+RDXG_TAB(9)
+RDXG_TAB(11)
+RDXG_TAB(13)
+RDXG_TAB(16)
+#undef RDXG_TAB
+
+template <int R, typename T> struct OddTab;
+template <typename T> struct OddTab<3, T> : Tab3<T> {};
+template <typename T> struct OddTab<5, T> : Tab5<T> {};
+template <typename T> struct OddTab<7, T> : Tab7<T> {};
+template <typename T> struct OddTab<9, T> : Tab9<T> {};
+template <typename T> struct OddTab<11, T> : Tab11<T> {};
+template <typename T> struct OddTab<13, T> : Tab13<T> {};
+
+// ------------------------------ butterflies ------------------------------
+
+template <int R, int DIR, typename T> struct Dft;
+
+template <int DIR, typename T> struct Dft<2, DIR, T> {
+    __device__ static __forceinline__ void run(cx<T>* v) {
+        cx<T> a = v[0], b = v[1];
+        v[0] = cadd<T>(a, b);
+        v[1] = csub<T>(a, b);
+    }
+};
+
+template <int DIR, typename T> struct Dft<4, DIR, T> {
+    __device__ static __forceinline__ void run(cx<T>* v) {
+        cx<T> a0 = cadd<T>(v[0], v[2]), a1 = csub<T>(v[0], v[2]);
+        cx<T> b0 = cadd<T>(v[1], v[3]), b1 = mul_is<DIR, T>(csub<T>(v[1], v[3]));
+        v[0] = cadd<T>(a0, b0);
+        v[2] = csub<T>(a0, b0);
+        v[1] = cadd<T>(a1, b1);
+        v[3] = csub<T>(a1, b1);
+    }
+};
+
+// y[u] = E[u mod H] + w^u O[u mod H], w = exp(DIR 2 pi i / R), for R = 8, 16
+template <int R, int DIR, typename T> struct DftSplit {
+    __device__ static __forceinline__ void run(cx<T>* v) {
+        constexpr int H = R / 2;
+        cx<T> e[H], o[H];
+#pragma unroll
+        for (int q = 0; q < H; ++q) { e[q] = v[2 * q]; o[q] = v[2 * q + 1]; }
+        Dft<H, DIR, T>::run(e);
+        Dft<H, DIR, T>::run(o);
+#pragma unroll
+        for (int u = 0; u < H; ++u) {
+            // w^u = cos(2 pi u / R) + i DIR sin(2 pi u / R); table of 16ths
+            constexpr int step = 16 / R;
+            const T c = Tab16<T>::c(u * step);
+            const T s = DIR * Tab16<T>::s(u * step);
+            cx<T> t = cmul<T>(o[u], mkc<T>(c, s));
+            v[u] = cadd<T>(e[u], t);
+            v[u + H] = csub<T>(e[u], t);
+        }
+    }
+};
+template <int DIR, typename T> struct Dft<8, DIR, T> : DftSplit<8, DIR, T> {};
+template <int DIR, typename T> struct Dft<16, DIR, T> : DftSplit<16, DIR, T> {};
+
+// odd R: pair x[q] with x[R-q] (halves the multiplications)
+template <int R, int DIR, typename T> struct DftOdd {
+    __device__ static __forceinline__ void run(cx<T>* v) {
+        constexpr int H = (R - 1) / 2;
+        cx<T> a[H], b[H];
+        cx<T> y0 = v[0];
+#pragma unroll
+        for (int q = 1; q <= H; ++q) {
+            a[q - 1] = cadd<T>(v[q], v[R - q]);
+            b[q - 1] = csub<T>(v[q], v[R - q]);
+            y0 = cadd<T>(y0, a[q - 1]);
+        }
+        const cx<T> x0 = v[0];
+        v[0] = y0;
+#pragma unroll
+        for (int u = 1; u <= H; ++u) {
+            cx<T> A = x0, B = mkc<T>(0, 0);
+#pragma unroll
+            for (int q = 1; q <= H; ++q) {
+                const int k = (q * u) % R;
+                const T c = OddTab<R, T>::c(k), s = OddTab<R, T>::s(k);
+                A.x += a[q - 1].x * c; A.y += a[q - 1].y * c;
+                B.x += b[q - 1].x * s; B.y += b[q - 1].y * s;
+            }
+            // y[u] = A + i DIR B ; y[R-u] = A - i DIR B
+            cx<T> iB = mul_is<DIR, T>(B);
+            v[u] = cadd<T>(A, iB);
+            v[R - u] = csub<T>(A, iB);
+        }
+    }
+};
+template <int DIR, typename T> struct Dft<3, DIR, T> : DftOdd<3, DIR, T> {};
+template <int DIR, typename T> struct Dft<5, DIR, T> : DftOdd<5, DIR, T> {};
+template <int DIR, typename T> struct Dft<7, DIR, T> : DftOdd<7, DIR, T> {};
+template <int DIR, typename T> struct Dft<9, DIR, T> : DftOdd<9, DIR, T> {};
+template <int DIR, typename T> struct Dft<11, DIR, T> : DftOdd<11, DIR, T> {};
+template <int DIR, typename T> struct Dft<13, DIR, T> : DftOdd<13, DIR, T> {};
+
+// ------------------------------ plans ------------------------------
+
+template <int N> struct Plan;
+template <> struct Plan<16> { static constexpr int R1 = 4, R2 = 4; };
+template <> struct Plan<32> { static constexpr int R1 = 8, R2 = 4; };
+template <> struct Plan<64> { static constexpr int R1 = 8, R2 = 8; };
+template <> struct Plan<88> { static constexpr int R1 = 8, R2 = 11; };
+template <> struct Plan<128> { static constexpr int R1 = 16, R2 = 8; };
+
+template <int N> struct Tile { static constexpr int LDS = N + 1; static constexpr int ELEMS = N * (N + 1); };
+
+// One Stockham stage over LINES lines starting at line0.  Element e of line l is at
+// s[l * lstride + e * estride].
+template <typename T, int N, int R, int NS, int DIR, int LINES, int THREADS>
+__device__ __forceinline__ void fft_stage(cx<T>* s, int line0, int lstride, int estride, const cx<T>* tw) {
+    constexpr int BF = N / R;
+    constexpr int TOTAL = LINES * BF;
+    constexpr int ITER = (TOTAL + THREADS - 1) / THREADS;
+    constexpr int TWS = N / (NS * R);
+    cx<T> v[ITER][R];
+#pragma unroll
+    for (int it = 0; it < ITER; ++it) {
+        const int b = threadIdx.x + it * THREADS;
+        if (TOTAL % THREADS == 0 || b < TOTAL) {
+            const int line = line0 + b % LINES;
+            const int j = b / LINES;
+            const cx<T>* base = s + line * lstride;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[it][r] = base[(j + r * BF) * estride];
+            if (NS > 1) {
+                const int k = j % NS;
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    cx<T> w = tw[r * k * TWS];
+                    if (DIR > 0) w.y = -w.y;
+                    v[it][r] = cmul<T>(v[it][r], w);
+                }
+            }
+            Dft<R, DIR, T>::run(v[it]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < ITER; ++it) {
+        const int b = threadIdx.x + it * THREADS;
+        if (TOTAL % THREADS == 0 || b < TOTAL) {
+            const int line = line0 + b % LINES;
+            const int j = b / LINES;
+            const int k = j % NS;
+            const int idxD = (j / NS) * NS * R + k;
+            cx<T>* base = s + line * lstride;
+#pragma unroll
+            for (int r = 0; r < R; ++r) base[(idxD + r * NS) * estride] = v[it][r];
+        }
+    }
+    __syncthreads();
+}
+
+// 1-D transforms of LINES lines (rows when ROWS, else columns).
+template <typename T, int N, int DIR, int LINES, bool ROWS, int THREADS>
+__device__ __forceinline__ void fft_lines(cx<T>* s, int line0, const cx<T>* tw) {
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
+    constexpr int ls = ROWS ? LDS : 1;
+    constexpr int es = ROWS ? 1 : LDS;
+    fft_stage<T, N, R1, 1, DIR, LINES, THREADS>(s, line0, ls, es, tw);
+    fft_stage<T, N, R2, R1, DIR, LINES, THREADS>(s, line0, ls, es, tw);
+}
+
+// Full 2-D transform.  IN_ROWS_PRUNED: only rows [N/4, 3N/4) of the input are non-zero
+// (an n x n pupil embedded at offset n/2), so only those rows are transformed first.
+template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED>
+__device__ __forceinline__ void fft2d(cx<T>* s, const cx<T>* tw) {
+    if (IN_ROWS_PRUNED) {
+        fft_lines<T, N, DIR, N / 2, true, THREADS>(s, N / 4, tw);
+    } else {
+        fft_lines<T, N, DIR, N, true, THREADS>(s, 0, tw);
+    }
+    fft_lines<T, N, DIR, N, false, THREADS>(s, 0, tw);
+}
+
+// 2-D transform whose output is only needed on rows [N/4, 3N/4): columns first, then the
+// needed rows.
+template <typename T, int N, int DIR, int THREADS>
+__device__ __forceinline__ void fft2d_out_rows_pruned(cx<T>* s, const cx<T>* tw) {
+    fft_lines<T, N, DIR, N, false, THREADS>(s, 0, tw);
+    fft_lines<T, N, DIR, N / 2, true, THREADS>(s, N / 4, tw);
+}
+
+}  // namespace rdxg

@@ -1,0 +1,7 @@
+// Kernel instantiations for an OTF size of 64.
+#include "rdxg_inst.cuh"
+
+namespace rdxg {
+template struct Launcher<float, 64>;
+template struct Launcher<double, 64>;
+}  // namespace rdxg

@@ -1,0 +1,7 @@
+// Kernel instantiations for an OTF size of 88.
+#include "rdxg_inst.cuh"
+
+namespace rdxg {
+template struct Launcher<float, 88>;
+template struct Launcher<double, 88>;
+}  // namespace rdxg

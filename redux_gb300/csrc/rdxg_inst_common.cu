@@ -1,0 +1,26 @@
+// Size-independent kernels: per-object accumulation, the solver state machine, re-shifts.
+#include "rdxg_launch.h"
+
+namespace rdxg {
+
+template <typename T>
+void launch_accum(const KParams<T>& kp, int nPo, cudaStream_t st) {
+    dim3 grid(kp.nTiles, nPo);
+    k_accum<T, kAccumThreads><<<grid, kAccumThreads, 0, st>>>(kp);
+}
+
+template <typename T>
+void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st) {
+    k_cg<T, kCgThreads><<<P, kCgThreads, 0, st>>>(a);
+}
+
+void launch_shift(const ShiftArgs& a, int P, cudaStream_t st) {
+    k_shift<0><<<P, 128, 0, st>>>(a);
+}
+
+template void launch_accum<float>(const KParams<float>&, int, cudaStream_t);
+template void launch_accum<double>(const KParams<double>&, int, cudaStream_t);
+template void launch_cg<float>(const CgArgs<float>&, int, cudaStream_t);
+template void launch_cg<double>(const CgArgs<double>&, int, cudaStream_t);
+
+}  // namespace rdxg

@@ -1,0 +1,476 @@
+// Per-image and per-object kernels of the batched MOMFBD solver.
+//
+// Data layout in device memory (g = patch * I + image, po = patch * nObj + object):
+//   D  [g][N*N]  complex  centred transform of the windowed image (SubImage::imgFT)
+//   S  [g][N*N]  complex  centred OTF (SubImage::OTF)
+//   X  [g][N*N]  complex  un-centred transform of c * pupil function (kept for gradients)
+//   PF [g][n*n]  complex  pupil function A exp(i phi) (SubImage::PF)
+//   O  [po][N*N] complex  object estimate conj(P)/Q (centred)
+//   Qt [po][N*N] real     Q = gamma + sum |S|^2
+// Every per-image kernel runs one thread block per image over an N x N shared-memory
+// tile; patches whose request does not need the kernel return at once.
+#pragma once
+
+#include "cg_machine.h"
+#include "rdxg_fft.cuh"
+
+namespace rdxg {
+
+template <typename T>
+struct KParams {
+    int32_t P, I, M, nObj, N, n, ps, cs, margin, nTiles;
+    // static
+    const T* Z;          // [M][n*n]
+    const T* A;          // [n*n] amplitude, zero outside the pupil support
+    const T* phiFixed;   // [C][n*n]
+    const T* otfNorm;    // [C]
+    const uint8_t* otfMask;   // [N*N] centred OTF support
+    const int32_t* imgObj;    // [I]
+    const int32_t* imgCh;     // [I]
+    const int32_t* objFirst;  // [nObj]
+    const int32_t* objCount;  // [nObj]
+    const double* objWeight;  // [nObj]
+    const double* objGradStep;// [nObj]
+    const double* window;     // [ps*ps]
+    const double* noiseWindow;// [ps*ps]
+    const cx<T>* tw;          // [N] exp(-2 pi i k/N)
+    double area;
+    int32_t tiltX, tiltY;
+    // per patch
+    const float* cutouts;     // [g][cs*cs]
+    int32_t* shift;           // [g][2] (y, x)
+    double* statMean;         // [g]
+    double* statStd;          // [g]
+    double* statNoise;        // [g]
+    double* rg;               // [g] noise / stddev
+    const T* alphaEff;        // [g][M]
+    cx<T>* D;
+    cx<T>* S;
+    cx<T>* X;
+    cx<T>* PF;
+    cx<T>* O;
+    T* Qt;
+    const double* gamma;      // [po]
+    double* partial;          // [po][nTiles]
+    double* galpha;           // [g][M]
+    const int32_t* req;       // [P]
+    const int32_t* gmethod;   // [P]
+    const int32_t* modeCount; // [P]
+    const uint8_t* reinit;    // [g] image must be re-initialised (re-shift)
+};
+
+enum GradKind : int32_t { GK_VOGEL = 0, GK_EXACT = 1 };
+
+template <typename T> __device__ __forceinline__ void sincos_t(T x, T* s, T* c);
+template <> __device__ __forceinline__ void sincos_t<float>(float x, float* s, float* c) { sincosf(x, s, c); }
+template <> __device__ __forceinline__ void sincos_t<double>(double x, double* s, double* c) { sincos(x, s, c); }
+
+// deterministic block reduction of a double (fixed tree); result valid in all threads
+template <int THREADS>
+__device__ __forceinline__ double block_sum(double v, double* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double t = (lane < THREADS / 32) ? red[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) red[32] = t;
+    }
+    __syncthreads();
+    double r = red[32];
+    __syncthreads();
+    return r;
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void load_twiddles(cx<T>* tw, const cx<T>* src) {
+    for (int k = threadIdx.x; k < N; k += blockDim.x) tw[k] = src[k];
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void zero_tile(cx<T>* s) {
+    for (int i = threadIdx.x; i < Tile<N>::ELEMS; i += blockDim.x) s[i] = mkc<T>(0, 0);
+}
+
+// ----------------------------------------------------------------------------------
+// Image preparation: SubImage::initialize (subimage.cpp:155-209) with getWindowedImg
+// (106-150) and the noise estimate FourierTransform::noise(-1,-1) (fouriertransform.cpp:
+// 448-495).  mode 1: full initialisation (noise and rg); mode 0: re-initialise only the
+// images flagged in reinit (after a re-shift).
+// ----------------------------------------------------------------------------------
+template <typename T, int N, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_prep(KParams<T> kp, int full) {
+    const int g = blockIdx.x;
+    if (!full && !kp.reinit[g]) return;
+    constexpr int LDS = Tile<N>::LDS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* tw = s + Tile<N>::ELEMS;
+    double* red = reinterpret_cast<double*>(tw + N);
+    load_twiddles<T, N>(tw, kp.tw);
+    const int ps = kp.ps, cs = kp.cs;
+    const int oy = kp.margin + kp.shift[2 * g + 0];
+    const int ox = kp.margin + kp.shift[2 * g + 1];
+    const float* cut = kp.cutouts + (size_t)g * cs * cs;
+    // raw mean
+    double sum = 0;
+    for (int i = threadIdx.x; i < ps * ps; i += THREADS) {
+        const int y = i / ps, x = i % ps;
+        sum += (double)cut[(oy + y) * cs + ox + x];
+    }
+    const double avg = block_sum<THREADS>(sum, red) / (double)(ps * ps);
+    // windowed image statistics
+    double s1 = 0, s2 = 0;
+    for (int i = threadIdx.x; i < ps * ps; i += THREADS) {
+        const int y = i / ps, x = i % ps;
+        const double w = ((double)cut[(oy + y) * cs + ox + x] - avg) * kp.window[i] + avg;
+        s1 += w;
+        s2 += w * w;
+    }
+    const double t1 = block_sum<THREADS>(s1, red);
+    const double t2 = block_sum<THREADS>(s2, red);
+    const double mean = t1 / (double)(ps * ps);
+    const double stddev = sqrt(t2 / (double)(ps * ps) - mean * mean);
+    if (full) {
+        // noise estimate from (windowed - mean) * noiseWindow, un-centred transform
+        for (int i = threadIdx.x; i < N * N; i += THREADS) {
+            const int y = i / N, x = i % N;
+            const double w = ((double)cut[(oy + y) * cs + ox + x] - avg) * kp.window[i] + avg;
+            s[y * LDS + x] = mkc<T>((T)((w - mean) * kp.noiseWindow[i]), 0);
+        }
+        __syncthreads();
+        fft2d<T, N, -1, THREADS, false>(s, tw);
+        const int mask = N / 6 + 1;
+        const double limits = (double)N * N / 4.0;
+        double np = 0, cnt = 0;
+        for (int i = threadIdx.x; i < N * N; i += THREADS) {
+            const int y = i / N, x = i % N;
+            if (x < mask || x >= N - mask + 1 || y < mask || y >= N - mask + 1) continue;
+            const double xx = (double)(x < N - x ? x : N - x);
+            const double yy = (double)(y < N - y ? y : N - y);
+            if (xx * xx + yy * yy < limits) continue;
+            const cx<T> v = s[y * LDS + x];
+            np += (double)v.x * v.x + (double)v.y * v.y;
+            cnt += 1.0;
+        }
+        const double tp = block_sum<THREADS>(np, red);
+        const double tc = block_sum<THREADS>(cnt, red);
+        const double noise = tc > 0 ? sqrt(tp / (tc * N * N)) : 0.0;
+        if (threadIdx.x == 0) {
+            kp.statNoise[g] = noise;
+            kp.rg[g] = noise / stddev;
+        }
+    }
+    if (threadIdx.x == 0) {
+        kp.statMean[g] = mean;
+        kp.statStd[g] = stddev;
+    }
+    // D = FT(windowed) = FT(windowed - mean) + N^2 mean delta: the mean is taken out before
+    // the transform so that the large DC term does not swamp the other frequencies.
+    for (int i = threadIdx.x; i < N * N; i += THREADS) {
+        const int y = i / N, x = i % N;
+        const double w = ((double)cut[(oy + y) * cs + ox + x] - avg) * kp.window[i] + avg;
+        s[y * LDS + x] = mkc<T>((T)(w - mean), 0);
+    }
+    __syncthreads();
+    fft2d<T, N, -1, THREADS, false>(s, tw);
+    cx<T>* D = kp.D + (size_t)g * N * N;
+    for (int i = threadIdx.x; i < N * N; i += THREADS) {
+        const int cy = i / N, cxx = i % N;          // centred index (REORDER_FT)
+        const int y = (cy + N / 2) % N, x = (cxx + N / 2) % N;
+        cx<T> v = s[y * LDS + x];
+        if (y == 0 && x == 0) v = mkc<T>((T)(mean * (double)N * (double)N), 0);
+        D[i] = v;
+    }
+}
+
+// ----------------------------------------------------------------------------------
+// Forward model: SubImage::calcPhi + calcPFOTF (subimage.cpp:509-544, 586-612).
+// phi = phi_fixed + sum_m alpha_eff[m] Z_m; PF = A exp(i phi);
+// OTF = fftshift(ifft(|fft(c PF embedded at n/2)|^2) / N^2).
+// ----------------------------------------------------------------------------------
+template <typename T, int N, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_forward(KParams<T> kp) {
+    const int g = blockIdx.x;
+    const int p = g / kp.I, j = g % kp.I;
+    const int rq = kp.req[p];
+    if (rq != REQ_F && rq != REQ_DF) return;
+    const bool df = (rq == REQ_DF);
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int n = N / 2, n2 = n * n;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* tw = s + Tile<N>::ELEMS;
+    T* al = reinterpret_cast<T*>(tw + N);
+    load_twiddles<T, N>(tw, kp.tw);
+    const int M = kp.M;
+    for (int m = threadIdx.x; m < M; m += THREADS) al[m] = kp.alphaEff[(size_t)g * M + m];
+    zero_tile<T, N>(s);
+    __syncthreads();
+    const int ch = kp.imgCh[j];
+    const T c = kp.otfNorm[ch];
+    const T* phf = kp.phiFixed + (size_t)ch * n2;
+    for (int q = threadIdx.x; q < n2; q += THREADS) {
+        const T a = kp.A[q];
+        cx<T> pf = mkc<T>(0, 0);
+        if (a > (T)0) {
+            T phi = phf[q];
+            for (int m = 0; m < M; ++m) phi += al[m] * kp.Z[(size_t)m * n2 + q];
+            T sn, cs;
+            sincos_t<T>(phi, &sn, &cs);
+            pf = mkc<T>(a * cs, a * sn);
+        }
+        if (df) kp.PF[(size_t)g * n2 + q] = pf;
+        const int y = q / n, x = q % n;
+        s[(y + n / 2) * LDS + x + n / 2] = cscale<T>(pf, c);
+    }
+    __syncthreads();
+    fft2d<T, N, -1, THREADS, true>(s, tw);
+    cx<T>* X = kp.X + (size_t)g * N * N;
+    for (int i = threadIdx.x; i < N * N; i += THREADS) {
+        const int y = i / N, x = i % N;
+        const cx<T> v = s[y * LDS + x];
+        if (df) X[i] = v;
+        s[y * LDS + x] = mkc<T>(cnorm<T>(v), 0);
+    }
+    __syncthreads();
+    fft2d<T, N, +1, THREADS, false>(s, tw);
+    const T inv = (T)1 / (T)(N * N);
+    cx<T>* S = kp.S + (size_t)g * N * N;
+    for (int i = threadIdx.x; i < N * N; i += THREADS) {
+        const int cy = i / N, cxx = i % N;
+        const int y = (cy + N / 2) % N, x = (cxx + N / 2) % N;
+        S[i] = cscale<T>(s[y * LDS + x], inv);
+    }
+}
+
+// ----------------------------------------------------------------------------------
+// Per-object accumulation and metric: Object::initPQ/addToPQ/calcMetric
+// (object.cpp:459-518, 597-615).  The reference's per-frequency term
+//     sum_j |D_j|^2 - |P|^2 / Q,   P = sum_j conj(D_j) S_j,  Q = gamma + sum_j |S_j|^2
+// is a small difference of large numbers.  With O = conj(P) / Q it equals exactly
+//     sum_j |D_j - O S_j|^2 + gamma |O|^2,
+// a sum of non-negative terms, which is what is evaluated here (two passes over the
+// object's images per frequency; the second pass hits L2).  Per-block partial sums are in
+// double and are added in a fixed order by the solver kernel.
+// ----------------------------------------------------------------------------------
+template <typename T, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_accum(KParams<T> kp) {
+    const int po = blockIdx.y;
+    const int p = po / kp.nObj, o = po % kp.nObj;
+    const int rq = kp.req[p];
+    if (rq != REQ_F && rq != REQ_DF) return;
+    __shared__ double red[33];
+    const int N2 = kp.N * kp.N;
+    const int u = blockIdx.x * THREADS + threadIdx.x;
+    double term = 0;
+    const bool df = (rq == REQ_DF);
+    if (u < N2) {
+        const size_t fbase = (size_t)p * kp.I + kp.objFirst[o];
+        const int cnt = kp.objCount[o];
+        const T gam = (T)kp.gamma[po];
+        cx<T> O = mkc<T>(0, 0);
+        T Qt = (T)1;
+        if (kp.otfMask[u]) {
+            cx<T> Pa = mkc<T>(0, 0);
+            T Qa = (T)0;
+            for (int k = 0; k < cnt; ++k) {
+                const cx<T> d = kp.D[(fbase + k) * N2 + u];
+                const cx<T> sv = kp.S[(fbase + k) * N2 + u];
+                Pa = cadd<T>(Pa, cmulc<T>(sv, d));          // conj(D) S
+                Qa += cnorm<T>(sv);
+            }
+            Qt = gam + Qa;
+            O = mkc<T>(Pa.x / Qt, -Pa.y / Qt);             // conj(P) / Q
+            T R = (T)0;
+            for (int k = 0; k < cnt; ++k) {
+                const cx<T> d = kp.D[(fbase + k) * N2 + u];
+                const cx<T> sv = kp.S[(fbase + k) * N2 + u];
+                const cx<T> r = csub<T>(d, cmul<T>(O, sv));
+                R += cnorm<T>(r);
+            }
+            term = (double)R + (double)gam * (double)cnorm<T>(O);
+        }
+        if (df) {
+            kp.O[(size_t)po * N2 + u] = O;
+            kp.Qt[(size_t)po * N2 + u] = Qt;
+        }
+    }
+    const double tot = block_sum<THREADS>(term, red);
+    if (threadIdx.x == 0) kp.partial[(size_t)po * kp.nTiles + blockIdx.x] = tot;
+}
+
+// ----------------------------------------------------------------------------------
+// Adjoint gradient: SubImage::calcVogelWeight + gradientVogel (subimage.cpp:312-390).
+// With G = conj(O) (D - O S) = (PQ D - PS S) / QS on the OTF support, the reference forms
+// U = fftshift(fft(ifft(corner-embedded PF)/N^2 * Re(ifft(ifftshift G)/N^2))) which is the
+// convolution (G * PF)/N^2 on the pupil; here it is evaluated as
+//     ifft( fft(ifftshift G) * fft(PF embedded at n/2) )
+// where the second factor is the forward transform X kept from the forward pass (two
+// transforms instead of three).  The DC term of G is left out: G(0) is real and its exact
+// contribution Im(conj(PF) G(0) PF) is zero, while its size would swamp the FP32 result.
+// kind GK_VOGEL: the reference's weights (pupil amplitude per pixel, -2 area/N^2, object
+// weight twice); GK_EXACT: dL/dalpha of the metric.
+// ----------------------------------------------------------------------------------
+template <typename T, int N, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
+    const int g = blockIdx.x;
+    const int p = g / kp.I, j = g % kp.I;
+    if (kp.req[p] != REQ_DF || kp.gmethod[p] != GM_VOGEL) return;
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int n = N / 2, n2 = n * n, N2 = N * N;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* tw = s + Tile<N>::ELEMS;
+    T* v = reinterpret_cast<T*>(tw + N);            // [n2]
+    load_twiddles<T, N>(tw, kp.tw);
+    const int o = kp.imgObj[j];
+    const size_t po = (size_t)p * kp.nObj + o;
+    const cx<T>* Oo = kp.O + po * N2;
+    const cx<T>* Dg = kp.D + (size_t)g * N2;
+    const cx<T>* Sg = kp.S + (size_t)g * N2;
+    for (int i = threadIdx.x; i < N2; i += THREADS) {
+        const int y = i / N, x = i % N;                 // un-centred (lag) position
+        const int c = ((y + N / 2) % N) * N + (x + N / 2) % N;
+        cx<T> G = mkc<T>(0, 0);
+        if (kp.otfMask[c] && !(y == 0 && x == 0)) {
+            const cx<T> O = Oo[c];
+            const cx<T> r = csub<T>(Dg[c], cmul<T>(O, Sg[c]));
+            G = cmulc<T>(r, O);                           // conj(O) r
+        }
+        s[y * LDS + x] = G;
+    }
+    __syncthreads();
+    fft2d<T, N, -1, THREADS, false>(s, tw);
+    const cx<T>* X = kp.X + (size_t)g * N2;
+    for (int i = threadIdx.x; i < N2; i += THREADS) {
+        const int y = i / N, x = i % N;
+        s[y * LDS + x] = cmul<T>(s[y * LDS + x], X[i]);
+    }
+    __syncthreads();
+    fft2d_out_rows_pruned<T, N, +1, THREADS>(s, tw);
+    const cx<T>* PF = kp.PF + (size_t)g * n2;
+    for (int q = threadIdx.x; q < n2; q += THREADS) {
+        const int y = q / n, x = q % n;
+        const cx<T> U = s[(y + n / 2) * LDS + x + n / 2];
+        const cx<T> pf = PF[q];
+        // Im(conj(pf) U)
+        const T a = kp.A[q];
+        const T wq = (kind == GK_VOGEL) ? a : (a > (T)0 ? (T)1 : (T)0);
+        v[q] = (pf.x * U.y - pf.y * U.x) * wq;
+    }
+    __syncthreads();
+    // projection on the modes: one warp per mode
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int mc = kp.modeCount[p];
+    const int ch = kp.imgCh[j];
+    const double c = (double)kp.otfNorm[ch];
+    const double w = kp.objWeight[o];
+    double scale;
+    if (kind == GK_VOGEL) {
+        // X carries the factor c: result = c N^2 (G (*) PF); reference: -2 area w^2 / N^6 * sum
+        scale = -2.0 * kp.area * w * w / ((double)N2 * (double)N2 * (double)N2) / c;
+    } else {
+        scale = -4.0 * c * c * w / ((double)kp.ps * kp.ps * (double)N2) / c;
+    }
+    for (int m = wid; m < kp.M; m += THREADS / 32) {
+        double acc = 0;
+        if (m < mc) {
+            const T* Zm = kp.Z + (size_t)m * n2;
+            T part = 0;
+            for (int q = lane; q < n2; q += 32) part += v[q] * Zm[q];
+            acc = (double)part;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+        }
+        if (lane == 0) kp.galpha[(size_t)g * kp.M + m] = (m < mc) ? acc * scale : 0.0;
+    }
+}
+
+// ----------------------------------------------------------------------------------
+// Finite-difference gradient: SubImage::gradientFiniteDifference + metricChange
+// (subimage.cpp:261-292), used by the reference for the first gradient of a patch.
+// The OTF change dS = S(phi + h Z_m) - S(phi) is formed directly as
+//     ifft(2 Re(conj(X) dX) + |dX|^2) / N^2,  dX = fft(c PF (exp(i h Z_m) - 1))
+// instead of as a difference of two transforms, and metricChange is rearranged with
+// G = conj(O)(D - O S) so that no large terms cancel:
+//     dl = -sum [2 Q Re(dS conj G) + |dS|^2 (|D|^2 - Q |O|^2)] / (Q + dq) / N^2.
+// One block per (image, mode).
+// ----------------------------------------------------------------------------------
+template <typename T, int N, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_fd(KParams<T> kp) {
+    const int g = blockIdx.x;
+    const int m = blockIdx.y;
+    const int p = g / kp.I, j = g % kp.I;
+    if (kp.req[p] != REQ_DF || kp.gmethod[p] != GM_FD) return;
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int n = N / 2, n2 = n * n, N2 = N * N;
+    const int o = kp.imgObj[j];
+    if (m >= kp.modeCount[p] || kp.objWeight[o] == 0.0) {
+        if (threadIdx.x == 0) kp.galpha[(size_t)g * kp.M + m] = 0.0;
+        return;
+    }
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* tw = s + Tile<N>::ELEMS;
+    double* red = reinterpret_cast<double*>(tw + N);
+    load_twiddles<T, N>(tw, kp.tw);
+    zero_tile<T, N>(s);
+    __syncthreads();
+    const int ch = kp.imgCh[j];
+    const T c = kp.otfNorm[ch];
+    const double h = kp.objGradStep[o];
+    const cx<T>* PF = kp.PF + (size_t)g * n2;
+    const T* Zm = kp.Z + (size_t)m * n2;
+    for (int q = threadIdx.x; q < n2; q += THREADS) {
+        if (kp.A[q] > (T)0) {
+            const T t = (T)h * Zm[q];
+            T sh, ch2, sn, cs;
+            sincos_t<T>(t * (T)0.5, &sh, &ch2);
+            sincos_t<T>(t, &sn, &cs);
+            const cx<T> e = mkc<T>((T)-2 * sh * sh, sn);   // exp(i t) - 1
+            const int y = q / n, x = q % n;
+            s[(y + n / 2) * LDS + x + n / 2] = cscale<T>(cmul<T>(PF[q], e), c);
+        }
+    }
+    __syncthreads();
+    fft2d<T, N, -1, THREADS, true>(s, tw);
+    const cx<T>* X = kp.X + (size_t)g * N2;
+    for (int i = threadIdx.x; i < N2; i += THREADS) {
+        const int y = i / N, x = i % N;
+        const cx<T> dX = s[y * LDS + x];
+        const cx<T> x0 = X[i];
+        s[y * LDS + x] = mkc<T>((T)2 * (x0.x * dX.x + x0.y * dX.y) + cnorm<T>(dX), 0);
+    }
+    __syncthreads();
+    fft2d<T, N, +1, THREADS, false>(s, tw);
+    const size_t po = (size_t)p * kp.nObj + o;
+    const T inv = (T)1 / (T)N2;
+    double dl = 0;
+    for (int i = threadIdx.x; i < N2; i += THREADS) {
+        if (!kp.otfMask[i]) continue;
+        const int cy = i / N, cxx = i % N;
+        if (cy == N / 2 && cxx == N / 2) continue;       // dS(0) = 0 exactly
+        const int y = (cy + N / 2) % N, x = (cxx + N / 2) % N;
+        const cx<T> dS = cscale<T>(s[y * LDS + x], inv);
+        const cx<T> S = kp.S[(size_t)g * N2 + i];
+        const cx<T> D = kp.D[(size_t)g * N2 + i];
+        const cx<T> O = kp.O[po * N2 + i];
+        const T Q = kp.Qt[po * N2 + i];
+        const cx<T> G = cmulc<T>(csub<T>(D, cmul<T>(O, S)), O);
+        const T dq = (T)2 * (S.x * dS.x + S.y * dS.y) + cnorm<T>(dS);
+        const T num = (T)2 * Q * (dS.x * G.x + dS.y * G.y) + cnorm<T>(dS) * (cnorm<T>(D) - Q * cnorm<T>(O));
+        dl -= (double)num / (double)(Q + dq);
+    }
+    const double tot = block_sum<THREADS>(dl, red);
+    if (threadIdx.x == 0) {
+        const double w = kp.objWeight[o];
+        kp.galpha[(size_t)g * kp.M + m] = w * (tot / (double)N2 / h * w);
+    }
+}
+
+}  // namespace rdxg

@@ -1,0 +1,203 @@
+"""Python mirror of redux's ``momfbd::Solver`` over the GB300 solver core.
+
+The reference interface (include/redux/momfbd/solver.hpp:86-179) is a C++ object built once
+per job (``Solver(MomfbdJob&, io_service&, nThreads)``) whose ``run(PatchData::Ptr)``
+solves one patch.  Here one ``Solver`` holds the job's static data on the GPU and solves a
+batch of patches per ``run``; ``metric``/``gradient`` expose the reference's metric and
+gradient evaluations (``Solver::metric``, ``Solver::gradient``) for whole batches.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+
+
+class SolverError(RuntimeError):
+    pass
+
+
+@dataclass
+class SolveSettings:
+    """GlobalCfg fields read by Solver::run (defaults of config.cpp:629-636)."""
+    mode_start: int = 5
+    mode_step: int = 5
+    max_iterations: int = 500
+    min_iterations: int = 5
+    target_iterations: int = 3
+    fd_first: bool = True
+    ftol: float = 1e-3
+    eps: float = 1e-10
+    max_metrics: int = 1024
+    check_every: int = 8
+
+    def to_c(self) -> _lib.SolveParams:
+        return _lib.SolveParams(mode_start=self.mode_start, mode_step=self.mode_step,
+                                max_iterations=self.max_iterations, min_iterations=self.min_iterations,
+                                target_iterations=self.target_iterations, fd_first=int(self.fd_first),
+                                max_metrics=self.max_metrics, check_every=self.check_every,
+                                ftol=self.ftol, eps=self.eps)
+
+
+def fixed_iterations(n_modes: int, iterations: int, **kw) -> SolveSettings:
+    """All modes at once, exactly `iterations` CG iterations (FTOL = 0)."""
+    return SolveSettings(mode_start=n_modes, mode_step=n_modes, max_iterations=iterations,
+                         min_iterations=iterations, ftol=0.0, **kw)
+
+
+class Solver:
+    """Batched per-patch MOMFBD solver for one job on one GPU."""
+
+    def __init__(self, job, max_patches: int, precision: str = "fp32", device: int = 0):
+        L = _lib.load()
+        self.job = job
+        self._keep = []
+
+        def c(a, dt):
+            a = np.ascontiguousarray(a, dt)
+            self._keep.append(a)
+            return _lib.ptr(a)
+
+        sup = job.support
+        ns = job.nullspace
+        self.geo = _lib.Geometry(
+            otf_size=job.otf_size, pupil_pixels=job.pupil_pixels, patch_size=job.patch_size,
+            n_modes=job.n_modes, n_objects=job.n_objects, n_images=job.n_images, n_channels=job.n_channels,
+            tilt_x=job.tilt_x, tilt_y=job.tilt_y, n_free=ns.n_free, cutout_size=job.cutout_size,
+            max_patches=max_patches, precision=_lib.RDXG_FP64 if precision == "fp64" else _lib.RDXG_FP32,
+            device=device)
+        st = _lib.Static(
+            modes=c(job.modes, np.float64), pupil=c(job.pupil, np.float64),
+            n_pupil_support=int(sup.pupil_support.size), pupil_support=c(sup.pupil_support, np.int32),
+            n_otf_support=int(sup.otf_support.size), otf_support=c(sup.otf_support, np.int32),
+            image_object=c(job.img_object, np.int32), image_channel=c(job.img_channel, np.int32),
+            phi_fixed=c(job.phi_fixed, np.float64), object_weight=c(job.obj_weight, np.float64),
+            object_grad_step=c(job.obj_grad_step, np.float64), window=c(job.window, np.float64),
+            noise_window=c(job.noise_window, np.float64), ns_nnz=int(ns.vals.size),
+            ns_rows=c(ns.rows, np.int32), ns_cols=c(ns.cols, np.int32), ns_vals=c(ns.vals, np.float64),
+            tilt_jacobian=c(np.asarray(job.J_T_xy).ravel(), np.float64))
+        h = C.c_void_p()
+        r = L.rdxg_create(C.byref(self.geo), C.byref(st), C.byref(h))
+        self.h = h
+        self._check(r, "rdxg_create")
+        self.precision = precision
+        self.max_patches = max_patches
+        self.P = 0
+        self.I, self.M = job.n_images, job.n_modes
+
+    def _check(self, r, what):
+        if r != _lib.RDXG_OK:
+            msg = _lib.load().rdxg_last_error(self.h).decode() if self.h else ""
+            raise SolverError(f"{what} failed with status {r}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.load().rdxg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, cuda_stream_ptr: int | None):
+        self._check(_lib.load().rdxg_set_stream(self.h, C.c_void_p(cuda_stream_ptr or 0)), "rdxg_set_stream")
+
+    def set_patches(self, cutouts, residual_alpha=None, fixed_gamma=None):
+        """cutouts: (P, I, cs, cs) float32 host array or an int device pointer with n_patches."""
+        cut = np.ascontiguousarray(cutouts, np.float32)
+        P = cut.shape[0]
+        ra = None if residual_alpha is None else np.ascontiguousarray(residual_alpha, np.float64)
+        fg = None if fixed_gamma is None else np.ascontiguousarray(fixed_gamma, np.float64)
+        self._check(_lib.load().rdxg_set_patches(self.h, P, _lib.ptr(cut), _lib.ptr(ra), _lib.ptr(fg)),
+                    "rdxg_set_patches")
+        self.P = P
+
+    def set_patches_device(self, n_patches: int, dev_ptr: int, residual_alpha=None, fixed_gamma=None):
+        ra = None if residual_alpha is None else np.ascontiguousarray(residual_alpha, np.float64)
+        fg = None if fixed_gamma is None else np.ascontiguousarray(fixed_gamma, np.float64)
+        self._check(_lib.load().rdxg_set_patches_device(self.h, n_patches, C.c_void_p(dev_ptr), _lib.ptr(ra),
+                                                        _lib.ptr(fg)), "rdxg_set_patches_device")
+        self.P = n_patches
+
+    def metric(self, alpha) -> np.ndarray:
+        a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
+        out = np.zeros(self.P)
+        self._check(_lib.load().rdxg_metric(self.h, _lib.ptr(a), _lib.ptr(out)), "rdxg_metric")
+        return out
+
+    def gradient(self, alpha, method: str = "vogel", enabled=None):
+        a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
+        g = np.zeros((self.P, self.I, self.M))
+        m = np.zeros(self.P)
+        en = None if enabled is None else np.ascontiguousarray(enabled, np.uint8)
+        code = {"vogel": _lib.RDXG_GRAD_VOGEL, "exact": _lib.RDXG_GRAD_EXACT, "fd": _lib.RDXG_GRAD_FD}[method]
+        self._check(_lib.load().rdxg_gradient(self.h, _lib.ptr(a), _lib.ptr(en), code, _lib.ptr(g), _lib.ptr(m)),
+                    "rdxg_gradient")
+        return g, m
+
+    def run(self, settings: SolveSettings):
+        """Solver::run for every loaded patch."""
+        prm = settings.to_c()
+        alpha = np.zeros((self.P, self.I, self.M))
+        reps = (_lib.PatchReport * self.P)()
+        mets = np.zeros((self.P, max(1, settings.max_metrics)))
+        self._check(_lib.load().rdxg_solve(self.h, C.byref(prm), _lib.ptr(alpha), reps, _lib.ptr(mets)), "rdxg_solve")
+        return dict(alpha=alpha, reports=list(reps), metrics=mets)
+
+    def run_async(self, settings: SolveSettings):
+        self._prm = settings.to_c()
+        self._check(_lib.load().rdxg_solve_async(self.h, C.byref(self._prm)), "rdxg_solve_async")
+
+    def fetch(self, max_metrics: int):
+        alpha = np.zeros((self.P, self.I, self.M))
+        reps = (_lib.PatchReport * self.P)()
+        mets = np.zeros((self.P, max(1, max_metrics)))
+        self._check(_lib.load().rdxg_fetch_results(self.h, _lib.ptr(alpha), reps, _lib.ptr(mets)), "rdxg_fetch_results")
+        return dict(alpha=alpha, reports=list(reps), metrics=mets)
+
+    def launch_count(self) -> int:
+        return int(_lib.load().rdxg_last_launch_count(self.h))
+
+    def debug(self, which: str):
+        P, I, N, nObj = self.P, self.I, self.job.otf_size, self.job.n_objects
+        ct = np.complex128 if self.precision == "fp64" else np.complex64
+        spec = {"D": (0, (P, I, N, N), ct), "otf": (1, (P, I, N, N), ct), "gamma": (2, (P, nObj), np.float64),
+                "stats": (3, (P, I, 3), np.float64), "object": (4, (P, nObj, N, N), ct),
+                "shifts": (5, (P, I, 2), np.int32)}[which]
+        out = np.zeros(spec[1], spec[2])
+        self._check(_lib.load().rdxg_debug_copy(self.h, spec[0], _lib.ptr(out), out.nbytes), "rdxg_debug_copy")
+        return out
+
+
+def cg_minimize(n_free: int, n_modes: int, settings: SolveSettings, grad_scale: float, f, df, shift=None):
+    """Host drop-in of the reference's conjugate_rdx + Solver::run stage loop (rdxg_cg_minimize).
+
+    f(x) -> float; df(x, method, mode_count) -> gradient (n_free); shift(x) -> None."""
+    L = _lib.load()
+
+    def _f(xp, user):
+        return float(f(np.ctypeslib.as_array(xp, shape=(n_free,)).copy()))
+
+    def _df(xp, method, mc, gp, user):
+        g = df(np.ctypeslib.as_array(xp, shape=(n_free,)).copy(), int(method), int(mc))
+        np.ctypeslib.as_array(gp, shape=(n_free,))[:] = g
+
+    def _sh(xp, user):
+        if shift is not None:
+            shift(np.ctypeslib.as_array(xp, shape=(n_free,)).copy())
+
+    cf, cdf, csh = _lib.F_FN(_f), _lib.DF_FN(_df), _lib.SHIFT_FN(_sh)
+    x = np.zeros(n_free)
+    rep = _lib.PatchReport()
+    mets = np.zeros(max(1, settings.max_metrics))
+    prm = settings.to_c()
+    r = L.rdxg_cg_minimize(n_free, n_modes, C.byref(prm), grad_scale, cf, cdf, csh, None, _lib.ptr(x),
+                           C.byref(rep), _lib.ptr(mets))
+    if r != _lib.RDXG_OK:
+        raise SolverError(f"rdxg_cg_minimize failed with status {r}")
+    return dict(x=x, report=rep, metrics=mets[:rep.n_metrics].copy())

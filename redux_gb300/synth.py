@@ -1,0 +1,234 @@
+"""Seeded synthetic MOMFBD workloads.
+
+No SST data is available, so every workload is synthetic: an object field (Gaussian
+random field with a k^-2 power spectrum, mean 1, 10 % RMS contrast), per-frame
+Kolmogorov wavefronts expanded in Zernike modes, images = object (x) PSF with
+Poisson noise at 1e4 photons/px plus N(0, 10^2) read noise, stored as float32.
+
+The generator follows the workload descriptions of the five benchmark configurations
+(plain FP64 single patch; adjoint check; 225-patch production field; uneven batch;
+large mixed-precision batch).  The Karhunen-Loeve basis is not generated yet: those
+configurations use the same number of Zernike modes (Noll 2..M+1), which leaves the
+solver's work per iteration unchanged (a dense modes x pixels matrix either way).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import jobsetup as js
+
+WAVELENGTH = 630.2e-9
+TELESCOPE_D = 0.97
+ARCSEC_PER_PX = WAVELENGTH / (2.0 * TELESCOPE_D) / js.RADIANS_PER_ARCSEC   # critical sampling
+MAX_LOCAL_SHIFT = 5
+
+
+@dataclass
+class Job:
+    """Static (per job) inputs of the per-patch solver."""
+    otf_size: int
+    pupil_pixels: int
+    patch_size: int
+    n_modes: int
+    modes: np.ndarray            # (M, n, n) float64, scaled by 1/lambda
+    mode_list: list
+    tilt_x: int
+    tilt_y: int
+    J_T_xy: np.ndarray
+    pupil: np.ndarray            # (n, n)
+    support: js.PupilSupport
+    img_object: np.ndarray       # (I,) int32
+    img_channel: np.ndarray      # (I,) int32, global channel index
+    img_wavefront: np.ndarray    # (I,) int32
+    phi_fixed: np.ndarray        # (C, n, n) float64, diversity phase per channel
+    obj_weight: np.ndarray       # (nObj,)
+    obj_grad_step: np.ndarray    # (nObj,) GRADDIFF_STEP * wavelength
+    window: np.ndarray           # (ps, ps)
+    noise_window: np.ndarray     # (ps, ps)
+    nullspace: js.NullSpace
+    cutout_size: int
+    channel_div_pv: np.ndarray   # (C,) diversity defocus of each channel, waves PV
+    wavelength: float = WAVELENGTH
+
+    @property
+    def n_images(self):
+        return int(self.img_object.shape[0])
+
+    @property
+    def n_objects(self):
+        return int(self.obj_weight.shape[0])
+
+    @property
+    def n_channels(self):
+        return int(self.phi_fixed.shape[0])
+
+
+@dataclass
+class Patches:
+    cutouts: np.ndarray          # (P, I, cs, cs) float32
+    residual_alpha: np.ndarray   # (P, I, 2) float64 (y, x)
+    fixed_gamma: np.ndarray | None  # (P, nObj) or None (noise-derived)
+    alpha_true: np.ndarray       # (P, I, M) float64 (reference units, lambda * rad)
+
+
+@dataclass
+class Workload:
+    name: str
+    job: Job
+    patches: Patches
+    cfg: dict = field(default_factory=dict)
+
+
+def _grf(rng, size, contrast=0.1):
+    """Gaussian random field with power ~ k^-2, mean 1 and RMS contrast `contrast`."""
+    w = rng.standard_normal((size, size))
+    f = np.fft.fft2(w)
+    ky = np.fft.fftfreq(size)[:, None]
+    kx = np.fft.fftfreq(size)[None, :]
+    k = np.sqrt(kx * kx + ky * ky)
+    amp = np.zeros_like(k)
+    amp[k > 0] = 1.0 / k[k > 0]
+    g = np.real(np.fft.ifft2(f * amp))
+    g -= g.mean()
+    g *= contrast / g.std()
+    return 1.0 + g
+
+
+def _psf_kernel(alpha_rad, mode_list, phi_fixed_rad_fn, K):
+    """PSF on a K x K grid at critical sampling, from the analytic phase on a K/2 pupil."""
+    n = K // 2
+    radius = n / 2.0
+    pupil, _ = js.make_pupil(n, radius)
+    phi = np.zeros((n, n))
+    for a, j in zip(alpha_rad, mode_list):
+        if a != 0.0:
+            phi += a * _zernike_cached(j, n, radius)
+    phi += phi_fixed_rad_fn(n, radius)
+    pf = np.zeros((K, K), complex)
+    o = (K - n) // 2
+    pf[o:o + n, o:o + n] = pupil * np.exp(1j * phi)
+    # the solver's OTF is S = c^2 ifft(|fft(P)|^2), i.e. the PSF is |ifft(P)|^2
+    psf = np.abs(np.fft.ifft2(pf)) ** 2
+    psf /= psf.sum()
+    return psf   # centred at (0, 0) (periodic)
+
+
+_ZCACHE = {}
+
+
+def _zernike_cached(j, n, radius):
+    key = (j, n, radius)
+    z = _ZCACHE.get(key)
+    if z is None:
+        z = js.zernike(j, n, radius)
+        _ZCACHE[key] = z
+    return z
+
+
+def make_job(N: int, n_modes: int, layout, grad_step=1e-2, apodization=-1) -> Job:
+    """layout: list of objects, each a list of channels (diversity PV waves), and the
+    number of frames; e.g. [[0.0, 1.0]] = one object with a focus and a +1 wave channel."""
+    frames = layout["frames"]
+    objects = layout["objects"]
+    fc, radius, npup = js.calculate_pupil_size(N, WAVELENGTH, TELESCOPE_D, ARCSEC_PER_PX)
+    assert npup * 2 == 2 * (N // 2) and 2 * npup == 2 * npup
+    n = npup
+    otf = 2 * n
+    mode_list = list(range(2, 2 + n_modes))
+    jscale = WAVELENGTH * (0.5 * fc) / ((math.pi * math.pi / 648000.0) * ARCSEC_PER_PX * TELESCOPE_D)
+    ms = js.zernike_modeset(mode_list, n, radius, WAVELENGTH, jscale)
+    pupil, _ = js.make_pupil(n, radius)
+    sup = js.pupil_support(pupil)
+    img_obj, img_ch, img_wf, phis, ref = [], [], [], [], []
+    ch_index = 0
+    z4 = js.zernike(4, n, radius)
+    for o, chans in enumerate(objects):
+        for c, pv_waves in enumerate(chans):
+            phis.append((math.pi / math.sqrt(3.0)) * pv_waves * z4)
+            for t in range(frames):
+                if o == 0 and c == 0:
+                    ref.append(len(img_obj))
+                img_obj.append(o); img_ch.append(ch_index); img_wf.append(t)
+            ch_index += 1
+    win, nwin = js.solver_windows(N, apodization)
+    ns = js.build_constraints(img_wf, n_modes, ref)
+    return Job(otf_size=otf, pupil_pixels=n, patch_size=N, n_modes=n_modes, modes=ms.modes,
+               mode_list=mode_list, tilt_x=ms.tilt_x, tilt_y=ms.tilt_y, J_T_xy=ms.J_T_xy,
+               pupil=pupil, support=sup,
+               img_object=np.array(img_obj, np.int32), img_channel=np.array(img_ch, np.int32),
+               img_wavefront=np.array(img_wf, np.int32), phi_fixed=np.stack(phis),
+               obj_weight=np.ones(len(objects)), obj_grad_step=np.full(len(objects), grad_step * WAVELENGTH),
+               window=win, noise_window=nwin, nullspace=ns, cutout_size=N + 2 * MAX_LOCAL_SHIFT,
+               channel_div_pv=np.array([pv for chans in objects for pv in chans]))
+
+
+def make_patches(job: Job, n_patches: int, d_r0: float, rng, fixed_gamma=None,
+                 photons=1e4, read_noise=10.0, K=None, tilt_scale=1.0) -> Patches:
+    """Images of `n_patches` independent patches (one object field per object and patch)."""
+    N, cs = job.patch_size, job.cutout_size
+    I, M = job.n_images, job.n_modes
+    frames = int(job.img_wavefront.max()) + 1
+    if K is None:
+        K = 1 << int(math.ceil(math.log2(cs + 64)))
+    var = np.array([js.zernike_covariance(j, j) for j in job.mode_list]) * d_r0 ** (5.0 / 3.0)
+    sd = np.sqrt(var)
+    n_obj = job.n_objects
+    cut = np.zeros((n_patches, I, cs, cs), np.float32)
+    alpha = np.zeros((n_patches, I, M))
+    for p in range(n_patches):
+        a_wf = rng.standard_normal((frames, M)) * sd
+        for tm in (job.tilt_x, job.tilt_y):
+            if tm >= 0:
+                a_wf[:, tm] *= tilt_scale
+        # tilts of the reference channel sum to zero (the constraint the solver imposes)
+        for tm in (job.tilt_x, job.tilt_y):
+            if tm >= 0:
+                a_wf[:, tm] -= a_wf[:, tm].mean()
+        objs = [_grf(rng, K) for _ in range(n_obj)]
+        objs_ft = [np.fft.fft2(o) for o in objs]
+        for j in range(I):
+            o = int(job.img_object[j]); c = int(job.img_channel[j]); t = int(job.img_wavefront[j])
+            pv = float(job.channel_div_pv[c])
+            psf = _psf_kernel(a_wf[t], job.mode_list,
+                              lambda n_, r_, pv=pv: pv * _zernike_cached(4, n_, r_), K)
+            img = np.real(np.fft.ifft2(objs_ft[o] * np.fft.fft2(psf)))
+            o0 = (K - cs) // 2
+            reg = np.clip(img[o0:o0 + cs, o0:o0 + cs], 0, None) * photons
+            noisy = rng.poisson(reg).astype(np.float64) + rng.normal(0.0, read_noise, reg.shape)
+            cut[p, j] = noisy.astype(np.float32)
+            alpha[p, j] = a_wf[t] * job.wavelength
+    fg = None
+    if fixed_gamma is not None:
+        fg = np.full((n_patches, n_obj), float(fixed_gamma))
+    return Patches(cutouts=cut, residual_alpha=np.zeros((n_patches, I, 2)), fixed_gamma=fg,
+                   alpha_true=alpha)
+
+
+LAYOUT_1OBJ = lambda frames: {"frames": frames, "objects": [[0.0, 1.0]]}          # focus + diversity
+LAYOUT_WB_NB = lambda frames: {"frames": frames, "objects": [[0.0], [0.0, 1.0]]}  # WB; NB focus + div
+
+
+def config(index: int, n_patches: int | None = None, seed_offset: int = 0, frames=None) -> Workload:
+    """The benchmark workloads, seeded with 20261203 + index (+ seed_offset)."""
+    rng = np.random.default_rng(20261203 + index + seed_offset)
+    if index == 0:
+        job = make_job(64, 20, LAYOUT_1OBJ(frames or 4))
+        pt = make_patches(job, n_patches or 1, 10.0, rng, fixed_gamma=1e-3)
+        cfg = dict(iterations=50, gamma=1e-3)
+        return Workload("plain FP64 64x64, 2ch x 4fr, Z2-21", job, pt, cfg)
+    if index == 1:
+        job = make_job(88, 36, LAYOUT_WB_NB(frames or 8))
+        pt = make_patches(job, n_patches or 1, 10.0, rng)
+        return Workload("adjoint check 88x88, 3ch x 8fr, 36 modes", job, pt, {})
+    if index == 2:
+        job = make_job(88, 36, LAYOUT_WB_NB(frames or 12))
+        pt = make_patches(job, n_patches or 225, 15.0, rng)
+        return Workload("production 88x88, 3ch x 12fr, 36 modes", job, pt, dict(iterations=100))
+    if index == 4:
+        job = make_job(128, 100, LAYOUT_WB_NB(frames or 32))
+        pt = make_patches(job, n_patches or 256, 25.0, rng)
+        return Workload("mixed precision 128x128, 3ch x 32fr, 100 modes", job, pt, {})
+    raise ValueError(f"unknown config {index}")

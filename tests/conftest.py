@@ -1,0 +1,35 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+
+
+_CACHE = {}
+
+
+def workload(index, **kw):
+    """Seeded synthetic workloads, generated once per session."""
+    from redux_gb300 import synth
+    key = (index, tuple(sorted(kw.items())))
+    if key not in _CACHE:
+        _CACHE[key] = synth.config(index, **kw)
+    return _CACHE[key]
+
+
+@pytest.fixture(scope="session")
+def w0():
+    return workload(0)
+
+
+@pytest.fixture(scope="session")
+def w2small():
+    # the production geometry (88 x 88, 36 modes, 3 channels) with 4 frames and 2 patches
+    return workload(2, n_patches=2, frames=4)
