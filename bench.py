@@ -1,0 +1,316 @@
+"""Benchmark: converged MOMFBD patches/s on the production workload (one GB300).
+
+Workload (default): 225 patches of 88 x 88 px, 36 modes, 3 channels x 12 frames
+(wide-band + narrow-band focus + narrow-band +1 wave defocus), per-patch Kolmogorov
+wavefronts at D/r0 = 15, 100 CG iterations per patch (all modes at once, FTOL = 0),
+seeded synthetic data.  One step = one complete solve of the batch: image preparation
+(windowing, transforms, noise, regularisation) and 100 iterations of the reference's
+conjugate-gradient/line-search for every patch.
+
+value: patches/s with the cutouts resident in HBM (set_patches_device + solve).
+e2e:   patches/s through the public API from pinned host memory (cutouts H2D, solve,
+       coefficients/reports/metric histories D2H), per step.
+--impl reference: the reference's CPU path timed on the host cores -- redux itself does not
+       build here (Boost, FFTW3, GSL, OpenCV missing), so its FP64 restatement (oracle/) is
+       timed with all host threads on a bounded sample (one patch, same settings).
+Multi-GPU: independent replicas (patches are independent); value = all patches / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "converged MOMFBD patches/s at 1e-5 rel metric vs FP64: chosen vs plain GPU"
+UNIT = "patches/s"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return dict(hbm=d.get("hbm_gbs", 6800.0), src="measured", sm_max=d.get("sm_max_mhz", 2070.0))
+    return dict(hbm=6800.0, src="fallback", sm_max=2070.0)
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                self.rows.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if len(r) >= 7 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 7 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) >= 7:
+                for k, nm in enumerate(names):
+                    if r[3 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def workload(patches, frames, iterations):
+    from redux_gb300 import synth
+    cache = os.path.join("/tmp", f"rdxg_bench_w2_{patches}_{frames}.npz")
+    job = synth.make_job(88, 36, synth.LAYOUT_WB_NB(frames))
+    if os.path.exists(cache):
+        d = np.load(cache)
+        cut = d["cutouts"]
+    else:
+        rng = np.random.default_rng(20261203 + 2)
+        pt = synth.make_patches(job, patches, 15.0, rng)
+        cut = pt.cutouts
+        try:
+            np.savez(cache, cutouts=cut)
+        except OSError:
+            pass
+    return job, np.ascontiguousarray(cut, np.float32)
+
+
+def cpu_port(job, cut, iterations, threads, n_patches=1):
+    """FP64 restatement of the reference CPU path on `n_patches` patches; returns seconds."""
+    import oracle
+    t = 0.0
+    finals = []
+    for p in range(n_patches):
+        op = oracle.OraclePatch(job, threads=threads)
+        op.set_images(cut[p], None, None)
+        cfg = oracle.default_cfg(max_iterations=iterations, n_modes=job.n_modes)
+        t0 = time.perf_counter()
+        r = op.solve(cfg)
+        t += time.perf_counter() - t0
+        finals.append(r["report"].final_metric)
+    return t, finals
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    job, cut = workload(args.patches, args.frames, args.iterations)
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        pass   # the oracle has no warm-up state; each step is a fresh patch solve
+    for s in range(args.steps):
+        t, _ = cpu_port(job, cut[s % cut.shape[0]:s % cut.shape[0] + 1], args.iterations, threads)
+        vals.append(1.0 / t)
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"{args.patches} patches 88x88, 36 modes, 3ch x {args.frames} frames, "
+                                   f"{args.iterations} CG iterations (one patch per step on the CPU)",
+                       "l2": "cpu"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"1 patch x {args.iterations} iterations per step, FP64, "
+                                       f"{threads} OpenMP threads over images (redux does not build here)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours")
+    ap.add_argument("--patches", type=int, default=225)
+    ap.add_argument("--frames", type=int, default=12)
+    ap.add_argument("--iterations", type=int, default=100)
+    ap.add_argument("--no-baselines", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from redux_gb300 import solver as S
+
+    job, cut = workload(args.patches, args.frames, args.iterations)
+    P = cut.shape[0]
+    settings = S.fixed_iterations(job.n_modes, args.iterations, max_metrics=args.iterations + 8)
+    solver = S.Solver(job, max_patches=P, device=local)
+    stream = torch.cuda.Stream()
+    solver.set_stream(stream.cuda_stream)
+    cut_dev = torch.from_numpy(cut).to(f"cuda:{local}")
+    cut_pin = torch.from_numpy(cut).pin_memory()
+    cut_pin_np = cut_pin.numpy()
+    torch.cuda.synchronize()
+
+    def step_device():
+        solver.set_patches_device(P, cut_dev.data_ptr())
+        solver.run_async(settings)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step_device()
+    barrier()
+    launches = 0
+    with ClockSampler(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step_device()
+            launches += solver.launch_count() + 1
+        e1.record(stream)
+        e1.synchronize()
+        barrier()
+        ms_dev = e0.elapsed_time(e1) / args.steps
+    out = solver.fetch(settings.max_metrics)
+    reps = out["reports"]
+    iters = [r.iterations for r in reps]
+    nf = sum(r.n_f_evals for r in reps) / P
+    ndf = sum(r.n_df_evals for r in reps) / P
+
+    # end to end through the public API from pinned host memory
+    ms_e2e = []
+    alpha_bytes = P * job.n_images * job.n_modes * 8
+    for _ in range(args.steps):
+        barrier()
+        t0 = time.perf_counter()
+        solver.set_patches(cut_pin_np)
+        r = solver.run(settings)
+        torch.cuda.synchronize()
+        ms_e2e.append((time.perf_counter() - t0) * 1000.0)
+    e2e_ms = statistics.median(ms_e2e)
+    h2d = cut.nbytes
+    d2h = alpha_bytes + P * 48 + P * settings.max_metrics * 8
+
+    if dist is not None:
+        t = torch.tensor([ms_dev, e2e_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_dev, e2e_ms = t.tolist()
+    value = world * P / (ms_dev / 1000.0)
+    e2e_value = world * P / (e2e_ms / 1000.0)
+
+    # roofline of the dominant kernel, measured on the same batch
+    kt = solver.profile_kernels(reps=5)
+    peaks = _peaks()
+    N, n, M = job.otf_size, job.pupil_pixels, job.n_modes
+    G = P * job.n_images
+    # per image and metric evaluation: the transforms of the OTF and the mode expansion
+    fft_flops = 5.0 * N * N * math.log2(N * N)
+    f_eval_flops = 2 * fft_flops + 2.0 * M * n * n
+    per_launch = {
+        "forward": dict(bytes=G * 8.0 * N * N, flops=G * f_eval_flops),
+        "accum": dict(bytes=G * 2 * 8.0 * N * N, flops=G * 16.0 * N * N),
+        "adjoint": dict(bytes=G * 4 * 8.0 * N * N, flops=G * (2 * fft_flops + 2.0 * M * n * n)),
+    }
+    # time share per step: forward and accumulation run every round, the adjoint only does
+    # work in rounds where a patch needs a gradient (about one in ten)
+    rounds = launches / max(1, args.steps) / 6.0
+    share = {"forward": rounds * kt["forward"], "accum": rounds * kt["accum"], "adjoint": ndf * kt["adjoint"]}
+    dom = max(share, key=share.get)
+    achieved = per_launch[dom]["bytes"] / (kt[dom] / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm"], "traffic": None, "kernel": dom,
+                "peak_source": peaks["src"], "kernel_ms": kt,
+                "share_ms_per_step": share,
+                "fp32_tflops": {k: per_launch[k]["flops"] / (kt[k] / 1000.0) / 1e12 for k in per_launch}}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_dev, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP64 sums and CG scalars)", "data": "synthetic",
+            "config": {"workload": f"{P} patches 88x88, 36 modes, 3ch x {args.frames} frames, D/r0=15, "
+                                   f"{args.iterations} CG iterations, all modes at once",
+                       "patches_per_gpu": P, "iterations": args.iterations,
+                       "l2": "inputs larger than L2 (D, OTF: 2 x 500 MB per batch)",
+                       "metric_evals_per_patch": nf, "gradient_evals_per_patch": ndf,
+                       "cg_iterations_per_s": world * P * args.iterations / (ms_dev / 1000.0)},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches), "roofline": roofline, "clocks": clk.summary()}
+
+    if rank == 0 and not args.no_baselines:
+        # plain FP64 GPU form: same algorithm in double precision, one patch per launch sequence
+        nplain = min(4, P)
+        s64 = S.Solver(job, max_patches=1, precision="fp64", device=local)
+        t_plain = 0.0
+        finals64 = []
+        for p in range(nplain):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s64.set_patches(cut[p:p + 1])
+            r64 = s64.run(settings)
+            torch.cuda.synchronize()
+            t_plain += time.perf_counter() - t0
+            finals64.append(r64["reports"][0].final_metric)
+        plain_v = nplain / t_plain
+        f32 = [reps[p].final_metric for p in range(nplain)]
+        rel = [abs(a - b) / abs(b) for a, b in zip(f32, finals64)]
+        line["plain_fp64_gpu"] = {"value": plain_v, "unit": UNIT, "sample": f"{nplain} patches, per-patch launches",
+                                  "speedup_chosen_vs_plain": value / world / plain_v,
+                                  "final_metric_rel_diff_vs_fp64": rel,
+                                  "within_1e-5": sum(1 for x in rel if x <= 1e-5)}
+        s64.close()
+        # CPU baseline: the FP64 restatement on all host cores, one patch
+        threads = os.cpu_count() or 1
+        tc, finals_cpu = cpu_port(job, cut, args.iterations, threads, 1)
+        line["cpu_baseline"] = {"value": 1.0 / tc, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"1 patch x {args.iterations} iterations, FP64 restatement, "
+                                          f"{threads} OpenMP threads over images",
+                                "final_metric_rel_diff_gpu_vs_cpu": abs(reps[0].final_metric - finals_cpu[0]) / abs(finals_cpu[0])}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -150,6 +150,13 @@ int rdxg_fetch_results(rdxg_solver* h, double* alpha_out, rdxg_patch_report* rep
 /* Number of kernel launches issued by the last rdxg_solve / rdxg_solve_async. */
 int64_t rdxg_last_launch_count(const rdxg_solver* h);
 
+/* Times the per-image and per-object kernels on the loaded batch at the current point with
+ * CUDA events on the handle's stream: ms[0] forward (metric evaluation), ms[1] per-object
+ * accumulation, ms[2] forward (gradient evaluation, also keeps the transforms), ms[3]
+ * analytic adjoint gradient, ms[4] finite-difference gradient; average ms per launch over
+ * reps launches.  Used to pick kernel shapes and to report the roofline. */
+int rdxg_profile_kernels(rdxg_solver* h, int32_t reps, double* ms);
+
 /* Debug copies of device state (host buffers sized by the caller):
  * which = 0 D [P][I][N][N] complex, 1 OTF [P][I][N][N] complex, 2 gamma [P][nObj],
  *         3 image stats [P][I][3] (mean, stddev, noise), 4 object O [P][nObj][N][N] complex,

@@ -634,6 +634,47 @@ int rdxg_solve(rdxg_solver* h, const rdxg_solve_params* s, double* alpha_out, rd
 
 int64_t rdxg_last_launch_count(const rdxg_solver* h) { return h ? h->launches : 0; }
 
+int rdxg_profile_kernels(rdxg_solver* h, int32_t reps, double* ms) {
+    if (!h || !ms || reps < 1) return RDXG_ERR_ARG;
+    if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
+    cudaEvent_t e0, e1;
+    CK(h, cudaEventCreate(&e0));
+    CK(h, cudaEventCreate(&e1));
+    const int G = h->P * h->I, PO = h->P * h->nObj;
+    int r = RDXG_OK;
+    for (int k = 0; k < 5 && !r; ++k) {
+        const int req = (k < 2) ? REQ_F : REQ_DF;
+        const int gm = (k == 4) ? GM_FD : GM_VOGEL;
+        if ((r = set_requests(h, req, gm, h->M))) break;
+        auto launch = [&](int which) {
+            with_size(h->N, h->fp64, [&](auto L, auto t) {
+                using T = decltype(t);
+                KParams<T> kp = make_kparams<T>(h);
+                switch (which) {
+                    case 0: case 2: decltype(L)::forward(kp, G, h->stream); break;
+                    case 1: launch_accum<T>(kp, PO, h->stream); break;
+                    case 3: decltype(L)::adjoint(kp, G, GK_VOGEL, h->stream); break;
+                    case 4: decltype(L)::fd(kp, G, h->M, h->stream); break;
+                }
+            });
+        };
+        // inputs of the timed kernel: forward and accumulation in the requested mode
+        if (k >= 3) { launch(2); launch(1); }
+        launch(k);   // warm-up
+        CK(h, cudaEventRecord(e0, h->stream));
+        for (int i = 0; i < reps; ++i) launch(k);
+        CK(h, cudaEventRecord(e1, h->stream));
+        CK(h, cudaEventSynchronize(e1));
+        CKL(h);
+        float t = 0;
+        CK(h, cudaEventElapsedTime(&t, e0, e1));
+        ms[k] = (double)t / reps;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return r;
+}
+
 int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes) {
     if (!h || !out) return RDXG_ERR_ARG;
     const size_t G = (size_t)h->P * h->I, N2 = (size_t)h->N * h->N, PO = (size_t)h->P * h->nObj;

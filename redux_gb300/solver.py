@@ -160,6 +160,12 @@ class Solver:
         self._check(_lib.load().rdxg_fetch_results(self.h, _lib.ptr(alpha), reps, _lib.ptr(mets)), "rdxg_fetch_results")
         return dict(alpha=alpha, reports=list(reps), metrics=mets)
 
+    def profile_kernels(self, reps: int = 5) -> dict:
+        """Average ms per launch of each kernel on the loaded batch (CUDA events)."""
+        ms = np.zeros(5)
+        self._check(_lib.load().rdxg_profile_kernels(self.h, reps, _lib.ptr(ms)), "rdxg_profile_kernels")
+        return dict(zip(("forward", "accum", "forward_grad", "adjoint", "fd"), ms.tolist()))
+
     def launch_count(self) -> int:
         return int(_lib.load().rdxg_last_launch_count(self.h))
 

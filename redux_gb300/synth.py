@@ -17,6 +17,7 @@ import math
 from dataclasses import dataclass, field
 
 import numpy as np
+import scipy.fft as sfft
 
 from . import jobsetup as js
 
@@ -97,11 +98,21 @@ def _grf(rng, size, contrast=0.1):
     return 1.0 + g
 
 
+_PUPILS = {}
+
+
+def _pupil_cached(n, radius):
+    key = (n, radius)
+    if key not in _PUPILS:
+        _PUPILS[key] = js.make_pupil(n, radius)[0]
+    return _PUPILS[key]
+
+
 def _psf_kernel(alpha_rad, mode_list, phi_fixed_rad_fn, K):
     """PSF on a K x K grid at critical sampling, from the analytic phase on a K/2 pupil."""
     n = K // 2
     radius = n / 2.0
-    pupil, _ = js.make_pupil(n, radius)
+    pupil = _pupil_cached(n, radius)
     phi = np.zeros((n, n))
     for a, j in zip(alpha_rad, mode_list):
         if a != 0.0:
@@ -111,7 +122,7 @@ def _psf_kernel(alpha_rad, mode_list, phi_fixed_rad_fn, K):
     o = (K - n) // 2
     pf[o:o + n, o:o + n] = pupil * np.exp(1j * phi)
     # the solver's OTF is S = c^2 ifft(|fft(P)|^2), i.e. the PSF is |ifft(P)|^2
-    psf = np.abs(np.fft.ifft2(pf)) ** 2
+    psf = np.abs(sfft.ifft2(pf, workers=-1)) ** 2
     psf /= psf.sum()
     return psf   # centred at (0, 0) (periodic)
 
@@ -178,6 +189,13 @@ def make_patches(job: Job, n_patches: int, d_r0: float, rng, fixed_gamma=None,
     n_obj = job.n_objects
     cut = np.zeros((n_patches, I, cs, cs), np.float32)
     alpha = np.zeros((n_patches, I, M))
+    n = K // 2
+    radius = n / 2.0
+    pupil = _pupil_cached(n, radius)
+    Zk = np.stack([_zernike_cached(jm, n, radius) for jm in job.mode_list])
+    z4 = _zernike_cached(4, n, radius)
+    o0 = (K - cs) // 2
+    op = (K - n) // 2
     for p in range(n_patches):
         a_wf = rng.standard_normal((frames, M)) * sd
         for tm in (job.tilt_x, job.tilt_y):
@@ -188,18 +206,24 @@ def make_patches(job: Job, n_patches: int, d_r0: float, rng, fixed_gamma=None,
             if tm >= 0:
                 a_wf[:, tm] -= a_wf[:, tm].mean()
         objs = [_grf(rng, K) for _ in range(n_obj)]
-        objs_ft = [np.fft.fft2(o) for o in objs]
+        objs_ft = np.stack([sfft.fft2(o, workers=-1) for o in objs])
+        # all images of the patch at once: phase on a K/2 pupil, PSF = |ifft(P)|^2 (the
+        # solver's convention, S = c^2 ifft(|fft(P)|^2)), circular convolution on K x K
+        phase = np.tensordot(a_wf, Zk, 1)                     # (frames, n, n)
+        pf = np.zeros((I, K, K), np.complex64)
         for j in range(I):
-            o = int(job.img_object[j]); c = int(job.img_channel[j]); t = int(job.img_wavefront[j])
-            pv = float(job.channel_div_pv[c])
-            psf = _psf_kernel(a_wf[t], job.mode_list,
-                              lambda n_, r_, pv=pv: pv * _zernike_cached(4, n_, r_), K)
-            img = np.real(np.fft.ifft2(objs_ft[o] * np.fft.fft2(psf)))
-            o0 = (K - cs) // 2
-            reg = np.clip(img[o0:o0 + cs, o0:o0 + cs], 0, None) * photons
-            noisy = rng.poisson(reg).astype(np.float64) + rng.normal(0.0, read_noise, reg.shape)
-            cut[p, j] = noisy.astype(np.float32)
-            alpha[p, j] = a_wf[t] * job.wavelength
+            c = int(job.img_channel[j]); t = int(job.img_wavefront[j])
+            ph = phase[t] + float(job.channel_div_pv[c]) * (math.pi / math.sqrt(3.0)) * z4
+            pf[j, op:op + n, op:op + n] = (pupil * np.exp(1j * ph)).astype(np.complex64)
+        psf = np.abs(sfft.ifft2(pf, axes=(-2, -1), workers=-1)) ** 2
+        psf /= psf.sum(axis=(-2, -1), keepdims=True)
+        otf = sfft.fft2(psf, axes=(-2, -1), workers=-1)
+        img = np.real(sfft.ifft2(objs_ft[job.img_object].astype(np.complex64) * otf, axes=(-2, -1), workers=-1))
+        reg = np.clip(img[:, o0:o0 + cs, o0:o0 + cs], 0, None) * photons
+        noisy = rng.poisson(reg).astype(np.float64) + rng.normal(0.0, read_noise, reg.shape)
+        cut[p] = noisy.astype(np.float32)
+        for j in range(I):
+            alpha[p, j] = a_wf[int(job.img_wavefront[j])] * job.wavelength
     fg = None
     if fixed_gamma is not None:
         fg = np.full((n_patches, n_obj), float(fixed_gamma))
