@@ -162,6 +162,8 @@ def main():
     ap.add_argument("--frames", type=int, default=12)
     ap.add_argument("--iterations", type=int, default=100)
     ap.add_argument("--no-baselines", action="store_true")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="load the batch and time each kernel once (profiling target)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -183,6 +185,13 @@ def main():
     solver = S.Solver(job, max_patches=P, device=local)
     stream = torch.cuda.Stream()
     solver.set_stream(stream.cuda_stream)
+    if args.kernels_only:
+        solver.set_patches(cut)
+        kt = solver.profile_kernels(reps=1)
+        torch.cuda.synchronize()
+        print(json.dumps({"kernel_ms": kt, "patches": P}), flush=True)
+        solver.close()
+        return
     cut_dev = torch.from_numpy(cut).to(f"cuda:{local}")
     cut_pin = torch.from_numpy(cut).pin_memory()
     cut_pin_np = cut_pin.numpy()
@@ -232,10 +241,8 @@ def main():
     h2d = cut.nbytes
     d2h = alpha_bytes + P * 48 + P * settings.max_metrics * 8
 
-    if dist is not None:
-        t = torch.tensor([ms_dev, e2e_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_dev, e2e_ms = t.tolist()
+    from redux_gb300.replicas import max_over_ranks
+    ms_dev, e2e_ms = max_over_ranks([ms_dev, e2e_ms], device=f"cuda:{local}")
     value = world * P / (ms_dev / 1000.0)
     e2e_value = world * P / (e2e_ms / 1000.0)
 

@@ -75,6 +75,8 @@ def lib():
         L.orc_get_stats.argtypes = [C.c_void_p, f64p, f64p, f64p]
         L.orc_get_shifts.argtypes = [C.c_void_p, i32p, f64p]
         L.orc_shift.argtypes = [C.c_void_p, f64p]
+        L.orc_reorder_into.restype = C.c_int
+        L.orc_reorder_into.argtypes = [f64p, C.c_int, C.c_int, f64p, C.c_int, C.c_int, C.c_int]
         L.orc_cons_apply.argtypes = [C.c_void_p, f64p, f64p]
         L.orc_cons_reverse_add.argtypes = [C.c_void_p, f64p, f64p, f64p]
         _LIB = L
@@ -96,6 +98,16 @@ def reorder(a: np.ndarray) -> np.ndarray:
     buf = np.ascontiguousarray(a, np.float64).copy()
     lib().orc_reorder(buf, a.shape[0], a.shape[1], 0)
     return buf
+
+
+def reorder_into(a: np.ndarray, out_shape=None, center: bool = False) -> np.ndarray:
+    a = np.ascontiguousarray(a, np.float64)
+    oy, ox = out_shape if out_shape is not None else a.shape
+    out = np.zeros((oy, ox))
+    r = lib().orc_reorder_into(a, a.shape[0], a.shape[1], out, oy, ox, int(center))
+    if r:
+        raise ValueError("reorderInto: target smaller than source")
+    return out
 
 
 def autocorrelate(a: np.ndarray, center: bool = False) -> np.ndarray:

@@ -1,0 +1,86 @@
+"""Independent numpy FP64 restatement of the per-image model (test infrastructure).
+
+Written directly from the reference's formulas, with numpy's FFT instead of the oracle's
+own, to cross-check oracle.c:
+  OTF  S = fftshift(ifft(|fft(c PF embedded at n/2)|^2))     subimage.cpp:586-612
+  P = sum_j conj(D_j) S_j,  Q = gamma + sum_j |S_j|^2          subimage.cpp:226-234
+  L = sum_obj w sum_support (sum_j |D_j|^2 - |P|^2/Q) / ps^2   object.cpp:597-615
+  Vogel gradient, literally as calcVogelWeight/gradientVogel   subimage.cpp:312-390
+  exact gradient  dL/dphi = -4 c^2 / ps^2 Im(conj(PF) (G * PF))
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+class NumpyModel:
+    def __init__(self, job, D, gamma, otf_norm):
+        self.job = job
+        self.D = D                      # (I, N, N) centred image transforms
+        self.gamma = np.asarray(gamma)  # (nObj,)
+        self.c = np.asarray(otf_norm)   # (C,)
+        N = job.otf_size
+        m = np.zeros(N * N, bool)
+        m[job.support.otf_support] = True
+        self.mask = m.reshape(N, N)
+
+    def phase(self, alpha):
+        j = self.job
+        return j.phi_fixed[j.img_channel] + np.tensordot(alpha, j.modes, axes=([1], [0]))
+
+    def otf(self, alpha):
+        j = self.job
+        N, n = j.otf_size, j.pupil_pixels
+        phi = self.phase(alpha)
+        PF = j.pupil[None] * np.exp(1j * phi)
+        big = np.zeros((j.n_images, N, N), complex)
+        big[:, n // 2:n // 2 + n, n // 2:n // 2 + n] = PF * self.c[j.img_channel][:, None, None]
+        X = np.fft.fft2(big)
+        S = np.fft.fftshift(np.fft.ifft2(np.abs(X) ** 2), axes=(-2, -1))
+        return S, PF
+
+    def pq(self, S):
+        j = self.job
+        P = np.zeros((j.n_objects,) + S.shape[1:], complex)
+        Q = np.zeros((j.n_objects,) + S.shape[1:]) + self.gamma[:, None, None]
+        F = np.zeros_like(Q)
+        for i in range(j.n_images):
+            o = j.img_object[i]
+            P[o] += np.conj(self.D[i]) * S[i]
+            Q[o] += np.abs(S[i]) ** 2
+            F[o] += np.abs(self.D[i]) ** 2
+        return P, Q, F
+
+    def metric(self, alpha):
+        j = self.job
+        S, _ = self.otf(alpha)
+        P, Q, F = self.pq(S)
+        L = 0.0
+        for o in range(j.n_objects):
+            t = (F[o] - np.abs(P[o]) ** 2 / Q[o])[self.mask].sum() / j.patch_size ** 2
+            L += j.obj_weight[o] * t
+        return L
+
+    def gradient(self, alpha, kind="vogel"):
+        j = self.job
+        N, n, M = j.otf_size, j.pupil_pixels, j.n_modes
+        S, PF = self.otf(alpha)
+        P, Q, _ = self.pq(S)
+        A = j.pupil
+        area = float(A.ravel()[j.support.pupil_support].sum())
+        g = np.zeros((j.n_images, M))
+        for i in range(j.n_images):
+            o = j.img_object[i]
+            G = (P[o] * Q[o] * self.D[i] - np.abs(P[o]) ** 2 * S[i]) / Q[o] ** 2 * self.mask
+            p = np.zeros((N, N), complex)
+            p[:n, :n] = PF[i]
+            conv = np.fft.ifft2(np.fft.fft2(np.fft.ifftshift(G)) * np.fft.fft2(p))[:n, :n]   # (G * PF)
+            w = j.obj_weight[o]
+            if kind == "vogel":
+                v = np.imag(np.conj(PF[i]) * conv) * A / N ** 2
+                g[i] = (-2.0 * area / N ** 2) * w * w * np.tensordot(j.modes, v, 2)
+            else:
+                c = self.c[j.img_channel[i]]
+                dphi = -(4.0 * c * c / j.patch_size ** 2) * np.imag(np.conj(PF[i]) * conv) * (A > 0)
+                g[i] = w * np.tensordot(j.modes, dphi, 2)
+        return g

@@ -1354,3 +1354,33 @@ void orc_get_shifts(const orc_patch* p, int32_t* shift, double* tiltoff) {
 
 /* Solver::shiftAndInit(alpha, false) for an external driver */
 void orc_shift(orc_patch* p, const double* alpha) { shift_and_init(p, alpha); }
+
+/* FourierTransform::reorderInto (fouriertransform.hpp:112-171) for real data: the four
+ * quadrants of in (inY x inX) into the corners (center=0) or around the centre (center=1)
+ * of out (outY x outX), which the caller has zeroed. */
+int orc_reorder_into(const double* in, int inY, int inX, double* out, int outY, int outX, int center) {
+    if (!in || !out) return 1;
+    if (outY == 0 && outX == 0) { outY = inY; outX = inX; }
+    if (inY > outY || inX > outX) return 2;
+    if (inY == outY && inX == outX) center = 0;
+    const int inMidY = inY / 2, inMidX = inX / 2, oddY = inY % 2, oddX = inX % 2;
+    const int diffY = outY - inY, diffX = outX - inX, diffYh = diffY / 2, diffXh = diffX / 2;
+    const int wDx = center ? diffXh : 0, eDx = center ? (diffXh - diffX) : 0;
+    const int sDy = center ? diffYh * outX : 0, nDy = center ? (diffYh - diffY) * outX : 0;
+    const double* southEastIn = in + inMidX + oddX;
+    const double* northWestIn = in + (long)(inMidY + oddY) * inX;
+    const double* northEastIn = southEastIn + (long)(inMidY + oddY) * inX;
+    double* southWestOut = out + sDy + wDx;
+    double* southEastOut = out + outX - inMidX - oddX + sDy + eDx;
+    double* northWestOut = out + (long)(outY - inMidY - oddY) * outX + nDy + wDx;
+    double* northEastOut = out + (long)(outY - inMidY - oddY + 1) * outX - inMidX - oddX + nDy + eDx;
+    for (int y = 0; y < inMidY; ++y) {
+        memcpy(southWestOut + (long)y * outX, northEastIn + (long)y * inX, sizeof(double) * inMidX);
+        memcpy(southEastOut + (long)y * outX, northWestIn + (long)y * inX, sizeof(double) * (inMidX + oddX));
+    }
+    for (int y = inMidY + oddY - 1; y >= 0; --y) {
+        memcpy(northEastOut + (long)y * outX, in + (long)y * inX, sizeof(double) * (inMidX + oddX));
+        memcpy(northWestOut + (long)y * outX, southEastIn + (long)y * inX, sizeof(double) * inMidX);
+    }
+    return 0;
+}
