@@ -132,6 +132,11 @@ int rdxg_set_patches_device(rdxg_solver* h, int32_t n_patches, const float* d_cu
  * solver.cpp:219-225, 763-817).  metric: [P]. */
 int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric);
 
+/* Metric at alpha [P][I][M] evaluated the way the solver's line search does: with the
+ * reference object of the batched metric taken at alpha_ref (the last gradient point) instead
+ * of alpha.  Same result as rdxg_metric up to rounding; used to check that rounding. */
+int rdxg_metric_with_reference(rdxg_solver* h, const double* alpha_ref, const double* alpha, double* metric);
+
 /* Gradient in alpha space [P][I][M] at alpha (Solver::my_df without the constraint map,
  * solver.cpp:228-234, 860-894); enabled: [M] flags or NULL (all); metric: [P] or NULL. */
 int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, int32_t method,

@@ -39,6 +39,7 @@ struct rdxg_solver {
     void *dZ = nullptr, *dA = nullptr, *dPhi = nullptr, *dOtfNorm = nullptr, *dTw = nullptr;
     uint8_t* dMask = nullptr;
     int32_t *dImgObj = nullptr, *dImgCh = nullptr, *dObjFirst = nullptr, *dObjCount = nullptr;
+    const int32_t *dObjFirstC = nullptr, *dObjCountC = nullptr;
     double *dObjW = nullptr, *dGradStep = nullptr, *dWin = nullptr, *dNWin = nullptr;
     int32_t *dRowPtr = nullptr, *dRowCol = nullptr, *dColPtr = nullptr, *dColRow = nullptr;
     double *dRowVal = nullptr, *dColVal = nullptr;
@@ -63,6 +64,20 @@ struct rdxg_solver {
     bool haveFixedGamma = false;
     int64_t launches = 0;
     rdxg_solve_params lastParams{};
+    // fused evaluation path (FP32, N <= 88)
+    bool fused = false;
+    int npt = 0, chunk = 6, chunksPerPatch = 0, nH = 0, evalGrid = 0, reduceGrid = 0, numSMs = 0;
+    std::vector<int32_t> objChunk0, hIdx, hPos;
+    int nTilesH = 0;
+    int32_t *dHPos = nullptr;
+    int32_t *dHIdx = nullptr, *dObjChunk0 = nullptr, *dCounters = nullptr, *dAux = nullptr;
+    void *dDh = nullptr, *dOh = nullptr, *dPart = nullptr, *dPhiImg = nullptr;
+    int phaseGrid = 0;
+    double* dObjMetric = nullptr;
+    EvalItem* dEval = nullptr;
+    PoItem* dPoList = nullptr;
+    int32_t *dGradP = nullptr, *dFdP = nullptr;
+    int adjGrid = 0, fdGrid = 0;
 };
 
 namespace {
@@ -131,6 +146,16 @@ void with_size(int N, bool fp64, F&& f) {
 #undef RDXG_CASE
 }
 
+template <typename F>
+void with_eval(int N, F&& f) {
+    switch (N) {
+        case 32: f(EvalLauncher<float, 32>{}); break;
+        case 64: f(EvalLauncher<float, 64>{}); break;
+        case 88: f(EvalLauncher<float, 88>{}); break;
+        default: break;
+    }
+}
+
 template <typename T>
 KParams<T> make_kparams(rdxg_solver* h) {
     KParams<T> k{};
@@ -148,7 +173,31 @@ KParams<T> make_kparams(rdxg_solver* h) {
     k.O = (cx<T>*)h->dO; k.Qt = (T*)h->dQt;
     k.gamma = h->dGamma; k.partial = h->dPartial; k.galpha = h->dGalpha;
     k.req = h->dReq; k.gmethod = h->dGm; k.modeCount = h->dMc; k.reinit = h->dReinit;
+    k.Dh = (cx<T>*)h->dDh; k.hIdx = h->dHIdx; k.nH = h->nH;
+    k.gradP = h->dGradP; k.nGradP = h->dCounters + 2; k.fdP = h->dFdP; k.nFdP = h->dCounters + 3;
     return k;
+}
+
+Lists make_lists(rdxg_solver* h) {
+    Lists L{};
+    L.eval = h->dEval; L.po = h->dPoList;
+    L.counters = h->dCounters;
+    L.nEval = h->dCounters + 0; L.nPo = h->dCounters + 1;
+    L.gradP = h->dGradP; L.nGradP = h->dCounters + 2;
+    L.fdP = h->dFdP; L.nFdP = h->dCounters + 3;
+    return L;
+}
+
+template <typename T>
+EvalParams<T> make_evalparams(rdxg_solver* h) {
+    EvalParams<T> e{};
+    e.k = make_kparams<T>(h);
+    e.hp.nH = h->nH; e.hp.idx = h->dHIdx; e.hp.chunkSize = h->chunk;
+    e.hp.chunksPerPatch = h->chunksPerPatch; e.hp.objChunk0 = h->dObjChunk0;
+    e.Dh = (const cx<T>*)h->dDh; e.Oh = (cx<T>*)h->dOh; e.part = (T*)h->dPart;
+    e.objMetric = h->dObjMetric; e.L = make_lists(h);
+    e.hPos = h->dHPos; e.nTilesH = h->nTilesH; e.phi = (T*)h->dPhiImg;
+    return e;
 }
 
 template <typename T>
@@ -162,6 +211,10 @@ CgArgs<T> make_cgargs(rdxg_solver* h, const CgParams& prm) {
     a.colPtr = h->dColPtr; a.colRow = h->dColRow; a.colVal = h->dColVal;
     a.curTilt = h->dCurTilt; a.resAlpha = h->dResAlpha; a.tiltX = h->geo.tilt_x; a.tiltY = h->geo.tilt_y;
     a.alphaEff = (T*)h->dAlphaEff; a.req = h->dReq; a.gmethod = h->dGm; a.modeCount = h->dMc; a.active = h->dActive;
+    a.fused = h->fused ? 1 : 0;
+    a.objMetric = h->dObjMetric; a.L = make_lists(h); a.nTilesH = h->nTilesH;
+    a.chunkSize = h->chunk; a.chunksPerPatch = h->chunksPerPatch; a.objChunk0 = h->dObjChunk0;
+    a.objFirst = h->dObjFirstC; a.objCount = h->dObjCountC; a.aux = h->dAux;
     return a;
 }
 
@@ -223,7 +276,8 @@ int alloc_patch_buffers(rdxg_solver* h) {
         (r = dalloc_t(h, &h->dCurTilt, G * 2)) || (r = dalloc_t(h, &h->dResAlpha, G * 2)) ||
         (r = dalloc_t(h, &h->dStates, P)) || (r = dalloc_t(h, &h->dVec, P * 5 * h->nFree)) ||
         (r = dalloc_t(h, &h->dAlpha, P * h->nPar)) || (r = dalloc_t(h, &h->dAlphaOff, P * h->nPar)) ||
-        (r = dalloc_t(h, &h->dActive, 1)))
+        (r = dalloc_t(h, &h->dActive, 1)) || (r = dalloc_t(h, &h->dGradP, P)) || (r = dalloc_t(h, &h->dFdP, P)) ||
+        (r = dalloc_t(h, &h->dCounters, 4)))
         return r;
     CK(h, cudaMallocHost((void**)&h->hActive, sizeof(int32_t)));
     CK(h, cudaMemset(h->dReinit, 0, G));
@@ -353,7 +407,13 @@ int metric_from_partials(rdxg_solver* h, double* metric) {
 }
 
 int set_requests(rdxg_solver* h, int req, int gm, int mc) {
-    std::vector<int32_t> a(h->P, req), b(h->P, gm), c(h->P, mc);
+    std::vector<int32_t> a(h->P, req), b(h->P, gm), c(h->P, mc), all(h->P);
+    for (int p = 0; p < h->P; ++p) all[p] = p;
+    int32_t cnt[2] = {0, 0};
+    if (req == REQ_DF) { if (gm == GM_FD) cnt[1] = h->P; else cnt[0] = h->P; }
+    CK(h, cudaMemcpyAsync(h->dGradP, all.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->dFdP, all.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->dCounters + 2, cnt, 2 * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaMemcpyAsync(h->dReq, a.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaMemcpyAsync(h->dGm, b.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaMemcpyAsync(h->dMc, c.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
@@ -380,6 +440,129 @@ CgParams make_cg_params(rdxg_solver* h, const rdxg_solve_params* s) {
     prm.brent_tol = 0.1;
     prm.init_step = 1E-21;
     return prm;
+}
+
+// Half-plane of the OTF support and buffers of the fused evaluation path.
+int setup_fused(rdxg_solver* h, const rdxg_static* s) {
+    const int N = h->N;
+    h->fused = false;
+    if (h->fp64 || !(N == 32 || N == 64 || N == 88)) return RDXG_OK;
+    std::vector<uint8_t> mask((size_t)N * N, 0);
+    for (int k = 0; k < s->n_otf_support; ++k) mask[s->otf_support[k]] = 1;
+    h->hIdx.clear();
+    for (int c = 0; c < N * N; ++c) {
+        if (!mask[c]) continue;
+        const int cy = c / N, cx = c % N;
+        if (cy == 0 || cx == 0) return RDXG_OK;                  // Nyquist terms: use the general path
+        if (!mask[(N - cy) * N + (N - cx)]) return RDXG_OK;      // not symmetric: general path
+        if (cy > N / 2 || (cy == N / 2 && cx >= N / 2)) h->hIdx.push_back(c);
+    }
+    h->nH = (int)h->hIdx.size();
+    h->hPos.resize(h->nH);
+    for (int k = 0; k < h->nH; ++k) {
+        const int c = h->hIdx[k];
+        h->hPos[k] = (((c / N) + N / 2) % N) * (N + 1) + ((c % N) + N / 2) % N;
+    }
+    h->nTilesH = (h->nH + kReduceThreads - 1) / kReduceThreads;
+    h->npt = 1;
+    if (EvalLauncher<float, 88>::smem(h->M, h->nH) > 227 * 1024) return RDXG_OK;   // does not fit
+    const char* env = getenv("RDXG_CHUNK");
+    h->chunk = env ? atoi(env) : 6;
+    if (h->chunk < 1 || h->chunk > kMaxChunk) h->chunk = 6;
+    h->objChunk0.assign(h->nObj, 0);
+    int c0 = 0;
+    for (int o = 0; o < h->nObj; ++o) {
+        h->objChunk0[o] = c0;
+        c0 += (h->objCount[o] + h->chunk - 1) / h->chunk;
+    }
+    h->chunksPerPatch = c0;
+    const size_t P = h->Pmax, G = P * h->I, PO = P * h->nObj;
+    int r;
+    void* v;
+    if ((r = upload(h, &v, h->hIdx))) return r;
+    h->dHIdx = (int32_t*)v;
+    if ((r = upload(h, &v, h->objChunk0))) return r;
+    h->dObjChunk0 = (int32_t*)v;
+    if ((r = upload(h, &v, h->hPos))) return r;
+    h->dHPos = (int32_t*)v;
+    if ((r = dalloc(h, &h->dDh, G * h->nH * sizeof(float2))) || (r = dalloc(h, &h->dOh, PO * h->nH * sizeof(float2))) ||
+        (r = dalloc(h, &h->dPart, P * h->chunksPerPatch * 4 * (size_t)h->nH * sizeof(float))) ||
+        (r = dalloc_t(h, &h->dObjMetric, PO * h->nTilesH)) || (r = dalloc_t(h, &h->dEval, P * h->chunksPerPatch)) ||
+        (r = dalloc_t(h, &h->dPoList, PO)) || (r = dalloc_t(h, &h->dAux, P * 2)) ||
+        (r = dalloc(h, &h->dPhiImg, G * (size_t)h->n * h->n * sizeof(float))))
+        return r;
+    cudaError_t e = cudaSuccess;
+    int occ = 0;
+    with_eval(N, [&](auto L) {
+        e = decltype(L)::setup(h->M, h->npt, h->nH);
+        occ = decltype(L)::occupancy(h->M, h->npt, h->nH);
+    });
+    if (e != cudaSuccess) { h->err = std::string("fused setup: ") + cudaGetErrorString(e); return RDXG_ERR_CUDA; }
+    if (occ < 1) occ = 1;
+    h->evalGrid = h->numSMs * occ;
+    h->reduceGrid = h->numSMs * 8;
+    h->phaseGrid = h->numSMs * 8;
+    h->fused = true;
+    return RDXG_OK;
+}
+
+// evaluation work lists built on the host for single evaluations of every patch
+int host_lists(rdxg_solver* h, int req, int mode) {
+    std::vector<EvalItem> ev;
+    std::vector<PoItem> po;
+    for (int p = 0; p < h->P; ++p) {
+        for (int o = 0; o < h->nObj; ++o) {
+            const int cnt = h->objCount[o];
+            const int nc = (cnt + h->chunk - 1) / h->chunk;
+            for (int c = 0; c < nc; ++c) {
+                EvalItem it;
+                it.p = p; it.o = o; it.first = h->objFirst[o] + c * h->chunk;
+                it.count = std::min(h->chunk, cnt - c * h->chunk);
+                it.chunk = h->objChunk0[o] + c; it.df = req == REQ_DF ? 1 : 0;
+                ev.push_back(it);
+            }
+            PoItem pi;
+            pi.p = p; pi.o = o; pi.mode = mode;
+            po.push_back(pi);
+        }
+    }
+    int32_t cnt[2] = {(int32_t)ev.size(), (int32_t)po.size()};
+    CK(h, cudaMemcpyAsync(h->dEval, ev.data(), ev.size() * sizeof(EvalItem), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->dPoList, po.data(), po.size() * sizeof(PoItem), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->dCounters, cnt, sizeof(cnt), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return RDXG_OK;
+}
+
+int fused_pass(rdxg_solver* h, int req, int mode) {
+    int r;
+    if ((r = host_lists(h, req, mode))) return r;
+    with_eval(h->N, [&](auto L) {
+        EvalParams<float> e = make_evalparams<float>(h);
+        decltype(L)::phase(e, h->phaseGrid, h->stream);
+        decltype(L)::eval(e, h->npt, h->evalGrid, h->stream);
+        decltype(L)::reduce(e, h->reduceGrid, h->stream);
+    });
+    CKL(h);
+    return RDXG_OK;
+}
+
+int metric_from_objects(rdxg_solver* h, double* metric) {
+    const size_t PO = (size_t)h->P * h->nObj;
+    std::vector<double> om(PO * h->nTilesH);
+    CK(h, cudaMemcpyAsync(om.data(), h->dObjMetric, om.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int p = 0; p < h->P; ++p) {
+        double sum = 0;
+        for (int o = 0; o < h->nObj; ++o) {
+            if (h->objWeight[o] == 0.0) continue;
+            double m = 0;
+            for (int t = 0; t < h->nTilesH; ++t) m += om[((size_t)p * h->nObj + o) * h->nTilesH + t];
+            sum += h->objWeight[o] * (m / ((double)h->ps * h->ps));
+        }
+        metric[p] = sum;
+    }
+    return RDXG_OK;
 }
 
 }  // namespace
@@ -461,6 +644,16 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
         with_size(h->N, h->fp64, [&](auto L, auto) { se = decltype(L)::setup(h->M); });
         if (se != cudaSuccess) { h->err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(se); r = RDXG_ERR_CUDA; }
     }
+    h->dObjFirstC = h->dObjFirst;
+    h->dObjCountC = h->dObjCount;
+    if (!r) {
+        cudaError_t de = cudaDeviceGetAttribute(&h->numSMs, cudaDevAttrMultiProcessorCount, g->device);
+        if (de != cudaSuccess) { h->err = cudaGetErrorString(de); r = RDXG_ERR_CUDA; }
+        h->adjGrid = h->numSMs * 8;
+        h->fdGrid = h->numSMs * 8;
+    }
+    const char* nf = getenv("RDXG_NO_FUSED");
+    if (!r && !(nf && atoi(nf))) r = setup_fused(h, s);
     *out = h;
     return r;
 }
@@ -500,6 +693,12 @@ int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric) {
     int r = h->fp64 ? upload_alpha<double>(h, alpha) : upload_alpha<float>(h, alpha);
     if (r) return r;
     if ((r = set_requests(h, REQ_F, GM_VOGEL, h->M))) return r;
+    if (h->fused) {
+        // a first pass sets the reference object to this point, the second evaluates
+        if ((r = fused_pass(h, REQ_F, 2))) return r;
+        if ((r = fused_pass(h, REQ_F, 0))) return r;
+        return metric_from_objects(h, metric);
+    }
     with_size(h->N, h->fp64, [&](auto L, auto t) {
         using T = decltype(t);
         KParams<T> kp = make_kparams<T>(h);
@@ -508,6 +707,18 @@ int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric) {
     });
     CKL(h);
     return metric_from_partials(h, metric);
+}
+
+int rdxg_metric_with_reference(rdxg_solver* h, const double* alpha_ref, const double* alpha, double* metric) {
+    if (!h || !alpha_ref || !alpha || !metric) return RDXG_ERR_ARG;
+    if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
+    if (!h->fused) return rdxg_metric(h, alpha, metric);
+    int r;
+    if ((r = upload_alpha<float>(h, alpha_ref)) || (r = set_requests(h, REQ_F, GM_VOGEL, h->M)) ||
+        (r = fused_pass(h, REQ_F, 2)))
+        return r;
+    if ((r = upload_alpha<float>(h, alpha)) || (r = fused_pass(h, REQ_F, 0))) return r;
+    return metric_from_objects(h, metric);
 }
 
 int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, int32_t method, double* grad,
@@ -519,13 +730,18 @@ int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, i
     if (r) return r;
     const int gm = method == RDXG_GRAD_FD ? GM_FD : GM_VOGEL;
     if ((r = set_requests(h, REQ_DF, gm, h->M))) return r;
+    if (h->fused) {
+        if ((r = fused_pass(h, REQ_DF, 1))) return r;
+    }
     with_size(h->N, h->fp64, [&](auto L, auto t) {
         using T = decltype(t);
         KParams<T> kp = make_kparams<T>(h);
-        decltype(L)::forward(kp, h->P * h->I, h->stream);
-        launch_accum<T>(kp, h->P * h->nObj, h->stream);
-        if (method == RDXG_GRAD_FD) decltype(L)::fd(kp, h->P * h->I, h->M, h->stream);
-        else decltype(L)::adjoint(kp, h->P * h->I, method == RDXG_GRAD_EXACT ? GK_EXACT : GK_VOGEL, h->stream);
+        if (!h->fused) {
+            decltype(L)::forward(kp, h->P * h->I, h->stream);
+            launch_accum<T>(kp, h->P * h->nObj, h->stream);
+        }
+        if (method == RDXG_GRAD_FD) decltype(L)::fd(kp, h->fdGrid, h->M, h->stream);
+        else decltype(L)::adjoint(kp, h->adjGrid, method == RDXG_GRAD_EXACT ? GK_EXACT : GK_VOGEL, h->stream);
     });
     CKL(h);
     const size_t G = (size_t)h->P * h->I;
@@ -535,7 +751,14 @@ int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, i
         for (size_t g = 0; g < G; ++g)
             for (int m = 0; m < h->M; ++m)
                 if (!enabled[m]) grad[g * h->M + m] = 0.0;
-    if (metric) return metric_from_partials(h, metric);
+    if (metric) {
+        if (h->fused) {
+            // the gradient pass left the exact object of this point as the reference
+            if ((r = set_requests(h, REQ_F, GM_VOGEL, h->M)) || (r = fused_pass(h, REQ_F, 0))) return r;
+            return metric_from_objects(h, metric);
+        }
+        return metric_from_partials(h, metric);
+    }
     return RDXG_OK;
 }
 
@@ -562,17 +785,22 @@ int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
     CK(h, cudaMemsetAsync(h->dVec, 0, (size_t)P * 5 * h->nFree * sizeof(double), h->stream));
     CK(h, cudaMemsetAsync(h->dAlphaOff, 0, (size_t)P * h->nPar * sizeof(double), h->stream));
     CK(h, cudaMemsetAsync(h->dAlpha, 0, (size_t)P * h->nPar * sizeof(double), h->stream));
+    if (h->fused) {
+        CK(h, cudaMemsetAsync(h->dOh, 0, (size_t)P * h->nObj * h->nH * sizeof(float2), h->stream));
+        CK(h, cudaMemsetAsync(h->dAux, 0, (size_t)P * 2 * sizeof(int32_t), h->stream));
+    }
     const int check = s->check_every > 0 ? s->check_every : 8;
     ShiftArgs sa{};
     sa.P = P; sa.I = h->I; sa.M = h->M; sa.nObj = h->nObj; sa.ps = h->ps; sa.cs = h->cs; sa.margin = h->margin;
     sa.tiltX = h->haveJ ? h->geo.tilt_x : -1; sa.tiltY = h->haveJ ? h->geo.tilt_y : -1;
     sa.req = h->dReq; sa.alpha = h->dAlpha; sa.tiltOff = h->dCurTilt; sa.shift = h->dShift;
-    sa.reinit = h->dReinit; sa.imgObj = h->dImgObj;
+    sa.reinit = h->dReinit; sa.imgObj = h->dImgObj; sa.aux = h->fused ? h->dAux : nullptr;
     std::memcpy(sa.J, h->J, sizeof(sa.J));
     std::memcpy(sa.Jinv, h->Jinv, sizeof(sa.Jinv));
     const int G = P * h->I;
     for (long round = 0;; ++round) {
         CK(h, cudaMemsetAsync(h->dActive, 0, sizeof(int32_t), h->stream));
+        CK(h, cudaMemsetAsync(h->dCounters, 0, 4 * sizeof(int32_t), h->stream));
         with_size(h->N, h->fp64, [&](auto L, auto t) {
             using T = decltype(t);
             KParams<T> kp = make_kparams<T>(h);
@@ -580,14 +808,21 @@ int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
             launch_cg<T>(ca, P, h->stream);
             launch_shift(sa, P, h->stream);
             decltype(L)::prep(kp, 0, G, h->stream);
-            decltype(L)::forward(kp, G, h->stream);
-            launch_accum<T>(kp, P * h->nObj, h->stream);
-            decltype(L)::adjoint(kp, G, GK_VOGEL, h->stream);
-            // all patches reach their first gradient together (round 2 of the first stage);
-            // later gradients use the analytic method
-            if (prm.fd_first && round == 2) { decltype(L)::fd(kp, G, h->M, h->stream); h->launches++; }
+            if (h->fused) {
+                with_eval(h->N, [&](auto E) {
+                    EvalParams<float> e = make_evalparams<float>(h);
+                    decltype(E)::phase(e, h->phaseGrid, h->stream);
+                    decltype(E)::eval(e, h->npt, h->evalGrid, h->stream);
+                    decltype(E)::reduce(e, h->reduceGrid, h->stream);
+                });
+            } else {
+                decltype(L)::forward(kp, G, h->stream);
+                launch_accum<T>(kp, P * h->nObj, h->stream);
+            }
+            decltype(L)::adjoint(kp, h->adjGrid, GK_VOGEL, h->stream);
+            decltype(L)::fd(kp, h->fdGrid, h->M, h->stream);
         });
-        h->launches += 6;
+        h->launches += h->fused ? 8 : 7;
         CKL(h);
         if ((round + 1) % check == 0) {
             CK(h, cudaMemcpyAsync(h->hActive, h->dActive, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
@@ -646,20 +881,34 @@ int rdxg_profile_kernels(rdxg_solver* h, int32_t reps, double* ms) {
         const int req = (k < 2) ? REQ_F : REQ_DF;
         const int gm = (k == 4) ? GM_FD : GM_VOGEL;
         if ((r = set_requests(h, req, gm, h->M))) break;
+        if (h->fused && (r = host_lists(h, req, req == REQ_DF ? 1 : 0))) break;
         auto launch = [&](int which) {
             with_size(h->N, h->fp64, [&](auto L, auto t) {
                 using T = decltype(t);
                 KParams<T> kp = make_kparams<T>(h);
+                if (h->fused && which <= 2) {
+                    with_eval(h->N, [&](auto E) {
+                        EvalParams<float> e = make_evalparams<float>(h);
+                        if (which == 1) {
+                            decltype(E)::reduce(e, h->reduceGrid, h->stream);
+                        } else {
+                            decltype(E)::phase(e, h->phaseGrid, h->stream);
+                            decltype(E)::eval(e, h->npt, h->evalGrid, h->stream);
+                        }
+                    });
+                    return;
+                }
                 switch (which) {
                     case 0: case 2: decltype(L)::forward(kp, G, h->stream); break;
                     case 1: launch_accum<T>(kp, PO, h->stream); break;
-                    case 3: decltype(L)::adjoint(kp, G, GK_VOGEL, h->stream); break;
-                    case 4: decltype(L)::fd(kp, G, h->M, h->stream); break;
+                    case 3: decltype(L)::adjoint(kp, h->adjGrid, GK_VOGEL, h->stream); break;
+                    case 4: decltype(L)::fd(kp, h->fdGrid, h->M, h->stream); break;
                 }
             });
         };
         // inputs of the timed kernel: forward and accumulation in the requested mode
         if (k >= 3) { launch(2); launch(1); }
+        if (k == 1) launch(0);
         launch(k);   // warm-up
         CK(h, cudaEventRecord(e0, h->stream));
         for (int i = 0; i < reps; ++i) launch(k);

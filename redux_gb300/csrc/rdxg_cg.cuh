@@ -8,6 +8,7 @@
 #pragma once
 
 #include "cg_machine.h"
+#include "rdxg_eval.cuh"
 #include "rdxg_kernels.cuh"
 
 namespace rdxg {
@@ -76,6 +77,16 @@ struct CgArgs {
     int32_t* gmethod;
     int32_t* modeCount;
     int32_t* active;
+    // fused evaluation path (FP32): object metrics, work lists, reference-object state
+    int32_t fused;
+    const double* objMetric;       // [P][nObj][nTilesH] per-tile partial sums
+    int32_t nTilesH;
+    Lists L;
+    int32_t chunkSize, chunksPerPatch;
+    const int32_t* objChunk0;      // [nObj]
+    const int32_t* objFirst;       // [nObj]
+    const int32_t* objCount;       // [nObj]
+    int32_t* aux;                  // [P][2]: reference object valid, refresh pending
 };
 
 // alpha = offset + N x1; alpha_eff = alpha + currentTiltOffset - residual for the tilt modes
@@ -99,6 +110,29 @@ __device__ void map_point(const CgArgs<T>& a, int p, const double* x1) {
     __syncthreads();
 }
 
+// append the chunks and objects of patch p to the evaluation work lists
+template <typename T>
+__device__ void enqueue_eval(const CgArgs<T>& a, int p, int rq, int mode) {
+    for (int o = 0; o < a.nObj; ++o) {
+        const int cnt = a.objCount[o];
+        const int nc = (cnt + a.chunkSize - 1) / a.chunkSize;
+        for (int c = 0; c < nc; ++c) {
+            EvalItem it;
+            it.p = p; it.o = o;
+            it.first = a.objFirst[o] + c * a.chunkSize;
+            it.count = min(a.chunkSize, cnt - c * a.chunkSize);
+            it.chunk = a.objChunk0[o] + c;
+            it.df = (rq == REQ_DF) ? 1 : 0;
+            const int k = atomicAdd(a.L.nEval, 1);
+            a.L.eval[k] = it;
+        }
+        PoItem pi;
+        pi.p = p; pi.o = o; pi.mode = mode;
+        const int k = atomicAdd(a.L.nPo, 1);
+        a.L.po[k] = pi;
+    }
+}
+
 template <typename T, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
     const int p = blockIdx.x;
@@ -116,6 +150,18 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
         return;
     }
     double f = 0;
+    if (a.fused && st.req == REQ_F && a.aux[2 * p + 1]) {
+        // the last evaluation only refreshed the reference object: repeat the request
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            a.aux[2 * p + 0] = 1;
+            a.aux[2 * p + 1] = 0;
+            a.req[p] = REQ_F;
+            atomicAdd(a.active, 1);
+            enqueue_eval(a, p, REQ_F, 0);
+        }
+        return;
+    }
     if (st.req == REQ_F) {
         if (threadIdx.x == 0) {
             double sum = 0;
@@ -123,8 +169,13 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
                 const double w = a.objWeight[o];
                 if (w == 0.0) continue;
                 double m = 0;
-                const double* pp = a.partial + ((size_t)p * a.nObj + o) * a.nTiles;
-                for (int t = 0; t < a.nTiles; ++t) m += pp[t];
+                if (a.fused) {
+                    const double* om = a.objMetric + ((size_t)p * a.nObj + o) * a.nTilesH;
+                    for (int t = 0; t < a.nTilesH; ++t) m += om[t];
+                } else {
+                    const double* pp = a.partial + ((size_t)p * a.nObj + o) * a.nTiles;
+                    for (int t = 0; t < a.nTiles; ++t) m += pp[t];
+                }
                 sum += w * (m / ((double)a.ps * a.ps));
             }
             fsh = sum;
@@ -156,6 +207,21 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
         a.gmethod[p] = st.grad_method;
         a.modeCount[p] = st.mode_count;
         if (rq != REQ_DONE) atomicAdd(a.active, 1);
+        if (rq == REQ_DF) {
+            if (st.grad_method == GM_FD) a.L.fdP[atomicAdd(a.L.nFdP, 1)] = p;
+            else a.L.gradP[atomicAdd(a.L.nGradP, 1)] = p;
+        }
+        if (a.fused && (rq == REQ_F || rq == REQ_DF)) {
+            int mode = 0;
+            if (rq == REQ_DF) {
+                mode = 1;
+                a.aux[2 * p + 0] = 1;     // the gradient pass leaves the exact object behind
+            } else if (!a.aux[2 * p + 0]) {
+                mode = 2;                 // refresh the reference object first
+                a.aux[2 * p + 1] = 1;
+            }
+            enqueue_eval(a, p, rq, mode);
+        }
     }
 }
 
@@ -169,6 +235,7 @@ struct ShiftArgs {
     int32_t* shift;          // [P][I][2]
     uint8_t* reinit;         // [P][I]
     const int32_t* imgObj;
+    int32_t* aux;            // [P][2] reference object valid flag (cleared on re-initialisation)
     double J[2][2], Jinv[2][2];
 };
 
@@ -210,8 +277,11 @@ __global__ void k_shift(ShiftArgs a) {
         }
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < a.I; j += blockDim.x)
-        a.reinit[(size_t)p * a.I + j] = objShifted[a.imgObj[j]] ? 1 : 0;
+    for (int j = threadIdx.x; j < a.I; j += blockDim.x) {
+        const int sh = objShifted[a.imgObj[j]];
+        a.reinit[(size_t)p * a.I + j] = sh ? 1 : 0;
+        if (sh && a.aux) a.aux[2 * p + 0] = 0;
+    }
 }
 
 }  // namespace rdxg

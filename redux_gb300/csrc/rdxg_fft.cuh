@@ -171,8 +171,18 @@ template <int N> struct Tile { static constexpr int LDS = N + 1; static constexp
 
 // One Stockham stage over LINES lines starting at line0.  Element e of line l is at
 // s[l * lstride + e * estride].
+// Thread index read through volatile asm: kernels that run several transforms inside a
+// loop pass it so that the compiler cannot hoist the per-stage index arithmetic out of the
+// loop (which keeps all of it live at once and spills).
+__device__ __forceinline__ int opaque_tid() {
+    int t;
+    asm volatile("mov.u32 %0, %%tid.x;" : "=r"(t));
+    return t;
+}
+
 template <typename T, int N, int R, int NS, int DIR, int LINES, int THREADS>
-__device__ __forceinline__ void fft_stage(cx<T>* s, int line0, int lstride, int estride, const cx<T>* tw) {
+__device__ __forceinline__ void fft_stage(cx<T>* s, int line0, int lstride, int estride, const cx<T>* tw,
+                                          int tid) {
     constexpr int BF = N / R;
     constexpr int TOTAL = LINES * BF;
     constexpr int ITER = (TOTAL + THREADS - 1) / THREADS;
@@ -180,7 +190,7 @@ __device__ __forceinline__ void fft_stage(cx<T>* s, int line0, int lstride, int 
     cx<T> v[ITER][R];
 #pragma unroll
     for (int it = 0; it < ITER; ++it) {
-        const int b = threadIdx.x + it * THREADS;
+        const int b = tid + it * THREADS;
         if (TOTAL % THREADS == 0 || b < TOTAL) {
             const int line = line0 + b % LINES;
             const int j = b / LINES;
@@ -202,7 +212,7 @@ __device__ __forceinline__ void fft_stage(cx<T>* s, int line0, int lstride, int 
     __syncthreads();
 #pragma unroll
     for (int it = 0; it < ITER; ++it) {
-        const int b = threadIdx.x + it * THREADS;
+        const int b = tid + it * THREADS;
         if (TOTAL % THREADS == 0 || b < TOTAL) {
             const int line = line0 + b % LINES;
             const int j = b / LINES;
@@ -218,33 +228,107 @@ __device__ __forceinline__ void fft_stage(cx<T>* s, int line0, int lstride, int 
 
 // 1-D transforms of LINES lines (rows when ROWS, else columns).
 template <typename T, int N, int DIR, int LINES, bool ROWS, int THREADS>
-__device__ __forceinline__ void fft_lines(cx<T>* s, int line0, const cx<T>* tw) {
+__device__ __forceinline__ void fft_lines(cx<T>* s, int line0, const cx<T>* tw, int tid) {
     constexpr int LDS = Tile<N>::LDS;
     constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
     constexpr int ls = ROWS ? LDS : 1;
     constexpr int es = ROWS ? 1 : LDS;
-    fft_stage<T, N, R1, 1, DIR, LINES, THREADS>(s, line0, ls, es, tw);
-    fft_stage<T, N, R2, R1, DIR, LINES, THREADS>(s, line0, ls, es, tw);
+    fft_stage<T, N, R1, 1, DIR, LINES, THREADS>(s, line0, ls, es, tw, tid);
+    fft_stage<T, N, R2, R1, DIR, LINES, THREADS>(s, line0, ls, es, tw, tid);
 }
 
 // Full 2-D transform.  IN_ROWS_PRUNED: only rows [N/4, 3N/4) of the input are non-zero
 // (an n x n pupil embedded at offset n/2), so only those rows are transformed first.
 template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED>
-__device__ __forceinline__ void fft2d(cx<T>* s, const cx<T>* tw) {
+__device__ __forceinline__ void fft2d(cx<T>* s, const cx<T>* tw, int tid) {
     if (IN_ROWS_PRUNED) {
-        fft_lines<T, N, DIR, N / 2, true, THREADS>(s, N / 4, tw);
+        fft_lines<T, N, DIR, N / 2, true, THREADS>(s, N / 4, tw, tid);
     } else {
-        fft_lines<T, N, DIR, N, true, THREADS>(s, 0, tw);
+        fft_lines<T, N, DIR, N, true, THREADS>(s, 0, tw, tid);
     }
-    fft_lines<T, N, DIR, N, false, THREADS>(s, 0, tw);
+    fft_lines<T, N, DIR, N, false, THREADS>(s, 0, tw, tid);
+}
+template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED>
+__device__ __forceinline__ void fft2d(cx<T>* s, const cx<T>* tw) {
+    fft2d<T, N, DIR, THREADS, IN_ROWS_PRUNED>(s, tw, (int)threadIdx.x);
+}
+
+// ---- ping-pong variant: out-of-place stages between two tiles (a -> b -> a), one barrier
+// per stage and one butterfly in registers at a time ----
+template <typename T, int N, int R, int NS, int DIR, int LINES, int THREADS>
+__device__ __forceinline__ void fft_stage_pp(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst, int line0,
+                                             int lstride, int estride, const cx<T>* tw) {
+    constexpr int BF = N / R;
+    constexpr int TOTAL = LINES * BF;
+    constexpr int TWS = N / (NS * R);
+#pragma unroll 2
+    for (int b = threadIdx.x; b < TOTAL; b += THREADS) {
+        const int line = line0 + b % LINES;
+        const int j = b / LINES;
+        const int k = j % NS;
+        const cx<T>* in = src + line * lstride;
+        cx<T> v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = in[(j + r * BF) * estride];
+        if (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                cx<T> w = tw[r * k * TWS];
+                if (DIR > 0) w.y = -w.y;
+                v[r] = cmul<T>(v[r], w);
+            }
+        }
+        Dft<R, DIR, T>::run(v);
+        const int idxD = (j / NS) * NS * R + k;
+        cx<T>* out = dst + line * lstride;
+#pragma unroll
+        for (int r = 0; r < R; ++r) out[(idxD + r * NS) * estride] = v[r];
+    }
+    __syncthreads();
+}
+
+// 2-D transform in tile a (result in a), b is scratch of the same shape.
+template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED>
+__device__ __forceinline__ void fft2d_pp(cx<T>* a, cx<T>* b, const cx<T>* tw) {
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
+    constexpr int RL = IN_ROWS_PRUNED ? N / 2 : N;
+    constexpr int r0 = IN_ROWS_PRUNED ? N / 4 : 0;
+    fft_stage_pp<T, N, R1, 1, DIR, RL, THREADS>(a, b, r0, LDS, 1, tw);
+    fft_stage_pp<T, N, R2, R1, DIR, RL, THREADS>(b, a, r0, LDS, 1, tw);
+    fft_stage_pp<T, N, R1, 1, DIR, N, THREADS>(a, b, 0, 1, LDS, tw);
+    fft_stage_pp<T, N, R2, R1, DIR, N, THREADS>(b, a, 0, 1, LDS, tw);
+}
+
+// ping-pong transform whose output is only needed on rows [N/4, 3N/4): columns first
+template <typename T, int N, int DIR, int THREADS>
+__device__ __forceinline__ void fft2d_pp_out_rows_pruned(cx<T>* a, cx<T>* b, const cx<T>* tw) {
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
+    fft_stage_pp<T, N, R1, 1, DIR, N, THREADS>(a, b, 0, 1, LDS, tw);
+    fft_stage_pp<T, N, R2, R1, DIR, N, THREADS>(b, a, 0, 1, LDS, tw);
+    fft_stage_pp<T, N, R1, 1, DIR, N / 2, THREADS>(a, b, N / 4, LDS, 1, tw);
+    fft_stage_pp<T, N, R2, R1, DIR, N / 2, THREADS>(b, a, N / 4, LDS, 1, tw);
+}
+
+// Two tiles of FP32 fit in shared memory up to N = 88: kernels that loop over work items
+// use the ping-pong transforms there (no register staging, nothing to hoist out of loops).
+template <typename T, int N> struct PingPong {
+    static constexpr bool value = sizeof(T) == 4 && N <= 88;
+};
+
+template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED>
+__device__ __forceinline__ void fft2d_any(cx<T>* a, cx<T>* b, const cx<T>* tw) {
+    if constexpr (PingPong<T, N>::value) fft2d_pp<T, N, DIR, THREADS, IN_ROWS_PRUNED>(a, b, tw);
+    else fft2d<T, N, DIR, THREADS, IN_ROWS_PRUNED>(a, tw);
 }
 
 // 2-D transform whose output is only needed on rows [N/4, 3N/4): columns first, then the
 // needed rows.
 template <typename T, int N, int DIR, int THREADS>
 __device__ __forceinline__ void fft2d_out_rows_pruned(cx<T>* s, const cx<T>* tw) {
-    fft_lines<T, N, DIR, N, false, THREADS>(s, 0, tw);
-    fft_lines<T, N, DIR, N / 2, true, THREADS>(s, N / 4, tw);
+    fft_lines<T, N, DIR, N, false, THREADS>(s, 0, tw, (int)threadIdx.x);
+    fft_lines<T, N, DIR, N / 2, true, THREADS>(s, N / 4, tw, (int)threadIdx.x);
 }
 
 }  // namespace rdxg

@@ -15,8 +15,14 @@ static size_t extra_smem(int M) {
 }
 
 template <typename T, int N>
+static size_t smem_pp(int M) {
+    return (size_t)(PingPong<T, N>::value ? Tile<N>::ELEMS : 0) * sizeof(cx<T>) +
+           (size_t)(Tile<N>::ELEMS + N) * sizeof(cx<T>) + extra_smem<T, N>(M);
+}
+
+template <typename T, int N>
 cudaError_t Launcher<T, N>::setup(int M) {
-    const int sm = (int)(smem_base() + extra_smem<T, N>(M));
+    const int sm = (int)smem_pp<T, N>(M);
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_prep<T, N, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
     if ((e = cudaFuncSetAttribute(k_forward<T, N, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
@@ -38,16 +44,72 @@ void Launcher<T, N>::forward(const KParams<T>& kp, int nImg, cudaStream_t st) {
 }
 
 template <typename T, int N>
-void Launcher<T, N>::adjoint(const KParams<T>& kp, int nImg, int kind, cudaStream_t st) {
+void Launcher<T, N>::adjoint(const KParams<T>& kp, int grid, int kind, cudaStream_t st) {
+    (void)grid;
     const size_t sm = smem_base() + extra_smem<T, N>(kp.M);
-    k_adjoint<T, N, THREADS><<<nImg, THREADS, sm, st>>>(kp, kind);
+    grid = kp.P * kp.I;
+    k_adjoint<T, N, THREADS><<<grid, THREADS, sm, st>>>(kp, kind);
 }
 
 template <typename T, int N>
-void Launcher<T, N>::fd(const KParams<T>& kp, int nImg, int M, cudaStream_t st) {
-    const size_t sm = smem_base() + extra_smem<T, N>(kp.M);
-    dim3 grid(nImg, M);
+void Launcher<T, N>::fd(const KParams<T>& kp, int grid, int M, cudaStream_t st) {
+    const size_t sm = smem_pp<T, N>(kp.M);
+    if (!PingPong<T, N>::value) grid = kp.P * kp.I * M;
     k_fd<T, N, THREADS><<<grid, THREADS, sm, st>>>(kp);
+}
+
+template <typename T, int N>
+size_t EvalLauncher<T, N>::smem(int M, int nH) {
+    return (size_t)(2 * Tile<N>::ELEMS + N + nH) * sizeof(cx<T>) + (size_t)4 * nH * sizeof(T) +
+           (size_t)nH * sizeof(int) + (size_t)M * sizeof(T) + 16;
+}
+
+#define RDXG_NPT_SWITCH(npt, CALL) \
+    do {                             \
+        (void)(npt);                 \
+        CALL(1);                     \
+    } while (0)
+
+template <typename T, int N>
+cudaError_t EvalLauncher<T, N>::setup(int M, int npt, int nH) {
+    cudaError_t e = cudaSuccess;
+    const int sm = (int)smem(M, nH);
+#define RDXG_SET(NPT) e = cudaFuncSetAttribute(k_eval<T, N, kEvalThreads, NPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm)
+    RDXG_NPT_SWITCH(npt, RDXG_SET);
+#undef RDXG_SET
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_phase<T, N, kPhasePix, kMaxChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)((size_t)M * (kPhasePix + kMaxChunk) * sizeof(T)));
+    return e;
+}
+
+template <typename T, int N>
+int EvalLauncher<T, N>::occupancy(int M, int npt, int nH) {
+    int b = 0;
+    const size_t sm = smem(M, nH);
+#define RDXG_OCC(NPT) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_eval<T, N, kEvalThreads, NPT>, kEvalThreads, sm)
+    RDXG_NPT_SWITCH(npt, RDXG_OCC);
+#undef RDXG_OCC
+    return b;
+}
+
+template <typename T, int N>
+void EvalLauncher<T, N>::eval(const EvalParams<T>& e, int npt, int grid, cudaStream_t st) {
+    const size_t sm = smem(e.k.M, e.hp.nH);
+#define RDXG_LAUNCH(NPT) k_eval<T, N, kEvalThreads, NPT><<<grid, kEvalThreads, sm, st>>>(e)
+    RDXG_NPT_SWITCH(npt, RDXG_LAUNCH);
+#undef RDXG_LAUNCH
+}
+
+template <typename T, int N>
+void EvalLauncher<T, N>::phase(const EvalParams<T>& e, int grid, cudaStream_t st) {
+    const size_t sm = (size_t)e.k.M * (kPhasePix + kMaxChunk) * sizeof(T);
+    k_phase<T, N, kPhasePix, kMaxChunk><<<grid, kPhasePix, sm, st>>>(e);
+}
+
+template <typename T, int N>
+void EvalLauncher<T, N>::reduce(const EvalParams<T>& e, int grid, cudaStream_t st) {
+    k_reduce<T, N, kReduceThreads><<<grid, kReduceThreads, 0, st>>>(e);
 }
 
 }  // namespace rdxg

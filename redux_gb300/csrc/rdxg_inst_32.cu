@@ -4,4 +4,5 @@
 namespace rdxg {
 template struct Launcher<float, 32>;
 template struct Launcher<double, 32>;
+template struct EvalLauncher<float, 32>;
 }  // namespace rdxg

@@ -4,4 +4,5 @@
 namespace rdxg {
 template struct Launcher<float, 64>;
 template struct Launcher<double, 64>;
+template struct EvalLauncher<float, 64>;
 }  // namespace rdxg

@@ -4,4 +4,5 @@
 namespace rdxg {
 template struct Launcher<float, 88>;
 template struct Launcher<double, 88>;
+template struct EvalLauncher<float, 88>;
 }  // namespace rdxg

