@@ -455,7 +455,8 @@ int setup_fused(rdxg_solver* h, const rdxg_static* s) {
         const int cy = c / N, cx = c % N;
         if (cy == 0 || cx == 0) return RDXG_OK;                  // Nyquist terms: use the general path
         if (!mask[(N - cy) * N + (N - cx)]) return RDXG_OK;      // not symmetric: general path
-        if (cy > N / 2 || (cy == N / 2 && cx >= N / 2)) h->hIdx.push_back(c);
+        // half plane along x: its points sit in the un-centred columns [0, N/2)
+        if (cx > N / 2 || (cx == N / 2 && cy >= N / 2)) h->hIdx.push_back(c);
     }
     h->nH = (int)h->hIdx.size();
     h->hPos.resize(h->nH);
@@ -465,7 +466,11 @@ int setup_fused(rdxg_solver* h, const rdxg_static* s) {
     }
     h->nTilesH = (h->nH + kReduceThreads - 1) / kReduceThreads;
     h->npt = 1;
-    if (EvalLauncher<float, 88>::smem(h->M, h->nH) > 227 * 1024) return RDXG_OK;   // does not fit
+    if (h->nH > N * (N / 2 + 1)) return RDXG_OK;   // more points than the staging area holds
+    const size_t smem = N == 32 ? EvalLauncher<float, 32>::smem(h->M, h->nH)
+                      : N == 64 ? EvalLauncher<float, 64>::smem(h->M, h->nH)
+                                : EvalLauncher<float, 88>::smem(h->M, h->nH);
+    if (smem > 227 * 1024) return RDXG_OK;   // does not fit
     const char* env = getenv("RDXG_CHUNK");
     h->chunk = env ? atoi(env) : 6;
     if (h->chunk < 1 || h->chunk > kMaxChunk) h->chunk = 6;

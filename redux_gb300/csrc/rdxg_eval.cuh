@@ -12,7 +12,7 @@
 // and it is free of cancellation when O' is close to conj(P)/Q.  O' is refreshed from every
 // gradient evaluation (O = O' + (conj(P') - gamma O') / Q, exact) and by one extra pass
 // after image re-initialisation.  D, S and O' are Hermitian (real images and PSFs), so only
-// the half of the OTF support with (cy > N/2) or (cy == N/2 and cx >= N/2) is accumulated,
+// the half of the OTF support with (cx > N/2) or (cx == N/2 and cy >= N/2) is accumulated,
 // the other half counting through a weight of 2 (1 for the DC term).
 // The OTF is written to HBM only for gradient evaluations, which need it again.
 // Measured against the FP64 oracle with O' taken at the last gradient point and steps along
@@ -106,51 +106,130 @@ __global__ void __launch_bounds__(PIX) k_phase(EvalParams<T> e) {
     }
 }
 
-// One image of a chunk: forward model in the shared tile (transforms ping-pong between s
-// and s2), then the accumulation.
+// Asynchronous 8-byte global -> shared copies (cp.async): the phases of the next image and
+// the transforms of the current one are fetched into parts of the two tiles that the
+// transforms leave unused at that time, so no thread waits on global memory.
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Staging places (W = N/2 + 1 slots per tile row, columns [N/2, N] of a row are never used
+// by the half-plane inverse transform):
+//   phases of the next image: tile b, rows [3N/4, N), columns [N/2, N]: free from the end of
+//     the forward transform until the next image's column pass;
+//   image transforms Dh: tile a, columns [N/2, N]; rows [N/2, N) are free once |X|^2 has been
+//     read, rows [0, N/2) once the packed inverse along x is done.
+template <int N> struct Stage {
+    static constexpr int LDS = N + 1, W = N / 2 + 1;
+    static __device__ __forceinline__ int phi_slot(int pair) {
+        return (3 * N / 4 + pair / W) * LDS + N / 2 + pair % W;
+    }
+    static __device__ __forceinline__ int dh_slot(int h) {
+        return ((N / 2 + h / W) % N) * LDS + N / 2 + h % W;
+    }
+    static constexpr int kMaxPhiPairs = (N / 4) * W;
+    static constexpr int kMaxH = N * W;
+    static constexpr int kFirstPart = (N / 2) * W;    // Dh points staged into rows [N/2, N)
+};
+
 template <typename T, int N, int THREADS>
-__device__ __forceinline__ void eval_image(const T* __restrict__ phi_g, const T* __restrict__ A, T c, int df,
+__device__ __forceinline__ void stage_phi(cx<T>* b, const T* __restrict__ phi_g) {
+    constexpr int pairs = (N / 2) * (N / 2) / 2;
+    static_assert(pairs <= Stage<N>::kMaxPhiPairs, "phase staging area too small");
+    for (int p = threadIdx.x; p < pairs; p += THREADS) cp_async8(b + Stage<N>::phi_slot(p), phi_g + 2 * p);
+}
+
+// One image of a chunk.  Forward: the pupil function (rows and columns [N/4, 3N/4) of tile
+// a, nothing else is read) is transformed with the first stage of each pass loading only
+// the middle half of its inputs.  |X|^2 is real: rows 2m and 2m+1 are packed as the real
+// and imaginary parts of row m of tile b, the N/2 packed rows are inverse-transformed and
+// split again (A = (Z(k) + conj Z(-k))/2, B = (Z(k) - conj Z(-k))/2i), and only the columns
+// [0, N/2) that hold the half-plane points are transformed along y.
+// On entry the phases of this image are staged in b; phiNext (or null) is the next image's.
+template <typename T, int N, int THREADS>
+__device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, const T* A, T c, int df,
                                            cx<T>* PF, cx<T>* X, cx<T>* S, const cx<T>* __restrict__ Dg,
-                                           cx<T>* s, cx<T>* s2, const cx<T>* tw, const cx<T>* oh,
-                                           T* acc, const int* hpos, int nH) {
+                                           cx<T>* a, cx<T>* b, const cx<T>* tw, const cx<T>* oh,
+                                           T* acc, const int* hpos, const int* hidx, int nH) {
     constexpr int LDS = Tile<N>::LDS;
-    constexpr int n = N / 2, n2 = n * n, N2 = N * N;
+    constexpr int n = N / 2, n2 = n * n, N2 = N * N, H2 = N / 2;
+    constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
+    constexpr int LO = R1 / 4, HI = 3 * R1 / 4;      // non-zero inputs of the pruned first stage
+    static_assert(R1 % 4 == 0, "the pruned first stage needs a radix divisible by 4");
+    static_assert(sizeof(cx<T>) == 8, "staging copies 8-byte elements");
+    using St = Stage<N>;
     const T inv = (T)1 / (T)N2;
-    __syncthreads();    // previous image's tile fully consumed
-    zero_tile<T, N>(s);
-    __syncthreads();
+    __syncthreads();    // previous image's tiles fully consumed, staged phases visible
     for (int q = threadIdx.x; q < n2; q += THREADS) {
-        const T a = A[q];
+        const T amp = A[q];
         cx<T> pf = mkc<T>(0, 0);
-        if (a > (T)0) {
+        if (amp > (T)0) {
+            const T* ph = reinterpret_cast<const T*>(b + St::phi_slot(q >> 1));
             T sn, cs;
-            sincos_t<T>(phi_g[q], &sn, &cs);
-            pf = mkc<T>(a * cs, a * sn);
+            sincos_t<T>(ph[q & 1], &sn, &cs);
+            pf = mkc<T>(amp * cs, amp * sn);
         }
         if (df) PF[q] = pf;
         const int y = q / n, x = q % n;
-        s[(y + n / 2) * LDS + x + n / 2] = cscale<T>(pf, c);
+        a[(y + n / 2) * LDS + x + n / 2] = cscale<T>(pf, c);
     }
     __syncthreads();
-    fft2d_pp<T, N, -1, THREADS, true>(s, s2, tw);
-    for (int i = threadIdx.x; i < N2; i += THREADS) {
-        const int y = i / N, x = i % N;
-        const cx<T> v = s[y * LDS + x];
-        if (df) X[i] = v;
-        s[y * LDS + x] = mkc<T>(cnorm<T>(v), 0);
+    // forward: rows [N/4, 3N/4) (a -> b -> a), then all columns (a -> b -> a)
+    fft_stage_pp<T, N, R1, 1, -1, N / 2, THREADS, LO, HI>(a, b, N / 4, LDS, 1, tw);
+    fft_stage_pp<T, N, R2, R1, -1, N / 2, THREADS>(b, a, N / 4, LDS, 1, tw);
+    fft_stage_pp<T, N, R1, 1, -1, N, THREADS, LO, HI>(a, b, 0, 1, LDS, tw);
+    fft_stage_pp<T, N, R2, R1, -1, N, THREADS>(b, a, 0, 1, LDS, tw);
+    // |X|^2 of rows 2m, 2m+1 packed into row m of b
+    for (int i = threadIdx.x; i < H2 * N; i += THREADS) {
+        const int m = i / N, x = i % N;
+        const cx<T> v0 = a[(2 * m) * LDS + x];
+        const cx<T> v1 = a[(2 * m + 1) * LDS + x];
+        if (df) {
+            X[(2 * m) * N + x] = v0;
+            X[(2 * m + 1) * N + x] = v1;
+        }
+        b[m * LDS + x] = mkc<T>(cnorm<T>(v0), cnorm<T>(v1));
     }
     __syncthreads();
-    fft2d_pp<T, N, +1, THREADS, false>(s, s2, tw);
+    const int nFirst = nH < St::kFirstPart ? nH : St::kFirstPart;
+    for (int h = threadIdx.x; h < nFirst; h += THREADS) cp_async8(a + St::dh_slot(h), Dg + h);
+    if (phiNext) stage_phi<T, N, THREADS>(b, phiNext);
+    cp_async_commit();
+    // inverse along x on the N/2 packed rows (b -> a -> b)
+    fft_stage_pp<T, N, R1, 1, +1, N / 2, THREADS>(b, a, 0, LDS, 1, tw);
+    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS>(a, b, 0, LDS, 1, tw);
+    for (int h = nFirst + threadIdx.x; h < nH; h += THREADS) cp_async8(a + St::dh_slot(h), Dg + h);
+    cp_async_commit();
+    // split the packed rows: columns [0, N/2) of rows 2m and 2m+1 into a
+    for (int i = threadIdx.x; i < H2 * H2; i += THREADS) {
+        const int m = i / H2, k = i % H2;
+        const cx<T> z = b[m * LDS + k];
+        const cx<T> zc = b[m * LDS + ((N - k) % N)];
+        // A = (z + conj zc)/2 ; B = (z - conj zc)/(2i)
+        a[(2 * m) * LDS + k] = mkc<T>((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y - zc.y));
+        a[(2 * m + 1) * LDS + k] = mkc<T>((T)0.5 * (z.y + zc.y), (T)0.5 * (zc.x - z.x));
+    }
+    __syncthreads();
+    // inverse along y on columns [0, N/2) (a -> b -> a)
+    fft_stage_pp<T, N, R1, 1, +1, N / 2, THREADS>(a, b, 0, 1, LDS, tw);
+    cp_async_wait_all();
+    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS>(b, a, 0, 1, LDS, tw);
     if (df) {
-        for (int i = threadIdx.x; i < N2; i += THREADS) {
-            const int cy = i / N, cxx = i % N;
-            const int y = (cy + N / 2) % N, x = (cxx + N / 2) % N;
-            S[i] = cscale<T>(s[y * LDS + x], inv);
+        // the full OTF from the half plane (S(-u) = conj S(u)) for the gradient kernels
+        for (int h = threadIdx.x; h < nH; h += THREADS) {
+            const cx<T> v = cscale<T>(a[hpos[h]], inv);
+            const int cidx = hidx[h];
+            const int cy = cidx / N, cxx = cidx % N;
+            S[cidx] = v;
+            S[((N - cy) % N) * N + (N - cxx) % N] = mkc<T>(v.x, -v.y);
         }
     }
     for (int h = threadIdx.x; h < nH; h += THREADS) {
-        const cx<T> sv = cscale<T>(s[hpos[h]], inv);
-        const cx<T> r = csub<T>(Dg[h], cmul<T>(oh[h], sv));
+        const cx<T> sv = cscale<T>(a[hpos[h]], inv);
+        const cx<T> r = csub<T>(a[St::dh_slot(h)], cmul<T>(oh[h], sv));
         // R += |r|^2, Q += |S|^2, P' += conj(r) S
         acc[h] += cnorm<T>(r);
         acc[nH + h] += cnorm<T>(sv);
@@ -166,32 +245,55 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nH = e.hp.nH;
     // shared memory: two tiles | twiddles | reference object | accumulators (4 x nH) |
-    //                tile positions
+    //                tile positions | pupil amplitude
     cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* s2 = s + Tile<N>::ELEMS;
     cx<T>* tw = s2 + Tile<N>::ELEMS;
     cx<T>* oh = tw + N;
     T* acc = reinterpret_cast<T*>(oh + nH);
     int* hpos = reinterpret_cast<int*>(acc + 4 * nH);
+    T* amp = reinterpret_cast<T*>(hpos + nH);
+    const int nItems = *e.L.nEval;
+    int item = blockIdx.x;
+    if (item >= nItems) return;
     load_twiddles<T, N>(tw, e.k.tw);
     for (int h = threadIdx.x; h < nH; h += THREADS) hpos[h] = e.hPos[h];
-    const int nItems = *e.L.nEval;
-    for (int item = blockIdx.x; item < nItems; item += gridDim.x) {
-        const EvalItem it = e.L.eval[item];
+    for (int q = threadIdx.x; q < n2; q += THREADS) amp[q] = e.k.A[q];
+    EvalItem it = e.L.eval[item];
+    stage_phi<T, N, THREADS>(s2, e.phi + ((size_t)it.p * e.k.I + it.first) * n2);
+    cp_async_commit();
+    cp_async_wait_all();
+    int jj = 0;
+    while (true) {
         const size_t po = (size_t)it.p * e.k.nObj + it.o;
-        __syncthreads();    // previous item's accumulators written out
-        for (int h = threadIdx.x; h < nH; h += THREADS) oh[h] = e.Oh[po * nH + h];
-        for (int i = threadIdx.x; i < 4 * nH; i += THREADS) acc[i] = (T)0;
-        for (int jj = 0; jj < it.count; ++jj) {
-            const int j = it.first + jj;
-            const size_t g = (size_t)it.p * e.k.I + j;
-            const int ch = e.k.imgCh[j];
-            eval_image<T, N, THREADS>(e.phi + g * n2, e.k.A, e.k.otfNorm[ch], it.df, e.k.PF + g * n2,
-                                      e.k.X + g * N2, e.k.S + g * N2, e.Dh + g * nH, s, s2, tw, oh, acc, hpos, nH);
+        if (jj == 0) {
+            __syncthreads();    // previous item's accumulators written out
+            for (int h = threadIdx.x; h < nH; h += THREADS) oh[h] = e.Oh[po * nH + h];
+            for (int i = threadIdx.x; i < 4 * nH; i += THREADS) acc[i] = (T)0;
         }
-        __syncthreads();
-        T* part = e.part + (size_t)(it.p * e.hp.chunksPerPatch + it.chunk) * 4 * nH;
-        for (int i = threadIdx.x; i < 4 * nH; i += THREADS) part[i] = acc[i];
+        // the image after this one (same item, or the first of the block's next item)
+        int nextItem = item, nextJj = jj + 1;
+        EvalItem nit = it;
+        if (nextJj >= it.count) {
+            nextItem = item + gridDim.x;
+            nextJj = 0;
+            if (nextItem < nItems) nit = e.L.eval[nextItem];
+        }
+        const T* phiNext = nextItem < nItems ? e.phi + ((size_t)nit.p * e.k.I + nit.first + nextJj) * n2 : nullptr;
+        const int j = it.first + jj;
+        const size_t g = (size_t)it.p * e.k.I + j;
+        const int ch = e.k.imgCh[j];
+        eval_image<T, N, THREADS>(phiNext, amp, e.k.otfNorm[ch], it.df, e.k.PF + g * n2, e.k.X + g * N2,
+                                  e.k.S + g * N2, e.Dh + g * nH, s, s2, tw, oh, acc, hpos, e.hp.idx, nH);
+        if (nextJj == 0) {
+            __syncthreads();
+            T* part = e.part + (size_t)(it.p * e.hp.chunksPerPatch + it.chunk) * 4 * nH;
+            for (int i = threadIdx.x; i < 4 * nH; i += THREADS) part[i] = acc[i];
+            if (nextItem >= nItems) break;
+            item = nextItem;
+            it = nit;
+        }
+        jj = nextJj;
     }
 }
 

@@ -255,7 +255,9 @@ __device__ __forceinline__ void fft2d(cx<T>* s, const cx<T>* tw) {
 
 // ---- ping-pong variant: out-of-place stages between two tiles (a -> b -> a), one barrier
 // per stage and one butterfly in registers at a time ----
-template <typename T, int N, int R, int NS, int DIR, int LINES, int THREADS>
+// RLO, RHI: only inputs r in [RLO, RHI) of each butterfly can be non-zero (the others are
+// known zeros and are neither loaded nor multiplied)
+template <typename T, int N, int R, int NS, int DIR, int LINES, int THREADS, int RLO = 0, int RHI = R>
 __device__ __forceinline__ void fft_stage_pp(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst, int line0,
                                              int lstride, int estride, const cx<T>* tw) {
     constexpr int BF = N / R;
@@ -269,10 +271,11 @@ __device__ __forceinline__ void fft_stage_pp(const cx<T>* __restrict__ src, cx<T
         const cx<T>* in = src + line * lstride;
         cx<T> v[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = in[(j + r * BF) * estride];
+        for (int r = 0; r < R; ++r) v[r] = (r >= RLO && r < RHI) ? in[(j + r * BF) * estride] : mkc<T>(0, 0);
         if (NS > 1) {
 #pragma unroll
             for (int r = 1; r < R; ++r) {
+                if (r < RLO || r >= RHI) continue;
                 cx<T> w = tw[r * k * TWS];
                 if (DIR > 0) w.y = -w.y;
                 v[r] = cmul<T>(v[r], w);
