@@ -76,7 +76,7 @@ struct rdxg_solver {
     double* dObjMetric = nullptr;
     EvalItem* dEval = nullptr;
     PoItem* dPoList = nullptr;
-    int32_t *dGradP = nullptr, *dFdP = nullptr;
+    int32_t *dGradP = nullptr, *dFdP = nullptr, *dEvalP = nullptr;
     int adjGrid = 0, fdGrid = 0;
 };
 
@@ -185,6 +185,7 @@ Lists make_lists(rdxg_solver* h) {
     L.nEval = h->dCounters + 0; L.nPo = h->dCounters + 1;
     L.gradP = h->dGradP; L.nGradP = h->dCounters + 2;
     L.fdP = h->dFdP; L.nFdP = h->dCounters + 3;
+    L.evalP = h->dEvalP; L.nEvalP = h->dCounters + 4;
     return L;
 }
 
@@ -197,6 +198,7 @@ EvalParams<T> make_evalparams(rdxg_solver* h) {
     e.Dh = (const cx<T>*)h->dDh; e.Oh = (cx<T>*)h->dOh; e.part = (T*)h->dPart;
     e.objMetric = h->dObjMetric; e.L = make_lists(h);
     e.hPos = h->dHPos; e.nTilesH = h->nTilesH; e.phi = (T*)h->dPhiImg;
+    e.nCh = h->C;
     return e;
 }
 
@@ -277,7 +279,7 @@ int alloc_patch_buffers(rdxg_solver* h) {
         (r = dalloc_t(h, &h->dStates, P)) || (r = dalloc_t(h, &h->dVec, P * 5 * h->nFree)) ||
         (r = dalloc_t(h, &h->dAlpha, P * h->nPar)) || (r = dalloc_t(h, &h->dAlphaOff, P * h->nPar)) ||
         (r = dalloc_t(h, &h->dActive, 1)) || (r = dalloc_t(h, &h->dGradP, P)) || (r = dalloc_t(h, &h->dFdP, P)) ||
-        (r = dalloc_t(h, &h->dCounters, 4)))
+        (r = dalloc_t(h, &h->dEvalP, P)) || (r = dalloc_t(h, &h->dCounters, kNumCounters)))
         return r;
     CK(h, cudaMallocHost((void**)&h->hActive, sizeof(int32_t)));
     CK(h, cudaMemset(h->dReinit, 0, G));
@@ -506,7 +508,7 @@ int setup_fused(rdxg_solver* h, const rdxg_static* s) {
     if (occ < 1) occ = 1;
     h->evalGrid = h->numSMs * occ;
     h->reduceGrid = h->numSMs * 8;
-    h->phaseGrid = h->numSMs * 8;
+    h->phaseGrid = h->numSMs * 4;
     h->fused = true;
     return RDXG_OK;
 }
@@ -531,10 +533,15 @@ int host_lists(rdxg_solver* h, int req, int mode) {
             po.push_back(pi);
         }
     }
+    std::vector<int32_t> pl(h->P);
+    for (int p = 0; p < h->P; ++p) pl[p] = p;
     int32_t cnt[2] = {(int32_t)ev.size(), (int32_t)po.size()};
+    const int32_t nP = h->P;
     CK(h, cudaMemcpyAsync(h->dEval, ev.data(), ev.size() * sizeof(EvalItem), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaMemcpyAsync(h->dPoList, po.data(), po.size() * sizeof(PoItem), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->dEvalP, pl.data(), pl.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaMemcpyAsync(h->dCounters, cnt, sizeof(cnt), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->dCounters + 4, &nP, sizeof(nP), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     return RDXG_OK;
 }
@@ -805,7 +812,7 @@ int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
     const int G = P * h->I;
     for (long round = 0;; ++round) {
         CK(h, cudaMemsetAsync(h->dActive, 0, sizeof(int32_t), h->stream));
-        CK(h, cudaMemsetAsync(h->dCounters, 0, 4 * sizeof(int32_t), h->stream));
+        CK(h, cudaMemsetAsync(h->dCounters, 0, kNumCounters * sizeof(int32_t), h->stream));
         with_size(h->N, h->fp64, [&](auto L, auto t) {
             using T = decltype(t);
             KParams<T> kp = make_kparams<T>(h);

@@ -113,6 +113,7 @@ __device__ void map_point(const CgArgs<T>& a, int p, const double* x1) {
 // append the chunks and objects of patch p to the evaluation work lists
 template <typename T>
 __device__ void enqueue_eval(const CgArgs<T>& a, int p, int rq, int mode) {
+    a.L.evalP[atomicAdd(a.L.nEvalP, 1)] = p;
     for (int o = 0; o < a.nObj; ++o) {
         const int cnt = a.objCount[o];
         const int nc = (cnt + a.chunkSize - 1) / a.chunkSize;

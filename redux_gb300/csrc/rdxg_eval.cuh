@@ -37,6 +37,7 @@ struct Lists {
     PoItem* po;      int32_t* nPo;
     int32_t* gradP;  int32_t* nGradP;   // patches that need the analytic gradient
     int32_t* fdP;    int32_t* nFdP;     // patches that need the finite-difference gradient
+    int32_t* evalP;  int32_t* nEvalP;   // patches with an evaluation this round
     int32_t* counters;                  // base of the counters (reset every round)
 };
 
@@ -59,6 +60,7 @@ struct EvalParams {
     const int32_t* hPos; // [nH] tile position (row * (N+1) + column) of each half-plane point
     int32_t nTilesH;    // point tiles per object in the reduction
     T* phi;             // [g][n*n] phases of the images being evaluated (k_phase)
+    int32_t nCh;        // channels (fixed phases)
     Lists L;
 };
 
@@ -115,6 +117,92 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// Mode expansion per patch with the modes in registers.  The grid is a multiple of the
+// number of pixel tiles: block b always takes pixel tile b % nPix (its thread holds Z_m at
+// its pixel for m < MAXM in registers, zero beyond M) and walks the patches to evaluate
+// with stride gridDim.x / nPix.  A patch's coefficients are one contiguous block
+// alphaEff[p*I .. p*I + I) x M; the next patch's block is copied into the other of two
+// shared buffers (cp.async) while the current one is expanded, four images at a time (four
+// independent sums, coefficients read four modes at a time).  Each sum runs over m in
+// order, then the fixed phase of the image's channel is added, as in k_phase.
+template <typename T, int N, int PIX, int MAXM, int MAXI, int MAXCH>
+__global__ void __launch_bounds__(PIX, 4) k_phase_patch(EvalParams<T> e) {
+    constexpr int n2 = (N / 2) * (N / 2);
+    constexpr int nPix = (n2 + PIX - 1) / PIX;
+    static_assert(MAXM % 4 == 0 && MAXI % 4 == 0, "modes and images go four at a time");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* as = reinterpret_cast<T*>(smem_raw);          // [2][MAXI][MAXM]
+    T* pfs = as + 2 * MAXI * MAXM;                   // [MAXCH][PIX]
+    int* chs = reinterpret_cast<int*>(pfs + MAXCH * PIX);   // [MAXI]
+    const int M = e.k.M, I = e.k.I;
+    const int nP = *e.L.nEvalP;
+    const int S = gridDim.x / nPix;
+    const int s0 = blockIdx.x / nPix;
+    if (s0 >= nP) return;
+    const int q0 = (blockIdx.x % nPix) * PIX;
+    const int q = q0 + threadIdx.x;
+    T z[MAXM];
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m) z[m] = (m < M && q < n2) ? e.k.Z[(size_t)m * n2 + q] : (T)0;
+    // zero both buffers once: the copies only fill m < M of rows < I
+    for (int i = threadIdx.x; i < 2 * MAXI * MAXM; i += PIX) as[i] = (T)0;
+    for (int i = threadIdx.x; i < e.nCh * PIX; i += PIX) {
+        const int qq = q0 + i % PIX;
+        pfs[i] = qq < n2 ? e.k.phiFixed[(size_t)(i / PIX) * n2 + qq] : (T)0;
+    }
+    for (int i = threadIdx.x; i < MAXI; i += PIX) chs[i] = i < I ? e.k.imgCh[i] : 0;
+    __syncthreads();
+    const int IM = I * M;
+    auto fetch = [&](int k, int buf) {
+        const int p = e.L.evalP[k];
+        const T* src = e.k.alphaEff + (size_t)p * IM;
+        T* dst = as + buf * MAXI * MAXM;
+        for (int i = threadIdx.x; i < IM; i += PIX) cp_async4(dst + (i / M) * MAXM + i % M, src + i);
+    };
+    fetch(s0, 0);
+    cp_async_commit();
+    int buf = 0;
+    for (int k = s0; k < nP; k += S) {
+        if (k + S < nP) fetch(k + S, buf ^ 1);
+        cp_async_commit();
+        cp_async_wait_one();
+        __syncthreads();
+        if (q < n2) {
+            const int p = e.L.evalP[k];
+            const T* ab = as + buf * MAXI * MAXM;
+            for (int i = 0; i < I; i += 4) {
+                const T* al = ab + i * MAXM;
+                T acc0 = (T)0, acc1 = (T)0, acc2 = (T)0, acc3 = (T)0;
+#pragma unroll
+                for (int m = 0; m < MAXM; m += 4) {
+                    const float4 a0 = *reinterpret_cast<const float4*>(al + m);
+                    const float4 a1 = *reinterpret_cast<const float4*>(al + MAXM + m);
+                    const float4 a2 = *reinterpret_cast<const float4*>(al + 2 * MAXM + m);
+                    const float4 a3 = *reinterpret_cast<const float4*>(al + 3 * MAXM + m);
+                    acc0 += a0.x * z[m]; acc0 += a0.y * z[m + 1]; acc0 += a0.z * z[m + 2]; acc0 += a0.w * z[m + 3];
+                    acc1 += a1.x * z[m]; acc1 += a1.y * z[m + 1]; acc1 += a1.z * z[m + 2]; acc1 += a1.w * z[m + 3];
+                    acc2 += a2.x * z[m]; acc2 += a2.y * z[m + 1]; acc2 += a2.z * z[m + 2]; acc2 += a2.w * z[m + 3];
+                    acc3 += a3.x * z[m]; acc3 += a3.y * z[m + 1]; acc3 += a3.z * z[m + 2]; acc3 += a3.w * z[m + 3];
+                }
+                const T accs[4] = {acc0, acc1, acc2, acc3};
+                T* out = e.phi + ((size_t)p * I + i) * n2 + q;
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (i + j < I) out[(size_t)j * n2] = pfs[chs[i + j] * PIX + threadIdx.x] + accs[j];
+            }
+        }
+        __syncthreads();    // buffer fully read before the next copy into it
+        buf ^= 1;
+    }
+    cp_async_wait_all();
+}
 
 // Staging places (W = N/2 + 1 slots per tile row, columns [N/2, N] of a row are never used
 // by the half-plane inverse transform):

@@ -101,8 +101,38 @@ void EvalLauncher<T, N>::eval(const EvalParams<T>& e, int npt, int grid, cudaStr
 #undef RDXG_LAUNCH
 }
 
+template <typename T>
+static size_t phase_patch_smem(int maxm) {
+    return ((size_t)2 * kPhaseMaxImg * maxm + kPhaseMaxCh * kPhaseRegPix) * sizeof(T) + kPhaseMaxImg * sizeof(int);
+}
+
+template <typename T, int N>
+int EvalLauncher<T, N>::phase_tiles() {
+    return ((N / 2) * (N / 2) + kPhaseRegPix - 1) / kPhaseRegPix;
+}
+
 template <typename T, int N>
 void EvalLauncher<T, N>::phase(const EvalParams<T>& e, int grid, cudaStream_t st) {
+    if (e.k.M <= kPhaseRegModes && e.nCh <= kPhaseMaxCh && e.k.I <= kPhaseMaxImg) {
+        // grid: a multiple of the pixel tiles
+        const int nPix = phase_tiles();
+        const int g = (grid / nPix > 0 ? grid / nPix : 1) * nPix;
+#define RDXG_PHASE_PATCH(MM)                                                                     \
+    k_phase_patch<T, N, kPhaseRegPix, MM, kPhaseMaxImg, kPhaseMaxCh>                              \
+        <<<g, kPhaseRegPix, phase_patch_smem<T>(MM), st>>>(e)
+        switch ((e.k.M + 7) / 8) {
+            case 0: case 1: RDXG_PHASE_PATCH(8); break;
+            case 2: RDXG_PHASE_PATCH(16); break;
+            case 3: RDXG_PHASE_PATCH(24); break;
+            case 4: RDXG_PHASE_PATCH(32); break;
+            case 5: RDXG_PHASE_PATCH(40); break;
+            case 6: RDXG_PHASE_PATCH(48); break;
+            case 7: RDXG_PHASE_PATCH(56); break;
+            default: RDXG_PHASE_PATCH(64); break;
+        }
+#undef RDXG_PHASE_PATCH
+        return;
+    }
     const size_t sm = (size_t)e.k.M * (kPhasePix + kMaxChunk) * sizeof(T);
     k_phase<T, N, kPhasePix, kMaxChunk><<<grid, kPhasePix, sm, st>>>(e);
 }

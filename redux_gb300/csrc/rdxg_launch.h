@@ -31,6 +31,11 @@ constexpr int kEvalThreads = 512;
 constexpr int kReduceThreads = 256;
 constexpr int kPhasePix = 256;      // pixels per block of the mode expansion
 constexpr int kMaxChunk = 8;        // images per chunk (upper bound)
+constexpr int kPhaseRegPix = 128;   // pixels per block of the per-patch mode expansion
+constexpr int kPhaseRegModes = 64;  // modes it holds in registers (more: the staged kernel)
+constexpr int kPhaseMaxImg = 64;    // images per patch it stages
+constexpr int kPhaseMaxCh = 16;     // channels whose fixed phases it stages
+constexpr int kNumCounters = 5;     // work-list counters reset every round
 template <typename T, int N> struct EvalLauncher {
     static cudaError_t setup(int M, int npt, int nH);
     static void eval(const EvalParams<T>& e, int npt, int grid, cudaStream_t st);
@@ -38,6 +43,7 @@ template <typename T, int N> struct EvalLauncher {
     static void phase(const EvalParams<T>& e, int grid, cudaStream_t st);
     static size_t smem(int M, int nH);
     static int occupancy(int M, int npt, int nH);   // resident blocks per SM
+    static int phase_tiles();                        // pixel tiles of the per-patch mode expansion
 };
 template <typename T> void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st);
 void launch_shift(const ShiftArgs& a, int P, cudaStream_t st);
