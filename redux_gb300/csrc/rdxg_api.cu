@@ -66,6 +66,7 @@ struct rdxg_solver {
     rdxg_solve_params lastParams{};
     // fused evaluation path (FP32, N <= 88)
     bool fused = false;
+    bool fusedFd = false;     // half-plane finite-difference gradient (fits in shared memory)
     int npt = 0, chunk = 6, chunksPerPatch = 0, nH = 0, evalGrid = 0, reduceGrid = 0, numSMs = 0;
     std::vector<int32_t> objChunk0, hIdx, hPos;
     int nTilesH = 0;
@@ -200,6 +201,22 @@ EvalParams<T> make_evalparams(rdxg_solver* h) {
     e.hPos = h->dHPos; e.nTilesH = h->nTilesH; e.phi = (T*)h->dPhiImg;
     e.nCh = h->C;
     return e;
+}
+
+// finite-difference gradient of the patches in the FD list
+void launch_fd(rdxg_solver* h) {
+    if (h->fusedFd) {
+        with_eval(h->N, [&](auto E) {
+            EvalParams<float> e = make_evalparams<float>(h);
+            decltype(E)::fd_half(e, h->numSMs, h->stream);
+        });
+        return;
+    }
+    with_size(h->N, h->fp64, [&](auto L, auto t) {
+        using T = decltype(t);
+        KParams<T> kp = make_kparams<T>(h);
+        decltype(L)::fd(kp, h->fdGrid, h->M, h->stream);
+    });
 }
 
 template <typename T>
@@ -448,6 +465,7 @@ CgParams make_cg_params(rdxg_solver* h, const rdxg_solve_params* s) {
 int setup_fused(rdxg_solver* h, const rdxg_static* s) {
     const int N = h->N;
     h->fused = false;
+    h->fusedFd = false;
     if (h->fp64 || !(N == 32 || N == 64 || N == 88)) return RDXG_OK;
     std::vector<uint8_t> mask((size_t)N * N, 0);
     for (int k = 0; k < s->n_otf_support; ++k) mask[s->otf_support[k]] = 1;
@@ -506,6 +524,9 @@ int setup_fused(rdxg_solver* h, const rdxg_static* s) {
     });
     if (e != cudaSuccess) { h->err = std::string("fused setup: ") + cudaGetErrorString(e); return RDXG_ERR_CUDA; }
     if (occ < 1) occ = 1;
+    size_t fdSmem = 0;
+    with_eval(N, [&](auto L) { fdSmem = decltype(L)::fd_smem(h->nH); });
+    h->fusedFd = fdSmem + 1024 <= kMaxSmem;   // 1 KB left for static shared memory
     h->evalGrid = h->numSMs * occ;
     h->reduceGrid = h->numSMs * 8;
     h->phaseGrid = h->numSMs * 4;
@@ -752,9 +773,10 @@ int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, i
             decltype(L)::forward(kp, h->P * h->I, h->stream);
             launch_accum<T>(kp, h->P * h->nObj, h->stream);
         }
-        if (method == RDXG_GRAD_FD) decltype(L)::fd(kp, h->fdGrid, h->M, h->stream);
-        else decltype(L)::adjoint(kp, h->adjGrid, method == RDXG_GRAD_EXACT ? GK_EXACT : GK_VOGEL, h->stream);
+        if (method != RDXG_GRAD_FD)
+            decltype(L)::adjoint(kp, h->adjGrid, method == RDXG_GRAD_EXACT ? GK_EXACT : GK_VOGEL, h->stream);
     });
+    if (method == RDXG_GRAD_FD) launch_fd(h);
     CKL(h);
     const size_t G = (size_t)h->P * h->I;
     CK(h, cudaMemcpyAsync(grad, h->dGalpha, G * h->M * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -832,8 +854,8 @@ int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
                 launch_accum<T>(kp, P * h->nObj, h->stream);
             }
             decltype(L)::adjoint(kp, h->adjGrid, GK_VOGEL, h->stream);
-            decltype(L)::fd(kp, h->fdGrid, h->M, h->stream);
         });
+        launch_fd(h);
         h->launches += h->fused ? 8 : 7;
         CKL(h);
         if ((round + 1) % check == 0) {
@@ -914,7 +936,7 @@ int rdxg_profile_kernels(rdxg_solver* h, int32_t reps, double* ms) {
                     case 0: case 2: decltype(L)::forward(kp, G, h->stream); break;
                     case 1: launch_accum<T>(kp, PO, h->stream); break;
                     case 3: decltype(L)::adjoint(kp, h->adjGrid, GK_VOGEL, h->stream); break;
-                    case 4: decltype(L)::fd(kp, h->fdGrid, h->M, h->stream); break;
+                    case 4: launch_fd(h); break;
                 }
             });
         };

@@ -164,23 +164,32 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
         return;
     }
     if (st.req == REQ_F) {
-        if (threadIdx.x == 0) {
-            double sum = 0;
-            for (int o = 0; o < a.nObj; ++o) {
-                const double w = a.objWeight[o];
-                if (w == 0.0) continue;
-                double m = 0;
-                if (a.fused) {
-                    const double* om = a.objMetric + ((size_t)p * a.nObj + o) * a.nTilesH;
-                    for (int t = 0; t < a.nTilesH; ++t) m += om[t];
-                } else {
-                    const double* pp = a.partial + ((size_t)p * a.nObj + o) * a.nTiles;
-                    for (int t = 0; t < a.nTiles; ++t) m += pp[t];
+        // the block loads the per-tile sums of the patch's objects in parallel; thread 0
+        // adds them tile by tile, object by object, in a fixed order
+        __shared__ double tiles[THREADS];
+        const int nT = a.fused ? a.nTilesH : a.nTiles;
+        const double* src = (a.fused ? a.objMetric : a.partial) + (size_t)p * a.nObj * nT;
+        const int total = a.nObj * nT;
+        double sum = 0, m = 0;
+        for (int base = 0; base < total; base += THREADS) {
+            const int i = base + threadIdx.x;
+            tiles[threadIdx.x] = i < total ? src[i] : 0.0;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                const int cnt = min(THREADS, total - base);
+                for (int k = 0; k < cnt; ++k) {
+                    const int o = (base + k) / nT, t = (base + k) % nT;
+                    m += tiles[k];
+                    if (t == nT - 1) {
+                        const double w = a.objWeight[o];
+                        if (w != 0.0) sum += w * (m / ((double)a.ps * a.ps));
+                        m = 0;
+                    }
                 }
-                sum += w * (m / ((double)a.ps * a.ps));
             }
-            fsh = sum;
+            __syncthreads();
         }
+        if (threadIdx.x == 0) fsh = sum;
         __syncthreads();
         f = fsh;
     } else if (st.req == REQ_DF) {

@@ -230,23 +230,65 @@ __device__ __forceinline__ void stage_phi(cx<T>* b, const T* __restrict__ phi_g)
     for (int p = threadIdx.x; p < pairs; p += THREADS) cp_async8(b + Stage<N>::phi_slot(p), phi_g + 2 * p);
 }
 
-// One image of a chunk.  Forward: the pupil function (rows and columns [N/4, 3N/4) of tile
-// a, nothing else is read) is transformed with the first stage of each pass loading only
-// the middle half of its inputs.  |X|^2 is real: rows 2m and 2m+1 are packed as the real
-// and imaginary parts of row m of tile b, the N/2 packed rows are inverse-transformed and
-// split again (A = (Z(k) + conj Z(-k))/2, B = (Z(k) - conj Z(-k))/2i), and only the columns
-// [0, N/2) that hold the half-plane points are transformed along y.
-// On entry the phases of this image are staged in b; phiNext (or null) is the next image's.
+// Half-plane OTF core.  On entry tile a holds a pupil-plane field in rows and columns
+// [N/4, 3N/4) (nothing else of a is read).  Forward: the field is transformed with the first
+// stage of each pass loading only the middle half of its inputs.  pack(m, x, v0, v1) turns
+// the transforms v0, v1 at rows 2m, 2m+1 of column x into two real values (|X|^2 for the
+// OTF), which are stored as the real and imaginary parts of row m of tile b; the N/2 packed
+// rows are inverse-transformed along x and split again (A = (Z(k) + conj Z(-k))/2,
+// B = (Z(k) - conj Z(-k))/2i), and only the columns [0, N/2) that hold the half-plane points
+// are transformed along y.  On return a holds N^2 times the inverse transform in those
+// columns.  afterPack, afterRows and midColumns run after the packing, after the inverse
+// along x and between the two stages along y (where the caller issues or awaits copies).
+template <typename T, int N, int THREADS, typename Pack, typename H1, typename H2, typename H3>
+__device__ __forceinline__ void half_plane_core(cx<T>* a, cx<T>* b, const cx<T>* tw, Pack pack, H1 afterPack,
+                                                H2 afterRows, H3 midColumns) {
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int H2N = N / 2;
+    constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
+    constexpr int LO = R1 / 4, HI = 3 * R1 / 4;      // non-zero inputs of the pruned first stage
+    static_assert(R1 % 4 == 0, "the pruned first stage needs a radix divisible by 4");
+    // forward: rows [N/4, 3N/4) (a -> b -> a), then all columns (a -> b -> a)
+    fft_stage_pp<T, N, R1, 1, -1, N / 2, THREADS, LO, HI>(a, b, N / 4, LDS, 1, tw);
+    fft_stage_pp<T, N, R2, R1, -1, N / 2, THREADS>(b, a, N / 4, LDS, 1, tw);
+    fft_stage_pp<T, N, R1, 1, -1, N, THREADS, LO, HI>(a, b, 0, 1, LDS, tw);
+    fft_stage_pp<T, N, R2, R1, -1, N, THREADS>(b, a, 0, 1, LDS, tw);
+    for (int i = threadIdx.x; i < H2N * N; i += THREADS) {
+        const int m = i / N, x = i % N;
+        b[m * LDS + x] = pack(m, x, a[(2 * m) * LDS + x], a[(2 * m + 1) * LDS + x]);
+    }
+    __syncthreads();
+    afterPack();
+    // inverse along x on the N/2 packed rows (b -> a -> b)
+    fft_stage_pp<T, N, R1, 1, +1, N / 2, THREADS>(b, a, 0, LDS, 1, tw);
+    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS>(a, b, 0, LDS, 1, tw);
+    afterRows();
+    // split the packed rows: columns [0, N/2) of rows 2m and 2m+1 into a
+    for (int i = threadIdx.x; i < H2N * H2N; i += THREADS) {
+        const int m = i / H2N, k = i % H2N;
+        const cx<T> z = b[m * LDS + k];
+        const cx<T> zc = b[m * LDS + ((N - k) % N)];
+        // A = (z + conj zc)/2 ; B = (z - conj zc)/(2i)
+        a[(2 * m) * LDS + k] = mkc<T>((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y - zc.y));
+        a[(2 * m + 1) * LDS + k] = mkc<T>((T)0.5 * (z.y + zc.y), (T)0.5 * (zc.x - z.x));
+    }
+    __syncthreads();
+    // inverse along y on columns [0, N/2) (a -> b -> a)
+    fft_stage_pp<T, N, R1, 1, +1, N / 2, THREADS>(a, b, 0, 1, LDS, tw);
+    midColumns();
+    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS>(b, a, 0, 1, LDS, tw);
+}
+
+// One image of a chunk: the OTF on the half plane (half_plane_core with pack = |X|^2),
+// folded into the chunk's accumulators.  On entry the phases of this image are staged in
+// b; phiNext (or null) is the next image's, fetched while this one is transformed.
 template <typename T, int N, int THREADS>
 __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, const T* A, T c, int df,
                                            cx<T>* PF, cx<T>* X, cx<T>* S, const cx<T>* __restrict__ Dg,
                                            cx<T>* a, cx<T>* b, const cx<T>* tw, const cx<T>* oh,
                                            T* acc, const int* hpos, const int* hidx, int nH) {
     constexpr int LDS = Tile<N>::LDS;
-    constexpr int n = N / 2, n2 = n * n, N2 = N * N, H2 = N / 2;
-    constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
-    constexpr int LO = R1 / 4, HI = 3 * R1 / 4;      // non-zero inputs of the pruned first stage
-    static_assert(R1 % 4 == 0, "the pruned first stage needs a radix divisible by 4");
+    constexpr int n = N / 2, n2 = n * n, N2 = N * N;
     static_assert(sizeof(cx<T>) == 8, "staging copies 8-byte elements");
     using St = Stage<N>;
     const T inv = (T)1 / (T)N2;
@@ -265,46 +307,26 @@ __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, const 
         a[(y + n / 2) * LDS + x + n / 2] = cscale<T>(pf, c);
     }
     __syncthreads();
-    // forward: rows [N/4, 3N/4) (a -> b -> a), then all columns (a -> b -> a)
-    fft_stage_pp<T, N, R1, 1, -1, N / 2, THREADS, LO, HI>(a, b, N / 4, LDS, 1, tw);
-    fft_stage_pp<T, N, R2, R1, -1, N / 2, THREADS>(b, a, N / 4, LDS, 1, tw);
-    fft_stage_pp<T, N, R1, 1, -1, N, THREADS, LO, HI>(a, b, 0, 1, LDS, tw);
-    fft_stage_pp<T, N, R2, R1, -1, N, THREADS>(b, a, 0, 1, LDS, tw);
-    // |X|^2 of rows 2m, 2m+1 packed into row m of b
-    for (int i = threadIdx.x; i < H2 * N; i += THREADS) {
-        const int m = i / N, x = i % N;
-        const cx<T> v0 = a[(2 * m) * LDS + x];
-        const cx<T> v1 = a[(2 * m + 1) * LDS + x];
-        if (df) {
-            X[(2 * m) * N + x] = v0;
-            X[(2 * m + 1) * N + x] = v1;
-        }
-        b[m * LDS + x] = mkc<T>(cnorm<T>(v0), cnorm<T>(v1));
-    }
-    __syncthreads();
     const int nFirst = nH < St::kFirstPart ? nH : St::kFirstPart;
-    for (int h = threadIdx.x; h < nFirst; h += THREADS) cp_async8(a + St::dh_slot(h), Dg + h);
-    if (phiNext) stage_phi<T, N, THREADS>(b, phiNext);
-    cp_async_commit();
-    // inverse along x on the N/2 packed rows (b -> a -> b)
-    fft_stage_pp<T, N, R1, 1, +1, N / 2, THREADS>(b, a, 0, LDS, 1, tw);
-    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS>(a, b, 0, LDS, 1, tw);
-    for (int h = nFirst + threadIdx.x; h < nH; h += THREADS) cp_async8(a + St::dh_slot(h), Dg + h);
-    cp_async_commit();
-    // split the packed rows: columns [0, N/2) of rows 2m and 2m+1 into a
-    for (int i = threadIdx.x; i < H2 * H2; i += THREADS) {
-        const int m = i / H2, k = i % H2;
-        const cx<T> z = b[m * LDS + k];
-        const cx<T> zc = b[m * LDS + ((N - k) % N)];
-        // A = (z + conj zc)/2 ; B = (z - conj zc)/(2i)
-        a[(2 * m) * LDS + k] = mkc<T>((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y - zc.y));
-        a[(2 * m + 1) * LDS + k] = mkc<T>((T)0.5 * (z.y + zc.y), (T)0.5 * (zc.x - z.x));
-    }
-    __syncthreads();
-    // inverse along y on columns [0, N/2) (a -> b -> a)
-    fft_stage_pp<T, N, R1, 1, +1, N / 2, THREADS>(a, b, 0, 1, LDS, tw);
-    cp_async_wait_all();
-    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS>(b, a, 0, 1, LDS, tw);
+    half_plane_core<T, N, THREADS>(
+        a, b, tw,
+        [&](int m, int x, cx<T> v0, cx<T> v1) {
+            if (df) {
+                X[(2 * m) * N + x] = v0;
+                X[(2 * m + 1) * N + x] = v1;
+            }
+            return mkc<T>(cnorm<T>(v0), cnorm<T>(v1));
+        },
+        [&] {
+            for (int h = threadIdx.x; h < nFirst; h += THREADS) cp_async8(a + St::dh_slot(h), Dg + h);
+            if (phiNext) stage_phi<T, N, THREADS>(b, phiNext);
+            cp_async_commit();
+        },
+        [&] {
+            for (int h = nFirst + threadIdx.x; h < nH; h += THREADS) cp_async8(a + St::dh_slot(h), Dg + h);
+            cp_async_commit();
+        },
+        [&] { cp_async_wait_all(); });
     if (df) {
         // the full OTF from the half plane (S(-u) = conj S(u)) for the gradient kernels
         for (int h = threadIdx.x; h < nH; h += THREADS) {
@@ -382,6 +404,114 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
             it = nit;
         }
         jj = nextJj;
+    }
+}
+
+// ----------------------------------------------------------------------------------
+// Finite-difference gradient on the half plane (SubImage::gradientFiniteDifference +
+// metricChange, subimage.cpp:261-292; the same rearrangement as k_fd):
+//     dS = ifft(2 Re(conj(X) dX) + |dX|^2) / N^2,  dX = fft(c PF (exp(i h Z_m) - 1)),
+//     dl = -sum [2 Q Re(dS conj G) + |dS|^2 (|D|^2 - Q |O|^2)] / (Q + dq),  G = conj(O)(D - O S).
+// dS, G, D, O, S and Q are Hermitian or real and even, so the sum over the support is twice
+// the sum over the half plane (the DC term is zero: dS(0) = 0).  One block per image, all
+// modes in turn: the per-point factors and c PF are staged in shared memory once per image
+// (about 221 KB at N = 88 with 3237 half-plane points);
+// X (62 KB per image) is read from L2 for every mode.
+// ----------------------------------------------------------------------------------
+template <typename T, int N, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1) k_fd_half(EvalParams<T> e) {
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int n = N / 2, n2 = n * n, N2 = N * N;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const KParams<T>& kp = e.k;
+    const int nH = e.hp.nH;
+    // shared memory: two tiles | twiddles | c PF | G (nH) | S (nH) | Q (nH) | |D|^2-Q|O|^2 (nH) |
+    //                tile positions (nH)
+    cx<T>* a = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* b = a + Tile<N>::ELEMS;
+    cx<T>* tw = b + Tile<N>::ELEMS;
+    cx<T>* pfs = tw + N;
+    cx<T>* hg = pfs + n2;
+    cx<T>* hs = hg + nH;
+    T* hq = reinterpret_cast<T*>(hs + nH);
+    T* hb = hq + nH;
+    unsigned short* hpos = reinterpret_cast<unsigned short*>(hb + nH);   // N*(N+1) < 65536
+    static_assert(Tile<N>::ELEMS <= 65536, "tile positions are 16-bit");
+    __shared__ double red[33];
+    const int nWork = *kp.nFdP * kp.I;
+    if ((int)blockIdx.x >= nWork) return;
+    load_twiddles<T, N>(tw, kp.tw);
+    for (int h = threadIdx.x; h < nH; h += THREADS) hpos[h] = (unsigned short)e.hPos[h];
+    const T inv = (T)1 / (T)N2;
+    for (int w = blockIdx.x; w < nWork; w += gridDim.x) {
+        const int p = kp.fdP[w / kp.I], j = w % kp.I;
+        const size_t g = (size_t)p * kp.I + j;
+        const int o = kp.imgObj[j];
+        const double wgt = kp.objWeight[o];
+        const int mc = kp.modeCount[p];
+        double* ga = kp.galpha + g * kp.M;
+        if (wgt == 0.0) {
+            for (int m = threadIdx.x; m < kp.M; m += THREADS) ga[m] = 0.0;
+            continue;
+        }
+        const size_t po = (size_t)p * kp.nObj + o;
+        const T c = kp.otfNorm[kp.imgCh[j]];
+        const double hstep = kp.objGradStep[o];
+        __syncthreads();    // previous image's staged factors consumed
+        for (int h = threadIdx.x; h < nH; h += THREADS) {
+            const int cidx = e.hp.idx[h];
+            const cx<T> S = kp.S[g * N2 + cidx];
+            const cx<T> D = kp.D[g * N2 + cidx];
+            const cx<T> O = kp.O[po * N2 + cidx];
+            const T Q = kp.Qt[po * N2 + cidx];
+            hg[h] = cmulc<T>(csub<T>(D, cmul<T>(O, S)), O);
+            hs[h] = S;
+            // Q < 0 marks the DC point (Q >= gamma > 0 elsewhere)
+            hq[h] = (cidx == (N / 2) * N + N / 2) ? (T)-1 : Q;
+            hb[h] = cnorm<T>(D) - Q * cnorm<T>(O);
+        }
+        for (int q = threadIdx.x; q < n2; q += THREADS) pfs[q] = cscale<T>(kp.PF[g * n2 + q], c);
+        const cx<T>* Xg = kp.X + g * N2;
+        for (int m = 0; m < kp.M; ++m) {
+            if (m >= mc) {
+                if (threadIdx.x == 0) ga[m] = 0.0;
+                continue;
+            }
+            const T* Zm = kp.Z + (size_t)m * n2;
+            __syncthreads();    // staged factors visible, previous mode's tiles consumed
+            for (int q = threadIdx.x; q < n2; q += THREADS) {
+                const T t = (T)hstep * Zm[q];
+                T sh, ch2, sn, cs;
+                sincos_t<T>(t * (T)0.5, &sh, &ch2);
+                sincos_t<T>(t, &sn, &cs);
+                const cx<T> ex = mkc<T>((T)-2 * sh * sh, sn);   // exp(i t) - 1
+                const int y = q / n, x = q % n;
+                a[(y + n / 2) * LDS + x + n / 2] = cmul<T>(pfs[q], ex);
+            }
+            __syncthreads();
+            half_plane_core<T, N, THREADS>(
+                a, b, tw,
+                [&](int mm, int x, cx<T> v0, cx<T> v1) {
+                    const cx<T> x0 = Xg[(2 * mm) * N + x];
+                    const cx<T> x1 = Xg[(2 * mm + 1) * N + x];
+                    return mkc<T>((T)2 * (x0.x * v0.x + x0.y * v0.y) + cnorm<T>(v0),
+                                  (T)2 * (x1.x * v1.x + x1.y * v1.y) + cnorm<T>(v1));
+                },
+                [] {}, [] {}, [] {});
+            T dl = 0;
+            for (int h = threadIdx.x; h < nH; h += THREADS) {
+                const T Q = hq[h];
+                if (Q < (T)0) continue;
+                const cx<T> dS = cscale<T>(a[hpos[h]], inv);
+                const cx<T> S = hs[h], G = hg[h];
+                const T dS2 = cnorm<T>(dS);
+                const T dq = (T)2 * (S.x * dS.x + S.y * dS.y) + dS2;
+                const T num = (T)2 * Q * (dS.x * G.x + dS.y * G.y) + dS2 * hb[h];
+                dl -= num / (Q + dq);
+            }
+            const double tot = 2.0 * block_sum<THREADS>((double)dl, red);
+            if (threadIdx.x == 0) ga[m] = wgt * (tot / (double)N2 / hstep * wgt);
+        }
     }
 }
 

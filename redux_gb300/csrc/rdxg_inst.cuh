@@ -80,6 +80,9 @@ cudaError_t EvalLauncher<T, N>::setup(int M, int npt, int nH) {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_phase<T, N, kPhasePix, kMaxChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)((size_t)M * (kPhasePix + kMaxChunk) * sizeof(T)));
+    if (e == cudaSuccess && fd_smem(nH) + 1024 <= kMaxSmem)
+        e = cudaFuncSetAttribute(k_fd_half<T, N, kEvalThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)fd_smem(nH));
     return e;
 }
 
@@ -135,6 +138,17 @@ void EvalLauncher<T, N>::phase(const EvalParams<T>& e, int grid, cudaStream_t st
     }
     const size_t sm = (size_t)e.k.M * (kPhasePix + kMaxChunk) * sizeof(T);
     k_phase<T, N, kPhasePix, kMaxChunk><<<grid, kPhasePix, sm, st>>>(e);
+}
+
+template <typename T, int N>
+size_t EvalLauncher<T, N>::fd_smem(int nH) {
+    return (size_t)(2 * Tile<N>::ELEMS + N + (N / 2) * (N / 2) + 2 * nH) * sizeof(cx<T>) +
+           (size_t)2 * nH * sizeof(T) + (size_t)nH * sizeof(unsigned short) + 16;
+}
+
+template <typename T, int N>
+void EvalLauncher<T, N>::fd_half(const EvalParams<T>& e, int grid, cudaStream_t st) {
+    k_fd_half<T, N, kEvalThreads><<<grid, kEvalThreads, fd_smem(e.hp.nH), st>>>(e);
 }
 
 template <typename T, int N>

@@ -36,6 +36,7 @@ constexpr int kPhaseRegModes = 64;  // modes it holds in registers (more: the st
 constexpr int kPhaseMaxImg = 64;    // images per patch it stages
 constexpr int kPhaseMaxCh = 16;     // channels whose fixed phases it stages
 constexpr int kNumCounters = 5;     // work-list counters reset every round
+constexpr size_t kMaxSmem = 227 * 1024;   // dynamic shared memory per block
 template <typename T, int N> struct EvalLauncher {
     static cudaError_t setup(int M, int npt, int nH);
     static void eval(const EvalParams<T>& e, int npt, int grid, cudaStream_t st);
@@ -44,6 +45,8 @@ template <typename T, int N> struct EvalLauncher {
     static size_t smem(int M, int nH);
     static int occupancy(int M, int npt, int nH);   // resident blocks per SM
     static int phase_tiles();                        // pixel tiles of the per-patch mode expansion
+    static size_t fd_smem(int nH);                   // shared memory of the half-plane FD gradient
+    static void fd_half(const EvalParams<T>& e, int grid, cudaStream_t st);
 };
 template <typename T> void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st);
 void launch_shift(const ShiftArgs& a, int P, cudaStream_t st);
