@@ -484,7 +484,7 @@ int setup_fused(rdxg_solver* h, const rdxg_static* s) {
         const int c = h->hIdx[k];
         h->hPos[k] = (((c / N) + N / 2) % N) * (N + 1) + ((c % N) + N / 2) % N;
     }
-    h->nTilesH = (h->nH + kReduceThreads - 1) / kReduceThreads;
+    h->nTilesH = (h->nH + 31) / 32;
     h->npt = 1;
     if (h->nH > N * (N / 2 + 1)) return RDXG_OK;   // more points than the staging area holds
     const size_t smem = N == 32 ? EvalLauncher<float, 32>::smem(h->M, h->nH)

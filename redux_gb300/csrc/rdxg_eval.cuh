@@ -56,9 +56,9 @@ struct EvalParams {
     const cx<T>* Dh;    // [g][nH] half-plane image transforms
     cx<T>* Oh;          // [po][nH] reference objects
     T* part;            // [P*chunksPerPatch][4][nH]  (R, Q, P're, P'im)
-    double* objMetric;  // [po][tiles] per-tile partial sums of the object metric
+    double* objMetric;  // [po][tiles] object metric summed over tiles of 32 half-plane points
     const int32_t* hPos; // [nH] tile position (row * (N+1) + column) of each half-plane point
-    int32_t nTilesH;    // point tiles per object in the reduction
+    int32_t nTilesH;    // point tiles (32 points) per object in the reduction
     T* phi;             // [g][n*n] phases of the images being evaluated (k_phase)
     int32_t nCh;        // channels (fixed phases)
     Lists L;
@@ -516,17 +516,20 @@ __global__ void __launch_bounds__(THREADS, 1) k_fd_half(EvalParams<T> e) {
 }
 
 // ----------------------------------------------------------------------------------
-// Per-object reduction over the chunks (fixed order) and the object metric: one block per
-// (object, tile of points); the per-tile partial sums (double) are added in a fixed order by
-// the solver.  mode 1 (gradient) and 2 (refresh) replace O' by the exact object O of this
-// point; mode 1 also writes O and Q on the full plane for the gradient kernels.
+// Per-object reduction over the chunks (fixed order) and the object metric: one warp per
+// (object, tile of 32 points); each tile's sum is formed in double by a fixed shuffle tree
+// and the solver adds the tiles in order.  mode 1 (gradient) and 2 (refresh) replace O' by
+// the exact object O of this point; mode 1 also writes O and Q on the full plane for the
+// gradient kernels.
 // ----------------------------------------------------------------------------------
 template <typename T, int N, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_reduce(EvalParams<T> e) {
-    __shared__ double red[33];
+    constexpr int WPB = THREADS / 32;
+    static_assert(THREADS % 32 == 0, "tiles are warps");
     const int nItems = *e.L.nPo * e.nTilesH;
     const int nH = e.hp.nH;
-    for (int w = blockIdx.x; w < nItems; w += gridDim.x) {
+    const int lane = threadIdx.x & 31;
+    for (int w = blockIdx.x * WPB + threadIdx.x / 32; w < nItems; w += gridDim.x * WPB) {
         const PoItem it = e.L.po[w / e.nTilesH];
         const int tile = w % e.nTilesH;
         const size_t po = (size_t)it.p * e.k.nObj + it.o;
@@ -535,7 +538,7 @@ __global__ void __launch_bounds__(THREADS) k_reduce(EvalParams<T> e) {
         const int nc = (e.k.objCount[it.o] + e.hp.chunkSize - 1) / e.hp.chunkSize;
         const T* base = e.part + (size_t)(it.p * e.hp.chunksPerPatch + c0) * 4 * nH;
         double acc = 0;
-        const int h = tile * THREADS + threadIdx.x;
+        const int h = tile * 32 + lane;
         if (h < nH) {
             T R = 0, Q = 0, Pr = 0, Pi = 0;
             for (int c = 0; c < nc; ++c) {
@@ -563,8 +566,9 @@ __global__ void __launch_bounds__(THREADS) k_reduce(EvalParams<T> e) {
                 }
             }
         }
-        const double tot = block_sum<THREADS>(acc, red);
-        if (threadIdx.x == 0) e.objMetric[po * e.nTilesH + tile] = tot;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) e.objMetric[po * e.nTilesH + tile] = acc;
     }
 }
 
