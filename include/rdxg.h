@@ -137,6 +137,26 @@ int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric);
  * of alpha.  Same result as rdxg_metric up to rounding; used to check that rounding. */
 int rdxg_metric_with_reference(rdxg_solver* h, const double* alpha_ref, const double* alpha, double* metric);
 
+/* rdxg_metric without any allocation.  No counterpart in the reference (its Solver::metric
+ * works on buffers allocated per patch).  Same kernels, same work-item order and the same
+ * result as rdxg_metric; every temporary of the evaluation (alpha, mode-expanded phases,
+ * per-chunk accumulators, per-tile sums, work lists, per-patch metrics) lives in one
+ * file-scope static device array of 16 MiB instead of buffers of the handle, and the work
+ * lists are built on the device, so the call makes no device or host allocation (no
+ * cudaMalloc, cudaFree or heap allocation).  For callers that cannot allocate: a process
+ * whose caching allocator (e.g. PyTorch's) already holds nearly all device memory, where a
+ * raw cudaMalloc fails or forces the cache to be emptied, and latency-critical loops where
+ * cudaMalloc/cudaFree would synchronize the device and stall other streams.
+ * Limits: the fused FP32 path only (OTF size 32, 64 or 88 with a symmetric OTF support;
+ * otherwise RDXG_ERR_UNSUPPORTED), and a batch whose temporaries exceed 16 MiB (about 600 KB
+ * per patch at N = 88 with 36 images and 36 modes, i.e. at most 26 such patches) is rejected
+ * with RDXG_ERR_UNSUPPORTED and a message giving the sizes.  The handle's device must be the
+ * current device.  The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress, cached afterwards); make that first call before any stream capture.
+ * The scratch is shared by every handle on the device: calls that overlap in time (from two
+ * threads, or on two streams) race on it and must be serialized by the caller. */
+int rdxg_metric_noalloc(rdxg_solver* h, const double* alpha, double* metric);
+
 /* Gradient in alpha space [P][I][M] at alpha (Solver::my_df without the constraint map,
  * solver.cpp:228-234, 860-894); enabled: [M] flags or NULL (all); metric: [P] or NULL. */
 int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, int32_t method,

@@ -16,7 +16,8 @@ RDXG_GRAD_VOGEL, RDXG_GRAD_EXACT, RDXG_GRAD_FD = 0, 1, 2
 EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "rdxg_set_stream",
             "rdxg_set_patches", "rdxg_set_patches_device", "rdxg_metric", "rdxg_gradient",
             "rdxg_solve", "rdxg_solve_async", "rdxg_fetch_results", "rdxg_last_launch_count",
-            "rdxg_debug_copy", "rdxg_cg_minimize", "rdxg_profile_kernels", "rdxg_metric_with_reference")
+            "rdxg_debug_copy", "rdxg_cg_minimize", "rdxg_profile_kernels", "rdxg_metric_with_reference",
+            "rdxg_metric_noalloc")
 
 
 class Geometry(C.Structure):
@@ -76,6 +77,7 @@ def load(path: str = LIB_PATH):
     L.rdxg_set_patches_device.argtypes = [vp, C.c_int32, vp, vp, vp]
     L.rdxg_metric.argtypes = [vp, vp, vp]
     L.rdxg_metric_with_reference.argtypes = [vp, vp, vp, vp]
+    L.rdxg_metric_noalloc.argtypes = [vp, vp, vp]
     L.rdxg_gradient.argtypes = [vp, vp, vp, C.c_int32, vp, vp]
     L.rdxg_solve.argtypes = [vp, C.POINTER(SolveParams), vp, vp, vp]
     L.rdxg_solve_async.argtypes = [vp, C.POINTER(SolveParams)]

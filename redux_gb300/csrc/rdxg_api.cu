@@ -742,6 +742,85 @@ int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric) {
     return metric_from_partials(h, metric);
 }
 
+int rdxg_metric_noalloc(rdxg_solver* h, const double* alpha, double* metric) {
+    if (!h || !alpha || !metric) return RDXG_ERR_ARG;
+    if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
+    if (!h->fused) {
+        h->err = "rdxg_metric_noalloc: needs the FP32 half-plane evaluation (OTF size 32, 64 or 88 with a "
+                 "symmetric OTF support)";
+        return RDXG_ERR_UNSUPPORTED;
+    }
+    int dev = -1;
+    CK(h, cudaGetDevice(&dev));
+    if (dev != h->geo.device) {
+        h->err = "rdxg_metric_noalloc: the handle's device must be the current device";
+        return RDXG_ERR_STATE;
+    }
+    void* base = nullptr;
+    CK(h, noalloc_scratch(dev, &base));
+    // carve the scratch into 256-byte aligned sections
+    const size_t P = (size_t)h->P, G = P * h->I, PO = P * h->nObj, M = (size_t)h->M, n2 = (size_t)h->n * h->n;
+    const size_t nH = (size_t)h->nH, cpp = (size_t)h->chunksPerPatch;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    const size_t oAlpha = take(G * M * sizeof(double)), oAe = take(G * M * sizeof(float));
+    const size_t oPhi = take(G * n2 * sizeof(float)), oPart = take(P * cpp * 4 * nH * sizeof(float));
+    const size_t oObj = take(PO * h->nTilesH * sizeof(double)), oEval = take(P * cpp * sizeof(EvalItem));
+    const size_t oPo = take(PO * sizeof(PoItem)), oEvalP = take(P * sizeof(int32_t));
+    const size_t oCnt = take(kNumCounters * sizeof(int32_t)), oMetric = take(P * sizeof(double));
+    if (off > kNoAllocScratchBytes) {
+        char msg[256];
+        std::snprintf(msg, sizeof(msg),
+                      "rdxg_metric_noalloc: %zu patches need %zu bytes of scratch; the static scratch holds %zu "
+                      "bytes (at most %zu patches of this geometry)",
+                      P, off, kNoAllocScratchBytes, kNoAllocScratchBytes / ((off + P - 1) / P));
+        h->err = msg;
+        return RDXG_ERR_UNSUPPORTED;
+    }
+    unsigned char* sb = static_cast<unsigned char*>(base);
+    double* dAlpha = reinterpret_cast<double*>(sb + oAlpha);
+    float* dAe = reinterpret_cast<float*>(sb + oAe);
+    int32_t* cnt = reinterpret_cast<int32_t*>(sb + oCnt);
+    double* dObj = reinterpret_cast<double*>(sb + oObj);
+    double* dMetric = reinterpret_cast<double*>(sb + oMetric);
+    Lists L{};
+    L.eval = reinterpret_cast<EvalItem*>(sb + oEval);
+    L.po = reinterpret_cast<PoItem*>(sb + oPo);
+    L.evalP = reinterpret_cast<int32_t*>(sb + oEvalP);
+    L.counters = cnt;
+    L.nEval = cnt + 0; L.nPo = cnt + 1; L.nGradP = cnt + 2; L.nFdP = cnt + 3; L.nEvalP = cnt + 4;
+    CK(h, cudaMemcpyAsync(dAlpha, alpha, G * M * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    // the list counters start at zero; every other word read below is written first
+    CK(h, cudaMemsetAsync(cnt, 0, kNumCounters * sizeof(int32_t), h->stream));
+    launch_noalloc_alpha(dAlpha, h->dCurTilt, h->dResAlpha, (int)G, (int)M, h->geo.tilt_x, h->geo.tilt_y, dAe,
+                         h->stream);
+    // as rdxg_metric: a first pass sets the reference object to this point, the second evaluates
+    for (int mode : {2, 0}) {
+        launch_noalloc_lists(h->P, h->nObj, h->dObjFirst, h->dObjCount, h->dObjChunk0, h->chunk, h->chunksPerPatch,
+                             mode, L, h->stream);
+        with_eval(h->N, [&](auto E) {
+            EvalParams<float> e = make_evalparams<float>(h);
+            e.k.alphaEff = dAe;
+            e.phi = reinterpret_cast<float*>(sb + oPhi);
+            e.part = reinterpret_cast<float*>(sb + oPart);
+            e.objMetric = dObj;
+            e.L = L;
+            decltype(E)::phase(e, h->phaseGrid, h->stream);
+            decltype(E)::eval(e, h->npt, h->evalGrid, h->stream);
+            decltype(E)::reduce(e, h->reduceGrid, h->stream);
+        });
+    }
+    launch_noalloc_metric(dObj, h->P, h->nObj, h->nTilesH, h->dObjW, (double)h->ps * h->ps, dMetric, h->stream);
+    CKL(h);
+    CK(h, cudaMemcpyAsync(metric, dMetric, P * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return RDXG_OK;
+}
+
 int rdxg_metric_with_reference(rdxg_solver* h, const double* alpha_ref, const double* alpha, double* metric) {
     if (!h || !alpha_ref || !alpha || !metric) return RDXG_ERR_ARG;
     if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }

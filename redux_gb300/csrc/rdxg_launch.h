@@ -51,4 +51,14 @@ template <typename T, int N> struct EvalLauncher {
 template <typename T> void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st);
 void launch_shift(const ShiftArgs& a, int P, cudaStream_t st);
 
+// rdxg_metric_noalloc: a fixed static device array holds every temporary of the evaluation
+constexpr size_t kNoAllocScratchBytes = (size_t)16 << 20;
+cudaError_t noalloc_scratch(int device, void** ptr);   // its address on a device (looked up once)
+void launch_noalloc_alpha(const double* alpha, const double* curTilt, const double* resAlpha, int G, int M,
+                          int tiltX, int tiltY, float* alphaEff, cudaStream_t st);
+void launch_noalloc_lists(int P, int nObj, const int32_t* objFirst, const int32_t* objCount, const int32_t* objChunk0,
+                          int chunkSize, int chunksPerPatch, int mode, const Lists& L, cudaStream_t st);
+void launch_noalloc_metric(const double* objMetric, int P, int nObj, int nTiles, const double* objWeight, double ps2,
+                           double* metric, cudaStream_t st);
+
 }  // namespace rdxg

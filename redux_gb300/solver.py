@@ -139,6 +139,13 @@ class Solver:
                     "rdxg_metric_with_reference")
         return out
 
+    def metric_noalloc(self, alpha) -> np.ndarray:
+        """rdxg_metric with every temporary in the library's fixed static device scratch."""
+        a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
+        out = np.zeros(self.P)
+        self._check(_lib.load().rdxg_metric_noalloc(self.h, _lib.ptr(a), _lib.ptr(out)), "rdxg_metric_noalloc")
+        return out
+
     def gradient(self, alpha, method: str = "vogel", enabled=None):
         a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
         g = np.zeros((self.P, self.I, self.M))

@@ -1,0 +1,52 @@
+"""rdxg_metric_noalloc (the metric with its temporaries in the library's static device scratch)
+against rdxg_metric, two calls in a row, and the size limit.  Named to be collected last, so
+it also runs after every other test has used the library in the same process."""
+import numpy as np
+import pytest
+
+from redux_gb300 import solver as S
+from tests.conftest import workload
+
+pytestmark = pytest.mark.gpu
+
+# Same kernels and summation order as rdxg_metric, but both refresh the handle's reference
+# object starting from its previous value, so two evaluations at one point (by either entry
+# point) agree to the rounding of the FP32 accumulation (1e-10 ... 3e-8 measured), not bit for
+# bit; the metric itself is within 1e-5 of FP64.
+TOL = 1e-6
+
+
+def _solver(w):
+    P = w.patches.cutouts.shape[0]
+    s = S.Solver(w.job, max_patches=P, precision="fp32")
+    s.set_patches(w.patches.cutouts, None, w.patches.fixed_gamma)
+    return s
+
+
+@pytest.mark.parametrize("cfg", [0, 2])
+def test_noalloc_matches_metric_two_calls(cfg):
+    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    s = _solver(w)
+    for scale in (0.5, 1.0):
+        a = w.patches.alpha_true * scale
+        ref = s.metric(a)
+        first = s.metric_noalloc(a)
+        second = s.metric_noalloc(a)
+        np.testing.assert_allclose(first, ref, rtol=TOL, atol=0)
+        np.testing.assert_allclose(second, ref, rtol=TOL, atol=0)
+        np.testing.assert_allclose(second, first, rtol=TOL, atol=0)
+
+
+def test_noalloc_rejects_batches_beyond_the_scratch():
+    # 88 x 88, 12 images per patch: about 255 KB of temporaries per patch, 70 patches > 16 MiB
+    w = workload(2, n_patches=70, frames=4)
+    s = _solver(w)
+    with pytest.raises(S.SolverError, match="static scratch holds"):
+        s.metric_noalloc(w.patches.alpha_true)
+    # the handle stays usable
+    assert np.all(np.isfinite(s.metric(w.patches.alpha_true)))
+    # and a batch that fits still agrees with rdxg_metric
+    small = workload(2, n_patches=2, frames=4)
+    s2 = _solver(small)
+    np.testing.assert_allclose(s2.metric_noalloc(small.patches.alpha_true), s2.metric(small.patches.alpha_true),
+                               rtol=TOL, atol=0)
