@@ -43,6 +43,7 @@ struct rdxg_solver {
     double *dObjW = nullptr, *dGradStep = nullptr, *dWin = nullptr, *dNWin = nullptr;
     int32_t *dRowPtr = nullptr, *dRowCol = nullptr, *dColPtr = nullptr, *dColRow = nullptr;
     double *dRowVal = nullptr, *dColVal = nullptr;
+    float* dRowVal32 = nullptr;   // FP32 copy of the row values (metric requests of the FP32 path)
     // device per patch
     float* dCut = nullptr;
     const float* dCutExt = nullptr;   // caller-owned device cutouts
@@ -226,11 +227,13 @@ CgArgs<T> make_cgargs(rdxg_solver* h, const CgParams& prm) {
     a.P = h->P; a.I = h->I; a.M = h->M; a.nObj = h->nObj; a.nPar = h->nPar; a.nTiles = h->nTiles; a.ps = h->ps;
     a.states = h->dStates; a.vec = h->dVec; a.metrics = h->dMetrics; a.alpha = h->dAlpha; a.alphaOff = h->dAlphaOff;
     a.galpha = h->dGalpha; a.partial = h->dPartial; a.objWeight = h->dObjW;
-    a.rowPtr = h->dRowPtr; a.rowCol = h->dRowCol; a.rowVal = h->dRowVal;
+    a.rowPtr = h->dRowPtr; a.rowCol = h->dRowCol; a.rowVal = h->dRowVal; a.rowVal32 = h->dRowVal32;
     a.colPtr = h->dColPtr; a.colRow = h->dColRow; a.colVal = h->dColVal;
     a.curTilt = h->dCurTilt; a.resAlpha = h->dResAlpha; a.tiltX = h->geo.tilt_x; a.tiltY = h->geo.tilt_y;
     a.alphaEff = (T*)h->dAlphaEff; a.req = h->dReq; a.gmethod = h->dGm; a.modeCount = h->dMc; a.active = h->dActive;
     a.fused = h->fused ? 1 : 0;
+    // FP32 map of metric requests: the point as float in dynamic shared memory (under 44 KB)
+    a.x1Smem = (!h->fp64 && (size_t)h->nFree * sizeof(float) <= 44 * 1024) ? 1 : 0;
     a.objMetric = h->dObjMetric; a.L = make_lists(h); a.nTilesH = h->nTilesH;
     a.chunkSize = h->chunk; a.chunksPerPatch = h->chunksPerPatch; a.objChunk0 = h->dObjChunk0;
     a.objFirst = h->dObjFirstC; a.objCount = h->dObjCountC; a.aux = h->dAux;
@@ -329,6 +332,9 @@ int build_nullspace(rdxg_solver* h, const rdxg_static* s) {
     h->dRowCol = (int32_t*)v;
     if ((r = upload(h, &v, rval))) return r;
     h->dRowVal = (double*)v;
+    std::vector<float> rval32(rval.begin(), rval.end());
+    if ((r = upload(h, &v, rval32))) return r;
+    h->dRowVal32 = (float*)v;
     if ((r = upload(h, &v, cc))) return r;
     h->dColPtr = (int32_t*)v;
     if ((r = upload(h, &v, crow))) return r;

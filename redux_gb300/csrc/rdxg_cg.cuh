@@ -68,6 +68,8 @@ struct CgArgs {
     const double* objWeight;
     // null-space map, by parameter row and by free column
     const int32_t* rowPtr; const int32_t* rowCol; const double* rowVal;
+    const float* rowVal32;  // FP32 copy of rowVal
+    int32_t x1Smem;         // FP32 metric-request map enabled (dynamic shared memory n_free floats)
     const int32_t* colPtr; const int32_t* colRow; const double* colVal;
     const double* curTilt;  // [P][I][2] (y, x): currentTiltOffset of each image
     const double* resAlpha; // [P][I][2] (y, x): channel residual tilt (phi_channel term)
@@ -106,6 +108,30 @@ __device__ void map_point(const CgArgs<T>& a, int p, const double* x1) {
         if (m == a.tiltX) ve += a.curTilt[b + 1] - a.resAlpha[b + 1];
         else if (m == a.tiltY) ve += a.curTilt[b + 0] - a.resAlpha[b + 0];
         ae[r] = (T)ve;
+    }
+    __syncthreads();
+}
+
+// The FP32 path's metric requests: alphaEff only, in FP32 arithmetic (it is rounded to FP32
+// for the evaluation anyway), with the point staged in shared memory as float.  GB300's FP64
+// rate makes the FP64 map the largest cost of the solver kernel; the FP64 alpha is formed by
+// map_point for every gradient, re-shift and final point, where it is used.
+template <typename T, int THREADS>
+__device__ void map_point_f32(const CgArgs<T>& a, int p, const double* x1, float* xs) {
+    const int nF = a.prm.n_free;
+    for (int c = threadIdx.x; c < nF; c += THREADS) xs[c] = (float)x1[c];
+    __syncthreads();
+    const double* off = a.alphaOff + (size_t)p * a.nPar;
+    T* ae = a.alphaEff + (size_t)p * a.nPar;
+    for (int r = threadIdx.x; r < a.nPar; r += THREADS) {
+        float v = 0.f;
+        for (int e = a.rowPtr[r]; e < a.rowPtr[r + 1]; ++e) v = fmaf(a.rowVal32[e], xs[a.rowCol[e]], v);
+        v += (float)off[r];
+        const int j = r / a.M, m = r % a.M;
+        const size_t b = ((size_t)p * a.I + j) * 2;
+        if (m == a.tiltX) v += (float)(a.curTilt[b + 1] - a.resAlpha[b + 1]);
+        else if (m == a.tiltY) v += (float)(a.curTilt[b + 0] - a.resAlpha[b + 0]);
+        ae[r] = (T)v;
     }
     __syncthreads();
 }
@@ -209,7 +235,13 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
     DevVec<THREADS> V{nF, red};
     Machine<DevVec<THREADS>> mc(a.prm, st, V, x, pv, g, g0, x1, a.metrics + (size_t)p * a.prm.max_metrics);
     const int rq = mc.advance(f);
-    if (rq == REQ_F || rq == REQ_DF || rq == REQ_SHIFT) map_point<T, THREADS>(a, p, x1);
+    if (sizeof(T) == sizeof(float) && a.x1Smem) {
+        extern __shared__ float xs[];
+        if (rq == REQ_F) map_point_f32<T, THREADS>(a, p, x1, xs);
+        else if (rq == REQ_DF || rq == REQ_SHIFT || rq == REQ_DONE) map_point<T, THREADS>(a, p, x1);
+    } else if (rq == REQ_F || rq == REQ_DF || rq == REQ_SHIFT) {
+        map_point<T, THREADS>(a, p, x1);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         a.states[p] = st;

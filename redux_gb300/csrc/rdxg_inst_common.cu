@@ -11,7 +11,8 @@ void launch_accum(const KParams<T>& kp, int nPo, cudaStream_t st) {
 
 template <typename T>
 void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st) {
-    k_cg<T, kCgThreads><<<P, kCgThreads, 0, st>>>(a);
+    const size_t sm = a.x1Smem ? (size_t)a.prm.n_free * sizeof(float) : 0;
+    k_cg<T, kCgThreads><<<P, kCgThreads, sm, st>>>(a);
 }
 
 void launch_shift(const ShiftArgs& a, int P, cudaStream_t st) {
