@@ -1,6 +1,6 @@
-// Device side of the per-patch optimiser: one thread block per patch runs the state
-// machine of cg_machine.h (scalar logic replicated in every thread, vector operations
-// block-parallel, all sums in double in a fixed order), maps the point of the next
+// Device side of the per-patch optimiser: one thread block per patch; its first warp runs the
+// state machine of cg_machine.h (scalar logic replicated in the warp's lanes, vector
+// operations warp-parallel, all sums in double in a fixed order), the block maps the point of the next
 // evaluation through the null-space map (Constraints::reverseAndAdd,
 // constraints.hpp:141-146) and the gradient back (Constraints::apply, 128-133), and
 // performs the integer image re-shifts between mode stages (SubImage::adjustShifts,
@@ -13,44 +13,53 @@
 
 namespace rdxg {
 
-template <int THREADS>
-struct DevVec {
+// Vector operations of the state machine, run by one warp (warp 0 of the block): the scalar
+// logic (FP64, including divisions) is then issued by one warp instead of every warp of the
+// block, on GB300's narrow FP64 pipe.  Sums: a fixed shuffle tree into lane 0, broadcast, so
+// every lane holds the same bits.
+struct WarpVec {
     int n;
-    double* red;
+    __device__ static double wsum(double a) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        return __shfl_sync(0xffffffffu, a, 0);
+    }
+    __device__ static int lane() { return threadIdx.x & 31; }
     __device__ void copy(double* d, const double* s) {
-        for (int i = threadIdx.x; i < n; i += THREADS) d[i] = s[i];
-        __syncthreads();
+        for (int i = lane(); i < n; i += 32) d[i] = s[i];
+        __syncwarp();
     }
     __device__ void zero(double* d) {
-        for (int i = threadIdx.x; i < n; i += THREADS) d[i] = 0.0;
-        __syncthreads();
+        for (int i = lane(); i < n; i += 32) d[i] = 0.0;
+        __syncwarp();
     }
     __device__ double nrm2(const double* v) {
         double a = 0;
-        for (int i = threadIdx.x; i < n; i += THREADS) a += v[i] * v[i];
-        return sqrt(block_sum<THREADS>(a, red));
+        for (int i = lane(); i < n; i += 32) a += v[i] * v[i];
+        return sqrt(wsum(a));
     }
     __device__ double dot(const double* x, const double* y) {
         double a = 0;
-        for (int i = threadIdx.x; i < n; i += THREADS) a += x[i] * y[i];
-        return block_sum<THREADS>(a, red);
+        for (int i = lane(); i < n; i += 32) a += x[i] * y[i];
+        return wsum(a);
     }
     __device__ double pr_update(double* g0, const double* g) {
         double a = 0;
-        for (int i = threadIdx.x; i < n; i += THREADS) {
+        for (int i = lane(); i < n; i += 32) {
             const double t = g0[i] - g[i];
             a += t * g[i];
             g0[i] = t;
         }
-        return block_sum<THREADS>(a, red);
+        __syncwarp();
+        return wsum(a);
     }
     __device__ void dir_update(double* p, const double* g, double beta) {
-        for (int i = threadIdx.x; i < n; i += THREADS) p[i] = g[i] - beta * p[i];
-        __syncthreads();
+        for (int i = lane(); i < n; i += 32) p[i] = g[i] - beta * p[i];
+        __syncwarp();
     }
     __device__ void step(double* x1, const double* x, const double* p, double s) {
-        for (int i = threadIdx.x; i < n; i += THREADS) x1[i] = x[i] + s * p[i];
-        __syncthreads();
+        for (int i = lane(); i < n; i += 32) x1[i] = x[i] + s * p[i];
+        __syncwarp();
     }
 };
 
@@ -139,7 +148,11 @@ __device__ void map_point_f32(const CgArgs<T>& a, int p, const double* x1, float
 // append the chunks and objects of patch p to the evaluation work lists
 template <typename T>
 __device__ void enqueue_eval(const CgArgs<T>& a, int p, int rq, int mode) {
-    a.L.evalP[atomicAdd(a.L.nEvalP, 1)] = p;
+    // one reservation per list (the atomics go out together), then the writes
+    const int kp = atomicAdd(a.L.nEvalP, 1);
+    const int k0 = atomicAdd(a.L.nEval, a.chunksPerPatch);
+    const int j0 = atomicAdd(a.L.nPo, a.nObj);
+    a.L.evalP[kp] = p;
     for (int o = 0; o < a.nObj; ++o) {
         const int cnt = a.objCount[o];
         const int nc = (cnt + a.chunkSize - 1) / a.chunkSize;
@@ -150,36 +163,39 @@ __device__ void enqueue_eval(const CgArgs<T>& a, int p, int rq, int mode) {
             it.count = min(a.chunkSize, cnt - c * a.chunkSize);
             it.chunk = a.objChunk0[o] + c;
             it.df = (rq == REQ_DF) ? 1 : 0;
-            const int k = atomicAdd(a.L.nEval, 1);
-            a.L.eval[k] = it;
+            a.L.eval[k0 + a.objChunk0[o] + c] = it;
         }
         PoItem pi;
         pi.p = p; pi.o = o; pi.mode = mode;
-        const int k = atomicAdd(a.L.nPo, 1);
-        a.L.po[k] = pi;
+        a.L.po[j0 + o] = pi;
     }
 }
 
 template <typename T, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
     const int p = blockIdx.x;
-    __shared__ double red[33];
     __shared__ double fsh;
-    CgState st = a.states[p];
+    __shared__ double objSum[64];
+    __shared__ int32_t pcShared, reqShared;
+    // the state is read by the first warp, which runs the machine; the block needs pc and req
+    CgState st;
+    if (threadIdx.x < 32) st = a.states[p];
+    if (threadIdx.x == 0) { pcShared = st.pc; reqShared = st.req; }
+    __syncthreads();
+    const int pc0 = pcShared, req0 = reqShared;
     const int nF = a.prm.n_free;
     double* x = a.vec + (size_t)p * 5 * nF;
     double* pv = x + nF;
     double* g = pv + nF;
     double* g0 = g + nF;
     double* x1 = g0 + nF;
-    if (st.pc == PC_DONE) {
+    if (pc0 == PC_DONE) {
         if (threadIdx.x == 0) a.req[p] = REQ_DONE;
         return;
     }
     double f = 0;
-    if (a.fused && st.req == REQ_F && a.aux[2 * p + 1]) {
+    if (a.fused && req0 == REQ_F && a.aux[2 * p + 1]) {
         // the last evaluation only refreshed the reference object: repeat the request
-        __syncthreads();
         if (threadIdx.x == 0) {
             a.aux[2 * p + 0] = 1;
             a.aux[2 * p + 1] = 0;
@@ -189,36 +205,31 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
         }
         return;
     }
-    if (st.req == REQ_F) {
-        // the block loads the per-tile sums of the patch's objects in parallel; thread 0
-        // adds them tile by tile, object by object, in a fixed order
-        __shared__ double tiles[THREADS];
+    if (req0 == REQ_F) {
+        // object sums: one warp per object, each lane adds its tiles in order, then a fixed
+        // shuffle tree; the objects are added in order
         const int nT = a.fused ? a.nTilesH : a.nTiles;
         const double* src = (a.fused ? a.objMetric : a.partial) + (size_t)p * a.nObj * nT;
-        const int total = a.nObj * nT;
-        double sum = 0, m = 0;
-        for (int base = 0; base < total; base += THREADS) {
-            const int i = base + threadIdx.x;
-            tiles[threadIdx.x] = i < total ? src[i] : 0.0;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                const int cnt = min(THREADS, total - base);
-                for (int k = 0; k < cnt; ++k) {
-                    const int o = (base + k) / nT, t = (base + k) % nT;
-                    m += tiles[k];
-                    if (t == nT - 1) {
-                        const double w = a.objWeight[o];
-                        if (w != 0.0) sum += w * (m / ((double)a.ps * a.ps));
-                        m = 0;
-                    }
-                }
-            }
-            __syncthreads();
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        for (int o = wid; o < a.nObj; o += THREADS / 32) {
+            double m = 0;
+            for (int t = lane; t < nT; t += 32) m += src[(size_t)o * nT + t];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) m += __shfl_down_sync(0xffffffffu, m, off);
+            if (lane == 0) objSum[o] = m;
         }
-        if (threadIdx.x == 0) fsh = sum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sum = 0;
+            for (int o = 0; o < a.nObj; ++o) {
+                const double w = a.objWeight[o];
+                if (w != 0.0) sum += w * (objSum[o] / ((double)a.ps * a.ps));
+            }
+            fsh = sum;
+        }
         __syncthreads();
         f = fsh;
-    } else if (st.req == REQ_DF) {
+    } else if (req0 == REQ_DF) {
         const double* ga = a.galpha + (size_t)p * a.nPar;
         for (int c = threadIdx.x; c < nF; c += THREADS) {
             double v = 0;
@@ -226,15 +237,21 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
             g[c] = v;
         }
         __syncthreads();
-    } else if (st.req == REQ_SHIFT) {
+    } else if (req0 == REQ_SHIFT) {
         double* off = a.alphaOff + (size_t)p * a.nPar;
         const double* al = a.alpha + (size_t)p * a.nPar;
         for (int r = threadIdx.x; r < a.nPar; r += THREADS) off[r] = al[r];
         __syncthreads();
     }
-    DevVec<THREADS> V{nF, red};
-    Machine<DevVec<THREADS>> mc(a.prm, st, V, x, pv, g, g0, x1, a.metrics + (size_t)p * a.prm.max_metrics);
-    const int rq = mc.advance(f);
+    __shared__ int rqShared;
+    if (threadIdx.x < 32) {
+        WarpVec V{nF};
+        Machine<WarpVec> mc(a.prm, st, V, x, pv, g, g0, x1, a.metrics + (size_t)p * a.prm.max_metrics);
+        const int r = mc.advance(f);
+        if (threadIdx.x == 0) rqShared = r;
+    }
+    __syncthreads();    // the point x1 and the request are visible to the block
+    const int rq = rqShared;
     if (sizeof(T) == sizeof(float) && a.x1Smem) {
         extern __shared__ float xs[];
         if (rq == REQ_F) map_point_f32<T, THREADS>(a, p, x1, xs);
