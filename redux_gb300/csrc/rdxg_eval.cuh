@@ -204,126 +204,118 @@ __global__ void __launch_bounds__(PIX, 4) k_phase_patch(EvalParams<T> e) {
     cp_async_wait_all();
 }
 
-// Staging places (W = N/2 + 1 slots per tile row, columns [N/2, N] of a row are never used
-// by the half-plane inverse transform):
-//   phases of the next image: tile b, rows [3N/4, N), columns [N/2, N]: free from the end of
-//     the forward transform until the next image's column pass;
-//   image transforms Dh: tile a, columns [N/2, N]; rows [N/2, N) are free once |X|^2 has been
-//     read, rows [0, N/2) once the packed inverse along x is done.
+// Staging places of the image transforms Dh (W = N/2 + 1 slots per tile row; the columns
+// [N/2, N] of the rows [N/2, N) of both tiles are left alone by the half-plane core after
+// its first column stage): h < N/2 * W in tile a, the rest in tile b.
 template <int N> struct Stage {
     static constexpr int LDS = N + 1, W = N / 2 + 1;
-    static __device__ __forceinline__ int phi_slot(int pair) {
-        return (3 * N / 4 + pair / W) * LDS + N / 2 + pair % W;
+    static constexpr int kPart = (N / 2) * W;     // points per tile
+    static constexpr int kMaxH = 2 * kPart;
+    static __device__ __forceinline__ int dh_slot(int h) {   // within its tile
+        const int k = h < kPart ? h : h - kPart;
+        return (N / 2 + k / W) * LDS + N / 2 + k % W;
     }
-    static __device__ __forceinline__ int dh_slot(int h) {
-        return ((N / 2 + h / W) % N) * LDS + N / 2 + h % W;
-    }
-    static constexpr int kMaxPhiPairs = (N / 4) * W;
-    static constexpr int kMaxH = N * W;
-    static constexpr int kFirstPart = (N / 2) * W;    // Dh points staged into rows [N/2, N)
 };
 
 template <typename T, int N, int THREADS>
-__device__ __forceinline__ void stage_phi(cx<T>* b, const T* __restrict__ phi_g) {
+__device__ __forceinline__ void stage_phi(T* buf, const T* __restrict__ phi_g) {
     constexpr int pairs = (N / 2) * (N / 2) / 2;
-    static_assert(pairs <= Stage<N>::kMaxPhiPairs, "phase staging area too small");
-    for (int p = threadIdx.x; p < pairs; p += THREADS) cp_async8(b + Stage<N>::phi_slot(p), phi_g + 2 * p);
+    for (int p = threadIdx.x; p < pairs; p += THREADS) cp_async8(buf + 2 * p, phi_g + 2 * p);
 }
 
-// Half-plane OTF core.  On entry tile a holds a pupil-plane field in rows and columns
-// [N/4, 3N/4) (nothing else of a is read).  Forward: the field is transformed with the first
-// stage of each pass loading only the middle half of its inputs.  pack(m, x, v0, v1) turns
-// the transforms v0, v1 at rows 2m, 2m+1 of column x into two real values (|X|^2 for the
-// OTF), which are stored as the real and imaginary parts of row m of tile b; the N/2 packed
-// rows are inverse-transformed along x and split again (A = (Z(k) + conj Z(-k))/2,
-// B = (Z(k) - conj Z(-k))/2i), and only the columns [0, N/2) that hold the half-plane points
-// are transformed along y.  On return a holds N^2 times the inverse transform in those
-// columns.  afterPack, afterRows and midColumns run after the packing, after the inverse
-// along x and between the two stages along y (where the caller issues or awaits copies).
-template <typename T, int N, int THREADS, typename Pack, typename H1, typename H2, typename H3>
-__device__ __forceinline__ void half_plane_core(cx<T>* a, cx<T>* b, const cx<T>* tw, Pack pack, H1 afterPack,
-                                                H2 afterRows, H3 midColumns) {
+// Half-plane OTF core.  pupil(y, x) gives the pupil-plane field at pupil pixel (y, x)
+// (embedded at rows and columns [N/4, 3N/4)); it is read by the first stage of the row pass,
+// which loads only those columns.  The column pass loads only those rows in its first stage;
+// its last stage hands every transform value v at (row e, column x) to elem(e, x, v), which
+// returns a real value (|X|^2 for the OTF) stored as the real (e even) or imaginary (e odd)
+// part of row e/2 of tile a: two real rows packed as one complex row.  The N/2 packed rows are
+// inverse-transformed along x; the first stage along y splits them again as it loads
+// (A = (Z(k) + conj Z(-k))/2, B = (Z(k) - conj Z(-k))/2i) and only the columns [0, N/2),
+// which hold the half-plane points, are transformed along y.  On return tile a holds N^2
+// times the inverse transform in those columns.  afterRows, afterCols1, afterPack run after
+// the row pass, the first column stage and the packing stage (where the caller issues copies
+// into the free parts of the tiles); midColumns runs between the two stages along y.
+template <typename T, int N, int THREADS, typename Pupil, typename Elem, typename HR, typename HC, typename HP,
+          typename HM>
+__device__ __forceinline__ void half_plane_core(cx<T>* a, cx<T>* b, const cx<T>* tw, Pupil pupil, Elem elem,
+                                                HR afterRows, HC afterCols1, HP afterPack, HM midColumns) {
     constexpr int LDS = Tile<N>::LDS;
-    constexpr int H2N = N / 2;
     constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
     constexpr int LO = R1 / 4, HI = 3 * R1 / 4;      // non-zero inputs of the pruned first stage
     static_assert(R1 % 4 == 0, "the pruned first stage needs a radix divisible by 4");
-    // forward: rows [N/4, 3N/4) (a -> b -> a), then all columns (a -> b -> a)
-    fft_stage_pp<T, N, R1, 1, -1, N / 2, THREADS, LO, HI>(a, b, N / 4, LDS, 1, tw);
-    fft_stage_pp<T, N, R2, R1, -1, N / 2, THREADS>(b, a, N / 4, LDS, 1, tw);
-    fft_stage_pp<T, N, R1, 1, -1, N, THREADS, LO, HI>(a, b, 0, 1, LDS, tw);
-    fft_stage_pp<T, N, R2, R1, -1, N, THREADS>(b, a, 0, 1, LDS, tw);
-    for (int i = threadIdx.x; i < H2N * N; i += THREADS) {
-        const int m = i / N, x = i % N;
-        b[m * LDS + x] = pack(m, x, a[(2 * m) * LDS + x], a[(2 * m + 1) * LDS + x]);
-    }
-    __syncthreads();
-    afterPack();
-    // inverse along x on the N/2 packed rows (b -> a -> b)
-    fft_stage_pp<T, N, R1, 1, +1, N / 2, THREADS>(b, a, 0, LDS, 1, tw);
-    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS>(a, b, 0, LDS, 1, tw);
+    T* af = reinterpret_cast<T*>(a);
+    // rows [N/4, 3N/4): the pupil field -> b -> a
+    fft_stage_fn<T, N, R1, 1, -1, N / 2, THREADS, LO, HI>(
+        N / 4, tw, [&](int y, int x) { return pupil(y - N / 4, x - N / 4); },
+        [&](int y, int e, cx<T> v) { b[y * LDS + e] = v; });
     afterRows();
-    // split the packed rows: columns [0, N/2) of rows 2m and 2m+1 into a
-    for (int i = threadIdx.x; i < H2N * H2N; i += THREADS) {
-        const int m = i / H2N, k = i % H2N;
-        const cx<T> z = b[m * LDS + k];
-        const cx<T> zc = b[m * LDS + ((N - k) % N)];
-        // A = (z + conj zc)/2 ; B = (z - conj zc)/(2i)
-        a[(2 * m) * LDS + k] = mkc<T>((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y - zc.y));
-        a[(2 * m + 1) * LDS + k] = mkc<T>((T)0.5 * (z.y + zc.y), (T)0.5 * (zc.x - z.x));
-    }
-    __syncthreads();
-    // inverse along y on columns [0, N/2) (a -> b -> a)
-    fft_stage_pp<T, N, R1, 1, +1, N / 2, THREADS>(a, b, 0, 1, LDS, tw);
+    fft_stage_pp<T, N, R2, R1, -1, N / 2, THREADS>(b, a, N / 4, LDS, 1, tw);
+    // all columns (a -> b), then the last stage into the packed rows of a
+    fft_stage_pp<T, N, R1, 1, -1, N, THREADS, LO, HI>(a, b, 0, 1, LDS, tw);
+    afterCols1();
+    fft_stage_fn<T, N, R2, R1, -1, N, THREADS, 0, R2>(
+        0, tw, [&](int x, int e) { return b[e * LDS + x]; },
+        [&](int x, int e, cx<T> v) { af[(e >> 1) * 2 * LDS + 2 * x + (e & 1)] = elem(e, x, v); });
+    afterPack();
+    // inverse along x on the N/2 packed rows (a -> b -> a)
+    fft_stage_pp<T, N, R1, 1, +1, N / 2, THREADS>(a, b, 0, LDS, 1, tw);
+    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS>(b, a, 0, LDS, 1, tw);
+    // inverse along y on the columns [0, N/2), splitting the packed rows as they are loaded
+    fft_stage_fn<T, N, R1, 1, +1, N / 2, THREADS, 0, R1>(
+        0, tw,
+        [&](int k, int e) {
+            const cx<T> z = a[(e >> 1) * LDS + k];
+            const cx<T> zc = a[(e >> 1) * LDS + ((N - k) % N)];
+            return (e & 1) ? mkc<T>((T)0.5 * (z.y + zc.y), (T)0.5 * (zc.x - z.x))    // (z - conj zc)/2i
+                           : mkc<T>((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y - zc.y));   // (z + conj zc)/2
+        },
+        [&](int k, int e, cx<T> v) { b[e * LDS + k] = v; });
     midColumns();
     fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS>(b, a, 0, 1, LDS, tw);
 }
 
-// One image of a chunk: the OTF on the half plane (half_plane_core with pack = |X|^2),
-// folded into the chunk's accumulators.  On entry the phases of this image are staged in
-// b; phiNext (or null) is the next image's, fetched while this one is transformed.
+// One image of a chunk: the OTF on the half plane (half_plane_core with elem = |X|^2),
+// folded into the chunk's accumulators.  On entry the phases of this image are in phiBuf;
+// phiNext (or null) is the next image's, fetched into phiBuf once the row pass has read it.
 template <typename T, int N, int THREADS>
-__device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, const T* A, T c, int df,
+__device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phiBuf, const T* A, T c, int df,
                                            cx<T>* PF, cx<T>* X, cx<T>* S, const cx<T>* __restrict__ Dg,
                                            cx<T>* a, cx<T>* b, const cx<T>* tw, const cx<T>* oh,
-                                           T* acc, const int* hpos, const int* hidx, int nH) {
-    constexpr int LDS = Tile<N>::LDS;
-    constexpr int n = N / 2, n2 = n * n, N2 = N * N;
+                                           T* acc, const uint16_t* hpos, const int* hidx, int nH) {
+    constexpr int n = N / 2, N2 = N * N;
     static_assert(sizeof(cx<T>) == 8, "staging copies 8-byte elements");
     using St = Stage<N>;
     const T inv = (T)1 / (T)N2;
     __syncthreads();    // previous image's tiles fully consumed, staged phases visible
-    for (int q = threadIdx.x; q < n2; q += THREADS) {
-        const T amp = A[q];
-        cx<T> pf = mkc<T>(0, 0);
-        if (amp > (T)0) {
-            const T* ph = reinterpret_cast<const T*>(b + St::phi_slot(q >> 1));
-            T sn, cs;
-            sincos_t<T>(ph[q & 1], &sn, &cs);
-            pf = mkc<T>(amp * cs, amp * sn);
-        }
-        if (df) PF[q] = pf;
-        const int y = q / n, x = q % n;
-        a[(y + n / 2) * LDS + x + n / 2] = cscale<T>(pf, c);
-    }
-    __syncthreads();
-    const int nFirst = nH < St::kFirstPart ? nH : St::kFirstPart;
+    const int nFirst = nH < St::kPart ? nH : St::kPart;
     half_plane_core<T, N, THREADS>(
         a, b, tw,
-        [&](int m, int x, cx<T> v0, cx<T> v1) {
-            if (df) {
-                X[(2 * m) * N + x] = v0;
-                X[(2 * m + 1) * N + x] = v1;
+        [&](int y, int x) {
+            const int q = y * n + x;
+            const T amp = A[q];
+            cx<T> pf = mkc<T>(0, 0);
+            if (amp > (T)0) {
+                T sn, cs;
+                sincos_t<T>(phiBuf[q], &sn, &cs);
+                pf = mkc<T>(amp * cs, amp * sn);
             }
-            return mkc<T>(cnorm<T>(v0), cnorm<T>(v1));
+            if (df) PF[q] = pf;
+            return cscale<T>(pf, c);
+        },
+        [&](int e, int x, cx<T> v) {
+            if (df) X[e * N + x] = v;
+            return cnorm<T>(v);
         },
         [&] {
-            for (int h = threadIdx.x; h < nFirst; h += THREADS) cp_async8(a + St::dh_slot(h), Dg + h);
-            if (phiNext) stage_phi<T, N, THREADS>(b, phiNext);
+            if (phiNext) stage_phi<T, N, THREADS>(phiBuf, phiNext);
             cp_async_commit();
         },
         [&] {
-            for (int h = nFirst + threadIdx.x; h < nH; h += THREADS) cp_async8(a + St::dh_slot(h), Dg + h);
+            for (int h = threadIdx.x; h < nFirst; h += THREADS) cp_async8(a + St::dh_slot(h), Dg + h);
+            cp_async_commit();
+        },
+        [&] {
+            for (int h = nFirst + threadIdx.x; h < nH; h += THREADS) cp_async8(b + St::dh_slot(h), Dg + h);
             cp_async_commit();
         },
         [&] { cp_async_wait_all(); });
@@ -339,7 +331,8 @@ __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, const 
     }
     for (int h = threadIdx.x; h < nH; h += THREADS) {
         const cx<T> sv = cscale<T>(a[hpos[h]], inv);
-        const cx<T> r = csub<T>(a[St::dh_slot(h)], cmul<T>(oh[h], sv));
+        const cx<T> d = (h < St::kPart ? a : b)[St::dh_slot(h)];
+        const cx<T> r = csub<T>(d, cmul<T>(oh[h], sv));
         // R += |r|^2, Q += |S|^2, P' += conj(r) S
         acc[h] += cnorm<T>(r);
         acc[nH + h] += cnorm<T>(sv);
@@ -355,22 +348,24 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nH = e.hp.nH;
     // shared memory: two tiles | twiddles | reference object | accumulators (4 x nH) |
-    //                tile positions | pupil amplitude
+    //                pupil amplitude | phases of the image | tile positions (16-bit)
     cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* s2 = s + Tile<N>::ELEMS;
     cx<T>* tw = s2 + Tile<N>::ELEMS;
     cx<T>* oh = tw + N;
     T* acc = reinterpret_cast<T*>(oh + nH);
-    int* hpos = reinterpret_cast<int*>(acc + 4 * nH);
-    T* amp = reinterpret_cast<T*>(hpos + nH);
+    T* amp = acc + 4 * nH;
+    T* phiBuf = amp + n2;
+    uint16_t* hpos = reinterpret_cast<uint16_t*>(phiBuf + n2);
+    static_assert(Tile<N>::ELEMS <= 65536, "tile positions are 16-bit");
     const int nItems = *e.L.nEval;
     int item = blockIdx.x;
     if (item >= nItems) return;
     load_twiddles<T, N>(tw, e.k.tw);
-    for (int h = threadIdx.x; h < nH; h += THREADS) hpos[h] = e.hPos[h];
+    for (int h = threadIdx.x; h < nH; h += THREADS) hpos[h] = (uint16_t)e.hPos[h];
     for (int q = threadIdx.x; q < n2; q += THREADS) amp[q] = e.k.A[q];
     EvalItem it = e.L.eval[item];
-    stage_phi<T, N, THREADS>(s2, e.phi + ((size_t)it.p * e.k.I + it.first) * n2);
+    stage_phi<T, N, THREADS>(phiBuf, e.phi + ((size_t)it.p * e.k.I + it.first) * n2);
     cp_async_commit();
     cp_async_wait_all();
     int jj = 0;
@@ -393,7 +388,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
         const int j = it.first + jj;
         const size_t g = (size_t)it.p * e.k.I + j;
         const int ch = e.k.imgCh[j];
-        eval_image<T, N, THREADS>(phiNext, amp, e.k.otfNorm[ch], it.df, e.k.PF + g * n2, e.k.X + g * N2,
+        eval_image<T, N, THREADS>(phiNext, phiBuf, amp, e.k.otfNorm[ch], it.df, e.k.PF + g * n2, e.k.X + g * N2,
                                   e.k.S + g * N2, e.Dh + g * nH, s, s2, tw, oh, acc, hpos, e.hp.idx, nH);
         if (nextJj == 0) {
             __syncthreads();
@@ -479,25 +474,21 @@ __global__ void __launch_bounds__(THREADS, 1) k_fd_half(EvalParams<T> e) {
             }
             const T* Zm = kp.Z + (size_t)m * n2;
             __syncthreads();    // staged factors visible, previous mode's tiles consumed
-            for (int q = threadIdx.x; q < n2; q += THREADS) {
-                const T t = (T)hstep * Zm[q];
-                T sh, ch2, sn, cs;
-                sincos_t<T>(t * (T)0.5, &sh, &ch2);
-                sincos_t<T>(t, &sn, &cs);
-                const cx<T> ex = mkc<T>((T)-2 * sh * sh, sn);   // exp(i t) - 1
-                const int y = q / n, x = q % n;
-                a[(y + n / 2) * LDS + x + n / 2] = cmul<T>(pfs[q], ex);
-            }
-            __syncthreads();
             half_plane_core<T, N, THREADS>(
                 a, b, tw,
-                [&](int mm, int x, cx<T> v0, cx<T> v1) {
-                    const cx<T> x0 = Xg[(2 * mm) * N + x];
-                    const cx<T> x1 = Xg[(2 * mm + 1) * N + x];
-                    return mkc<T>((T)2 * (x0.x * v0.x + x0.y * v0.y) + cnorm<T>(v0),
-                                  (T)2 * (x1.x * v1.x + x1.y * v1.y) + cnorm<T>(v1));
+                [&](int y, int x) {
+                    const int q = y * n + x;
+                    const T t = (T)hstep * Zm[q];
+                    T sh, ch2, sn, cs;
+                    sincos_t<T>(t * (T)0.5, &sh, &ch2);
+                    sincos_t<T>(t, &sn, &cs);
+                    return cmul<T>(pfs[q], mkc<T>((T)-2 * sh * sh, sn));   // c PF (exp(i t) - 1)
                 },
-                [] {}, [] {}, [] {});
+                [&](int e, int x, cx<T> v) {
+                    const cx<T> x0 = Xg[e * N + x];
+                    return (T)2 * (x0.x * v.x + x0.y * v.y) + cnorm<T>(v);
+                },
+                [] {}, [] {}, [] {}, [] {});
             T dl = 0;
             for (int h = threadIdx.x; h < nH; h += THREADS) {
                 const T Q = hq[h];

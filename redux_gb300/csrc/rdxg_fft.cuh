@@ -290,6 +290,40 @@ __device__ __forceinline__ void fft_stage_pp(const cx<T>* __restrict__ src, cx<T
     __syncthreads();
 }
 
+// The same stage with the element loads and stores supplied by the caller: ld(line, e)
+// returns element e of a line, st(line, e, v) stores output element e.  Used to fold
+// element-wise work into the first or last stage of a pass.
+template <typename T, int N, int R, int NS, int DIR, int LINES, int THREADS, int RLO, int RHI, typename LD,
+          typename ST>
+__device__ __forceinline__ void fft_stage_fn(int line0, const cx<T>* tw, LD ld, ST st) {
+    constexpr int BF = N / R;
+    constexpr int TOTAL = LINES * BF;
+    constexpr int TWS = N / (NS * R);
+#pragma unroll 2
+    for (int b = threadIdx.x; b < TOTAL; b += THREADS) {
+        const int line = line0 + b % LINES;
+        const int j = b / LINES;
+        const int k = j % NS;
+        cx<T> v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = (r >= RLO && r < RHI) ? ld(line, j + r * BF) : mkc<T>(0, 0);
+        if (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                if (r < RLO || r >= RHI) continue;
+                cx<T> w = tw[r * k * TWS];
+                if (DIR > 0) w.y = -w.y;
+                v[r] = cmul<T>(v[r], w);
+            }
+        }
+        Dft<R, DIR, T>::run(v);
+        const int idxD = (j / NS) * NS * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) st(line, idxD + r * NS, v[r]);
+    }
+    __syncthreads();
+}
+
 // 2-D transform in tile a (result in a), b is scratch of the same shape.
 template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED>
 __device__ __forceinline__ void fft2d_pp(cx<T>* a, cx<T>* b, const cx<T>* tw) {

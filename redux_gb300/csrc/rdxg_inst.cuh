@@ -60,8 +60,11 @@ void Launcher<T, N>::fd(const KParams<T>& kp, int grid, int M, cudaStream_t st) 
 
 template <typename T, int N>
 size_t EvalLauncher<T, N>::smem(int M, int nH) {
+    (void)M;
+    // two tiles | twiddles | reference object | accumulators (4 x nH) | pupil amplitude |
+    // phases of the image | tile positions (16-bit)
     return (size_t)(2 * Tile<N>::ELEMS + N + nH) * sizeof(cx<T>) + (size_t)4 * nH * sizeof(T) +
-           (size_t)nH * sizeof(int) + (size_t)(N / 2) * (N / 2) * sizeof(T) + (size_t)M * sizeof(T) + 16;
+           (size_t)2 * (N / 2) * (N / 2) * sizeof(T) + (size_t)nH * sizeof(uint16_t) + 16;
 }
 
 #define RDXG_NPT_SWITCH(npt, CALL) \
