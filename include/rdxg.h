@@ -162,6 +162,15 @@ int rdxg_metric_noalloc(rdxg_solver* h, const double* alpha, double* metric);
 int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, int32_t method,
                   double* grad, double* metric);
 
+/* Restored objects of every patch at alpha [P][I][M]: Object::restorePatch
+ * (object.cpp:278-334) for the object image, with the Scharmer filter (image/utils.cpp:
+ * 334-392) unless no_filter (RF_NO_FILTER); FP64 on the device.  frequency_cutoff: [nObj]
+ * Object::frequencyCutoff (pupil.cpp:87; the filter cuts at 0.9 of it).  objects:
+ * [P][nObj][patch_size][patch_size] float32 (ObjectData::img).  The PSF, convolved-object and
+ * residual outputs and the fitted-plane re-addition of the reference are not produced. */
+int rdxg_restore(rdxg_solver* h, const double* alpha, const double* frequency_cutoff, int32_t no_filter,
+                 float* objects);
+
 /* Full per-patch solve (Solver::run, solver.cpp:330-580) for every loaded patch.
  * alpha_out: [P][I][M]; reports: [P]; metrics: [P][max_metrics] or NULL. */
 int rdxg_solve(rdxg_solver* h, const rdxg_solve_params* params, double* alpha_out,

@@ -79,6 +79,8 @@ def lib():
         L.orc_reorder_into.argtypes = [f64p, C.c_int, C.c_int, f64p, C.c_int, C.c_int, C.c_int]
         L.orc_cons_apply.argtypes = [C.c_void_p, f64p, f64p]
         L.orc_cons_reverse_add.argtypes = [C.c_void_p, f64p, f64p, f64p]
+        L.orc_restore.restype = C.c_int
+        L.orc_restore.argtypes = [C.c_void_p, f64p, f64p, C.c_int, f64p]
         _LIB = L
     return _LIB
 
@@ -250,6 +252,13 @@ class OraclePatch:
         t = np.zeros(2 * self.I)
         lib().orc_get_shifts(self.h, s, t)
         return s.reshape(self.I, 2), t.reshape(self.I, 2)
+
+    def restore(self, alpha, frequency_cutoff, no_filter=False):
+        """Restored objects [nObj][ps][ps] at alpha (Object::restorePatch)."""
+        fc = np.ascontiguousarray(np.broadcast_to(np.asarray(frequency_cutoff, np.float64), (self.nObj,)))
+        out = np.zeros(self.nObj * self.job.patch_size * self.job.patch_size)
+        lib().orc_restore(self.h, np.ascontiguousarray(alpha, np.float64).ravel(), fc, int(bool(no_filter)), out)
+        return out.reshape(self.nObj, self.job.patch_size, self.job.patch_size)
 
     def stats(self):
         m, s, n = np.zeros(self.I), np.zeros(self.I), np.zeros(self.I)

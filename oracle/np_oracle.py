@@ -84,3 +84,59 @@ class NumpyModel:
                 dphi = -(4.0 * c * c / j.patch_size ** 2) * np.imag(np.conj(PF[i]) * conv) * (A > 0)
                 g[i] = w * np.tensordot(j.modes, dphi, 2)
         return g
+
+
+# ---------------------------------------------------------------------------------------
+# Restoration (Object::restorePatch, object.cpp:278-334; ScharmerFilter, smooth,
+# connectedRegion in image/utils.cpp:49-57, 295-392), an independent numpy statement used
+# to cross-check the C restatement.
+# ---------------------------------------------------------------------------------------
+def smooth(d, nY, nX):
+    """Mean over the clipped window [y-nY, y+nY) x [x-nX, x+nX) (upper bounds exclusive)."""
+    ny, nx = d.shape
+    ii = np.zeros((ny + 1, nx + 1))
+    ii[1:, 1:] = np.cumsum(np.cumsum(d, 0), 1)
+    y = np.arange(ny)[:, None]
+    x = np.arange(nx)[None, :]
+    yl, yh = np.maximum(y - nY, 0), np.minimum(y + nY, ny)
+    xl, xh = np.maximum(x - nX, 0), np.minimum(x + nX, nx)
+    tot = ii[yh, xh] - ii[yl, xh] - ii[yh, xl] + ii[yl, xl]
+    return tot / ((yh - yl) * (xh - xl))
+
+
+def scharmer_filter(data, q2, noise_power, frequency_cutoff):
+    from scipy import ndimage
+    N = data.shape[0]
+    with np.errstate(divide="ignore"):
+        pt = (noise_power * N * N) / smooth(np.abs(data) ** 2 * q2, 1, 1)
+    mirror = pt[(-np.arange(N)) % N][:, (-np.arange(N)) % N]
+    rr = np.maximum(1.0 - 0.5 * (mirror + pt), 0.0)
+    rr[rr < 0.2] = 0.0
+    rr[rr > 1.0] = 1.0
+    rr[N // 2, N // 2] = 1.0
+    lab, _ = ndimage.label(rr > 0.0, structure=[[0, 1, 0], [1, 1, 1], [0, 1, 0]])
+    rr = rr * (lab == lab[N // 2, N // 2])
+    rr = smooth(rr, 4, 4)
+    y, x = np.mgrid[0:N, 0:N]
+    out = data * rr
+    out[(y - N // 2) ** 2 + (x - N // 2) ** 2 > frequency_cutoff ** 2] = 0.0
+    return out
+
+
+def restore(D, S, noise, image_object, obj, frequency_cutoff, ps, support, no_filter=False):
+    """Restored object obj from centred image transforms D and OTFs S [I][N][N]; sums over
+    the OTF support (flat centred indices) only, as SubImage::restore."""
+    idx = [j for j in range(len(image_object)) if image_object[j] == obj]
+    mask = np.zeros(D[0].size, bool)
+    mask[np.asarray(support)] = True
+    mask = mask.reshape(D[0].shape)
+    num = sum(np.conj(D[j]) * S[j] for j in idx) * mask
+    den = sum(np.abs(S[j]) ** 2 for j in idx) * mask
+    nv = float(np.mean([noise[j] ** 2 for j in idx]))
+    O = np.where(den != 0.0, np.conj(num) / np.where(den != 0.0, den, 1.0), 0.0)
+    if not no_filter:
+        O = scharmer_filter(O, den, nv, 0.9 * frequency_cutoff)
+    N = O.shape[0]
+    img = np.real(np.fft.ifft2(np.fft.ifftshift(O)))
+    off = (N - ps) // 2
+    return img[off:off + ps, off:off + ps]

@@ -1384,3 +1384,135 @@ int orc_reorder_into(const double* in, int inY, int inX, double* out, int outY, 
     }
     return 0;
 }
+
+/* ---------------------------------------------------------------------------------------
+ * Restoration: Object::restorePatch (object.cpp:278-334) for the restored object only, with
+ * SubImage::restore (subimage.cpp:242-256) and redux::image::ScharmerFilter, smooth and
+ * connectedRegion (image/utils.cpp:49-57, 295-392).
+ * ------------------------------------------------------------------------------------- */
+
+/* smooth (utils.cpp:304-328): mean over [y-nY, y+nY) x [x-nX, x+nX), clipped to the array;
+ * the window is asymmetric (upper bounds exclusive), as in the reference */
+static void smooth_d(double* d, int ny, int nx, int nY, int nX, double* tmp) {
+    for (int y = 0; y < ny; ++y) {
+        const int yl = y - nY > 0 ? y - nY : 0, yh = y + nY < ny ? y + nY : ny;
+        for (int x = 0; x < nx; ++x) {
+            const int xl = x - nX > 0 ? x - nX : 0, xh = x + nX < nx ? x + nX : nx;
+            double t = 0;
+            int cnt = 0;
+            for (int yy = yl; yy < yh; ++yy)
+                for (int xx = xl; xx < xh; ++xx) { t += d[(long)yy * nx + xx]; cnt++; }
+            tmp[(long)y * nx + x] = t / cnt;
+        }
+    }
+    memcpy(d, tmp, sizeof(double) * (size_t)ny * nx);
+}
+
+/* connectedRegion (utils.cpp:49-57, 295-299; utils.hpp:103-108): keeps the 4-connected
+ * region of points > threshold that contains the start point (which is always kept); the
+ * reference recurses, here an explicit stack visits the same set */
+static void connected_region(double* d, int ny, int nx, int y0, int x0, double threshold) {
+    const long n = (long)ny * nx;
+    uint8_t* mask = (uint8_t*)xcalloc((size_t)n, 1);
+    int32_t* stack = (int32_t*)xcalloc((size_t)n * 4 + 4, sizeof(int32_t));
+    long top = 0;
+    stack[top++] = y0 * nx + x0;
+    while (top > 0) {
+        const int32_t c = stack[--top];
+        const int y = c / nx, x = c % nx;
+        if (mask[c]) continue;
+        if (!((y == y0 && x == x0) || d[c] > threshold)) continue;
+        mask[c] = 1;
+        if (y + 1 < ny) stack[top++] = c + nx;
+        if (y - 1 >= 0) stack[top++] = c - nx;
+        if (x + 1 < nx) stack[top++] = c + 1;
+        if (x - 1 >= 0) stack[top++] = c - 1;
+    }
+    for (long i = 0; i < n; ++i) d[i] *= mask[i];
+    free(stack);
+    free(mask);
+}
+
+/* ScharmerFilter (utils.cpp:334-392) on a centred N x N transform */
+static void scharmer_filter(cplx* data, const double* q2, int N, double noise_power, double frequency_cutoff) {
+    const long N2 = (long)N * N;
+    const double hi = 1.0, lo = 0.2;
+    const double noiseFactor = noise_power * N * N;
+    double* pt = (double*)xcalloc((size_t)N2, sizeof(double));
+    double* rr = (double*)xcalloc((size_t)N2, sizeof(double));
+    double* tmp = (double*)xcalloc((size_t)N2, sizeof(double));
+    for (long i = 0; i < N2; ++i) pt[i] = (creal(data[i]) * creal(data[i]) + cimag(data[i]) * cimag(data[i])) * q2[i];
+    smooth_d(pt, N, N, 1, 1, tmp);
+    for (long i = 0; i < N2; ++i) pt[i] = noiseFactor / pt[i];
+    /* rr(y, x) = max(1 - (pt(-y, -x) + pt(y, x)) / 2, 0), indices modulo N */
+    for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+            const double m = pt[(long)((N - y) % N) * N + (N - x) % N];
+            const double v = 1.0 - 0.5 * (m + pt[(long)y * N + x]);
+            rr[(long)y * N + x] = v > 0.0 ? v : 0.0;
+        }
+    for (long i = 0; i < N2; ++i) {
+        if (rr[i] < lo) rr[i] = 0.0;
+        if (rr[i] > hi) rr[i] = 1.0;
+    }
+    rr[(long)(N / 2) * N + N / 2] = 1.0;   /* DC gain = 1 */
+    connected_region(rr, N, N, N / 2, N / 2, 0.0);
+    smooth_d(rr, N, N, 4, 4, tmp);
+    const double fc2 = frequency_cutoff * frequency_cutoff;
+    for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+            const double r2 = (double)(y - N / 2) * (y - N / 2) + (double)(x - N / 2) * (x - N / 2);
+            if (r2 > fc2) data[(long)y * N + x] = 0.0;
+            else data[(long)y * N + x] *= rr[(long)y * N + x];
+        }
+    free(tmp);
+    free(rr);
+    free(pt);
+}
+
+/* Restored objects at alpha: out [nObj][ps][ps]; frequency_cutoff [nObj] (Object::
+ * frequencyCutoff; the filter uses 0.9 of it); no_filter: RF_NO_FILTER */
+int orc_restore(orc_patch* p, const double* alpha, const double* frequency_cutoff, int no_filter, double* out) {
+    const int N = p->N;
+    const long N2 = p->N2;
+    apply_alpha(p, alpha);
+    cplx* obj = (cplx*)xcalloc((size_t)N2, sizeof(cplx));
+    double* den = (double*)xcalloc((size_t)N2, sizeof(double));
+    cplx* work = (cplx*)xcalloc((size_t)2 * N, sizeof(cplx));
+    for (int o = 0; o < p->nObj; ++o) {
+        memset(obj, 0, sizeof(cplx) * (size_t)N2);
+        memset(den, 0, sizeof(double) * (size_t)N2);
+        double noiseVar = 0;
+        int count = 0;
+        for (int j = 0; j < p->nImg; ++j) {
+            if (p->imgObj[j] != o) continue;
+            const cplx* S = p->OTF + (long)j * N2;
+            const cplx* Dv = p->D + (long)j * N2;
+            for (int k = 0; k < p->nOtfSup; ++k) {
+                const int32_t u = p->otfSup[k];
+                den[u] += creal(S[u]) * creal(S[u]) + cimag(S[u]) * cimag(S[u]);
+                obj[u] += conj(Dv[u]) * S[u];
+            }
+            noiseVar += p->statNoise[j] * p->statNoise[j];
+            count++;
+        }
+        if (!count) continue;
+        noiseVar /= count;
+        for (long i = 0; i < N2; ++i) {
+            obj[i] = conj(obj[i]);
+            obj[i] = den[i] != 0.0 ? obj[i] / den[i] : 0.0;      /* Array::safeDivide, eps = 0 */
+        }
+        if (!no_filter) scharmer_filter(obj, den, N, noiseVar, 0.9 * frequency_cutoff[o]);
+        /* ift: un-centre, backward transform, real part / N^2 */
+        reorder_c(obj, N, N, (cplx*)p->scr[0].tmpc);
+        fft2(&p->planN, &p->planN, obj, +1, work);
+        const int off = (N - p->ps) / 2;
+        for (int y = 0; y < p->ps; ++y)
+            for (int x = 0; x < p->ps; ++x)
+                out[((long)o * p->ps + y) * p->ps + x] = creal(obj[(long)(y + off) * N + x + off]) / (double)N2;
+    }
+    free(work);
+    free(den);
+    free(obj);
+    return 0;
+}

@@ -17,7 +17,7 @@ EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "r
             "rdxg_set_patches", "rdxg_set_patches_device", "rdxg_metric", "rdxg_gradient",
             "rdxg_solve", "rdxg_solve_async", "rdxg_fetch_results", "rdxg_last_launch_count",
             "rdxg_debug_copy", "rdxg_cg_minimize", "rdxg_profile_kernels", "rdxg_metric_with_reference",
-            "rdxg_metric_noalloc")
+            "rdxg_metric_noalloc", "rdxg_restore")
 
 
 class Geometry(C.Structure):
@@ -78,6 +78,7 @@ def load(path: str = LIB_PATH):
     L.rdxg_metric.argtypes = [vp, vp, vp]
     L.rdxg_metric_with_reference.argtypes = [vp, vp, vp, vp]
     L.rdxg_metric_noalloc.argtypes = [vp, vp, vp]
+    L.rdxg_restore.argtypes = [vp, vp, vp, C.c_int32, vp]
     L.rdxg_gradient.argtypes = [vp, vp, vp, C.c_int32, vp, vp]
     L.rdxg_solve.argtypes = [vp, C.POINTER(SolveParams), vp, vp, vp]
     L.rdxg_solve_async.argtypes = [vp, C.POINTER(SolveParams)]

@@ -67,6 +67,9 @@ struct rdxg_solver {
     rdxg_solve_params lastParams{};
     // fused evaluation path (FP32, N <= 88)
     bool fused = false;
+    double* dRestore = nullptr;      // restoration scratch (allocated on first use)
+    double* dFc = nullptr;           // [nObj] frequency cutoffs of the restoration
+    float* dRestoreOut = nullptr;    // [P][nObj][ps][ps] restored objects
     bool fusedFd = false;     // half-plane finite-difference gradient (fits in shared memory)
     int npt = 0, chunk = 6, chunksPerPatch = 0, nH = 0, evalGrid = 0, reduceGrid = 0, numSMs = 0;
     std::vector<int32_t> objChunk0, hIdx, hPos;
@@ -837,6 +840,45 @@ int rdxg_metric_with_reference(rdxg_solver* h, const double* alpha_ref, const do
         return r;
     if ((r = upload_alpha<float>(h, alpha)) || (r = fused_pass(h, REQ_F, 0))) return r;
     return metric_from_objects(h, metric);
+}
+
+int rdxg_restore(rdxg_solver* h, const double* alpha, const double* frequency_cutoff, int32_t no_filter,
+                 float* objects) {
+    if (!h || !alpha || !frequency_cutoff || !objects) return RDXG_ERR_ARG;
+    if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
+    int r = h->fp64 ? upload_alpha<double>(h, alpha) : upload_alpha<float>(h, alpha);
+    if (r) return r;
+    // the OTFs at alpha on the full plane: a gradient-type evaluation keeps them
+    if ((r = set_requests(h, REQ_DF, GM_VOGEL, h->M))) return r;
+    if (h->fused) {
+        if ((r = fused_pass(h, REQ_DF, 1))) return r;
+    } else {
+        with_size(h->N, h->fp64, [&](auto L, auto t) {
+            using T = decltype(t);
+            KParams<T> kp = make_kparams<T>(h);
+            decltype(L)::forward(kp, h->P * h->I, h->stream);
+        });
+    }
+    const size_t N2 = (size_t)h->N * h->N;
+    if (!h->dRestore) {
+        if ((r = dalloc_t(h, &h->dRestore, (size_t)h->Pmax * h->nObj * kRestoreScratch * N2)) ||
+            (r = dalloc_t(h, &h->dFc, (size_t)h->nObj)))
+            return r;
+    }
+    CK(h, cudaMemcpyAsync(h->dFc, frequency_cutoff, h->nObj * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (!h->dRestoreOut && (r = dalloc_t(h, &h->dRestoreOut, (size_t)h->Pmax * h->nObj * h->ps * h->ps))) return r;
+    RestoreArgs ra{h->dFc, no_filter ? 1 : 0, h->dRestore, h->dRestoreOut};
+    cudaError_t ce = cudaSuccess;
+    with_size(h->N, h->fp64, [&](auto L, auto t) {
+        using T = decltype(t);
+        KParams<T> kp = make_kparams<T>(h);
+        ce = decltype(L)::restore(kp, ra, h->P * h->nObj, h->stream);
+    });
+    if (ce != cudaSuccess) { h->err = std::string("restore: ") + cudaGetErrorString(ce); return RDXG_ERR_CUDA; }
+    CK(h, cudaMemcpyAsync(objects, h->dRestoreOut, (size_t)h->P * h->nObj * h->ps * h->ps * sizeof(float),
+                          cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return RDXG_OK;
 }
 
 int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, int32_t method, double* grad,

@@ -59,6 +59,13 @@ void Launcher<T, N>::fd(const KParams<T>& kp, int grid, int M, cudaStream_t st) 
 }
 
 template <typename T, int N>
+cudaError_t Launcher<T, N>::restore(const KParams<T>& kp, const RestoreArgs& ra, int nBlocks, cudaStream_t st) {
+    const int sm = (int)((size_t)(kRestoreBand * Tile<N>::LDS + N) * sizeof(cx<double>));
+    k_restore<T, N, THREADS><<<nBlocks, THREADS, sm, st>>>(kp, ra);
+    return cudaGetLastError();   // the launch only (no device synchronisation)
+}
+
+template <typename T, int N>
 size_t EvalLauncher<T, N>::smem(int M, int nH) {
     (void)M;
     // two tiles | twiddles | reference object | accumulators (4 x nH) | pupil amplitude |

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "rdxg_cg.cuh"
+#include "rdxg_restore.cuh"
 
 namespace rdxg {
 
@@ -19,6 +20,7 @@ struct Launcher {
     static void forward(const KParams<T>& kp, int nImg, cudaStream_t st);
     static void adjoint(const KParams<T>& kp, int grid, int kind, cudaStream_t st);   // grid-strides over the work list
     static void fd(const KParams<T>& kp, int grid, int M, cudaStream_t st);
+    static cudaError_t restore(const KParams<T>& kp, const RestoreArgs& ra, int nBlocks, cudaStream_t st);
 };
 
 constexpr int kAccumThreads = 256;

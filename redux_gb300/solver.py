@@ -146,6 +146,17 @@ class Solver:
         self._check(_lib.load().rdxg_metric_noalloc(self.h, _lib.ptr(a), _lib.ptr(out)), "rdxg_metric_noalloc")
         return out
 
+    def restore(self, alpha, frequency_cutoff, no_filter: bool = False) -> np.ndarray:
+        """Restored objects [P][nObj][ps][ps] at alpha (Object::restorePatch)."""
+        a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
+        nObj = self.job.n_objects
+        fc = np.ascontiguousarray(np.broadcast_to(np.asarray(frequency_cutoff, np.float64), (nObj,)))
+        ps = self.job.patch_size
+        out = np.zeros((self.P, nObj, ps, ps), np.float32)
+        self._check(_lib.load().rdxg_restore(self.h, _lib.ptr(a), _lib.ptr(fc), int(bool(no_filter)), _lib.ptr(out)),
+                    "rdxg_restore")
+        return out
+
     def gradient(self, alpha, method: str = "vogel", enabled=None):
         a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
         g = np.zeros((self.P, self.I, self.M))

@@ -222,3 +222,33 @@ def test_staged_solve_with_reshifts(w0):
     sg, so = s.debug("shifts")[0], op.shifts()[0]
     assert np.any(so != 0)
     np.testing.assert_array_equal(sg, so)
+
+
+# restored object within 1e-4 relative of the FP64 oracle (relative to the image's peak)
+TOL_RESTORE = 1e-4
+
+
+@pytest.mark.parametrize("cfg", [0, 2])
+def test_restore(cfg):
+    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    s = _solver(w)
+    fc = w.job.otf_size / 2.0
+    a = w.patches.alpha_true
+    out = s.restore(a, fc)
+    for p in range(a.shape[0]):
+        ref = _oracle(w, p).restore(a[p], fc)
+        for o in range(w.job.n_objects):
+            err = np.abs(out[p, o] - ref[o]).max() / np.abs(ref[o]).max()
+            assert err <= TOL_RESTORE, (p, o, err)
+
+
+def test_restore_fp64_with_and_without_filter(w0):
+    s = _solver(w0, precision="fp64")
+    fc = w0.job.otf_size / 2.0
+    a = w0.patches.alpha_true
+    op = _oracle(w0)
+    for nf in (False, True):
+        out = s.restore(a, fc, no_filter=nf)
+        ref = op.restore(a[0], fc, no_filter=nf)
+        err = np.abs(out[0, 0] - ref[0]).max() / np.abs(ref[0]).max()
+        assert err <= 1e-6, (nf, err)

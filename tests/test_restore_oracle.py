@@ -1,0 +1,39 @@
+"""Restoration (Object::restorePatch with the Scharmer filter): the C restatement against an
+independent numpy statement of the same steps (CPU only)."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import np_oracle
+from tests.conftest import workload
+
+
+@pytest.mark.parametrize("cfg", [0, 2])
+def test_restore_c_vs_numpy(cfg):
+    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    op = oracle.OraclePatch(w.job)
+    fg = None if w.patches.fixed_gamma is None else w.patches.fixed_gamma[0]
+    op.set_images(w.patches.cutouts[0], None, fg)
+    a = w.patches.alpha_true[0]
+    fc = w.job.otf_size / 2.0
+    filt = op.restore(a, fc)
+    raw = op.restore(a, fc, no_filter=True)
+    op.metric(a)
+    D, S = op.D(), op.otf()
+    noise = op.stats()[2]
+    for o in range(w.job.n_objects):
+        args = (D, S, noise, w.job.img_object, o, fc, w.job.patch_size, w.job.support.otf_support)
+        ref = np_oracle.restore(*args)
+        ref_raw = np_oracle.restore(*args, no_filter=True)
+        # the filter's smoothing is summed directly in C and by an integral image in numpy
+        assert np.abs(filt[o] - ref).max() <= 1e-9 * np.abs(ref).max()
+        assert np.abs(raw[o] - ref_raw).max() <= 1e-12 * np.abs(ref_raw).max()
+
+
+def test_smooth_window_is_the_references():
+    # smooth(d, 1, 1) averages [y-1, y+1) x [x-1, x+1): the pixel and its upper/left neighbours
+    d = np.arange(16.0).reshape(4, 4)
+    s = np_oracle.smooth(d, 1, 1)
+    assert s[0, 0] == 0.0
+    assert s[1, 1] == (d[0, 0] + d[0, 1] + d[1, 0] + d[1, 1]) / 4
+    assert s[3, 0] == (d[2, 0] + d[3, 0]) / 2
