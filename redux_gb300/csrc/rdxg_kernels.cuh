@@ -349,6 +349,8 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
     const cx<T>* Oo = kp.O + po * N2;
     const cx<T>* Dg = kp.D + (size_t)g * N2;
     const cx<T>* Sg = kp.S + (size_t)g * N2;
+    // unrolled so that each thread has several iterations' global loads in flight
+#pragma unroll 8
     for (int i = threadIdx.x; i < N2; i += THREADS) {
         const int y = i / N, x = i % N;                 // un-centred (lag) position
         const int c = ((y + N / 2) % N) * N + (x + N / 2) % N;
@@ -364,6 +366,7 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
     fft2d<T, N, -1, THREADS, false>(s, tw);
     (void)s2;
     const cx<T>* X = kp.X + (size_t)g * N2;
+#pragma unroll 8
     for (int i = threadIdx.x; i < N2; i += THREADS) {
         const int y = i / N, x = i % N;
         s[y * LDS + x] = cmul<T>(s[y * LDS + x], X[i]);
@@ -372,6 +375,7 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
     if constexpr (PP) fft2d_pp_out_rows_pruned<T, N, +1, THREADS>(s, s2, tw);
     else fft2d_out_rows_pruned<T, N, +1, THREADS>(s, tw);
     const cx<T>* PF = kp.PF + (size_t)g * n2;
+#pragma unroll 4
     for (int q = threadIdx.x; q < n2; q += THREADS) {
         const int y = q / n, x = q % n;
         const cx<T> U = s[(y + n / 2) * LDS + x + n / 2];
@@ -400,6 +404,7 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
         if (m < mc) {
             const T* Zm = kp.Z + (size_t)m * n2;
             T part = 0;
+#pragma unroll 8
             for (int q = lane; q < n2; q += 32) part += v[q] * Zm[q];
             acc = (double)part;
 #pragma unroll
