@@ -94,8 +94,8 @@ class ClockSampler:
 
 def workload(patches, frames, iterations):
     from redux_gb300 import synth
-    cache = os.path.join("/tmp", f"rdxg_bench_w2_{patches}_{frames}.npz")
-    job = synth.make_job(88, 36, synth.LAYOUT_WB_NB(frames))
+    cache = os.path.join("/tmp", f"rdxg_bench_w2kl_{patches}_{frames}.npz")
+    job = synth.make_job(88, 36, synth.LAYOUT_WB_NB(frames), basis="kl")
     if os.path.exists(cache):
         d = np.load(cache)
         cut = d["cutouts"]
@@ -274,7 +274,7 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_dev, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (FP64 sums and CG scalars)", "data": "synthetic",
-            "config": {"workload": f"{P} patches 88x88, 36 modes, 3ch x {args.frames} frames, D/r0=15, "
+            "config": {"workload": f"{P} patches 88x88, 36 KL modes, 3ch x {args.frames} frames, D/r0=15, "
                                    f"{args.iterations} CG iterations, all modes at once",
                        "patches_per_gpu": P, "iterations": args.iterations,
                        "l2": "inputs larger than L2 (D, OTF: 2 x 500 MB per batch)",

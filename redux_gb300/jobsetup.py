@@ -242,6 +242,107 @@ def zernike_modeset(mode_list, n_pixels: int, radius: float, wavelength: float,
     return ModeSet(out, list(mode_list), tx, ty, atm, J)
 
 
+@dataclass
+class KLMode:
+    covariance: float        # eigenvalue of the Zernike covariance block
+    weights: list            # [(Noll index, coefficient)]
+
+
+def kl_expansion(first: int, last: int) -> dict:
+    """Zernike::karhunenLoeveExpansion (src/lib/image/zernike.cpp:367-479).
+
+    The Zernike modes first..last are reordered so that modes coupled by the Noll
+    covariance form contiguous blocks (the reference's exchange pass); each block's
+    covariance matrix is decomposed (singular values in decreasing order, as
+    gsl_linalg_SV_decomp returns them); KL mode i takes the singular vector whose column
+    is i's position within its block, signed so that its largest coefficient is
+    positive.  Returns {i: KLMode}."""
+    cov = zernike_covariance
+    mapping = {i: i for i in range(first, last + 1)}
+    for i in range(first, last):
+        cov1 = cov(mapping[i], mapping[last])
+        for j in range(last - 1, i, -1):
+            cov2 = cov(mapping[i], mapping[j])
+            if cov2 == 0.0 and cov1 != 0.0:
+                mapping[j], mapping[j + 1] = mapping[j + 1], mapping[j]
+            else:
+                cov1 = cov2
+    reverse = {v: k for k, v in mapping.items()}
+    values = {}
+    for k in range(first + 1, last + 1):
+        values[k] = cov(mapping[k - 1], mapping[k])
+    blocks = []
+    n = first
+    while n <= last:
+        b0 = n
+        n += 1
+        while n <= last and values[n] != 0.0:
+            n += 1
+        blocks.append((b0, n - 1))
+    vectors, singular = {}, {}
+    for b0, b1 in blocks:
+        size = b1 - b0 + 1
+        C = np.array([[cov(mapping[i], mapping[j]) for j in range(b0, b1 + 1)] for i in range(b0, b1 + 1)])
+        if size > 1:
+            U, S, _ = np.linalg.svd(C)
+        else:
+            U, S = np.ones((1, 1)), np.array([C[0, 0]])
+        vectors[b0] = U
+        for k in range(size):
+            singular[b0 + k] = float(S[k])
+    out = {}
+    for i in range(first, last + 1):
+        im = reverse[i]
+        b0, b1 = next(b for b in blocks if b[0] <= im <= b[1])
+        U = vectors[b0]
+        col = U[:, im - b0]
+        big = int(np.argmax(np.abs(col)))
+        sign = -1.0 if col[big] < 0 else 1.0
+        out[i] = KLMode(singular[im], [(mapping[b0 + m], sign * float(col[m])) for m in range(b1 - b0 + 1)])
+    return out
+
+
+def kl_modeset(mode_list, n_pixels: int, radius: float, wavelength: float, jacobian_scale: float,
+               kl_first: int = 2, kl_last: int = 2000, cutoff: float = 1e-3, angle: float = 0.0) -> ModeSet:
+    """ModeSet::generate for Karhunen-Loeve modes (src/lib/momfbd/modes.cpp:158-197, 399-437):
+    tilts (Noll 2, 3) stay Zernike; KL mode i is the sum of the normalised Zernike modes
+    with |weight| >= cutoff (SVD_REG, default 1e-3), normalised over the pupil; then the same
+    getNorms/normalize(1/wavelength) and Jacobian as the Zernike set."""
+    pupil, _ = make_pupil(n_pixels, radius)
+    sup = pupil_support(pupil)
+    kle = kl_expansion(kl_first, kl_last)
+    zcache = {}
+
+    def z(j):
+        if j not in zcache:
+            zcache[j] = zernike(j, n_pixels, radius, angle)
+        return zcache[j]
+
+    raw, atm = [], []
+    for i in mode_list:
+        if i in (2, 3):
+            raw.append(z(i))
+            atm.append(math.sqrt(zernike_covariance(i, i)))
+            continue
+        k = kle[i]
+        m = np.zeros((n_pixels, n_pixels))
+        for j, c in k.weights:
+            if abs(c) >= cutoff:
+                m += c * z(j)
+        nrm = math.sqrt(float(sup.area) / float((m * m * pupil)[pupil > 0].sum()))
+        raw.append(m * nrm)
+        atm.append(math.sqrt(k.covariance))
+    raw = np.stack(raw)
+    out = np.empty_like(raw)
+    for i in range(raw.shape[0]):
+        nrm = math.sqrt(float((raw[i] * raw[i] * pupil)[pupil > 0].sum()) / sup.area)
+        out[i] = raw[i] * ((1.0 / wavelength) / nrm)
+    tx = list(mode_list).index(2) if 2 in mode_list else -1
+    ty = list(mode_list).index(3) if 3 in mode_list else -1
+    J = measure_jacobian(out, pupil, jacobian_scale)
+    return ModeSet(out, list(mode_list), tx, ty, np.array(atm), J)
+
+
 def measure_jacobian(modes: np.ndarray, pupil: np.ndarray, scale: float) -> np.ndarray:
     """ModeSet::measureJacobian (src/lib/momfbd/modes.cpp:464-512); returns J_T_xy."""
     fits = []

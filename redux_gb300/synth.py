@@ -53,6 +53,10 @@ class Job:
     cutout_size: int
     channel_div_pv: np.ndarray   # (C,) diversity defocus of each channel, waves PV
     wavelength: float = WAVELENGTH
+    basis: str = "zernike"       # "zernike" or "kl"
+    atm_var: np.ndarray = None   # (M,) Kolmogorov variance of each mode at D/r0 = 1
+    kl_weights: dict = None      # KL mode -> [(Noll index, weight)] (basis "kl")
+    kl_cutoff: float = 1e-3
 
     @property
     def n_images(self):
@@ -108,25 +112,6 @@ def _pupil_cached(n, radius):
     return _PUPILS[key]
 
 
-def _psf_kernel(alpha_rad, mode_list, phi_fixed_rad_fn, K):
-    """PSF on a K x K grid at critical sampling, from the analytic phase on a K/2 pupil."""
-    n = K // 2
-    radius = n / 2.0
-    pupil = _pupil_cached(n, radius)
-    phi = np.zeros((n, n))
-    for a, j in zip(alpha_rad, mode_list):
-        if a != 0.0:
-            phi += a * _zernike_cached(j, n, radius)
-    phi += phi_fixed_rad_fn(n, radius)
-    pf = np.zeros((K, K), complex)
-    o = (K - n) // 2
-    pf[o:o + n, o:o + n] = pupil * np.exp(1j * phi)
-    # the solver's OTF is S = c^2 ifft(|fft(P)|^2), i.e. the PSF is |ifft(P)|^2
-    psf = np.abs(sfft.ifft2(pf, workers=-1)) ** 2
-    psf /= psf.sum()
-    return psf   # centred at (0, 0) (periodic)
-
-
 _ZCACHE = {}
 
 
@@ -139,9 +124,12 @@ def _zernike_cached(j, n, radius):
     return z
 
 
-def make_job(N: int, n_modes: int, layout, grad_step=1e-2, apodization=-1) -> Job:
+def make_job(N: int, n_modes: int, layout, grad_step=1e-2, apodization=-1, basis="zernike",
+             kl_last=None) -> Job:
     """layout: list of objects, each a list of channels (diversity PV waves), and the
-    number of frames; e.g. [[0.0, 1.0]] = one object with a focus and a +1 wave channel."""
+    number of frames; e.g. [[0.0, 1.0]] = one object with a focus and a +1 wave channel.
+    basis "kl": Karhunen-Loeve modes 2..n_modes+1 (tilts Zernike) from the expansion over
+    Noll 2..kl_last (default 2 * n_modes + 1, KL_MAX_MODE >= 2 M)."""
     frames = layout["frames"]
     objects = layout["objects"]
     fc, radius, npup = js.calculate_pupil_size(N, WAVELENGTH, TELESCOPE_D, ARCSEC_PER_PX)
@@ -150,7 +138,13 @@ def make_job(N: int, n_modes: int, layout, grad_step=1e-2, apodization=-1) -> Jo
     otf = 2 * n
     mode_list = list(range(2, 2 + n_modes))
     jscale = WAVELENGTH * (0.5 * fc) / ((math.pi * math.pi / 648000.0) * ARCSEC_PER_PX * TELESCOPE_D)
-    ms = js.zernike_modeset(mode_list, n, radius, WAVELENGTH, jscale)
+    kl = None
+    if basis == "kl":
+        kl_last = kl_last or 2 * n_modes + 1
+        ms = js.kl_modeset(mode_list, n, radius, WAVELENGTH, jscale, 2, kl_last)
+        kl = {i: e.weights for i, e in js.kl_expansion(2, kl_last).items() if i in mode_list}
+    else:
+        ms = js.zernike_modeset(mode_list, n, radius, WAVELENGTH, jscale)
     pupil, _ = js.make_pupil(n, radius)
     sup = js.pupil_support(pupil)
     img_obj, img_ch, img_wf, phis, ref = [], [], [], [], []
@@ -173,7 +167,26 @@ def make_job(N: int, n_modes: int, layout, grad_step=1e-2, apodization=-1) -> Jo
                img_wavefront=np.array(img_wf, np.int32), phi_fixed=np.stack(phis),
                obj_weight=np.ones(len(objects)), obj_grad_step=np.full(len(objects), grad_step * WAVELENGTH),
                window=win, noise_window=nwin, nullspace=ns, cutout_size=N + 2 * MAX_LOCAL_SHIFT,
-               channel_div_pv=np.array([pv for chans in objects for pv in chans]))
+               channel_div_pv=np.array([pv for chans in objects for pv in chans]),
+               basis=basis, atm_var=np.asarray(ms.atm_rms) ** 2, kl_weights=kl)
+
+
+def _basis_cached(job: Job, n, radius):
+    """The job's modes at unit RMS on an n x n generator pupil (Zernike or KL combinations,
+    normalised over that pupil as ModeSet normalises them)."""
+    zs = []
+    for i in job.mode_list:
+        if job.basis != "kl" or i in (2, 3):
+            zs.append(_zernike_cached(i, n, radius))
+            continue
+        m = np.zeros((n, n))
+        for j, c in job.kl_weights[i]:
+            if abs(c) >= job.kl_cutoff:
+                m += c * _zernike_cached(j, n, radius)
+        pupil = _pupil_cached(n, radius)
+        m *= math.sqrt(float(pupil.sum()) / float((m * m * pupil)[pupil > 0].sum()))
+        zs.append(m)
+    return np.stack(zs)
 
 
 def make_patches(job: Job, n_patches: int, d_r0: float, rng, fixed_gamma=None,
@@ -184,7 +197,7 @@ def make_patches(job: Job, n_patches: int, d_r0: float, rng, fixed_gamma=None,
     frames = int(job.img_wavefront.max()) + 1
     if K is None:
         K = 1 << int(math.ceil(math.log2(cs + 64)))
-    var = np.array([js.zernike_covariance(j, j) for j in job.mode_list]) * d_r0 ** (5.0 / 3.0)
+    var = np.asarray(job.atm_var) * d_r0 ** (5.0 / 3.0)
     sd = np.sqrt(var)
     n_obj = job.n_objects
     cut = np.zeros((n_patches, I, cs, cs), np.float32)
@@ -192,7 +205,7 @@ def make_patches(job: Job, n_patches: int, d_r0: float, rng, fixed_gamma=None,
     n = K // 2
     radius = n / 2.0
     pupil = _pupil_cached(n, radius)
-    Zk = np.stack([_zernike_cached(jm, n, radius) for jm in job.mode_list])
+    Zk = _basis_cached(job, n, radius)
     z4 = _zernike_cached(4, n, radius)
     o0 = (K - cs) // 2
     op = (K - n) // 2
@@ -244,15 +257,15 @@ def config(index: int, n_patches: int | None = None, seed_offset: int = 0, frame
         cfg = dict(iterations=50, gamma=1e-3)
         return Workload("plain FP64 64x64, 2ch x 4fr, Z2-21", job, pt, cfg)
     if index == 1:
-        job = make_job(88, 36, LAYOUT_WB_NB(frames or 8))
+        job = make_job(88, 36, LAYOUT_WB_NB(frames or 8), basis="kl")
         pt = make_patches(job, n_patches or 1, 10.0, rng)
         return Workload("adjoint check 88x88, 3ch x 8fr, 36 modes", job, pt, {})
     if index == 2:
-        job = make_job(88, 36, LAYOUT_WB_NB(frames or 12))
+        job = make_job(88, 36, LAYOUT_WB_NB(frames or 12), basis="kl")
         pt = make_patches(job, n_patches or 225, 15.0, rng)
-        return Workload("production 88x88, 3ch x 12fr, 36 modes", job, pt, dict(iterations=100))
+        return Workload("production 88x88, 3ch x 12fr, 36 KL modes", job, pt, dict(iterations=100))
     if index == 4:
-        job = make_job(128, 100, LAYOUT_WB_NB(frames or 32))
+        job = make_job(128, 100, LAYOUT_WB_NB(frames or 32), basis="kl")
         pt = make_patches(job, n_patches or 256, 25.0, rng)
-        return Workload("mixed precision 128x128, 3ch x 32fr, 100 modes", job, pt, {})
+        return Workload("mixed precision 128x128, 3ch x 32fr, 100 KL modes", job, pt, {})
     raise ValueError(f"unknown config {index}")

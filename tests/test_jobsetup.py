@@ -65,3 +65,43 @@ def test_nullspace(frames, objects):
             assert np.ptp(v) < 1e-12
     for m in (0, 1):
         assert abs(a[ref, m].sum()) < 1e-12
+
+
+def test_kl_expansion_diagonalises_the_noll_covariance():
+    from redux_gb300 import jobsetup as J
+    first, last = 2, 73
+    kle = J.kl_expansion(first, last)
+    ids = list(range(first, last + 1))
+    W = np.zeros((len(ids), len(ids)))
+    for a, i in enumerate(ids):
+        for j, c in kle[i].weights:
+            W[a, j - first] = c
+    C = np.array([[J.zernike_covariance(i, j) for j in ids] for i in ids])
+    K = W @ C @ W.T
+    assert np.abs(K - np.diag(np.diag(K))).max() <= 1e-12 * np.abs(np.diag(K)).max()
+    np.testing.assert_allclose(np.diag(K), [kle[i].covariance for i in ids], rtol=1e-10)
+    # each KL mode mixes only Zernikes of one azimuthal order and parity (one covariance block)
+    for i in ids:
+        ms = {abs(J.noll_to_nm(j)[1]) for j, c in kle[i].weights if abs(c) > 1e-12}
+        assert len(ms) == 1
+        # sign rule of the reference: the largest weight is positive
+        cs = np.array([c for _, c in kle[i].weights])
+        assert cs[np.argmax(np.abs(cs))] > 0
+
+
+def test_kl_modeset_tilts_stay_zernike_and_modes_have_unit_rms():
+    from redux_gb300 import jobsetup as J
+    lam = 630.2e-9
+    mode_list = list(range(2, 22))
+    kl = J.kl_modeset(mode_list, 32, 16.0, lam, 1.0, 2, 41)
+    zn = J.zernike_modeset(mode_list, 32, 16.0, lam, 1.0)
+    np.testing.assert_allclose(kl.modes[0], zn.modes[0])   # Noll 2
+    np.testing.assert_allclose(kl.modes[1], zn.modes[1])   # Noll 3
+    pupil, _ = J.make_pupil(32, 16.0)
+    area = J.pupil_support(pupil).area
+    for m in kl.modes:
+        rms = np.sqrt(((m * lam) ** 2 * pupil)[pupil > 0].sum() / area)
+        assert abs(rms - 1.0) < 1e-12
+    # KL mode 4 is dominated by defocus
+    k = J.kl_expansion(2, 41)[4]
+    assert max(k.weights, key=lambda t: abs(t[1]))[0] == 4
