@@ -67,6 +67,8 @@ struct rdxg_solver {
     rdxg_solve_params lastParams{};
     // fused evaluation path (FP32, N <= 88)
     bool fused = false;
+    cudaStream_t side = nullptr;     // capture stream of the graph's conditional bodies
+    unsigned long long* dLaunchCount = nullptr;   // kernel launches of a graph-run solve
     double* dRestore = nullptr;      // restoration scratch (allocated on first use)
     double* dFc = nullptr;           // [nObj] frequency cutoffs of the restoration
     float* dRestoreOut = nullptr;    // [P][nObj][ps][ps] restored objects
@@ -208,20 +210,21 @@ EvalParams<T> make_evalparams(rdxg_solver* h) {
 }
 
 // finite-difference gradient of the patches in the FD list
-void launch_fd(rdxg_solver* h) {
+void launch_fd(rdxg_solver* h, cudaStream_t st) {
     if (h->fusedFd) {
         with_eval(h->N, [&](auto E) {
             EvalParams<float> e = make_evalparams<float>(h);
-            decltype(E)::fd_half(e, h->numSMs, h->stream);
+            decltype(E)::fd_half(e, h->numSMs, st);
         });
         return;
     }
     with_size(h->N, h->fp64, [&](auto L, auto t) {
         using T = decltype(t);
         KParams<T> kp = make_kparams<T>(h);
-        decltype(L)::fd(kp, h->fdGrid, h->M, h->stream);
+        decltype(L)::fd(kp, h->fdGrid, h->M, st);
     });
 }
+void launch_fd(rdxg_solver* h) { launch_fd(h, h->stream); }
 
 template <typename T>
 CgArgs<T> make_cgargs(rdxg_solver* h, const CgParams& prm) {
@@ -705,6 +708,7 @@ int rdxg_destroy(rdxg_solver* h) {
     for (void* p : h->allocs) cudaFree(p);
     if (h->hActive) cudaFreeHost(h->hActive);
     if (h->own) cudaStreamDestroy(h->own);
+    if (h->side) cudaStreamDestroy(h->side);
     delete h;
     return RDXG_OK;
 }
@@ -923,6 +927,107 @@ int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, i
     return RDXG_OK;
 }
 
+// Runs the rounds as a CUDA graph of `check` rounds: the kernels that are only needed in
+// some rounds (image re-initialisation after a re-shift, the adjoint, the finite-difference
+// gradient) sit in conditional nodes whose conditions k_shift sets from the round's work-list
+// counters.  The host launches the graph and reads the active-patch counter after each launch.
+extern "C++" {
+template <typename RoundFn>
+int solve_rounds_graph(rdxg_solver* h, ShiftArgs sa, int check, RoundFn&& round_launches) {
+    cudaStream_t st = h->stream;
+    if (!h->side) CK(h, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+    if (!h->dLaunchCount) {
+        int r = dalloc_t(h, &h->dLaunchCount, 1);
+        if (r) return r;
+    }
+    CK(h, cudaMemsetAsync(h->dLaunchCount, 0, sizeof(unsigned long long), st));
+    CK(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaSuccess;
+    const char* what = "capture info";
+    {
+        cudaStreamCaptureStatus status;
+        ce = cudaStreamGetCaptureInfo(st, &status, nullptr, &graph, nullptr, nullptr, nullptr);
+    }
+    // a handle belongs to one conditional node: three new ones per round
+    cudaGraphConditionalHandle cond[3] = {};
+    sa.useConditions = 1;
+    sa.counters = h->dCounters;
+    sa.fixedLaunches = h->fused ? 5 : 4;
+    sa.launchCount = h->dLaunchCount;
+    // optional kernel k: an IF node on cond[k] after the captured work so far, its body
+    // captured on the side stream
+    auto optional = [&](int k, auto issue) {
+        if (ce != cudaSuccess) return;
+        cudaStreamCaptureStatus status;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nDeps = 0;
+        what = "capture info";
+        if ((ce = cudaStreamGetCaptureInfo(st, &status, nullptr, &g, &deps, nullptr, &nDeps)) != cudaSuccess) return;
+        what = "conditional node";
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = cond[k];
+        np.conditional.type = cudaGraphCondTypeIf;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        if ((ce = cudaGraphAddNode(&node, g, deps, nullptr, nDeps, &np)) != cudaSuccess) return;
+        what = "capture dependencies";
+        if ((ce = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+            cudaSuccess)
+            return;
+        what = "body capture";
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        if ((ce = cudaStreamBeginCaptureToGraph(h->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+            cudaSuccess)
+            return;
+        issue(h->side);
+        ce = cudaStreamEndCapture(h->side, &body);
+    };
+    for (int r = 0; r < check && ce == cudaSuccess; ++r) {
+        what = "conditional handle";
+        for (int k = 0; k < 3 && ce == cudaSuccess; ++k) ce = cudaGraphConditionalHandleCreate(&cond[k], graph, 0, 0);
+        if (ce != cudaSuccess) break;
+        sa.condPrep = cond[0];
+        sa.condAdjoint = cond[1];
+        sa.condFd = cond[2];
+        if (round_launches(st, sa, optional)) { ce = cudaErrorUnknown; what = "round"; }
+        if (ce == cudaSuccess && (ce = cudaGetLastError()) != cudaSuccess) what = "kernel launch";
+    }
+    cudaGraph_t captured = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(st, &captured);
+    if (ce == cudaSuccess && ee != cudaSuccess) { ce = ee; what = "end capture"; }
+    cudaGraphExec_t exec = nullptr;
+    if (ce == cudaSuccess && (ce = cudaGraphInstantiate(&exec, captured, 0)) != cudaSuccess) what = "instantiate";
+    if (ce != cudaSuccess) {
+        if (captured) cudaGraphDestroy(captured);
+        cudaGetLastError();
+        h->err = std::string("solver graph (") + what + "): " + cudaGetErrorString(ce);
+        return RDXG_ERR_CUDA;
+    }
+    int r = RDXG_OK;
+    for (long round = 0;; round += check) {
+        if ((ce = cudaGraphLaunch(exec, st)) != cudaSuccess ||
+            (ce = cudaMemcpyAsync(h->hActive, h->dActive, sizeof(int32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (ce = cudaStreamSynchronize(st)) != cudaSuccess) {
+            h->err = std::string("solver graph launch: ") + cudaGetErrorString(ce);
+            r = RDXG_ERR_CUDA;
+            break;
+        }
+        if (*h->hActive == 0) break;
+        if (round > 2000000L) { h->err = "solver did not terminate"; r = RDXG_ERR_STATE; break; }
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(captured);
+    if (r) return r;
+    unsigned long long n = 0;
+    CK(h, cudaMemcpy(&n, h->dLaunchCount, sizeof(n), cudaMemcpyDeviceToHost));
+    h->launches = (int64_t)n;
+    return RDXG_OK;
+}
+}  // extern "C++"
+
 int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
     if (!h || !s) return RDXG_ERR_ARG;
     if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
@@ -959,30 +1064,42 @@ int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
     std::memcpy(sa.J, h->J, sizeof(sa.J));
     std::memcpy(sa.Jinv, h->Jinv, sizeof(sa.Jinv));
     const int G = P * h->I;
-    for (long round = 0;; ++round) {
-        CK(h, cudaMemsetAsync(h->dActive, 0, sizeof(int32_t), h->stream));
-        CK(h, cudaMemsetAsync(h->dCounters, 0, kNumCounters * sizeof(int32_t), h->stream));
+    // one round: the solver kernel, re-shift, [re-initialisation], evaluation, [adjoint],
+    // [finite differences]; optional(k, issue) issues the bracketed kernels
+    auto round_launches = [&](cudaStream_t st, const ShiftArgs& sar, auto optional) -> int {
+        if (cudaMemsetAsync(h->dActive, 0, sizeof(int32_t), st) != cudaSuccess ||
+            cudaMemsetAsync(h->dCounters, 0, kNumCounters * sizeof(int32_t), st) != cudaSuccess)
+            return 1;
         with_size(h->N, h->fp64, [&](auto L, auto t) {
             using T = decltype(t);
             KParams<T> kp = make_kparams<T>(h);
             CgArgs<T> ca = make_cgargs<T>(h, prm);
-            launch_cg<T>(ca, P, h->stream);
-            launch_shift(sa, P, h->stream);
-            decltype(L)::prep(kp, 0, G, h->stream);
+            launch_cg<T>(ca, P, st);
+            launch_shift(sar, P, st);
+            optional(0, [&](cudaStream_t s2) { decltype(L)::prep(kp, 0, G, s2); });
             if (h->fused) {
                 with_eval(h->N, [&](auto E) {
                     EvalParams<float> e = make_evalparams<float>(h);
-                    decltype(E)::phase(e, h->phaseGrid, h->stream);
-                    decltype(E)::eval(e, h->npt, h->evalGrid, h->stream);
-                    decltype(E)::reduce(e, h->reduceGrid, h->stream);
+                    decltype(E)::phase(e, h->phaseGrid, st);
+                    decltype(E)::eval(e, h->npt, h->evalGrid, st);
+                    decltype(E)::reduce(e, h->reduceGrid, st);
                 });
             } else {
-                decltype(L)::forward(kp, G, h->stream);
-                launch_accum<T>(kp, P * h->nObj, h->stream);
+                decltype(L)::forward(kp, G, st);
+                launch_accum<T>(kp, P * h->nObj, st);
             }
-            decltype(L)::adjoint(kp, h->adjGrid, GK_VOGEL, h->stream);
+            optional(1, [&](cudaStream_t s2) { decltype(L)::adjoint(kp, h->adjGrid, GK_VOGEL, s2); });
         });
-        launch_fd(h);
+        optional(2, [&](cudaStream_t s2) { launch_fd(h, s2); });
+        return 0;
+    };
+    const char* ng = getenv("RDXG_NO_GRAPH");
+    if (!(ng && atoi(ng))) return solve_rounds_graph(h, sa, check, round_launches);
+    for (long round = 0;; ++round) {
+        if (round_launches(h->stream, sa, [&](int, auto issue) { issue(h->stream); })) {
+            h->err = "cudaMemsetAsync failed";
+            return RDXG_ERR_CUDA;
+        }
         h->launches += h->fused ? 8 : 7;
         CKL(h);
         if ((round + 1) % check == 0) {

@@ -266,6 +266,7 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
         a.gmethod[p] = st.grad_method;
         a.modeCount[p] = st.mode_count;
         if (rq != REQ_DONE) atomicAdd(a.active, 1);
+        if (rq == REQ_SHIFT) atomicAdd(a.L.counters + kCounterShift, 1);
         if (rq == REQ_DF) {
             if (st.grad_method == GM_FD) a.L.fdP[atomicAdd(a.L.nFdP, 1)] = p;
             else a.L.gradP[atomicAdd(a.L.nGradP, 1)] = p;
@@ -296,11 +297,28 @@ struct ShiftArgs {
     const int32_t* imgObj;
     int32_t* aux;            // [P][2] reference object valid flag (cleared on re-initialisation)
     double J[2][2], Jinv[2][2];
+    // rounds run as a CUDA graph: the conditions of the graph's optional kernels (image
+    // re-initialisation, adjoint, finite differences), set once per round from the work-list
+    // counters, and the kernel launches of the round added to launchCount
+    int32_t useConditions;
+    cudaGraphConditionalHandle condPrep, condAdjoint, condFd;
+    const int32_t* counters;
+    int32_t fixedLaunches;
+    unsigned long long* launchCount;
 };
 
 template <int UNUSED = 0>
 __global__ void k_shift(ShiftArgs a) {
     const int p = blockIdx.x;
+    if (a.useConditions && p == 0 && threadIdx.x == 0) {
+        // written by k_cg, the previous kernel; one thread sets each condition
+        const unsigned prep = a.counters[kCounterShift] > 0, adj = a.counters[kCounterGrad] > 0,
+                       fd = a.counters[kCounterFd] > 0;
+        cudaGraphSetConditional(a.condPrep, prep);
+        cudaGraphSetConditional(a.condAdjoint, adj);
+        cudaGraphSetConditional(a.condFd, fd);
+        *a.launchCount += (unsigned long long)(a.fixedLaunches + prep + adj + fd);
+    }
     if (a.req[p] != REQ_SHIFT) {
         for (int j = threadIdx.x; j < a.I; j += blockDim.x) a.reinit[(size_t)p * a.I + j] = 0;
         return;

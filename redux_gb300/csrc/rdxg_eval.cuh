@@ -32,6 +32,10 @@ struct PoItem {
     int32_t p, o, mode;   // mode: 0 metric, 1 gradient (write O, Qt), 2 refresh O'
 };
 
+// work-list counters (reset every round)
+enum : int32_t { kCounterEval = 0, kCounterPo = 1, kCounterGrad = 2, kCounterFd = 3, kCounterEvalP = 4,
+                 kCounterShift = 5 };
+
 struct Lists {
     EvalItem* eval;  int32_t* nEval;
     PoItem* po;      int32_t* nPo;

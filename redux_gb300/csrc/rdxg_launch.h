@@ -37,7 +37,7 @@ constexpr int kPhaseRegPix = 128;   // pixels per block of the per-patch mode ex
 constexpr int kPhaseRegModes = 64;  // modes it holds in registers (more: the staged kernel)
 constexpr int kPhaseMaxImg = 64;    // images per patch it stages
 constexpr int kPhaseMaxCh = 16;     // channels whose fixed phases it stages
-constexpr int kNumCounters = 5;     // work-list counters reset every round
+constexpr int kNumCounters = 6;     // work-list counters reset every round
 constexpr size_t kMaxSmem = 227 * 1024;   // dynamic shared memory per block
 template <typename T, int N> struct EvalLauncher {
     static cudaError_t setup(int M, int npt, int nH);
