@@ -252,3 +252,40 @@ def test_restore_fp64_with_and_without_filter(w0):
         ref = op.restore(a[0], fc, no_filter=nf)
         err = np.abs(out[0, 0] - ref[0]).max() / np.abs(ref[0]).max()
         assert err <= 1e-6, (nf, err)
+
+
+# the general (unfused) FP32 path at N = 128 with 100 KL modes (config 4's geometry, 2 frames)
+def _w4():
+    return workload(4, n_patches=1, frames=2)
+
+
+@pytest.mark.parametrize("scale", [0.0, 1.0])
+def test_metric_n128_kl100(scale):
+    w = _w4()
+    s = _solver(w)
+    a = w.patches.alpha_true * scale
+    L = s.metric(a)
+    Lo = _oracle(w).metric(a[0])
+    assert abs(L[0] - Lo) <= TOL_METRIC * abs(Lo), (L[0], Lo)
+
+
+def test_gradient_vogel_n128_kl100():
+    w = _w4()
+    s = _solver(w)
+    a = w.patches.alpha_true * 0.5
+    g, _ = s.gradient(a, "vogel")
+    _, go = _oracle(w).gradient(a[0], method="vogel")
+    rel = np.linalg.norm(g[0] - go) / np.linalg.norm(go)
+    assert rel < TOL_GRAD, rel
+
+
+def test_solve_n128_kl100_first_metrics():
+    w = _w4()
+    s = _solver(w)
+    st = S.fixed_iterations(w.job.n_modes, 3, max_metrics=64)
+    out = s.run(st)
+    ref = _oracle(w).solve(oracle.Cfg(n_initial_modes=w.job.n_modes, n_mode_increment=w.job.n_modes,
+                                      max_iterations=3, min_iterations=3, target_iterations=3, fd_first=1,
+                                      ftol=0.0, eps=1e-10, brent_tol=0.1))
+    n = min(3, out["reports"][0].n_metrics, len(ref["metrics"]))
+    np.testing.assert_allclose(out["metrics"][0, :n], ref["metrics"][:n], rtol=1e-5)
