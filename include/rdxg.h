@@ -184,6 +184,17 @@ int rdxg_fetch_results(rdxg_solver* h, double* alpha_out, rdxg_patch_report* rep
 /* Number of kernel launches issued by the last rdxg_solve / rdxg_solve_async. */
 int64_t rdxg_last_launch_count(const rdxg_solver* h);
 
+/* Mode expansion phi = phi_fixed + sum_m alpha_m Z_m of the fused FP32 path
+ * (SubImage::calcPhi / addToPhi, subimage.cpp:509-544) on the tensor cores (tcgen05, FP32
+ * accumulation) with the FP32 operands split into BF16 parts: mode 3 (the default) three parts
+ * (6xBF16 products, FP32-like: metric, OTF and gradient within 1e-6 of FP64), mode 2 two parts
+ * (3xBF16: phases within ~1e-5 of their magnitude, gradients within ~3e-5); mode 0 on the
+ * CUDA cores in FP32.  The general path (FP64, or OTF sizes the fused path does not take) expands the modes
+ * inside its transform kernel and only accepts mode 0 (RDXG_ERR_STATE otherwise).
+ * rdxg_phase_mode returns the mode in use (0, 2 or 3). */
+int rdxg_set_phase_mode(rdxg_solver* h, int32_t mode);
+int32_t rdxg_phase_mode(const rdxg_solver* h);
+
 /* Times the per-image and per-object kernels on the loaded batch at the current point with
  * CUDA events on the handle's stream: ms[0] forward (metric evaluation), ms[1] per-object
  * accumulation, ms[2] forward (gradient evaluation, also keeps the transforms), ms[3]
@@ -194,8 +205,9 @@ int rdxg_profile_kernels(rdxg_solver* h, int32_t reps, double* ms);
 /* Debug copies of device state (host buffers sized by the caller):
  * which = 0 D [P][I][N][N] complex, 1 OTF [P][I][N][N] complex, 2 gamma [P][nObj],
  *         3 image stats [P][I][3] (mean, stddev, noise), 4 object O [P][nObj][N][N] complex,
- *         5 shifts [P][I][2] int32.  Complex values are float pairs in FP32 mode and
- *         double pairs in FP64 mode. */
+ *         5 shifts [P][I][2] int32, 6 phases of the last fused evaluation [P][I][n][n] float
+ *         (fused FP32 path only).  Complex values are float pairs in FP32 mode and double
+ *         pairs in FP64 mode. */
 int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes);
 
 /* Host drop-in for redux's conjugate_rdx minimiser with the Solver::run stage loop

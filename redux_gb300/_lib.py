@@ -17,7 +17,7 @@ EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "r
             "rdxg_set_patches", "rdxg_set_patches_device", "rdxg_metric", "rdxg_gradient",
             "rdxg_solve", "rdxg_solve_async", "rdxg_fetch_results", "rdxg_last_launch_count",
             "rdxg_debug_copy", "rdxg_cg_minimize", "rdxg_profile_kernels", "rdxg_metric_with_reference",
-            "rdxg_metric_noalloc", "rdxg_restore")
+            "rdxg_metric_noalloc", "rdxg_restore", "rdxg_set_phase_mode", "rdxg_phase_mode")
 
 
 class Geometry(C.Structure):
@@ -86,6 +86,9 @@ def load(path: str = LIB_PATH):
     L.rdxg_last_launch_count.restype = C.c_int64
     L.rdxg_last_launch_count.argtypes = [vp]
     L.rdxg_debug_copy.argtypes = [vp, C.c_int32, vp, C.c_size_t]
+    L.rdxg_set_phase_mode.argtypes = [vp, C.c_int32]
+    L.rdxg_phase_mode.restype = C.c_int32
+    L.rdxg_phase_mode.argtypes = [vp]
     L.rdxg_profile_kernels.argtypes = [vp, C.c_int32, vp]
     L.rdxg_cg_minimize.argtypes = [C.c_int32, C.c_int32, C.POINTER(SolveParams), C.c_double, F_FN, DF_FN,
                                    SHIFT_FN, vp, vp, C.POINTER(PatchReport), vp]

@@ -85,6 +85,11 @@ struct rdxg_solver {
     PoItem* dPoList = nullptr;
     int32_t *dGradP = nullptr, *dFdP = nullptr, *dEvalP = nullptr;
     int adjGrid = 0, fdGrid = 0;
+    // mode expansion of the fused path: 0 CUDA cores (FP32), 2 tensor cores 3xBF16, 3 6xBF16
+    int phaseParts = 3;
+    PhaseTcPlan tcPlan{};
+    __nv_bfloat16* dZt = nullptr;    // split modes (room for three parts)
+    int32_t* dTcStatus = nullptr;
 };
 
 namespace {
@@ -206,7 +211,52 @@ EvalParams<T> make_evalparams(rdxg_solver* h) {
     e.objMetric = h->dObjMetric; e.L = make_lists(h);
     e.hPos = h->dHPos; e.nTilesH = h->nTilesH; e.phi = (T*)h->dPhiImg;
     e.nCh = h->C;
+    e.Zt = h->tcPlan.valid ? h->dZt : nullptr;
+    e.tcStatus = h->dTcStatus;
+    e.tc = h->tcPlan;
     return e;
+}
+
+// Chooses the mode expansion of the fused path and splits the modes for the tensor cores.
+int setup_phase_tc(rdxg_solver* h, int parts) {
+    h->phaseParts = parts;
+    h->tcPlan = PhaseTcPlan{};
+    if (parts == 0) return RDXG_OK;
+    const int n2 = h->n * h->n;
+    if (!h->dZt) {
+        const PhaseTcPlan p3 = phase_tc_plan(h->I, h->M, n2, h->C, 3, h->numSMs);
+        const PhaseTcPlan p2 = phase_tc_plan(h->I, h->M, n2, h->C, 2, h->numSMs);
+        const size_t elems = p3.valid ? p3.zElems : p2.zElems;
+        if (!p2.valid) return RDXG_OK;   // shape the tensor-core kernel does not take: CUDA cores
+        int r;
+        if ((r = dalloc(h, (void**)&h->dZt, elems * sizeof(__nv_bfloat16))) || (r = dalloc_t(h, &h->dTcStatus, 1)))
+            return r;
+        CK(h, cudaMemsetAsync(h->dTcStatus, 0, sizeof(int32_t), h->stream));
+    }
+    const PhaseTcPlan p = phase_tc_plan(h->I, h->M, n2, h->C, parts, h->numSMs);
+    cudaGetLastError();
+    if (!p.valid) return RDXG_OK;
+    launch_tc_pack_modes((const float*)h->dZ, (const float*)h->dPhi, h->M, h->C, n2, p, h->dZt, h->stream);
+    CKL(h);
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->tcPlan = p;
+    if (getenv("RDXG_VERBOSE"))
+        fprintf(stderr, "tensor-core mode expansion: parts %d, K %d, images per tile %d (%d patches), smem %zu, "
+                "occupancy %d, grid %d\n", p.parts, p.KP, p.NT, p.G, p.smem, p.occ, p.grid);
+    return RDXG_OK;
+}
+
+// Reports (once) a wait of the tensor-core mode expansion that gave up.
+int tc_check(rdxg_solver* h) {
+    if (!h->dTcStatus) return RDXG_OK;
+    int32_t st = 0;
+    CK(h, cudaMemcpyAsync(&st, h->dTcStatus, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (st == 0) return RDXG_OK;
+    CK(h, cudaMemsetAsync(h->dTcStatus, 0, sizeof(int32_t), h->stream));
+    h->err = std::string("tensor-core mode expansion: ") +
+             (st == 1 ? "the mode tile copy" : "the products") + " did not complete within the wait limit";
+    return RDXG_ERR_CUDA;
 }
 
 // finite-difference gradient of the patches in the FD list
@@ -543,7 +593,9 @@ int setup_fused(rdxg_solver* h, const rdxg_static* s) {
     h->reduceGrid = h->numSMs * 8;
     h->phaseGrid = h->numSMs * 4;
     h->fused = true;
-    return RDXG_OK;
+    const char* pm = getenv("RDXG_PHASE_PARTS");
+    const int parts = pm ? atoi(pm) : 3;
+    return setup_phase_tc(h, parts == 0 || parts == 2 ? parts : 3);
 }
 
 // evaluation work lists built on the host for single evaluations of every patch
@@ -743,7 +795,8 @@ int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric) {
         // a first pass sets the reference object to this point, the second evaluates
         if ((r = fused_pass(h, REQ_F, 2))) return r;
         if ((r = fused_pass(h, REQ_F, 0))) return r;
-        return metric_from_objects(h, metric);
+        if ((r = metric_from_objects(h, metric))) return r;
+        return tc_check(h);
     }
     with_size(h->N, h->fp64, [&](auto L, auto t) {
         using T = decltype(t);
@@ -831,7 +884,7 @@ int rdxg_metric_noalloc(rdxg_solver* h, const double* alpha, double* metric) {
     CKL(h);
     CK(h, cudaMemcpyAsync(metric, dMetric, P * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
-    return RDXG_OK;
+    return tc_check(h);
 }
 
 int rdxg_metric_with_reference(rdxg_solver* h, const double* alpha_ref, const double* alpha, double* metric) {
@@ -843,7 +896,8 @@ int rdxg_metric_with_reference(rdxg_solver* h, const double* alpha_ref, const do
         (r = fused_pass(h, REQ_F, 2)))
         return r;
     if ((r = upload_alpha<float>(h, alpha)) || (r = fused_pass(h, REQ_F, 0))) return r;
-    return metric_from_objects(h, metric);
+    if ((r = metric_from_objects(h, metric))) return r;
+    return tc_check(h);
 }
 
 int rdxg_restore(rdxg_solver* h, const double* alpha, const double* frequency_cutoff, int32_t no_filter,
@@ -912,6 +966,7 @@ int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, i
     const size_t G = (size_t)h->P * h->I;
     CK(h, cudaMemcpyAsync(grad, h->dGalpha, G * h->M * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
+    if ((r = tc_check(h))) return r;
     if (enabled)
         for (size_t g = 0; g < G; ++g)
             for (int m = 0; m < h->M; ++m)
@@ -1122,6 +1177,8 @@ int rdxg_fetch_results(rdxg_solver* h, double* alpha_out, rdxg_patch_report* rep
     if (metrics && h->dMetrics)
         CK(h, cudaMemcpyAsync(metrics, h->dMetrics, (size_t)P * h->maxMetrics * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
+    int r = tc_check(h);
+    if (r) return r;
     if (reports) {
         for (int p = 0; p < P; ++p) {
             rdxg_patch_report& r = reports[p];
@@ -1146,6 +1203,27 @@ int rdxg_solve(rdxg_solver* h, const rdxg_solve_params* s, double* alpha_out, rd
 }
 
 int64_t rdxg_last_launch_count(const rdxg_solver* h) { return h ? h->launches : 0; }
+
+int rdxg_set_phase_mode(rdxg_solver* h, int32_t mode) {
+    if (!h || (mode != 0 && mode != 2 && mode != 3)) return RDXG_ERR_ARG;
+    if (!h->fused) {
+        if (mode == 0) return RDXG_OK;
+        h->err = "the general path expands the modes inside its transform kernel (CUDA cores only)";
+        return RDXG_ERR_STATE;
+    }
+    const int r = setup_phase_tc(h, mode);
+    if (r) return r;
+    if (mode != 0 && !h->tcPlan.valid) {
+        h->err = "the tensor-core mode expansion does not take this shape";
+        return RDXG_ERR_STATE;
+    }
+    return RDXG_OK;
+}
+
+int32_t rdxg_phase_mode(const rdxg_solver* h) {
+    if (!h || !h->fused) return 0;
+    return h->tcPlan.valid ? h->tcPlan.parts : 0;
+}
 
 int rdxg_profile_kernels(rdxg_solver* h, int32_t reps, double* ms) {
     if (!h || !ms || reps < 1) return RDXG_ERR_ARG;
@@ -1223,6 +1301,12 @@ int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes) {
         }
         case 4: if (bytes < PO * N2 * cxs) return RDXG_ERR_ARG; CK(h, cudaMemcpy(out, h->dO, PO * N2 * cxs, cudaMemcpyDeviceToHost)); break;
         case 5: if (bytes < G * 2 * 4) return RDXG_ERR_ARG; CK(h, cudaMemcpy(out, h->dShift, G * 8, cudaMemcpyDeviceToHost)); break;
+        case 6: {
+            const size_t nb = G * (size_t)h->n * h->n * sizeof(float);
+            if (!h->fused || !h->dPhiImg || bytes < nb) return RDXG_ERR_ARG;
+            CK(h, cudaMemcpy(out, h->dPhiImg, nb, cudaMemcpyDeviceToHost));
+            break;
+        }
         default: return RDXG_ERR_ARG;
     }
     return RDXG_OK;

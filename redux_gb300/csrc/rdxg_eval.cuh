@@ -20,6 +20,8 @@
 // same as with O' taken at the evaluated point (FP32 accumulation is enough).
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include "rdxg_kernels.cuh"
 
 namespace rdxg {
@@ -53,6 +55,25 @@ struct HalfPlane {
     const int32_t* objChunk0;  // [nObj] first chunk of each object within a patch
 };
 
+// Mode expansion on the tensor cores (rdxg_phase_tc.cu): the launch shape chosen per job.
+struct PhaseTcPlan {
+    int32_t valid, ntmax, G, NT, KP, parts, nTiles, grid;   // G patches (G*I images) per column tile
+    int32_t occ;                                             // resident blocks per SM (occupancy query)
+    size_t smem, zElems;                                     // dynamic shared memory; split mode elements
+};
+
+struct PhaseTcArgs {
+    const __nv_bfloat16* Zt;   // [tile][part][128 x KP] split modes in the operand layout
+    const float* alphaEff;     // [g][M]
+    const float* phiFixed;     // [C][n*n]
+    const int32_t* imgCh;      // [I]
+    const int32_t* evalP;      // patches with an evaluation this round
+    const int32_t* nEvalP;
+    float* phi;                // [g][n*n]
+    int32_t* status;           // non-zero once a wait on the tensor core or copy engine gave up
+    int32_t I, M, n2, nCh, G, NT, KP, parts;
+};
+
 template <typename T>
 struct EvalParams {
     KParams<T> k;
@@ -66,6 +87,9 @@ struct EvalParams {
     T* phi;             // [g][n*n] phases of the images being evaluated (k_phase)
     int32_t nCh;        // channels (fixed phases)
     Lists L;
+    const __nv_bfloat16* Zt;   // split modes of the tensor-core mode expansion (null: CUDA cores)
+    int32_t* tcStatus;
+    PhaseTcPlan tc;
 };
 
 // ----------------------------------------------------------------------------------

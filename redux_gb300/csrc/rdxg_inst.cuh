@@ -1,6 +1,8 @@
 // Definitions of Launcher<T, N>; included once per OTF size by rdxg_inst_<N>.cu.
 #pragma once
 
+#include <type_traits>
+
 #include "rdxg_launch.h"
 
 namespace rdxg {
@@ -126,6 +128,17 @@ int EvalLauncher<T, N>::phase_tiles() {
 
 template <typename T, int N>
 void EvalLauncher<T, N>::phase(const EvalParams<T>& e, int grid, cudaStream_t st) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (e.Zt && e.tc.valid) {
+            PhaseTcArgs a;
+            a.Zt = e.Zt; a.alphaEff = e.k.alphaEff; a.phiFixed = e.k.phiFixed; a.imgCh = e.k.imgCh;
+            a.evalP = e.L.evalP; a.nEvalP = e.L.nEvalP; a.phi = e.phi; a.status = e.tcStatus;
+            a.I = e.k.I; a.M = e.k.M; a.n2 = (N / 2) * (N / 2); a.nCh = e.nCh;
+            a.G = e.tc.G; a.NT = e.tc.NT; a.KP = e.tc.KP; a.parts = e.tc.parts;
+            launch_phase_tc(a, e.tc, st);
+            return;
+        }
+    }
     if (e.k.M <= kPhaseRegModes && e.nCh <= kPhaseMaxCh && e.k.I <= kPhaseMaxImg) {
         // grid: a multiple of the pixel tiles
         const int nPix = phase_tiles();

@@ -53,6 +53,12 @@ template <typename T, int N> struct EvalLauncher {
 template <typename T> void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st);
 void launch_shift(const ShiftArgs& a, int P, cudaStream_t st);
 
+// mode expansion on the tensor cores (rdxg_phase_tc.cu); parts: 2 (3xBF16) or 3 (6xBF16)
+PhaseTcPlan phase_tc_plan(int I, int M, int n2, int nCh, int parts, int numSMs);
+void launch_tc_pack_modes(const float* Z, const float* phiFixed, int M, int C, int n2, const PhaseTcPlan& p,
+                          __nv_bfloat16* out, cudaStream_t st);
+void launch_phase_tc(const PhaseTcArgs& a, const PhaseTcPlan& p, cudaStream_t st);
+
 // rdxg_metric_noalloc: a fixed static device array holds every temporary of the evaluation
 constexpr size_t kNoAllocScratchBytes = (size_t)16 << 20;
 cudaError_t noalloc_scratch(int device, void** ptr);   // its address on a device (looked up once)

@@ -196,12 +196,21 @@ class Solver:
     def launch_count(self) -> int:
         return int(_lib.load().rdxg_last_launch_count(self.h))
 
+    def set_phase_mode(self, mode: int) -> None:
+        """Mode expansion of the fused path: 0 CUDA cores (FP32), 2 tensor cores with the
+        3xBF16 split, 3 tensor cores with the 6xBF16 split (rdxg_set_phase_mode)."""
+        self._check(_lib.load().rdxg_set_phase_mode(self.h, int(mode)), "rdxg_set_phase_mode")
+
+    def phase_mode(self) -> int:
+        return int(_lib.load().rdxg_phase_mode(self.h))
+
     def debug(self, which: str):
         P, I, N, nObj = self.P, self.I, self.job.otf_size, self.job.n_objects
         ct = np.complex128 if self.precision == "fp64" else np.complex64
         spec = {"D": (0, (P, I, N, N), ct), "otf": (1, (P, I, N, N), ct), "gamma": (2, (P, nObj), np.float64),
                 "stats": (3, (P, I, 3), np.float64), "object": (4, (P, nObj, N, N), ct),
-                "shifts": (5, (P, I, 2), np.int32)}[which]
+                "shifts": (5, (P, I, 2), np.int32),
+                "phases": (6, (P, I, self.job.pupil_pixels, self.job.pupil_pixels), np.float32)}[which]
         out = np.zeros(spec[1], spec[2])
         self._check(_lib.load().rdxg_debug_copy(self.h, spec[0], _lib.ptr(out), out.nbytes), "rdxg_debug_copy")
         return out

@@ -10,7 +10,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_functions():
     src = open(os.path.join(ROOT, "include", "rdxg.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(rdxg_\w+)\s*\(", src, flags=re.M))
+    names = set(re.findall(r"^\s*(?:int|int32_t|int64_t|const char\*)\s+(rdxg_\w+)\s*\(", src, flags=re.M))
     return names
 
 
