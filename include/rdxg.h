@@ -166,10 +166,25 @@ int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, i
  * (object.cpp:278-334) for the object image, with the Scharmer filter (image/utils.cpp:
  * 334-392) unless no_filter (RF_NO_FILTER); FP64 on the device.  frequency_cutoff: [nObj]
  * Object::frequencyCutoff (pupil.cpp:87; the filter cuts at 0.9 of it).  objects:
- * [P][nObj][patch_size][patch_size] float32 (ObjectData::img).  The PSF, convolved-object and
- * residual outputs and the fitted-plane re-addition of the reference are not produced. */
+ * [P][nObj][patch_size][patch_size] float32 (ObjectData::img). */
 int rdxg_restore(rdxg_solver* h, const double* alpha, const double* frequency_cutoff, int32_t no_filter,
                  float* objects);
+
+/* rdxg_restore with the other outputs of Object::restorePatch (object.cpp:335-410, the
+ * SF_SAVE_PSF / SF_SAVE_PSF_AVG / SF_SAVE_COBJ / SF_SAVE_RESIDUAL flags), FP64 on the device,
+ * stored as float32 and trimmed to patch_size like the object:
+ *   RDXG_RESTORE_PSF      psf [P][I][ps][ps]      SubImage::getPSF of every image
+ *   RDXG_RESTORE_PSF_AVG  psf [P][nObj][ps][ps]   their mean per object (takes precedence)
+ *   RDXG_RESTORE_COBJ     cobj [P][I][ps][ps]     SubImage::convolveImage of the float object
+ *   RDXG_RESTORE_RESIDUAL res [P][I][ps][ps]      convolved object minus the image
+ * Images are in the order of the geometry (objects' channels, frames).  Buffers for flags not
+ * set may be NULL.  The reference's fitted-plane re-addition (FIT_PLANE) is not supported. */
+#define RDXG_RESTORE_PSF 1
+#define RDXG_RESTORE_PSF_AVG 2
+#define RDXG_RESTORE_COBJ 4
+#define RDXG_RESTORE_RESIDUAL 8
+int rdxg_restore_ex(rdxg_solver* h, const double* alpha, const double* frequency_cutoff, int32_t no_filter,
+                    int32_t outputs, float* objects, float* psf, float* cobj, float* res);
 
 /* Full per-patch solve (Solver::run, solver.cpp:330-580) for every loaded patch.
  * alpha_out: [P][I][M]; reports: [P]; metrics: [P][max_metrics] or NULL. */

@@ -6,7 +6,8 @@
 // (solver.cpp:219-225) and the public alpha vector.  The job-side types of the reference
 // (MomfbdJob, PatchData, ObjectData) are represented by the plain structs below, which hold
 // what Solver::run reads and writes: the float32 channel cutouts in, the mode coefficients,
-// metric history, final metric and restored objects out (solver.cpp:551-566).
+// metric history, final metric and restored objects out (solver.cpp:551-566), with the PSFs,
+// convolved objects and residuals that Object::restorePatch saves when asked (object.cpp:335-383).
 //
 // Errors: every failing rdxg_* call throws std::runtime_error with rdxg_last_error()
 // (the reference throws std::logic_error for a corrupt constraint set, solver.cpp:102-110,
@@ -39,6 +40,9 @@ struct Settings {
     int32_t maxMetrics = 1024;      // capacity of the metric history per patch
     bool restore = true;            // restore the objects after the solve
     bool noFilter = false;          // RF_NO_FILTER
+    // further outputs of the restoration (Object::saveMask): RDXG_RESTORE_PSF,
+    // RDXG_RESTORE_PSF_AVG, RDXG_RESTORE_COBJ, RDXG_RESTORE_RESIDUAL
+    int32_t saveMask = 0;
 };
 
 // What Solver::run takes from and gives back to PatchData (data.hpp:144-196).
@@ -53,6 +57,9 @@ struct PatchData {
     int32_t iterations = 0;
     int32_t status = 0;                  // 0 ok, 1 gave up after too many failures
     std::vector<float> objects;          // [nObj][ps][ps] restored objects (ObjectData::img)
+    std::vector<float> psf;              // [I][ps][ps] or, with RDXG_RESTORE_PSF_AVG, [nObj][ps][ps]
+    std::vector<float> cobj;             // [I][ps][ps] convolved objects (ObjectData::cobj)
+    std::vector<float> res;              // [I][ps][ps] residuals (ObjectData::res)
 };
 
 class Solver {
@@ -112,11 +119,19 @@ public:
         std::vector<rdxg_patch_report> rep(P);
         std::vector<double> met((size_t)P * set_.maxMetrics);
         check(rdxg_solve(h_, &prm, al.data(), rep.data(), met.data()), "rdxg_solve");
-        std::vector<float> obj;
-        const size_t ps = geo_.patch_size, nObj = geo_.n_objects;
+        std::vector<float> obj, psf, cobj, resid;
+        const size_t ps = geo_.patch_size, nObj = geo_.n_objects, ps2 = ps * ps;
+        const int32_t mask = set_.restore ? set_.saveMask : 0;
+        const size_t nPsf = (mask & RDXG_RESTORE_PSF_AVG) ? nObj : (mask & RDXG_RESTORE_PSF) ? I : 0;
         if (set_.restore) {
-            obj.resize(P * nObj * ps * ps);
-            check(rdxg_restore(h_, al.data(), fc_.data(), set_.noFilter ? 1 : 0, obj.data()), "rdxg_restore");
+            obj.resize(P * nObj * ps2);
+            psf.resize(P * nPsf * ps2);
+            if (mask & RDXG_RESTORE_COBJ) cobj.resize(P * I * ps2);
+            if (mask & RDXG_RESTORE_RESIDUAL) resid.resize(P * I * ps2);
+            check(rdxg_restore_ex(h_, al.data(), fc_.data(), set_.noFilter ? 1 : 0, mask, obj.data(),
+                                  psf.empty() ? nullptr : psf.data(), cobj.empty() ? nullptr : cobj.data(),
+                                  resid.empty() ? nullptr : resid.data()),
+                  "rdxg_restore_ex");
         }
         for (int p = 0; p < P; ++p) {
             PatchData& d = *batch[p];
@@ -126,7 +141,14 @@ public:
             d.finalMetric = rep[p].final_metric;
             d.iterations = rep[p].iterations;
             d.status = rep[p].status;
-            if (set_.restore) d.objects.assign(obj.begin() + p * nObj * ps * ps, obj.begin() + (p + 1) * nObj * ps * ps);
+            if (set_.restore) d.objects.assign(obj.begin() + p * nObj * ps2, obj.begin() + (p + 1) * nObj * ps2);
+            auto part = [&](const std::vector<float>& v, size_t per, std::vector<float>& dst) {
+                if (v.empty()) dst.clear();
+                else dst.assign(v.begin() + p * per, v.begin() + (p + 1) * per);
+            };
+            part(psf, nPsf * ps2, d.psf);
+            part(cobj, I * ps2, d.cobj);
+            part(resid, I * ps2, d.res);
         }
         alpha.assign(al.begin() + (P - 1) * I * M, al.end());
         loaded_ = P;

@@ -140,3 +140,33 @@ def restore(D, S, noise, image_object, obj, frequency_cutoff, ps, support, no_fi
     img = np.real(np.fft.ifft2(np.fft.ifftshift(O)))
     off = (N - ps) // 2
     return img[off:off + ps, off:off + ps]
+
+
+def restore_outputs(D, S, image_object, objects, ps):
+    """The other outputs of Object::restorePatch (object.cpp:335-383) from centred image
+    transforms D and OTFs S [I][N][N] and the untrimmed float objects [nObj][N][N]:
+      PSF_j  = reorder(real(ift(reorder(S_j))) / N^2)   SubImage::addPSF (subimage.cpp:615-626)
+               with the OTF's flags REORDER_IMG|REORDER_FT|NORMALIZE_FT, centred (89-90)
+      mean   = float(float(sum_j PSF_j) / count)         object.cpp:345-350
+      cobj_j = real(ift(ft(img_o) / N^2 * reorder(S_j)))  FourierTransform::convolve
+               (fouriertransform.hpp:310-324): image not reordered, product un-centred
+      res_j  = float(float(cobj_j) - real(ift(reorder(D_j))) / N^2)   subimage.hpp:118-129
+    All trimmed to ps around the centre.  Returns (psf [I], psf_mean [nObj], cobj [I], res [I])."""
+    I, N = S.shape[0], S.shape[1]
+    off = (N - ps) // 2
+    cut = (slice(off, off + ps), slice(off, off + ps))
+    psf = np.array([np.fft.fftshift(np.real(np.fft.ifft2(np.fft.ifftshift(S[j])))) for j in range(I)])
+    nObj = len(objects)
+    psf_mean = []
+    for o in range(nObj):
+        idx = [j for j in range(I) if image_object[j] == o]
+        acc = np.zeros((N, N))
+        for j in idx:
+            acc += psf[j]
+        psf_mean.append((acc.astype(np.float32).astype(np.float64) * (1.0 / len(idx))).astype(np.float32)[cut])
+    F = [np.fft.fft2(np.asarray(objects[o], np.float32).astype(np.float64)) for o in range(nObj)]
+    cobj = np.array([np.real(np.fft.ifft2(F[image_object[j]] * np.fft.ifftshift(S[j]))) for j in range(I)])
+    img = np.array([np.real(np.fft.ifft2(np.fft.ifftshift(D[j]))) for j in range(I)])
+    res = (cobj.astype(np.float32).astype(np.float64) - img).astype(np.float32)
+    return (psf.astype(np.float32)[:, cut[0], cut[1]], np.array(psf_mean),
+            cobj.astype(np.float32)[:, cut[0], cut[1]], res[:, cut[0], cut[1]])

@@ -12,12 +12,13 @@ LIB_PATH = os.path.join(HERE, "libredux_gb300.so")
 RDXG_OK, RDXG_ERR_ARG, RDXG_ERR_UNSUPPORTED, RDXG_ERR_CUDA, RDXG_ERR_STATE, RDXG_ERR_NONFINITE, RDXG_ERR_NOMEM = range(7)
 RDXG_FP32, RDXG_FP64 = 0, 1
 RDXG_GRAD_VOGEL, RDXG_GRAD_EXACT, RDXG_GRAD_FD = 0, 1, 2
+RDXG_RESTORE_PSF, RDXG_RESTORE_PSF_AVG, RDXG_RESTORE_COBJ, RDXG_RESTORE_RESIDUAL = 1, 2, 4, 8
 
 EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "rdxg_set_stream",
             "rdxg_set_patches", "rdxg_set_patches_device", "rdxg_metric", "rdxg_gradient",
             "rdxg_solve", "rdxg_solve_async", "rdxg_fetch_results", "rdxg_last_launch_count",
             "rdxg_debug_copy", "rdxg_cg_minimize", "rdxg_profile_kernels", "rdxg_metric_with_reference",
-            "rdxg_metric_noalloc", "rdxg_restore", "rdxg_set_phase_mode", "rdxg_phase_mode")
+            "rdxg_metric_noalloc", "rdxg_restore", "rdxg_restore_ex", "rdxg_set_phase_mode", "rdxg_phase_mode")
 
 
 class Geometry(C.Structure):
@@ -79,6 +80,7 @@ def load(path: str = LIB_PATH):
     L.rdxg_metric_with_reference.argtypes = [vp, vp, vp, vp]
     L.rdxg_metric_noalloc.argtypes = [vp, vp, vp]
     L.rdxg_restore.argtypes = [vp, vp, vp, C.c_int32, vp]
+    L.rdxg_restore_ex.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, vp, vp, vp, vp]
     L.rdxg_gradient.argtypes = [vp, vp, vp, C.c_int32, vp, vp]
     L.rdxg_solve.argtypes = [vp, C.POINTER(SolveParams), vp, vp, vp]
     L.rdxg_solve_async.argtypes = [vp, C.POINTER(SolveParams)]

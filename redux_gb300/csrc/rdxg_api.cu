@@ -72,6 +72,9 @@ struct rdxg_solver {
     double* dRestore = nullptr;      // restoration scratch (allocated on first use)
     double* dFc = nullptr;           // [nObj] frequency cutoffs of the restoration
     float* dRestoreOut = nullptr;    // [P][nObj][ps][ps] restored objects
+    // optional restoration outputs (allocated on first use)
+    float *dObjFull = nullptr, *dPsf = nullptr, *dCobj = nullptr, *dRes = nullptr;
+    double *dFo = nullptr, *dOutPool = nullptr;
     bool fusedFd = false;     // half-plane finite-difference gradient (fits in shared memory)
     int npt = 0, chunk = 6, chunksPerPatch = 0, nH = 0, evalGrid = 0, reduceGrid = 0, numSMs = 0;
     std::vector<int32_t> objChunk0, hIdx, hPos;
@@ -902,8 +905,20 @@ int rdxg_metric_with_reference(rdxg_solver* h, const double* alpha_ref, const do
 
 int rdxg_restore(rdxg_solver* h, const double* alpha, const double* frequency_cutoff, int32_t no_filter,
                  float* objects) {
+    return rdxg_restore_ex(h, alpha, frequency_cutoff, no_filter, 0, objects, nullptr, nullptr, nullptr);
+}
+
+int rdxg_restore_ex(rdxg_solver* h, const double* alpha, const double* frequency_cutoff, int32_t no_filter,
+                    int32_t outputs, float* objects, float* psf, float* cobj, float* res) {
     if (!h || !alpha || !frequency_cutoff || !objects) return RDXG_ERR_ARG;
+    if (outputs & ~(RDXG_RESTORE_PSF | RDXG_RESTORE_PSF_AVG | RDXG_RESTORE_COBJ | RDXG_RESTORE_RESIDUAL))
+        return RDXG_ERR_ARG;
+    if ((outputs & (RDXG_RESTORE_PSF | RDXG_RESTORE_PSF_AVG)) && !psf) return RDXG_ERR_ARG;
+    if ((outputs & RDXG_RESTORE_COBJ) && !cobj) return RDXG_ERR_ARG;
+    if ((outputs & RDXG_RESTORE_RESIDUAL) && !res) return RDXG_ERR_ARG;
     if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
+    // the mean PSF takes precedence over the per-image PSFs (object.cpp:337)
+    if (outputs & RDXG_RESTORE_PSF_AVG) outputs &= ~RDXG_RESTORE_PSF;
     int r = h->fp64 ? upload_alpha<double>(h, alpha) : upload_alpha<float>(h, alpha);
     if (r) return r;
     // the OTFs at alpha on the full plane: a gradient-type evaluation keeps them
@@ -925,16 +940,34 @@ int rdxg_restore(rdxg_solver* h, const double* alpha, const double* frequency_cu
     }
     CK(h, cudaMemcpyAsync(h->dFc, frequency_cutoff, h->nObj * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (!h->dRestoreOut && (r = dalloc_t(h, &h->dRestoreOut, (size_t)h->Pmax * h->nObj * h->ps * h->ps))) return r;
-    RestoreArgs ra{h->dFc, no_filter ? 1 : 0, h->dRestore, h->dRestoreOut};
+    const size_t PO = (size_t)h->Pmax * h->nObj, G = (size_t)h->Pmax * h->I, ps2 = (size_t)h->ps * h->ps;
+    const int outGrid = h->numSMs * 2;
+    if (outputs && !h->dObjFull) {
+        if ((r = dalloc_t(h, &h->dObjFull, PO * N2)) || (r = dalloc(h, (void**)&h->dFo, PO * N2 * 2 * sizeof(double))) ||
+            (r = dalloc_t(h, &h->dOutPool, (size_t)outGrid * 3 * N2)) || (r = dalloc_t(h, &h->dPsf, G * ps2)) ||
+            (r = dalloc_t(h, &h->dCobj, G * ps2)) || (r = dalloc_t(h, &h->dRes, G * ps2)))
+            return r;
+    }
+    RestoreArgs ra{h->dFc, no_filter ? 1 : 0, h->dRestore, h->dRestoreOut, outputs ? h->dObjFull : nullptr};
+    RestoreOutArgs oa{outputs, h->dObjFull, (cx<double>*)h->dFo, h->dOutPool, h->dPsf, h->dCobj, h->dRes};
     cudaError_t ce = cudaSuccess;
     with_size(h->N, h->fp64, [&](auto L, auto t) {
         using T = decltype(t);
         KParams<T> kp = make_kparams<T>(h);
         ce = decltype(L)::restore(kp, ra, h->P * h->nObj, h->stream);
+        if (ce == cudaSuccess && outputs) ce = decltype(L)::restore_outputs(kp, oa, outGrid, h->stream);
     });
     if (ce != cudaSuccess) { h->err = std::string("restore: ") + cudaGetErrorString(ce); return RDXG_ERR_CUDA; }
-    CK(h, cudaMemcpyAsync(objects, h->dRestoreOut, (size_t)h->P * h->nObj * h->ps * h->ps * sizeof(float),
-                          cudaMemcpyDeviceToHost, h->stream));
+    const size_t P = h->P;
+    CK(h, cudaMemcpyAsync(objects, h->dRestoreOut, P * h->nObj * ps2 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    if (outputs & RDXG_RESTORE_PSF_AVG)
+        CK(h, cudaMemcpyAsync(psf, h->dPsf, P * h->nObj * ps2 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    if (outputs & RDXG_RESTORE_PSF)
+        CK(h, cudaMemcpyAsync(psf, h->dPsf, P * h->I * ps2 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    if (outputs & RDXG_RESTORE_COBJ)
+        CK(h, cudaMemcpyAsync(cobj, h->dCobj, P * h->I * ps2 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    if (outputs & RDXG_RESTORE_RESIDUAL)
+        CK(h, cudaMemcpyAsync(res, h->dRes, P * h->I * ps2 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     return RDXG_OK;
 }

@@ -68,6 +68,17 @@ cudaError_t Launcher<T, N>::restore(const KParams<T>& kp, const RestoreArgs& ra,
 }
 
 template <typename T, int N>
+cudaError_t Launcher<T, N>::restore_outputs(const KParams<T>& kp, const RestoreOutArgs& oa, int grid,
+                                            cudaStream_t st) {
+    const int sm = (int)((size_t)(kRestoreBand * Tile<N>::LDS + N) * sizeof(cx<double>));
+    const int nPo = kp.P * kp.nObj, nImg = kp.P * kp.I;
+    k_restore_objft<T, N, THREADS><<<grid < nPo ? grid : nPo, THREADS, sm, st>>>(kp, oa);
+    if (oa.flags & (kRestorePsf | kRestoreCobj | kRestoreResidual))
+        k_restore_images<T, N, THREADS><<<grid < nImg ? grid : nImg, THREADS, sm, st>>>(kp, oa);
+    return cudaGetLastError();
+}
+
+template <typename T, int N>
 size_t EvalLauncher<T, N>::smem(int M, int nH) {
     (void)M;
     // two tiles | twiddles | reference object | accumulators (4 x nH) | pupil amplitude |

@@ -21,6 +21,9 @@ struct Launcher {
     static void adjoint(const KParams<T>& kp, int grid, int kind, cudaStream_t st);   // grid-strides over the work list
     static void fd(const KParams<T>& kp, int grid, int M, cudaStream_t st);
     static cudaError_t restore(const KParams<T>& kp, const RestoreArgs& ra, int nBlocks, cudaStream_t st);
+    // PSF / convolved-object / residual outputs after restore(); grid: blocks (each with its
+    // 3 N^2 doubles of oa.pool)
+    static cudaError_t restore_outputs(const KParams<T>& kp, const RestoreOutArgs& oa, int grid, cudaStream_t st);
 };
 
 constexpr int kAccumThreads = 256;

@@ -14,9 +14,62 @@ struct RestoreArgs {
     int32_t noFilter;      // RF_NO_FILTER
     double* scratch;       // [P * nObj][kRestoreScratch * N * N]
     float* out;            // [P][nObj][ps][ps]
+    float* objFull;        // [P][nObj][N][N] the untrimmed float object (ObjectData::img before trim), or null
+};
+
+// Optional outputs of Object::restorePatch (object.cpp:335-383): PSFs, convolved objects and
+// residuals, trimmed to the patch like the object.
+enum : int32_t { kRestorePsf = 1, kRestorePsfAvg = 2, kRestoreCobj = 4, kRestoreResidual = 8 };
+struct RestoreOutArgs {
+    int32_t flags;
+    const float* objFull;  // [P][nObj][N][N]
+    cx<double>* Fo;        // [P][nObj][N][N] unnormalised transform of the float object
+    double* pool;          // [blocks][3 * N * N] per-block work: W (complex N x N) + one real N x N
+    float* psf;            // [P][I][ps][ps] (kRestorePsf) or [P][nObj][ps][ps] (kRestorePsfAvg)
+    float* cobj;           // [P][I][ps][ps]
+    float* res;            // [P][I][ps][ps]
 };
 constexpr int kRestoreScratch = 7;   // doubles per frequency: object (2), den, pt, rr, tmp, mask
-constexpr int kRestoreBand = 16;     // lines per band of the final inverse transform
+constexpr int kRestoreBand = 16;     // lines per band of the banded transforms (at most)
+// lines per band for an N x N transform: a divisor of N (16, or 8 for N = 88)
+template <int N> struct Band { static constexpr int value = N % kRestoreBand == 0 ? kRestoreBand : 8; };
+
+// 2-D transform (DIR -1 forward, +1 backward, unnormalised) of the N x N array given by
+// load(y, x), in bands of Band<N> lines through shared memory s ([B][LDS]) with the row
+// results in W (N x N, global); store(y, x, v) receives every output value once.
+template <int N, int DIR, int THREADS, typename Load, typename Store>
+__device__ __forceinline__ void fft2_banded(Load load, Store store, cx<double>* W, cx<double>* s,
+                                            const cx<double>* tw) {
+    constexpr int B = Band<N>::value, LDS = Tile<N>::LDS;
+    static_assert(N % B == 0, "bands tile the array");
+    for (int r0 = 0; r0 < N; r0 += B) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < B * N; i += THREADS) s[(i / N) * LDS + i % N] = load(r0 + i / N, i % N);
+        __syncthreads();
+        fft_lines<double, N, DIR, B, true, THREADS>(s, 0, tw, threadIdx.x);
+        for (int i = threadIdx.x; i < B * N; i += THREADS) W[(r0 + i / N) * N + i % N] = s[(i / N) * LDS + i % N];
+    }
+    for (int c0 = 0; c0 < N; c0 += B) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < B * N; i += THREADS) {
+            const int col = c0 + i % B, y = i / B;
+            s[(i % B) * LDS + y] = W[y * N + col];
+        }
+        __syncthreads();
+        fft_lines<double, N, DIR, B, true, THREADS>(s, 0, tw, threadIdx.x);
+        for (int i = threadIdx.x; i < B * N; i += THREADS) store(i % N, c0 + i / N, s[(i / N) * LDS + i % N]);
+    }
+    __syncthreads();
+}
+
+template <int N, int THREADS>
+__device__ __forceinline__ void restore_twiddles(cx<double>* tw) {
+    for (int k = threadIdx.x; k < N; k += THREADS) {
+        double sn, cs;
+        sincospi(2.0 * k / N, &sn, &cs);
+        tw[k] = mkc<double>(cs, -sn);
+    }
+}
 
 // smooth (utils.cpp:304-328): mean over [y-nY, y+nY) x [x-nX, x+nX) clipped to the array, the
 // sum in the reference's order
@@ -126,10 +179,11 @@ __global__ void __launch_bounds__(THREADS) k_restore(KParams<T> kp, RestoreArgs 
         __syncthreads();
     }
     // ift: un-centre, backward transform, real part / N^2.  The rows and then the columns
-    // are transformed in bands of kRestoreBand lines through shared memory (an N x N FP64
+    // are transformed in bands of Band<N> lines through shared memory (an N x N FP64
     // tile does not fit for N = 128); the row results go to W (the den and pt arrays).
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int B = kRestoreBand;
+    constexpr int B = Band<N>::value;
+    static_assert(N % B == 0, "bands tile the array");
     cx<double>* s = reinterpret_cast<cx<double>*>(smem_raw);     // [B][LDS]
     cx<double>* tw = s + B * LDS;
     cx<double>* W = reinterpret_cast<cx<double>*>(den);
@@ -161,9 +215,118 @@ __global__ void __launch_bounds__(THREADS) k_restore(KParams<T> kp, RestoreArgs 
         fft_lines<double, N, +1, B, true, THREADS>(s, 0, tw, threadIdx.x);
         for (int i = threadIdx.x; i < B * N; i += THREADS) {
             const int x = c0 + i / N, y = i % N;
-            if (x >= off && x < off + ps && y >= off && y < off + ps)
-                out[(y - off) * ps + (x - off)] = (float)(s[(i / N) * LDS + y].x / (double)N2);
+            const float v = (float)(s[(i / N) * LDS + y].x / (double)N2);
+            if (x >= off && x < off + ps && y >= off && y < off + ps) out[(y - off) * ps + (x - off)] = v;
+            if (ra.objFull) ra.objFull[(size_t)b * N2 + y * N + x] = v;
         }
+    }
+}
+
+// Per (patch, object): the unnormalised transform of the float object (the convolution of
+// SubImage::convolveImage transforms ObjectData::img, fouriertransform.hpp:310-324) and, for
+// kRestorePsfAvg, the mean PSF of the object's images (SubImage::addPSF summed in image order
+// in FP64, stored as float and scaled by 1/count, object.cpp:345-350).
+template <typename T, int N, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_restore_objft(KParams<T> kp, RestoreOutArgs oa) {
+    constexpr int N2 = N * N, LDS = Tile<N>::LDS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<double>* s = reinterpret_cast<cx<double>*>(smem_raw);
+    cx<double>* tw = s + kRestoreBand * LDS;
+    restore_twiddles<N, THREADS>(tw);
+    cx<double>* W = reinterpret_cast<cx<double>*>(oa.pool + (size_t)blockIdx.x * 3 * N2);
+    double* acc = oa.pool + (size_t)blockIdx.x * 3 * N2 + 2 * N2;
+    const int ps = kp.ps, off = (N - ps) / 2;
+    for (int b = blockIdx.x; b < kp.P * kp.nObj; b += gridDim.x) {
+        const float* img = oa.objFull + (size_t)b * N2;
+        cx<double>* F = oa.Fo + (size_t)b * N2;
+        fft2_banded<N, -1, THREADS>([&](int y, int x) { return mkc<double>((double)img[y * N + x], 0.0); },
+                                    [&](int y, int x, cx<double> v) { F[y * N + x] = v; }, W, s, tw);
+        if (!(oa.flags & kRestorePsfAvg)) continue;
+        const int p = b / kp.nObj, o = b % kp.nObj;
+        const int first = kp.objFirst[o], cnt = kp.objCount[o];
+        for (int c = threadIdx.x; c < N2; c += THREADS) acc[c] = 0.0;
+        for (int j = 0; j < cnt; ++j) {
+            const cx<T>* S = kp.S + ((size_t)p * kp.I + first + j) * N2;
+            // PSF = reorder(real(ift(reorder(OTF))) / N^2) (OTF flags REORDER_IMG|REORDER_FT|
+            // NORMALIZE_FT, subimage.cpp:89-90, 615-626)
+            fft2_banded<N, +1, THREADS>(
+                [&](int y, int x) {
+                    const cx<T> v = S[((y + N / 2) % N) * N + (x + N / 2) % N];
+                    return mkc<double>((double)v.x, (double)v.y);
+                },
+                [&](int y, int x, cx<double> v) {
+                    acc[((y + N / 2) % N) * N + (x + N / 2) % N] += v.x / (double)N2;
+                },
+                W, s, tw);
+        }
+        float* out = oa.psf + (size_t)b * ps * ps;
+        const double inv = 1.0 / cnt;
+        for (int c = threadIdx.x; c < ps * ps; c += THREADS) {
+            const int y = c / ps + off, x = c % ps + off;
+            out[c] = (float)((double)(float)acc[y * N + x] * inv);
+        }
+        __syncthreads();
+    }
+}
+
+// Per image: the PSF (SubImage::getPSF), the convolved object (SubImage::convolveImage of the
+// float object: real(ift(ft(img) / N^2 * OTF)) with the OTF un-centred) and the residual
+// (convolved object as float minus the image, SubImage::convolvedResidual / residual,
+// subimage.hpp:110-129, the image being real(ift(D)) / N^2, the windowed and padded cutout).
+template <typename T, int N, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_restore_images(KParams<T> kp, RestoreOutArgs oa) {
+    constexpr int N2 = N * N, LDS = Tile<N>::LDS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<double>* s = reinterpret_cast<cx<double>*>(smem_raw);
+    cx<double>* tw = s + kRestoreBand * LDS;
+    restore_twiddles<N, THREADS>(tw);
+    cx<double>* W = reinterpret_cast<cx<double>*>(oa.pool + (size_t)blockIdx.x * 3 * N2);
+    double* img = oa.pool + (size_t)blockIdx.x * 3 * N2 + 2 * N2;
+    const int ps = kp.ps, off = (N - ps) / 2;
+    auto trimmed = [&](int y, int x) { return y >= off && y < off + ps && x >= off && x < off + ps; };
+    for (int g = blockIdx.x; g < kp.P * kp.I; g += gridDim.x) {
+        const int p = g / kp.I, j = g % kp.I, o = kp.imgObj[j];
+        const cx<T>* S = kp.S + (size_t)g * N2;
+        auto otfU = [&](int y, int x) {   // the OTF with the zero frequency at (0, 0)
+            const cx<T> v = S[((y + N / 2) % N) * N + (x + N / 2) % N];
+            return mkc<double>((double)v.x, (double)v.y);
+        };
+        if (oa.flags & kRestorePsf) {
+            float* out = oa.psf + (size_t)g * ps * ps;
+            fft2_banded<N, +1, THREADS>(otfU,
+                                        [&](int y, int x, cx<double> v) {
+                                            const int yy = (y + N / 2) % N, xx = (x + N / 2) % N;
+                                            if (trimmed(yy, xx))
+                                                out[(yy - off) * ps + (xx - off)] = (float)(v.x / (double)N2);
+                                        },
+                                        W, s, tw);
+        }
+        if (!(oa.flags & (kRestoreCobj | kRestoreResidual))) continue;
+        if (oa.flags & kRestoreResidual) {
+            const cx<T>* D = kp.D + (size_t)g * N2;
+            fft2_banded<N, +1, THREADS>(
+                [&](int y, int x) {
+                    const cx<T> v = D[((y + N / 2) % N) * N + (x + N / 2) % N];
+                    return mkc<double>((double)v.x, (double)v.y);
+                },
+                [&](int y, int x, cx<double> v) { img[y * N + x] = v.x / (double)N2; }, W, s, tw);
+        }
+        const cx<double>* F = oa.Fo + ((size_t)p * kp.nObj + o) * N2;
+        float* co = oa.cobj ? oa.cobj + (size_t)g * ps * ps : nullptr;
+        float* re = oa.res ? oa.res + (size_t)g * ps * ps : nullptr;
+        fft2_banded<N, +1, THREADS>(
+            [&](int y, int x) {
+                const cx<double> f = F[y * N + x], t = otfU(y, x);
+                return mkc<double>(f.x * t.x - f.y * t.y, f.x * t.y + f.y * t.x);
+            },
+            [&](int y, int x, cx<double> v) {
+                if (!trimmed(y, x)) return;
+                const float c = (float)(v.x / (double)N2);
+                const int q = (y - off) * ps + (x - off);
+                if ((oa.flags & kRestoreCobj) && co) co[q] = c;
+                if ((oa.flags & kRestoreResidual) && re) re[q] = (float)((double)c - img[y * N + x]);
+            },
+            W, s, tw);
     }
 }
 

@@ -157,6 +157,36 @@ class Solver:
                     "rdxg_restore")
         return out
 
+    def restore_outputs(self, alpha, frequency_cutoff, no_filter: bool = False, psf: str = None,
+                        cobj: bool = False, residual: bool = False) -> dict:
+        """Restored objects plus the optional outputs of Object::restorePatch
+        (rdxg_restore_ex): psf None, "each" ([P][I][ps][ps]) or "mean" ([P][nObj][ps][ps]);
+        cobj and residual [P][I][ps][ps]."""
+        a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
+        nObj, ps = self.job.n_objects, self.job.patch_size
+        fc = np.ascontiguousarray(np.broadcast_to(np.asarray(frequency_cutoff, np.float64), (nObj,)))
+        flags = 0
+        out = {"objects": np.zeros((self.P, nObj, ps, ps), np.float32)}
+        if psf == "each":
+            flags |= _lib.RDXG_RESTORE_PSF
+            out["psf"] = np.zeros((self.P, self.I, ps, ps), np.float32)
+        elif psf == "mean":
+            flags |= _lib.RDXG_RESTORE_PSF_AVG
+            out["psf"] = np.zeros((self.P, nObj, ps, ps), np.float32)
+        elif psf is not None:
+            raise ValueError("psf: None, 'each' or 'mean'")
+        if cobj:
+            flags |= _lib.RDXG_RESTORE_COBJ
+            out["cobj"] = np.zeros((self.P, self.I, ps, ps), np.float32)
+        if residual:
+            flags |= _lib.RDXG_RESTORE_RESIDUAL
+            out["residual"] = np.zeros((self.P, self.I, ps, ps), np.float32)
+        self._check(_lib.load().rdxg_restore_ex(self.h, _lib.ptr(a), _lib.ptr(fc), int(bool(no_filter)), flags,
+                                                _lib.ptr(out["objects"]), _lib.ptr(out.get("psf")),
+                                                _lib.ptr(out.get("cobj")), _lib.ptr(out.get("residual"))),
+                    "rdxg_restore_ex")
+        return out
+
     def gradient(self, alpha, method: str = "vogel", enabled=None):
         a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
         g = np.zeros((self.P, self.I, self.M))

@@ -1,6 +1,7 @@
 // Test driver for include/rdxg_solver.hpp: reads a job and patches written by
 // tests/test_cpp_shim.py (raw little-endian arrays, one file each), solves them through
-// rdxg::Solver and writes alpha, metrics, reports and restored objects back.
+// rdxg::Solver and writes alpha, metrics, reports, restored objects, PSFs, convolved objects
+// and residuals back.
 #include <cstdio>
 #include <stdexcept>
 #include <string>
@@ -65,6 +66,7 @@ int main(int argc, char** argv) {
         set.minIterations = (int32_t)sv[3]; set.targetIterations = (int32_t)sv[4];
         set.finiteDifferenceFirst = sv[5] != 0; set.ftol = sv[6]; set.eps = sv[7]; set.maxMetrics = (int32_t)sv[8];
         set.restore = true;
+        if (sv.size() > 9) set.saveMask = (int32_t)sv[9];
         rdxg::Solver solver(g, s, set, load<double>(dir, "fc.f64"));
         solver.init();
         const auto cut = load<float>(dir, "cutouts.f32");
@@ -80,8 +82,11 @@ int main(int argc, char** argv) {
         }
         solver.run(batch);
         std::vector<double> alpha, metrics, rep;
-        std::vector<float> obj;
+        std::vector<float> obj, psf, cobj, res;
         for (int p = 0; p < P; ++p) {
+            psf.insert(psf.end(), pd[p].psf.begin(), pd[p].psf.end());
+            cobj.insert(cobj.end(), pd[p].cobj.begin(), pd[p].cobj.end());
+            res.insert(res.end(), pd[p].res.begin(), pd[p].res.end());
             alpha.insert(alpha.end(), pd[p].alpha.begin(), pd[p].alpha.end());
             std::vector<double> m(set.maxMetrics, 0.0);
             std::copy(pd[p].metrics.begin(), pd[p].metrics.end(), m.begin());
@@ -98,6 +103,9 @@ int main(int argc, char** argv) {
         save(dir, "metrics.out.f64", metrics);
         save(dir, "report.out.f64", rep);
         save(dir, "objects.out.f32", obj);
+        save(dir, "psf.out.f32", psf);
+        save(dir, "cobj.out.f32", cobj);
+        save(dir, "res.out.f32", res);
     } catch (const std::exception& e) {
         std::fprintf(stderr, "shim_solve: %s\n", e.what());
         return 1;

@@ -31,7 +31,7 @@ def test_shim_compiles_and_links(tmp_path):
     assert os.path.exists(exe)
 
 
-def _dump(job, cutouts, fixed_gamma, st, fc, d):
+def _dump(job, cutouts, fixed_gamma, st, fc, d, save_mask=0):
     sup, ns = job.support, job.nullspace
     geom = [job.otf_size, job.pupil_pixels, job.patch_size, job.n_modes, job.n_objects, job.n_images,
             job.n_channels, job.tilt_x, job.tilt_y, ns.n_free, job.cutout_size, cutouts.shape[0], 0, 0]
@@ -44,7 +44,8 @@ def _dump(job, cutouts, fixed_gamma, st, fc, d):
         "noise_window.f64": job.noise_window, "ns_rows.i32": ns.rows, "ns_cols.i32": ns.cols,
         "ns_vals.f64": ns.vals, "tilt_jacobian.f64": np.asarray(job.J_T_xy).ravel(),
         "settings.f64": [st.mode_start, st.mode_step, st.max_iterations, st.min_iterations,
-                         st.target_iterations, float(st.fd_first), st.ftol, st.eps, st.max_metrics],
+                         st.target_iterations, float(st.fd_first), st.ftol, st.eps, st.max_metrics,
+                         float(save_mask)],
         "fc.f64": np.full(job.n_objects, fc), "cutouts.f32": cutouts,
     }
     if fixed_gamma is not None:
@@ -62,7 +63,11 @@ def test_shim_solve_matches_the_python_harness(tmp_path, cfg):
     st = S.SolveSettings(mode_start=5, mode_step=5, max_iterations=6, min_iterations=3, ftol=1e-3, max_metrics=128)
     fc = job.otf_size / 2.0
     d = str(tmp_path)
-    _dump(job, w.patches.cutouts, w.patches.fixed_gamma, st, fc, d)
+    # per-image PSFs for one configuration, the object means for the other
+    from redux_gb300 import _lib
+    psf_flag = _lib.RDXG_RESTORE_PSF if cfg == 0 else _lib.RDXG_RESTORE_PSF_AVG
+    _dump(job, w.patches.cutouts, w.patches.fixed_gamma, st, fc, d,
+          save_mask=psf_flag | _lib.RDXG_RESTORE_COBJ | _lib.RDXG_RESTORE_RESIDUAL)
     exe = _build(d)
     r = subprocess.run([exe, d], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
@@ -85,6 +90,13 @@ def test_shim_solve_matches_the_python_harness(tmp_path, cfg):
         assert rep[3 * p] == out["reports"][p].final_metric
         assert rep[3 * p + 1] == out["reports"][p].iterations
     np.testing.assert_allclose(obj, ref_obj, rtol=0, atol=1e-5 * np.abs(ref_obj).max())
+    ps = job.patch_size
+    ref = s.restore_outputs(out["alpha"], fc, psf="each" if cfg == 0 else "mean", cobj=True, residual=True)
+    for name in ("psf", "cobj", "res"):
+        key = "residual" if name == "res" else name
+        got = np.fromfile(os.path.join(d, f"{name}.out.f32"), np.float32).reshape(ref[key].shape)
+        scale = np.abs(ref["cobj"]).max() if name == "res" else np.abs(ref[key]).max()
+        np.testing.assert_allclose(got, ref[key], rtol=0, atol=1e-5 * scale)
     # Solver::metric at the final alpha of the last patch
     m = s.metric(np.repeat(out["alpha"][P - 1:P], P, axis=0))[P - 1]
     assert abs(rep[3 * P] - m) <= 1e-6 * abs(m)

@@ -37,3 +37,29 @@ def test_smooth_window_is_the_references():
     assert s[0, 0] == 0.0
     assert s[1, 1] == (d[0, 0] + d[0, 1] + d[1, 0] + d[1, 1]) / 4
     assert s[3, 0] == (d[2, 0] + d[3, 0]) / 2
+
+
+def test_restore_outputs_properties(w0):
+    # the statement of the PSF, convolved-object and residual outputs: a PSF sums to the OTF
+    # at zero frequency; the convolved object of a unit impulse at the origin is the
+    # un-centred PSF; the residual of the convolved object is that minus the cutout image
+    op = oracle.OraclePatch(w0.job)
+    op.set_images(w0.patches.cutouts[0], None, w0.patches.fixed_gamma[0])
+    a = w0.patches.alpha_true[0]
+    op.metric(a)
+    D, S = op.D(), op.otf()
+    N, ps, I = w0.job.otf_size, w0.job.patch_size, w0.job.n_images
+    obj = op.restore(a, N / 2.0)
+    psf, psf_mean, cobj, res = np_oracle.restore_outputs(D, S, w0.job.img_object, obj, ps)
+    for j in range(I):
+        assert abs(psf[j].astype(np.float64).sum() - S[j, N // 2, N // 2].real) <= 1e-6 * abs(S[j, N // 2, N // 2])
+    np.testing.assert_allclose(psf_mean[0], psf[w0.job.img_object == 0].astype(np.float64).mean(0),
+                               rtol=0, atol=1e-6 * np.abs(psf).max())
+    delta = np.zeros((1, N, N))
+    delta[0, 0, 0] = 1.0
+    _, _, cd, _ = np_oracle.restore_outputs(D, S, np.zeros(I, int), delta, ps)
+    np.testing.assert_allclose(cd[0], np.fft.ifftshift(psf[0]), rtol=0, atol=1e-6 * np.abs(psf[0]).max())
+    img = np.real(np.fft.ifft2(np.fft.ifftshift(D[0])))
+    np.testing.assert_allclose(res[0], cobj[0].astype(np.float64) - img, rtol=0, atol=1e-3)
+    # the image is the windowed, mean-padded cutout: its mean is the cutout mean
+    assert abs(img.mean() - op.stats()[0][0]) <= 1e-6 * abs(op.stats()[0][0])
