@@ -265,8 +265,14 @@ def main():
     share = {"forward": rounds * kt["forward"], "accum": rounds * kt["accum"], "adjoint": ndf * kt["adjoint"]}
     dom = max(share, key=share.get)
     achieved = per_launch[dom]["bytes"] / (kt[dom] / 1000.0) / 1e9
+    # DRAM bytes per image of the forward pass from ncu captures of the 64-patch batch
+    # (k_eval: 80.9 MB read + 3.4 MB written for 2304 images; k_phase_tc: 0.95 MB read, its
+    # phases stay in L2), scaled to this launch by the images it evaluates
+    traffic = {"forward": G * (84.3e6 + 0.95e6) / 2304.0} if (N, M) == (88, 36) else {}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm"], "traffic": None, "kernel": dom,
+                "frac": achieved / peaks["hbm"], "traffic": traffic.get(dom),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 64-patch capture scaled by images"
+                if dom in traffic else None, "kernel": dom,
                 "peak_source": peaks["src"], "kernel_ms": kt,
                 "share_ms_per_step": share,
                 "fp32_tflops": {k: per_launch[k]["flops"] / (kt[k] / 1000.0) / 1e12 for k in per_launch}}
