@@ -210,7 +210,7 @@ EvalParams<T> make_evalparams(rdxg_solver* h) {
     e.k = make_kparams<T>(h);
     e.hp.nH = h->nH; e.hp.idx = h->dHIdx; e.hp.chunkSize = h->chunk;
     e.hp.chunksPerPatch = h->chunksPerPatch; e.hp.objChunk0 = h->dObjChunk0;
-    e.Dh = (const cx<T>*)h->dDh; e.Oh = (cx<T>*)h->dOh; e.part = (T*)h->dPart;
+    e.Dh = (const cx<T>*)h->dDh; e.Oh = (cx<T>*)h->dOh; e.part = (Acc4<T>*)h->dPart;
     e.objMetric = h->dObjMetric; e.L = make_lists(h);
     e.hPos = h->dHPos; e.nTilesH = h->nTilesH; e.phi = (T*)h->dPhiImg;
     e.nCh = h->C;
@@ -875,7 +875,7 @@ int rdxg_metric_noalloc(rdxg_solver* h, const double* alpha, double* metric) {
             EvalParams<float> e = make_evalparams<float>(h);
             e.k.alphaEff = dAe;
             e.phi = reinterpret_cast<float*>(sb + oPhi);
-            e.part = reinterpret_cast<float*>(sb + oPart);
+            e.part = reinterpret_cast<Acc4<float>*>(sb + oPart);
             e.objMetric = dObj;
             e.L = L;
             decltype(E)::phase(e, h->phaseGrid, h->stream);

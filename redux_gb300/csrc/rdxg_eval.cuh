@@ -47,6 +47,10 @@ struct Lists {
     int32_t* counters;                  // base of the counters (reset every round)
 };
 
+// Per half-plane point sums of a chunk: R = sum |D - O'S|^2, Q = sum |S|^2, P' = sum conj(D - O'S) S,
+// one 16-byte record per point (one vector load and store per update)
+template <typename T> struct alignas(4 * sizeof(T)) Acc4 { T r, q, pr, pi; };
+
 struct HalfPlane {
     int32_t nH;
     const int32_t* idx;     // [nH] centred index of each half-plane support point
@@ -80,7 +84,7 @@ struct EvalParams {
     HalfPlane hp;
     const cx<T>* Dh;    // [g][nH] half-plane image transforms
     cx<T>* Oh;          // [po][nH] reference objects
-    T* part;            // [P*chunksPerPatch][4][nH]  (R, Q, P're, P'im)
+    Acc4<T>* part;      // [P*chunksPerPatch][nH] (R, Q, P're, P'im)
     double* objMetric;  // [po][tiles] object metric summed over tiles of 32 half-plane points
     const int32_t* hPos; // [nH] tile position (row * (N+1) + column) of each half-plane point
     int32_t nTilesH;    // point tiles (32 points) per object in the reduction
@@ -309,7 +313,7 @@ template <typename T, int N, int THREADS>
 __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phiBuf, const T* A, T c, int df,
                                            cx<T>* PF, cx<T>* X, cx<T>* S, const cx<T>* __restrict__ Dg,
                                            cx<T>* a, cx<T>* b, const cx<T>* tw, const cx<T>* oh,
-                                           T* acc, const uint16_t* hpos, const int* hidx, int nH) {
+                                           Acc4<T>* acc, const uint16_t* hpos, const int* hidx, int nH) {
     constexpr int n = N / 2, N2 = N * N;
     static_assert(sizeof(cx<T>) == 8, "staging copies 8-byte elements");
     using St = Stage<N>;
@@ -362,10 +366,12 @@ __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phi
         const cx<T> d = (h < St::kPart ? a : b)[St::dh_slot(h)];
         const cx<T> r = csub<T>(d, cmul<T>(oh[h], sv));
         // R += |r|^2, Q += |S|^2, P' += conj(r) S
-        acc[h] += cnorm<T>(r);
-        acc[nH + h] += cnorm<T>(sv);
-        acc[2 * nH + h] += r.x * sv.x + r.y * sv.y;
-        acc[3 * nH + h] += r.x * sv.y - r.y * sv.x;
+        Acc4<T> u = acc[h];
+        u.r += cnorm<T>(r);
+        u.q += cnorm<T>(sv);
+        u.pr += r.x * sv.x + r.y * sv.y;
+        u.pi += r.x * sv.y - r.y * sv.x;
+        acc[h] = u;
     }
 }
 
@@ -375,14 +381,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
     constexpr int n = N / 2, n2 = n * n, N2 = N * N;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nH = e.hp.nH;
-    // shared memory: two tiles | twiddles | reference object | accumulators (4 x nH) |
+    // shared memory: two tiles | twiddles | accumulators (nH records) | reference object |
     //                pupil amplitude | phases of the image | tile positions (16-bit)
     cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* s2 = s + Tile<N>::ELEMS;
     cx<T>* tw = s2 + Tile<N>::ELEMS;
-    cx<T>* oh = tw + N;
-    T* acc = reinterpret_cast<T*>(oh + nH);
-    T* amp = acc + 4 * nH;
+    Acc4<T>* acc = reinterpret_cast<Acc4<T>*>(tw + N);
+    static_assert((2 * Tile<N>::ELEMS + N) % 2 == 0, "accumulator records 16-byte aligned");
+    cx<T>* oh = reinterpret_cast<cx<T>*>(acc + nH);
+    T* amp = reinterpret_cast<T*>(oh + nH);
     T* phiBuf = amp + n2;
     uint16_t* hpos = reinterpret_cast<uint16_t*>(phiBuf + n2);
     static_assert(Tile<N>::ELEMS <= 65536, "tile positions are 16-bit");
@@ -401,8 +408,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
         const size_t po = (size_t)it.p * e.k.nObj + it.o;
         if (jj == 0) {
             __syncthreads();    // previous item's accumulators written out
-            for (int h = threadIdx.x; h < nH; h += THREADS) oh[h] = e.Oh[po * nH + h];
-            for (int i = threadIdx.x; i < 4 * nH; i += THREADS) acc[i] = (T)0;
+            for (int h = threadIdx.x; h < nH; h += THREADS) {
+                oh[h] = e.Oh[po * nH + h];
+                acc[h] = Acc4<T>{0, 0, 0, 0};
+            }
         }
         // the image after this one (same item, or the first of the block's next item)
         int nextItem = item, nextJj = jj + 1;
@@ -420,8 +429,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
                                   e.k.S + g * N2, e.Dh + g * nH, s, s2, tw, oh, acc, hpos, e.hp.idx, nH);
         if (nextJj == 0) {
             __syncthreads();
-            T* part = e.part + (size_t)(it.p * e.hp.chunksPerPatch + it.chunk) * 4 * nH;
-            for (int i = threadIdx.x; i < 4 * nH; i += THREADS) part[i] = acc[i];
+            Acc4<T>* part = e.part + (size_t)(it.p * e.hp.chunksPerPatch + it.chunk) * nH;
+            for (int h = threadIdx.x; h < nH; h += THREADS) part[h] = acc[h];
             if (nextItem >= nItems) break;
             item = nextItem;
             it = nit;
@@ -555,14 +564,14 @@ __global__ void __launch_bounds__(THREADS) k_reduce(EvalParams<T> e) {
         const T gam = (T)e.k.gamma[po];
         const int c0 = e.hp.objChunk0[it.o];
         const int nc = (e.k.objCount[it.o] + e.hp.chunkSize - 1) / e.hp.chunkSize;
-        const T* base = e.part + (size_t)(it.p * e.hp.chunksPerPatch + c0) * 4 * nH;
+        const Acc4<T>* base = e.part + (size_t)(it.p * e.hp.chunksPerPatch + c0) * nH;
         double acc = 0;
         const int h = tile * 32 + lane;
         if (h < nH) {
             T R = 0, Q = 0, Pr = 0, Pi = 0;
             for (int c = 0; c < nc; ++c) {
-                const T* pc = base + (size_t)c * 4 * nH + h;
-                R += pc[0]; Q += pc[nH]; Pr += pc[2 * nH]; Pi += pc[3 * nH];
+                const Acc4<T> u = base[(size_t)c * nH + h];
+                R += u.r; Q += u.q; Pr += u.pr; Pi += u.pi;
             }
             const cx<T> oh = e.Oh[po * nH + h];
             const T Qt = gam + Q;
