@@ -48,8 +48,11 @@ def _headers():
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
+    """Compiles what changed (everything with force).  RDXG_NVCC_FLAGS adds nvcc options,
+    e.g. -DRDXG_EVAL_THREADS=384 for the block size of the evaluation kernels."""
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
+    extra = os.environ.get("RDXG_NVCC_FLAGS", "").split()
     hdrs = _headers()
     jobs = []
     objs = []
@@ -58,7 +61,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
         if force or _newer(o, [s] + hdrs):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-c", s, "-o", o])
+            jobs.append([nvcc] + NVCC_FLAGS + extra + ["-c", s, "-o", o])
     cxx = os.environ.get("CXX", "g++")
     for src in CXX_SOURCES:
         s = os.path.join(CSRC, src)

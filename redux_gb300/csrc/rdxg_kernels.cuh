@@ -349,18 +349,16 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
     const cx<T>* Oo = kp.O + po * N2;
     const cx<T>* Dg = kp.D + (size_t)g * N2;
     const cx<T>* Sg = kp.S + (size_t)g * N2;
-    // unrolled so that each thread has several iterations' global loads in flight
+    // unrolled, and the loads issued before the support test, so that each thread has
+    // several iterations' global loads in flight in one round trip
 #pragma unroll 8
     for (int i = threadIdx.x; i < N2; i += THREADS) {
         const int y = i / N, x = i % N;                 // un-centred (lag) position
         const int c = ((y + N / 2) % N) * N + (x + N / 2) % N;
-        cx<T> G = mkc<T>(0, 0);
-        if (kp.otfMask[c] && !(y == 0 && x == 0)) {
-            const cx<T> O = Oo[c];
-            const cx<T> r = csub<T>(Dg[c], cmul<T>(O, Sg[c]));
-            G = cmulc<T>(r, O);                           // conj(O) r
-        }
-        s[y * LDS + x] = G;
+        const uint8_t m = kp.otfMask[c];
+        const cx<T> O = Oo[c], D = Dg[c], S = Sg[c];
+        const cx<T> G = cmulc<T>(csub<T>(D, cmul<T>(O, S)), O);   // conj(O) (D - O S)
+        s[y * LDS + x] = (m && !(y == 0 && x == 0)) ? G : mkc<T>(0, 0);
     }
     __syncthreads();
     fft2d<T, N, -1, THREADS, false>(s, tw);

@@ -31,8 +31,13 @@ constexpr int kCgThreads = 256;
 
 template <typename T> void launch_accum(const KParams<T>& kp, int nPo, cudaStream_t st);
 
-// fused evaluation (FP32, N <= 88): points per thread chosen at run time
-constexpr int kEvalThreads = 512;
+// fused evaluation (FP32, N <= 88): block size of k_eval and k_fd_half (a multiple of 32;
+// the transform stages stride over any size)
+#ifndef RDXG_EVAL_THREADS
+#define RDXG_EVAL_THREADS 512
+#endif
+constexpr int kEvalThreads = RDXG_EVAL_THREADS;
+static_assert(kEvalThreads % 32 == 0 && kEvalThreads <= 1024, "block size");
 constexpr int kReduceThreads = 256;
 constexpr int kPhasePix = 256;      // pixels per block of the mode expansion
 constexpr int kMaxChunk = 8;        // images per chunk (upper bound)
