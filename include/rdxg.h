@@ -196,6 +196,15 @@ int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* params);
 int rdxg_fetch_results(rdxg_solver* h, double* alpha_out, rdxg_patch_report* reports,
                        double* metrics);
 
+/* Solver::run for the patches of several handles at once, e.g. one handle per patch
+ * geometry (OTF size, frames, modes) of an uneven batch: the rounds of every handle are
+ * captured into one CUDA graph, one branch per handle forked from the first handle's stream
+ * (give each handle its own stream for the branches to run concurrently), and the graph is
+ * launched until no handle has an active patch.  Every handle's results are then read with
+ * rdxg_fetch_results; they are the same as those of rdxg_solve on that handle alone.  All
+ * handles on one device, each listed once. */
+int rdxg_solve_many(rdxg_solver* const* handles, int32_t n, const rdxg_solve_params* params);
+
 /* Number of kernel launches issued by the last rdxg_solve / rdxg_solve_async. */
 int64_t rdxg_last_launch_count(const rdxg_solver* h);
 

@@ -16,7 +16,7 @@ RDXG_RESTORE_PSF, RDXG_RESTORE_PSF_AVG, RDXG_RESTORE_COBJ, RDXG_RESTORE_RESIDUAL
 
 EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "rdxg_set_stream",
             "rdxg_set_patches", "rdxg_set_patches_device", "rdxg_metric", "rdxg_gradient",
-            "rdxg_solve", "rdxg_solve_async", "rdxg_fetch_results", "rdxg_last_launch_count",
+            "rdxg_solve", "rdxg_solve_async", "rdxg_solve_many", "rdxg_fetch_results", "rdxg_last_launch_count",
             "rdxg_debug_copy", "rdxg_cg_minimize", "rdxg_profile_kernels", "rdxg_metric_with_reference",
             "rdxg_metric_noalloc", "rdxg_restore", "rdxg_restore_ex", "rdxg_set_phase_mode", "rdxg_phase_mode")
 
@@ -84,6 +84,7 @@ def load(path: str = LIB_PATH):
     L.rdxg_gradient.argtypes = [vp, vp, vp, C.c_int32, vp, vp]
     L.rdxg_solve.argtypes = [vp, C.POINTER(SolveParams), vp, vp, vp]
     L.rdxg_solve_async.argtypes = [vp, C.POINTER(SolveParams)]
+    L.rdxg_solve_many.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(SolveParams)]
     L.rdxg_fetch_results.argtypes = [vp, vp, vp, vp]
     L.rdxg_last_launch_count.restype = C.c_int64
     L.rdxg_last_launch_count.argtypes = [vp]

@@ -1015,108 +1015,19 @@ int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, i
     return RDXG_OK;
 }
 
-// Runs the rounds as a CUDA graph of `check` rounds: the kernels that are only needed in
-// some rounds (image re-initialisation after a re-shift, the adjoint, the finite-difference
-// gradient) sit in conditional nodes whose conditions k_shift sets from the round's work-list
-// counters.  The host launches the graph and reads the active-patch counter after each launch.
 extern "C++" {
-template <typename RoundFn>
-int solve_rounds_graph(rdxg_solver* h, ShiftArgs sa, int check, RoundFn&& round_launches) {
-    cudaStream_t st = h->stream;
-    if (!h->side) CK(h, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
-    if (!h->dLaunchCount) {
-        int r = dalloc_t(h, &h->dLaunchCount, 1);
-        if (r) return r;
-    }
-    CK(h, cudaMemsetAsync(h->dLaunchCount, 0, sizeof(unsigned long long), st));
-    CK(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    cudaGraph_t graph = nullptr;
-    cudaError_t ce = cudaSuccess;
-    const char* what = "capture info";
-    {
-        cudaStreamCaptureStatus status;
-        ce = cudaStreamGetCaptureInfo(st, &status, nullptr, &graph, nullptr, nullptr, nullptr);
-    }
-    // a handle belongs to one conditional node: three new ones per round
-    cudaGraphConditionalHandle cond[3] = {};
-    sa.useConditions = 1;
-    sa.counters = h->dCounters;
-    sa.fixedLaunches = h->fused ? 5 : 4;
-    sa.launchCount = h->dLaunchCount;
-    // optional kernel k: an IF node on cond[k] after the captured work so far, its body
-    // captured on the side stream
-    auto optional = [&](int k, auto issue) {
-        if (ce != cudaSuccess) return;
-        cudaStreamCaptureStatus status;
-        cudaGraph_t g = nullptr;
-        const cudaGraphNode_t* deps = nullptr;
-        size_t nDeps = 0;
-        what = "capture info";
-        if ((ce = cudaStreamGetCaptureInfo(st, &status, nullptr, &g, &deps, nullptr, &nDeps)) != cudaSuccess) return;
-        what = "conditional node";
-        cudaGraphNodeParams np{};
-        np.type = cudaGraphNodeTypeConditional;
-        np.conditional.handle = cond[k];
-        np.conditional.type = cudaGraphCondTypeIf;
-        np.conditional.size = 1;
-        cudaGraphNode_t node;
-        if ((ce = cudaGraphAddNode(&node, g, deps, nullptr, nDeps, &np)) != cudaSuccess) return;
-        what = "capture dependencies";
-        if ((ce = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
-            cudaSuccess)
-            return;
-        what = "body capture";
-        cudaGraph_t body = np.conditional.phGraph_out[0];
-        if ((ce = cudaStreamBeginCaptureToGraph(h->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
-            cudaSuccess)
-            return;
-        issue(h->side);
-        ce = cudaStreamEndCapture(h->side, &body);
-    };
-    for (int r = 0; r < check && ce == cudaSuccess; ++r) {
-        what = "conditional handle";
-        for (int k = 0; k < 3 && ce == cudaSuccess; ++k) ce = cudaGraphConditionalHandleCreate(&cond[k], graph, 0, 0);
-        if (ce != cudaSuccess) break;
-        sa.condPrep = cond[0];
-        sa.condAdjoint = cond[1];
-        sa.condFd = cond[2];
-        if (round_launches(st, sa, optional)) { ce = cudaErrorUnknown; what = "round"; }
-        if (ce == cudaSuccess && (ce = cudaGetLastError()) != cudaSuccess) what = "kernel launch";
-    }
-    cudaGraph_t captured = nullptr;
-    const cudaError_t ee = cudaStreamEndCapture(st, &captured);
-    if (ce == cudaSuccess && ee != cudaSuccess) { ce = ee; what = "end capture"; }
-    cudaGraphExec_t exec = nullptr;
-    if (ce == cudaSuccess && (ce = cudaGraphInstantiate(&exec, captured, 0)) != cudaSuccess) what = "instantiate";
-    if (ce != cudaSuccess) {
-        if (captured) cudaGraphDestroy(captured);
-        cudaGetLastError();
-        h->err = std::string("solver graph (") + what + "): " + cudaGetErrorString(ce);
-        return RDXG_ERR_CUDA;
-    }
-    int r = RDXG_OK;
-    for (long round = 0;; round += check) {
-        if ((ce = cudaGraphLaunch(exec, st)) != cudaSuccess ||
-            (ce = cudaMemcpyAsync(h->hActive, h->dActive, sizeof(int32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-            (ce = cudaStreamSynchronize(st)) != cudaSuccess) {
-            h->err = std::string("solver graph launch: ") + cudaGetErrorString(ce);
-            r = RDXG_ERR_CUDA;
-            break;
-        }
-        if (*h->hActive == 0) break;
-        if (round > 2000000L) { h->err = "solver did not terminate"; r = RDXG_ERR_STATE; break; }
-    }
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(captured);
-    if (r) return r;
-    unsigned long long n = 0;
-    CK(h, cudaMemcpy(&n, h->dLaunchCount, sizeof(n), cudaMemcpyDeviceToHost));
-    h->launches = (int64_t)n;
-    return RDXG_OK;
-}
-}  // extern "C++"
+namespace {
 
-int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
+// What a solve of one handle needs once its state is reset: the solver kernel's parameters
+// and the re-shift kernel's arguments.
+struct SolvePlan {
+    rdxg_solver* h = nullptr;
+    CgParams prm{};
+    ShiftArgs sa{};
+};
+
+// Everything rdxg_solve_async does before the rounds: state reset on the handle's stream.
+int prepare_solve(rdxg_solver* h, const rdxg_solve_params* s, SolvePlan& pl) {
     if (!h || !s) return RDXG_ERR_ARG;
     if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
     int r;
@@ -1124,15 +1035,16 @@ int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
     h->dirty = true;
     h->launches = 0;
     h->lastParams = *s;
-    const CgParams prm = make_cg_params(h, s);
-    if (prm.max_metrics != h->maxMetrics) {
+    pl.h = h;
+    pl.prm = make_cg_params(h, s);
+    if (pl.prm.max_metrics != h->maxMetrics) {
         if (h->dMetrics) {
             for (auto it = h->allocs.begin(); it != h->allocs.end(); ++it)
                 if (*it == h->dMetrics) { cudaFree(*it); h->allocs.erase(it); break; }
             h->dMetrics = nullptr;
         }
-        if ((r = dalloc_t(h, &h->dMetrics, (size_t)h->Pmax * prm.max_metrics))) return r;
-        h->maxMetrics = prm.max_metrics;
+        if ((r = dalloc_t(h, &h->dMetrics, (size_t)h->Pmax * pl.prm.max_metrics))) return r;
+        h->maxMetrics = pl.prm.max_metrics;
     }
     const int P = h->P;
     CK(h, cudaMemsetAsync(h->dStates, 0, P * sizeof(CgState), h->stream));
@@ -1143,48 +1055,210 @@ int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
         CK(h, cudaMemsetAsync(h->dOh, 0, (size_t)P * h->nObj * h->nH * sizeof(float2), h->stream));
         CK(h, cudaMemsetAsync(h->dAux, 0, (size_t)P * 2 * sizeof(int32_t), h->stream));
     }
-    const int check = s->check_every > 0 ? s->check_every : 8;
-    ShiftArgs sa{};
+    ShiftArgs& sa = pl.sa;
+    sa = ShiftArgs{};
     sa.P = P; sa.I = h->I; sa.M = h->M; sa.nObj = h->nObj; sa.ps = h->ps; sa.cs = h->cs; sa.margin = h->margin;
     sa.tiltX = h->haveJ ? h->geo.tilt_x : -1; sa.tiltY = h->haveJ ? h->geo.tilt_y : -1;
     sa.req = h->dReq; sa.alpha = h->dAlpha; sa.tiltOff = h->dCurTilt; sa.shift = h->dShift;
     sa.reinit = h->dReinit; sa.imgObj = h->dImgObj; sa.aux = h->fused ? h->dAux : nullptr;
     std::memcpy(sa.J, h->J, sizeof(sa.J));
     std::memcpy(sa.Jinv, h->Jinv, sizeof(sa.Jinv));
-    const int G = P * h->I;
-    // one round: the solver kernel, re-shift, [re-initialisation], evaluation, [adjoint],
-    // [finite differences]; optional(k, issue) issues the bracketed kernels
-    auto round_launches = [&](cudaStream_t st, const ShiftArgs& sar, auto optional) -> int {
-        if (cudaMemsetAsync(h->dActive, 0, sizeof(int32_t), st) != cudaSuccess ||
-            cudaMemsetAsync(h->dCounters, 0, kNumCounters * sizeof(int32_t), st) != cudaSuccess)
-            return 1;
-        with_size(h->N, h->fp64, [&](auto L, auto t) {
-            using T = decltype(t);
-            KParams<T> kp = make_kparams<T>(h);
-            CgArgs<T> ca = make_cgargs<T>(h, prm);
-            launch_cg<T>(ca, P, st);
-            launch_shift(sar, P, st);
-            optional(0, [&](cudaStream_t s2) { decltype(L)::prep(kp, 0, G, s2); });
-            if (h->fused) {
-                with_eval(h->N, [&](auto E) {
-                    EvalParams<float> e = make_evalparams<float>(h);
-                    decltype(E)::phase(e, h->phaseGrid, st);
-                    decltype(E)::eval(e, h->npt, h->evalGrid, st);
-                    decltype(E)::reduce(e, h->reduceGrid, st);
-                });
-            } else {
-                decltype(L)::forward(kp, G, st);
-                launch_accum<T>(kp, P * h->nObj, st);
+    return RDXG_OK;
+}
+
+// One round of one handle on stream st: the solver kernel, re-shift, [re-initialisation],
+// evaluation, [adjoint], [finite differences]; optional(k, issue) issues the bracketed kernels.
+template <typename Opt>
+int issue_round(const SolvePlan& pl, cudaStream_t st, const ShiftArgs& sar, Opt&& optional) {
+    rdxg_solver* h = pl.h;
+    if (cudaMemsetAsync(h->dActive, 0, sizeof(int32_t), st) != cudaSuccess ||
+        cudaMemsetAsync(h->dCounters, 0, kNumCounters * sizeof(int32_t), st) != cudaSuccess)
+        return 1;
+    const int P = h->P, G = P * h->I;
+    with_size(h->N, h->fp64, [&](auto L, auto t) {
+        using T = decltype(t);
+        KParams<T> kp = make_kparams<T>(h);
+        CgArgs<T> ca = make_cgargs<T>(h, pl.prm);
+        launch_cg<T>(ca, P, st);
+        launch_shift(sar, P, st);
+        optional(0, [&](cudaStream_t s2) { decltype(L)::prep(kp, 0, G, s2); });
+        if (h->fused) {
+            with_eval(h->N, [&](auto E) {
+                EvalParams<float> e = make_evalparams<float>(h);
+                decltype(E)::phase(e, h->phaseGrid, st);
+                decltype(E)::eval(e, h->npt, h->evalGrid, st);
+                decltype(E)::reduce(e, h->reduceGrid, st);
+            });
+        } else {
+            decltype(L)::forward(kp, G, st);
+            launch_accum<T>(kp, P * h->nObj, st);
+        }
+        optional(1, [&](cudaStream_t s2) { decltype(L)::adjoint(kp, h->adjGrid, GK_VOGEL, s2); });
+    });
+    optional(2, [&](cudaStream_t s2) { launch_fd(h, s2); });
+    return 0;
+}
+
+// Runs the rounds of every plan as one CUDA graph of `check` rounds per plan, one branch per
+// handle (forked from the first handle's stream; handles sharing a stream are issued one
+// after the other).  The kernels that are only needed in some rounds (image
+// re-initialisation after a re-shift, the adjoint, the finite-difference gradient) sit in
+// conditional nodes whose conditions k_shift sets from the round's work-list counters.  The
+// host launches the graph until no handle has an active patch.
+int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
+    rdxg_solver* h0 = plans[0].h;
+    cudaStream_t origin = h0->stream;
+    for (SolvePlan& pl : plans) {
+        rdxg_solver* h = pl.h;
+        if (!h->side) CK(h, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        if (!h->dLaunchCount) {
+            int r = dalloc_t(h, &h->dLaunchCount, 1);
+            if (r) return r;
+        }
+        CK(h, cudaMemsetAsync(h->dLaunchCount, 0, sizeof(unsigned long long), h->stream));
+        // the reset of every handle's state is complete before the graph runs on the origin
+        if (h->stream != origin) CK(h, cudaStreamSynchronize(h->stream));
+    }
+    const size_t nPlans = plans.size();
+    std::vector<cudaEvent_t> ev(nPlans + 1, nullptr);
+    cudaError_t ce = cudaSuccess;
+    const char* what = "events";
+    for (size_t k = 0; k <= nPlans && ce == cudaSuccess; ++k) ce = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+    bool capturing = false;
+    if (ce == cudaSuccess) {
+        what = "begin capture";
+        ce = cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal);
+        capturing = ce == cudaSuccess;
+    }
+    cudaGraph_t graph = nullptr;
+    if (ce == cudaSuccess) {
+        cudaStreamCaptureStatus status;
+        what = "capture info";
+        ce = cudaStreamGetCaptureInfo(origin, &status, nullptr, &graph, nullptr, nullptr, nullptr);
+    }
+    // fork: every other stream joins the capture after the origin's start
+    if (ce == cudaSuccess && (ce = cudaEventRecord(ev[nPlans], origin)) == cudaSuccess) {
+        for (size_t k = 0; k < nPlans && ce == cudaSuccess; ++k)
+            if (plans[k].h->stream != origin) ce = cudaStreamWaitEvent(plans[k].h->stream, ev[nPlans], 0);
+    }
+    for (int r = 0; r < check && ce == cudaSuccess; ++r) {
+        for (size_t k = 0; k < nPlans && ce == cudaSuccess; ++k) {
+            SolvePlan& pl = plans[k];
+            rdxg_solver* h = pl.h;
+            cudaStream_t st = h->stream;
+            // a conditional handle belongs to one conditional node: three new ones per round
+            cudaGraphConditionalHandle cond[3] = {};
+            what = "conditional handle";
+            for (int c = 0; c < 3 && ce == cudaSuccess; ++c) ce = cudaGraphConditionalHandleCreate(&cond[c], graph, 0, 0);
+            if (ce != cudaSuccess) break;
+            ShiftArgs sa = pl.sa;
+            sa.useConditions = 1;
+            sa.counters = h->dCounters;
+            sa.fixedLaunches = h->fused ? 5 : 4;
+            sa.launchCount = h->dLaunchCount;
+            sa.condPrep = cond[0];
+            sa.condAdjoint = cond[1];
+            sa.condFd = cond[2];
+            // optional kernel c: an IF node on cond[c] after the stream's captured work so far,
+            // its body captured on the handle's side stream
+            auto optional = [&](int c, auto issue) {
+                if (ce != cudaSuccess) return;
+                cudaStreamCaptureStatus status;
+                cudaGraph_t g = nullptr;
+                const cudaGraphNode_t* deps = nullptr;
+                size_t nDeps = 0;
+                what = "capture info";
+                if ((ce = cudaStreamGetCaptureInfo(st, &status, nullptr, &g, &deps, nullptr, &nDeps)) != cudaSuccess)
+                    return;
+                what = "conditional node";
+                cudaGraphNodeParams np{};
+                np.type = cudaGraphNodeTypeConditional;
+                np.conditional.handle = cond[c];
+                np.conditional.type = cudaGraphCondTypeIf;
+                np.conditional.size = 1;
+                cudaGraphNode_t node;
+                if ((ce = cudaGraphAddNode(&node, g, deps, nullptr, nDeps, &np)) != cudaSuccess) return;
+                what = "capture dependencies";
+                if ((ce = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
+                                                              cudaStreamSetCaptureDependencies)) != cudaSuccess)
+                    return;
+                what = "body capture";
+                cudaGraph_t body = np.conditional.phGraph_out[0];
+                if ((ce = cudaStreamBeginCaptureToGraph(h->side, body, nullptr, nullptr, 0,
+                                                        cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+                    return;
+                issue(h->side);
+                ce = cudaStreamEndCapture(h->side, &body);
+            };
+            if (issue_round(pl, st, sa, optional)) { ce = cudaErrorUnknown; what = "round"; }
+            if (ce == cudaSuccess && (ce = cudaGetLastError()) != cudaSuccess) what = "kernel launch";
+        }
+    }
+    // join: the origin waits for every branch
+    for (size_t k = 0; k < nPlans && ce == cudaSuccess; ++k) {
+        cudaStream_t st = plans[k].h->stream;
+        if (st == origin) continue;
+        what = "join";
+        if ((ce = cudaEventRecord(ev[k], st)) == cudaSuccess) ce = cudaStreamWaitEvent(origin, ev[k], 0);
+    }
+    cudaGraph_t captured = nullptr;
+    if (capturing) {
+        const cudaError_t ee = cudaStreamEndCapture(origin, &captured);
+        if (ce == cudaSuccess && ee != cudaSuccess) { ce = ee; what = "end capture"; }
+    }
+    cudaGraphExec_t exec = nullptr;
+    if (ce == cudaSuccess && (ce = cudaGraphInstantiate(&exec, captured, 0)) != cudaSuccess) what = "instantiate";
+    int r = RDXG_OK;
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        h0->err = std::string("solver graph (") + what + "): " + cudaGetErrorString(ce);
+        r = RDXG_ERR_CUDA;
+    }
+    for (long round = 0; r == RDXG_OK; round += check) {
+        bool active = false;
+        if ((ce = cudaGraphLaunch(exec, origin)) == cudaSuccess) {
+            for (SolvePlan& pl : plans) {
+                if ((ce = cudaMemcpyAsync(pl.h->hActive, pl.h->dActive, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                          origin)) != cudaSuccess)
+                    break;
             }
-            optional(1, [&](cudaStream_t s2) { decltype(L)::adjoint(kp, h->adjGrid, GK_VOGEL, s2); });
-        });
-        optional(2, [&](cudaStream_t s2) { launch_fd(h, s2); });
-        return 0;
-    };
+        }
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(origin);
+        if (ce != cudaSuccess) {
+            h0->err = std::string("solver graph launch: ") + cudaGetErrorString(ce);
+            r = RDXG_ERR_CUDA;
+            break;
+        }
+        for (SolvePlan& pl : plans) active = active || *pl.h->hActive != 0;
+        if (!active) break;
+        if (round > 2000000L) { h0->err = "solver did not terminate"; r = RDXG_ERR_STATE; }
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (captured) cudaGraphDestroy(captured);
+    for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
+    if (r) return r;
+    for (SolvePlan& pl : plans) {
+        unsigned long long n = 0;
+        CK(pl.h, cudaMemcpy(&n, pl.h->dLaunchCount, sizeof(n), cudaMemcpyDeviceToHost));
+        pl.h->launches = (int64_t)n;
+    }
+    return RDXG_OK;
+}
+
+}  // namespace
+}  // extern "C++"
+
+int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
+    std::vector<SolvePlan> plans(1);
+    int r = prepare_solve(h, s, plans[0]);
+    if (r) return r;
+    const int check = s->check_every > 0 ? s->check_every : 8;
     const char* ng = getenv("RDXG_NO_GRAPH");
-    if (!(ng && atoi(ng))) return solve_rounds_graph(h, sa, check, round_launches);
+    if (!(ng && atoi(ng))) return solve_rounds_graph(plans, check);
+    const SolvePlan& pl = plans[0];
     for (long round = 0;; ++round) {
-        if (round_launches(h->stream, sa, [&](int, auto issue) { issue(h->stream); })) {
+        if (issue_round(pl, h->stream, pl.sa, [&](int, auto issue) { issue(h->stream); })) {
             h->err = "cudaMemsetAsync failed";
             return RDXG_ERR_CUDA;
         }
@@ -1198,6 +1272,24 @@ int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
         if (round > 2000000L) { h->err = "solver did not terminate"; return RDXG_ERR_STATE; }
     }
     return RDXG_OK;
+}
+
+int rdxg_solve_many(rdxg_solver* const* handles, int32_t n, const rdxg_solve_params* s) {
+    if (!handles || n < 1 || !s) return RDXG_ERR_ARG;
+    std::vector<SolvePlan> plans(n);
+    for (int k = 0; k < n; ++k) {
+        if (!handles[k]) return RDXG_ERR_ARG;
+        for (int j = 0; j < k; ++j)
+            if (handles[j] == handles[k]) { handles[k]->err = "a handle appears twice"; return RDXG_ERR_ARG; }
+        if (handles[k]->geo.device != handles[0]->geo.device) {
+            handles[k]->err = "handles on different devices";
+            return RDXG_ERR_ARG;
+        }
+        const int r = prepare_solve(handles[k], s, plans[k]);
+        if (r) return r;
+    }
+    const int check = s->check_every > 0 ? s->check_every : 8;
+    return solve_rounds_graph(plans, check);
 }
 
 int rdxg_fetch_results(rdxg_solver* h, double* alpha_out, rdxg_patch_report* reports, double* metrics) {

@@ -246,6 +246,19 @@ class Solver:
         return out
 
 
+def solve_many(solvers, settings: SolveSettings):
+    """Solver::run for the loaded patches of several handles (e.g. one per geometry of an
+    uneven batch) in one CUDA graph (rdxg_solve_many); returns each handle's results."""
+    L = _lib.load()
+    hs = (C.c_void_p * len(solvers))(*[s.h for s in solvers])
+    prm = settings.to_c()
+    r = L.rdxg_solve_many(hs, len(solvers), C.byref(prm))
+    if r != _lib.RDXG_OK:
+        msgs = "; ".join(L.rdxg_last_error(s.h).decode() for s in solvers)
+        raise SolverError(f"rdxg_solve_many failed with status {r}: {msgs}")
+    return [s.fetch(settings.max_metrics) for s in solvers]
+
+
 def cg_minimize(n_free: int, n_modes: int, settings: SolveSettings, grad_scale: float, f, df, shift=None):
     """Host drop-in of the reference's conjugate_rdx + Solver::run stage loop (rdxg_cg_minimize).
 

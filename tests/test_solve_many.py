@@ -1,0 +1,43 @@
+"""Uneven batches: several handles of different geometries (OTF size, frames, modes, the fused
+and the general path) solved in one CUDA graph with rdxg_solve_many, against each handle
+solved alone (marked gpu)."""
+import numpy as np
+import pytest
+
+from redux_gb300 import solver as S
+from tests.conftest import workload
+
+pytestmark = pytest.mark.gpu
+
+
+def _handles():
+    ws = [workload(0), workload(2, n_patches=2, frames=4), workload(4, n_patches=1, frames=2)]
+    out = []
+    for w in ws:
+        s = S.Solver(w.job, max_patches=w.patches.cutouts.shape[0])
+        s.set_patches(w.patches.cutouts, None, w.patches.fixed_gamma)
+        out.append(s)
+    return ws, out
+
+
+def test_many_equals_each_alone():
+    # staged modes and per-patch convergence (FTOL as a relative metric change)
+    st = S.SolveSettings(mode_start=5, mode_step=5, max_iterations=12, min_iterations=3, ftol=1e-6,
+                         max_metrics=256)
+    ws, hs = _handles()
+    together = S.solve_many(hs, st)
+    for w, s, got in zip(ws, hs, together):
+        alone = s.run(st)
+        np.testing.assert_array_equal(got["alpha"], alone["alpha"])
+        for p in range(w.patches.cutouts.shape[0]):
+            a, b = got["reports"][p], alone["reports"][p]
+            assert (a.n_metrics, a.iterations, a.final_metric) == (b.n_metrics, b.iterations, b.final_metric)
+            np.testing.assert_array_equal(got["metrics"][p, :a.n_metrics], alone["metrics"][p, :b.n_metrics])
+        assert s.launch_count() > 0
+
+
+def test_many_rejects_a_repeated_handle():
+    ws, hs = _handles()
+    st = S.fixed_iterations(ws[0].job.n_modes, 2, max_metrics=64)
+    with pytest.raises(S.SolverError, match="twice"):
+        S.solve_many([hs[0], hs[1], hs[0]], st)
