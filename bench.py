@@ -152,6 +152,80 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_uneven(args):
+    """Configuration 3, the uneven batch: patches of sizes {64, 88, 128}, 8-24 frames per
+    channel and 36-60 KL modes, staged modes and per-patch convergence (FTOL 1e-6), one
+    handle per geometry and every handle's rounds in one CUDA graph (rdxg_solve_many), against
+    per-patch launches (each patch its own handle, solved one after the other).  Not the
+    headline line: `python bench.py --config 3`."""
+    import torch
+    from redux_gb300 import solver as S, synth
+    torch.cuda.set_device(0)
+    n = args.patches if args.patches != 225 else 120
+    t0 = time.perf_counter()
+    ws = synth.uneven_batch(n, levels=args.levels or None)
+    t_gen = time.perf_counter() - t0
+    st = S.SolveSettings(mode_start=5, mode_step=5, max_iterations=args.iterations if args.iterations != 100 else 30,
+                         min_iterations=5, ftol=1e-6, max_metrics=4096)
+    hs = []
+    for w in ws:
+        h = S.Solver(w.job, max_patches=w.patches.cutouts.shape[0])
+        h.set_patches(w.patches.cutouts)
+        hs.append(h)
+    for _ in range(args.warmup):
+        S.solve_many(hs, st)
+    torch.cuda.synchronize()
+    times, iters, evals = [], [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            for h, w in zip(hs, ws):
+                h.set_patches(w.patches.cutouts)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            outs = S.solve_many(hs, st)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+    for out in outs:
+        iters += [r.iterations for r in out["reports"]]
+        evals += [r.n_f_evals + r.n_df_evals for r in out["reports"]]
+    t_many = statistics.median(times)
+    launches = sum(h.launch_count() for h in hs)
+    # per-patch launches on one patch of each of 8 geometries spread over the sizes
+    sample = ws[::max(1, len(ws) // 8)][:8]
+    t_single, n_single = 0.0, 0
+    for w in sample:
+        h1 = S.Solver(w.job, max_patches=1)
+        for rep in range(2):     # the first solve of a handle builds its graph: time the second
+            h1.set_patches(w.patches.cutouts[:1])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            h1.run(st)
+            torch.cuda.synchronize()
+            if rep:
+                t_single += time.perf_counter() - t0
+        n_single += 1
+        h1.close()
+    # the same patches inside the batch: their share of the batch time
+    line = {"metric": "uneven-batch converged patches/s (configuration 3)", "value": n / t_many, "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_many * 1000.0,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (FP64 sums and CG scalars)", "data": "synthetic",
+            "config": {"workload": f"{n} patches, sizes {{64, 88, 128}}, frames 8-24, 36-60 KL modes"
+                                   + (f" ({args.levels} levels)" if args.levels else "")
+                                   + ", staged modes, FTOL 1e-6, at most "
+                                   + f"{st.max_iterations} iterations per stage",
+                       "geometries": len(ws), "iterations_median": float(np.median(iters)),
+                       "evaluations_per_patch": float(np.mean(evals)), "generation_s": t_gen},
+            "gpu_launches": int(launches),
+            "per_patch_launches": {"value": n_single / t_single, "unit": UNIT,
+                                   "sample": f"{n_single} patches, one per geometry, each its own handle: "
+                                             + ", ".join(w.name for w in sample)},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    for h in hs:
+        h.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -162,6 +236,9 @@ def main():
     ap.add_argument("--frames", type=int, default=12)
     ap.add_argument("--iterations", type=int, default=100)
     ap.add_argument("--no-baselines", action="store_true")
+    ap.add_argument("--config", type=int, default=2, help="2: the headline batch; 3: the uneven batch")
+    ap.add_argument("--levels", type=int, default=3,
+                    help="uneven batch: frames and modes from this many values (0: uniform draws)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="load the batch and time each kernel once (profiling target)")
     args = ap.parse_args()
@@ -170,6 +247,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank)
+    if args.config == 3:
+        return run_uneven(args)
 
     import torch
     torch.cuda.set_device(local)

@@ -26,10 +26,10 @@ template <typename T, int N>
 cudaError_t Launcher<T, N>::setup(int M) {
     const int sm = (int)smem_pp<T, N>(M);
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_prep<T, N, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
-    if ((e = cudaFuncSetAttribute(k_forward<T, N, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
-    if ((e = cudaFuncSetAttribute(k_adjoint<T, N, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
-    if ((e = cudaFuncSetAttribute(k_fd<T, N, THREADS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
+    if ((e = raise_smem_limit(k_prep<T, N, THREADS>, sm))) return e;
+    if ((e = raise_smem_limit(k_forward<T, N, THREADS>, sm))) return e;
+    if ((e = raise_smem_limit(k_adjoint<T, N, THREADS>, sm))) return e;
+    if ((e = raise_smem_limit(k_fd<T, N, THREADS>, sm))) return e;
     return cudaSuccess;
 }
 
@@ -97,15 +97,13 @@ template <typename T, int N>
 cudaError_t EvalLauncher<T, N>::setup(int M, int npt, int nH) {
     cudaError_t e = cudaSuccess;
     const int sm = (int)smem(M, nH);
-#define RDXG_SET(NPT) e = cudaFuncSetAttribute(k_eval<T, N, kEvalThreads, NPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm)
+#define RDXG_SET(NPT) e = raise_smem_limit(k_eval<T, N, kEvalThreads, NPT>, sm)
     RDXG_NPT_SWITCH(npt, RDXG_SET);
 #undef RDXG_SET
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_phase<T, N, kPhasePix, kMaxChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)((size_t)M * (kPhasePix + kMaxChunk) * sizeof(T)));
+        e = raise_smem_limit(k_phase<T, N, kPhasePix, kMaxChunk>, (size_t)M * (kPhasePix + kMaxChunk) * sizeof(T));
     if (e == cudaSuccess && fd_smem(nH) + 1024 <= kMaxSmem)
-        e = cudaFuncSetAttribute(k_fd_half<T, N, kEvalThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)fd_smem(nH));
+        e = raise_smem_limit(k_fd_half<T, N, kEvalThreads>, fd_smem(nH));
     return e;
 }
 

@@ -4,10 +4,29 @@
 
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "rdxg_cg.cuh"
 #include "rdxg_restore.cuh"
 
 namespace rdxg {
+
+// Raises a kernel's dynamic shared memory limit to at least `bytes`, never lowering it: the
+// attribute belongs to the function for the whole process, so every handle (of any geometry)
+// shares it, and one set by a handle with smaller needs must not break another's launches.
+inline std::mutex& smem_limit_mutex() {
+    static std::mutex m;
+    return m;
+}
+template <typename K>
+cudaError_t raise_smem_limit(K* kernel, size_t bytes) {
+    std::lock_guard<std::mutex> lock(smem_limit_mutex());
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    if ((size_t)fa.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
 
 template <int N> struct Threads { static constexpr int value = (N >= 128) ? 512 : 256; };
 

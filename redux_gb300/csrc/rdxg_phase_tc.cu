@@ -248,7 +248,7 @@ PhaseTcPlan phase_tc_plan(int I, int M, int n2, int nCh, int parts, int numSMs) 
     cudaError_t e;
     // all of the unified L1 as shared memory, so that several blocks fit per SM
     auto setup = [&](auto kern) {
-        cudaError_t r = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem);
+        cudaError_t r = raise_smem_limit(kern, p.smem);
         if (r == cudaSuccess)
             r = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      (int)cudaSharedmemCarveoutMaxShared);

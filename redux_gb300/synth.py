@@ -7,9 +7,9 @@ Poisson noise at 1e4 photons/px plus N(0, 10^2) read noise, stored as float32.
 
 The generator follows the workload descriptions of the five benchmark configurations
 (plain FP64 single patch; adjoint check; 225-patch production field; uneven batch;
-large mixed-precision batch).  The Karhunen-Loeve basis is not generated yet: those
-configurations use the same number of Zernike modes (Noll 2..M+1), which leaves the
-solver's work per iteration unchanged (a dense modes x pixels matrix either way).
+large mixed-precision batch).  Configuration 0 uses Zernike modes Noll 2..21, the others
+Karhunen-Loeve modes (tilts Zernike) from the expansion of the Noll covariance.  The uneven
+batch (configuration 3, `uneven_batch`) is a list of workloads, one per patch geometry.
 """
 from __future__ import annotations
 
@@ -246,6 +246,39 @@ def make_patches(job: Job, n_patches: int, d_r0: float, rng, fixed_gamma=None,
 
 LAYOUT_1OBJ = lambda frames: {"frames": frames, "objects": [[0.0, 1.0]]}          # focus + diversity
 LAYOUT_WB_NB = lambda frames: {"frames": frames, "objects": [[0.0], [0.0, 1.0]]}  # WB; NB focus + div
+
+
+UNEVEN_SIZES = (64, 88, 128)
+UNEVEN_KL_LAST = 121   # one expansion over Noll 2..121 for every mode count (its first M modes)
+
+
+def uneven_batch(n_patches: int = 400, frames=(8, 24), modes=(36, 60), levels: int | None = None,
+                 d_r0: float = 15.0, seed_offset: int = 0) -> list:
+    """Configuration 3: patches whose size ({64, 88, 128}), frames per channel (8..24) and
+    number of KL modes (36..60) are drawn uniformly per patch, 3 channels (wideband; narrowband
+    focus and +1 wave), grouped by geometry.  levels: draw frames and modes from that many
+    evenly spaced values instead (e.g. 3: frames {8, 16, 24}, modes {36, 48, 60}) so that
+    patches share geometries.  Returns one Workload per distinct (size, frames, modes), its
+    cfg["patch_index"] the positions of its patches in the draw order."""
+    rng = np.random.default_rng(20261203 + 3 + seed_offset)
+
+    def draw(lo, hi):
+        if levels:
+            return int(np.linspace(lo, hi, levels).round().astype(int)[rng.integers(levels)])
+        return int(rng.integers(lo, hi + 1))
+
+    draws = [(int(UNEVEN_SIZES[rng.integers(len(UNEVEN_SIZES))]), draw(*frames), draw(*modes))
+             for _ in range(n_patches)]
+    groups = {}
+    for i, g in enumerate(draws):
+        groups.setdefault(g, []).append(i)
+    out = []
+    for (N, F, M), idx in sorted(groups.items()):
+        job = make_job(N, M, LAYOUT_WB_NB(F), basis="kl", kl_last=UNEVEN_KL_LAST)
+        prng = np.random.default_rng([20261203 + 3 + seed_offset, N, F, M])
+        pt = make_patches(job, len(idx), d_r0, prng)
+        out.append(Workload(f"uneven {N}x{N}, 3ch x {F}fr, {M} KL modes", job, pt, dict(patch_index=idx)))
+    return out
 
 
 def config(index: int, n_patches: int | None = None, seed_offset: int = 0, frames=None) -> Workload:

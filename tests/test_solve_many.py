@@ -41,3 +41,22 @@ def test_many_rejects_a_repeated_handle():
     st = S.fixed_iterations(ws[0].job.n_modes, 2, max_metrics=64)
     with pytest.raises(S.SolverError, match="twice"):
         S.solve_many([hs[0], hs[1], hs[0]], st)
+
+
+def test_handles_of_different_sizes_keep_their_shared_memory():
+    # the dynamic shared memory limit of a kernel is one process-wide attribute: a handle
+    # created later with smaller needs (64 x 64, 8 images, 20 modes) must not lower it below
+    # what an earlier one needs (64 x 64, 24 images, 60 modes: a larger tensor-core tile)
+    from redux_gb300 import synth
+    big_job = synth.make_job(64, 60, synth.LAYOUT_WB_NB(8), basis="kl", kl_last=121)
+    big = synth.make_patches(big_job, 2, 15.0, np.random.default_rng(7))
+    hb = S.Solver(big_job, max_patches=2)
+    hb.set_patches(big.cutouts)
+    w0 = workload(0)
+    hs = S.Solver(w0.job, max_patches=1)
+    hs.set_patches(w0.patches.cutouts, None, w0.patches.fixed_gamma)
+    st = S.fixed_iterations(big_job.n_modes, 2, max_metrics=64)
+    out = hb.run(st)
+    assert all(r.n_metrics > 0 for r in out["reports"])
+    L = hb.metric(big.alpha_true)
+    assert np.all(np.isfinite(L))
