@@ -217,6 +217,7 @@ def run_uneven(args):
                        "geometries": len(ws), "iterations_median": float(np.median(iters)),
                        "evaluations_per_patch": float(np.mean(evals)), "generation_s": t_gen},
             "gpu_launches": int(launches),
+            "launch_shapes": {w.name: h.launch_shape() for w, h in zip(ws, hs)},
             "per_patch_launches": {"value": n_single / t_single, "unit": UNIT,
                                    "sample": f"{n_single} patches, one per geometry, each its own handle: "
                                              + ", ".join(w.name for w in sample)},
@@ -226,22 +227,142 @@ def run_uneven(args):
         h.close()
 
 
+def run_large(args):
+    """Configuration 4, mixed precision at large size: 128 x 128 patches, 3 channels x 32
+    frames, 100 KL modes at D/r0 = 25; mode expansion on the CUDA cores in FP32 (the tensor-core
+    expansion belongs to the fused path, which covers N <= 88), FP32 transforms, FP64 metric
+    sums and CG scalars.  `--iterations` CG iterations per patch with all modes at once, as the
+    headline workload.  Reports patches/s and CG iterations/s, the kernel times with their
+    nominal FP32 rates and HBM fractions, and the errors against the FP64 restatement on one
+    patch: the metric, gradient and restored object at the same alpha (per-evaluation
+    precision) and the metric history, alpha and restored object after a short solve of both.
+    Defaults to 1 warm-up and 2 timed solves.  Not the headline line: `python bench.py --config 4`."""
+    import torch
+    from redux_gb300 import solver as S, synth
+    torch.cuda.set_device(0)
+    P = args.patches if args.patches != 225 else 256
+    t0 = time.perf_counter()
+    w = synth.config(4, n_patches=P)
+    t_gen = time.perf_counter() - t0
+    job, cut = w.job, np.ascontiguousarray(w.patches.cutouts, np.float32)
+    settings = S.fixed_iterations(job.n_modes, args.iterations, max_metrics=args.iterations + 8)
+    s = S.Solver(job, max_patches=P)
+    for _ in range(args.warmup):
+        s.set_patches(cut)
+        s.run(settings)
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            s.set_patches(cut)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = s.run(settings)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+    t_solve = statistics.median(times)
+    reps = out["reports"]
+    nf = sum(r.n_f_evals for r in reps) / P
+    ndf = sum(r.n_df_evals for r in reps) / P
+    launches = s.launch_count()
+    # kernel times on the loaded batch at its last point
+    kt = s.profile_kernels(reps=3)
+    peaks = _peaks()
+    N, n, M, I = job.otf_size, job.pupil_pixels, job.n_modes, job.n_images
+    G = P * I
+    fft_flops = 5.0 * N * N * math.log2(N * N)
+    flops = {"forward": G * (2 * fft_flops + 2.0 * M * n * n), "accum": G * 16.0 * N * N,
+             "adjoint": G * (2 * fft_flops + 2.0 * M * n * n)}
+    # compulsory HBM bytes per launch: forward reads nothing per image but writes S (8 N^2);
+    # the accumulation reads D and S twice and writes O and Q; the adjoint reads D, S, X, O, Q, PF
+    hbm = {"forward": G * 8.0 * N * N, "accum": G * 4 * 8.0 * N * N, "adjoint": G * (4 * 8.0 * N * N + 8.0 * n * n)}
+    kern = {k: {"ms": kt[k], "fp32_tflops": flops[k] / (kt[k] / 1e3) / 1e12,
+                "hbm_gbs": hbm[k] / (kt[k] / 1e3) / 1e9, "hbm_frac": hbm[k] / (kt[k] / 1e3) / 1e9 / peaks["hbm"]}
+            for k in ("forward", "accum", "adjoint")}
+    # errors against the FP64 restatement (CPU) on one patch: the metric, gradient and restored
+    # object at the same alpha, and a short solve of both (the FP64 GPU form does not take
+    # N = 128: a double tile of 128 x 129 exceeds the shared memory of a block)
+    import oracle
+    threads = os.cpu_count() or 1
+    check_iters = args.check_iterations
+    s1 = S.Solver(job, max_patches=1)
+    s1.set_patches(cut[:1])
+    op = oracle.OraclePatch(job, threads=threads)
+    op.set_images(cut[0], None, None)
+    at = w.patches.alpha_true[:1]
+    fc = N / 2.0
+    m_o = op.metric(at[0])
+    _, g_o = op.gradient(at[0], method="vogel")
+    g_1, _ = s1.gradient(at)
+    obj_o = op.restore(at[0], fc)
+    obj_1 = s1.restore(at, fc)[0]
+    st_short = S.fixed_iterations(M, check_iters, max_metrics=check_iters + 8)
+    r1 = s1.run(st_short)
+    t0 = time.perf_counter()
+    ro = op.solve(oracle.default_cfg(max_iterations=check_iters, n_modes=M))
+    t_cpu = time.perf_counter() - t0
+    obj_1s = s1.restore(r1["alpha"], fc)[0]
+    obj_os = op.restore(ro["alpha"], fc)
+    fin_1, fin_o = r1["reports"][0].final_metric, ro["report"].final_metric
+    nm = min(r1["reports"][0].n_metrics, len(ro["metrics"]))
+    hist_rel = np.abs(r1["metrics"][0, :nm] - ro["metrics"][:nm]) / np.abs(ro["metrics"][:nm])
+    errors = {
+        "reference": "FP64 restatement of the reference (CPU), 1 patch",
+        "metric_rel_same_alpha": abs(s1.metric(at)[0] - m_o) / abs(m_o),
+        "gradient_rel_norm_same_alpha": float(np.linalg.norm(g_1[0] - g_o) / np.linalg.norm(g_o)),
+        "object_rel_peak_same_alpha": float(np.abs(obj_1 - obj_o).max() / np.abs(obj_o).max()),
+        "short_solve_iterations": check_iters,
+        "short_solve_metric_history_rel_max": float(hist_rel.max()) if nm else None,
+        "short_solve_final_metric_rel": abs(fin_1 - fin_o) / abs(fin_o),
+        "short_solve_alpha_rms_rad": float(np.sqrt(np.mean((r1["alpha"][0] - ro["alpha"]) ** 2)) / job.wavelength),
+        "short_solve_object_rel_peak": float(np.abs(obj_1s - obj_os).max() / np.abs(obj_os).max()),
+    }
+    s1.close()
+    line = {"metric": "large-patch patches/s (configuration 4)", "value": P / t_solve, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_solve * 1000.0, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 sums and CG scalars)", "data": "synthetic",
+            "config": {"workload": f"{P} patches 128x128, 100 KL modes, 3ch x 32 frames, D/r0=25, "
+                                   f"{args.iterations} CG iterations, all modes at once",
+                       "metric_evals_per_patch": nf, "gradient_evals_per_patch": ndf,
+                       "cg_iterations_per_s": P * args.iterations / t_solve, "generation_s": t_gen,
+                       "mode_expansion": "CUDA cores, FP32 (inside the transform kernel)",
+                       "l2": "inputs larger than L2 (D, S: 2 x %.1f GB)" % (G * 8.0 * N * N / 1e9)},
+            "gpu_launches": int(launches), "kernels": kern, "peak_hbm_gbs": peaks["hbm"],
+            "launch_shapes": s.launch_shape(),
+            "errors_vs_fp64": errors,
+            "cpu_baseline": {"value": 1.0 / t_cpu * check_iters / args.iterations, "unit": UNIT, "cores": threads,
+                             "kind": "port", "sample": f"1 patch x {check_iters} iterations, FP64 restatement, "
+                                                       f"{threads} OpenMP threads over images, scaled to "
+                                                       f"{args.iterations} iterations"},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 5; 2 for --config 4)")
+    ap.add_argument("--warmup", type=int, default=None, help="warm-up steps (default 3; 1 for --config 4)")
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--patches", type=int, default=225)
     ap.add_argument("--frames", type=int, default=12)
     ap.add_argument("--iterations", type=int, default=100)
     ap.add_argument("--no-baselines", action="store_true")
-    ap.add_argument("--config", type=int, default=2, help="2: the headline batch; 3: the uneven batch")
+    ap.add_argument("--config", type=int, default=2,
+                    help="2: the headline batch; 3: the uneven batch; 4: large patches (128 x 128, 100 modes)")
     ap.add_argument("--levels", type=int, default=3,
                     help="uneven batch: frames and modes from this many values (0: uniform draws)")
+    ap.add_argument("--check-iterations", type=int, default=10,
+                    help="large patches: CG iterations of the solve compared with the FP64 restatement")
     ap.add_argument("--kernels-only", action="store_true",
                     help="load the batch and time each kernel once (profiling target)")
     args = ap.parse_args()
+    large = args.config == 4 and args.impl != "reference"
+    if args.warmup is None:
+        args.warmup = 1 if large else 3
+    if args.steps is None:
+        args.steps = 2 if large else 5
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -249,6 +370,8 @@ def main():
         return run_reference(args, rank)
     if args.config == 3:
         return run_uneven(args)
+    if args.config == 4:
+        return run_large(args)
 
     import torch
     torch.cuda.set_device(local)
@@ -366,7 +489,8 @@ def main():
                        "metric_evals_per_patch": nf, "gradient_evals_per_patch": ndf,
                        "cg_iterations_per_s": world * P * args.iterations / (ms_dev / 1000.0)},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": int(launches), "roofline": roofline, "clocks": clk.summary()}
+            "gpu_launches": int(launches), "roofline": roofline, "clocks": clk.summary(),
+            "launch_shapes": solver.launch_shape()}
 
     if rank == 0 and not args.no_baselines:
         # plain FP64 GPU form: same algorithm in double precision, one patch per launch sequence

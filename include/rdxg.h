@@ -54,7 +54,7 @@ typedef struct {
     int32_t n_free;        /* columns of the null-space map (Constraints::nFreeParameters) */
     int32_t cutout_size;   /* image cutout size incl. the max-local-shift margins */
     int32_t max_patches;   /* batch capacity */
-    int32_t precision;     /* rdxg_precision */
+    int32_t precision;     /* rdxg_precision (RDXG_FP64 takes otf_size <= 88) */
     int32_t device;        /* CUDA device ordinal */
 } rdxg_geometry;
 
@@ -225,6 +225,31 @@ int32_t rdxg_phase_mode(const rdxg_solver* h);
  * analytic adjoint gradient, ms[4] finite-difference gradient; average ms per launch over
  * reps launches.  Used to pick kernel shapes and to report the roofline. */
 int rdxg_profile_kernels(rdxg_solver* h, int32_t reps, double* ms);
+
+/* Launch shapes: threads per block of the kernels that dominate a round.  eval_threads: the
+ * fused evaluation k_eval (512 or 384; 0 on the general path); forward_threads: the general
+ * path's transform kernel k_forward (256 or 512, 512 or 1024 at OTF size 128; 0 on the fused
+ * path); adjoint_threads: the analytic gradient k_adjoint (same choices as forward).  No
+ * shape changes a result: every element is computed by the same arithmetic. */
+typedef struct {
+    int32_t eval_threads;
+    int32_t forward_threads;
+    int32_t adjoint_threads;
+} rdxg_launch_shape;
+
+/* The launch-shape planner, in place of the FFTW_MEASURE planning of the reference's
+ * FourierTransform (image/fouriertransform.cpp:73-90, which times candidate plans once per
+ * transform size and keeps the fastest): times every compiled shape of each kernel on the
+ * loaded batch (reps launches each, CUDA events) and keeps the fastest.  The first solve of a
+ * handle does this by itself (or takes the shapes measured by an earlier handle of the same
+ * geometry, device and batch size in this process); RDXG_AUTOTUNE=0 in the environment keeps
+ * the default shapes.  FP64 handles have one shape.  chosen (or NULL): the shapes kept;
+ * ms (or NULL): [6] ms per launch of eval (default, alternative), forward (...), adjoint (...),
+ * 0 for kernels the handle's path does not use. */
+int rdxg_autotune(rdxg_solver* h, int32_t reps, rdxg_launch_shape* chosen, double* ms);
+/* Pins the shapes (0 in a field keeps that kernel's current shape); no measurement follows. */
+int rdxg_set_launch_shape(rdxg_solver* h, const rdxg_launch_shape* shape);
+int rdxg_get_launch_shape(const rdxg_solver* h, rdxg_launch_shape* shape);
 
 /* Debug copies of device state (host buffers sized by the caller):
  * which = 0 D [P][I][N][N] complex, 1 OTF [P][I][N][N] complex, 2 gamma [P][nObj],

@@ -18,7 +18,8 @@ EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "r
             "rdxg_set_patches", "rdxg_set_patches_device", "rdxg_metric", "rdxg_gradient",
             "rdxg_solve", "rdxg_solve_async", "rdxg_solve_many", "rdxg_fetch_results", "rdxg_last_launch_count",
             "rdxg_debug_copy", "rdxg_cg_minimize", "rdxg_profile_kernels", "rdxg_metric_with_reference",
-            "rdxg_metric_noalloc", "rdxg_restore", "rdxg_restore_ex", "rdxg_set_phase_mode", "rdxg_phase_mode")
+            "rdxg_metric_noalloc", "rdxg_restore", "rdxg_restore_ex", "rdxg_set_phase_mode", "rdxg_phase_mode",
+            "rdxg_autotune", "rdxg_set_launch_shape", "rdxg_get_launch_shape")
 
 
 class Geometry(C.Structure):
@@ -43,6 +44,10 @@ class SolveParams(C.Structure):
                 ("min_iterations", C.c_int32), ("target_iterations", C.c_int32), ("fd_first", C.c_int32),
                 ("max_metrics", C.c_int32), ("check_every", C.c_int32), ("ftol", C.c_double),
                 ("eps", C.c_double)]
+
+
+class LaunchShape(C.Structure):
+    _fields_ = [("eval_threads", C.c_int32), ("forward_threads", C.c_int32), ("adjoint_threads", C.c_int32)]
 
 
 class PatchReport(C.Structure):
@@ -93,6 +98,9 @@ def load(path: str = LIB_PATH):
     L.rdxg_phase_mode.restype = C.c_int32
     L.rdxg_phase_mode.argtypes = [vp]
     L.rdxg_profile_kernels.argtypes = [vp, C.c_int32, vp]
+    L.rdxg_autotune.argtypes = [vp, C.c_int32, C.POINTER(LaunchShape), vp]
+    L.rdxg_set_launch_shape.argtypes = [vp, C.POINTER(LaunchShape)]
+    L.rdxg_get_launch_shape.argtypes = [vp, C.POINTER(LaunchShape)]
     L.rdxg_cg_minimize.argtypes = [C.c_int32, C.c_int32, C.POINTER(SolveParams), C.c_double, F_FN, DF_FN,
                                    SHIFT_FN, vp, vp, C.POINTER(PatchReport), vp]
     _LIB = L

@@ -1,9 +1,12 @@
 // C ABI of the batched MOMFBD solver core (include/rdxg.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -93,6 +96,11 @@ struct rdxg_solver {
     PhaseTcPlan tcPlan{};
     __nv_bfloat16* dZt = nullptr;    // split modes (room for three parts)
     int32_t* dTcStatus = nullptr;
+    // launch shapes (0 default block size, 1 the alternative) and how they are chosen:
+    // tune 1 = measured on the first solve (or taken from the planner's table), 0 = pinned
+    int shapeEval = 0, shapeFwd = 0, shapeAdj = 0;
+    int tune = 1;
+    bool tuned = false;
 };
 
 namespace {
@@ -190,6 +198,7 @@ KParams<T> make_kparams(rdxg_solver* h) {
     k.req = h->dReq; k.gmethod = h->dGm; k.modeCount = h->dMc; k.reinit = h->dReinit;
     k.Dh = (cx<T>*)h->dDh; k.hIdx = h->dHIdx; k.nH = h->nH;
     k.gradP = h->dGradP; k.nGradP = h->dCounters + 2; k.fdP = h->dFdP; k.nFdP = h->dCounters + 3;
+    k.shapeEval = h->shapeEval; k.shapeFwd = h->shapeFwd; k.shapeAdj = h->shapeAdj;
     return k;
 }
 
@@ -693,6 +702,8 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
     if (h->N != 2 * h->n) return fail(RDXG_ERR_ARG, "otf_size must be 2 * pupil_pixels");
     if (!supported_N(h->N)) return fail(RDXG_ERR_UNSUPPORTED, "otf_size not compiled (supported: 32, 64, 88, 128)");
     if (h->ps != h->N) return fail(RDXG_ERR_UNSUPPORTED, "patch_size must equal otf_size");
+    if (h->fp64 && (size_t)(Tile<128>::ELEMS + 128) * sizeof(cx<double>) > kMaxSmem && h->N == 128)
+        return fail(RDXG_ERR_UNSUPPORTED, "FP64 at otf_size 128: a double tile of 128 x 129 exceeds the shared memory of a block");
     if (h->cs < h->ps || ((h->cs - h->ps) & 1)) return fail(RDXG_ERR_ARG, "bad cutout_size");
     if (h->M < 1 || h->I < 1 || h->nObj < 1 || h->nObj > 64 || h->C < 1 || h->Pmax < 1 || h->nFree < 1)
         return fail(RDXG_ERR_ARG, "bad geometry");
@@ -752,6 +763,8 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
         h->adjGrid = h->numSMs * 8;
         h->fdGrid = h->numSMs * 8;
     }
+    const char* at = getenv("RDXG_AUTOTUNE");
+    if (at && atoi(at) == 0) h->tune = 0;   // default shapes, no measurement
     const char* nf = getenv("RDXG_NO_FUSED");
     if (!r && !(nf && atoi(nf))) r = setup_fused(h, s);
     *out = h;
@@ -1026,11 +1039,14 @@ struct SolvePlan {
     ShiftArgs sa{};
 };
 
+int plan_shapes_once(rdxg_solver* h);   // the launch-shape planner (below)
+
 // Everything rdxg_solve_async does before the rounds: state reset on the handle's stream.
 int prepare_solve(rdxg_solver* h, const rdxg_solve_params* s, SolvePlan& pl) {
     if (!h || !s) return RDXG_ERR_ARG;
     if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
     int r;
+    if ((r = plan_shapes_once(h))) return r;
     if (h->dirty && (r = prepare_patches(h))) return r;
     h->dirty = true;
     h->launches = 0;
@@ -1350,59 +1366,203 @@ int32_t rdxg_phase_mode(const rdxg_solver* h) {
     return h->tcPlan.valid ? h->tcPlan.parts : 0;
 }
 
+extern "C++" {
+namespace {
+
+// Times kernel `k` (0 forward of a metric evaluation, 1 per-object accumulation, 2 forward of
+// a gradient evaluation, 3 analytic adjoint, 4 finite-difference gradient) on the loaded batch
+// at its current point: average ms per launch over reps launches after one warm-up, with
+// CUDA events on the handle's stream.
+int time_kernel(rdxg_solver* h, int k, int reps, cudaEvent_t e0, cudaEvent_t e1, double* ms) {
+    const int G = h->P * h->I, PO = h->P * h->nObj;
+    const int req = (k < 2) ? REQ_F : REQ_DF;
+    const int gm = (k == 4) ? GM_FD : GM_VOGEL;
+    int r;
+    if ((r = set_requests(h, req, gm, h->M))) return r;
+    if (h->fused && (r = host_lists(h, req, req == REQ_DF ? 1 : 0))) return r;
+    auto launch = [&](int which) {
+        with_size(h->N, h->fp64, [&](auto L, auto t) {
+            using T = decltype(t);
+            KParams<T> kp = make_kparams<T>(h);
+            if (h->fused && which <= 2) {
+                with_eval(h->N, [&](auto E) {
+                    EvalParams<float> e = make_evalparams<float>(h);
+                    if (which == 1) {
+                        decltype(E)::reduce(e, h->reduceGrid, h->stream);
+                    } else {
+                        decltype(E)::phase(e, h->phaseGrid, h->stream);
+                        decltype(E)::eval(e, h->npt, h->evalGrid, h->stream);
+                    }
+                });
+                return;
+            }
+            switch (which) {
+                case 0: case 2: decltype(L)::forward(kp, G, h->stream); break;
+                case 1: launch_accum<T>(kp, PO, h->stream); break;
+                case 3: decltype(L)::adjoint(kp, h->adjGrid, GK_VOGEL, h->stream); break;
+                case 4: launch_fd(h); break;
+            }
+        });
+    };
+    // inputs of the timed kernel: forward and accumulation in the requested mode
+    if (k >= 3) { launch(2); launch(1); }
+    if (k == 1) launch(0);
+    launch(k);   // warm-up
+    CK(h, cudaEventRecord(e0, h->stream));
+    for (int i = 0; i < reps; ++i) launch(k);
+    CK(h, cudaEventRecord(e1, h->stream));
+    CK(h, cudaEventSynchronize(e1));
+    CKL(h);
+    float t = 0;
+    CK(h, cudaEventElapsedTime(&t, e0, e1));
+    *ms = (double)t / reps;
+    return RDXG_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Launch-shape planner: the counterpart of the reference's FFTW_MEASURE planning
+// (fouriertransform.cpp:73-90), which times candidate transform plans once per size and
+// keeps the fastest.  The candidates are the block sizes compiled for the kernels that
+// dominate a round -- k_eval (fused path: 512 or 384 threads), k_forward (general path) and
+// k_adjoint (256 or 512 threads, 512 or 1024 at N = 128) -- and no choice changes a result:
+// every element of these kernels is computed by the same arithmetic whatever the block size.
+// (The radix plan of each size is fixed by its shared-memory tile.)  The first solve of a
+// handle measures the candidates on its loaded batch, unless a handle of the same geometry
+// on the same device has already done so in this process (the table below, the planner's
+// wisdom).  FP64 handles, the plain baseline form, have one shape.
+// ---------------------------------------------------------------------------------------
+struct ShapeKey {
+    int device, N, fused, M, I, P;
+    bool operator<(const ShapeKey& o) const {
+        const int a[6] = {device, N, fused, M, I, P}, b[6] = {o.device, o.N, o.fused, o.M, o.I, o.P};
+        return std::lexicographical_compare(a, a + 6, b, b + 6);
+    }
+};
+struct ShapeChoice { int eval, fwd, adj; };
+std::mutex& wisdom_mutex() {
+    static std::mutex m;
+    return m;
+}
+std::map<ShapeKey, ShapeChoice>& wisdom() {
+    static std::map<ShapeKey, ShapeChoice> w;
+    return w;
+}
+ShapeKey shape_key(const rdxg_solver* h) { return ShapeKey{h->geo.device, h->N, h->fused ? 1 : 0, h->M, h->I, h->P}; }
+
+// Measures both shapes of every tuned kernel of the handle's path and keeps the faster.
+// ms (or null): [6] eval (default, alternative), forward (...), adjoint (...); 0 where a
+// kernel is not tuned on this path.
+int plan_shapes(rdxg_solver* h, int reps, double* ms) {
+    double t[6] = {0, 0, 0, 0, 0, 0};
+    if (h->fp64) {
+        h->shapeEval = h->shapeFwd = h->shapeAdj = 0;
+        if (ms) std::memcpy(ms, t, sizeof(t));
+        return RDXG_OK;
+    }
+    CK(h, cudaMemsetAsync(h->dAlphaEff, 0, (size_t)h->P * h->I * h->M * sizeof(float), h->stream));
+    cudaEvent_t e0, e1;
+    CK(h, cudaEventCreate(&e0));
+    CK(h, cudaEventCreate(&e1));
+    int* field[3] = {&h->shapeEval, &h->shapeFwd, &h->shapeAdj};
+    const bool used[3] = {h->fused, !h->fused, true};
+    const int which[3] = {0, 0, 3};
+    int r = RDXG_OK;
+    for (int f = 0; f < 3 && !r; ++f) {
+        if (!used[f]) { *field[f] = 0; continue; }
+        for (int v = 0; v < 2 && !r; ++v) {
+            *field[f] = v;
+            r = time_kernel(h, which[f], reps, e0, e1, &t[2 * f + v]);
+        }
+        *field[f] = t[2 * f + 1] < t[2 * f] ? 1 : 0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (r) return r;
+    h->dirty = true;     // the timed kernels overwrote per-image state: the solve re-initialises
+    {
+        std::lock_guard<std::mutex> lock(wisdom_mutex());
+        wisdom()[shape_key(h)] = ShapeChoice{h->shapeEval, h->shapeFwd, h->shapeAdj};
+    }
+    if (getenv("RDXG_VERBOSE"))
+        fprintf(stderr, "launch shapes (N %d, P %d): eval %d [%.3f %.3f ms], forward %d [%.3f %.3f], adjoint %d "
+                "[%.3f %.3f]\n", h->N, h->P, h->shapeEval, t[0], t[1], h->shapeFwd, t[2], t[3], h->shapeAdj, t[4], t[5]);
+    if (ms) std::memcpy(ms, t, sizeof(t));
+    return RDXG_OK;
+}
+
+// The first solve of a handle: shapes from the planner's table, or measured.
+int plan_shapes_once(rdxg_solver* h) {
+    if (h->tune != 1 || h->tuned) return RDXG_OK;
+    h->tuned = true;
+    {
+        std::lock_guard<std::mutex> lock(wisdom_mutex());
+        auto it = wisdom().find(shape_key(h));
+        if (it != wisdom().end()) {
+            h->shapeEval = it->second.eval; h->shapeFwd = it->second.fwd; h->shapeAdj = it->second.adj;
+            return RDXG_OK;
+        }
+    }
+    return plan_shapes(h, 3, nullptr);
+}
+
+int threads_of(const rdxg_solver* h, int family, int variant) {
+    if (family == 0) return h->fused ? (variant ? kEvalThreadsAlt : kEvalThreads) : 0;
+    if (family == 1 && h->fused) return 0;
+    const int base = h->N >= 128 ? 512 : 256;
+    return (variant && !h->fp64) ? 2 * base : base;
+}
+
+}  // namespace
+}  // extern "C++"
+
 int rdxg_profile_kernels(rdxg_solver* h, int32_t reps, double* ms) {
     if (!h || !ms || reps < 1) return RDXG_ERR_ARG;
     if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
     cudaEvent_t e0, e1;
     CK(h, cudaEventCreate(&e0));
     CK(h, cudaEventCreate(&e1));
-    const int G = h->P * h->I, PO = h->P * h->nObj;
     int r = RDXG_OK;
-    for (int k = 0; k < 5 && !r; ++k) {
-        const int req = (k < 2) ? REQ_F : REQ_DF;
-        const int gm = (k == 4) ? GM_FD : GM_VOGEL;
-        if ((r = set_requests(h, req, gm, h->M))) break;
-        if (h->fused && (r = host_lists(h, req, req == REQ_DF ? 1 : 0))) break;
-        auto launch = [&](int which) {
-            with_size(h->N, h->fp64, [&](auto L, auto t) {
-                using T = decltype(t);
-                KParams<T> kp = make_kparams<T>(h);
-                if (h->fused && which <= 2) {
-                    with_eval(h->N, [&](auto E) {
-                        EvalParams<float> e = make_evalparams<float>(h);
-                        if (which == 1) {
-                            decltype(E)::reduce(e, h->reduceGrid, h->stream);
-                        } else {
-                            decltype(E)::phase(e, h->phaseGrid, h->stream);
-                            decltype(E)::eval(e, h->npt, h->evalGrid, h->stream);
-                        }
-                    });
-                    return;
-                }
-                switch (which) {
-                    case 0: case 2: decltype(L)::forward(kp, G, h->stream); break;
-                    case 1: launch_accum<T>(kp, PO, h->stream); break;
-                    case 3: decltype(L)::adjoint(kp, h->adjGrid, GK_VOGEL, h->stream); break;
-                    case 4: launch_fd(h); break;
-                }
-            });
-        };
-        // inputs of the timed kernel: forward and accumulation in the requested mode
-        if (k >= 3) { launch(2); launch(1); }
-        if (k == 1) launch(0);
-        launch(k);   // warm-up
-        CK(h, cudaEventRecord(e0, h->stream));
-        for (int i = 0; i < reps; ++i) launch(k);
-        CK(h, cudaEventRecord(e1, h->stream));
-        CK(h, cudaEventSynchronize(e1));
-        CKL(h);
-        float t = 0;
-        CK(h, cudaEventElapsedTime(&t, e0, e1));
-        ms[k] = (double)t / reps;
-    }
+    for (int k = 0; k < 5 && !r; ++k) r = time_kernel(h, k, reps, e0, e1, &ms[k]);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return r;
+}
+
+int rdxg_autotune(rdxg_solver* h, int32_t reps, rdxg_launch_shape* chosen, double* ms) {
+    if (!h || reps < 1) return RDXG_ERR_ARG;
+    if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
+    int r = plan_shapes(h, reps, ms);
+    if (r) return r;
+    h->tuned = true;
+    h->tune = 1;
+    return rdxg_get_launch_shape(h, chosen);
+}
+
+int rdxg_set_launch_shape(rdxg_solver* h, const rdxg_launch_shape* shape) {
+    if (!h || !shape) return RDXG_ERR_ARG;
+    int v[3] = {h->shapeEval, h->shapeFwd, h->shapeAdj};
+    const int32_t want[3] = {shape->eval_threads, shape->forward_threads, shape->adjoint_threads};
+    for (int f = 0; f < 3; ++f) {
+        if (want[f] == 0) continue;
+        if (want[f] == threads_of(h, f, 0)) v[f] = 0;
+        else if (want[f] == threads_of(h, f, 1)) v[f] = 1;
+        else {
+            h->err = "launch shape " + std::to_string(want[f]) + " is not compiled for this kernel (" +
+                     std::to_string(threads_of(h, f, 0)) + " or " + std::to_string(threads_of(h, f, 1)) + ")";
+            return RDXG_ERR_ARG;
+        }
+    }
+    h->shapeEval = v[0]; h->shapeFwd = v[1]; h->shapeAdj = v[2];
+    h->tune = 0;
+    return RDXG_OK;
+}
+
+int rdxg_get_launch_shape(const rdxg_solver* h, rdxg_launch_shape* shape) {
+    if (!h || !shape) return RDXG_ERR_ARG;
+    shape->eval_threads = threads_of(h, 0, h->shapeEval);
+    shape->forward_threads = threads_of(h, 1, h->shapeFwd);
+    shape->adjoint_threads = threads_of(h, 2, h->shapeAdj);
+    return RDXG_OK;
 }
 
 int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes) {

@@ -7,6 +7,10 @@
 
 namespace rdxg {
 
+// FP32 handles have a second block size of k_forward and k_adjoint for the planner; the FP64
+// form (the plain baseline) keeps one.
+template <typename T> struct HasAlt { static constexpr bool value = std::is_same<T, float>::value; };
+
 template <typename T, int N>
 static size_t extra_smem(int M) {
     size_t a = (size_t)M * sizeof(T);
@@ -30,6 +34,11 @@ cudaError_t Launcher<T, N>::setup(int M) {
     if ((e = raise_smem_limit(k_forward<T, N, THREADS>, sm))) return e;
     if ((e = raise_smem_limit(k_adjoint<T, N, THREADS>, sm))) return e;
     if ((e = raise_smem_limit(k_fd<T, N, THREADS>, sm))) return e;
+    if constexpr (HasAlt<T>::value) {
+        constexpr int ALT = ThreadsAlt<N>::value;
+        if ((e = raise_smem_limit(k_forward<T, N, ALT>, sm))) return e;
+        if ((e = raise_smem_limit(k_adjoint<T, N, ALT>, sm))) return e;
+    }
     return cudaSuccess;
 }
 
@@ -42,6 +51,13 @@ void Launcher<T, N>::prep(const KParams<T>& kp, int full, int nImg, cudaStream_t
 template <typename T, int N>
 void Launcher<T, N>::forward(const KParams<T>& kp, int nImg, cudaStream_t st) {
     const size_t sm = smem_base() + extra_smem<T, N>(kp.M);
+    if constexpr (HasAlt<T>::value) {
+        constexpr int ALT = ThreadsAlt<N>::value;
+        if (kp.shapeFwd == 1) {
+            k_forward<T, N, ALT><<<nImg, ALT, sm, st>>>(kp);
+            return;
+        }
+    }
     k_forward<T, N, THREADS><<<nImg, THREADS, sm, st>>>(kp);
 }
 
@@ -50,6 +66,13 @@ void Launcher<T, N>::adjoint(const KParams<T>& kp, int grid, int kind, cudaStrea
     (void)grid;
     const size_t sm = smem_base() + extra_smem<T, N>(kp.M);
     grid = kp.P * kp.I;
+    if constexpr (HasAlt<T>::value) {
+        constexpr int ALT = ThreadsAlt<N>::value;
+        if (kp.shapeAdj == 1) {
+            k_adjoint<T, N, ALT><<<grid, ALT, sm, st>>>(kp, kind);
+            return;
+        }
+    }
     k_adjoint<T, N, THREADS><<<grid, THREADS, sm, st>>>(kp, kind);
 }
 
@@ -100,6 +123,9 @@ cudaError_t EvalLauncher<T, N>::setup(int M, int npt, int nH) {
 #define RDXG_SET(NPT) e = raise_smem_limit(k_eval<T, N, kEvalThreads, NPT>, sm)
     RDXG_NPT_SWITCH(npt, RDXG_SET);
 #undef RDXG_SET
+#define RDXG_SET(NPT) e = raise_smem_limit(k_eval<T, N, kEvalThreadsAlt, NPT>, sm)
+    if (e == cudaSuccess) RDXG_NPT_SWITCH(npt, RDXG_SET);
+#undef RDXG_SET
     if (e == cudaSuccess)
         e = raise_smem_limit(k_phase<T, N, kPhasePix, kMaxChunk>, (size_t)M * (kPhasePix + kMaxChunk) * sizeof(T));
     if (e == cudaSuccess && fd_smem(nH) + 1024 <= kMaxSmem)
@@ -120,6 +146,12 @@ int EvalLauncher<T, N>::occupancy(int M, int npt, int nH) {
 template <typename T, int N>
 void EvalLauncher<T, N>::eval(const EvalParams<T>& e, int npt, int grid, cudaStream_t st) {
     const size_t sm = smem(e.k.M, e.hp.nH);
+    if (e.k.shapeEval == 1) {
+#define RDXG_LAUNCH(NPT) k_eval<T, N, kEvalThreadsAlt, NPT><<<grid, kEvalThreadsAlt, sm, st>>>(e)
+        RDXG_NPT_SWITCH(npt, RDXG_LAUNCH);
+#undef RDXG_LAUNCH
+        return;
+    }
 #define RDXG_LAUNCH(NPT) k_eval<T, N, kEvalThreads, NPT><<<grid, kEvalThreads, sm, st>>>(e)
     RDXG_NPT_SWITCH(npt, RDXG_LAUNCH);
 #undef RDXG_LAUNCH
@@ -180,6 +212,7 @@ size_t EvalLauncher<T, N>::fd_smem(int nH) {
 
 template <typename T, int N>
 void EvalLauncher<T, N>::fd_half(const EvalParams<T>& e, int grid, cudaStream_t st) {
+    // one block size only: its per-thread partial sums of the metric change depend on it
     k_fd_half<T, N, kEvalThreads><<<grid, kEvalThreads, fd_smem(e.hp.nH), st>>>(e);
 }
 

@@ -66,6 +66,9 @@ struct KParams {
     cx<T>* Dh;                // [g][nH]
     const int32_t* hIdx;      // [nH] centred indices
     int32_t nH;
+    // launch-shape variants picked by the planner (read by the host-side launchers only):
+    // 0 the default block size, 1 the alternative (see rdxg_launch.h)
+    int32_t shapeEval, shapeFwd, shapeAdj;
 };
 
 enum GradKind : int32_t { GK_VOGEL = 0, GK_EXACT = 1 };

@@ -29,6 +29,10 @@ cudaError_t raise_smem_limit(K* kernel, size_t bytes) {
 }
 
 template <int N> struct Threads { static constexpr int value = (N >= 128) ? 512 : 256; };
+// The alternative block size of the one-image-per-block kernels (k_forward, k_adjoint) in
+// FP32, picked by the launch-shape planner when it measures faster: the per-element
+// arithmetic does not depend on the block size, so neither do the results.
+template <int N> struct ThreadsAlt { static constexpr int value = 2 * Threads<N>::value; };
 
 template <typename T, int N>
 struct Launcher {
@@ -57,6 +61,9 @@ template <typename T> void launch_accum(const KParams<T>& kp, int nPo, cudaStrea
 #endif
 constexpr int kEvalThreads = RDXG_EVAL_THREADS;
 static_assert(kEvalThreads % 32 == 0 && kEvalThreads <= 1024, "block size");
+// the planner's alternative block size of k_eval (results are the same: each half-plane
+// point is accumulated by one thread, whatever the block size)
+constexpr int kEvalThreadsAlt = kEvalThreads == 384 ? 512 : 384;
 constexpr int kReduceThreads = 256;
 constexpr int kPhasePix = 256;      // pixels per block of the mode expansion
 constexpr int kMaxChunk = 8;        // images per chunk (upper bound)

@@ -223,6 +223,25 @@ class Solver:
         self._check(_lib.load().rdxg_profile_kernels(self.h, reps, _lib.ptr(ms)), "rdxg_profile_kernels")
         return dict(zip(("forward", "accum", "forward_grad", "adjoint", "fd"), ms.tolist()))
 
+    def autotune(self, reps: int = 3) -> dict:
+        """The launch-shape planner on the loaded batch (rdxg_autotune): the shapes kept and the
+        measured ms per launch of each candidate."""
+        sh = _lib.LaunchShape()
+        ms = np.zeros(6)
+        self._check(_lib.load().rdxg_autotune(self.h, reps, C.byref(sh), _lib.ptr(ms)), "rdxg_autotune")
+        return dict(shape=self.launch_shape(), ms=dict(eval=ms[0:2].tolist(), forward=ms[2:4].tolist(),
+                                                       adjoint=ms[4:6].tolist()))
+
+    def set_launch_shape(self, eval_threads: int = 0, forward_threads: int = 0, adjoint_threads: int = 0) -> None:
+        """Pins the threads per block of k_eval, k_forward and k_adjoint (0: keep)."""
+        sh = _lib.LaunchShape(eval_threads, forward_threads, adjoint_threads)
+        self._check(_lib.load().rdxg_set_launch_shape(self.h, C.byref(sh)), "rdxg_set_launch_shape")
+
+    def launch_shape(self) -> dict:
+        sh = _lib.LaunchShape()
+        self._check(_lib.load().rdxg_get_launch_shape(self.h, C.byref(sh)), "rdxg_get_launch_shape")
+        return dict(eval=sh.eval_threads, forward=sh.forward_threads, adjoint=sh.adjoint_threads)
+
     def launch_count(self) -> int:
         return int(_lib.load().rdxg_last_launch_count(self.h))
 
