@@ -510,10 +510,19 @@ def main():
         plain_v = nplain / t_plain
         f32 = [reps[p].final_metric for p in range(nplain)]
         rel = [abs(a - b) / abs(b) for a, b in zip(f32, finals64)]
+        # the metric at the chosen path's final alpha, evaluated by both forms on fresh handles
+        s32c = S.Solver(job, max_patches=nplain, device=local)
+        s32c.set_patches(cut[:nplain])
+        s64c = S.Solver(job, max_patches=nplain, precision="fp64", device=local)
+        s64c.set_patches(cut[:nplain])
+        m32c, m64c = s32c.metric(out["alpha"][:nplain]), s64c.metric(out["alpha"][:nplain])
+        s32c.close(); s64c.close()
         line["plain_fp64_gpu"] = {"value": plain_v, "unit": UNIT, "sample": f"{nplain} patches, per-patch launches",
                                   "speedup_chosen_vs_plain": value / world / plain_v,
                                   "final_metric_rel_diff_vs_fp64": rel,
+                                  "final_metric_signed_rel_vs_fp64": [(a - b) / abs(b) for a, b in zip(f32, finals64)],
                                   "within_1e-5": sum(1 for x in rel if x <= 1e-5),
+                                  "metric_rel_fp64_at_final_alpha": (np.abs(m32c - m64c) / np.abs(m64c)).tolist(),
                                   # alpha is in the reference's units (wavefront, lambda * rad)
                                   "alpha_rms_diff_rad": [float(np.sqrt(np.mean((out["alpha"][p] - alphas64[p]) ** 2))
                                                                / job.wavelength) for p in range(nplain)],

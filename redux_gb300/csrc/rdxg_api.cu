@@ -1372,8 +1372,9 @@ namespace {
 // Times kernel `k` (0 forward of a metric evaluation, 1 per-object accumulation, 2 forward of
 // a gradient evaluation, 3 analytic adjoint, 4 finite-difference gradient) on the loaded batch
 // at its current point: average ms per launch over reps launches after one warm-up, with
-// CUDA events on the handle's stream.
-int time_kernel(rdxg_solver* h, int k, int reps, cudaEvent_t e0, cudaEvent_t e1, double* ms) {
+// CUDA events on the handle's stream.  nGrad > 0: the adjoint works on the first nGrad
+// patches only (the size of a solve round's gradient list).
+int time_kernel(rdxg_solver* h, int k, int reps, cudaEvent_t e0, cudaEvent_t e1, double* ms, int nGrad = 0) {
     const int G = h->P * h->I, PO = h->P * h->nObj;
     const int req = (k < 2) ? REQ_F : REQ_DF;
     const int gm = (k == 4) ? GM_FD : GM_VOGEL;
@@ -1407,6 +1408,11 @@ int time_kernel(rdxg_solver* h, int k, int reps, cudaEvent_t e0, cudaEvent_t e1,
     // inputs of the timed kernel: forward and accumulation in the requested mode
     if (k >= 3) { launch(2); launch(1); }
     if (k == 1) launch(0);
+    if (k == 3 && nGrad > 0 && nGrad < h->P) {
+        const int32_t n = nGrad;
+        CK(h, cudaMemcpyAsync(h->dCounters + 2, &n, sizeof(n), cudaMemcpyHostToDevice, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
     launch(k);   // warm-up
     CK(h, cudaEventRecord(e0, h->stream));
     for (int i = 0; i < reps; ++i) launch(k);
@@ -1427,7 +1433,8 @@ int time_kernel(rdxg_solver* h, int k, int reps, cudaEvent_t e0, cudaEvent_t e1,
 // k_adjoint (256 or 512 threads, 512 or 1024 at N = 128) -- and no choice changes a result:
 // every element of these kernels is computed by the same arithmetic whatever the block size.
 // (The radix plan of each size is fixed by its shared-memory tile.)  The first solve of a
-// handle measures the candidates on its loaded batch, unless a handle of the same geometry
+// handle measures the candidates on its loaded batch (the adjoint on a tenth of the patches,
+// the share of a solve round that asks for gradients), unless a handle of the same geometry
 // on the same device has already done so in this process (the table below, the planner's
 // wisdom).  FP64 handles, the plain baseline form, have one shape.
 // ---------------------------------------------------------------------------------------
@@ -1466,12 +1473,15 @@ int plan_shapes(rdxg_solver* h, int reps, double* ms) {
     int* field[3] = {&h->shapeEval, &h->shapeFwd, &h->shapeAdj};
     const bool used[3] = {h->fused, !h->fused, true};
     const int which[3] = {0, 0, 3};
+    // a solve round evaluates every active patch but takes the gradients of about one in ten
+    // (the others are in their line searches): the adjoint is timed on such a list
+    const int nGrad[3] = {0, 0, std::max(1, (h->P + 9) / 10)};
     int r = RDXG_OK;
     for (int f = 0; f < 3 && !r; ++f) {
         if (!used[f]) { *field[f] = 0; continue; }
         for (int v = 0; v < 2 && !r; ++v) {
             *field[f] = v;
-            r = time_kernel(h, which[f], reps, e0, e1, &t[2 * f + v]);
+            r = time_kernel(h, which[f], reps, e0, e1, &t[2 * f + v], nGrad[f]);
         }
         *field[f] = t[2 * f + 1] < t[2 * f] ? 1 : 0;
     }
