@@ -389,9 +389,10 @@ def main():
     solver.set_stream(stream.cuda_stream)
     if args.kernels_only:
         solver.set_patches(cut)
+        tuned = solver.autotune(reps=3)     # the shapes a solve would use
         kt = solver.profile_kernels(reps=1)
         torch.cuda.synchronize()
-        print(json.dumps({"kernel_ms": kt, "patches": P}), flush=True)
+        print(json.dumps({"kernel_ms": kt, "patches": P, "launch_shapes": tuned}), flush=True)
         solver.close()
         return
     cut_dev = torch.from_numpy(cut).to(f"cuda:{local}")

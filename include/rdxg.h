@@ -113,6 +113,13 @@ int rdxg_create(const rdxg_geometry* geometry, const rdxg_static* statics, rdxg_
 int rdxg_destroy(rdxg_solver* h);
 const char* rdxg_last_error(const rdxg_solver* h);
 
+/* FIT_PLANE (the RF_FIT_PLANE run flag): before the images are windowed, subtract the plane
+ * fitted to the mean of each object's images, refit it when an object's images are
+ * re-shifted, and add it back to the restored object (Object::fitAvgPlane, object.cpp:
+ * 553-594; SubImage::getWindowedImg, subimage.cpp:106-150; Object::restorePatch,
+ * object.cpp:410-413).  Loaded patches are prepared again. */
+int rdxg_set_fit_plane(rdxg_solver* h, int32_t enable);
+
 /* Work on a caller-provided CUDA stream (cudaStream_t); NULL restores the handle's own. */
 int rdxg_set_stream(rdxg_solver* h, void* cuda_stream);
 
@@ -172,13 +179,14 @@ int rdxg_restore(rdxg_solver* h, const double* alpha, const double* frequency_cu
 
 /* rdxg_restore with the other outputs of Object::restorePatch (object.cpp:335-410, the
  * SF_SAVE_PSF / SF_SAVE_PSF_AVG / SF_SAVE_COBJ / SF_SAVE_RESIDUAL flags), FP64 on the device,
- * stored as float32 and trimmed to patch_size like the object:
+ * stored as float32 and trimmed to patch_size like the object (the fitted plane, with
+ * FIT_PLANE, is added to the object after them, as the reference does):
  *   RDXG_RESTORE_PSF      psf [P][I][ps][ps]      SubImage::getPSF of every image
  *   RDXG_RESTORE_PSF_AVG  psf [P][nObj][ps][ps]   their mean per object (takes precedence)
  *   RDXG_RESTORE_COBJ     cobj [P][I][ps][ps]     SubImage::convolveImage of the float object
  *   RDXG_RESTORE_RESIDUAL res [P][I][ps][ps]      convolved object minus the image
  * Images are in the order of the geometry (objects' channels, frames).  Buffers for flags not
- * set may be NULL.  The reference's fitted-plane re-addition (FIT_PLANE) is not supported. */
+ * set may be NULL. */
 #define RDXG_RESTORE_PSF 1
 #define RDXG_RESTORE_PSF_AVG 2
 #define RDXG_RESTORE_COBJ 4

@@ -40,6 +40,7 @@ struct Settings {
     int32_t maxMetrics = 1024;      // capacity of the metric history per patch
     bool restore = true;            // restore the objects after the solve
     bool noFilter = false;          // RF_NO_FILTER
+    bool fitPlane = false;          // RF_FIT_PLANE
     // further outputs of the restoration (Object::saveMask): RDXG_RESTORE_PSF,
     // RDXG_RESTORE_PSF_AVG, RDXG_RESTORE_COBJ, RDXG_RESTORE_RESIDUAL
     int32_t saveMask = 0;
@@ -70,6 +71,7 @@ public:
            std::vector<double> frequencyCutoff)
         : geo_(geometry), set_(settings), fc_(std::move(frequencyCutoff)) {
         check(rdxg_create(&geo_, &statics, &h_), "rdxg_create");
+        if (set_.fitPlane) check(rdxg_set_fit_plane(h_, 1), "rdxg_set_fit_plane");
         if ((int)fc_.size() != geo_.n_objects) fc_.assign(geo_.n_objects, geo_.otf_size / 2.0);
         alpha.assign((size_t)geo_.n_images * geo_.n_modes, 0.0);
     }

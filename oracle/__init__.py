@@ -81,6 +81,8 @@ def lib():
         L.orc_cons_reverse_add.argtypes = [C.c_void_p, f64p, f64p, f64p]
         L.orc_restore.restype = C.c_int
         L.orc_restore.argtypes = [C.c_void_p, f64p, f64p, C.c_int, f64p]
+        L.orc_set_fit_plane.argtypes = [C.c_void_p, C.c_int]
+        L.orc_get_plane.argtypes = [C.c_void_p, f32p]
         _LIB = L
     return _LIB
 
@@ -166,6 +168,17 @@ class OraclePatch:
         if getattr(self, "h", None):
             lib().orc_destroy(self.h)
             self.h = None
+
+    def set_fit_plane(self, on=True):
+        """RF_FIT_PLANE: fit and remove each object's mean-image plane (call before set_images)."""
+        lib().orc_set_fit_plane(self.h, int(bool(on)))
+
+    def plane(self):
+        """The fitted planes [nObj][ps][ps] (float32)."""
+        ps = self.job.patch_size
+        out = np.zeros((self.nObj, ps, ps), np.float32)
+        lib().orc_get_plane(self.h, out)
+        return out
 
     def set_images(self, cutouts, residual_alpha=None, fixed_gamma=None):
         cut = np.ascontiguousarray(cutouts, np.float32)

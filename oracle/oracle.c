@@ -309,6 +309,9 @@ typedef struct {
     double* regGamma;   /* nObj */
     int fixed_gamma;
     double* fixedGamma;
+    /* FIT_PLANE (RF_FIT_PLANE): the fitted plane of each object, float values as
+     * Object::fittedPlane, nObj * ps * ps; NULL when off */
+    float* plane;
     /* object work */
     cplx* P; double* Q; cplx* PQ; double* PS; double* QS; /* nObj*N2 */
     double* objMetric;
@@ -466,7 +469,7 @@ void orc_destroy(orc_patch* p) {
     free(p->nsRow); free(p->nsCol); free(p->nsVal);
     free(p->cutouts); free(p->phiChannel); free(p->otfNorm); free(p->curShift);
     free(p->curTiltOffset); free(p->statMean); free(p->statStd); free(p->statNoise);
-    free(p->D); free(p->ftSum); free(p->regGamma); free(p->fixedGamma);
+    free(p->D); free(p->ftSum); free(p->regGamma); free(p->fixedGamma); free(p->plane);
     free(p->P); free(p->Q); free(p->PQ); free(p->PS); free(p->QS); free(p->objMetric);
     free(p->OTF); free(p->PF); free(p->PHI);
     free(p->alpha); free(p->alphaOffset); free(p->gradAlpha); free(p->enabled);
@@ -574,6 +577,69 @@ static void img_stats(const double* x, long n, double* mean, double* stddev) {
     *stddev = sqrt(r - m * m);
 }
 
+/* Object::fitAvgPlane (object.cpp:553-594): the object's images (patch views at their
+ * current shifts) summed in float in image order, divided by their count in float, a plane
+ * z = a*dy + b*dx + c fitted over the whole grid by least squares (redux::image::fitPlane,
+ * image/utils.cpp:169-233, GSL multifit there; a 3x3 solve here) and stored without its
+ * constant (subtract_mean) through makePlane (image/utils.cpp:128-147) as float. */
+static void fit_avg_plane(orc_patch* p, int o) {
+    const int ps = p->ps, cs = p->cs;
+    const long ps2 = (long)ps * ps;
+    float* acc = (float*)xcalloc((size_t)ps2, sizeof(float));
+    int count = 0;
+    for (int j = 0; j < p->nImg; ++j) {
+        if (p->imgObj[j] != o) continue;
+        const int oy = p->margin + p->curShift[2 * j + 0], ox = p->margin + p->curShift[2 * j + 1];
+        const float* cut = p->cutouts + (long)j * cs * cs;
+        for (int y = 0; y < ps; ++y)
+            for (int x = 0; x < ps; ++x) {
+                volatile float t = acc[(long)y * ps + x] + cut[(long)(oy + y) * cs + ox + x];
+                acc[(long)y * ps + x] = t;
+            }
+        count++;
+    }
+    /* normal equations, unknowns (a, b, c), design columns (dy, dx, 1) */
+    double A[3][4] = {{0}};
+    for (int y = 0; y < ps; ++y)
+        for (int x = 0; x < ps; ++x) {
+            volatile float zf = acc[(long)y * ps + x] / (float)count;
+            const double z = zf, r[3] = {(double)(y - ps / 2), (double)(x - ps / 2), 1.0};
+            for (int i = 0; i < 3; ++i) {
+                for (int k = 0; k < 3; ++k) A[i][k] += r[i] * r[k];
+                A[i][3] += r[i] * z;
+            }
+        }
+    for (int c = 0; c < 3; ++c) {            /* Gaussian elimination with partial pivoting */
+        int piv = c;
+        for (int i = c + 1; i < 3; ++i) if (fabs(A[i][c]) > fabs(A[piv][c])) piv = i;
+        for (int k = 0; k < 4; ++k) { double t = A[c][k]; A[c][k] = A[piv][k]; A[piv][k] = t; }
+        for (int i = c + 1; i < 3; ++i) {
+            const double f = A[i][c] / A[c][c];
+            for (int k = c; k < 4; ++k) A[i][k] -= f * A[c][k];
+        }
+    }
+    double sol[3];
+    for (int i = 2; i >= 0; --i) {
+        double v = A[i][3];
+        for (int k = i + 1; k < 3; ++k) v -= A[i][k] * sol[k];
+        sol[i] = v / A[i][i];
+    }
+    float* pl = p->plane + (long)o * ps2;
+    for (int y = 0; y < ps; ++y)
+        for (int x = 0; x < ps; ++x)
+            pl[(long)y * ps + x] = (float)(sol[0] * (double)(y - ps / 2) + sol[1] * (double)(x - ps / 2));
+    free(acc);
+}
+
+void orc_set_fit_plane(orc_patch* p, int on) {
+    if (on && !p->plane) p->plane = (float*)xcalloc((size_t)p->nObj * p->ps * p->ps, sizeof(float));
+    if (!on && p->plane) { free(p->plane); p->plane = NULL; }
+}
+
+void orc_get_plane(const orc_patch* p, float* out) {
+    if (p->plane) memcpy(out, p->plane, sizeof(float) * (size_t)p->nObj * p->ps * p->ps);
+}
+
 /* SubImage::initialize(o, doReset) (subimage.cpp:155-209) with getWindowedImg (106-150);
  * returns the contribution rg to reg_gamma when doReset. */
 static void init_image(orc_patch* p, int j, int doReset, double* rg_out, cplx* oldFT) {
@@ -589,7 +655,12 @@ static void init_image(orc_patch* p, int j, int doReset, double* rg_out, cplx* o
         for (int x = 0; x < ps; ++x) img[(long)y * ps + x] = (double)cut[(long)(oy + y) * cs + ox + x];
     double avg, sd;
     img_stats(img, ps2, &avg, &sd);
-    for (long i = 0; i < ps2; ++i) img[i] = (img[i] - avg) * p->window[i] + avg;
+    if (p->plane) {   /* getWindowedImg with the object's fitted plane (subimage.cpp:117-123) */
+        const float* pl = p->plane + (long)p->imgObj[j] * ps2;
+        for (long i = 0; i < ps2; ++i) img[i] = (img[i] - avg - pl[i]) * p->window[i] + avg;
+    } else {
+        for (long i = 0; i < ps2; ++i) img[i] = (img[i] - avg) * p->window[i] + avg;
+    }
     double mean, stddev;
     img_stats(img, ps2, &mean, &stddev);
     p->statMean[j] = mean;
@@ -651,6 +722,8 @@ void orc_set_images(orc_patch* p, const float* cutouts, const double* residual_a
     /* shiftAndInit(alpha_offset = 0, doReset = true): no shift, full initialisation */
     memset(p->ftSum, 0, sizeof(double) * (size_t)p->nObj * p->N2);
     memset(p->regGamma, 0, sizeof(double) * (size_t)p->nObj);
+    if (p->plane)     /* ObjectData::initPatch fits the planes before the images are set up */
+        for (int o = 0; o < p->nObj; ++o) fit_avg_plane(p, o);
     double* rg = (double*)xcalloc((size_t)p->nImg, sizeof(double));
 #pragma omp parallel for schedule(dynamic, 1) num_threads(p->nthreads)
     for (int j = 0; j < p->nImg; ++j) init_image(p, j, 1, &rg[j], NULL);
@@ -1188,6 +1261,7 @@ static void shift_and_init(orc_patch* p, const double* a) {
         if (adjust_shifts(p, j, a + (long)j * p->M)) shifted[p->imgObj[j]] = 1;
     for (int o = 0; o < p->nObj; ++o) {
         if (!shifted[o]) continue;
+        if (p->plane) fit_avg_plane(p, o);   /* Object::reInitialize refits the plane */
         for (int j = 0; j < p->nImg; ++j) {
             if (p->imgObj[j] != o) continue;
             cplx* oldFT = p->scr[j].tmpc3;   /* reused after init_image's reorder */
@@ -1510,6 +1584,10 @@ int orc_restore(orc_patch* p, const double* alpha, const double* frequency_cutof
         for (int y = 0; y < p->ps; ++y)
             for (int x = 0; x < p->ps; ++x)
                 out[((long)o * p->ps + y) * p->ps + x] = creal(obj[(long)(y + off) * N + x + off]) / (double)N2;
+        if (p->plane) {   /* od.img += fittedPlane (object.cpp:410-413) */
+            const float* pl = p->plane + (long)o * p->ps * p->ps;
+            for (long i = 0; i < (long)p->ps * p->ps; ++i) out[(long)o * p->ps * p->ps + i] += pl[i];
+        }
     }
     free(work);
     free(den);

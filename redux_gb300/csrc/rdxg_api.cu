@@ -101,6 +101,9 @@ struct rdxg_solver {
     int shapeEval = 0, shapeFwd = 0, shapeAdj = 0;
     int tune = 1;
     bool tuned = false;
+    // FIT_PLANE: the fitted plane of every (patch, object), slopes along y and x
+    bool fitPlane = false;
+    double* dPlane = nullptr;
 };
 
 namespace {
@@ -199,6 +202,7 @@ KParams<T> make_kparams(rdxg_solver* h) {
     k.Dh = (cx<T>*)h->dDh; k.hIdx = h->dHIdx; k.nH = h->nH;
     k.gradP = h->dGradP; k.nGradP = h->dCounters + 2; k.fdP = h->dFdP; k.nFdP = h->dCounters + 3;
     k.shapeEval = h->shapeEval; k.shapeFwd = h->shapeFwd; k.shapeAdj = h->shapeAdj;
+    k.plane = h->fitPlane ? h->dPlane : nullptr;
     return k;
 }
 
@@ -422,9 +426,10 @@ int prepare_patches(rdxg_solver* h) {
     with_size(h->N, h->fp64, [&](auto L, auto t) {
         using T = decltype(t);
         KParams<T> kp = make_kparams<T>(h);
+        if (h->fitPlane) launch_fit_plane<T>(kp, 1, h->P * h->nObj, h->stream);   // ObjectData::initPatch
         decltype(L)::prep(kp, 1, (int)G, h->stream);
     });
-    h->launches++;
+    h->launches += h->fitPlane ? 2 : 1;
     CKL(h);
     std::vector<double> rg(G);
     CK(h, cudaMemcpyAsync(rg.data(), h->dRg, G * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -781,6 +786,17 @@ int rdxg_destroy(rdxg_solver* h) {
     return RDXG_OK;
 }
 
+int rdxg_set_fit_plane(rdxg_solver* h, int32_t enable) {
+    if (!h) return RDXG_ERR_ARG;
+    if (enable && !h->dPlane) {
+        const int r = dalloc_t(h, &h->dPlane, (size_t)h->Pmax * h->nObj * 2);
+        if (r) return r;
+    }
+    h->fitPlane = enable != 0;
+    // loaded patches are prepared again with (or without) the planes
+    return h->loaded ? prepare_patches(h) : RDXG_OK;
+}
+
 int rdxg_set_stream(rdxg_solver* h, void* st) {
     if (!h) return RDXG_ERR_ARG;
     h->stream = st ? (cudaStream_t)st : h->own;
@@ -971,6 +987,10 @@ int rdxg_restore_ex(rdxg_solver* h, const double* alpha, const double* frequency
         if (ce == cudaSuccess && outputs) ce = decltype(L)::restore_outputs(kp, oa, outGrid, h->stream);
     });
     if (ce != cudaSuccess) { h->err = std::string("restore: ") + cudaGetErrorString(ce); return RDXG_ERR_CUDA; }
+    if (h->fitPlane) {   // after the convolved objects and residuals, as the reference
+        launch_add_plane(h->dPlane, h->dRestoreOut, h->P * h->nObj, h->ps, h->stream);
+        CKL(h);
+    }
     const size_t P = h->P;
     CK(h, cudaMemcpyAsync(objects, h->dRestoreOut, P * h->nObj * ps2 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
     if (outputs & RDXG_RESTORE_PSF_AVG)
@@ -1097,7 +1117,12 @@ int issue_round(const SolvePlan& pl, cudaStream_t st, const ShiftArgs& sar, Opt&
         CgArgs<T> ca = make_cgargs<T>(h, pl.prm);
         launch_cg<T>(ca, P, st);
         launch_shift(sar, P, st);
-        optional(0, [&](cudaStream_t s2) { decltype(L)::prep(kp, 0, G, s2); });
+        optional(0, [&](cudaStream_t s2) {
+            // Object::reInitialize: refit the planes of objects with shifted images, then
+            // re-initialise their images
+            if (h->fitPlane) launch_fit_plane<T>(kp, 0, P * h->nObj, s2);
+            decltype(L)::prep(kp, 0, G, s2);
+        });
         if (h->fused) {
             with_eval(h->N, [&](auto E) {
                 EvalParams<float> e = make_evalparams<float>(h);
@@ -1171,6 +1196,7 @@ int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
             sa.useConditions = 1;
             sa.counters = h->dCounters;
             sa.fixedLaunches = h->fused ? 5 : 4;
+            sa.prepLaunches = h->fitPlane ? 2 : 1;
             sa.launchCount = h->dLaunchCount;
             sa.condPrep = cond[0];
             sa.condAdjoint = cond[1];
@@ -1278,7 +1304,7 @@ int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
             h->err = "cudaMemsetAsync failed";
             return RDXG_ERR_CUDA;
         }
-        h->launches += h->fused ? 8 : 7;
+        h->launches += (h->fused ? 8 : 7) + (h->fitPlane ? 1 : 0);
         CKL(h);
         if ((round + 1) % check == 0) {
             CK(h, cudaMemcpyAsync(h->hActive, h->dActive, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));

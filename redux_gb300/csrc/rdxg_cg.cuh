@@ -304,6 +304,7 @@ struct ShiftArgs {
     cudaGraphConditionalHandle condPrep, condAdjoint, condFd;
     const int32_t* counters;
     int32_t fixedLaunches;
+    int32_t prepLaunches;       // kernels of the re-initialisation node (plane fit + preparation)
     unsigned long long* launchCount;
 };
 
@@ -317,7 +318,7 @@ __global__ void k_shift(ShiftArgs a) {
         cudaGraphSetConditional(a.condPrep, prep);
         cudaGraphSetConditional(a.condAdjoint, adj);
         cudaGraphSetConditional(a.condFd, fd);
-        *a.launchCount += (unsigned long long)(a.fixedLaunches + prep + adj + fd);
+        *a.launchCount += (unsigned long long)(a.fixedLaunches + prep * a.prepLaunches + adj + fd);
     }
     if (a.req[p] != REQ_SHIFT) {
         for (int j = threadIdx.x; j < a.I; j += blockDim.x) a.reinit[(size_t)p * a.I + j] = 0;

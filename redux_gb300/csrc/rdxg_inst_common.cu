@@ -19,6 +19,17 @@ void launch_shift(const ShiftArgs& a, int P, cudaStream_t st) {
     k_shift<0><<<P, 128, 0, st>>>(a);
 }
 
+template <typename T>
+void launch_fit_plane(const KParams<T>& kp, int full, int nPo, cudaStream_t st) {
+    k_fit_plane<T, 256><<<nPo, 256, 0, st>>>(kp, full);
+}
+
+void launch_add_plane(const double* plane, float* objects, int nPo, int ps, cudaStream_t st) {
+    k_add_plane<0><<<nPo, 256, 0, st>>>(plane, objects, ps);
+}
+
+template void launch_fit_plane<float>(const KParams<float>&, int, int, cudaStream_t);
+template void launch_fit_plane<double>(const KParams<double>&, int, int, cudaStream_t);
 template void launch_accum<float>(const KParams<float>&, int, cudaStream_t);
 template void launch_accum<double>(const KParams<double>&, int, cudaStream_t);
 template void launch_cg<float>(const CgArgs<float>&, int, cudaStream_t);

@@ -66,6 +66,9 @@ struct KParams {
     cx<T>* Dh;                // [g][nH]
     const int32_t* hIdx;      // [nH] centred indices
     int32_t nH;
+    // fitted planes (FIT_PLANE): [po][2] slopes (a along y, b along x) of the plane fitted to
+    // the object's mean image, or null
+    double* plane;
     // launch-shape variants picked by the planner (read by the host-side launchers only):
     // 0 the default block size, 1 the alternative (see rdxg_launch.h)
     int32_t shapeEval, shapeFwd, shapeAdj;
@@ -108,6 +111,96 @@ __device__ __forceinline__ void zero_tile(cx<T>* s) {
     for (int i = threadIdx.x; i < Tile<N>::ELEMS; i += blockDim.x) s[i] = mkc<T>(0, 0);
 }
 
+// The fitted plane at pixel (y, x) of the patch, as redux stores it: makePlane
+// (image/utils.cpp:128-147) with the constant dropped (fitPlane(..., subtract_mean = true),
+// object.cpp:588), centred at (ps/2, ps/2), rounded to float (Object::fittedPlane is float).
+__device__ __forceinline__ double plane_value(const double* pl, int ps, int y, int x) {
+    return (double)(float)(pl[0] * (double)(y - ps / 2) + pl[1] * (double)(x - ps / 2));
+}
+
+// ----------------------------------------------------------------------------------
+// FIT_PLANE: Object::fitAvgPlane (object.cpp:553-594).  The object's images (the patch
+// views of the cutouts at their current shifts) are averaged in float, in image order, and
+// divided by their count in float; a plane z = a dy + b dx + c (dy = y - ps/2, dx = x - ps/2)
+// is fitted to the mean image by least squares over every pixel (fitPlane, image/utils.cpp:
+// 169-233, there by GSL's multifit; here by the 3x3 normal equations in double) and a, b
+// kept.  One block per (patch, object); with full = 0 only objects with a re-initialised
+// image are refitted (Object::reInitialize, object.cpp:885-904).
+// ----------------------------------------------------------------------------------
+template <typename T, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_fit_plane(KParams<T> kp, int full) {
+    const int po = blockIdx.x;
+    const int p = po / kp.nObj, o = po % kp.nObj;
+    const int j0 = kp.objFirst[o], cnt = kp.objCount[o];
+    __shared__ double red[33];
+    __shared__ int any;
+    if (!full) {
+        if (threadIdx.x == 0) any = 0;
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += THREADS)
+            if (kp.reinit[(size_t)p * kp.I + j0 + k]) any = 1;
+        __syncthreads();
+        if (!any) return;
+    }
+    const int ps = kp.ps, cs = kp.cs;
+    double sz = 0, szy = 0, szx = 0;
+    for (int i = threadIdx.x; i < ps * ps; i += THREADS) {
+        const int y = i / ps, x = i % ps;
+        float acc = 0.f;
+        for (int k = 0; k < cnt; ++k) {
+            const size_t g = (size_t)p * kp.I + j0 + k;
+            const int oy = kp.margin + kp.shift[2 * g + 0], ox = kp.margin + kp.shift[2 * g + 1];
+            acc = __fadd_rn(acc, kp.cutouts[g * cs * cs + (size_t)(oy + y) * cs + ox + x]);
+        }
+        const double z = (double)__fdiv_rn(acc, (float)cnt);
+        sz += z;
+        szy += z * (double)(y - ps / 2);
+        szx += z * (double)(x - ps / 2);
+    }
+    const double tz = block_sum<THREADS>(sz, red);
+    const double tzy = block_sum<THREADS>(szy, red);
+    const double tzx = block_sum<THREADS>(szx, red);
+    if (threadIdx.x == 0) {
+        // normal equations over the full grid: dy and dx run over [-ps/2, ps - 1 - ps/2]
+        double s1 = 0, s2 = 0;
+        for (int v = 0; v < ps; ++v) {
+            const double d = (double)(v - ps / 2);
+            s1 += d;
+            s2 += d * d;
+        }
+        const double n = (double)ps;
+        // [ n s2  s1^2  n s1 ] [a]   [ tzy ]
+        // [ s1^2  n s2  n s1 ] [b] = [ tzx ]
+        // [ n s1  n s1  n^2  ] [c]   [ tz  ]
+        const double A[3][3] = {{n * s2, s1 * s1, n * s1}, {s1 * s1, n * s2, n * s1}, {n * s1, n * s1, n * n}};
+        const double rhs[3] = {tzy, tzx, tz};
+        auto det3 = [](const double m[3][3]) {
+            return m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                   m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+        };
+        const double d0 = det3(A);
+        double sol[2];
+        for (int c = 0; c < 2; ++c) {
+            double B[3][3];
+            for (int r = 0; r < 3; ++r)
+                for (int q = 0; q < 3; ++q) B[r][q] = (q == c) ? rhs[r] : A[r][q];
+            sol[c] = det3(B) / d0;
+        }
+        kp.plane[2 * (size_t)po + 0] = sol[0];
+        kp.plane[2 * (size_t)po + 1] = sol[1];
+    }
+}
+
+// od.img += fittedPlane after the restoration (object.cpp:410-413): objects [po][ps][ps].
+template <int UNUSED = 0>
+__global__ void k_add_plane(const double* plane, float* objects, int ps) {
+    const int po = blockIdx.x;
+    const double* pl = plane + 2 * (size_t)po;
+    float* ob = objects + (size_t)po * ps * ps;
+    for (int i = threadIdx.x; i < ps * ps; i += blockDim.x)
+        ob[i] = __fadd_rn(ob[i], (float)plane_value(pl, ps, i / ps, i % ps));
+}
+
 // ----------------------------------------------------------------------------------
 // Image preparation: SubImage::initialize (subimage.cpp:155-209) with getWindowedImg
 // (106-150) and the noise estimate FourierTransform::noise(-1,-1) (fouriertransform.cpp:
@@ -128,6 +221,13 @@ __global__ void __launch_bounds__(THREADS) k_prep(KParams<T> kp, int full) {
     const int oy = kp.margin + kp.shift[2 * g + 0];
     const int ox = kp.margin + kp.shift[2 * g + 1];
     const float* cut = kp.cutouts + (size_t)g * cs * cs;
+    // FIT_PLANE: getWindowedImg subtracts the object's fitted plane inside the window,
+    // (img - avg - plane) * window + avg (subimage.cpp:117-123)
+    const double* pl = kp.plane ? kp.plane + 2 * ((size_t)(g / kp.I) * kp.nObj + kp.imgObj[g % kp.I]) : nullptr;
+    auto windowed = [&](int y, int x, int i, double avg) {
+        const double v = (double)cut[(oy + y) * cs + ox + x] - avg;
+        return (pl ? v - plane_value(pl, ps, y, x) : v) * kp.window[i] + avg;
+    };
     // raw mean
     double sum = 0;
     for (int i = threadIdx.x; i < ps * ps; i += THREADS) {
@@ -139,7 +239,7 @@ __global__ void __launch_bounds__(THREADS) k_prep(KParams<T> kp, int full) {
     double s1 = 0, s2 = 0;
     for (int i = threadIdx.x; i < ps * ps; i += THREADS) {
         const int y = i / ps, x = i % ps;
-        const double w = ((double)cut[(oy + y) * cs + ox + x] - avg) * kp.window[i] + avg;
+        const double w = windowed(y, x, i, avg);
         s1 += w;
         s2 += w * w;
     }
@@ -151,7 +251,7 @@ __global__ void __launch_bounds__(THREADS) k_prep(KParams<T> kp, int full) {
         // noise estimate from (windowed - mean) * noiseWindow, un-centred transform
         for (int i = threadIdx.x; i < N * N; i += THREADS) {
             const int y = i / N, x = i % N;
-            const double w = ((double)cut[(oy + y) * cs + ox + x] - avg) * kp.window[i] + avg;
+            const double w = windowed(y, x, i, avg);
             s[y * LDS + x] = mkc<T>((T)((w - mean) * kp.noiseWindow[i]), 0);
         }
         __syncthreads();
@@ -185,7 +285,7 @@ __global__ void __launch_bounds__(THREADS) k_prep(KParams<T> kp, int full) {
     // the transform so that the large DC term does not swamp the other frequencies.
     for (int i = threadIdx.x; i < N * N; i += THREADS) {
         const int y = i / N, x = i % N;
-        const double w = ((double)cut[(oy + y) * cs + ox + x] - avg) * kp.window[i] + avg;
+        const double w = windowed(y, x, i, avg);
         s[y * LDS + x] = mkc<T>((T)(w - mean), 0);
     }
     __syncthreads();

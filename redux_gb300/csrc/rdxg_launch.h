@@ -53,6 +53,10 @@ constexpr int kAccumThreads = 256;
 constexpr int kCgThreads = 256;
 
 template <typename T> void launch_accum(const KParams<T>& kp, int nPo, cudaStream_t st);
+// FIT_PLANE: fit the planes of every (patch, object) (full) or of those with a re-initialised
+// image, and add them to the restored objects
+template <typename T> void launch_fit_plane(const KParams<T>& kp, int full, int nPo, cudaStream_t st);
+void launch_add_plane(const double* plane, float* objects, int nPo, int ps, cudaStream_t st);
 
 // fused evaluation (FP32, N <= 88): block size of k_eval and k_fd_half (a multiple of 32;
 // the transform stages stride over any size)

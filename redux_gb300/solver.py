@@ -107,6 +107,11 @@ class Solver:
     def set_stream(self, cuda_stream_ptr: int | None):
         self._check(_lib.load().rdxg_set_stream(self.h, C.c_void_p(cuda_stream_ptr or 0)), "rdxg_set_stream")
 
+    def set_fit_plane(self, enable: bool = True) -> None:
+        """FIT_PLANE: remove each object's fitted mean-image plane before windowing and add it
+        back to the restored objects (rdxg_set_fit_plane)."""
+        self._check(_lib.load().rdxg_set_fit_plane(self.h, int(bool(enable))), "rdxg_set_fit_plane")
+
     def set_patches(self, cutouts, residual_alpha=None, fixed_gamma=None):
         """cutouts: (P, I, cs, cs) float32 host array or an int device pointer with n_patches."""
         cut = np.ascontiguousarray(cutouts, np.float32)
