@@ -505,8 +505,22 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
         if (m < mc) {
             const T* Zm = kp.Z + (size_t)m * n2;
             T part = 0;
+            if constexpr (sizeof(T) == 4 && n2 % 4 == 0) {
+                // four pixels per load (v and every mode row start on 16-byte boundaries: the
+                // shared-memory offset of v and n2 * 4 bytes are multiples of 16), so each
+                // lane has a quarter of the loads of the scalar loop in flight at once
+                static_assert(((size_t)(Tile<N>::ELEMS + N) * sizeof(cx<T>)) % 16 == 0, "v is 16-byte aligned");
+                const float4* Z4 = reinterpret_cast<const float4*>(Zm);
+                const float4* v4 = reinterpret_cast<const float4*>(v);
+#pragma unroll 4
+                for (int q = lane; q < n2 / 4; q += 32) {
+                    const float4 z = __ldg(Z4 + q), w = v4[q];
+                    part += w.x * z.x + w.y * z.y + w.z * z.z + w.w * z.w;
+                }
+            } else {
 #pragma unroll 8
-            for (int q = lane; q < n2; q += 32) part += v[q] * Zm[q];
+                for (int q = lane; q < n2; q += 32) part += v[q] * Zm[q];
+            }
             acc = (double)part;
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
