@@ -531,6 +531,39 @@ def main():
                                           "reference's CG line search amplifies rounding along the trajectory "
                                           "(FP64 GPU vs FP64 CPU: <5e-6 after 100 iterations, 1e-4 after 400)"}
         s64.close()
+        # converged solves with the reference's default settings (MODE_START 5, MODE_STEP 5,
+        # MIN_ITER 5, MAX_ITER 500, N_DONE_ITER 3, FTOL 1e-3: staged modes, re-shifts between
+        # stages, per-patch stop), the batch against the plain FP64 form on a sample
+        conv = S.SolveSettings(max_metrics=4096)
+        solver.set_patches_device(P, cut_dev.data_ptr())
+        solver.run(conv)                                   # warm-up (graph capture)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        solver.set_patches_device(P, cut_dev.data_ptr())
+        rc = solver.run(conv)
+        torch.cuda.synchronize()
+        t_conv = time.perf_counter() - t0
+        s64 = S.Solver(job, max_patches=1, precision="fp64", device=local)
+        t64, sr = 0.0, []
+        for p in range(nplain):
+            s64.set_patches(cut[p:p + 1])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r64 = s64.run(conv)
+            torch.cuda.synchronize()
+            t64 += time.perf_counter() - t0
+            b = r64["reports"][0].final_metric
+            sr.append((rc["reports"][p].final_metric - b) / abs(b))
+        s64.close()
+        line["converged_reference_settings"] = {
+            "value": world * P / t_conv, "unit": UNIT,
+            "settings": "MODE_START 5, MODE_STEP 5, MIN_ITER 5, MAX_ITER 500, N_DONE_ITER 3, FTOL 1e-3",
+            "iterations_median": float(np.median([r.iterations for r in rc["reports"]])),
+            "evaluations_per_patch": float(np.mean([r.n_f_evals + r.n_df_evals for r in rc["reports"]])),
+            "plain_fp64_gpu": {"value": nplain / t64, "unit": UNIT, "sample": f"{nplain} patches, per-patch launches"},
+            "speedup_chosen_vs_plain": P / t_conv / (nplain / t64),
+            "final_metric_signed_rel_vs_fp64": sr,
+            "within_1e-5": sum(1 for x in sr if abs(x) <= 1e-5)}
         # CPU baseline: the FP64 restatement on all host cores, one patch
         threads = os.cpu_count() or 1
         tc, finals_cpu = cpu_port(job, cut, args.iterations, threads, 1)

@@ -772,6 +772,17 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
     if (at && atoi(at) == 0) h->tune = 0;   // default shapes, no measurement
     const char* nf = getenv("RDXG_NO_FUSED");
     if (!r && !(nf && atoi(nf))) r = setup_fused(h, s);
+    // RDXG_SHAPES="eval,forward,adjoint" (threads per block, 0 = default) pins the launch
+    // shapes, e.g. for profiling runs, where the planner's timing would be distorted
+    const char* shp = getenv("RDXG_SHAPES");
+    if (!r && shp) {
+        rdxg_launch_shape ls{};
+        if (sscanf(shp, "%d,%d,%d", &ls.eval_threads, &ls.forward_threads, &ls.adjoint_threads) == 3) {
+            if (ls.eval_threads && !h->fused) ls.eval_threads = 0;
+            if (ls.forward_threads && h->fused) ls.forward_threads = 0;
+            r = rdxg_set_launch_shape(h, &ls);
+        }
+    }
     *out = h;
     return r;
 }
