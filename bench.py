@@ -7,9 +7,11 @@ seeded synthetic data.  One step = one complete solve of the batch: image prepar
 (windowing, transforms, noise, regularisation) and 100 iterations of the reference's
 conjugate-gradient/line-search for every patch.
 
-value: patches/s with the cutouts resident in HBM (set_patches_device + solve).
-e2e:   patches/s through the public API from pinned host memory (cutouts H2D, solve,
-       coefficients/reports/metric histories D2H), per step.
+value: patches/s with the cutouts resident in HBM: the batch split over three handles, each
+       on its own stream (rdxg_set_patches_device per handle, then rdxg_solve_many: one CUDA
+       graph, a branch per handle).
+e2e:   patches/s through the public API from pinned host memory (cutouts H2D per handle,
+       rdxg_solve_many, coefficients/reports/metric histories D2H), per step.
 --impl reference: the reference's CPU path timed on the host cores -- redux itself does not
        build here (Boost, FFTW3, GSL, OpenCV missing), so its FP64 restatement (oracle/) is
        timed with all host threads on a bounded sample (one patch, same settings).
@@ -349,6 +351,8 @@ def main():
     ap.add_argument("--frames", type=int, default=12)
     ap.add_argument("--iterations", type=int, default=100)
     ap.add_argument("--no-baselines", action="store_true")
+    ap.add_argument("--handles", type=int, default=3,
+                    help="handles (each on its own stream) the batch is split over, solved together")
     ap.add_argument("--config", type=int, default=2,
                     help="2: the headline batch; 3: the uneven batch; 4: large patches (128 x 128, 100 modes)")
     ap.add_argument("--levels", type=int, default=3,
@@ -384,10 +388,8 @@ def main():
     job, cut = workload(args.patches, args.frames, args.iterations)
     P = cut.shape[0]
     settings = S.fixed_iterations(job.n_modes, args.iterations, max_metrics=args.iterations + 8)
-    solver = S.Solver(job, max_patches=P, device=local)
-    stream = torch.cuda.Stream()
-    solver.set_stream(stream.cuda_stream)
     if args.kernels_only:
+        solver = S.Solver(job, max_patches=P, device=local)
         solver.set_patches(cut)
         tuned = solver.autotune(reps=3)     # the shapes a solve would use
         kt = solver.profile_kernels(reps=1)
@@ -395,14 +397,37 @@ def main():
         print(json.dumps({"kernel_ms": kt, "patches": P, "launch_shapes": tuned}), flush=True)
         solver.close()
         return
+    # the batch split over H handles, each on its own stream, solved together (one CUDA graph,
+    # a branch per handle): one handle's latency-bound kernels of a round overlap the tail of
+    # another's evaluation (measured: 1 handle 780 ms, 2: 765, 3: 758, 4: 766, 6: 795 ms)
+    H = max(1, min(args.handles, P))
+    bounds = [int(round(P * k / H)) for k in range(H + 1)]
+    parts = [(bounds[k], bounds[k + 1]) for k in range(H)]
+    solvers, streams = [], []
+    for b0, b1 in parts:
+        sk = S.Solver(job, max_patches=b1 - b0, device=local)
+        st = torch.cuda.Stream()
+        sk.set_stream(st.cuda_stream)
+        solvers.append(sk)
+        streams.append(st)
+    stream = streams[0]           # the graph runs on the first handle's stream
     cut_dev = torch.from_numpy(cut).to(f"cuda:{local}")
     cut_pin = torch.from_numpy(cut).pin_memory()
     cut_pin_np = cut_pin.numpy()
     torch.cuda.synchronize()
 
+    def load_device():
+        for sk, (b0, b1) in zip(solvers, parts):
+            sk.set_patches_device(b1 - b0, cut_dev[b0:b1].data_ptr())
+
     def step_device():
-        solver.set_patches_device(P, cut_dev.data_ptr())
-        solver.run_async(settings)
+        load_device()
+        S.solve_many(solvers, settings, fetch=False)
+
+    def fetch_all(max_metrics):
+        outs = [sk.fetch(max_metrics) for sk in solvers]
+        return dict(alpha=np.concatenate([o["alpha"] for o in outs]),
+                    reports=[r for o in outs for r in o["reports"]])
 
     def barrier():
         if dist is not None:
@@ -419,12 +444,13 @@ def main():
         e0.record(stream)
         for _ in range(args.steps):
             step_device()
-            launches += solver.launch_count() + 1
+            launches += sum(sk.launch_count() for sk in solvers) + H   # + one preparation each
         e1.record(stream)
         e1.synchronize()
         barrier()
         ms_dev = e0.elapsed_time(e1) / args.steps
-    out = solver.fetch(settings.max_metrics)
+    rounds = solvers[0].launch_count() / 6.0
+    out = fetch_all(settings.max_metrics)
     reps = out["reports"]
     iters = [r.iterations for r in reps]
     nf = sum(r.n_f_evals for r in reps) / P
@@ -436,8 +462,9 @@ def main():
     for _ in range(args.steps):
         barrier()
         t0 = time.perf_counter()
-        solver.set_patches(cut_pin_np)
-        r = solver.run(settings)
+        for sk, (b0, b1) in zip(solvers, parts):
+            sk.set_patches(cut_pin_np[b0:b1])
+        S.solve_many(solvers, settings)
         torch.cuda.synchronize()
         ms_e2e.append((time.perf_counter() - t0) * 1000.0)
     e2e_ms = statistics.median(ms_e2e)
@@ -449,7 +476,10 @@ def main():
     value = world * P / (ms_dev / 1000.0)
     e2e_value = world * P / (e2e_ms / 1000.0)
 
-    # roofline of the dominant kernel, measured on the same batch
+    # roofline of the dominant kernel, measured on the whole batch in one handle
+    solver = S.Solver(job, max_patches=P, device=local)
+    solver.set_patches_device(P, cut_dev.data_ptr())
+    solver.autotune(reps=3)
     kt = solver.profile_kernels(reps=5)
     peaks = _peaks()
     N, n, M = job.otf_size, job.pupil_pixels, job.n_modes
@@ -464,7 +494,6 @@ def main():
     }
     # time share per step: forward and accumulation run every round, the adjoint only does
     # work in rounds where a patch needs a gradient (about one in ten)
-    rounds = launches / max(1, args.steps) / 6.0
     share = {"forward": rounds * kt["forward"], "accum": rounds * kt["accum"], "adjoint": ndf * kt["adjoint"]}
     dom = max(share, key=share.get)
     achieved = per_launch[dom]["bytes"] / (kt[dom] / 1000.0) / 1e9
@@ -492,12 +521,13 @@ def main():
             "config": {"workload": f"{P} patches 88x88, 36 KL modes, 3ch x {args.frames} frames, D/r0=15, "
                                    f"{args.iterations} CG iterations, all modes at once",
                        "patches_per_gpu": P, "iterations": args.iterations,
+                       "handles": H, "handle_patches": [b1 - b0 for b0, b1 in parts],
                        "l2": "inputs larger than L2 (D, OTF: 2 x 500 MB per batch)",
                        "metric_evals_per_patch": nf, "gradient_evals_per_patch": ndf,
                        "cg_iterations_per_s": world * P * args.iterations / (ms_dev / 1000.0)},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches), "roofline": roofline, "clocks": clk.summary(),
-            "launch_shapes": solver.launch_shape()}
+            "launch_shapes": solvers[0].launch_shape()}
 
     if rank == 0 and not args.no_baselines:
         # plain FP64 GPU form: same algorithm in double precision, one patch per launch sequence
@@ -541,14 +571,15 @@ def main():
         # MIN_ITER 5, MAX_ITER 500, N_DONE_ITER 3, FTOL 1e-3: staged modes, re-shifts between
         # stages, per-patch stop), the batch against the plain FP64 form on a sample
         conv = S.SolveSettings(max_metrics=4096)
-        solver.set_patches_device(P, cut_dev.data_ptr())
-        solver.run(conv)                                   # warm-up (graph capture)
+        load_device()
+        S.solve_many(solvers, conv, fetch=False)           # warm-up (graph capture)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        solver.set_patches_device(P, cut_dev.data_ptr())
-        rc = solver.run(conv)
+        load_device()
+        S.solve_many(solvers, conv, fetch=False)
         torch.cuda.synchronize()
         t_conv = time.perf_counter() - t0
+        rc = fetch_all(conv.max_metrics)
         s64 = S.Solver(job, max_patches=1, precision="fp64", device=local)
         t64, sr = 0.0, []
         for p in range(nplain):
@@ -580,6 +611,8 @@ def main():
     if rank == 0:
         print(json.dumps(line), flush=True)
     solver.close()
+    for sk in solvers:
+        sk.close()
     if dist is not None:
         dist.destroy_process_group()
 

@@ -270,9 +270,11 @@ class Solver:
         return out
 
 
-def solve_many(solvers, settings: SolveSettings):
+def solve_many(solvers, settings: SolveSettings, fetch: bool = True):
     """Solver::run for the loaded patches of several handles (e.g. one per geometry of an
-    uneven batch) in one CUDA graph (rdxg_solve_many); returns each handle's results."""
+    uneven batch, or one batch split over handles on their own streams) in one CUDA graph
+    (rdxg_solve_many); returns each handle's results (None with fetch=False: they stay on
+    the device for Solver.fetch)."""
     L = _lib.load()
     hs = (C.c_void_p * len(solvers))(*[s.h for s in solvers])
     prm = settings.to_c()
@@ -280,7 +282,7 @@ def solve_many(solvers, settings: SolveSettings):
     if r != _lib.RDXG_OK:
         msgs = "; ".join(L.rdxg_last_error(s.h).decode() for s in solvers)
         raise SolverError(f"rdxg_solve_many failed with status {r}: {msgs}")
-    return [s.fetch(settings.max_metrics) for s in solvers]
+    return [s.fetch(settings.max_metrics) for s in solvers] if fetch else None
 
 
 def cg_minimize(n_free: int, n_modes: int, settings: SolveSettings, grad_scale: float, f, df, shift=None):
