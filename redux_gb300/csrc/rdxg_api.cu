@@ -1591,6 +1591,10 @@ int rdxg_set_launch_shape(rdxg_solver* h, const rdxg_launch_shape* shape) {
     const int32_t want[3] = {shape->eval_threads, shape->forward_threads, shape->adjoint_threads};
     for (int f = 0; f < 3; ++f) {
         if (want[f] == 0) continue;
+        if (threads_of(h, f, 0) == 0) {
+            h->err = std::string(f == 0 ? "k_eval" : "k_forward") + " is not used on this handle's path";
+            return RDXG_ERR_ARG;
+        }
         if (want[f] == threads_of(h, f, 0)) v[f] = 0;
         else if (want[f] == threads_of(h, f, 1)) v[f] = 1;
         else {

@@ -77,6 +77,8 @@ def test_autotune_reports_the_candidates(case):
     assert r["shape"][untuned] == 0 and r["ms"][untuned] == [0.0, 0.0], r
     with pytest.raises(S.SolverError, match="not compiled"):
         s.set_launch_shape(adjoint_threads=300)
+    with pytest.raises(S.SolverError, match="not used on this handle's path"):
+        s.set_launch_shape(**{untuned + "_threads": 512})
     s.close()
 
 
