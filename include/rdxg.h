@@ -135,6 +135,15 @@ int rdxg_set_patches(rdxg_solver* h, int32_t n_patches, const float* cutouts,
 int rdxg_set_patches_device(rdxg_solver* h, int32_t n_patches, const float* d_cutouts,
                             const double* residual_alpha, const double* fixed_gamma);
 
+/* Warm start (INIT_FILES): the initial mode coefficients [P][I][M] of the loaded patches,
+ * the alpha_offset that Solver::loadInit fills from ObjectData::alpha (solver.cpp:412,
+ * 726-733; Object::getInit, object.cpp:446-456), or NULL to start at zero.  As
+ * Solver::shiftAndInit(alpha_offset, true) (solver.cpp:413, 584-605) the patches are prepared
+ * again with every image's window shifted by the integer part of its initial tilt
+ * (SubImage::adjustShifts, subimage.cpp:444-480), and every following solve starts from these
+ * coefficients.  Call after rdxg_set_patches / rdxg_set_patches_device (which start at zero). */
+int rdxg_set_initial_alpha(rdxg_solver* h, const double* alpha);
+
 /* Metric of every patch at alpha [P][I][M] (Solver::applyAlpha + Solver::metric,
  * solver.cpp:219-225, 763-817).  metric: [P]. */
 int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric);

@@ -51,6 +51,7 @@ struct PatchData {
     std::vector<float> cutouts;          // [I][cutout][cutout] channel images with margins
     std::vector<double> residualAlpha;   // [I][2] (y, x) residual tilt, or empty
     std::vector<double> fixedGamma;      // [nObj] fixed regularisation, or empty
+    std::vector<double> initAlpha;       // [I][M] initial coefficients (INIT_FILES), or empty
     // results
     std::vector<double> alpha;           // [I][M] mode coefficients (waveFronts.alpha)
     std::vector<double> metrics;         // metric history (PatchData::metrics)
@@ -106,6 +107,14 @@ public:
         }
         check(rdxg_set_patches(h_, P, cut.data(), haveRes ? res.data() : nullptr, haveGam ? gam.data() : nullptr),
               "rdxg_set_patches");
+        if (!batch[0]->initAlpha.empty()) {      // Solver::loadInit: a warm start for the batch
+            std::vector<double> init(P * I * M);
+            for (int p = 0; p < P; ++p) {
+                if (batch[p]->initAlpha.size() != I * M) throw std::runtime_error("rdxg::Solver::run: initAlpha size mismatch");
+                std::copy(batch[p]->initAlpha.begin(), batch[p]->initAlpha.end(), init.begin() + p * I * M);
+            }
+            check(rdxg_set_initial_alpha(h_, init.data()), "rdxg_set_initial_alpha");
+        }
         rdxg_solve_params prm{};
         prm.mode_start = set_.modeStart;
         prm.mode_step = set_.modeStep;

@@ -82,6 +82,7 @@ def lib():
         L.orc_restore.restype = C.c_int
         L.orc_restore.argtypes = [C.c_void_p, f64p, f64p, C.c_int, f64p]
         L.orc_set_fit_plane.argtypes = [C.c_void_p, C.c_int]
+        L.orc_set_initial_alpha.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_get_plane.argtypes = [C.c_void_p, f32p]
         _LIB = L
     return _LIB
@@ -172,6 +173,15 @@ class OraclePatch:
     def set_fit_plane(self, on=True):
         """RF_FIT_PLANE: fit and remove each object's mean-image plane (call before set_images)."""
         lib().orc_set_fit_plane(self.h, int(bool(on)))
+
+    def set_initial_alpha(self, alpha=None):
+        """Warm start (INIT_FILES): the initial coefficients [I][M] (None: start at zero); the
+        next set_images shifts the cutouts by their tilts, solve starts from them."""
+        if alpha is None:
+            lib().orc_set_initial_alpha(self.h, None)
+            return
+        self._init = np.ascontiguousarray(alpha, np.float64).ravel()
+        lib().orc_set_initial_alpha(self.h, self._init.ctypes.data)
 
     def plane(self):
         """The fitted planes [nObj][ps][ps] (float32)."""

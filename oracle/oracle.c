@@ -312,6 +312,9 @@ typedef struct {
     /* FIT_PLANE (RF_FIT_PLANE): the fitted plane of each object, float values as
      * Object::fittedPlane, nObj * ps * ps; NULL when off */
     float* plane;
+    /* warm start (INIT_FILES): the initial coefficients Solver::loadInit puts in alpha_offset
+     * (solver.cpp:412, 726-733), nPar; NULL for a start at zero */
+    double* initAlpha;
     /* object work */
     cplx* P; double* Q; cplx* PQ; double* PS; double* QS; /* nObj*N2 */
     double* objMetric;
@@ -469,7 +472,7 @@ void orc_destroy(orc_patch* p) {
     free(p->nsRow); free(p->nsCol); free(p->nsVal);
     free(p->cutouts); free(p->phiChannel); free(p->otfNorm); free(p->curShift);
     free(p->curTiltOffset); free(p->statMean); free(p->statStd); free(p->statNoise);
-    free(p->D); free(p->ftSum); free(p->regGamma); free(p->fixedGamma); free(p->plane);
+    free(p->D); free(p->ftSum); free(p->regGamma); free(p->fixedGamma); free(p->plane); free(p->initAlpha);
     free(p->P); free(p->Q); free(p->PQ); free(p->PS); free(p->QS); free(p->objMetric);
     free(p->OTF); free(p->PF); free(p->PHI);
     free(p->alpha); free(p->alphaOffset); free(p->gradAlpha); free(p->enabled);
@@ -636,6 +639,14 @@ void orc_set_fit_plane(orc_patch* p, int on) {
     if (!on && p->plane) { free(p->plane); p->plane = NULL; }
 }
 
+static int adjust_shifts(orc_patch* p, int j, const double* a);   /* SubImage::adjustShifts, below */
+
+void orc_set_initial_alpha(orc_patch* p, const double* a) {
+    if (!a) { free(p->initAlpha); p->initAlpha = NULL; return; }
+    if (!p->initAlpha) p->initAlpha = (double*)xcalloc((size_t)p->nPar, sizeof(double));
+    memcpy(p->initAlpha, a, sizeof(double) * (size_t)p->nPar);
+}
+
 void orc_get_plane(const orc_patch* p, float* out) {
     if (p->plane) memcpy(out, p->plane, sizeof(float) * (size_t)p->nObj * p->ps * p->ps);
 }
@@ -716,6 +727,10 @@ void orc_set_images(orc_patch* p, const float* cutouts, const double* residual_a
         p->curShift[2 * j] = p->curShift[2 * j + 1] = 0;
         p->curTiltOffset[2 * j] = p->curTiltOffset[2 * j + 1] = 0;
     }
+    /* Solver::shiftAndInit(alpha_offset, true) after loadInit: the cutout windows follow the
+     * tilts of the initial coefficients (SubImage::adjustShifts) before the images are set up */
+    if (p->initAlpha)
+        for (int j = 0; j < p->nImg; ++j) adjust_shifts(p, j, p->initAlpha + (long)j * p->M);
     compute_otf_norms(p);
     p->fixed_gamma = fixed_gamma != NULL;
     if (fixed_gamma) memcpy(p->fixedGamma, fixed_gamma, sizeof(double) * (size_t)p->nObj);
@@ -1293,7 +1308,8 @@ int orc_solve(orc_patch* p, const orc_cfg* cfg, double* alpha_out, orc_report* r
     p->n_f = p->n_df = 0;
     memset(p->alpha, 0, sizeof(double) * (size_t)nPar);
     memset(p->gradAlpha, 0, sizeof(double) * (size_t)nPar);
-    memset(p->alphaOffset, 0, sizeof(double) * (size_t)nPar);
+    if (p->initAlpha) memcpy(p->alphaOffset, p->initAlpha, sizeof(double) * (size_t)nPar);
+    else memset(p->alphaOffset, 0, sizeof(double) * (size_t)nPar);
     cg_state st;
     memset(&st, 0, sizeof(st));
     st.n = nFree;
@@ -1311,8 +1327,8 @@ int orc_solve(orc_patch* p, const orc_cfg* cfg, double* alpha_out, orc_report* r
     double tol = 1.0E-1;
     int failCount = 0, totalIterations = 0, maxIterations = 10, maxFails = 3;
     int status = 0;
-    /* loadInit: alpha_offset = 0 (no init file); shiftAndInit(alpha_offset, true) was done
-     * by orc_set_images. */
+    /* loadInit: alpha_offset = the initial coefficients (zero without them);
+     * shiftAndInit(alpha_offset, true) was done by orc_set_images. */
     double initialMetric = my_f(&c, beta_init);
     push_metric(&c, initialMetric);
     const double nTotalPixels = (double)p->nImg * p->ps * p->ps;

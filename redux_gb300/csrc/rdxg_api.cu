@@ -104,6 +104,9 @@ struct rdxg_solver {
     // FIT_PLANE: the fitted plane of every (patch, object), slopes along y and x
     bool fitPlane = false;
     double* dPlane = nullptr;
+    // warm start: the initial coefficients of the loaded patches [P][I][M] (loadInit)
+    bool haveInit = false;
+    double* dInitAlpha = nullptr;
 };
 
 namespace {
@@ -416,12 +419,35 @@ int build_nullspace(rdxg_solver* h, const rdxg_static* s) {
     return RDXG_OK;
 }
 
-// (re)initialise the loaded patches: shifts 0, full image preparation, gamma
+// Arguments of the re-shift kernel (SubImage::adjustShifts of patches that request it).
+ShiftArgs make_shift_args(rdxg_solver* h) {
+    ShiftArgs sa{};
+    sa.P = h->P; sa.I = h->I; sa.M = h->M; sa.nObj = h->nObj; sa.ps = h->ps; sa.cs = h->cs; sa.margin = h->margin;
+    sa.tiltX = h->haveJ ? h->geo.tilt_x : -1; sa.tiltY = h->haveJ ? h->geo.tilt_y : -1;
+    sa.req = h->dReq; sa.alpha = h->dAlpha; sa.tiltOff = h->dCurTilt; sa.shift = h->dShift;
+    sa.reinit = h->dReinit; sa.imgObj = h->dImgObj; sa.aux = h->fused ? h->dAux : nullptr;
+    std::memcpy(sa.J, h->J, sizeof(sa.J));
+    std::memcpy(sa.Jinv, h->Jinv, sizeof(sa.Jinv));
+    return sa;
+}
+
+// (re)initialise the loaded patches: shifts 0 (or those of the initial coefficients), full
+// image preparation, gamma
 int prepare_patches(rdxg_solver* h) {
     const size_t G = (size_t)h->P * h->I;
     CK(h, cudaMemsetAsync(h->dShift, 0, G * 2 * sizeof(int32_t), h->stream));
     CK(h, cudaMemsetAsync(h->dCurTilt, 0, G * 2 * sizeof(double), h->stream));
     CK(h, cudaMemcpyAsync(h->dResAlpha, h->hResAlpha.data(), G * 2 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (h->haveInit) {
+        // Solver::shiftAndInit(alpha_offset, true) after loadInit (solver.cpp:412-413): every
+        // image's window follows the tilts of the initial coefficients (SubImage::adjustShifts)
+        CK(h, cudaMemcpyAsync(h->dAlpha, h->dInitAlpha, G * h->M * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+        const std::vector<int32_t> shiftReq(h->P, REQ_SHIFT);
+        CK(h, cudaMemcpyAsync(h->dReq, shiftReq.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+        launch_shift(make_shift_args(h), h->P, h->stream);
+        h->launches++;
+        CKL(h);
+    }
     int rc = RDXG_OK;
     with_size(h->N, h->fp64, [&](auto L, auto t) {
         using T = decltype(t);
@@ -455,6 +481,7 @@ int prepare_patches(rdxg_solver* h) {
 int set_patches_common(rdxg_solver* h, int32_t P, const double* residual_alpha, const double* fixed_gamma) {
     if (P < 1 || P > h->Pmax) { h->err = "n_patches out of range"; return RDXG_ERR_ARG; }
     h->P = P;
+    h->haveInit = false;     // a new batch starts at zero unless rdxg_set_initial_alpha follows
     const size_t G = (size_t)P * h->I;
     h->hResAlpha.assign(G * 2, 0.0);
     if (residual_alpha) std::memcpy(h->hResAlpha.data(), residual_alpha, G * 2 * sizeof(double));
@@ -808,6 +835,21 @@ int rdxg_set_fit_plane(rdxg_solver* h, int32_t enable) {
     return h->loaded ? prepare_patches(h) : RDXG_OK;
 }
 
+int rdxg_set_initial_alpha(rdxg_solver* h, const double* alpha) {
+    if (!h) return RDXG_ERR_ARG;
+    if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
+    if (alpha) {
+        if (!h->dInitAlpha) {
+            const int r = dalloc_t(h, &h->dInitAlpha, (size_t)h->Pmax * h->nPar);
+            if (r) return r;
+        }
+        CK(h, cudaMemcpyAsync(h->dInitAlpha, alpha, (size_t)h->P * h->nPar * sizeof(double), cudaMemcpyHostToDevice,
+                              h->stream));
+    }
+    h->haveInit = alpha != nullptr;
+    return prepare_patches(h);
+}
+
 int rdxg_set_stream(rdxg_solver* h, void* st) {
     if (!h) return RDXG_ERR_ARG;
     h->stream = st ? (cudaStream_t)st : h->own;
@@ -1102,14 +1144,10 @@ int prepare_solve(rdxg_solver* h, const rdxg_solve_params* s, SolvePlan& pl) {
         CK(h, cudaMemsetAsync(h->dOh, 0, (size_t)P * h->nObj * h->nH * sizeof(float2), h->stream));
         CK(h, cudaMemsetAsync(h->dAux, 0, (size_t)P * 2 * sizeof(int32_t), h->stream));
     }
-    ShiftArgs& sa = pl.sa;
-    sa = ShiftArgs{};
-    sa.P = P; sa.I = h->I; sa.M = h->M; sa.nObj = h->nObj; sa.ps = h->ps; sa.cs = h->cs; sa.margin = h->margin;
-    sa.tiltX = h->haveJ ? h->geo.tilt_x : -1; sa.tiltY = h->haveJ ? h->geo.tilt_y : -1;
-    sa.req = h->dReq; sa.alpha = h->dAlpha; sa.tiltOff = h->dCurTilt; sa.shift = h->dShift;
-    sa.reinit = h->dReinit; sa.imgObj = h->dImgObj; sa.aux = h->fused ? h->dAux : nullptr;
-    std::memcpy(sa.J, h->J, sizeof(sa.J));
-    std::memcpy(sa.Jinv, h->Jinv, sizeof(sa.Jinv));
+    if (h->haveInit)   // alpha_offset = the initial coefficients
+        CK(h, cudaMemcpyAsync(h->dAlphaOff, h->dInitAlpha, (size_t)P * h->nPar * sizeof(double),
+                              cudaMemcpyDeviceToDevice, h->stream));
+    pl.sa = make_shift_args(h);
     return RDXG_OK;
 }
 

@@ -129,6 +129,15 @@ class Solver:
                                                         _lib.ptr(fg)), "rdxg_set_patches_device")
         self.P = n_patches
 
+    def set_initial_alpha(self, alpha=None) -> None:
+        """Warm start: initial coefficients [P][I][M] of the loaded patches (None: zero); the
+        images are re-cut by their tilts and every following solve starts there."""
+        if alpha is None:
+            self._check(_lib.load().rdxg_set_initial_alpha(self.h, None), "rdxg_set_initial_alpha")
+            return
+        a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
+        self._check(_lib.load().rdxg_set_initial_alpha(self.h, _lib.ptr(a)), "rdxg_set_initial_alpha")
+
     def metric(self, alpha) -> np.ndarray:
         a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
         out = np.zeros(self.P)
