@@ -144,6 +144,14 @@ int rdxg_set_patches_device(rdxg_solver* h, int32_t n_patches, const float* d_cu
  * coefficients.  Call after rdxg_set_patches / rdxg_set_patches_device (which start at zero). */
 int rdxg_set_initial_alpha(rdxg_solver* h, const double* alpha);
 
+/* REG_ALPHA: weights [I][M] (the same for every patch) of the regularisation term
+ * 0.5 sum alpha^2 w that Solver::metric adds to the metric (solver.cpp:804-811), the
+ * reference's Solver::regAlphaWeights = REG_ALPHA / wavelength * nTotalPixels / atm_rms^2
+ * (solver.cpp:147-156); NULL turns it off (REG_ALPHA = 0, the default).  As in
+ * Solver::gradient (solver.cpp:860-885) the gradient starts from alpha * w and the enabled
+ * modes are then assigned the data term, so alpha * w remains for the modes not yet enabled. */
+int rdxg_set_reg_alpha(rdxg_solver* h, const double* weights);
+
 /* Metric of every patch at alpha [P][I][M] (Solver::applyAlpha + Solver::metric,
  * solver.cpp:219-225, 763-817).  metric: [P]. */
 int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric);

@@ -41,6 +41,7 @@ struct Settings {
     bool restore = true;            // restore the objects after the solve
     bool noFilter = false;          // RF_NO_FILTER
     bool fitPlane = false;          // RF_FIT_PLANE
+    std::vector<double> regAlphaWeights;   // [I][M] Solver::regAlphaWeights, empty for REG_ALPHA = 0
     // further outputs of the restoration (Object::saveMask): RDXG_RESTORE_PSF,
     // RDXG_RESTORE_PSF_AVG, RDXG_RESTORE_COBJ, RDXG_RESTORE_RESIDUAL
     int32_t saveMask = 0;
@@ -73,6 +74,11 @@ public:
         : geo_(geometry), set_(settings), fc_(std::move(frequencyCutoff)) {
         check(rdxg_create(&geo_, &statics, &h_), "rdxg_create");
         if (set_.fitPlane) check(rdxg_set_fit_plane(h_, 1), "rdxg_set_fit_plane");
+        if (!set_.regAlphaWeights.empty()) {
+            if (set_.regAlphaWeights.size() != (size_t)geo_.n_images * geo_.n_modes)
+                throw std::runtime_error("rdxg::Solver: regAlphaWeights size mismatch");
+            check(rdxg_set_reg_alpha(h_, set_.regAlphaWeights.data()), "rdxg_set_reg_alpha");
+        }
         if ((int)fc_.size() != geo_.n_objects) fc_.assign(geo_.n_objects, geo_.otf_size / 2.0);
         alpha.assign((size_t)geo_.n_images * geo_.n_modes, 0.0);
     }

@@ -83,6 +83,7 @@ def lib():
         L.orc_restore.argtypes = [C.c_void_p, f64p, f64p, C.c_int, f64p]
         L.orc_set_fit_plane.argtypes = [C.c_void_p, C.c_int]
         L.orc_set_initial_alpha.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_set_reg_alpha.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_get_plane.argtypes = [C.c_void_p, f32p]
         _LIB = L
     return _LIB
@@ -182,6 +183,14 @@ class OraclePatch:
             return
         self._init = np.ascontiguousarray(alpha, np.float64).ravel()
         lib().orc_set_initial_alpha(self.h, self._init.ctypes.data)
+
+    def set_reg_alpha(self, weights=None):
+        """REG_ALPHA: the per-parameter weights [I][M] of 0.5 sum alpha^2 w (None: off)."""
+        if weights is None:
+            lib().orc_set_reg_alpha(self.h, None)
+            return
+        self._regw = np.ascontiguousarray(weights, np.float64).ravel()
+        lib().orc_set_reg_alpha(self.h, self._regw.ctypes.data)
 
     def plane(self):
         """The fitted planes [nObj][ps][ps] (float32)."""

@@ -315,6 +315,8 @@ typedef struct {
     /* warm start (INIT_FILES): the initial coefficients Solver::loadInit puts in alpha_offset
      * (solver.cpp:412, 726-733), nPar; NULL for a start at zero */
     double* initAlpha;
+    /* REG_ALPHA: Solver::regAlphaWeights (solver.cpp:147-156), nPar; NULL when REG_ALPHA = 0 */
+    double* regW;
     /* object work */
     cplx* P; double* Q; cplx* PQ; double* PS; double* QS; /* nObj*N2 */
     double* objMetric;
@@ -472,7 +474,7 @@ void orc_destroy(orc_patch* p) {
     free(p->nsRow); free(p->nsCol); free(p->nsVal);
     free(p->cutouts); free(p->phiChannel); free(p->otfNorm); free(p->curShift);
     free(p->curTiltOffset); free(p->statMean); free(p->statStd); free(p->statNoise);
-    free(p->D); free(p->ftSum); free(p->regGamma); free(p->fixedGamma); free(p->plane); free(p->initAlpha);
+    free(p->D); free(p->ftSum); free(p->regGamma); free(p->fixedGamma); free(p->plane); free(p->initAlpha); free(p->regW);
     free(p->P); free(p->Q); free(p->PQ); free(p->PS); free(p->QS); free(p->objMetric);
     free(p->OTF); free(p->PF); free(p->PHI);
     free(p->alpha); free(p->alphaOffset); free(p->gradAlpha); free(p->enabled);
@@ -641,6 +643,12 @@ void orc_set_fit_plane(orc_patch* p, int on) {
 
 static int adjust_shifts(orc_patch* p, int j, const double* a);   /* SubImage::adjustShifts, below */
 
+void orc_set_reg_alpha(orc_patch* p, const double* w) {
+    if (!w) { free(p->regW); p->regW = NULL; return; }
+    if (!p->regW) p->regW = (double*)xcalloc((size_t)p->nPar, sizeof(double));
+    memcpy(p->regW, w, sizeof(double) * (size_t)p->nPar);
+}
+
 void orc_set_initial_alpha(orc_patch* p, const double* a) {
     if (!a) { free(p->initAlpha); p->initAlpha = NULL; return; }
     if (!p->initAlpha) p->initAlpha = (double*)xcalloc((size_t)p->nPar, sizeof(double));
@@ -756,6 +764,7 @@ void orc_set_images(orc_patch* p, const float* cutouts, const double* residual_a
 /* ---------------- forward: applyAlpha + metric ---------------- */
 
 static void apply_alpha(orc_patch* p, const double* alpha) {
+    if (alpha != p->alpha) memcpy(p->alpha, alpha, sizeof(double) * (size_t)p->nPar);   /* Solver::alpha */
 #pragma omp parallel for schedule(dynamic, 1) num_threads(p->nthreads)
     for (int j = 0; j < p->nImg; ++j) {
         img_scratch* s = &p->scr[j];
@@ -823,6 +832,8 @@ static double calc_metric(orc_patch* p) {
         p->objMetric[o] = m;
         sum += p->objWeight[o] * m;
     }
+    if (p->regW)      /* Solver::metric: + 0.5 sum alpha^2 w (solver.cpp:804-811) */
+        for (int i = 0; i < p->nPar; ++i) sum += 0.5 * p->alpha[i] * p->alpha[i] * p->regW[i];
     return sum;
 }
 
@@ -936,7 +947,11 @@ static double gradient_fd(orc_patch* p, int j, int m, img_scratch* s) {
 /* Solver::gradient (solver.cpp:860-894): per image, per enabled mode.
  * method 1 = finite differences, 2 = Vogel.  grad is in alpha space (nPar). */
 static void gradient_alpha(orc_patch* p, int method, double* g) {
-    memset(g, 0, sizeof(double) * (size_t)p->nPar);   /* REG_ALPHA = 0 */
+    /* Solver::gradient (solver.cpp:860-894): alpha * w with REG_ALPHA, zero otherwise; the
+     * enabled modes' entries are then overwritten (assigned, not added) by the data term, so
+     * the regularisation reaches only the modes not yet enabled */
+    if (p->regW) for (int i = 0; i < p->nPar; ++i) g[i] = p->alpha[i] * p->regW[i];
+    else memset(g, 0, sizeof(double) * (size_t)p->nPar);
 #pragma omp parallel for schedule(dynamic, 1) num_threads(p->nthreads)
     for (int j = 0; j < p->nImg; ++j) {
         img_scratch* s = &p->scr[j];

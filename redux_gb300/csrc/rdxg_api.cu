@@ -107,6 +107,9 @@ struct rdxg_solver {
     // warm start: the initial coefficients of the loaded patches [P][I][M] (loadInit)
     bool haveInit = false;
     double* dInitAlpha = nullptr;
+    // REG_ALPHA: per-parameter weights [I][M] of 0.5 sum alpha^2 w (Solver::regAlphaWeights)
+    std::vector<double> hRegW;
+    double* dRegW = nullptr;
 };
 
 namespace {
@@ -312,6 +315,7 @@ CgArgs<T> make_cgargs(rdxg_solver* h, const CgParams& prm) {
     a.objMetric = h->dObjMetric; a.L = make_lists(h); a.nTilesH = h->nTilesH;
     a.chunkSize = h->chunk; a.chunksPerPatch = h->chunksPerPatch; a.objChunk0 = h->dObjChunk0;
     a.objFirst = h->dObjFirstC; a.objCount = h->dObjCountC; a.aux = h->dAux;
+    a.regW = h->hRegW.empty() ? nullptr : h->dRegW;
     return a;
 }
 
@@ -835,6 +839,21 @@ int rdxg_set_fit_plane(rdxg_solver* h, int32_t enable) {
     return h->loaded ? prepare_patches(h) : RDXG_OK;
 }
 
+int rdxg_set_reg_alpha(rdxg_solver* h, const double* weights) {
+    if (!h) return RDXG_ERR_ARG;
+    if (!weights) {
+        h->hRegW.clear();
+        return RDXG_OK;
+    }
+    if (!h->dRegW) {
+        const int r = dalloc_t(h, &h->dRegW, (size_t)h->nPar);
+        if (r) return r;
+    }
+    h->hRegW.assign(weights, weights + h->nPar);
+    CK(h, cudaMemcpy(h->dRegW, weights, (size_t)h->nPar * sizeof(double), cudaMemcpyHostToDevice));
+    return RDXG_OK;
+}
+
 int rdxg_set_initial_alpha(rdxg_solver* h, const double* alpha) {
     if (!h) return RDXG_ERR_ARG;
     if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
@@ -870,6 +889,28 @@ int rdxg_set_patches_device(rdxg_solver* h, int32_t P, const float* dcut, const 
     return set_patches_common(h, P, ra, fg);
 }
 
+// REG_ALPHA on the host paths: Solver::metric adds 0.5 sum alpha^2 w (solver.cpp:804-811);
+// Solver::gradient starts from alpha * w and assigns the data term to the enabled modes, so
+// only the modes not enabled keep alpha * w (solver.cpp:860-885).
+void add_reg_metric(const rdxg_solver* h, const double* alpha, double* metric) {
+    if (h->hRegW.empty()) return;
+    for (int p = 0; p < h->P; ++p) {
+        double sum = 0;
+        const double* a = alpha + (size_t)p * h->nPar;
+        for (int i = 0; i < h->nPar; ++i) sum += 0.5 * a[i] * a[i] * h->hRegW[i];
+        metric[p] += sum;
+    }
+}
+void add_reg_gradient(const rdxg_solver* h, const double* alpha, const uint8_t* enabled, double* grad) {
+    if (h->hRegW.empty() || !enabled) return;
+    for (int p = 0; p < h->P; ++p)
+        for (int i = 0; i < h->nPar; ++i)
+            if (!enabled[i % h->M]) {
+                const size_t k = (size_t)p * h->nPar + i;
+                grad[k] = alpha[k] * h->hRegW[i];
+            }
+}
+
 int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric) {
     if (!h || !alpha || !metric) return RDXG_ERR_ARG;
     if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
@@ -881,6 +922,7 @@ int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric) {
         if ((r = fused_pass(h, REQ_F, 2))) return r;
         if ((r = fused_pass(h, REQ_F, 0))) return r;
         if ((r = metric_from_objects(h, metric))) return r;
+        add_reg_metric(h, alpha, metric);
         return tc_check(h);
     }
     with_size(h->N, h->fp64, [&](auto L, auto t) {
@@ -890,7 +932,9 @@ int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric) {
         launch_accum<T>(kp, h->P * h->nObj, h->stream);
     });
     CKL(h);
-    return metric_from_partials(h, metric);
+    if ((r = metric_from_partials(h, metric))) return r;
+    add_reg_metric(h, alpha, metric);
+    return RDXG_OK;
 }
 
 int rdxg_metric_noalloc(rdxg_solver* h, const double* alpha, double* metric) {
@@ -969,6 +1013,7 @@ int rdxg_metric_noalloc(rdxg_solver* h, const double* alpha, double* metric) {
     CKL(h);
     CK(h, cudaMemcpyAsync(metric, dMetric, P * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
+    add_reg_metric(h, alpha, metric);
     return tc_check(h);
 }
 
@@ -982,6 +1027,7 @@ int rdxg_metric_with_reference(rdxg_solver* h, const double* alpha_ref, const do
         return r;
     if ((r = upload_alpha<float>(h, alpha)) || (r = fused_pass(h, REQ_F, 0))) return r;
     if ((r = metric_from_objects(h, metric))) return r;
+    add_reg_metric(h, alpha, metric);
     return tc_check(h);
 }
 
@@ -1090,13 +1136,16 @@ int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, i
         for (size_t g = 0; g < G; ++g)
             for (int m = 0; m < h->M; ++m)
                 if (!enabled[m]) grad[g * h->M + m] = 0.0;
+    add_reg_gradient(h, alpha, enabled, grad);
     if (metric) {
         if (h->fused) {
             // the gradient pass left the exact object of this point as the reference
             if ((r = set_requests(h, REQ_F, GM_VOGEL, h->M)) || (r = fused_pass(h, REQ_F, 0))) return r;
-            return metric_from_objects(h, metric);
+            if ((r = metric_from_objects(h, metric))) return r;
+        } else if ((r = metric_from_partials(h, metric))) {
+            return r;
         }
-        return metric_from_partials(h, metric);
+        add_reg_metric(h, alpha, metric);
     }
     return RDXG_OK;
 }

@@ -98,6 +98,7 @@ struct CgArgs {
     const int32_t* objFirst;       // [nObj]
     const int32_t* objCount;       // [nObj]
     int32_t* aux;                  // [P][2]: reference object valid, refresh pending
+    const double* regW;            // [nPar] REG_ALPHA weights, or null
 };
 
 // alpha = offset + N x1; alpha_eff = alpha + currentTiltOffset - residual for the tilt modes
@@ -229,11 +230,32 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
         }
         __syncthreads();
         f = fsh;
+        if (a.regW) {
+            // REG_ALPHA: + 0.5 sum alpha^2 w at the evaluated point (solver.cpp:804-811), alpha
+            // = alpha_offset + N x1 in FP64
+            __shared__ double red[33];
+            const double* off = a.alphaOff + (size_t)p * a.nPar;
+            double part = 0;
+            for (int r = threadIdx.x; r < a.nPar; r += THREADS) {
+                double v = off[r];
+                for (int e = a.rowPtr[r]; e < a.rowPtr[r + 1]; ++e) v += a.rowVal[e] * x1[a.rowCol[e]];
+                part += 0.5 * v * v * a.regW[r];
+            }
+            f += block_sum<THREADS>(part, red);
+        }
     } else if (req0 == REQ_DF) {
         const double* ga = a.galpha + (size_t)p * a.nPar;
+        // REG_ALPHA: the modes not enabled keep alpha * w (the enabled ones are assigned the
+        // data term, solver.cpp:860-885)
+        const double* al = a.alpha + (size_t)p * a.nPar;
+        const int mcount = a.modeCount[p];
         for (int c = threadIdx.x; c < nF; c += THREADS) {
             double v = 0;
-            for (int e = a.colPtr[c]; e < a.colPtr[c + 1]; ++e) v += a.colVal[e] * ga[a.colRow[e]];
+            for (int e = a.colPtr[c]; e < a.colPtr[c + 1]; ++e) {
+                const int row = a.colRow[e];
+                const double gr = (a.regW && row % a.M >= mcount) ? al[row] * a.regW[row] : ga[row];
+                v += a.colVal[e] * gr;
+            }
             g[c] = v;
         }
         __syncthreads();

@@ -466,3 +466,13 @@ def build_constraints(image_wavefronts, n_modes: int, ref_images, tilt_modes=(0,
                 col += 1
     return NullSpace(I * n_modes, col, np.array(rows, np.int32), np.array(cols, np.int32),
                      np.array(vals, np.float64))
+
+
+def reg_alpha_weights(atm_rms, n_images: int, patch_size: int, wavelength: float, reg_alpha: float):
+    """Solver::regAlphaWeights (solver.cpp:147-156): for every image and mode
+    reg_alpha / wavelength * nTotalPixels / atm_rms[m]^2 (0 where atm_rms is 0), nTotalPixels =
+    images * patch_size^2; the metric gains 0.5 sum alpha^2 w.  Returns [n_images][M]."""
+    rms = np.asarray(atm_rms, np.float64)
+    scale = reg_alpha / wavelength * (n_images * patch_size * patch_size)
+    w = np.where(rms == 0.0, 0.0, scale / np.where(rms == 0.0, 1.0, rms * rms))
+    return np.tile(w, (n_images, 1))

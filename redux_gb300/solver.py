@@ -129,6 +129,16 @@ class Solver:
                                                         _lib.ptr(fg)), "rdxg_set_patches_device")
         self.P = n_patches
 
+    def set_reg_alpha(self, weights=None) -> None:
+        """REG_ALPHA: weights [I][M] of 0.5 sum alpha^2 w added to the metric (None: off);
+        jobsetup.reg_alpha_weights gives the reference's."""
+        if weights is None:
+            self._check(_lib.load().rdxg_set_reg_alpha(self.h, None), "rdxg_set_reg_alpha")
+            return
+        w = np.ascontiguousarray(weights, np.float64).reshape(self.I, self.M)
+        self._keep.append(w)
+        self._check(_lib.load().rdxg_set_reg_alpha(self.h, _lib.ptr(w)), "rdxg_set_reg_alpha")
+
     def set_initial_alpha(self, alpha=None) -> None:
         """Warm start: initial coefficients [P][I][M] of the loaded patches (None: zero); the
         images are re-cut by their tilts and every following solve starts there."""
