@@ -67,6 +67,11 @@ int main(int argc, char** argv) {
         set.finiteDifferenceFirst = sv[5] != 0; set.ftol = sv[6]; set.eps = sv[7]; set.maxMetrics = (int32_t)sv[8];
         set.restore = true;
         if (sv.size() > 9) set.saveMask = (int32_t)sv[9];
+        // optional: FIT_PLANE, REG_ALPHA weights, warm-start coefficients
+        const auto flags = load<int32_t>(dir, "fit_plane.i32", false);
+        set.fitPlane = !flags.empty() && flags[0] != 0;
+        set.regAlphaWeights = load<double>(dir, "reg_alpha.f64", false);
+        const auto init = load<double>(dir, "init_alpha.f64", false);
         rdxg::Solver solver(g, s, set, load<double>(dir, "fc.f64"));
         solver.init();
         const auto cut = load<float>(dir, "cutouts.f32");
@@ -78,6 +83,8 @@ int main(int argc, char** argv) {
         for (int p = 0; p < P; ++p) {
             pd[p].cutouts.assign(cut.begin() + p * per, cut.begin() + (p + 1) * per);
             if (!gam.empty()) pd[p].fixedGamma.assign(gam.begin() + (size_t)p * g.n_objects, gam.begin() + (size_t)(p + 1) * g.n_objects);
+            const size_t nPar = (size_t)g.n_images * g.n_modes;
+            if (!init.empty()) pd[p].initAlpha.assign(init.begin() + p * nPar, init.begin() + (p + 1) * nPar);
             batch.push_back(&pd[p]);
         }
         solver.run(batch);

@@ -31,7 +31,7 @@ def test_shim_compiles_and_links(tmp_path):
     assert os.path.exists(exe)
 
 
-def _dump(job, cutouts, fixed_gamma, st, fc, d, save_mask=0):
+def _dump(job, cutouts, fixed_gamma, st, fc, d, save_mask=0, extras=None):
     sup, ns = job.support, job.nullspace
     geom = [job.otf_size, job.pupil_pixels, job.patch_size, job.n_modes, job.n_objects, job.n_images,
             job.n_channels, job.tilt_x, job.tilt_y, ns.n_free, job.cutout_size, cutouts.shape[0], 0, 0]
@@ -50,15 +50,29 @@ def _dump(job, cutouts, fixed_gamma, st, fc, d, save_mask=0):
     }
     if fixed_gamma is not None:
         arrays["fixed_gamma.f64"] = fixed_gamma
+    if extras:
+        arrays["fit_plane.i32"] = [1]
+        arrays["reg_alpha.f64"] = extras["reg_alpha"]
+        arrays["init_alpha.f64"] = extras["init_alpha"]
     for name, a in arrays.items():
         dt = {"i32": np.int32, "f64": np.float64, "f32": np.float32}[name.rsplit(".", 1)[1]]
         np.ascontiguousarray(a, dt).tofile(os.path.join(d, name))
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", [0, 2, "0+"])
 def test_shim_solve_matches_the_python_harness(tmp_path, cfg):
-    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    """cfg "0+": configuration 0 with FIT_PLANE, REG_ALPHA and a warm start."""
+    extras = None
+    if cfg == "0+":
+        from redux_gb300 import jobsetup as js
+        w = workload(0)
+        extras = dict(reg_alpha=js.reg_alpha_weights(np.sqrt(w.job.atm_var), w.job.n_images, w.job.patch_size,
+                                                     w.job.wavelength, 1e3),
+                      init_alpha=w.patches.alpha_true * 0.5)
+        cfg = 0
+    else:
+        w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
     job = w.job
     st = S.SolveSettings(mode_start=5, mode_step=5, max_iterations=6, min_iterations=3, ftol=1e-3, max_metrics=128)
     fc = job.otf_size / 2.0
@@ -67,7 +81,7 @@ def test_shim_solve_matches_the_python_harness(tmp_path, cfg):
     from redux_gb300 import _lib
     psf_flag = _lib.RDXG_RESTORE_PSF if cfg == 0 else _lib.RDXG_RESTORE_PSF_AVG
     _dump(job, w.patches.cutouts, w.patches.fixed_gamma, st, fc, d,
-          save_mask=psf_flag | _lib.RDXG_RESTORE_COBJ | _lib.RDXG_RESTORE_RESIDUAL)
+          save_mask=psf_flag | _lib.RDXG_RESTORE_COBJ | _lib.RDXG_RESTORE_RESIDUAL, extras=extras)
     exe = _build(d)
     r = subprocess.run([exe, d], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
@@ -79,7 +93,12 @@ def test_shim_solve_matches_the_python_harness(tmp_path, cfg):
         P, job.n_objects, job.patch_size, job.patch_size)
     # the same solve through the Python harness (same library, same kernels, same inputs)
     s = S.Solver(job, max_patches=P)
+    if extras:
+        s.set_fit_plane(True)
+        s.set_reg_alpha(extras["reg_alpha"])
     s.set_patches(w.patches.cutouts, None, w.patches.fixed_gamma)
+    if extras:
+        s.set_initial_alpha(extras["init_alpha"])
     out = s.run(st)
     ref_obj = s.restore(out["alpha"], fc)
     np.testing.assert_array_equal(alpha, out["alpha"])
