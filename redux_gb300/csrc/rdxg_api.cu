@@ -850,7 +850,10 @@ int rdxg_set_reg_alpha(rdxg_solver* h, const double* weights) {
         if (r) return r;
     }
     h->hRegW.assign(weights, weights + h->nPar);
-    CK(h, cudaMemcpy(h->dRegW, weights, (size_t)h->nPar * sizeof(double), cudaMemcpyHostToDevice));
+    // on the handle's stream, after any of its work still in flight
+    CK(h, cudaMemcpyAsync(h->dRegW, h->hRegW.data(), (size_t)h->nPar * sizeof(double), cudaMemcpyHostToDevice,
+                          h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
     return RDXG_OK;
 }
 

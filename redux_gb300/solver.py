@@ -136,7 +136,6 @@ class Solver:
             self._check(_lib.load().rdxg_set_reg_alpha(self.h, None), "rdxg_set_reg_alpha")
             return
         w = np.ascontiguousarray(weights, np.float64).reshape(self.I, self.M)
-        self._keep.append(w)
         self._check(_lib.load().rdxg_set_reg_alpha(self.h, _lib.ptr(w)), "rdxg_set_reg_alpha")
 
     def set_initial_alpha(self, alpha=None) -> None:
