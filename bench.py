@@ -155,11 +155,11 @@ def run_reference(args, rank):
 
 
 def run_uneven(args):
-    """Configuration 3, the uneven batch: patches of sizes {64, 88, 128}, 8-24 frames per
+    """The uneven batch: patches of sizes {64, 88, 128}, 8-24 frames per
     channel and 36-60 KL modes, staged modes and per-patch convergence (FTOL 1e-6), one
     handle per geometry and every handle's rounds in one CUDA graph (rdxg_solve_many), against
     per-patch launches (each patch its own handle, solved one after the other).  Not the
-    headline line: `python bench.py --config 3`."""
+    headline line: `python bench.py --workload uneven`."""
     import torch
     from redux_gb300 import solver as S, synth
     torch.cuda.set_device(0)
@@ -208,7 +208,7 @@ def run_uneven(args):
         n_single += 1
         h1.close()
     # the same patches inside the batch: their share of the batch time
-    line = {"metric": "uneven-batch converged patches/s (configuration 3)", "value": n / t_many, "unit": UNIT,
+    line = {"metric": "uneven-batch converged patches/s", "value": n / t_many, "unit": UNIT,
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_many * 1000.0,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (FP64 sums and CG scalars)", "data": "synthetic",
@@ -230,7 +230,7 @@ def run_uneven(args):
 
 
 def run_large(args):
-    """Configuration 4, mixed precision at large size: 128 x 128 patches, 3 channels x 32
+    """Large patches, mixed precision: 128 x 128 patches, 3 channels x 32
     frames, 100 KL modes at D/r0 = 25; mode expansion on the CUDA cores in FP32 (the tensor-core
     expansion belongs to the fused path, which covers N <= 88), FP32 transforms, FP64 metric
     sums and CG scalars.  `--iterations` CG iterations per patch with all modes at once, as the
@@ -238,13 +238,13 @@ def run_large(args):
     nominal FP32 rates and HBM fractions, and the errors against the FP64 restatement on one
     patch: the metric, gradient and restored object at the same alpha (per-evaluation
     precision) and the metric history, alpha and restored object after a short solve of both.
-    Defaults to 1 warm-up and 2 timed solves.  Not the headline line: `python bench.py --config 4`."""
+    Defaults to 1 warm-up and 2 timed solves.  Not the headline line: `python bench.py --workload large`."""
     import torch
     from redux_gb300 import solver as S, synth
     torch.cuda.set_device(0)
     P = args.patches if args.patches != 225 else 256
     t0 = time.perf_counter()
-    w = synth.config(4, n_patches=P)
+    w = synth.workload("large128", n_patches=P)
     t_gen = time.perf_counter() - t0
     job, cut = w.job, np.ascontiguousarray(w.patches.cutouts, np.float32)
     settings = S.fixed_iterations(job.n_modes, args.iterations, max_metrics=args.iterations + 8)
@@ -320,7 +320,7 @@ def run_large(args):
         "short_solve_object_rel_peak": float(np.abs(obj_1s - obj_os).max() / np.abs(obj_os).max()),
     }
     s1.close()
-    line = {"metric": "large-patch patches/s (configuration 4)", "value": P / t_solve, "unit": UNIT, "n_gpus": 1,
+    line = {"metric": "large-patch patches/s", "value": P / t_solve, "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_solve * 1000.0, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 sums and CG scalars)", "data": "synthetic",
             "config": {"workload": f"{P} patches 128x128, 100 KL modes, 3ch x 32 frames, D/r0=25, "
@@ -344,8 +344,8 @@ def run_large(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 5; 2 for --config 4)")
-    ap.add_argument("--warmup", type=int, default=None, help="warm-up steps (default 3; 1 for --config 4)")
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 5; 2 for --workload large)")
+    ap.add_argument("--warmup", type=int, default=None, help="warm-up steps (default 3; 1 for --workload large)")
     ap.add_argument("--impl", default="ours")
     ap.add_argument("--patches", type=int, default=225)
     ap.add_argument("--frames", type=int, default=12)
@@ -353,8 +353,9 @@ def main():
     ap.add_argument("--no-baselines", action="store_true")
     ap.add_argument("--handles", type=int, default=3,
                     help="handles (each on its own stream) the batch is split over, solved together")
-    ap.add_argument("--config", type=int, default=2,
-                    help="2: the headline batch; 3: the uneven batch; 4: large patches (128 x 128, 100 modes)")
+    ap.add_argument("--workload", default="production", choices=("production", "uneven", "large"),
+                    help="production: the headline batch (225 patches 88 x 88); uneven: 400 patches of "
+                         "{64, 88, 128} px; large: 256 patches 128 x 128 with 100 modes")
     ap.add_argument("--levels", type=int, default=3,
                     help="uneven batch: frames and modes from this many values (0: uniform draws)")
     ap.add_argument("--check-iterations", type=int, default=10,
@@ -362,7 +363,7 @@ def main():
     ap.add_argument("--kernels-only", action="store_true",
                     help="load the batch and time each kernel once (profiling target)")
     args = ap.parse_args()
-    large = args.config == 4 and args.impl != "reference"
+    large = args.workload == "large" and args.impl != "reference"
     if args.warmup is None:
         args.warmup = 1 if large else 3
     if args.steps is None:
@@ -372,9 +373,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank)
-    if args.config == 3:
+    if args.workload == "uneven":
         return run_uneven(args)
-    if args.config == 4:
+    if args.workload == "large":
         return run_large(args)
 
     import torch

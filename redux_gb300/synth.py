@@ -5,11 +5,13 @@ random field with a k^-2 power spectrum, mean 1, 10 % RMS contrast), per-frame
 Kolmogorov wavefronts expanded in Zernike modes, images = object (x) PSF with
 Poisson noise at 1e4 photons/px plus N(0, 10^2) read noise, stored as float32.
 
-The generator follows the workload descriptions of the five benchmark configurations
-(plain FP64 single patch; adjoint check; 225-patch production field; uneven batch;
-large mixed-precision batch).  Configuration 0 uses Zernike modes Noll 2..21, the others
-Karhunen-Loeve modes (tilts Zernike) from the expansion of the Noll covariance.  The uneven
-batch (configuration 3, `uneven_batch`) is a list of workloads, one per patch geometry.
+The named workloads (`workload`): "plain64", one 64 x 64 patch, 2 channels x 4 frames,
+Zernike modes Noll 2..21; "adjoint88", 88 x 88, 3 channels x 8 frames, 36 Karhunen-Loeve
+modes; "production88", 225 patches 88 x 88, 3 channels x 12 frames, 36 KL modes;
+"large128", 256 patches 128 x 128, 3 channels x 32 frames, 100 KL modes.  KL modes keep the
+tilts Zernike and come from the expansion of the Noll covariance.  The uneven batch
+(`uneven_batch`: sizes {64, 88, 128}, 8-24 frames, 36-60 modes) is a list of workloads,
+one per patch geometry.
 """
 from __future__ import annotations
 
@@ -254,13 +256,13 @@ UNEVEN_KL_LAST = 121   # one expansion over Noll 2..121 for every mode count (it
 
 def uneven_batch(n_patches: int = 400, frames=(8, 24), modes=(36, 60), levels: int | None = None,
                  d_r0: float = 15.0, seed_offset: int = 0) -> list:
-    """Configuration 3: patches whose size ({64, 88, 128}), frames per channel (8..24) and
+    """The uneven batch: patches whose size ({64, 88, 128}), frames per channel (8..24) and
     number of KL modes (36..60) are drawn uniformly per patch, 3 channels (wideband; narrowband
     focus and +1 wave), grouped by geometry.  levels: draw frames and modes from that many
     evenly spaced values instead (e.g. 3: frames {8, 16, 24}, modes {36, 48, 60}) so that
     patches share geometries.  Returns one Workload per distinct (size, frames, modes), its
     cfg["patch_index"] the positions of its patches in the draw order."""
-    rng = np.random.default_rng(20261203 + 3 + seed_offset)
+    rng = np.random.default_rng(20261203 + WORKLOAD_SEEDS["uneven"] + seed_offset)
 
     def draw(lo, hi):
         if levels:
@@ -275,30 +277,35 @@ def uneven_batch(n_patches: int = 400, frames=(8, 24), modes=(36, 60), levels: i
     out = []
     for (N, F, M), idx in sorted(groups.items()):
         job = make_job(N, M, LAYOUT_WB_NB(F), basis="kl", kl_last=UNEVEN_KL_LAST)
-        prng = np.random.default_rng([20261203 + 3 + seed_offset, N, F, M])
+        prng = np.random.default_rng([20261203 + WORKLOAD_SEEDS["uneven"] + seed_offset, N, F, M])
         pt = make_patches(job, len(idx), d_r0, prng)
         out.append(Workload(f"uneven {N}x{N}, 3ch x {F}fr, {M} KL modes", job, pt, dict(patch_index=idx)))
     return out
 
 
-def config(index: int, n_patches: int | None = None, seed_offset: int = 0, frames=None) -> Workload:
-    """The benchmark workloads, seeded with 20261203 + index (+ seed_offset)."""
-    rng = np.random.default_rng(20261203 + index + seed_offset)
-    if index == 0:
+# seed of each named workload: 20261203 + this (+ seed_offset)
+WORKLOAD_SEEDS = {"plain64": 0, "adjoint88": 1, "production88": 2, "uneven": 3, "large128": 4}
+
+
+def workload(name: str, n_patches: int | None = None, seed_offset: int = 0, frames=None) -> Workload:
+    """A named benchmark workload (module docstring), seeded with 20261203 + its
+    WORKLOAD_SEEDS entry (+ seed_offset); n_patches and frames override its sizes."""
+    if name not in WORKLOAD_SEEDS or name == "uneven":
+        raise ValueError(f"unknown workload {name!r} (the uneven batch comes from uneven_batch)")
+    rng = np.random.default_rng(20261203 + WORKLOAD_SEEDS[name] + seed_offset)
+    if name == "plain64":
         job = make_job(64, 20, LAYOUT_1OBJ(frames or 4))
         pt = make_patches(job, n_patches or 1, 10.0, rng, fixed_gamma=1e-3)
         cfg = dict(iterations=50, gamma=1e-3)
         return Workload("plain FP64 64x64, 2ch x 4fr, Z2-21", job, pt, cfg)
-    if index == 1:
+    if name == "adjoint88":
         job = make_job(88, 36, LAYOUT_WB_NB(frames or 8), basis="kl")
         pt = make_patches(job, n_patches or 1, 10.0, rng)
         return Workload("adjoint check 88x88, 3ch x 8fr, 36 modes", job, pt, {})
-    if index == 2:
+    if name == "production88":
         job = make_job(88, 36, LAYOUT_WB_NB(frames or 12), basis="kl")
         pt = make_patches(job, n_patches or 225, 15.0, rng)
         return Workload("production 88x88, 3ch x 12fr, 36 KL modes", job, pt, dict(iterations=100))
-    if index == 4:
-        job = make_job(128, 100, LAYOUT_WB_NB(frames or 32), basis="kl")
-        pt = make_patches(job, n_patches or 256, 25.0, rng)
-        return Workload("mixed precision 128x128, 3ch x 32fr, 100 KL modes", job, pt, {})
-    raise ValueError(f"unknown config {index}")
+    job = make_job(128, 100, LAYOUT_WB_NB(frames or 32), basis="kl")
+    pt = make_patches(job, n_patches or 256, 25.0, rng)
+    return Workload("mixed precision 128x128, 3ch x 32fr, 100 KL modes", job, pt, {})

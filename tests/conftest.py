@@ -15,21 +15,22 @@ def pytest_configure(config):
 _CACHE = {}
 
 
-def workload(index, **kw):
-    """Seeded synthetic workloads, generated once per session."""
+def workload(name, **kw):
+    """Seeded synthetic workloads by name (redux_gb300.synth.workload), generated once per
+    session."""
     from redux_gb300 import synth
-    key = (index, tuple(sorted(kw.items())))
+    key = (name, tuple(sorted(kw.items())))
     if key not in _CACHE:
-        _CACHE[key] = synth.config(index, **kw)
+        _CACHE[key] = synth.workload(name, **kw)
     return _CACHE[key]
 
 
 @pytest.fixture(scope="session")
 def w0():
-    return workload(0)
+    return workload("plain64")
 
 
 @pytest.fixture(scope="session")
 def w2small():
     # the production geometry (88 x 88, 36 modes, 3 channels) with 4 frames and 2 patches
-    return workload(2, n_patches=2, frames=4)
+    return workload("production88", n_patches=2, frames=4)

@@ -1,6 +1,6 @@
 """Writes the oracle's golden vectors (tests/golden/oracle_golden.npz): regression fixtures
 of the FP64 C restatement on the seeded synthetic workloads, so that a change to the oracle
-(the checker of every GPU test) shows up on the CPU.  The reference itself does not build
+(which every GPU test compares against) shows up on the CPU.  The reference itself does not build
 here, so these pin the restatement to itself, not to redux.
 
     python tests/golden/make_golden.py
@@ -23,8 +23,9 @@ OUT = os.path.join(HERE, "oracle_golden.npz")
 
 
 def cases():
-    """(name, workload): configuration 0, and configuration 2's geometry with 4 frames."""
-    return [("c0", synth.config(0)), ("c2", synth.config(2, n_patches=1, frames=4))]
+    """(name, workload): the plain 64 x 64 patch, and one 88 x 88 production patch with 4 frames."""
+    return [("plain64", synth.workload("plain64")),
+            ("production88", synth.workload("production88", n_patches=1, frames=4))]
 
 
 def compute(name, w):

@@ -16,8 +16,8 @@ TOL_GRAD = 1e-5        # gradient within 1e-5 relative (norm) of the FP64 refere
 TOL_FD = 1e-4          # exact derivative against FP64 central differences (sampled entries)
 
 
-def test_adjoint_check_config1():
-    w = workload(1, n_patches=1)
+def test_adjoint_check_88x88_3x8_36kl():
+    w = workload("adjoint88", n_patches=1)
     job = w.job
     I, M = job.n_images, job.n_modes
     s = S.Solver(job, max_patches=1)

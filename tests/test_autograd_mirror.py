@@ -35,7 +35,7 @@ class MomfbdMetric(torch.autograd.Function):
 
 @pytest.fixture(scope="module")
 def setup():
-    w = workload(1, n_patches=1)
+    w = workload("adjoint88", n_patches=1)
     s = S.Solver(w.job, max_patches=1)
     s.set_patches(w.patches.cutouts, None, w.patches.fixed_gamma)
     op = oracle.OraclePatch(w.job)

@@ -60,26 +60,26 @@ def _dump(job, cutouts, fixed_gamma, st, fc, d, save_mask=0, extras=None):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("cfg", [0, 2, "0+"])
+@pytest.mark.parametrize("cfg", ["plain64", "production88", "plain64+"])
 def test_shim_solve_matches_the_python_harness(tmp_path, cfg):
-    """cfg "0+": configuration 0 with FIT_PLANE, REG_ALPHA and a warm start."""
+    """cfg "plain64+": the plain 64 x 64 workload with FIT_PLANE, REG_ALPHA and a warm start."""
     extras = None
-    if cfg == "0+":
+    if cfg == "plain64+":
         from redux_gb300 import jobsetup as js
-        w = workload(0)
+        w = workload("plain64")
         extras = dict(reg_alpha=js.reg_alpha_weights(np.sqrt(w.job.atm_var), w.job.n_images, w.job.patch_size,
                                                      w.job.wavelength, 1e3),
                       init_alpha=w.patches.alpha_true * 0.5)
-        cfg = 0
+        cfg = "plain64"
     else:
-        w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+        w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
     job = w.job
     st = S.SolveSettings(mode_start=5, mode_step=5, max_iterations=6, min_iterations=3, ftol=1e-3, max_metrics=128)
     fc = job.otf_size / 2.0
     d = str(tmp_path)
     # per-image PSFs for one configuration, the object means for the other
     from redux_gb300 import _lib
-    psf_flag = _lib.RDXG_RESTORE_PSF if cfg == 0 else _lib.RDXG_RESTORE_PSF_AVG
+    psf_flag = _lib.RDXG_RESTORE_PSF if cfg == "plain64" else _lib.RDXG_RESTORE_PSF_AVG
     _dump(job, w.patches.cutouts, w.patches.fixed_gamma, st, fc, d,
           save_mask=psf_flag | _lib.RDXG_RESTORE_COBJ | _lib.RDXG_RESTORE_RESIDUAL, extras=extras)
     exe = _build(d)
@@ -110,7 +110,7 @@ def test_shim_solve_matches_the_python_harness(tmp_path, cfg):
         assert rep[3 * p + 1] == out["reports"][p].iterations
     np.testing.assert_allclose(obj, ref_obj, rtol=0, atol=1e-5 * np.abs(ref_obj).max())
     ps = job.patch_size
-    ref = s.restore_outputs(out["alpha"], fc, psf="each" if cfg == 0 else "mean", cobj=True, residual=True)
+    ref = s.restore_outputs(out["alpha"], fc, psf="each" if cfg == "plain64" else "mean", cobj=True, residual=True)
     for name in ("psf", "cobj", "res"):
         key = "residual" if name == "res" else name
         got = np.fromfile(os.path.join(d, f"{name}.out.f32"), np.float32).reshape(ref[key].shape)

@@ -49,7 +49,7 @@ def _oracle(job, cut, fg=None):
 def test_object_of_weight_zero():
     """Object::weight 0 drops the object from the metric and zeroes its gradient
     (solver.cpp:763-817, 881)."""
-    w = workload(2, n_patches=1, frames=4)
+    w = workload("production88", n_patches=1, frames=4)
     job = dataclasses.replace(w.job, obj_weight=np.array([1.0, 0.0]))
     s = S.Solver(job, max_patches=1)
     s.set_patches(w.patches.cutouts)
@@ -68,7 +68,7 @@ def test_object_of_weight_zero():
 def test_image_without_variance_is_reported():
     """A constant image has no noise estimate relative to its spread: the noise-derived
     regularisation is not finite and set_patches answers RDXG_ERR_NONFINITE."""
-    w = workload(0)
+    w = workload("plain64")
     cut = w.patches.cutouts.copy()
     cut[0, 1] = 1000.0
     s = S.Solver(w.job, max_patches=1)
@@ -78,7 +78,7 @@ def test_image_without_variance_is_reported():
 
 @gpu
 def test_batch_smaller_than_the_capacity():
-    w = workload(2, n_patches=2, frames=4)
+    w = workload("production88", n_patches=2, frames=4)
     s = S.Solver(w.job, max_patches=3)
     a = w.patches.alpha_true * 0.5
     s.set_patches(w.patches.cutouts[1:2])
@@ -116,7 +116,7 @@ def test_full_batch_patches_are_independent():
     """At the production size (225 patches 88x88, 3 channels x 12 frames): a patch's solve does
     not depend on the other patches of its batch (the same bits as a 5-patch batch of some of
     them), and every patch ends below its initial metric."""
-    w = workload(2)
+    w = workload("production88")
     P = w.patches.cutouts.shape[0]
     st = S.fixed_iterations(w.job.n_modes, 20, max_metrics=32)
     big = S.Solver(w.job, max_patches=P)

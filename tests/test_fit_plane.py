@@ -38,9 +38,9 @@ def _np_plane(job, cut):
     return np.stack(out)
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_oracle_plane_is_the_least_squares_plane(cfg):
-    w = workload(0) if cfg == 0 else workload(2, n_patches=1, frames=4)
+    w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=1, frames=4)
     op = _oracle(w)
     ref = _np_plane(w.job, w.patches.cutouts[0])
     np.testing.assert_allclose(op.plane(), ref, rtol=0, atol=1e-6 * np.abs(ref).max())
@@ -74,9 +74,9 @@ def _solver(w):
 
 
 @gpu
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_image_transform_metric_and_restore(cfg):
-    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
     s = _solver(w)
     D = s.debug("D")
     a = w.patches.alpha_true * 0.5

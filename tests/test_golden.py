@@ -1,5 +1,5 @@
 """The oracle against its committed golden vectors (tests/golden/make_golden.py): a change to
-the FP64 restatement, the checker of every GPU test, fails here on the CPU."""
+the FP64 restatement, which every GPU test compares against, fails here on the CPU."""
 import os
 
 import numpy as np

@@ -27,9 +27,9 @@ def _solver(w, precision="fp32"):
     return s
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_image_ft_and_gamma(cfg):
-    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
     s = _solver(w)
     D = s.debug("D")
     gam = s.debug("gamma")
@@ -46,10 +46,10 @@ def test_image_ft_and_gamma(cfg):
         np.testing.assert_allclose(st[:, 2], nz, rtol=1e-5)
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 @pytest.mark.parametrize("scale", [0.0, 0.5, 1.0])
 def test_metric(cfg, scale):
-    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
     s = _solver(w)
     a = w.patches.alpha_true * scale
     L = s.metric(a)
@@ -58,9 +58,9 @@ def test_metric(cfg, scale):
         assert abs(L[p] - Lo) <= TOL_METRIC * abs(Lo), (p, L[p], Lo)
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_otf(cfg):
-    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
     s = _solver(w)
     a = w.patches.alpha_true * 0.7
     s.gradient(a, "vogel")      # gradient evaluations keep the OTF in HBM
@@ -72,9 +72,9 @@ def test_otf(cfg):
     assert rel < 1e-6, rel
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_gradient_vogel(cfg):
-    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
     s = _solver(w)
     a = w.patches.alpha_true * 0.5
     g, L = s.gradient(a, "vogel")
@@ -148,11 +148,11 @@ def test_solve_fixed_iterations(w0):
     assert np.sqrt(np.mean(da ** 2)) < 5e-2
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_metric_with_stale_reference(cfg):
     """The line search evaluates the metric with the reference object of the last gradient
     point; the result must not depend on it beyond rounding."""
-    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
     s = _solver(w)
     base = w.patches.alpha_true * 0.5
     g, _ = s.gradient(base, "vogel")
@@ -189,9 +189,9 @@ def _general_path_solver(w, precision="fp32"):
         del os.environ["RDXG_NO_FUSED"]
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_fused_and_general_paths_agree(cfg):
-    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
     sf = _solver(w)
     sg = _general_path_solver(w)
     a = w.patches.alpha_true * 0.6
@@ -228,9 +228,9 @@ def test_staged_solve_with_reshifts(w0):
 TOL_RESTORE = 1e-4
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_restore(cfg):
-    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
     s = _solver(w)
     fc = w.job.otf_size / 2.0
     a = w.patches.alpha_true
@@ -254,9 +254,9 @@ def test_restore_fp64_with_and_without_filter(w0):
         assert err <= 1e-6, (nf, err)
 
 
-# the general (unfused) FP32 path at N = 128 with 100 KL modes (config 4's geometry, 2 frames)
+# the general (unfused) FP32 path at N = 128 with 100 KL modes (the large-patch geometry, 2 frames)
 def _w4():
-    return workload(4, n_patches=1, frames=2)
+    return workload("large128", n_patches=1, frames=2)
 
 
 @pytest.mark.parametrize("scale", [0.0, 1.0])

@@ -12,11 +12,11 @@ pytestmark = pytest.mark.gpu
 # (workload, shapes to compare): the fused path (64, 88) tunes k_eval and k_adjoint, the
 # general path (128) k_forward and k_adjoint
 CASES = {
-    "fused64": (lambda: workload(0), [dict(eval_threads=512, adjoint_threads=256),
+    "fused64": (lambda: workload("plain64"), [dict(eval_threads=512, adjoint_threads=256),
                                       dict(eval_threads=384, adjoint_threads=512)]),
-    "fused88": (lambda: workload(2, n_patches=2, frames=4), [dict(eval_threads=512, adjoint_threads=256),
+    "fused88": (lambda: workload("production88", n_patches=2, frames=4), [dict(eval_threads=512, adjoint_threads=256),
                                                              dict(eval_threads=384, adjoint_threads=512)]),
-    "general128": (lambda: workload(4, n_patches=1, frames=2), [dict(forward_threads=512, adjoint_threads=512),
+    "general128": (lambda: workload("large128", n_patches=1, frames=2), [dict(forward_threads=512, adjoint_threads=512),
                                                                 dict(forward_threads=1024, adjoint_threads=1024)]),
 }
 
@@ -83,7 +83,7 @@ def test_autotune_reports_the_candidates(case):
 
 
 def test_fp64_has_one_shape():
-    w = workload(0)
+    w = workload("plain64")
     s = S.Solver(w.job, max_patches=1, precision="fp64")
     s.set_patches(w.patches.cutouts, None, w.patches.fixed_gamma)
     r = s.autotune(reps=1)

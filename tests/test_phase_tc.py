@@ -19,7 +19,7 @@ TOL_PHASE = {3: 1e-6, 2: 2e-5}
 
 
 def _w(cfg):
-    return workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    return workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
 
 
 def _solver(w):
@@ -37,11 +37,11 @@ def _oracle(w, p=0):
 
 
 def test_default_is_6xbf16():
-    s = _solver(_w(0))
+    s = _solver(_w("plain64"))
     assert s.phase_mode() == 3
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_phases_against_cuda_cores(cfg):
     w = _w(cfg)
     s = _solver(w)
@@ -58,7 +58,7 @@ def test_phases_against_cuda_cores(cfg):
         assert err <= TOL_PHASE[mode], (mode, err)
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 @pytest.mark.parametrize("mode", [0, 2, 3])
 def test_metric_each_mode(cfg, mode):
     w = _w(cfg)
@@ -72,7 +72,7 @@ def test_metric_each_mode(cfg, mode):
             assert abs(L[p] - Lo) <= TOL_METRIC * abs(Lo), (mode, scale, p, L[p], Lo)
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_gradient_6xbf16(cfg):
     w = _w(cfg)
     s = _solver(w)
@@ -87,7 +87,7 @@ def test_gradient_6xbf16(cfg):
 def test_gradient_3xbf16_error_is_bounded():
     # the 3xBF16 split misses the 1e-5 gradient tolerance at 64 x 64 with Zernike phases of
     # up to 65 rad (measured 2.5e-5); it stays within 5e-5
-    w = _w(0)
+    w = _w("plain64")
     s = _solver(w)
     s.set_phase_mode(2)
     a = w.patches.alpha_true * 0.7
@@ -98,7 +98,7 @@ def test_gradient_3xbf16_error_is_bounded():
 
 
 def test_solve_first_metrics_6xbf16():
-    w = _w(0)
+    w = _w("plain64")
     s = _solver(w)
     s.set_phase_mode(3)
     st = S.fixed_iterations(w.job.n_modes, 3, max_metrics=64)
@@ -111,7 +111,7 @@ def test_solve_first_metrics_6xbf16():
 
 
 def test_mode_errors():
-    w = _w(0)
+    w = _w("plain64")
     s = _solver(w)
     with pytest.raises(S.SolverError):
         s.set_phase_mode(1)

@@ -8,9 +8,9 @@ from oracle import np_oracle
 from tests.conftest import workload
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_restore_c_vs_numpy(cfg):
-    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
     op = oracle.OraclePatch(w.job)
     fg = None if w.patches.fixed_gamma is None else w.patches.fixed_gamma[0]
     op.set_images(w.patches.cutouts[0], None, fg)

@@ -19,8 +19,9 @@ TOL = {"fp32": 2e-6, "fp64": 1e-7}
 
 
 def _setup(cfg, precision):
-    w = {0: lambda: workload(0), 2: lambda: workload(2, n_patches=2, frames=4),
-         4: lambda: workload(4, n_patches=1, frames=2)}[cfg]()
+    w = {"plain64": lambda: workload("plain64"),
+         "production88": lambda: workload("production88", n_patches=2, frames=4),
+         "large128": lambda: workload("large128", n_patches=1, frames=2)}[cfg]()
     P = w.patches.cutouts.shape[0]
     s = S.Solver(w.job, max_patches=P, precision=precision)
     s.set_patches(w.patches.cutouts, None, w.patches.fixed_gamma)
@@ -35,7 +36,8 @@ def _oracle_outputs(w, p, a, objects):
     return np_oracle.restore_outputs(op.D(), op.otf(), w.job.img_object, objects, w.job.patch_size)
 
 
-@pytest.mark.parametrize("cfg,precision", [(0, "fp32"), (0, "fp64"), (2, "fp32"), (4, "fp32")])
+@pytest.mark.parametrize("cfg,precision", [("plain64", "fp32"), ("plain64", "fp64"), ("production88", "fp32"),
+                                           ("large128", "fp32")])
 def test_psf_cobj_residual(cfg, precision):
     w, s = _setup(cfg, precision)
     a = w.patches.alpha_true * 0.8
@@ -55,7 +57,7 @@ def test_psf_cobj_residual(cfg, precision):
 
 
 def test_psf_mean():
-    w, s = _setup(2, "fp32")
+    w, s = _setup("production88", "fp32")
     a = w.patches.alpha_true * 0.8
     fc = w.job.otf_size / 2.0
     each = s.restore_outputs(a, fc, psf="each")["psf"]
@@ -72,7 +74,7 @@ def test_psf_mean():
 
 def test_flag_errors():
     from redux_gb300 import _lib
-    w, s = _setup(0, "fp32")
+    w, s = _setup("plain64", "fp32")
     a = np.ascontiguousarray(w.patches.alpha_true, np.float64)
     fc = np.full(w.job.n_objects, 16.0)
     obj = np.zeros((1, w.job.n_objects, w.job.patch_size, w.job.patch_size), np.float32)

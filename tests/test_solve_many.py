@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _handles():
-    ws = [workload(0), workload(2, n_patches=2, frames=4), workload(4, n_patches=1, frames=2)]
+    ws = [workload("plain64"), workload("production88", n_patches=2, frames=4), workload("large128", n_patches=1, frames=2)]
     out = []
     for w in ws:
         s = S.Solver(w.job, max_patches=w.patches.cutouts.shape[0])
@@ -52,7 +52,7 @@ def test_handles_of_different_sizes_keep_their_shared_memory():
     big = synth.make_patches(big_job, 2, 15.0, np.random.default_rng(7))
     hb = S.Solver(big_job, max_patches=2)
     hb.set_patches(big.cutouts)
-    w0 = workload(0)
+    w0 = workload("plain64")
     hs = S.Solver(w0.job, max_patches=1)
     hs.set_patches(w0.patches.cutouts, None, w0.patches.fixed_gamma)
     st = S.fixed_iterations(big_job.n_modes, 2, max_metrics=64)

@@ -23,9 +23,9 @@ def _solver(w):
     return s
 
 
-@pytest.mark.parametrize("cfg", [0, 2])
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
 def test_noalloc_matches_metric_two_calls(cfg):
-    w = workload(0) if cfg == 0 else workload(2, n_patches=2, frames=4)
+    w = workload("plain64") if cfg == "plain64" else workload("production88", n_patches=2, frames=4)
     s = _solver(w)
     for scale in (0.5, 1.0):
         a = w.patches.alpha_true * scale
@@ -39,14 +39,14 @@ def test_noalloc_matches_metric_two_calls(cfg):
 
 def test_noalloc_rejects_batches_beyond_the_scratch():
     # 88 x 88, 12 images per patch: about 255 KB of temporaries per patch, 70 patches > 16 MiB
-    w = workload(2, n_patches=70, frames=4)
+    w = workload("production88", n_patches=70, frames=4)
     s = _solver(w)
     with pytest.raises(S.SolverError, match="static scratch holds"):
         s.metric_noalloc(w.patches.alpha_true)
     # the handle stays usable
     assert np.all(np.isfinite(s.metric(w.patches.alpha_true)))
     # and a batch that fits still agrees with rdxg_metric
-    small = workload(2, n_patches=2, frames=4)
+    small = workload("production88", n_patches=2, frames=4)
     s2 = _solver(small)
     np.testing.assert_allclose(s2.metric_noalloc(small.patches.alpha_true), s2.metric(small.patches.alpha_true),
                                rtol=TOL, atol=0)
