@@ -1,6 +1,6 @@
 """ctypes front-end of the FP64 CPU oracle (oracle.c).
 
-TEST INFRASTRUCTURE ONLY: the checker for the GPU solver.  Only tests/, the smoke
+TEST INFRASTRUCTURE ONLY: the GPU solver is tested against it.  Only tests/, the smoke
 check in __graft_entry__ and bench.py's CPU-baseline leg may use it.
 """
 from __future__ import annotations

@@ -1,9 +1,9 @@
 /*
  * oracle.c -- FP64 CPU restatement of redux's per-patch MOMFBD solver.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU solver in
- * redux_gb300: only tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline leg may load it.  The product never links, imports or calls it.
+ * TEST INFRASTRUCTURE ONLY.  The GPU solver in redux_gb300 is tested against this
+ * restatement: only tests/, __graft_entry__.smoke() and bench.py's CPU baseline leg may
+ * load it.  The product never links, imports or calls it.
  *
  * It restates, in plain C99 and double precision, the reference code of the
  * MOMFBD hot path (paths relative to the ISP-SST/redux tree):
