@@ -175,10 +175,14 @@ int rdxg_metric_with_reference(rdxg_solver* h, const double* alpha_ref, const do
  * otherwise RDXG_ERR_UNSUPPORTED), and a batch whose temporaries exceed 16 MiB (about 600 KB
  * per patch at N = 88 with 36 images and 36 modes, i.e. at most 26 such patches) is rejected
  * with RDXG_ERR_UNSUPPORTED and a message giving the sizes.  The handle's device must be the
- * current device.  The first call on each device looks up the array's address
- * (cudaGetSymbolAddress, cached afterwards); make that first call before any stream capture.
- * The scratch is shared by every handle on the device: calls that overlap in time (from two
- * threads, or on two streams) race on it and must be serialized by the caller. */
+ * current device.  rdxg_create looks up the array's address in the current context
+ * (cudaGetSymbolAddress) and keeps it in the handle; with lazy module loading that lookup is
+ * also what loads the array, so its 16 MiB are reserved when the handle is created and the
+ * call itself neither loads nor allocates anything.  The address belongs to the context the
+ * handle was created in (the device's primary context, as for every other call); a handle does
+ * not survive cudaDeviceReset.  The scratch is shared by every handle on the device: calls that
+ * overlap in time (from two threads, or on two streams) race on it and must be serialized by
+ * the caller. */
 int rdxg_metric_noalloc(rdxg_solver* h, const double* alpha, double* metric);
 
 /* Gradient in alpha space [P][I][M] at alpha (Solver::my_df without the constraint map,
@@ -281,9 +285,15 @@ int rdxg_get_launch_shape(const rdxg_solver* h, rdxg_launch_shape* shape);
  * which = 0 D [P][I][N][N] complex, 1 OTF [P][I][N][N] complex, 2 gamma [P][nObj],
  *         3 image stats [P][I][3] (mean, stddev, noise), 4 object O [P][nObj][N][N] complex,
  *         5 shifts [P][I][2] int32, 6 phases of the last fused evaluation [P][I][n][n] float
- *         (fused FP32 path only).  Complex values are float pairs in FP32 mode and double
- *         pairs in FP64 mode. */
+ *         (fused FP32 path only), 7 the number of device allocations the handle holds
+ *         (int64).  Complex values are float pairs in FP32 mode and double pairs in FP64 mode. */
 int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes);
+
+/* Debug writes of device state, to test error paths from the host without a device fault:
+ * which = 0 the tensor-core mode expansion's status word (int32; non-zero is what a bounded
+ * wait that gave up leaves behind: the next call that checks it returns RDXG_ERR_CUDA with the
+ * message, and clears it).  No counterpart in the reference. */
+int rdxg_debug_set(rdxg_solver* h, int32_t which, const void* in, size_t bytes);
 
 /* Host drop-in for redux's conjugate_rdx minimiser with the Solver::run stage loop
  * (conjugate_gradient.cpp:128-256, helpers.cpp:58-215, solver.cpp:425-537) driving

@@ -85,8 +85,97 @@ def lib():
         L.orc_set_initial_alpha.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_set_reg_alpha.argtypes = [C.c_void_p, C.c_void_p]
         L.orc_get_plane.argtypes = [C.c_void_p, f32p]
+        L.orc_cg_minimize.restype = C.c_int
+        L.orc_cg_minimize.argtypes = [C.c_int, C.c_int, C.POINTER(Cfg), C.c_double, F_CB, DF_CB, SHIFT_CB,
+                                      C.c_void_p, f64p, C.POINTER(Report), C.c_void_p, C.c_int]
         _LIB = L
     return _LIB
+
+
+# callbacks of orc_cg_minimize (and of the compiled reference minimiser in oracle/_ref)
+F_CB = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_void_p)
+DF_CB = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.c_int32, C.c_int32, C.POINTER(C.c_double), C.c_void_p)
+SHIFT_CB = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.c_void_p)
+
+
+def _wrap_callbacks(n_free, f, df, shift):
+    def cf(x, _u):
+        return float(f(np.ctypeslib.as_array(x, (n_free,)).copy()))
+
+    def cdf(x, method, mc, g, _u):
+        out = np.asarray(df(np.ctypeslib.as_array(x, (n_free,)).copy(), int(method), int(mc)), np.float64)
+        np.ctypeslib.as_array(g, (n_free,))[:] = out
+
+    def csh(x, _u):
+        if shift is not None:
+            shift(np.ctypeslib.as_array(x, (n_free,)).copy())
+
+    return F_CB(cf), DF_CB(cdf), SHIFT_CB(csh)
+
+
+class RefCfg(C.Structure):
+    _fields_ = [("mode_start", C.c_int32), ("mode_step", C.c_int32), ("max_iterations", C.c_int32),
+                ("min_iterations", C.c_int32), ("target_iterations", C.c_int32), ("fd_first", C.c_int32),
+                ("ftol", C.c_double), ("eps", C.c_double)]
+
+
+_REF = None
+REF_PATH = os.path.join(_HERE, "_ref", "libref_cg.so")
+
+
+def ref_available() -> bool:
+    """Whether the reference's own compiled minimiser (oracle/_ref/libref_cg.so) is there; it
+    is built from the reference's sources by `make -C oracle ref` (build() does this when the
+    reference tree is present)."""
+    return os.path.exists(REF_PATH)
+
+
+def build_ref() -> bool:
+    """Builds oracle/_ref/libref_cg.so when the reference tree is present; returns whether the
+    library exists afterwards."""
+    r = subprocess.run(["make", "-s", "-C", _HERE, "ref"], capture_output=True, text=True)
+    return r.returncode == 0 and ref_available()
+
+
+def ref_lib():
+    global _REF
+    if _REF is None:
+        L = C.CDLL(REF_PATH)
+        L.ref_cg_minimize.restype = C.c_int
+        L.ref_cg_minimize.argtypes = [C.c_int32, C.c_int32, C.POINTER(RefCfg), C.c_double, F_CB, DF_CB, SHIFT_CB,
+                                      C.c_void_p, f64p, C.POINTER(Report), C.c_void_p, C.c_int32]
+        _REF = L
+    return _REF
+
+
+def ref_cg_minimize(n_free, n_modes, cfg, grad_scale, f, df, shift=None, cap_metrics=100000):
+    """The reference's compiled conjugate_rdx minimiser with its bracket and brent
+    (src/lib/util/gsl/conjugate_gradient.cpp, src/lib/math/helpers.cpp) under the Solver::run
+    stage loop, on callbacks as cg_minimize.  cfg: an oracle Cfg (brent_tol is the reference's
+    fixed 0.1)."""
+    rc = RefCfg(mode_start=cfg.n_initial_modes, mode_step=cfg.n_mode_increment, max_iterations=cfg.max_iterations,
+                min_iterations=cfg.min_iterations, target_iterations=cfg.target_iterations, fd_first=cfg.fd_first,
+                ftol=cfg.ftol, eps=cfg.eps)
+    cbs = _wrap_callbacks(n_free, f, df, shift)
+    x = np.zeros(n_free)
+    rep = Report()
+    metrics = np.zeros(cap_metrics)
+    ref_lib().ref_cg_minimize(n_free, n_modes, C.byref(rc), grad_scale, cbs[0], cbs[1], cbs[2], None, x,
+                              C.byref(rep), metrics.ctypes.data, cap_metrics)
+    return dict(x=x, report=rep, metrics=metrics[:min(rep.n_metrics, cap_metrics)].copy())
+
+
+def cg_minimize(n_free, n_modes, cfg, grad_scale, f, df, shift=None, cap_metrics=100000):
+    """The oracle's sequential Solver::run + conjugate_rdx on callbacks (orc_cg_minimize):
+    f(x) -> metric, df(x, method, mode_count) -> gradient (method 1 finite differences, 2 Vogel),
+    shift(x) between mode stages.  Returns the final x, the report and the metric history."""
+    cbs = _wrap_callbacks(n_free, f, df, shift)
+    x = np.zeros(n_free)
+    rep = Report()
+    metrics = np.zeros(cap_metrics)
+    lib().orc_cg_minimize(n_free, n_modes, C.byref(cfg), grad_scale, cbs[0], cbs[1], cbs[2], None, x,
+                          C.byref(rep), metrics.ctypes.data, cap_metrics)
+    return dict(x=x, report=rep, metrics=metrics[:min(rep.n_metrics, cap_metrics)].copy())
 
 
 def fft2(a: np.ndarray, sign: int = -1) -> np.ndarray:

@@ -34,11 +34,15 @@
  * testsuite/image/fourier.cpp restated in tests/test_oracle_fft.py.
  *
  * Parity status: the FFT/autocorrelation/reorder conventions are pinned by the
- * reference's known-answer tests.  The reference has no tests for the metric,
- * gradient, CG or line search, and it cannot be built here (Boost, FFTW3, GSL
- * and OpenCV are absent), so those parts are "parity unpinned": they follow the
- * cited source line by line and are cross-checked against an independent
- * numpy restatement (oracle/np_oracle.py) and against finite differences.
+ * reference's known-answer tests.  The conjugate-gradient iteration, bracket and
+ * brent (and the Solver::run stage loop around them, orc_cg_minimize) are pinned
+ * bit for bit against the reference's own conjugate_gradient.cpp and helpers.cpp
+ * compiled from its sources into oracle/_ref (tests/test_ref_minimizer.py).  The
+ * reference has no tests for the metric or gradient and the rest of it cannot be
+ * built here (Boost, FFTW3, GSL and OpenCV are absent), so those parts are
+ * "parity unpinned": they follow the cited source line by line and are
+ * cross-checked against an independent numpy restatement (oracle/np_oracle.py)
+ * and against finite differences.
  */
 #include <complex.h>
 #include <math.h>
@@ -999,16 +1003,29 @@ void orc_cons_reverse_add(const orc_patch* p, const double* in, const double* of
 
 /* ---------------- the solver (Solver::run with conjugate_rdx) ---------------- */
 
+/* Callbacks of orc_cg_minimize: the same sequential solver on a caller's metric and gradient
+ * (in place of a patch), e.g. to inject failures. */
+typedef double (*orc_f_cb)(const double* x, void* user);
+typedef void (*orc_df_cb)(const double* x, int32_t method, int32_t mode_count, double* g, void* user);
+typedef void (*orc_shift_cb)(const double* x, void* user);
+
 typedef struct {
-    orc_patch* p;
+    orc_patch* p;     /* NULL when the callbacks below drive the solver */
     int gradMethod;   /* 1 FD, 2 Vogel */
     double* beta_tmp;
     double* metrics; int nMetrics; int capMetrics;
     int logEvals; double* evalLog; int nEval; int capEval; /* (kind, step, f) */
+    orc_f_cb cb_f; orc_df_cb cb_df; orc_shift_cb cb_shift; void* user;
+    int modeCount;    /* enabled modes of the current stage (passed to cb_df) */
+    int64_t cb_nf, cb_ndf;
 } solver_ctx;
 
 /* my_f: applyBeta + metric */
 static double my_f(solver_ctx* c, const double* b) {
+    if (c->cb_f) {
+        c->cb_nf++;
+        return c->cb_f(b, c->user);
+    }
     orc_patch* p = c->p;
     cons_reverse_add(p, b, p->alphaOffset, p->alpha);
     double f = orc_metric(p, p->alpha);
@@ -1017,6 +1034,11 @@ static double my_f(solver_ctx* c, const double* b) {
 
 /* my_df: applyBeta + calcPQ + gradient; grad in beta space */
 static void my_df(solver_ctx* c, const double* b, double* df) {
+    if (c->cb_df) {
+        c->cb_ndf++;
+        c->cb_df(b, c->gradMethod, c->modeCount, df, c->user);
+        return;
+    }
     orc_patch* p = c->p;
     cons_reverse_add(p, b, p->alphaOffset, p->alpha);
     apply_alpha(p, p->alpha);
@@ -1309,22 +1331,13 @@ static void shift_and_init(orc_patch* p, const double* a) {
     free(shifted);
 }
 
-/* Solver::run (solver.cpp:330-580) with GETSTEP = conjugate_gradient.
- * alpha_out: nPar; metrics_out: optional buffer of cap_metrics entries;
- * eval_log: optional (step, f) pairs of every line-search evaluation. */
-int orc_solve(orc_patch* p, const orc_cfg* cfg, double* alpha_out, orc_report* rep,
-              double* metrics_out, int cap_metrics, double* eval_log, int cap_eval) {
-    const int nFree = p->nFree, nPar = p->nPar, M = p->M;
-    solver_ctx c;
-    memset(&c, 0, sizeof(c));
-    c.p = p;
-    c.gradMethod = cfg->fd_first ? 1 : 2;
-    c.logEvals = eval_log != NULL;
-    p->n_f = p->n_df = 0;
-    memset(p->alpha, 0, sizeof(double) * (size_t)nPar);
-    memset(p->gradAlpha, 0, sizeof(double) * (size_t)nPar);
-    if (p->initAlpha) memcpy(p->alphaOffset, p->initAlpha, sizeof(double) * (size_t)nPar);
-    else memset(p->alphaOffset, 0, sizeof(double) * (size_t)nPar);
+/* The stage loop of Solver::run (solver.cpp:330-580) with GETSTEP = conjugate_gradient, on
+ * beta (n free parameters) of M modes.  With a patch it evaluates the patch (applyBeta, metric,
+ * gradient; shiftAndInit between stages); with callbacks it calls them.  Leaves the final
+ * point in x_out and returns the GSL status of the last iteration. */
+static int run_stages(solver_ctx* c, const orc_cfg* cfg, int nFree, int M, double gradScale, double* x_out,
+                      orc_report* rep) {
+    orc_patch* p = c->p;
     cg_state st;
     memset(&st, 0, sizeof(st));
     st.n = nFree;
@@ -1336,7 +1349,8 @@ int orc_solve(orc_patch* p, const orc_cfg* cfg, double* alpha_out, orc_report* r
     double* gradient = (double*)xcalloc((size_t)nFree, sizeof(double));
     double* dx = (double*)xcalloc((size_t)nFree, sizeof(double));
     double* beta_init = (double*)xcalloc((size_t)nFree, sizeof(double));
-    memset(p->enabled, 0, (size_t)M);
+    if (p) memset(p->enabled, 0, (size_t)M);
+    c->modeCount = 0;
     double sf = 0;
     double previousMetric = 0, thisMetric = 0, gradNorm = 0;
     double tol = 1.0E-1;
@@ -1344,14 +1358,14 @@ int orc_solve(orc_patch* p, const orc_cfg* cfg, double* alpha_out, orc_report* r
     int status = 0;
     /* loadInit: alpha_offset = the initial coefficients (zero without them);
      * shiftAndInit(alpha_offset, true) was done by orc_set_images. */
-    double initialMetric = my_f(&c, beta_init);
-    push_metric(&c, initialMetric);
-    const double nTotalPixels = (double)p->nImg * p->ps * p->ps;
-    const double gradScale = 1.0 / (nTotalPixels * nTotalPixels);
+    double initialMetric = my_f(c, beta_init);
+    push_metric(c, initialMetric);
     int exitLoop = 0;
     for (int modeCount = cfg->n_initial_modes; !exitLoop; modeCount += cfg->n_mode_increment) {
         if (modeCount > M) modeCount = M;
-        for (int m = 0; m < modeCount; ++m) p->enabled[m] = 1;
+        if (p)
+            for (int m = 0; m < modeCount; ++m) p->enabled[m] = 1;
+        c->modeCount = modeCount;
         if (modeCount == M || cfg->max_iterations == 0) {
             exitLoop = 1;
             tol = cfg->ftol;
@@ -1361,22 +1375,22 @@ int orc_solve(orc_patch* p, const orc_cfg* cfg, double* alpha_out, orc_report* r
         memcpy(x, beta_init, sizeof(double) * (size_t)nFree);
         memset(dx, 0, sizeof(double) * (size_t)nFree);
         st.iter = 0;
-        sf = my_fdf(&c, x, gradient);
+        sf = my_fdf(c, x, gradient);
         int iter = 0, successCount = 0, done = 0;
         while ((!done || iter < cfg->min_iterations) && iter < maxIterations) {
             iter++;
-            status = cg_iterate(&c, &st, x, &sf, gradient, dx);
+            status = cg_iterate(c, &st, x, &sf, gradient, dx);
             if (failCount > maxFails) {
                 status = RDX_FAILURE;
                 exitLoop = 1;
                 done = 1;
                 break;
             }
-            c.gradMethod = 2;   /* switch to Vogel after the first iteration */
+            c->gradMethod = 2;   /* switch to Vogel after the first iteration */
             if (status == RDX_ENOPROG) { failCount++; break; }
             thisMetric = sf;
             if (!isfinite(thisMetric)) { failCount++; break; }
-            push_metric(&c, thisMetric);
+            push_metric(c, thisMetric);
             gradNorm = dnrm2(gradient, nFree) * gradScale;
             if (!isfinite(gradNorm)) { failCount++; break; }
             if (gradNorm < cfg->ftol) { exitLoop = 1; done = 1; break; }
@@ -1391,35 +1405,85 @@ int orc_solve(orc_patch* p, const orc_cfg* cfg, double* alpha_out, orc_report* r
             }
             previousMetric = thisMetric;
         }
-        thisMetric = my_f(&c, x);
+        thisMetric = my_f(c, x);
         totalIterations += iter;
         if (!exitLoop) {
-            shift_and_init(p, p->alpha);
-            memcpy(p->alphaOffset, p->alpha, sizeof(double) * (size_t)nPar);
+            if (p) {
+                shift_and_init(p, p->alpha);
+                memcpy(p->alphaOffset, p->alpha, sizeof(double) * (size_t)p->nPar);
+            } else if (c->cb_shift) {
+                c->cb_shift(x, c->user);
+            }
         }
     }
-    memcpy(alpha_out, p->alpha, sizeof(double) * (size_t)nPar);
+    memcpy(x_out, x, sizeof(double) * (size_t)nFree);
     if (rep) {
         rep->initial_metric = initialMetric;
         rep->final_metric = thisMetric;
         rep->iterations = totalIterations;
         rep->status = (status == RDX_FAILURE) ? 1 : 0;
-        rep->n_f_evals = (int32_t)p->n_f;
-        rep->n_df_evals = (int32_t)p->n_df;
+        rep->n_f_evals = (int32_t)(p ? p->n_f : c->cb_nf);
+        rep->n_df_evals = (int32_t)(p ? p->n_df : c->cb_ndf);
         rep->fail_count = failCount;
-        rep->n_metrics = c.nMetrics;
+        rep->n_metrics = c->nMetrics;
     }
-    if (metrics_out) {
-        int nm = c.nMetrics < cap_metrics ? c.nMetrics : cap_metrics;
-        memcpy(metrics_out, c.metrics, sizeof(double) * (size_t)nm);
-    }
-    if (eval_log) {
-        int ne = c.nEval < cap_eval ? c.nEval : cap_eval;
-        memcpy(eval_log, c.evalLog, sizeof(double) * 2 * (size_t)ne);
-    }
-    free(c.metrics); free(c.evalLog);
     free(st.x1); free(st.p); free(st.g0); free(st.dx);
     free(x); free(gradient); free(dx); free(beta_init);
+    return status;
+}
+
+static void copy_logs(solver_ctx* c, double* metrics_out, int cap_metrics, double* eval_log, int cap_eval) {
+    if (metrics_out) {
+        int nm = c->nMetrics < cap_metrics ? c->nMetrics : cap_metrics;
+        memcpy(metrics_out, c->metrics, sizeof(double) * (size_t)nm);
+    }
+    if (eval_log) {
+        int ne = c->nEval < cap_eval ? c->nEval : cap_eval;
+        memcpy(eval_log, c->evalLog, sizeof(double) * 2 * (size_t)ne);
+    }
+    free(c->metrics); free(c->evalLog);
+}
+
+/* Solver::run (solver.cpp:330-580) with GETSTEP = conjugate_gradient.
+ * alpha_out: nPar; metrics_out: optional buffer of cap_metrics entries;
+ * eval_log: optional (step, f) pairs of every line-search evaluation. */
+int orc_solve(orc_patch* p, const orc_cfg* cfg, double* alpha_out, orc_report* rep,
+              double* metrics_out, int cap_metrics, double* eval_log, int cap_eval) {
+    const int nFree = p->nFree, nPar = p->nPar;
+    solver_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.p = p;
+    c.gradMethod = cfg->fd_first ? 1 : 2;
+    c.logEvals = eval_log != NULL;
+    p->n_f = p->n_df = 0;
+    memset(p->alpha, 0, sizeof(double) * (size_t)nPar);
+    memset(p->gradAlpha, 0, sizeof(double) * (size_t)nPar);
+    if (p->initAlpha) memcpy(p->alphaOffset, p->initAlpha, sizeof(double) * (size_t)nPar);
+    else memset(p->alphaOffset, 0, sizeof(double) * (size_t)nPar);
+    const double nTotalPixels = (double)p->nImg * p->ps * p->ps;
+    double* x = (double*)xcalloc((size_t)nFree, sizeof(double));
+    const int status = run_stages(&c, cfg, nFree, p->M, 1.0 / (nTotalPixels * nTotalPixels), x, rep);
+    free(x);
+    /* the last evaluation (at the final point) left alpha = alpha_offset + N x */
+    memcpy(alpha_out, p->alpha, sizeof(double) * (size_t)nPar);
+    copy_logs(&c, metrics_out, cap_metrics, eval_log, cap_eval);
+    return status == RDX_FAILURE ? 1 : 0;
+}
+
+/* The same sequential solver on caller callbacks: f(x) the metric at beta = x, df(x, method,
+ * mode_count, g) the gradient in beta space (method 1 finite differences, 2 Vogel; the first
+ * mode_count modes enabled), shift(x) the re-shift between mode stages (may be NULL).  Writes
+ * the final x (n_free), the report and the metric history. */
+int orc_cg_minimize(int n_free, int n_modes, const orc_cfg* cfg, double grad_scale, orc_f_cb f, orc_df_cb df,
+                    orc_shift_cb shift, void* user, double* x_out, orc_report* rep, double* metrics_out,
+                    int cap_metrics) {
+    if (n_free < 1 || n_modes < 1 || !cfg || !f || !df || !x_out) return -2;
+    solver_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.gradMethod = cfg->fd_first ? 1 : 2;
+    c.cb_f = f; c.cb_df = df; c.cb_shift = shift; c.user = user;
+    const int status = run_stages(&c, cfg, n_free, n_modes, grad_scale, x_out, rep);
+    copy_logs(&c, metrics_out, cap_metrics, NULL, 0);
     return status == RDX_FAILURE ? 1 : 0;
 }
 

@@ -20,7 +20,7 @@ EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "r
             "rdxg_debug_copy", "rdxg_cg_minimize", "rdxg_profile_kernels", "rdxg_metric_with_reference",
             "rdxg_metric_noalloc", "rdxg_restore", "rdxg_restore_ex", "rdxg_set_phase_mode", "rdxg_phase_mode",
             "rdxg_autotune", "rdxg_set_launch_shape", "rdxg_get_launch_shape", "rdxg_set_fit_plane",
-            "rdxg_set_initial_alpha", "rdxg_set_reg_alpha")
+            "rdxg_set_initial_alpha", "rdxg_set_reg_alpha", "rdxg_debug_set")
 
 
 class Geometry(C.Structure):
@@ -98,6 +98,7 @@ def load(path: str = LIB_PATH):
     L.rdxg_last_launch_count.restype = C.c_int64
     L.rdxg_last_launch_count.argtypes = [vp]
     L.rdxg_debug_copy.argtypes = [vp, C.c_int32, vp, C.c_size_t]
+    L.rdxg_debug_set.argtypes = [vp, C.c_int32, vp, C.c_size_t]
     L.rdxg_set_phase_mode.argtypes = [vp, C.c_int32]
     L.rdxg_phase_mode.restype = C.c_int32
     L.rdxg_phase_mode.argtypes = [vp]

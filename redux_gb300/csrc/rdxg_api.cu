@@ -110,6 +110,9 @@ struct rdxg_solver {
     // REG_ALPHA: per-parameter weights [I][M] of 0.5 sum alpha^2 w (Solver::regAlphaWeights)
     std::vector<double> hRegW;
     double* dRegW = nullptr;
+    // rdxg_metric_noalloc: address of the library's static scratch in this handle's context,
+    // looked up when the handle is created (fused handles only)
+    void* dNoAlloc = nullptr;
 };
 
 namespace {
@@ -803,6 +806,12 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
     if (at && atoi(at) == 0) h->tune = 0;   // default shapes, no measurement
     const char* nf = getenv("RDXG_NO_FUSED");
     if (!r && !(nf && atoi(nf))) r = setup_fused(h, s);
+    if (!r && h->fused) {
+        // rdxg_metric_noalloc's static scratch: its address in this context, which also loads
+        // (and so reserves) it now rather than in that call
+        cudaError_t ne = noalloc_scratch(&h->dNoAlloc);
+        if (ne != cudaSuccess) { h->err = std::string("static scratch: ") + cudaGetErrorString(ne); r = RDXG_ERR_CUDA; }
+    }
     // RDXG_SHAPES="eval,forward,adjoint" (threads per block, 0 = default) pins the launch
     // shapes, e.g. for profiling runs, where the planner's timing would be distorted
     const char* shp = getenv("RDXG_SHAPES");
@@ -954,8 +963,8 @@ int rdxg_metric_noalloc(rdxg_solver* h, const double* alpha, double* metric) {
         h->err = "rdxg_metric_noalloc: the handle's device must be the current device";
         return RDXG_ERR_STATE;
     }
-    void* base = nullptr;
-    CK(h, noalloc_scratch(dev, &base));
+    void* base = h->dNoAlloc;
+    if (!base) { h->err = "rdxg_metric_noalloc: the static scratch was not found"; return RDXG_ERR_STATE; }
     // carve the scratch into 256-byte aligned sections
     const size_t P = (size_t)h->P, G = P * h->I, PO = P * h->nObj, M = (size_t)h->M, n2 = (size_t)h->n * h->n;
     const size_t nH = (size_t)h->nH, cpp = (size_t)h->chunksPerPatch;
@@ -1706,6 +1715,20 @@ int rdxg_get_launch_shape(const rdxg_solver* h, rdxg_launch_shape* shape) {
     return RDXG_OK;
 }
 
+int rdxg_debug_set(rdxg_solver* h, int32_t which, const void* in, size_t bytes) {
+    if (!h || !in) return RDXG_ERR_ARG;
+    switch (which) {
+        case 0: {
+            // the tensor-core expansion's status word, as a wait that gave up leaves it
+            if (!h->dTcStatus || bytes != sizeof(int32_t)) return RDXG_ERR_ARG;
+            CK(h, cudaMemcpyAsync(h->dTcStatus, in, sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+            CK(h, cudaStreamSynchronize(h->stream));
+            return RDXG_OK;
+        }
+        default: return RDXG_ERR_ARG;
+    }
+}
+
 int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes) {
     if (!h || !out) return RDXG_ERR_ARG;
     const size_t G = (size_t)h->P * h->I, N2 = (size_t)h->N * h->N, PO = (size_t)h->P * h->nObj;
@@ -1731,6 +1754,12 @@ int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes) {
             const size_t nb = G * (size_t)h->n * h->n * sizeof(float);
             if (!h->fused || !h->dPhiImg || bytes < nb) return RDXG_ERR_ARG;
             CK(h, cudaMemcpy(out, h->dPhiImg, nb, cudaMemcpyDeviceToHost));
+            break;
+        }
+        case 7: {
+            if (bytes < sizeof(int64_t)) return RDXG_ERR_ARG;
+            const int64_t n = (int64_t)h->allocs.size();
+            std::memcpy(out, &n, sizeof(n));
             break;
         }
         default: return RDXG_ERR_ARG;

@@ -99,7 +99,7 @@ void launch_phase_tc(const PhaseTcArgs& a, const PhaseTcPlan& p, cudaStream_t st
 
 // rdxg_metric_noalloc: a fixed static device array holds every temporary of the evaluation
 constexpr size_t kNoAllocScratchBytes = (size_t)16 << 20;
-cudaError_t noalloc_scratch(int device, void** ptr);   // its address on a device (looked up once)
+cudaError_t noalloc_scratch(void** ptr);   // its address in the current context (loads the module)
 void launch_noalloc_alpha(const double* alpha, const double* curTilt, const double* resAlpha, int G, int M,
                           int tiltX, int tiltY, float* alphaEff, cudaStream_t st);
 void launch_noalloc_lists(int P, int nObj, const int32_t* objFirst, const int32_t* objCount, const int32_t* objChunk0,

@@ -1,7 +1,5 @@
 // Static scratch and helper kernels of rdxg_metric_noalloc: the metric evaluation with every
 // temporary in one file-scope device array instead of buffers of the handle.
-#include <mutex>
-
 #include "rdxg_launch.h"
 
 namespace rdxg {
@@ -11,20 +9,12 @@ namespace rdxg {
 // it must not overlap.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-cudaError_t noalloc_scratch(int device, void** ptr) {
-    constexpr int kMaxDevices = 64;
-    static void* cache[kMaxDevices] = {};
-    static std::mutex mu;
-    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(mu);
-    if (!cache[device]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        cache[device] = p;
-    }
-    *ptr = cache[device];
-    return cudaSuccess;
+cudaError_t noalloc_scratch(void** ptr) {
+    // The address in the current context.  Looking it up also loads this file's module if the
+    // runtime loads modules lazily, which is when the array's memory is reserved: rdxg_create
+    // calls this, so that reservation happens when the handle is made, not in a later call.
+    *ptr = nullptr;
+    return cudaGetSymbolAddress(ptr, g_noalloc_scratch);
 }
 
 // alphaEff = alpha with the tilt modes moved by the current tilt offset minus the residual

@@ -282,10 +282,18 @@ class Solver:
         spec = {"D": (0, (P, I, N, N), ct), "otf": (1, (P, I, N, N), ct), "gamma": (2, (P, nObj), np.float64),
                 "stats": (3, (P, I, 3), np.float64), "object": (4, (P, nObj, N, N), ct),
                 "shifts": (5, (P, I, 2), np.int32),
-                "phases": (6, (P, I, self.job.pupil_pixels, self.job.pupil_pixels), np.float32)}[which]
+                "phases": (6, (P, I, self.job.pupil_pixels, self.job.pupil_pixels), np.float32),
+                "allocations": (7, (1,), np.int64)}[which]
         out = np.zeros(spec[1], spec[2])
         self._check(_lib.load().rdxg_debug_copy(self.h, spec[0], _lib.ptr(out), out.nbytes), "rdxg_debug_copy")
         return out
+
+
+    def debug_set_tc_status(self, value: int) -> None:
+        """Writes the tensor-core expansion's status word (rdxg_debug_set 0), as a bounded wait
+        that gave up would leave it."""
+        v = np.array([value], np.int32)
+        self._check(_lib.load().rdxg_debug_set(self.h, 0, _lib.ptr(v), v.nbytes), "rdxg_debug_set")
 
 
 def solve_many(solvers, settings: SolveSettings, fetch: bool = True):

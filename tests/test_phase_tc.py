@@ -121,3 +121,46 @@ def test_mode_errors():
     with pytest.raises(S.SolverError, match="general path"):
         s64.set_phase_mode(3)
     assert s64.phase_mode() == 0
+
+
+# phases on the pupil support against FP64 phi_fixed + sum alpha Z (numpy), in rad: the
+# 6xBF16 split is at the level of FP32 rounding, 3xBF16 keeps ~2^-18 of each product
+TOL_PHASE_RAD = {0: 3e-5, 3: 3e-5, 2: 5e-4}
+
+
+@pytest.mark.parametrize("cfg", ["plain64", "production88"])
+def test_phases_against_fp64(cfg):
+    w = _w(cfg)
+    job = w.job
+    s = _solver(w)
+    a = w.patches.alpha_true
+    n2 = job.pupil_pixels ** 2
+    Z = job.modes.reshape(job.n_modes, n2)
+    pf = job.phi_fixed.reshape(-1, n2)[job.img_channel]              # [I][n2]
+    ref = np.einsum("pim,mq->piq", a, Z) + pf[None]
+    sup = np.asarray(job.pupil).ravel() > 0
+    errs = {}
+    for mode in (0, 2, 3):
+        s.set_phase_mode(mode)
+        s.metric(a)
+        ph = s.debug("phases").astype(np.float64).reshape(ref.shape)
+        errs[mode] = np.abs(ph - ref)[..., sup].max()
+    print(f"phase error vs FP64 on the pupil (rad): {errs}")
+    for mode, e in errs.items():
+        assert e <= TOL_PHASE_RAD[mode], (mode, e)
+    assert errs[3] <= errs[2]
+
+
+@pytest.mark.parametrize("word, what", [(1, "mode tile copy"), (2, "products")])
+def test_status_word_reported_once(word, what):
+    """A bounded wait of the tensor-core kernel that gives up leaves a status word; the host
+    reports it as an error on the next call and clears it.  The word is written from the host
+    (no wait is made to run out on the GPU)."""
+    w = _w("plain64")
+    s = _solver(w)
+    a = w.patches.alpha_true * 0.5
+    ok = s.metric(a)
+    s.debug_set_tc_status(word)
+    with pytest.raises(S.SolverError, match=what):
+        s.metric(a)
+    np.testing.assert_allclose(s.metric(a), ok, rtol=1e-6)    # cleared, the handle still works

@@ -37,6 +37,30 @@ def test_noalloc_matches_metric_two_calls(cfg):
         np.testing.assert_allclose(second, first, rtol=TOL, atol=0)
 
 
+def _free_device_bytes():
+    # cudaMemGetInfo of the current device (torch.cuda.mem_get_info); the test makes no torch
+    # allocation in between
+    import torch
+    free, _ = torch.cuda.mem_get_info()
+    return free
+
+
+def test_noalloc_allocates_nothing():
+    """The entry point's defining property: neither the handle nor the device gains memory over
+    its first and second call (the static scratch is reserved when the handle is created)."""
+    w = workload("production88", n_patches=2, frames=4)
+    s = _solver(w)
+    a = w.patches.alpha_true * 0.5
+    n0 = int(s.debug("allocations")[0])
+    free0 = _free_device_bytes()
+    first = s.metric_noalloc(a)
+    second = s.metric_noalloc(a)
+    free1 = _free_device_bytes()
+    assert int(s.debug("allocations")[0]) == n0
+    assert free1 == free0, (free0, free1)
+    np.testing.assert_allclose(second, first, rtol=TOL, atol=0)
+
+
 def test_noalloc_rejects_batches_beyond_the_scratch():
     # 88 x 88, 12 images per patch: about 255 KB of temporaries per patch, 70 patches > 16 MiB
     w = workload("production88", n_patches=70, frames=4)
