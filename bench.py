@@ -229,6 +229,138 @@ def run_uneven(args):
         h.close()
 
 
+def _dist(v):
+    v = np.asarray(v, np.float64)
+    if v.size == 0:
+        return None
+    return {"n": int(v.size), "median": float(np.median(v)), "p90": float(np.percentile(v, 90)),
+            "min": float(v.min()), "max": float(v.max())}
+
+
+def run_convergence(args):
+    """Converged parity on the production batch (225 patches 88 x 88, 36 KL modes, 3 x 12
+    images): every patch solved to convergence (all modes at once, FTOL on the relative metric
+    change, at least 5 iterations, 3 consecutive changes below FTOL) in FP32 and in FP64, and:
+      * FP64 continuation: an FP64 handle takes each FP32 solution as its starting point (same
+        images, rdxg_set_start_alpha) and solves on with the same settings; the relative
+        metric drop it still finds says whether FP32 stopped at an FP64-converged point;
+      * the same continuation from the FP64 solutions (the control: how far FP64's own
+        converged points are from converged);
+      * the signed difference of the FP32 and FP64 converged metrics (both evaluated in
+        FP64) and, as the noise floor of the problem, of the FP64 GPU and the FP64 oracle on a
+        sample of patches (two FP64 implementations that differ only in rounding order).
+    Not the headline line: `python bench.py --workload convergence`."""
+    import torch
+    from redux_gb300 import solver as S
+    torch.cuda.set_device(0)
+    job, cut = workload(args.patches, args.frames, args.iterations)
+    P, M = cut.shape[0], job.n_modes
+    lam = job.wavelength
+    conv = S.SolveSettings(mode_start=M, mode_step=M, max_iterations=args.conv_max_iterations, min_iterations=5,
+                           target_iterations=3, ftol=args.conv_ftol, max_metrics=args.conv_max_iterations + 16)
+
+    def timed(s, settings):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = s.run(settings)
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    # FP32 (the chosen form), the whole batch in one handle; one warm-up solve (launch planner,
+    # graph capture)
+    s32 = S.Solver(job, max_patches=P)
+    s32.set_patches(cut)
+    s32.run(conv)
+    s32.set_patches(cut)
+    o32, t32 = timed(s32, conv)
+    a32 = o32["alpha"]
+    it32 = [r.iterations for r in o32["reports"]]
+    # FP64, the whole batch in one handle
+    s64 = S.Solver(job, max_patches=P, precision="fp64")
+    s64.set_patches(cut)
+    L64_at32 = s64.metric(a32)
+    o64, t64 = timed(s64, conv)
+    a64 = o64["alpha"]
+    L64 = np.array([r.final_metric for r in o64["reports"]])
+    it64 = [r.iterations for r in o64["reports"]]
+    # continuations in FP64 from both endpoints
+    s64.set_start_alpha(a32)
+    oc32, tc32 = timed(s64, conv)
+    s64.set_start_alpha(a64)
+    oc64, _ = timed(s64, conv)
+    s64.set_start_alpha(None)
+
+    def drops(o):
+        return [(r.initial_metric - r.final_metric) / abs(r.initial_metric) for r in o["reports"]]
+
+    drop32, drop64 = drops(oc32), drops(oc64)
+    init_check = float(np.max(np.abs(np.array([r.initial_metric for r in oc32["reports"]]) - L64_at32)
+                              / np.abs(L64_at32)))
+    signed = (L64_at32 - L64) / np.abs(L64)
+    rms = lambda a, b: np.sqrt(np.mean((a - b) ** 2, axis=(1, 2))) / lam
+    # plain FP64 GPU form (one patch per launch sequence) on a sample, for the speed ratio
+    nplain = min(4, P)
+    s1 = S.Solver(job, max_patches=1, precision="fp64")
+    t_plain = 0.0
+    for p in range(nplain):
+        s1.set_patches(cut[p:p + 1])
+        _, t = timed(s1, conv)
+        t_plain += t
+    s1.close()
+    # noise floor: the FP64 oracle (CPU) on a sample, same settings
+    import oracle
+    threads = os.cpu_count() or 1
+    noise, f32_vs_oracle = [], []
+    t_or = 0.0
+    for p in range(min(args.conv_oracle_patches, P)):
+        op = oracle.OraclePatch(job, threads=threads)
+        op.set_images(cut[p], None, None)
+        cfg = oracle.Cfg(n_initial_modes=M, n_mode_increment=M, max_iterations=conv.max_iterations,
+                         min_iterations=conv.min_iterations, target_iterations=conv.target_iterations,
+                         fd_first=1, ftol=conv.ftol, eps=conv.eps, brent_tol=0.1)
+        t0 = time.perf_counter()
+        ro = op.solve(cfg)
+        t_or += time.perf_counter() - t0
+        Lo = ro["report"].final_metric
+        noise.append((L64[p] - Lo) / abs(Lo))
+        f32_vs_oracle.append((L64_at32[p] - Lo) / abs(Lo))
+    line = {"metric": "converged patches/s, FP32 against FP64 (continuation drop <= 1e-5)",
+            "value": P / t32, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": t32 * 1000.0,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (FP64 sums and CG scalars)", "data": "synthetic",
+            "config": {"workload": f"{P} patches 88x88, 36 KL modes, 3ch x {args.frames} frames, D/r0=15, "
+                                   f"all modes at once, FTOL {args.conv_ftol:g} (3 consecutive), MIN_ITER 5, "
+                                   f"MAX_ITER {args.conv_max_iterations}"},
+            "fp32": {"patches_per_s": P / t32, "iterations": _dist(it32)},
+            "fp64_batch": {"patches_per_s": P / t64, "iterations": _dist(it64)},
+            "plain_fp64_gpu": {"patches_per_s": nplain / t_plain, "sample": f"{nplain} patches, per-patch launches"},
+            "speedup_fp32_vs_plain_fp64": (P / t32) / (nplain / t_plain),
+            "continuation_from_fp32": {
+                "rel_metric_drop": _dist(drop32),
+                "within_1e-5": int(sum(1 for d in drop32 if d <= 1e-5)),
+                "within_1e-6": int(sum(1 for d in drop32 if d <= 1e-6)),
+                "alpha_moved_rms_rad": _dist(rms(oc32["alpha"], a32)),
+                "iterations": _dist([r.iterations for r in oc32["reports"]]),
+                "start_metric_vs_fp64_at_fp32_alpha_max_rel": init_check,
+                "seconds": tc32},
+            "continuation_from_fp64": {
+                "rel_metric_drop": _dist(drop64),
+                "within_1e-5": int(sum(1 for d in drop64 if d <= 1e-5)),
+                "within_1e-6": int(sum(1 for d in drop64 if d <= 1e-6))},
+            "fp32_minus_fp64_final_rel": {"signed": _dist(signed), "abs": _dist(np.abs(signed)),
+                                           "within_1e-5": int(np.sum(np.abs(signed) <= 1e-5)),
+                                           "fp32_lower": int(np.sum(signed < 0)),
+                                           "alpha_rms_rad": _dist(rms(a32, a64))},
+            "noise_floor_fp64_gpu_minus_oracle_rel": {"signed": noise, "fp32_minus_oracle": f32_vs_oracle,
+                                                      "oracle_seconds": t_or, "oracle_threads": threads}}
+    print(json.dumps(line), flush=True)
+    if args.conv_save:
+        np.savez(args.conv_save, a32=a32, a64=a64, ac32=oc32["alpha"], ac64=oc64["alpha"], L64_at32=L64_at32,
+                 L64=L64, drop32=drop32, drop64=drop64, it32=it32, it64=it64)
+    s32.close()
+    s64.close()
+
+
 def run_large(args):
     """Large patches, mixed precision: 128 x 128 patches, 3 channels x 32
     frames, 100 KL modes at D/r0 = 25; mode expansion on the CUDA cores in FP32 (the tensor-core
@@ -353,9 +485,15 @@ def main():
     ap.add_argument("--no-baselines", action="store_true")
     ap.add_argument("--handles", type=int, default=3,
                     help="handles (each on its own stream) the batch is split over, solved together")
-    ap.add_argument("--workload", default="production", choices=("production", "uneven", "large"),
+    ap.add_argument("--workload", default="production", choices=("production", "uneven", "large", "convergence"),
                     help="production: the headline batch (225 patches 88 x 88); uneven: 400 patches of "
-                         "{64, 88, 128} px; large: 256 patches 128 x 128 with 100 modes")
+                         "{64, 88, 128} px; large: 256 patches 128 x 128 with 100 modes; convergence: the "
+                         "headline batch solved to convergence in FP32 and FP64 with FP64 continuations")
+    ap.add_argument("--conv-ftol", type=float, default=1e-6, help="convergence: FTOL")
+    ap.add_argument("--conv-max-iterations", type=int, default=2000, help="convergence: MAX_ITER")
+    ap.add_argument("--conv-oracle-patches", type=int, default=4,
+                    help="convergence: patches also solved by the FP64 oracle (noise floor)")
+    ap.add_argument("--conv-save", default="", help="convergence: write the coefficients to this .npz")
     ap.add_argument("--levels", type=int, default=3,
                     help="uneven batch: frames and modes from this many values (0: uniform draws)")
     ap.add_argument("--check-iterations", type=int, default=10,
@@ -373,6 +511,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank)
+    if args.workload == "convergence":
+        return run_convergence(args)
     if args.workload == "uneven":
         return run_uneven(args)
     if args.workload == "large":

@@ -144,6 +144,14 @@ int rdxg_set_patches_device(rdxg_solver* h, int32_t n_patches, const float* d_cu
  * coefficients.  Call after rdxg_set_patches / rdxg_set_patches_device (which start at zero). */
 int rdxg_set_initial_alpha(rdxg_solver* h, const double* alpha);
 
+/* Continuation: every following solve starts from the coefficients [P][I][M] (as
+ * alpha_offset, beta = 0) with the images as loaded, not re-cut -- the next iterations of a
+ * solve whose images were never re-shifted (all modes at once), e.g. an FP64 handle taking
+ * over an FP32 solution.  NULL starts at zero again.  The reference's Solver::run continues
+ * within one stage the same way (alpha_offset fixed, beta from zero, solver.cpp:446); it
+ * has no entry point for it. */
+int rdxg_set_start_alpha(rdxg_solver* h, const double* alpha);
+
 /* REG_ALPHA: weights [I][M] (the same for every patch) of the regularisation term
  * 0.5 sum alpha^2 w that Solver::metric adds to the metric (solver.cpp:804-811), the
  * reference's Solver::regAlphaWeights = REG_ALPHA / wavelength * nTotalPixels / atm_rms^2

@@ -106,6 +106,7 @@ struct rdxg_solver {
     double* dPlane = nullptr;
     // warm start: the initial coefficients of the loaded patches [P][I][M] (loadInit)
     bool haveInit = false;
+    bool initRecut = true;           // false: rdxg_set_start_alpha (the images stay as loaded)
     double* dInitAlpha = nullptr;
     // REG_ALPHA: per-parameter weights [I][M] of 0.5 sum alpha^2 w (Solver::regAlphaWeights)
     std::vector<double> hRegW;
@@ -445,7 +446,7 @@ int prepare_patches(rdxg_solver* h) {
     CK(h, cudaMemsetAsync(h->dShift, 0, G * 2 * sizeof(int32_t), h->stream));
     CK(h, cudaMemsetAsync(h->dCurTilt, 0, G * 2 * sizeof(double), h->stream));
     CK(h, cudaMemcpyAsync(h->dResAlpha, h->hResAlpha.data(), G * 2 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    if (h->haveInit) {
+    if (h->haveInit && h->initRecut) {
         // Solver::shiftAndInit(alpha_offset, true) after loadInit (solver.cpp:412-413): every
         // image's window follows the tilts of the initial coefficients (SubImage::adjustShifts)
         CK(h, cudaMemcpyAsync(h->dAlpha, h->dInitAlpha, G * h->M * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
@@ -866,7 +867,9 @@ int rdxg_set_reg_alpha(rdxg_solver* h, const double* weights) {
     return RDXG_OK;
 }
 
-int rdxg_set_initial_alpha(rdxg_solver* h, const double* alpha) {
+extern "C++" {
+namespace {
+int set_start(rdxg_solver* h, const double* alpha, bool recut) {
     if (!h) return RDXG_ERR_ARG;
     if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
     if (alpha) {
@@ -878,8 +881,15 @@ int rdxg_set_initial_alpha(rdxg_solver* h, const double* alpha) {
                               h->stream));
     }
     h->haveInit = alpha != nullptr;
+    h->initRecut = recut;
     return prepare_patches(h);
 }
+}  // namespace
+}  // extern "C++"
+
+int rdxg_set_initial_alpha(rdxg_solver* h, const double* alpha) { return set_start(h, alpha, true); }
+
+int rdxg_set_start_alpha(rdxg_solver* h, const double* alpha) { return set_start(h, alpha, false); }
 
 int rdxg_set_stream(rdxg_solver* h, void* st) {
     if (!h) return RDXG_ERR_ARG;

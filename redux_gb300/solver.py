@@ -147,6 +147,15 @@ class Solver:
         a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
         self._check(_lib.load().rdxg_set_initial_alpha(self.h, _lib.ptr(a)), "rdxg_set_initial_alpha")
 
+    def set_start_alpha(self, alpha=None) -> None:
+        """Continuation: every following solve starts from these coefficients [P][I][M] with the
+        images as loaded (not re-cut), e.g. an FP64 handle continuing an FP32 solution."""
+        if alpha is None:
+            self._check(_lib.load().rdxg_set_start_alpha(self.h, None), "rdxg_set_start_alpha")
+            return
+        a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
+        self._check(_lib.load().rdxg_set_start_alpha(self.h, _lib.ptr(a)), "rdxg_set_start_alpha")
+
     def metric(self, alpha) -> np.ndarray:
         a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
         out = np.zeros(self.P)
