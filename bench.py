@@ -353,6 +353,43 @@ def run_convergence(args):
                                            "alpha_rms_rad": _dist(rms(a32, a64))},
             "noise_floor_fp64_gpu_minus_oracle_rel": {"signed": noise, "fp32_minus_oracle": f32_vs_oracle,
                                                       "oracle_seconds": t_or, "oracle_threads": threads}}
+    # restarted solves: each precision continues from its own endpoint (a CG restart: beta from
+    # zero, steepest descent first) until a whole restart cycle lowers no patch's metric by more
+    # than the restart tolerance; then both endpoints are compared again, in FP64
+    if args.conv_restarts > 0:
+        def restart_loop(s, a0, L0):
+            a, L = a0, np.asarray(L0, np.float64)
+            cycles, tot_it, t = 0, 0, 0.0
+            hist = []
+            for _ in range(args.conv_restarts):
+                s.set_start_alpha(a)
+                o, dt = timed(s, conv)
+                t += dt
+                cycles += 1
+                Ln = np.array([r.final_metric for r in o["reports"]])
+                tot_it += int(np.sum([r.iterations for r in o["reports"]]))
+                d = (L - Ln) / np.abs(L)
+                hist.append(float(np.max(d)))
+                a, L = o["alpha"], Ln
+                if np.max(d) <= args.conv_restart_tol:
+                    break
+            s.set_start_alpha(None)
+            return a, L, cycles, tot_it, t, hist
+        ra32, rL32, cyc32, tit32, rt32, h32 = restart_loop(s32, a32, [r.final_metric for r in o32["reports"]])
+        ra64, rL64, cyc64, tit64, rt64, h64 = restart_loop(s64, a64, L64)
+        rL64_at32 = s64.metric(ra32)
+        rs = (rL64_at32 - rL64) / np.abs(rL64)
+        line["restarted"] = {
+            "restart_tol": args.conv_restart_tol,
+            "fp32": {"cycles": cyc32, "max_drop_per_cycle": h32, "extra_iterations_per_patch": tit32 / P,
+                     "seconds": rt32, "patches_per_s_total": P / (t32 + rt32)},
+            "fp64": {"cycles": cyc64, "max_drop_per_cycle": h64, "extra_iterations_per_patch": tit64 / P,
+                     "seconds": rt64, "patches_per_s_total": P / (t64 + rt64)},
+            "fp32_minus_fp64_final_rel": {"signed": _dist(rs), "abs": _dist(np.abs(rs)),
+                                           "within_1e-5": int(np.sum(np.abs(rs) <= 1e-5)),
+                                           "within_1e-4": int(np.sum(np.abs(rs) <= 1e-4)),
+                                           "fp32_lower": int(np.sum(rs < 0)),
+                                           "alpha_rms_rad": _dist(rms(ra32, ra64))}}
     print(json.dumps(line), flush=True)
     if args.conv_save:
         np.savez(args.conv_save, a32=a32, a64=a64, ac32=oc32["alpha"], ac64=oc64["alpha"], L64_at32=L64_at32,
@@ -494,6 +531,10 @@ def main():
     ap.add_argument("--conv-oracle-patches", type=int, default=4,
                     help="convergence: patches also solved by the FP64 oracle (noise floor)")
     ap.add_argument("--conv-save", default="", help="convergence: write the coefficients to this .npz")
+    ap.add_argument("--conv-restarts", type=int, default=0,
+                    help="convergence: restart cycles (continuations from the own endpoint) at most")
+    ap.add_argument("--conv-restart-tol", type=float, default=1e-6,
+                    help="convergence: stop restarting once no patch's metric drops by more than this")
     ap.add_argument("--levels", type=int, default=3,
                     help="uneven batch: frames and modes from this many values (0: uniform draws)")
     ap.add_argument("--check-iterations", type=int, default=10,

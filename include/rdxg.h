@@ -256,6 +256,21 @@ int64_t rdxg_last_launch_count(const rdxg_solver* h);
 int rdxg_set_phase_mode(rdxg_solver* h, int32_t mode);
 int32_t rdxg_phase_mode(const rdxg_solver* h);
 
+/* Recomputed transforms.  The reference keeps every image's pupil function and OTF
+ * (SubImage::PF, SubImage::OTF, subimage.hpp:156-158) from the metric evaluation to the
+ * gradient (calcVogelWeight, subimage.cpp:348-371).  With on = 1 the handle keeps neither: the
+ * gradient kernels form PF, its transform X and (where the evaluation keeps no full OTF, the
+ * fused FP32 path) the OTF again from the phases: 16 N^2 + 8 n^2 bytes per image in FP32
+ * (32 N^2 + 16 n^2 in FP64) are not held, and 8 N^2 more on the fused path, at the price of
+ * one or two more transforms per gradient image.  rdxg_create chooses it by itself when keeping the transforms
+ * of max_patches patches would exceed the device's free memory (RDXG_MEMORY_BUDGET in the
+ * environment: a budget in bytes for the handle instead; RDXG_RECOMPUTE=0/1 forces it).
+ * Results agree with the kept form to rounding (the general path bit for bit).  The
+ * restoration then holds the batch's OTFs only during its call.  rdxg_recompute returns the
+ * mode in use. */
+int rdxg_set_recompute(rdxg_solver* h, int32_t on);
+int32_t rdxg_recompute(const rdxg_solver* h);
+
 /* Times the per-image and per-object kernels on the loaded batch at the current point with
  * CUDA events on the handle's stream: ms[0] forward (metric evaluation), ms[1] per-object
  * accumulation, ms[2] forward (gradient evaluation, also keeps the transforms), ms[3]
@@ -294,7 +309,8 @@ int rdxg_get_launch_shape(const rdxg_solver* h, rdxg_launch_shape* shape);
  *         3 image stats [P][I][3] (mean, stddev, noise), 4 object O [P][nObj][N][N] complex,
  *         5 shifts [P][I][2] int32, 6 phases of the last fused evaluation [P][I][n][n] float
  *         (fused FP32 path only), 7 the number of device allocations the handle holds
- *         (int64).  Complex values are float pairs in FP32 mode and double pairs in FP64 mode. */
+ *         (int64), 8 their bytes (int64).  Complex values are float pairs in FP32 mode and
+ *         double pairs in FP64 mode. */
 int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes);
 
 /* Debug writes of device state, to test error paths from the host without a device fault:

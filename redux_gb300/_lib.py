@@ -20,7 +20,8 @@ EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "r
             "rdxg_debug_copy", "rdxg_cg_minimize", "rdxg_profile_kernels", "rdxg_metric_with_reference",
             "rdxg_metric_noalloc", "rdxg_restore", "rdxg_restore_ex", "rdxg_set_phase_mode", "rdxg_phase_mode",
             "rdxg_autotune", "rdxg_set_launch_shape", "rdxg_get_launch_shape", "rdxg_set_fit_plane",
-            "rdxg_set_initial_alpha", "rdxg_set_reg_alpha", "rdxg_debug_set", "rdxg_set_start_alpha")
+            "rdxg_set_initial_alpha", "rdxg_set_reg_alpha", "rdxg_debug_set", "rdxg_set_start_alpha",
+            "rdxg_set_recompute", "rdxg_recompute")
 
 
 class Geometry(C.Structure):
@@ -83,6 +84,9 @@ def load(path: str = LIB_PATH):
     L.rdxg_set_fit_plane.argtypes = [vp, C.c_int32]
     L.rdxg_set_initial_alpha.argtypes = [vp, vp]
     L.rdxg_set_start_alpha.argtypes = [vp, vp]
+    L.rdxg_set_recompute.argtypes = [vp, C.c_int32]
+    L.rdxg_recompute.restype = C.c_int32
+    L.rdxg_recompute.argtypes = [vp]
     L.rdxg_set_reg_alpha.argtypes = [vp, vp]
     L.rdxg_set_patches.argtypes = [vp, C.c_int32, vp, vp, vp]
     L.rdxg_set_patches_device.argtypes = [vp, C.c_int32, vp, vp, vp]

@@ -114,6 +114,15 @@ struct rdxg_solver {
     // rdxg_metric_noalloc: address of the library's static scratch in this handle's context,
     // looked up when the handle is created (fused handles only)
     void* dNoAlloc = nullptr;
+    // recomputed transforms: X and PF (and on the fused path S) are not kept per image; the
+    // gradient kernels form them again with one scratch slot of N^2 per resident block
+    bool recompute = false;
+    void* dXscr = nullptr;           // [nsmid * slotsPerSM][N*N] scratch tiles
+    int scrBlocks = 0;               // blocks of the persistent recomputing kernels
+    int nsmid = 0, slotsPerSM = 0;   // SM identifiers (%nsmid), slots per SM (occupancy)
+    unsigned* dSlotMask = nullptr;   // [nsmid] slots in use
+    int32_t* dRcStatus = nullptr;    // a block of a recomputing kernel found no free slot
+    size_t allocBytes = 0;           // device bytes the handle holds
 };
 
 namespace {
@@ -144,7 +153,22 @@ int dalloc(rdxg_solver* h, void** p, size_t bytes) {
         return RDXG_ERR_NOMEM;
     }
     h->allocs.push_back(*p);
+    h->allocBytes += bytes;
     return RDXG_OK;
+}
+
+// frees one allocation of the handle (bytes: its size, for the tally) and clears the pointer
+template <typename P>
+void dfree(rdxg_solver* h, P** p, size_t bytes) {
+    if (!*p) return;
+    for (auto it = h->allocs.begin(); it != h->allocs.end(); ++it)
+        if (*it == (void*)*p) {
+            cudaFree(*it);
+            h->allocs.erase(it);
+            h->allocBytes -= bytes ? bytes : 16;
+            break;
+        }
+    *p = nullptr;
 }
 
 template <typename P>
@@ -213,6 +237,13 @@ KParams<T> make_kparams(rdxg_solver* h) {
     k.gradP = h->dGradP; k.nGradP = h->dCounters + 2; k.fdP = h->dFdP; k.nFdP = h->dCounters + 3;
     k.shapeEval = h->shapeEval; k.shapeFwd = h->shapeFwd; k.shapeAdj = h->shapeAdj;
     k.plane = h->fitPlane ? h->dPlane : nullptr;
+    k.recompute = h->recompute ? 1 : 0;
+    k.phiImg = h->fused ? (const T*)h->dPhiImg : nullptr;
+    k.Xscr = (cx<T>*)h->dXscr;
+    k.scrBlocks = h->scrBlocks;
+    k.slotMask = h->dSlotMask;
+    k.slotsPerSM = h->slotsPerSM;
+    k.rcStatus = h->dRcStatus;
     return k;
 }
 
@@ -272,8 +303,19 @@ int setup_phase_tc(rdxg_solver* h, int parts) {
     return RDXG_OK;
 }
 
-// Reports (once) a wait of the tensor-core mode expansion that gave up.
+// Reports (once) a wait of the tensor-core mode expansion that gave up, or a block of the
+// recomputing kernels that found no scratch slot.
 int tc_check(rdxg_solver* h) {
+    if (h->dRcStatus) {
+        int32_t st = 0;
+        CK(h, cudaMemcpyAsync(&st, h->dRcStatus, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        if (st) {
+            CK(h, cudaMemsetAsync(h->dRcStatus, 0, sizeof(int32_t), h->stream));
+            h->err = "recomputed transforms: a gradient block found no free scratch slot";
+            return RDXG_ERR_CUDA;
+        }
+    }
     if (!h->dTcStatus) return RDXG_OK;
     int32_t st = 0;
     CK(h, cudaMemcpyAsync(&st, h->dTcStatus, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
@@ -372,8 +414,7 @@ int alloc_patch_buffers(rdxg_solver* h) {
     if ((r = dalloc_t(h, &h->dCut, G * h->cs * h->cs)) || (r = dalloc_t(h, &h->dShift, G * 2)) ||
         (r = dalloc_t(h, &h->dMean, G)) || (r = dalloc_t(h, &h->dStd, G)) || (r = dalloc_t(h, &h->dNoise, G)) ||
         (r = dalloc_t(h, &h->dRg, G)) || (r = dalloc(h, &h->dAlphaEff, G * h->M * sizeof(T))) ||
-        (r = dalloc(h, &h->dD, G * N2 * sizeof(cx<T>))) || (r = dalloc(h, &h->dS, G * N2 * sizeof(cx<T>))) ||
-        (r = dalloc(h, &h->dX, G * N2 * sizeof(cx<T>))) || (r = dalloc(h, &h->dPF, G * n2 * sizeof(cx<T>))) ||
+        (r = dalloc(h, &h->dD, G * N2 * sizeof(cx<T>))) ||
         (r = dalloc(h, &h->dO, PO * N2 * sizeof(cx<T>))) || (r = dalloc(h, &h->dQt, PO * N2 * sizeof(T))) ||
         (r = dalloc_t(h, &h->dGamma, PO)) || (r = dalloc_t(h, &h->dPartial, PO * h->nTiles)) ||
         (r = dalloc_t(h, &h->dGalpha, G * h->M)) || (r = dalloc_t(h, &h->dReq, P)) ||
@@ -386,6 +427,54 @@ int alloc_patch_buffers(rdxg_solver* h) {
         return r;
     CK(h, cudaMallocHost((void**)&h->hActive, sizeof(int32_t)));
     CK(h, cudaMemset(h->dReinit, 0, G));
+    return RDXG_OK;
+}
+
+// Bytes of the per-image transforms kept from an evaluation for the gradient kernels: X and PF
+// of every image, and S where it is needed only by them (the fused path, whose evaluation
+// keeps no full OTF otherwise); and of the scratch that replaces them when recomputed.
+size_t kept_transform_bytes(const rdxg_solver* h) {
+    const size_t G = (size_t)h->Pmax * h->I, cxs = h->fp64 ? 16 : 8;
+    const size_t N2 = (size_t)h->N * h->N, n2 = (size_t)h->n * h->n;
+    return G * cxs * (N2 + n2 + (h->fused ? N2 : 0));
+}
+size_t recompute_scratch_bytes(const rdxg_solver* h) {
+    return (size_t)h->nsmid * h->slotsPerSM * h->N * h->N * (h->fp64 ? 16 : 8) + (size_t)h->nsmid * sizeof(unsigned);
+}
+
+// Allocates (or frees) the kept transforms and the recomputation scratch for the mode chosen.
+int setup_transforms(rdxg_solver* h, bool recompute) {
+    const size_t G = (size_t)h->Pmax * h->I, cxs = h->fp64 ? 16 : 8;
+    const size_t N2 = (size_t)h->N * h->N, n2 = (size_t)h->n * h->n;
+    int r;
+    if (recompute) {
+        if (h->scrBlocks < 1) {
+            h->err = "recomputed transforms: the recomputing kernels do not fit this size's shared memory";
+            return RDXG_ERR_UNSUPPORTED;
+        }
+        dfree(h, &h->dX, G * N2 * cxs);
+        dfree(h, &h->dPF, G * n2 * cxs);
+        if (h->fused) dfree(h, &h->dS, G * N2 * cxs);
+        const size_t tiles = (size_t)h->nsmid * h->slotsPerSM * N2 * cxs;
+        if (!h->dXscr && (r = dalloc(h, &h->dXscr, tiles))) return r;
+        if (!h->dSlotMask) {
+            if ((r = dalloc_t(h, &h->dSlotMask, (size_t)h->nsmid))) return r;
+            CK(h, cudaMemsetAsync(h->dSlotMask, 0, (size_t)h->nsmid * sizeof(unsigned), h->stream));
+        }
+        if (!h->dRcStatus) {
+            if ((r = dalloc_t(h, &h->dRcStatus, 1))) return r;
+            CK(h, cudaMemsetAsync(h->dRcStatus, 0, sizeof(int32_t), h->stream));
+        }
+        CK(h, cudaStreamSynchronize(h->stream));
+    } else {
+        dfree(h, &h->dXscr, (size_t)h->nsmid * h->slotsPerSM * N2 * cxs);
+        dfree(h, &h->dSlotMask, (size_t)h->nsmid * sizeof(unsigned));
+        if (!h->dX && (r = dalloc(h, &h->dX, G * N2 * cxs))) return r;
+        if (!h->dPF && (r = dalloc(h, &h->dPF, G * n2 * cxs))) return r;
+    }
+    // the general path's per-object accumulation reads S in every round
+    if ((!recompute || !h->fused) && !h->dS && (r = dalloc(h, &h->dS, G * N2 * cxs))) return r;
+    h->recompute = recompute;
     return RDXG_OK;
 }
 
@@ -813,6 +902,39 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
         cudaError_t ne = noalloc_scratch(&h->dNoAlloc);
         if (ne != cudaSuccess) { h->err = std::string("static scratch: ") + cudaGetErrorString(ne); r = RDXG_ERR_CUDA; }
     }
+    if (!r) {
+        // Kept or recomputed transforms: recomputed when keeping X, PF (and on the fused path S)
+        // for every image would exceed the memory budget -- the device's free memory, or
+        // RDXG_MEMORY_BUDGET bytes for the whole handle; RDXG_RECOMPUTE=0/1 forces the choice.
+        with_size(h->N, h->fp64, [&](auto L, auto) { h->slotsPerSM = decltype(L)::recompute_occupancy(h->M); });
+        int32_t* dq = nullptr;
+        if ((r = dalloc_t(h, &dq, 1))) { *out = h; return r; }
+        const cudaError_t qe = query_nsmid(dq, &h->nsmid, h->stream);
+        dfree(h, &dq, sizeof(int32_t));
+        if (qe != cudaSuccess) { h->err = std::string("SM count: ") + cudaGetErrorString(qe); *out = h; return RDXG_ERR_CUDA; }
+        if (h->nsmid < h->numSMs) h->nsmid = h->numSMs;
+        // the persistent recomputing kernels (block = slot) run one wave of resident blocks
+        h->scrBlocks = h->slotsPerSM > 0 ? h->numSMs * h->slotsPerSM : 0;
+        const size_t G = (size_t)h->Pmax * h->I, cxs = h->fp64 ? 16 : 8;
+        const size_t S = h->fused ? 0 : G * (size_t)h->N * h->N * cxs;   // kept in both modes
+        const size_t keep = kept_transform_bytes(h), scr = recompute_scratch_bytes(h);
+        const char* mb = getenv("RDXG_MEMORY_BUDGET");
+        const char* rcEnv = getenv("RDXG_RECOMPUTE");
+        size_t budget = 0, freeB = 0, totalB = 0;
+        if (mb) budget = (size_t)strtoull(mb, nullptr, 10);
+        else if (cudaMemGetInfo(&freeB, &totalB) == cudaSuccess) budget = h->allocBytes + freeB;
+        bool want = budget > 0 && h->allocBytes + S + keep + ((size_t)64 << 20) > budget;
+        if (rcEnv) want = atoi(rcEnv) != 0;
+        if (want && h->scrBlocks > 0 && budget > 0 && h->allocBytes + S + scr > budget) {
+            char msg[256];
+            std::snprintf(msg, sizeof(msg), "the batch needs %zu bytes even with recomputed transforms; the budget is "
+                          "%zu bytes: fewer patches per handle", h->allocBytes + S + scr, budget);
+            h->err = msg;
+            r = RDXG_ERR_NOMEM;
+        } else {
+            r = setup_transforms(h, want && h->scrBlocks > 0);
+        }
+    }
     // RDXG_SHAPES="eval,forward,adjoint" (threads per block, 0 = default) pins the launch
     // shapes, e.g. for profiling runs, where the planner's timing would be distorted
     const char* shp = getenv("RDXG_SHAPES");
@@ -1058,8 +1180,36 @@ int rdxg_restore(rdxg_solver* h, const double* alpha, const double* frequency_cu
     return rdxg_restore_ex(h, alpha, frequency_cutoff, no_filter, 0, objects, nullptr, nullptr, nullptr);
 }
 
+extern "C++" {
+namespace {
+int restore_impl(rdxg_solver* h, const double* alpha, const double* frequency_cutoff, int32_t no_filter,
+                 int32_t outputs, float* objects, float* psf, float* cobj, float* res);
+}  // namespace
+}  // extern "C++"
+
 int rdxg_restore_ex(rdxg_solver* h, const double* alpha, const double* frequency_cutoff, int32_t no_filter,
                     int32_t outputs, float* objects, float* psf, float* cobj, float* res) {
+    if (!h) return RDXG_ERR_ARG;
+    // with recomputed transforms the fused path keeps no OTFs: the restoration holds them for
+    // the call
+    const size_t sBytes = (size_t)h->Pmax * h->I * h->N * h->N * sizeof(float2);
+    const bool tmpS = h->fused && !h->dS;
+    if (tmpS) {
+        const int r = dalloc(h, &h->dS, sBytes);
+        if (r) return r;
+    }
+    const int r = restore_impl(h, alpha, frequency_cutoff, no_filter, outputs, objects, psf, cobj, res);
+    if (tmpS) {
+        cudaStreamSynchronize(h->stream);
+        dfree(h, &h->dS, sBytes);
+    }
+    return r;
+}
+
+extern "C++" {
+namespace {
+int restore_impl(rdxg_solver* h, const double* alpha, const double* frequency_cutoff, int32_t no_filter,
+                 int32_t outputs, float* objects, float* psf, float* cobj, float* res) {
     if (!h || !alpha || !frequency_cutoff || !objects) return RDXG_ERR_ARG;
     if (outputs & ~(RDXG_RESTORE_PSF | RDXG_RESTORE_PSF_AVG | RDXG_RESTORE_COBJ | RDXG_RESTORE_RESIDUAL))
         return RDXG_ERR_ARG;
@@ -1125,6 +1275,8 @@ int rdxg_restore_ex(rdxg_solver* h, const double* alpha, const double* frequency
     CK(h, cudaStreamSynchronize(h->stream));
     return RDXG_OK;
 }
+}  // namespace
+}  // extern "C++"
 
 int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, int32_t method, double* grad,
                   double* metric) {
@@ -1512,6 +1664,14 @@ int32_t rdxg_phase_mode(const rdxg_solver* h) {
     return h->tcPlan.valid ? h->tcPlan.parts : 0;
 }
 
+int rdxg_set_recompute(rdxg_solver* h, int32_t on) {
+    if (!h || (on != 0 && on != 1)) return RDXG_ERR_ARG;
+    CK(h, cudaStreamSynchronize(h->stream));   // no kernel of the handle reads the buffers any more
+    return setup_transforms(h, on != 0);
+}
+
+int32_t rdxg_recompute(const rdxg_solver* h) { return h && h->recompute ? 1 : 0; }
+
 extern "C++" {
 namespace {
 
@@ -1746,7 +1906,11 @@ int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes) {
     CK(h, cudaStreamSynchronize(h->stream));
     switch (which) {
         case 0: if (bytes < G * N2 * cxs) return RDXG_ERR_ARG; CK(h, cudaMemcpy(out, h->dD, G * N2 * cxs, cudaMemcpyDeviceToHost)); break;
-        case 1: if (bytes < G * N2 * cxs) return RDXG_ERR_ARG; CK(h, cudaMemcpy(out, h->dS, G * N2 * cxs, cudaMemcpyDeviceToHost)); break;
+        case 1:
+            if (bytes < G * N2 * cxs) return RDXG_ERR_ARG;
+            if (!h->dS) { h->err = "the OTFs are not kept (recomputed transforms)"; return RDXG_ERR_STATE; }
+            CK(h, cudaMemcpy(out, h->dS, G * N2 * cxs, cudaMemcpyDeviceToHost));
+            break;
         case 2: if (bytes < PO * 8) return RDXG_ERR_ARG; CK(h, cudaMemcpy(out, h->dGamma, PO * 8, cudaMemcpyDeviceToHost)); break;
         case 3: {
             if (bytes < G * 3 * 8) return RDXG_ERR_ARG;
@@ -1769,6 +1933,12 @@ int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes) {
         case 7: {
             if (bytes < sizeof(int64_t)) return RDXG_ERR_ARG;
             const int64_t n = (int64_t)h->allocs.size();
+            std::memcpy(out, &n, sizeof(n));
+            break;
+        }
+        case 8: {
+            if (bytes < sizeof(int64_t)) return RDXG_ERR_ARG;
+            const int64_t n = (int64_t)h->allocBytes;
             std::memcpy(out, &n, sizeof(n));
             break;
         }

@@ -310,7 +310,8 @@ __device__ __forceinline__ void half_plane_core(cx<T>* a, cx<T>* b, const cx<T>*
 // folded into the chunk's accumulators.  On entry the phases of this image are in phiBuf;
 // phiNext (or null) is the next image's, fetched into phiBuf once the row pass has read it.
 template <typename T, int N, int THREADS>
-__device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phiBuf, const T* A, T c, int df,
+__device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phiBuf, const T* A, T c, int keepPX,
+                                           int keepS,
                                            cx<T>* PF, cx<T>* X, cx<T>* S, const cx<T>* __restrict__ Dg,
                                            cx<T>* a, cx<T>* b, const cx<T>* tw, const cx<T>* oh,
                                            Acc4<T>* acc, const uint16_t* hpos, const int* hidx, int nH) {
@@ -331,11 +332,11 @@ __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phi
                 sincos_t<T>(phiBuf[q], &sn, &cs);
                 pf = mkc<T>(amp * cs, amp * sn);
             }
-            if (df) PF[q] = pf;
+            if (keepPX) PF[q] = pf;
             return cscale<T>(pf, c);
         },
         [&](int e, int x, cx<T> v) {
-            if (df) X[e * N + x] = v;
+            if (keepPX) X[e * N + x] = v;
             return cnorm<T>(v);
         },
         [&] {
@@ -351,7 +352,7 @@ __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phi
             cp_async_commit();
         },
         [&] { cp_async_wait_all(); });
-    if (df) {
+    if (keepS) {
         // the full OTF from the half plane (S(-u) = conj S(u)) for the gradient kernels
         for (int h = threadIdx.x; h < nH; h += THREADS) {
             const cx<T> v = cscale<T>(a[hpos[h]], inv);
@@ -425,7 +426,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
         const int j = it.first + jj;
         const size_t g = (size_t)it.p * e.k.I + j;
         const int ch = e.k.imgCh[j];
-        eval_image<T, N, THREADS>(phiNext, phiBuf, amp, e.k.otfNorm[ch], it.df, e.k.PF + g * n2, e.k.X + g * N2,
+        // a gradient evaluation keeps PF, X and the full OTF for the gradient kernels, unless
+        // they recompute them (the OTF is still kept when a buffer for it is given)
+        eval_image<T, N, THREADS>(phiNext, phiBuf, amp, e.k.otfNorm[ch], it.df && !e.k.recompute,
+                                  it.df && e.k.S != nullptr, e.k.PF + g * n2, e.k.X + g * N2,
                                   e.k.S + g * N2, e.Dh + g * nH, s, s2, tw, oh, acc, hpos, e.hp.idx, nH);
         if (nextJj == 0) {
             __syncthreads();
@@ -450,7 +454,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
 // (about 221 KB at N = 88 with 3237 half-plane points);
 // X (62 KB per image) is read from L2 for every mode.
 // ----------------------------------------------------------------------------------
-template <typename T, int N, int THREADS>
+template <typename T, int N, int THREADS, bool RC>
 __global__ void __launch_bounds__(THREADS, 1) k_fd_half(EvalParams<T> e) {
     constexpr int LDS = Tile<N>::LDS;
     constexpr int n = N / 2, n2 = n * n, N2 = N * N;
@@ -490,9 +494,40 @@ __global__ void __launch_bounds__(THREADS, 1) k_fd_half(EvalParams<T> e) {
         const T c = kp.otfNorm[kp.imgCh[j]];
         const double hstep = kp.objGradStep[o];
         __syncthreads();    // previous image's staged factors consumed
+        const cx<T>* Xg = kp.X + g * N2;
+        if constexpr (RC) {
+            // recomputed transforms: c PF from the evaluation's phases, X = fft(c PF) into the
+            // block's scratch, N^2 S = ifft|X|^2 in tile b (un-centred)
+            cx<T>* Xw = kp.Xscr + (size_t)blockIdx.x * N2;
+            Xg = Xw;
+            for (int i = threadIdx.x; i < Tile<N>::ELEMS; i += THREADS) a[i] = mkc<T>(0, 0);
+            __syncthreads();
+            for (int q = threadIdx.x; q < n2; q += THREADS) {
+                const T amp = kp.A[q];
+                cx<T> pf = mkc<T>(0, 0);
+                if (amp > (T)0) {
+                    T sn, cs;
+                    sincos_t<T>(e.phi[g * n2 + q], &sn, &cs);
+                    pf = mkc<T>(amp * cs, amp * sn);
+                }
+                pfs[q] = cscale<T>(pf, c);
+                a[(q / n + n / 2) * LDS + q % n + n / 2] = pfs[q];
+            }
+            __syncthreads();
+            fft2d_pp<T, N, -1, THREADS, true>(a, b, tw);
+            for (int i = threadIdx.x; i < N2; i += THREADS) {
+                const cx<T> X = a[(i / N) * LDS + i % N];
+                Xw[i] = X;
+                b[(i / N) * LDS + i % N] = mkc<T>(cnorm<T>(X), 0);
+            }
+            __syncthreads();
+            fft2d_pp<T, N, +1, THREADS, false>(b, a, tw);
+        } else {
+            for (int q = threadIdx.x; q < n2; q += THREADS) pfs[q] = cscale<T>(kp.PF[g * n2 + q], c);
+        }
         for (int h = threadIdx.x; h < nH; h += THREADS) {
             const int cidx = e.hp.idx[h];
-            const cx<T> S = kp.S[g * N2 + cidx];
+            const cx<T> S = RC ? cscale<T>(b[hpos[h]], inv) : kp.S[g * N2 + cidx];
             const cx<T> D = kp.D[g * N2 + cidx];
             const cx<T> O = kp.O[po * N2 + cidx];
             const T Q = kp.Qt[po * N2 + cidx];
@@ -502,8 +537,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_fd_half(EvalParams<T> e) {
             hq[h] = (cidx == (N / 2) * N + N / 2) ? (T)-1 : Q;
             hb[h] = cnorm<T>(D) - Q * cnorm<T>(O);
         }
-        for (int q = threadIdx.x; q < n2; q += THREADS) pfs[q] = cscale<T>(kp.PF[g * n2 + q], c);
-        const cx<T>* Xg = kp.X + g * N2;
         for (int m = 0; m < kp.M; ++m) {
             if (m >= mc) {
                 if (threadIdx.x == 0) ga[m] = 0.0;

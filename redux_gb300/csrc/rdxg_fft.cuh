@@ -363,9 +363,13 @@ __device__ __forceinline__ void fft2d_any(cx<T>* a, cx<T>* b, const cx<T>* tw) {
 // 2-D transform whose output is only needed on rows [N/4, 3N/4): columns first, then the
 // needed rows.
 template <typename T, int N, int DIR, int THREADS>
+__device__ __forceinline__ void fft2d_out_rows_pruned(cx<T>* s, const cx<T>* tw, int tid) {
+    fft_lines<T, N, DIR, N, false, THREADS>(s, 0, tw, tid);
+    fft_lines<T, N, DIR, N / 2, true, THREADS>(s, N / 4, tw, tid);
+}
+template <typename T, int N, int DIR, int THREADS>
 __device__ __forceinline__ void fft2d_out_rows_pruned(cx<T>* s, const cx<T>* tw) {
-    fft_lines<T, N, DIR, N, false, THREADS>(s, 0, tw, (int)threadIdx.x);
-    fft_lines<T, N, DIR, N / 2, true, THREADS>(s, N / 4, tw, (int)threadIdx.x);
+    fft2d_out_rows_pruned<T, N, DIR, THREADS>(s, tw, (int)threadIdx.x);
 }
 
 }  // namespace rdxg

@@ -26,6 +26,21 @@ static size_t smem_pp(int M) {
            (size_t)(Tile<N>::ELEMS + N) * sizeof(cx<T>) + extra_smem<T, N>(M);
 }
 
+// shared memory of the recomputing adjoint: tile [| X tile] | twiddles | PF | projection
+// weights | alpha
+template <typename T, int N>
+static size_t adjoint_rc_smem(int M) {
+    constexpr size_t n2 = (size_t)(N / 2) * (N / 2);
+    constexpr size_t tiles = PingPong<T, N>::value ? 2 : 1;
+    return (size_t)(tiles * Tile<N>::ELEMS + N + n2) * sizeof(cx<T>) + (n2 + (size_t)M) * sizeof(T) + 16;
+}
+// ... of the recomputing finite-difference gradient: k_fd's | PF | alpha
+template <typename T, int N>
+static size_t fd_rc_smem(int M) {
+    constexpr size_t n2 = (size_t)(N / 2) * (N / 2);
+    return ((fd_base_smem<T, N>() + 15) & ~(size_t)15) + n2 * sizeof(cx<T>) + (size_t)M * sizeof(T) + 16;
+}
+
 template <typename T, int N>
 cudaError_t Launcher<T, N>::setup(int M) {
     const int sm = (int)smem_pp<T, N>(M);
@@ -34,12 +49,33 @@ cudaError_t Launcher<T, N>::setup(int M) {
     if ((e = raise_smem_limit(k_forward<T, N, THREADS>, sm))) return e;
     if ((e = raise_smem_limit(k_adjoint<T, N, THREADS>, sm))) return e;
     if ((e = raise_smem_limit(k_fd<T, N, THREADS>, sm))) return e;
+    const size_t arc = adjoint_rc_smem<T, N>(M), frc = fd_rc_smem<T, N>(M);
+    if (arc <= kMaxSmem && (e = raise_smem_limit(k_adjoint_rc<T, N, THREADS, false>, arc))) return e;
+    if (frc <= kMaxSmem && (e = raise_smem_limit(k_fd_rc<T, N, THREADS>, frc))) return e;
     if constexpr (HasAlt<T>::value) {
         constexpr int ALT = ThreadsAlt<N>::value;
         if ((e = raise_smem_limit(k_forward<T, N, ALT>, sm))) return e;
         if ((e = raise_smem_limit(k_adjoint<T, N, ALT>, sm))) return e;
+        if (arc <= kMaxSmem && (e = raise_smem_limit(k_adjoint_rc<T, N, ALT, false>, arc))) return e;
+    }
+    if constexpr (PingPong<T, N>::value) {
+        // the fused path recomputes S too
+        if (arc <= kMaxSmem && (e = raise_smem_limit(k_adjoint_rc<T, N, THREADS, true>, arc))) return e;
+        if (arc <= kMaxSmem && (e = raise_smem_limit(k_adjoint_rc<T, N, ThreadsAlt<N>::value, true>, arc))) return e;
     }
     return cudaSuccess;
+}
+
+template <typename T, int N>
+int Launcher<T, N>::recompute_occupancy(int M) {
+    if (adjoint_rc_smem<T, N>(M) > kMaxSmem || fd_rc_smem<T, N>(M) > kMaxSmem) return 0;
+    int a = 0, f = 0;
+    // the larger block size of the adjoint's two shapes has the same or a lower occupancy
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_adjoint_rc<T, N, THREADS, PingPong<T, N>::value>, THREADS,
+                                                  adjoint_rc_smem<T, N>(M));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_fd_rc<T, N, THREADS>, THREADS, fd_rc_smem<T, N>(M));
+    const int occ = a > f ? a : f;
+    return occ < 1 ? 1 : (occ > 32 ? 32 : occ);
 }
 
 template <typename T, int N>
@@ -64,6 +100,27 @@ void Launcher<T, N>::forward(const KParams<T>& kp, int nImg, cudaStream_t st) {
 template <typename T, int N>
 void Launcher<T, N>::adjoint(const KParams<T>& kp, int grid, int kind, cudaStream_t st) {
     (void)grid;
+    if (kp.recompute) {
+        // one image per block; S recomputed on the fused path (the phases given)
+        const size_t sm = adjoint_rc_smem<T, N>(kp.M);
+        const int g = kp.P * kp.I;
+        const bool alt = HasAlt<T>::value && kp.shapeAdj == 1;
+        if constexpr (PingPong<T, N>::value) {
+            if (kp.phiImg) {
+                if (alt) k_adjoint_rc<T, N, ThreadsAlt<N>::value, true><<<g, ThreadsAlt<N>::value, sm, st>>>(kp, kind);
+                else k_adjoint_rc<T, N, THREADS, true><<<g, THREADS, sm, st>>>(kp, kind);
+                return;
+            }
+        }
+        if constexpr (HasAlt<T>::value) {
+            if (alt) {
+                k_adjoint_rc<T, N, ThreadsAlt<N>::value, false><<<g, ThreadsAlt<N>::value, sm, st>>>(kp, kind);
+                return;
+            }
+        }
+        k_adjoint_rc<T, N, THREADS, false><<<g, THREADS, sm, st>>>(kp, kind);
+        return;
+    }
     const size_t sm = smem_base() + extra_smem<T, N>(kp.M);
     grid = kp.P * kp.I;
     if constexpr (HasAlt<T>::value) {
@@ -78,6 +135,11 @@ void Launcher<T, N>::adjoint(const KParams<T>& kp, int grid, int kind, cudaStrea
 
 template <typename T, int N>
 void Launcher<T, N>::fd(const KParams<T>& kp, int grid, int M, cudaStream_t st) {
+    if (kp.recompute) {
+        const int g = PingPong<T, N>::value ? kp.scrBlocks : kp.P * kp.I * M;
+        k_fd_rc<T, N, THREADS><<<g, THREADS, fd_rc_smem<T, N>(kp.M), st>>>(kp);
+        return;
+    }
     const size_t sm = smem_pp<T, N>(kp.M);
     if (!PingPong<T, N>::value) grid = kp.P * kp.I * M;
     k_fd<T, N, THREADS><<<grid, THREADS, sm, st>>>(kp);
@@ -129,7 +191,9 @@ cudaError_t EvalLauncher<T, N>::setup(int M, int npt, int nH) {
     if (e == cudaSuccess)
         e = raise_smem_limit(k_phase<T, N, kPhasePix, kMaxChunk>, (size_t)M * (kPhasePix + kMaxChunk) * sizeof(T));
     if (e == cudaSuccess && fd_smem(nH) + 1024 <= kMaxSmem)
-        e = raise_smem_limit(k_fd_half<T, N, kEvalThreads>, fd_smem(nH));
+        e = raise_smem_limit(k_fd_half<T, N, kEvalThreads, false>, fd_smem(nH));
+    if (e == cudaSuccess && fd_smem(nH) + 1024 <= kMaxSmem)
+        e = raise_smem_limit(k_fd_half<T, N, kEvalThreads, true>, fd_smem(nH));
     return e;
 }
 
@@ -213,7 +277,9 @@ size_t EvalLauncher<T, N>::fd_smem(int nH) {
 template <typename T, int N>
 void EvalLauncher<T, N>::fd_half(const EvalParams<T>& e, int grid, cudaStream_t st) {
     // one block size only: its per-thread partial sums of the metric change depend on it
-    k_fd_half<T, N, kEvalThreads><<<grid, kEvalThreads, fd_smem(e.hp.nH), st>>>(e);
+    // recomputed transforms: X of the block's image in its scratch slot (slot = block)
+    if (e.k.recompute) k_fd_half<T, N, kEvalThreads, true><<<grid, kEvalThreads, fd_smem(e.hp.nH), st>>>(e);
+    else k_fd_half<T, N, kEvalThreads, false><<<grid, kEvalThreads, fd_smem(e.hp.nH), st>>>(e);
 }
 
 template <typename T, int N>

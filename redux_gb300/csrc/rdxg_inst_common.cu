@@ -28,6 +28,22 @@ void launch_add_plane(const double* plane, float* objects, int nPo, int ps, cuda
     k_add_plane<0><<<nPo, 256, 0, st>>>(plane, objects, ps);
 }
 
+// %nsmid: one more than the largest SM identifier %smid can hold (identifiers need not be
+// contiguous), the size of the per-SM slot masks of the recomputing kernels
+__global__ void k_nsmid(int32_t* out) {
+    unsigned v;
+    asm volatile("mov.u32 %0, %%nsmid;" : "=r"(v));
+    if (threadIdx.x == 0) *out = (int32_t)v;
+}
+
+cudaError_t query_nsmid(int32_t* dOut, int32_t* hOut, cudaStream_t st) {
+    k_nsmid<<<1, 32, 0, st>>>(dOut);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hOut, dOut, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
+}
+
 template void launch_fit_plane<float>(const KParams<float>&, int, int, cudaStream_t);
 template void launch_fit_plane<double>(const KParams<double>&, int, int, cudaStream_t);
 template void launch_accum<float>(const KParams<float>&, int, cudaStream_t);

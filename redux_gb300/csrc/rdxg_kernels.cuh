@@ -72,6 +72,15 @@ struct KParams {
     // launch-shape variants picked by the planner (read by the host-side launchers only):
     // 0 the default block size, 1 the alternative (see rdxg_launch.h)
     int32_t shapeEval, shapeFwd, shapeAdj;
+    // Recomputed transforms: X and PF (and on the fused path S) are not kept between the
+    // evaluation and the gradient kernels, which form them again from the phases.
+    int32_t recompute;
+    const T* phiImg;          // [g][n*n] phases of the fused path's evaluation (null: from alphaEff)
+    cx<T>* Xscr;              // [slot][N*N] scratch of the recomputing kernels
+    int32_t scrBlocks;        // blocks of the persistent ones (slot = block)
+    unsigned* slotMask;       // [SM] slots in use, for the kernels with one item per block
+    int32_t slotsPerSM;
+    int32_t* rcStatus;        // non-zero: a block found no free slot
 };
 
 enum GradKind : int32_t { GK_VOGEL = 0, GK_EXACT = 1 };
@@ -317,7 +326,8 @@ __global__ void __launch_bounds__(THREADS) k_forward(KParams<T> kp) {
     const int p = g / kp.I, j = g % kp.I;
     const int rq = kp.req[p];
     if (rq != REQ_F && rq != REQ_DF) return;
-    const bool df = (rq == REQ_DF);
+    // X and PF are kept for the gradient kernels unless they recompute them
+    const bool df = (rq == REQ_DF) && !kp.recompute;
     constexpr int LDS = Tile<N>::LDS;
     constexpr int n = N / 2, n2 = n * n;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -434,6 +444,69 @@ __global__ void __launch_bounds__(THREADS) k_accum(KParams<T> kp) {
 // kind GK_VOGEL: the reference's weights (pupil amplitude per pixel, -2 area/N^2, object
 // weight twice); GK_EXACT: dL/dalpha of the metric.
 // ----------------------------------------------------------------------------------
+// The last step of the adjoint for image j of patch p: U = tile rows and columns [N/4, 3N/4)
+// (the pupil), v = Im(conj(PF) U) times the pupil weight, and its projection on the enabled
+// modes, one warp per mode (calcVogelWeight's last lines and gradientVogel,
+// subimage.cpp:312-326, 376-389).  v: n^2 values of shared memory on a 16-byte boundary.
+template <typename T, int N, int THREADS>
+__device__ __forceinline__ void project_modes(const KParams<T>& kp, int kind, int p, int j, const cx<T>* s,
+                                              const cx<T>* PF, T* v, int tid) {
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int n = N / 2, n2 = n * n, N2 = N * N;
+    const size_t g = (size_t)p * kp.I + j;
+    const int o = kp.imgObj[j];
+#pragma unroll 4
+    for (int q = tid; q < n2; q += THREADS) {
+        const int y = q / n, x = q % n;
+        const cx<T> U = s[(y + n / 2) * LDS + x + n / 2];
+        const cx<T> pf = PF[q];
+        // Im(conj(pf) U)
+        const T a = kp.A[q];
+        const T wq = (kind == GK_VOGEL) ? a : (a > (T)0 ? (T)1 : (T)0);
+        v[q] = (pf.x * U.y - pf.y * U.x) * wq;
+    }
+    __syncthreads();
+    // projection on the modes: one warp per mode
+    const int lane = tid & 31, wid = tid >> 5;
+    const int mc = kp.modeCount[p];
+    const int ch = kp.imgCh[j];
+    const double c = (double)kp.otfNorm[ch];
+    const double w = kp.objWeight[o];
+    double scale;
+    if (kind == GK_VOGEL) {
+        // X carries the factor c: result = c N^2 (G (*) PF); reference: -2 area w^2 / N^6 * sum
+        scale = -2.0 * kp.area * w * w / ((double)N2 * (double)N2 * (double)N2) / c;
+    } else {
+        scale = -4.0 * c * c * w / ((double)kp.ps * kp.ps * (double)N2) / c;
+    }
+    for (int m = wid; m < kp.M; m += THREADS / 32) {
+        double acc = 0;
+        if (m < mc) {
+            const T* Zm = kp.Z + (size_t)m * n2;
+            T part = 0;
+            if constexpr (sizeof(T) == 4 && n2 % 4 == 0) {
+                // four pixels per load (v and every mode row start on 16-byte boundaries: the
+                // callers place v there and n2 * 4 bytes is a multiple of 16), so each lane has
+                // a quarter of the loads of the scalar loop in flight at once
+                const float4* Z4 = reinterpret_cast<const float4*>(Zm);
+                const float4* v4 = reinterpret_cast<const float4*>(v);
+#pragma unroll 4
+                for (int q = lane; q < n2 / 4; q += 32) {
+                    const float4 z = __ldg(Z4 + q), w = v4[q];
+                    part += w.x * z.x + w.y * z.y + w.z * z.z + w.w * z.w;
+                }
+            } else {
+#pragma unroll 8
+                for (int q = lane; q < n2; q += 32) part += v[q] * Zm[q];
+            }
+            acc = (double)part;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+        }
+        if (lane == 0) kp.galpha[g * kp.M + m] = (m < mc) ? acc * scale : 0.0;
+    }
+}
+
 template <typename T, int N, int THREADS>
 __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, int p, int j) {
     const int g = p * kp.I + j;
@@ -475,58 +548,9 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
     __syncthreads();
     if constexpr (PP) fft2d_pp_out_rows_pruned<T, N, +1, THREADS>(s, s2, tw);
     else fft2d_out_rows_pruned<T, N, +1, THREADS>(s, tw);
+    static_assert(((size_t)(Tile<N>::ELEMS + N) * sizeof(cx<T>)) % 16 == 0, "v is 16-byte aligned");
     const cx<T>* PF = kp.PF + (size_t)g * n2;
-#pragma unroll 4
-    for (int q = threadIdx.x; q < n2; q += THREADS) {
-        const int y = q / n, x = q % n;
-        const cx<T> U = s[(y + n / 2) * LDS + x + n / 2];
-        const cx<T> pf = PF[q];
-        // Im(conj(pf) U)
-        const T a = kp.A[q];
-        const T wq = (kind == GK_VOGEL) ? a : (a > (T)0 ? (T)1 : (T)0);
-        v[q] = (pf.x * U.y - pf.y * U.x) * wq;
-    }
-    __syncthreads();
-    // projection on the modes: one warp per mode
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int mc = kp.modeCount[p];
-    const int ch = kp.imgCh[j];
-    const double c = (double)kp.otfNorm[ch];
-    const double w = kp.objWeight[o];
-    double scale;
-    if (kind == GK_VOGEL) {
-        // X carries the factor c: result = c N^2 (G (*) PF); reference: -2 area w^2 / N^6 * sum
-        scale = -2.0 * kp.area * w * w / ((double)N2 * (double)N2 * (double)N2) / c;
-    } else {
-        scale = -4.0 * c * c * w / ((double)kp.ps * kp.ps * (double)N2) / c;
-    }
-    for (int m = wid; m < kp.M; m += THREADS / 32) {
-        double acc = 0;
-        if (m < mc) {
-            const T* Zm = kp.Z + (size_t)m * n2;
-            T part = 0;
-            if constexpr (sizeof(T) == 4 && n2 % 4 == 0) {
-                // four pixels per load (v and every mode row start on 16-byte boundaries: the
-                // shared-memory offset of v and n2 * 4 bytes are multiples of 16), so each
-                // lane has a quarter of the loads of the scalar loop in flight at once
-                static_assert(((size_t)(Tile<N>::ELEMS + N) * sizeof(cx<T>)) % 16 == 0, "v is 16-byte aligned");
-                const float4* Z4 = reinterpret_cast<const float4*>(Zm);
-                const float4* v4 = reinterpret_cast<const float4*>(v);
-#pragma unroll 4
-                for (int q = lane; q < n2 / 4; q += 32) {
-                    const float4 z = __ldg(Z4 + q), w = v4[q];
-                    part += w.x * z.x + w.y * z.y + w.z * z.z + w.w * z.w;
-                }
-            } else {
-#pragma unroll 8
-                for (int q = lane; q < n2; q += 32) part += v[q] * Zm[q];
-            }
-            acc = (double)part;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-        }
-        if (lane == 0) kp.galpha[(size_t)g * kp.M + m] = (m < mc) ? acc * scale : 0.0;
-    }
+    project_modes<T, N, THREADS>(kp, kind, p, j, s, PF, v, (int)threadIdx.x);
 }
 
 
@@ -540,6 +564,159 @@ __global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
 }
 
 // ----------------------------------------------------------------------------------
+// Recomputed transforms (KParams::recompute).  The reference keeps the pupil function and the
+// OTF of every image (SubImage::PF, SubImage::OTF, subimage.hpp:156-158) from the metric
+// evaluation to calcVogelWeight (subimage.cpp:348-371); here, when the per-image arrays of a
+// batch would not fit the memory budget, the gradient kernels form them again from the
+// phases: PF = A exp(i phi) and its transform X (and, on the fused path, which keeps no full
+// OTF, S = ifft|X|^2 / N^2), so only the image transform D stays per image.  The phases are
+// those of the fused path's evaluation (phiImg) or phi_fixed + sum alpha Z in the order of
+// k_forward, so PF and X are the numbers the evaluation formed.  X lives in shared memory
+// where two tiles fit (FP32 up to N = 88) and otherwise in a scratch slot of the SM the
+// block runs on (acquire_slot).
+// ----------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T image_phase(const KParams<T>& kp, const T* al, const T* phf, size_t g, int q, int n2) {
+    if (kp.phiImg) return kp.phiImg[g * n2 + q];
+    T phi = phf[q];
+    for (int m = 0; m < kp.M; ++m) phi += al[m] * kp.Z[(size_t)m * n2 + q];
+    return phi;
+}
+
+// PF of image g into pf (shared memory) and c PF embedded at n/2 in the zeroed tile s; al
+// (shared memory) receives the image's coefficients first when the phases come from them.
+template <typename T, int N, int THREADS>
+__device__ __forceinline__ void recompute_pupil(const KParams<T>& kp, size_t g, int j, cx<T>* s, cx<T>* pf, T* al,
+                                                int tid) {
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int n = N / 2, n2 = n * n;
+    const int ch = kp.imgCh[j];
+    const T c = kp.otfNorm[ch];
+    const T* phf = kp.phiFixed + (size_t)ch * n2;
+    for (int i = tid; i < Tile<N>::ELEMS; i += THREADS) s[i] = mkc<T>(0, 0);
+    if (!kp.phiImg)
+        for (int m = tid; m < kp.M; m += THREADS) al[m] = kp.alphaEff[g * kp.M + m];
+    __syncthreads();
+    for (int q = tid; q < n2; q += THREADS) {
+        const T a = kp.A[q];
+        cx<T> v = mkc<T>(0, 0);
+        if (a > (T)0) {
+            T sn, cs;
+            sincos_t<T>(image_phase(kp, al, phf, g, q, n2), &sn, &cs);
+            v = mkc<T>(a * cs, a * sn);
+        }
+        pf[q] = v;
+        s[(q / n + n / 2) * LDS + q % n + n / 2] = cscale<T>(v, c);
+    }
+    __syncthreads();
+}
+
+// A scratch slot (one N x N tile of Xscr) for a block of a kernel that runs one work item per
+// block: a free bit of the mask of the SM the block runs on.  An SM holds at most slotsPerSM
+// blocks of these kernels at once (their occupancy, from which the slots were sized), so a
+// free bit exists when a block starts; the bounded retries only absorb contention between
+// blocks starting together.  A block that finds none records status 1 and skips its item
+// (the host reports it).  Returns the slot or -1, in every thread.
+__device__ __forceinline__ int acquire_slot(unsigned* masks, int perSM, int32_t* status, int* smidOut, int* bitOut) {
+    __shared__ int slotSh, smidSh, bitSh;
+    if (threadIdx.x == 0) {
+        unsigned smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        const unsigned all = perSM >= 32 ? 0xffffffffu : ((1u << perSM) - 1u);
+        int slot = -1, bit = -1;
+        for (int tries = 0; tries < 256 && slot < 0; ++tries) {
+            const unsigned freeBits = ~atomicOr(masks + smid, 0u) & all;
+            if (!freeBits) continue;
+            const int b = __ffs(freeBits) - 1;
+            if (!(atomicOr(masks + smid, 1u << b) & (1u << b))) {
+                slot = (int)smid * perSM + b;
+                bit = b;
+            }
+        }
+        if (slot < 0) atomicExch(status, 1);
+        slotSh = slot;
+        smidSh = (int)smid;
+        bitSh = bit;
+    }
+    __syncthreads();
+    *smidOut = smidSh;
+    *bitOut = bitSh;
+    return slotSh;
+}
+__device__ __forceinline__ void release_slot(unsigned* masks, int smid, int bit) {
+    __syncthreads();    // every thread done with the slot
+    if (threadIdx.x == 0 && bit >= 0) atomicAnd(masks + smid, ~(1u << bit));
+}
+
+// The adjoint with recomputed transforms, one image per block: PF -> X [-> S when SREC] ->
+// G -> fft(G) X -> U -> projection; four transforms with SREC, three without (the general
+// path keeps S, which its per-object accumulation reads).  (A persistent loop around the
+// in-place transforms makes the compiler hoist their index arithmetic and spill.)
+template <typename T, int N, int THREADS, bool SREC>
+__global__ void __launch_bounds__(THREADS) k_adjoint_rc(KParams<T> kp, int kind) {
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int n = N / 2, n2 = n * n, N2 = N * N;
+    constexpr bool XS = PingPong<T, N>::value;            // X in a second shared tile
+    constexpr int TILES = XS ? 2 : 1;
+    static_assert(((size_t)(TILES * Tile<N>::ELEMS + N + n2) * sizeof(cx<T>)) % 16 == 0, "v is 16-byte aligned");
+    const int nWork = *kp.nGradP * kp.I;
+    const int w = blockIdx.x;
+    if (w >= nWork) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* tw = s + TILES * Tile<N>::ELEMS;
+    cx<T>* pf = tw + N;                            // [n2] pupil function
+    T* v = reinterpret_cast<T*>(pf + n2);          // [n2] weights of the projection
+    T* al = v + n2;                                // [M] coefficients
+    int smid = -1, bit = -1;
+    cx<T>* Xb;
+    if constexpr (XS) {
+        Xb = s + Tile<N>::ELEMS;
+    } else {
+        const int slot = acquire_slot(kp.slotMask, kp.slotsPerSM, kp.rcStatus, &smid, &bit);
+        if (slot < 0) return;
+        Xb = kp.Xscr + (size_t)slot * N2;
+    }
+    const int tid = (int)threadIdx.x;
+    const T inv = (T)1 / (T)N2;
+    const int p = kp.gradP[w / kp.I], j = w % kp.I;
+    const size_t g = (size_t)p * kp.I + j;
+    load_twiddles<T, N>(tw, kp.tw);
+    recompute_pupil<T, N, THREADS>(kp, g, j, s, pf, al, tid);
+    fft2d<T, N, -1, THREADS, true>(s, tw, tid);
+    for (int i = tid; i < N2; i += THREADS) {
+        const int y = i / N, x = i % N;
+        const cx<T> X = s[y * LDS + x];
+        Xb[i] = X;
+        if (SREC) s[y * LDS + x] = mkc<T>(cnorm<T>(X), 0);
+    }
+    __syncthreads();
+    if (SREC) fft2d<T, N, +1, THREADS, false>(s, tw, tid);
+    const size_t po = (size_t)p * kp.nObj + kp.imgObj[j];
+    const cx<T>* Oo = kp.O + po * N2;
+    const cx<T>* Dg = kp.D + g * N2;
+    for (int i = tid; i < N2; i += THREADS) {
+        const int y = i / N, x = i % N;                 // un-centred (lag) position
+        const int c = ((y + N / 2) % N) * N + (x + N / 2) % N;
+        const uint8_t m = kp.otfMask[c];
+        const cx<T> O = Oo[c], D = Dg[c];
+        const cx<T> S = SREC ? cscale<T>(s[y * LDS + x], inv) : kp.S[g * N2 + c];
+        const cx<T> G = cmulc<T>(csub<T>(D, cmul<T>(O, S)), O);   // conj(O) (D - O S)
+        s[y * LDS + x] = (m && !(y == 0 && x == 0)) ? G : mkc<T>(0, 0);
+    }
+    __syncthreads();
+    fft2d<T, N, -1, THREADS, false>(s, tw, tid);
+    for (int i = tid; i < N2; i += THREADS) {
+        const int y = i / N, x = i % N;
+        s[y * LDS + x] = cmul<T>(s[y * LDS + x], Xb[i]);
+    }
+    __syncthreads();
+    fft2d_out_rows_pruned<T, N, +1, THREADS>(s, tw, tid);
+    project_modes<T, N, THREADS>(kp, kind, p, j, s, pf, v, tid);
+    if constexpr (!XS) release_slot(kp.slotMask, smid, bit);
+}
+
+// ----------------------------------------------------------------------------------
 // Finite-difference gradient: SubImage::gradientFiniteDifference + metricChange
 // (subimage.cpp:261-292), used by the reference for the first gradient of a patch.
 // The OTF change dS = S(phi + h Z_m) - S(phi) is formed directly as
@@ -550,14 +727,15 @@ __global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
 // One block per (image, mode).
 // ----------------------------------------------------------------------------------
 template <typename T, int N, int THREADS>
-__device__ __forceinline__ void fd_image(const KParams<T>& kp, int p, int j, int m) {
+__device__ __forceinline__ void fd_image(const KParams<T>& kp, int p, int j, int m, const cx<T>* PF,
+                                         const cx<T>* X, int tid) {
     const int g = p * kp.I + j;
     constexpr int LDS = Tile<N>::LDS;
     constexpr int n = N / 2, n2 = n * n, N2 = N * N;
     constexpr bool PP = PingPong<T, N>::value;
     const int o = kp.imgObj[j];
     if (m >= kp.modeCount[p] || kp.objWeight[o] == 0.0) {
-        if (threadIdx.x == 0) kp.galpha[(size_t)g * kp.M + m] = 0.0;
+        if (tid == 0) kp.galpha[(size_t)g * kp.M + m] = 0.0;
         return;
     }
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -567,14 +745,13 @@ __device__ __forceinline__ void fd_image(const KParams<T>& kp, int p, int j, int
     double* red = reinterpret_cast<double*>(tw + N);
     __syncthreads();    // previous item's shared memory consumed
     load_twiddles<T, N>(tw, kp.tw);
-    zero_tile<T, N>(s);
+    for (int i = tid; i < Tile<N>::ELEMS; i += THREADS) s[i] = mkc<T>(0, 0);
     __syncthreads();
     const int ch = kp.imgCh[j];
     const T c = kp.otfNorm[ch];
     const double h = kp.objGradStep[o];
-    const cx<T>* PF = kp.PF + (size_t)g * n2;
     const T* Zm = kp.Z + (size_t)m * n2;
-    for (int q = threadIdx.x; q < n2; q += THREADS) {
+    for (int q = tid; q < n2; q += THREADS) {
         if (kp.A[q] > (T)0) {
             const T t = (T)h * Zm[q];
             T sh, ch2, sn, cs;
@@ -586,20 +763,21 @@ __device__ __forceinline__ void fd_image(const KParams<T>& kp, int p, int j, int
         }
     }
     __syncthreads();
-    fft2d_any<T, N, -1, THREADS, true>(s, s2, tw);
-    const cx<T>* X = kp.X + (size_t)g * N2;
-    for (int i = threadIdx.x; i < N2; i += THREADS) {
+    if constexpr (PP) fft2d_pp<T, N, -1, THREADS, true>(s, s2, tw);
+    else fft2d<T, N, -1, THREADS, true>(s, tw, tid);
+    for (int i = tid; i < N2; i += THREADS) {
         const int y = i / N, x = i % N;
         const cx<T> dX = s[y * LDS + x];
         const cx<T> x0 = X[i];
         s[y * LDS + x] = mkc<T>((T)2 * (x0.x * dX.x + x0.y * dX.y) + cnorm<T>(dX), 0);
     }
     __syncthreads();
-    fft2d_any<T, N, +1, THREADS, false>(s, s2, tw);
+    if constexpr (PP) fft2d_pp<T, N, +1, THREADS, false>(s, s2, tw);
+    else fft2d<T, N, +1, THREADS, false>(s, tw, tid);
     const size_t po = (size_t)p * kp.nObj + o;
     const T inv = (T)1 / (T)N2;
     double dl = 0;
-    for (int i = threadIdx.x; i < N2; i += THREADS) {
+    for (int i = tid; i < N2; i += THREADS) {
         if (!kp.otfMask[i]) continue;
         const int cy = i / N, cxx = i % N;
         if (cy == N / 2 && cxx == N / 2) continue;       // dS(0) = 0 exactly
@@ -615,7 +793,7 @@ __device__ __forceinline__ void fd_image(const KParams<T>& kp, int p, int j, int
         dl -= (double)num / (double)(Q + dq);
     }
     const double tot = block_sum<THREADS>(dl, red);
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         const double w = kp.objWeight[o];
         kp.galpha[(size_t)g * kp.M + m] = w * (tot / (double)N2 / h * w);
     }
@@ -624,15 +802,80 @@ __device__ __forceinline__ void fd_image(const KParams<T>& kp, int p, int j, int
 template <typename T, int N, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_fd(KParams<T> kp) {
     const int nWork = *kp.nFdP * kp.I * kp.M;
+    auto item = [&](int w) {
+        const int p = kp.fdP[w / (kp.M * kp.I)], j = (w / kp.M) % kp.I, m = w % kp.M;
+        const size_t g = (size_t)p * kp.I + j;
+        fd_image<T, N, THREADS>(kp, p, j, m, kp.PF + g * (N / 2) * (N / 2), kp.X + g * N * N, (int)threadIdx.x);
+    };
     if constexpr (PingPong<T, N>::value) {
-        for (int w = blockIdx.x; w < nWork; w += gridDim.x) {
-            const int m = w % kp.M;
-            const int j = (w / kp.M) % kp.I;
-            fd_image<T, N, THREADS>(kp, kp.fdP[w / (kp.M * kp.I)], j, m);
+        for (int w = blockIdx.x; w < nWork; w += gridDim.x) item(w);
+    } else {
+        const int w = blockIdx.x;
+        if (w < nWork) item(w);
+    }
+}
+
+// Shared memory of k_fd (and of k_fd_rc before its own arrays): tiles, twiddles, reduction.
+template <typename T, int N>
+constexpr size_t fd_base_smem() {
+    return (size_t)((PingPong<T, N>::value ? 2 : 1) * Tile<N>::ELEMS + N) * sizeof(cx<T>) + 33 * sizeof(double);
+}
+
+// The finite-difference gradient with recomputed transforms.  FP32 up to N = 88 (ping-pong
+// transforms, which a loop does not make spill): persistent, each block taking a contiguous
+// range of (image, mode) items, modes fastest, and forming PF (shared memory) and X (its
+// scratch slot, blockIdx.x) when its image changes.  Otherwise one (image, mode) item per
+// block with X in a slot of its SM, formed for the item.
+template <typename T, int N, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_fd_rc(KParams<T> kp) {
+    constexpr int LDS = Tile<N>::LDS;
+    constexpr int n2 = (N / 2) * (N / 2), N2 = N * N;
+    constexpr bool PP = PingPong<T, N>::value;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* tw = s + (PP ? 2 : 1) * Tile<N>::ELEMS;
+    cx<T>* pf = reinterpret_cast<cx<T>*>(smem_raw + ((fd_base_smem<T, N>() + 15) & ~(size_t)15));
+    T* al = reinterpret_cast<T*>(pf + n2);
+    const int nWork = *kp.nFdP * kp.I * kp.M;
+    auto prepare = [&](size_t g, int j, cx<T>* Xb) {
+        __syncthreads();    // the previous item's tiles consumed
+        load_twiddles<T, N>(tw, kp.tw);
+        recompute_pupil<T, N, THREADS>(kp, g, j, s, pf, al, (int)threadIdx.x);
+        if constexpr (PP) fft2d_pp<T, N, -1, THREADS, true>(s, s + Tile<N>::ELEMS, tw);
+        else fft2d<T, N, -1, THREADS, true>(s, tw, (int)threadIdx.x);
+        for (int i = threadIdx.x; i < N2; i += THREADS) Xb[i] = s[(i / N) * LDS + i % N];
+    };
+    if constexpr (PP) {
+        if ((int)blockIdx.x >= kp.scrBlocks) return;
+        const int per = (nWork + (int)gridDim.x - 1) / (int)gridDim.x;
+        const int w0 = (int)blockIdx.x * per, w1 = min(nWork, w0 + per);
+        cx<T>* Xb = kp.Xscr + (size_t)blockIdx.x * N2;
+        long gPrev = -1;
+        for (int w = w0; w < w1; ++w) {
+            const int p = kp.fdP[w / (kp.M * kp.I)], j = (w / kp.M) % kp.I, m = w % kp.M;
+            const size_t g = (size_t)p * kp.I + j;
+            if (m < kp.modeCount[p] && kp.objWeight[kp.imgObj[j]] != 0.0 && (long)g != gPrev) {
+                prepare(g, j, Xb);
+                gPrev = (long)g;
+            }
+            fd_image<T, N, THREADS>(kp, p, j, m, pf, Xb, (int)threadIdx.x);
         }
     } else {
         const int w = blockIdx.x;
-        if (w < nWork) fd_image<T, N, THREADS>(kp, kp.fdP[w / (kp.M * kp.I)], (w / kp.M) % kp.I, w % kp.M);
+        if (w >= nWork) return;
+        const int p = kp.fdP[w / (kp.M * kp.I)], j = (w / kp.M) % kp.I, m = w % kp.M;
+        const size_t g = (size_t)p * kp.I + j;
+        if (m >= kp.modeCount[p] || kp.objWeight[kp.imgObj[j]] == 0.0) {
+            if (threadIdx.x == 0) kp.galpha[g * kp.M + m] = 0.0;
+            return;
+        }
+        int smid = -1, bit = -1;
+        const int slot = acquire_slot(kp.slotMask, kp.slotsPerSM, kp.rcStatus, &smid, &bit);
+        if (slot < 0) return;
+        cx<T>* Xb = kp.Xscr + (size_t)slot * N2;
+        prepare(g, j, Xb);
+        fd_image<T, N, THREADS>(kp, p, j, m, pf, Xb, (int)threadIdx.x);
+        release_slot(kp.slotMask, smid, bit);
     }
 }
 

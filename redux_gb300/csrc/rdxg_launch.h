@@ -43,6 +43,9 @@ struct Launcher {
     static void forward(const KParams<T>& kp, int nImg, cudaStream_t st);
     static void adjoint(const KParams<T>& kp, int grid, int kind, cudaStream_t st);   // grid-strides over the work list
     static void fd(const KParams<T>& kp, int grid, int M, cudaStream_t st);
+    // resident blocks per SM of the kernels that recompute the transforms (the scratch slots
+    // per SM), 0 when their shared memory does not fit
+    static int recompute_occupancy(int M);
     static cudaError_t restore(const KParams<T>& kp, const RestoreArgs& ra, int nBlocks, cudaStream_t st);
     // PSF / convolved-object / residual outputs after restore(); grid: blocks (each with its
     // 3 N^2 doubles of oa.pool)
@@ -89,6 +92,7 @@ template <typename T, int N> struct EvalLauncher {
     static void fd_half(const EvalParams<T>& e, int grid, cudaStream_t st);
 };
 template <typename T> void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st);
+cudaError_t query_nsmid(int32_t* dOut, int32_t* hOut, cudaStream_t st);   // %nsmid of the device
 void launch_shift(const ShiftArgs& a, int P, cudaStream_t st);
 
 // mode expansion on the tensor cores (rdxg_phase_tc.cu); parts: 2 (3xBF16) or 3 (6xBF16)

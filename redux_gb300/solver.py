@@ -147,6 +147,14 @@ class Solver:
         a = np.ascontiguousarray(alpha, np.float64).reshape(self.P, self.I, self.M)
         self._check(_lib.load().rdxg_set_initial_alpha(self.h, _lib.ptr(a)), "rdxg_set_initial_alpha")
 
+    def set_recompute(self, on: bool = True) -> None:
+        """Recomputed transforms (rdxg_set_recompute): the gradient kernels form PF, X (and on
+        the fused path the OTF) again instead of keeping them per image."""
+        self._check(_lib.load().rdxg_set_recompute(self.h, int(bool(on))), "rdxg_set_recompute")
+
+    def recompute(self) -> bool:
+        return bool(_lib.load().rdxg_recompute(self.h))
+
     def set_start_alpha(self, alpha=None) -> None:
         """Continuation: every following solve starts from these coefficients [P][I][M] with the
         images as loaded (not re-cut), e.g. an FP64 handle continuing an FP32 solution."""
@@ -292,7 +300,7 @@ class Solver:
                 "stats": (3, (P, I, 3), np.float64), "object": (4, (P, nObj, N, N), ct),
                 "shifts": (5, (P, I, 2), np.int32),
                 "phases": (6, (P, I, self.job.pupil_pixels, self.job.pupil_pixels), np.float32),
-                "allocations": (7, (1,), np.int64)}[which]
+                "allocations": (7, (1,), np.int64), "allocated_bytes": (8, (1,), np.int64)}[which]
         out = np.zeros(spec[1], spec[2])
         self._check(_lib.load().rdxg_debug_copy(self.h, spec[0], _lib.ptr(out), out.nbytes), "rdxg_debug_copy")
         return out

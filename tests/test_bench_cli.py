@@ -24,4 +24,4 @@ def test_workload_choices():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--help"], capture_output=True, text=True,
                        timeout=120, cwd=ROOT)
     assert r.returncode == 0
-    assert "--workload {production,uneven,large}" in r.stdout
+    assert "--workload {production,uneven,large,convergence}" in r.stdout
