@@ -400,9 +400,9 @@ def run_convergence(args):
 
 def run_large(args):
     """Large patches, mixed precision: 128 x 128 patches, 3 channels x 32
-    frames, 100 KL modes at D/r0 = 25; mode expansion on the CUDA cores in FP32 (the tensor-core
-    expansion belongs to the fused path, which covers N <= 88), FP32 transforms, FP64 metric
-    sums and CG scalars.  `--iterations` CG iterations per patch with all modes at once, as the
+    frames, 100 KL modes at D/r0 = 25; mode expansion on the tensor cores (tcgen05, BF16-split
+    FP32 operands, 6xBF16 by default; `--phase-mode 2` for the 3xBF16 split, 0 for the CUDA
+    cores), FP32 transforms, FP64 metric sums and CG scalars.  `--iterations` CG iterations per patch with all modes at once, as the
     headline workload.  Reports patches/s and CG iterations/s, the kernel times with their
     nominal FP32 rates and HBM fractions, and the errors against the FP64 restatement on one
     patch: the metric, gradient and restored object at the same alpha (per-evaluation
@@ -418,6 +418,8 @@ def run_large(args):
     job, cut = w.job, np.ascontiguousarray(w.patches.cutouts, np.float32)
     settings = S.fixed_iterations(job.n_modes, args.iterations, max_metrics=args.iterations + 8)
     s = S.Solver(job, max_patches=P)
+    if args.phase_mode is not None:
+        s.set_phase_mode(args.phase_mode)
     for _ in range(args.warmup):
         s.set_patches(cut)
         s.run(settings)
@@ -496,7 +498,10 @@ def run_large(args):
                                    f"{args.iterations} CG iterations, all modes at once",
                        "metric_evals_per_patch": nf, "gradient_evals_per_patch": ndf,
                        "cg_iterations_per_s": P * args.iterations / t_solve, "generation_s": t_gen,
-                       "mode_expansion": "CUDA cores, FP32 (inside the transform kernel)",
+                       "mode_expansion": {0: "CUDA cores, FP32 (inside the transform kernel)",
+                                          2: "tensor cores, 3xBF16 split, FP32 accumulation (k_phase_tc)",
+                                          3: "tensor cores, 6xBF16 split, FP32 accumulation (k_phase_tc)"}[
+                                              s.phase_mode()],
                        "l2": "inputs larger than L2 (D, S: 2 x %.1f GB)" % (G * 8.0 * N * N / 1e9)},
             "gpu_launches": int(launches), "kernels": kern, "peak_hbm_gbs": peaks["hbm"],
             "launch_shapes": s.launch_shape(),
@@ -526,6 +531,9 @@ def main():
                     help="production: the headline batch (225 patches 88 x 88); uneven: 400 patches of "
                          "{64, 88, 128} px; large: 256 patches 128 x 128 with 100 modes; convergence: the "
                          "headline batch solved to convergence in FP32 and FP64 with FP64 continuations")
+    ap.add_argument("--phase-mode", type=int, default=None, choices=(0, 2, 3),
+                    help="large patches: mode expansion (3: tensor cores 6xBF16, the default; 2: 3xBF16; "
+                         "0: CUDA cores)")
     ap.add_argument("--conv-ftol", type=float, default=1e-6, help="convergence: FTOL")
     ap.add_argument("--conv-max-iterations", type=int, default=2000, help="convergence: MAX_ITER")
     ap.add_argument("--conv-oracle-patches", type=int, default=4,

@@ -245,14 +245,14 @@ int rdxg_solve_many(rdxg_solver* const* handles, int32_t n, const rdxg_solve_par
 /* Number of kernel launches issued by the last rdxg_solve / rdxg_solve_async. */
 int64_t rdxg_last_launch_count(const rdxg_solver* h);
 
-/* Mode expansion phi = phi_fixed + sum_m alpha_m Z_m of the fused FP32 path
- * (SubImage::calcPhi / addToPhi, subimage.cpp:509-544) on the tensor cores (tcgen05, FP32
- * accumulation) with the FP32 operands split into BF16 parts: mode 3 (the default) three parts
- * (6xBF16 products, FP32-like: metric, OTF and gradient within 1e-6 of FP64), mode 2 two parts
- * (3xBF16: phases within ~1e-5 of their magnitude, gradients within ~3e-5); mode 0 on the
- * CUDA cores in FP32.  The general path (FP64, or OTF sizes the fused path does not take) expands the modes
- * inside its transform kernel and only accepts mode 0 (RDXG_ERR_STATE otherwise).
- * rdxg_phase_mode returns the mode in use (0, 2 or 3). */
+/* Mode expansion phi = phi_fixed + sum_m alpha_m Z_m of FP32 handles (SubImage::calcPhi /
+ * addToPhi, subimage.cpp:509-544) on the tensor cores (tcgen05, FP32 accumulation) with the FP32
+ * operands split into BF16 parts: mode 3 (the default) three parts (6xBF16 products, FP32-like:
+ * metric, OTF and gradient within 1e-6 of FP64), mode 2 two parts (3xBF16: phases within ~1e-5
+ * of their magnitude, gradients within ~3e-5); mode 0 on the CUDA cores in FP32 (on the general
+ * path, OTF size 128, inside the transform kernel).  FP64 handles expand the modes inside their
+ * transform kernel and only accept mode 0 (RDXG_ERR_STATE otherwise).  rdxg_phase_mode returns
+ * the mode in use (0, 2 or 3). */
 int rdxg_set_phase_mode(rdxg_solver* h, int32_t mode);
 int32_t rdxg_phase_mode(const rdxg_solver* h);
 

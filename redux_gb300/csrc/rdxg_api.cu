@@ -238,7 +238,7 @@ KParams<T> make_kparams(rdxg_solver* h) {
     k.shapeEval = h->shapeEval; k.shapeFwd = h->shapeFwd; k.shapeAdj = h->shapeAdj;
     k.plane = h->fitPlane ? h->dPlane : nullptr;
     k.recompute = h->recompute ? 1 : 0;
-    k.phiImg = h->fused ? (const T*)h->dPhiImg : nullptr;
+    k.phiImg = (h->fused || h->tcPlan.valid) ? (const T*)h->dPhiImg : nullptr;
     k.Xscr = (cx<T>*)h->dXscr;
     k.scrBlocks = h->scrBlocks;
     k.slotMask = h->dSlotMask;
@@ -358,10 +358,14 @@ CgArgs<T> make_cgargs(rdxg_solver* h, const CgParams& prm) {
     a.fused = h->fused ? 1 : 0;
     // FP32 map of metric requests: the point as float in dynamic shared memory (under 44 KB)
     a.x1Smem = (!h->fp64 && (size_t)h->nFree * sizeof(float) <= 44 * 1024) ? 1 : 0;
+    // RDXG_MAP64=1: the FP64 map for metric requests too (precision studies)
+    const char* m64 = getenv("RDXG_MAP64");
+    if (m64 && atoi(m64)) a.x1Smem = 0;
     a.objMetric = h->dObjMetric; a.L = make_lists(h); a.nTilesH = h->nTilesH;
     a.chunkSize = h->chunk; a.chunksPerPatch = h->chunksPerPatch; a.objChunk0 = h->dObjChunk0;
     a.objFirst = h->dObjFirstC; a.objCount = h->dObjCountC; a.aux = h->dAux;
     a.regW = h->hRegW.empty() ? nullptr : h->dRegW;
+    a.phaseList = (!h->fused && h->tcPlan.valid) ? 1 : 0;
     return a;
 }
 
@@ -639,8 +643,28 @@ int set_requests(rdxg_solver* h, int req, int gm, int mc) {
     CK(h, cudaMemcpyAsync(h->dReq, a.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaMemcpyAsync(h->dGm, b.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaMemcpyAsync(h->dMc, c.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    if (!h->fused) {
+        // the general path's tensor-core expansion takes the patches of this evaluation: all
+        const int32_t nP = h->P;
+        CK(h, cudaMemcpyAsync(h->dEvalP, all.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+        CK(h, cudaMemcpyAsync(h->dCounters + 4, &nP, sizeof(nP), cudaMemcpyHostToDevice, h->stream));
+    }
     CK(h, cudaStreamSynchronize(h->stream));
     return RDXG_OK;
+}
+
+// The mode expansion of the general path on the tensor cores (FP32 handles whose shape the
+// tensor-core kernel takes): the phases of the listed patches' images, which k_forward and
+// the recomputing gradient kernels then read instead of expanding the modes themselves.
+void phase_general(rdxg_solver* h, cudaStream_t st) {
+    if (h->fused || !h->tcPlan.valid) return;
+    PhaseTcArgs a;
+    a.Zt = h->dZt; a.alphaEff = (const float*)h->dAlphaEff; a.phiFixed = (const float*)h->dPhi;
+    a.imgCh = h->dImgCh; a.evalP = h->dEvalP; a.nEvalP = h->dCounters + kCounterEvalP;
+    a.phi = (float*)h->dPhiImg; a.status = h->dTcStatus;
+    a.I = h->I; a.M = h->M; a.n2 = h->n * h->n; a.nCh = h->C;
+    a.G = h->tcPlan.G; a.NT = h->tcPlan.NT; a.KP = h->tcPlan.KP; a.parts = h->tcPlan.parts;
+    launch_phase_tc(a, h->tcPlan, st);
 }
 
 CgParams make_cg_params(rdxg_solver* h, const rdxg_solve_params* s) {
@@ -896,6 +920,15 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
     if (at && atoi(at) == 0) h->tune = 0;   // default shapes, no measurement
     const char* nf = getenv("RDXG_NO_FUSED");
     if (!r && !(nf && atoi(nf))) r = setup_fused(h, s);
+    if (!r && !h->fused && !h->fp64) {
+        // the general FP32 path (OTF size 128, or a support the half-plane evaluation does not
+        // take): the mode expansion on the tensor cores ahead of the transform kernel
+        const size_t G = (size_t)h->Pmax * h->I;
+        r = dalloc(h, &h->dPhiImg, G * (size_t)h->n * h->n * sizeof(float));
+        const char* pm = getenv("RDXG_PHASE_PARTS");
+        const int parts = pm ? atoi(pm) : 3;
+        if (!r) r = setup_phase_tc(h, parts == 0 || parts == 2 ? parts : 3);
+    }
     if (!r && h->fused) {
         // rdxg_metric_noalloc's static scratch: its address in this context, which also loads
         // (and so reserves) it now rather than in that call
@@ -1072,6 +1105,7 @@ int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric) {
     with_size(h->N, h->fp64, [&](auto L, auto t) {
         using T = decltype(t);
         KParams<T> kp = make_kparams<T>(h);
+        phase_general(h, h->stream);
         decltype(L)::forward(kp, h->P * h->I, h->stream);
         launch_accum<T>(kp, h->P * h->nObj, h->stream);
     });
@@ -1229,6 +1263,7 @@ int restore_impl(rdxg_solver* h, const double* alpha, const double* frequency_cu
         with_size(h->N, h->fp64, [&](auto L, auto t) {
             using T = decltype(t);
             KParams<T> kp = make_kparams<T>(h);
+            phase_general(h, h->stream);
             decltype(L)::forward(kp, h->P * h->I, h->stream);
         });
     }
@@ -1294,6 +1329,7 @@ int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, i
         using T = decltype(t);
         KParams<T> kp = make_kparams<T>(h);
         if (!h->fused) {
+            phase_general(h, h->stream);
             decltype(L)::forward(kp, h->P * h->I, h->stream);
             launch_accum<T>(kp, h->P * h->nObj, h->stream);
         }
@@ -1403,6 +1439,7 @@ int issue_round(const SolvePlan& pl, cudaStream_t st, const ShiftArgs& sar, Opt&
                 decltype(E)::reduce(e, h->reduceGrid, st);
             });
         } else {
+            phase_general(h, st);
             decltype(L)::forward(kp, G, st);
             launch_accum<T>(kp, P * h->nObj, st);
         }
@@ -1467,7 +1504,7 @@ int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
             ShiftArgs sa = pl.sa;
             sa.useConditions = 1;
             sa.counters = h->dCounters;
-            sa.fixedLaunches = h->fused ? 5 : 4;
+            sa.fixedLaunches = (h->fused || h->tcPlan.valid) ? 5 : 4;
             sa.prepLaunches = h->fitPlane ? 2 : 1;
             sa.launchCount = h->dLaunchCount;
             sa.condPrep = cond[0];
@@ -1576,7 +1613,7 @@ int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
             h->err = "cudaMemsetAsync failed";
             return RDXG_ERR_CUDA;
         }
-        h->launches += (h->fused ? 8 : 7) + (h->fitPlane ? 1 : 0);
+        h->launches += (h->fused ? 8 : (h->tcPlan.valid ? 8 : 7)) + (h->fitPlane ? 1 : 0);
         CKL(h);
         if ((round + 1) % check == 0) {
             CK(h, cudaMemcpyAsync(h->hActive, h->dActive, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
@@ -1645,9 +1682,9 @@ int64_t rdxg_last_launch_count(const rdxg_solver* h) { return h ? h->launches : 
 
 int rdxg_set_phase_mode(rdxg_solver* h, int32_t mode) {
     if (!h || (mode != 0 && mode != 2 && mode != 3)) return RDXG_ERR_ARG;
-    if (!h->fused) {
+    if (h->fp64) {
         if (mode == 0) return RDXG_OK;
-        h->err = "the general path expands the modes inside its transform kernel (CUDA cores only)";
+        h->err = "the general path in FP64 expands the modes inside its transform kernel (CUDA cores only)";
         return RDXG_ERR_STATE;
     }
     const int r = setup_phase_tc(h, mode);
@@ -1660,7 +1697,7 @@ int rdxg_set_phase_mode(rdxg_solver* h, int32_t mode) {
 }
 
 int32_t rdxg_phase_mode(const rdxg_solver* h) {
-    if (!h || !h->fused) return 0;
+    if (!h || h->fp64) return 0;
     return h->tcPlan.valid ? h->tcPlan.parts : 0;
 }
 
@@ -1704,7 +1741,7 @@ int time_kernel(rdxg_solver* h, int k, int reps, cudaEvent_t e0, cudaEvent_t e1,
                 return;
             }
             switch (which) {
-                case 0: case 2: decltype(L)::forward(kp, G, h->stream); break;
+                case 0: case 2: phase_general(h, h->stream); decltype(L)::forward(kp, G, h->stream); break;
                 case 1: launch_accum<T>(kp, PO, h->stream); break;
                 case 3: decltype(L)::adjoint(kp, h->adjGrid, GK_VOGEL, h->stream); break;
                 case 4: launch_fd(h); break;
@@ -1926,7 +1963,7 @@ int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes) {
         case 5: if (bytes < G * 2 * 4) return RDXG_ERR_ARG; CK(h, cudaMemcpy(out, h->dShift, G * 8, cudaMemcpyDeviceToHost)); break;
         case 6: {
             const size_t nb = G * (size_t)h->n * h->n * sizeof(float);
-            if (!h->fused || !h->dPhiImg || bytes < nb) return RDXG_ERR_ARG;
+            if (!h->dPhiImg || (!h->fused && !h->tcPlan.valid) || bytes < nb) return RDXG_ERR_ARG;
             CK(h, cudaMemcpy(out, h->dPhiImg, nb, cudaMemcpyDeviceToHost));
             break;
         }

@@ -99,6 +99,7 @@ struct CgArgs {
     const int32_t* objCount;       // [nObj]
     int32_t* aux;                  // [P][2]: reference object valid, refresh pending
     const double* regW;            // [nPar] REG_ALPHA weights, or null
+    int32_t phaseList;             // general path: list the evaluated patches (tensor-core expansion)
 };
 
 // alpha = offset + N x1; alpha_eff = alpha + currentTiltOffset - residual for the tilt modes
@@ -303,6 +304,9 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
                 a.aux[2 * p + 1] = 1;
             }
             enqueue_eval(a, p, rq, mode);
+        } else if (a.phaseList && (rq == REQ_F || rq == REQ_DF)) {
+            // general path with the tensor-core mode expansion: the patches to expand
+            a.L.evalP[atomicAdd(a.L.nEvalP, 1)] = p;
         }
     }
 }

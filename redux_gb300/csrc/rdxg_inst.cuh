@@ -101,12 +101,12 @@ template <typename T, int N>
 void Launcher<T, N>::adjoint(const KParams<T>& kp, int grid, int kind, cudaStream_t st) {
     (void)grid;
     if (kp.recompute) {
-        // one image per block; S recomputed on the fused path (the phases given)
+        // one image per block; S recomputed where it is not kept (the fused path)
         const size_t sm = adjoint_rc_smem<T, N>(kp.M);
         const int g = kp.P * kp.I;
         const bool alt = HasAlt<T>::value && kp.shapeAdj == 1;
         if constexpr (PingPong<T, N>::value) {
-            if (kp.phiImg) {
+            if (!kp.S) {
                 if (alt) k_adjoint_rc<T, N, ThreadsAlt<N>::value, true><<<g, ThreadsAlt<N>::value, sm, st>>>(kp, kind);
                 else k_adjoint_rc<T, N, THREADS, true><<<g, THREADS, sm, st>>>(kp, kind);
                 return;

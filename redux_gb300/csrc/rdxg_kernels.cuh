@@ -75,7 +75,10 @@ struct KParams {
     // Recomputed transforms: X and PF (and on the fused path S) are not kept between the
     // evaluation and the gradient kernels, which form them again from the phases.
     int32_t recompute;
-    const T* phiImg;          // [g][n*n] phases of the fused path's evaluation (null: from alphaEff)
+    // [g][n*n] phases of this evaluation when the mode expansion ran before the transforms
+    // (the fused path, and the tensor-core expansion on the general path); null: the
+    // transform kernels form phi_fixed + sum alpha Z themselves
+    const T* phiImg;
     cx<T>* Xscr;              // [slot][N*N] scratch of the recomputing kernels
     int32_t scrBlocks;        // blocks of the persistent ones (slot = block)
     unsigned* slotMask;       // [SM] slots in use, for the kernels with one item per block
@@ -346,8 +349,13 @@ __global__ void __launch_bounds__(THREADS) k_forward(KParams<T> kp) {
         const T a = kp.A[q];
         cx<T> pf = mkc<T>(0, 0);
         if (a > (T)0) {
-            T phi = phf[q];
-            for (int m = 0; m < M; ++m) phi += al[m] * kp.Z[(size_t)m * n2 + q];
+            T phi;
+            if (kp.phiImg) {
+                phi = kp.phiImg[(size_t)g * n2 + q];     // expanded on the tensor cores (k_phase_tc)
+            } else {
+                phi = phf[q];
+                for (int m = 0; m < M; ++m) phi += al[m] * kp.Z[(size_t)m * n2 + q];
+            }
             T sn, cs;
             sincos_t<T>(phi, &sn, &cs);
             pf = mkc<T>(a * cs, a * sn);
@@ -570,8 +578,8 @@ __global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
 // batch would not fit the memory budget, the gradient kernels form them again from the
 // phases: PF = A exp(i phi) and its transform X (and, on the fused path, which keeps no full
 // OTF, S = ifft|X|^2 / N^2), so only the image transform D stays per image.  The phases are
-// those of the fused path's evaluation (phiImg) or phi_fixed + sum alpha Z in the order of
-// k_forward, so PF and X are the numbers the evaluation formed.  X lives in shared memory
+// those of the evaluation (phiImg) or phi_fixed + sum alpha Z in the order of k_forward, so
+// PF and X are the numbers the evaluation formed.  X lives in shared memory
 // where two tiles fit (FP32 up to N = 88) and otherwise in a scratch slot of the SM the
 // block runs on (acquire_slot).
 // ----------------------------------------------------------------------------------

@@ -125,10 +125,12 @@ def test_fp64_mode_matches_oracle(w0):
 
 
 # FP32 rounding (1e-7 in the metric) flips some of the line search's comparisons, and
-# Brent's 10 % step tolerance turns each flip into a different accepted point; FP64 runs
-# that differ only by 1e-9 relative noise drift apart the same way.  Solver histories in
-# FP32 are therefore compared loosely; exactness is checked in FP64 and per evaluation.
-TOL_TRAJECTORY = 2e-3
+# Brent's 10 % step tolerance turns each flip into a different accepted point, so FP32 and
+# FP64 trajectories part after a few iterations and converge to different points of this
+# non-convex metric (FP64 runs whose rounding differs part the same way).  Solves are
+# therefore checked by what does not depend on the trajectory: the first evaluations, exact
+# sequences in FP64, and -- below -- that the converged FP32 points are converged points of
+# the FP64 metric (an FP64 continuation from them finds no more than it finds from FP64's own).
 
 
 def test_solve_fixed_iterations(w0):
@@ -142,10 +144,39 @@ def test_solve_fixed_iterations(w0):
     m = out["metrics"][0, :rep.n_metrics]
     # the first line searches see the same comparisons as the FP64 solver
     np.testing.assert_allclose(m[:3], ref["metrics"][:3], rtol=1e-5)
-    assert abs(rep.final_metric - ref["report"].final_metric) <= TOL_TRAJECTORY * ref["report"].final_metric
     assert np.all(np.diff(m) <= 0)                 # every iteration lowers the metric
-    da = (out["alpha"][0] - ref["alpha"]) / job.wavelength
-    assert np.sqrt(np.mean(da ** 2)) < 5e-2
+
+
+# FP64 continuation of converged solves (FTOL 1e-6 on the relative metric change, 3
+# consecutive, all modes at once): measured on the 225 production patches, the metric drop an
+# FP64 handle still finds from the FP32 endpoints is 2.4e-5 median / 9.6e-5 max, from FP64's
+# own endpoints 2.3e-5 / 1.1e-4 (the reference's stopping rule stops short of a minimum by
+# about that much, in either precision).
+TOL_CONTINUATION_MAX = 2e-4
+
+
+def test_converged_fp32_points_are_fp64_converged():
+    w = workload("production88", n_patches=8, frames=4)
+    job = w.job
+    M = job.n_modes
+    conv = S.SolveSettings(mode_start=M, mode_step=M, max_iterations=2000, min_iterations=5, target_iterations=3,
+                           ftol=1e-6, max_metrics=2100)
+    s32 = _solver(w)
+    a32 = s32.run(conv)["alpha"]
+    s64 = _solver(w, "fp64")
+    a64 = s64.run(conv)["alpha"]
+
+    def drops(a):
+        s64.set_start_alpha(a)
+        reps = s64.run(conv)["reports"]
+        return np.array([(r.initial_metric - r.final_metric) / r.initial_metric for r in reps])
+
+    d32, d64 = drops(a32), drops(a64)
+    print(f"\nFP64 continuation drop from FP32 endpoints: median {np.median(d32):.2e} max {d32.max():.2e}; "
+          f"from FP64 endpoints: median {np.median(d64):.2e} max {d64.max():.2e}")
+    assert np.all(d32 >= -1e-9) and np.all(d64 >= -1e-9)     # a continuation never goes up
+    assert d32.max() <= TOL_CONTINUATION_MAX, d32
+    assert np.median(d32) <= 2.0 * np.median(d64) + 1e-6, (np.median(d32), np.median(d64))
 
 
 @pytest.mark.parametrize("cfg", ["plain64", "production88"])
@@ -216,8 +247,6 @@ def test_staged_solve_with_reshifts(w0):
     rep = out["reports"][0]
     assert rep.iterations == ref["report"].iterations
     np.testing.assert_allclose(out["metrics"][0, :3], ref["metrics"][:3], rtol=1e-5)
-    n = min(rep.n_metrics, len(ref["metrics"]))
-    np.testing.assert_allclose(out["metrics"][0, :n], ref["metrics"][:n], rtol=TOL_TRAJECTORY)
     # images were re-cut between the stages on the GPU exactly as in the FP64 solver
     sg, so = s.debug("shifts")[0], op.shifts()[0]
     assert np.any(so != 0)
@@ -289,3 +318,36 @@ def test_solve_n128_kl100_first_metrics():
                                       ftol=0.0, eps=1e-10, brent_tol=0.1))
     n = min(3, out["reports"][0].n_metrics, len(ref["metrics"]))
     np.testing.assert_allclose(out["metrics"][0, :n], ref["metrics"][:n], rtol=1e-5)
+
+
+def test_production_geometry_3x12():
+    """The production geometry exactly (88 x 88, 36 KL modes, 3 channels x 12 frames), one patch
+    of the production batch's generator: metric, Vogel and finite-difference gradients against
+    the FP64 oracle, and the exact derivative against central differences of the oracle's
+    metric on sampled entries."""
+    w = workload("production88", n_patches=1, frames=12)
+    job = w.job
+    assert job.n_images == 36 and job.n_modes == 36
+    s = _solver(w)
+    op = _oracle(w)
+    for scale in (0.0, 0.5, 1.0):
+        a = w.patches.alpha_true * scale
+        L = s.metric(a)[0]
+        Lo = op.metric(a[0])
+        assert abs(L - Lo) <= TOL_METRIC * abs(Lo), (scale, L, Lo)
+    a = w.patches.alpha_true * 0.7
+    g, _ = s.gradient(a, "vogel")
+    _, go = op.gradient(a[0], "vogel")
+    assert np.linalg.norm(g[0] - go) / np.linalg.norm(go) < TOL_GRAD
+    gf, _ = s.gradient(a, "fd")
+    _, gfo = op.gradient(a[0], "fd")
+    assert np.linalg.norm(gf[0] - gfo) / np.linalg.norm(gfo) < 1e-4
+    ge, _ = s.gradient(a, "exact")
+    h = 1e-4 * job.wavelength
+    rng = np.random.default_rng(7)
+    for _ in range(6):
+        j, m = int(rng.integers(job.n_images)), int(rng.integers(2, job.n_modes))
+        ap = a[0].copy(); ap[j, m] += h
+        am = a[0].copy(); am[j, m] -= h
+        fd = (op.metric(ap) - op.metric(am)) / (2 * h)
+        assert abs(ge[0, j, m] - fd) <= 1e-4 * max(abs(fd), 1e-3 * np.abs(ge[0]).max()), (j, m, ge[0, j, m], fd)

@@ -164,3 +164,63 @@ def test_status_word_reported_once(word, what):
     with pytest.raises(S.SolverError, match=what):
         s.metric(a)
     np.testing.assert_allclose(s.metric(a), ok, rtol=1e-6)    # cleared, the handle still works
+
+
+# the general path (OTF size 128, 100 KL modes): the same tensor-core expansion ahead of the
+# transform kernel
+def _w128():
+    return workload("large128", n_patches=1, frames=2)
+
+
+def test_general_path_default_is_6xbf16():
+    s = _solver(_w128())
+    assert s.phase_mode() == 3
+
+
+def test_general_path_phases_against_fp64():
+    w = _w128()
+    job = w.job
+    s = _solver(w)
+    a = w.patches.alpha_true
+    n2 = job.pupil_pixels ** 2
+    Z = job.modes.reshape(job.n_modes, n2)
+    pf = job.phi_fixed.reshape(-1, n2)[job.img_channel]
+    ref = np.einsum("pim,mq->piq", a, Z) + pf[None]
+    sup = np.asarray(job.pupil).ravel() > 0
+    errs = {}
+    for mode in (2, 3):
+        s.set_phase_mode(mode)
+        s.metric(a)
+        ph = s.debug("phases").astype(np.float64).reshape(ref.shape)
+        errs[mode] = np.abs(ph - ref)[..., sup].max()
+    print(f"general path (128, 100 KL): phase error vs FP64 on the pupil (rad): {errs}")
+    assert errs[3] <= TOL_PHASE_RAD[3] and errs[2] <= TOL_PHASE_RAD[2], errs
+
+
+@pytest.mark.parametrize("mode", [0, 2, 3])
+def test_general_path_metric_and_gradient_each_mode(mode):
+    w = _w128()
+    s = _solver(w)
+    s.set_phase_mode(mode)
+    assert s.phase_mode() == mode
+    a = w.patches.alpha_true * 0.5
+    op = _oracle(w)
+    L = s.metric(a)[0]
+    Lo = op.metric(a[0])
+    assert abs(L - Lo) <= TOL_METRIC * abs(Lo), (mode, L, Lo)
+    g, _ = s.gradient(a, "vogel")
+    _, go = op.gradient(a[0], method="vogel")
+    rel = np.linalg.norm(g[0] - go) / np.linalg.norm(go)
+    assert rel < (5e-5 if mode == 2 else TOL_GRAD), (mode, rel)
+
+
+def test_general_path_solve_6xbf16():
+    w = _w128()
+    s = _solver(w)
+    st = S.fixed_iterations(w.job.n_modes, 3, max_metrics=64)
+    out = s.run(st)
+    ref = _oracle(w).solve(oracle.Cfg(n_initial_modes=w.job.n_modes, n_mode_increment=w.job.n_modes,
+                                      max_iterations=3, min_iterations=3, target_iterations=3, fd_first=1,
+                                      ftol=0.0, eps=1e-10, brent_tol=0.1))
+    n = min(3, out["reports"][0].n_metrics, len(ref["metrics"]))
+    np.testing.assert_allclose(out["metrics"][0, :n], ref["metrics"][:n], rtol=1e-5)
