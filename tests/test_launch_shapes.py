@@ -9,13 +9,20 @@ from tests.conftest import workload
 
 pytestmark = pytest.mark.gpu
 
+# k_eval: 512 threads, or the warp-specialised k_eval_ws with 512 transform and 64 helper threads
+EVAL_WS = 576
+
 # (workload, shapes to compare): the fused path (64, 88) tunes k_eval and k_adjoint, the
-# general path (128) k_forward and k_adjoint
+# general path (128) k_forward and k_adjoint.  fused88batch gives every block of the
+# evaluation several work items (chunks of several objects and patches), with gradient
+# evaluations among them.
 CASES = {
     "fused64": (lambda: workload("plain64"), [dict(eval_threads=512, adjoint_threads=256),
-                                      dict(eval_threads=384, adjoint_threads=512)]),
+                                      dict(eval_threads=EVAL_WS, adjoint_threads=512)]),
     "fused88": (lambda: workload("production88", n_patches=2, frames=4), [dict(eval_threads=512, adjoint_threads=256),
-                                                             dict(eval_threads=384, adjoint_threads=512)]),
+                                                             dict(eval_threads=EVAL_WS, adjoint_threads=512)]),
+    "fused88batch": (lambda: workload("production88", n_patches=64, frames=12),
+                     [dict(eval_threads=512, adjoint_threads=512), dict(eval_threads=EVAL_WS, adjoint_threads=512)]),
     "general128": (lambda: workload("large128", n_patches=1, frames=2), [dict(forward_threads=512, adjoint_threads=512),
                                                                 dict(forward_threads=1024, adjoint_threads=1024)]),
 }
