@@ -321,6 +321,53 @@ int rdxg_debug_copy(rdxg_solver* h, int32_t which, void* out, size_t bytes);
  * message, and clears it).  No counterpart in the reference. */
 int rdxg_debug_set(rdxg_solver* h, int32_t which, const void* in, size_t bytes);
 
+/* ---- Once-per-job static inputs (host code, no device work) ----
+ * What redux computes once per job on the master and ships in GlobalData; a caller may keep
+ * using redux's own classes for these, or call these and pass the results in rdxg_static. */
+
+/* Pupil::calculatePupilSize (src/lib/image/pupil.cpp:78-100): frequency cutoff, pupil radius
+ * in pixels and the pupil grid size (pupilPixels, doubled as the reference returns it) for an
+ * image of n_pixels at the given wavelength [m], telescope diameter [m] and image scale. */
+int rdxg_pupil_size(int32_t n_pixels, double wavelength, double telescope_d, double arcsec_per_pixel,
+                    double* frequency_cutoff, double* radius, int32_t* pupil_pixels);
+/* makePupil (src/lib/image/utils.cpp:68-124) centred on pixel (n/2, n/2), then
+ * Pupil::normalize (pupil.cpp:280-300): the anti-aliased annulus on an n x n grid scaled to
+ * [0, 1]; area = the makePupil sum before scaling. */
+int rdxg_make_pupil(int32_t n, double radius, double inner_radius, double* pupil, double* area);
+/* Pupil::generateSupport (pupil.cpp:245-277): pupil_support (capacity n*n) = indices where the
+ * pupil exceeds threshold, pupil_in_otf (or NULL; capacity n*n) = those indices in the N = 2n
+ * OTF grid, otf_support (capacity 4 n*n) = indices of the centred N x N grid where the
+ * pupil's autocorrelation exceeds threshold, area = the pupil summed over its support. */
+int rdxg_pupil_support(const double* pupil, int32_t n, double threshold, int32_t* pupil_support,
+                       int32_t* n_pupil_support, int32_t* pupil_in_otf, int32_t* otf_support, int32_t* n_otf_support,
+                       double* area);
+
+enum { RDXG_MODES_ZERNIKE = 0, RDXG_MODES_KL = 1 };
+typedef struct {
+    int32_t kind;            /* RDXG_MODES_ZERNIKE or RDXG_MODES_KL (BASIS) */
+    int32_t pupil_pixels;    /* n */
+    double radius;           /* pupil radius in pixels */
+    double wavelength;       /* [m]: the modes are scaled by 1/wavelength (GlobalData::get) */
+    double angle;            /* rotation of the basis (ModeInfo angle), radians */
+    double jacobian_scale;   /* scale of the tilt Jacobian (ModeSet::measureJacobian) */
+    int32_t kl_first;        /* KL_MIN_MODE: first Zernike of the KL expansion */
+    int32_t kl_last;         /* KL_MAX_MODE: last Zernike of the KL expansion */
+    double kl_cutoff;        /* SVD_REG: Zernike weights below this are dropped */
+} rdxg_mode_params;
+/* ModeSet::generate (src/lib/momfbd/modes.cpp:158-197, 348-437) with getNorms/normalize
+ * (443-462, 524-535) and measureJacobian (464-512): modes [n_modes][n][n] for the Noll
+ * indices mode_list (Zernike::getZernike, image/zernike.cpp:234-274; KL modes from the
+ * Karhunen-Loeve expansion of the Noll covariance, zernike.cpp:82-125, 367-479, with the tilts
+ * 2 and 3 kept Zernike), each with unit RMS over the pupil times 1/wavelength; atm_rms (or
+ * NULL) = the square root of each mode's Kolmogorov variance at D/r0 = 1; tilt_jacobian (or
+ * NULL) = [2][2] J_T_xy. */
+int rdxg_make_modes(const rdxg_mode_params* params, const int32_t* mode_list, int32_t n_modes, double* modes,
+                    double* atm_rms, double* tilt_jacobian);
+/* Solver::init's windows (solver.cpp:113-126): apodizeInPlace (image/utils.cpp:584-614) of
+ * all-ones patch_size^2 arrays with a blend of apodization (patch_size / 8 when negative)
+ * and half of it. */
+int rdxg_apodization_windows(int32_t patch_size, int32_t apodization, double* window, double* noise_window);
+
 /* Host drop-in for redux's conjugate_rdx minimiser with the Solver::run stage loop
  * (conjugate_gradient.cpp:128-256, helpers.cpp:58-215, solver.cpp:425-537) driving
  * caller-supplied callbacks.  n_modes stages the enabled-mode count exactly as Solver::run;

@@ -21,7 +21,8 @@ EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "r
             "rdxg_metric_noalloc", "rdxg_restore", "rdxg_restore_ex", "rdxg_set_phase_mode", "rdxg_phase_mode",
             "rdxg_autotune", "rdxg_set_launch_shape", "rdxg_get_launch_shape", "rdxg_set_fit_plane",
             "rdxg_set_initial_alpha", "rdxg_set_reg_alpha", "rdxg_debug_set", "rdxg_set_start_alpha",
-            "rdxg_set_recompute", "rdxg_recompute")
+            "rdxg_set_recompute", "rdxg_recompute", "rdxg_pupil_size", "rdxg_make_pupil", "rdxg_pupil_support",
+            "rdxg_make_modes", "rdxg_apodization_windows")
 
 
 class Geometry(C.Structure):
@@ -46,6 +47,12 @@ class SolveParams(C.Structure):
                 ("min_iterations", C.c_int32), ("target_iterations", C.c_int32), ("fd_first", C.c_int32),
                 ("max_metrics", C.c_int32), ("check_every", C.c_int32), ("ftol", C.c_double),
                 ("eps", C.c_double)]
+
+
+class ModeParams(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("pupil_pixels", C.c_int32), ("radius", C.c_double),
+                ("wavelength", C.c_double), ("angle", C.c_double), ("jacobian_scale", C.c_double),
+                ("kl_first", C.c_int32), ("kl_last", C.c_int32), ("kl_cutoff", C.c_double)]
 
 
 class LaunchShape(C.Structure):
@@ -113,6 +120,11 @@ def load(path: str = LIB_PATH):
     L.rdxg_get_launch_shape.argtypes = [vp, C.POINTER(LaunchShape)]
     L.rdxg_cg_minimize.argtypes = [C.c_int32, C.c_int32, C.POINTER(SolveParams), C.c_double, F_FN, DF_FN,
                                    SHIFT_FN, vp, vp, C.POINTER(PatchReport), vp]
+    L.rdxg_pupil_size.argtypes = [C.c_int32, C.c_double, C.c_double, C.c_double, vp, vp, vp]
+    L.rdxg_make_pupil.argtypes = [C.c_int32, C.c_double, C.c_double, vp, vp]
+    L.rdxg_pupil_support.argtypes = [vp, C.c_int32, C.c_double, vp, vp, vp, vp, vp, vp]
+    L.rdxg_make_modes.argtypes = [C.POINTER(ModeParams), vp, C.c_int32, vp, vp, vp]
+    L.rdxg_apodization_windows.argtypes = [C.c_int32, C.c_int32, vp, vp]
     _LIB = L
     return L
 

@@ -21,7 +21,7 @@ CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC"]
 
 CU_SOURCES = ["rdxg_api.cu", "rdxg_inst_common.cu", "rdxg_inst_32.cu", "rdxg_inst_64.cu",
               "rdxg_inst_88.cu", "rdxg_inst_128.cu", "rdxg_noalloc.cu", "rdxg_phase_tc.cu"]
-CXX_SOURCES = ["rdxg_host_cg.cpp"]
+CXX_SOURCES = ["rdxg_host_cg.cpp", "rdxg_setup.cpp"]
 
 
 def _nvcc():
