@@ -686,24 +686,31 @@ def main():
     # work in rounds where a patch needs a gradient (about one in ten)
     share = {"forward": rounds * kt["forward"], "accum": rounds * kt["accum"], "adjoint": ndf * kt["adjoint"]}
     dom = max(share, key=share.get)
-    achieved = per_launch[dom]["bytes"] / (kt[dom] / 1000.0) / 1e9
+    hbm_achieved = per_launch[dom]["bytes"] / (kt[dom] / 1000.0) / 1e9
+    fp32_tflops = {k: per_launch[k]["flops"] / (kt[k] / 1000.0) / 1e12 for k in per_launch}
     # DRAM bytes per image of the forward pass from ncu captures of the 64-patch batch
     # (k_eval: 80.9 MB read + 3.4 MB written for 2304 images; k_phase_tc: 0.95 MB read, its
-    # phases stay in L2), scaled to this launch by the images it evaluates
+    # phases stay in L2), scaled to this launch by the images it evaluates: a constant, not
+    # measured in this run
     traffic = {"forward": G * (84.3e6 + 0.95e6) / 2304.0} if (N, M) == (88, 36) else {}
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm"], "traffic": traffic.get(dom),
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 64-patch capture scaled by images"
-                if dom in traffic else None, "kernel": dom,
-                "peak_source": peaks["src"], "kernel_ms": kt,
-                "share_ms_per_step": share,
-                "fp32_tflops": {k: per_launch[k]["flops"] / (kt[k] / 1000.0) / 1e12 for k in per_launch}}
-    # the evaluation is bound by FP32 issue and shared-memory traffic, not by HBM: its nominal
-    # FFT flops against the FP32 CUDA-core peak (SMs x 128 lanes x 2 flops x maximum clock)
+    # the evaluation is bound by FP32 issue and shared-memory traffic of its transforms, not
+    # by HBM (ncu: issue-bound, DRAM well below its peak): the primary fraction is its nominal
+    # FFT flops (5 P log2 P per transform) plus the mode expansion against the FP32 CUDA-core
+    # peak (SMs x 128 lanes x 2 flops x maximum SM clock; computed, there is no measured FP32
+    # peak), the HBM fraction of its algorithmic bytes (8 N^2 per image) beside it
     props = torch.cuda.get_device_properties(local)
     fp32_peak = props.multi_processor_count * 128 * 2 * peaks["sm_max"] * 1e6 / 1e12
-    roofline["fp32_peak_tflops"] = fp32_peak
-    roofline["fp32_frac"] = {k: v / fp32_peak for k, v in roofline["fp32_tflops"].items()}
+    roofline = {"bound": "fp32", "achieved": fp32_tflops[dom], "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": fp32_tflops[dom] / fp32_peak,
+                "peak_source": "computed: SMs x 128 FP32 lanes x 2 flops x maximum SM clock",
+                "traffic": traffic.get(dom),
+                "traffic_source": "constant: ncu dram__bytes_read.sum + dram__bytes_write.sum of a 64-patch capture "
+                                  "(profiles/k_eval_88x88_64patches.md), scaled by images" if dom in traffic else None,
+                "kernel": dom, "kernel_ms": kt, "share_ms_per_step": share,
+                "hbm": {"achieved": hbm_achieved, "peak": peaks["hbm"], "unit": "GB/s",
+                        "frac": hbm_achieved / peaks["hbm"], "peak_source": peaks["src"]},
+                "fp32_tflops": fp32_tflops,
+                "fp32_frac": {k: v / fp32_peak for k, v in fp32_tflops.items()}}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_dev, "higher_is_better": True, "scaling": "weak",
@@ -793,11 +800,13 @@ def main():
             "within_1e-5": sum(1 for x in sr if abs(x) <= 1e-5)}
         # CPU baseline: the FP64 restatement on all host cores, one patch
         threads = os.cpu_count() or 1
-        tc, finals_cpu = cpu_port(job, cut, args.iterations, threads, 1)
-        line["cpu_baseline"] = {"value": 1.0 / tc, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"1 patch x {args.iterations} iterations, FP64 restatement, "
+        ncpu = min(4, P)
+        tc, finals_cpu = cpu_port(job, cut, args.iterations, threads, ncpu)
+        line["cpu_baseline"] = {"value": ncpu / tc, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{ncpu} patches x {args.iterations} iterations, FP64 restatement, "
                                           f"{threads} OpenMP threads over images",
-                                "final_metric_rel_diff_gpu_vs_cpu": abs(reps[0].final_metric - finals_cpu[0]) / abs(finals_cpu[0])}
+                                "final_metric_rel_diff_gpu_vs_cpu": [abs(reps[p].final_metric - finals_cpu[p]) /
+                                                                     abs(finals_cpu[p]) for p in range(ncpu)]}
     if rank == 0:
         print(json.dumps(line), flush=True)
     solver.close()

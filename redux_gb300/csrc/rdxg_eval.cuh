@@ -306,6 +306,42 @@ __device__ __forceinline__ void half_plane_core(cx<T>* a, cx<T>* b, const cx<T>*
     fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS, 0, R2, BAR>(b, a, 0, 1, LDS, tw);
 }
 
+// Arithmetic shared by k_eval and k_eval_ws, written with explicitly rounded operations so
+// that the compiler has no choice of contraction left and both kernels form the same bits.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// c PF at a pupil pixel of amplitude amp and phase ph; the pupil function itself in *pf
+template <typename T>
+__device__ __forceinline__ cx<T> pupil_field(T amp, T ph, T c, cx<T>* pf) {
+    cx<T> v = mkc<T>(0, 0);
+    if (amp > (T)0) {
+        T sn, cs;
+        sincos_t<T>(ph, &sn, &cs);
+        v = mkc<T>(mul_rn(amp, cs), mul_rn(amp, sn));
+    }
+    *pf = v;
+    return mkc<T>(mul_rn(v.x, c), mul_rn(v.y, c));
+}
+
+// One half-plane point of a chunk's sums: s = N^2 S (the transform's output), d = D, o = O'
+//     R += |D - O'S|^2,  Q += |S|^2,  P' += conj(D - O'S) S
+template <typename T>
+__device__ __forceinline__ void acc_point(Acc4<T>& u, cx<T> d, cx<T> o, cx<T> s, T inv) {
+    const T sx = mul_rn(s.x, inv), sy = mul_rn(s.y, inv);
+    const T osr = fma_rn(o.x, sx, -mul_rn(o.y, sy));
+    const T osi = fma_rn(o.x, sy, mul_rn(o.y, sx));
+    const T rx = add_rn(d.x, -osr), ry = add_rn(d.y, -osi);
+    u.r = add_rn(u.r, fma_rn(rx, rx, mul_rn(ry, ry)));
+    u.q = add_rn(u.q, fma_rn(sx, sx, mul_rn(sy, sy)));
+    u.pr = add_rn(u.pr, fma_rn(rx, sx, mul_rn(ry, sy)));
+    u.pi = add_rn(u.pi, fma_rn(rx, sy, -mul_rn(ry, sx)));
+}
+
 // One image of a chunk: the OTF on the half plane (half_plane_core with elem = |X|^2),
 // folded into the chunk's accumulators.  On entry the phases of this image are in phiBuf;
 // phiNext (or null) is the next image's, fetched into phiBuf once the row pass has read it.
@@ -325,15 +361,10 @@ __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phi
         a, b, tw,
         [&](int y, int x) {
             const int q = y * n + x;
-            const T amp = A[q];
-            cx<T> pf = mkc<T>(0, 0);
-            if (amp > (T)0) {
-                T sn, cs;
-                sincos_t<T>(phiBuf[q], &sn, &cs);
-                pf = mkc<T>(amp * cs, amp * sn);
-            }
+            cx<T> pf;
+            const cx<T> v = pupil_field<T>(A[q], phiBuf[q], c, &pf);
             if (keepPX) PF[q] = pf;
-            return cscale<T>(pf, c);
+            return v;
         },
         [&](int e, int x, cx<T> v) {
             if (keepPX) X[e * N + x] = v;
@@ -363,15 +394,9 @@ __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phi
         }
     }
     for (int h = threadIdx.x; h < nH; h += THREADS) {
-        const cx<T> sv = cscale<T>(a[hpos[h]], inv);
         const cx<T> d = (h < St::kPart ? a : b)[St::dh_slot(h)];
-        const cx<T> r = csub<T>(d, cmul<T>(oh[h], sv));
-        // R += |r|^2, Q += |S|^2, P' += conj(r) S
         Acc4<T> u = acc[h];
-        u.r += cnorm<T>(r);
-        u.q += cnorm<T>(sv);
-        u.pr += r.x * sv.x + r.y * sv.y;
-        u.pi += r.x * sv.y - r.y * sv.x;
+        acc_point<T>(u, d, oh[h], a[hpos[h]], inv);
         acc[h] = u;
     }
 }
@@ -578,14 +603,9 @@ __global__ void __launch_bounds__(TT + HT, 1) k_eval_ws(EvalParams<T> e) {
                 for (int k = 0; k < B; ++k) {
                     const int q = q0 + k * HT;
                     if (q >= n2) break;
-                    cx<T> pf = mkc<T>(0, 0);
-                    if (amp[k] > (T)0) {
-                        T sn, cs;
-                        sincos_t<T>(phv[k], &sn, &cs);
-                        pf = mkc<T>(amp[k] * cs, amp[k] * sn);
-                    }
+                    cx<T> pf;
+                    pfb[q] = pupil_field<T>(amp[k], phv[k], cn, &pf);
                     if (keepPX) PFg[q] = pf;
-                    pfb[q] = cscale<T>(pf, cn);
                 }
             }
         };
@@ -622,14 +642,8 @@ __global__ void __launch_bounds__(TT + HT, 1) k_eval_ws(EvalParams<T> e) {
                 for (int k = 0; k < B; ++k) {
                     const int h = h0 + k * HT;
                     if (h >= nH) break;
-                    const cx<T> sv = cscale<T>(sbuf[h], inv);
-                    const cx<T> r = csub<T>(dv[k], cmul<T>(ov[k], sv));
-                    // R += |r|^2, Q += |S|^2, P' += conj(r) S
                     Acc4<T> u = first ? Acc4<T>{0, 0, 0, 0} : acc[h];
-                    u.r += cnorm<T>(r);
-                    u.q += cnorm<T>(sv);
-                    u.pr += r.x * sv.x + r.y * sv.y;
-                    u.pi += r.x * sv.y - r.y * sv.x;
+                    acc_point<T>(u, dv[k], ov[k], sbuf[h], inv);
                     if (last) part[h] = u;
                     else acc[h] = u;
                 }
