@@ -78,6 +78,7 @@ def lib():
         L.orc_reorder_into.restype = C.c_int
         L.orc_reorder_into.argtypes = [f64p, C.c_int, C.c_int, f64p, C.c_int, C.c_int, C.c_int]
         L.orc_cons_apply.argtypes = [C.c_void_p, f64p, f64p]
+        L.orc_set_fast_fft.argtypes = [C.c_int]
         L.orc_cons_reverse_add.argtypes = [C.c_void_p, f64p, f64p, f64p]
         L.orc_restore.restype = C.c_int
         L.orc_restore.argtypes = [C.c_void_p, f64p, f64p, C.c_int, f64p]
@@ -221,6 +222,13 @@ def default_cfg(max_iterations=50, n_initial_modes=None, n_modes=None, min_itera
                min_iterations=max_iterations if min_iterations is None else min_iterations,
                target_iterations=target_iterations, fd_first=fd_first, ftol=ftol, eps=eps,
                brent_tol=0.1)
+
+
+def set_fast_fft(on: bool) -> None:
+    """Selects the transform of every later solve: the recursive FFT of the oracle proper
+    (False, the default) or the iterative Stockham form with precomputed tables (True; the
+    same factorisation, rounded differently), which bench.py's CPU baseline times."""
+    lib().orc_set_fast_fft(1 if on else 0)
 
 
 class OraclePatch:

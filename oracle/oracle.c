@@ -66,7 +66,21 @@ typedef struct {
     int fac[40];
     cplx* tw_fwd; /* exp(-2 pi i k / n), k < n */
     cplx* tw_bwd; /* exp(+2 pi i k / n) */
+    /* iterative form (fft1_fast): per stage s, twiddles exp(-+2 pi i r k / (NS R)) for k < NS,
+     * r < R (interleaved cos, sin), NS = product of the earlier radices; cos and sin of
+     * 2 pi q / R for each odd radix */
+    double* st_tw[2];
+    int st_off[41];
+    double* odd_cs;
+    int odd_off[40];
 } fft_plan;
+
+/* Which transform the solver's FFTs use: 0 the recursive one above (the oracle proper), 1 the
+ * iterative Stockham form with precomputed tables and real arithmetic (orc_set_fast_fft; used
+ * to time the CPU baseline: the same factorisation and the same DFT, rounded differently). */
+static int g_fast_fft = 0;
+void orc_set_fast_fft(int on) { g_fast_fft = on ? 1 : 0; }
+static void plan_fast_init(fft_plan* p);
 
 static void plan_init(fft_plan* p, int n) {
     p->n = n;
@@ -85,12 +99,51 @@ static void plan_init(fft_plan* p, int n) {
         p->tw_fwd[k] = cos(a) - I * sin(a);
         p->tw_bwd[k] = cos(a) + I * sin(a);
     }
+    plan_fast_init(p);
+}
+
+static void plan_fast_init(fft_plan* p) {
+    const int n = p->n;
+    int tot = 0, ns = 1, nodd = 0;
+    for (int s = 0; s < p->nfac; ++s) {
+        p->st_off[s] = tot;
+        tot += ns * p->fac[s];
+        ns *= p->fac[s];
+        p->odd_off[s] = nodd;
+        if (p->fac[s] % 2) nodd += p->fac[s];
+    }
+    p->st_off[p->nfac] = tot;
+    for (int d = 0; d < 2; ++d) p->st_tw[d] = (double*)malloc(sizeof(double) * 2 * (size_t)(tot > 0 ? tot : 1));
+    p->odd_cs = (double*)malloc(sizeof(double) * 2 * (size_t)(nodd > 0 ? nodd : 1));
+    ns = 1;
+    for (int s = 0; s < p->nfac; ++s) {
+        const int R = p->fac[s];
+        for (int k = 0; k < ns; ++k)
+            for (int r = 0; r < R; ++r) {
+                const double a = 2.0 * M_PI * (double)r * (double)k / (double)(ns * R);
+                const int o = 2 * (p->st_off[s] + k * R + r);
+                p->st_tw[0][o] = cos(a); p->st_tw[0][o + 1] = -sin(a);
+                p->st_tw[1][o] = cos(a); p->st_tw[1][o + 1] = sin(a);
+            }
+        if (R % 2)
+            for (int q = 0; q < R; ++q) {
+                p->odd_cs[2 * (p->odd_off[s] + q)] = cos(2.0 * M_PI * q / R);
+                p->odd_cs[2 * (p->odd_off[s] + q) + 1] = sin(2.0 * M_PI * q / R);
+            }
+        ns *= R;
+    }
+    (void)n;
 }
 
 static void plan_free(fft_plan* p) {
     free(p->tw_fwd);
     free(p->tw_bwd);
+    free(p->st_tw[0]);
+    free(p->st_tw[1]);
+    free(p->odd_cs);
     p->tw_fwd = p->tw_bwd = NULL;
+    p->st_tw[0] = p->st_tw[1] = NULL;
+    p->odd_cs = NULL;
 }
 
 /* out[0..L) = DFT_L of in[q*istride]; fi = index into p->fac; L = prod fac[fi..] */
@@ -136,9 +189,93 @@ static void fft_rec(const fft_plan* p, const cplx* tw, cplx* out, const cplx* in
     if (tt != t) free(tt);
 }
 
+/* Iterative Stockham transform of the n values in a (interleaved re, im); b is scratch of the
+ * same size.  Returns the buffer holding the result. */
+static double* fft1_fast_core(const fft_plan* p, double* a, double* b, int sign) {
+    const int n = p->n;
+    const double* tws = p->st_tw[sign < 0 ? 0 : 1];
+    const double dsg = sign < 0 ? -1.0 : 1.0;
+    int ns = 1;
+    double vr[64], vi[64];
+    for (int s = 0; s < p->nfac; ++s) {
+        const int R = p->fac[s];
+        const int bf = n / R;
+        const double* tw = tws + 2 * p->st_off[s];
+        for (int j = 0; j < bf; ++j) {
+            const int k = j % ns;
+            for (int r = 0; r < R; ++r) {
+                vr[r] = a[2 * (j + r * bf)];
+                vi[r] = a[2 * (j + r * bf) + 1];
+            }
+            if (ns > 1) {
+                const double* w = tw + 2 * k * R;
+                for (int r = 1; r < R; ++r) {
+                    const double xr = vr[r], xi = vi[r];
+                    vr[r] = xr * w[2 * r] - xi * w[2 * r + 1];
+                    vi[r] = xr * w[2 * r + 1] + xi * w[2 * r];
+                }
+            }
+            const int d0 = (j / ns) * ns * R + k;
+            if (R == 2) {
+                b[2 * d0] = vr[0] + vr[1]; b[2 * d0 + 1] = vi[0] + vi[1];
+                b[2 * (d0 + ns)] = vr[0] - vr[1]; b[2 * (d0 + ns) + 1] = vi[0] - vi[1];
+            } else if (R == 4) {
+                const double a0r = vr[0] + vr[2], a0i = vi[0] + vi[2], a1r = vr[0] - vr[2], a1i = vi[0] - vi[2];
+                const double b0r = vr[1] + vr[3], b0i = vi[1] + vi[3];
+                /* (v1 - v3) * i sign */
+                const double tr = vr[1] - vr[3], ti = vi[1] - vi[3];
+                const double b1r = -dsg * ti, b1i = dsg * tr;
+                b[2 * d0] = a0r + b0r; b[2 * d0 + 1] = a0i + b0i;
+                b[2 * (d0 + ns)] = a1r + b1r; b[2 * (d0 + ns) + 1] = a1i + b1i;
+                b[2 * (d0 + 2 * ns)] = a0r - b0r; b[2 * (d0 + 2 * ns) + 1] = a0i - b0i;
+                b[2 * (d0 + 3 * ns)] = a1r - b1r; b[2 * (d0 + 3 * ns) + 1] = a1i - b1i;
+            } else {
+                /* odd radix: pair x[q] with x[R-q] */
+                const double* cs = p->odd_cs + 2 * p->odd_off[s];
+                const int H = (R - 1) / 2;
+                double ar[32], ai[32], br[32], bi[32];
+                double y0r = vr[0], y0i = vi[0];
+                for (int q = 1; q <= H; ++q) {
+                    ar[q] = vr[q] + vr[R - q]; ai[q] = vi[q] + vi[R - q];
+                    br[q] = vr[q] - vr[R - q]; bi[q] = vi[q] - vi[R - q];
+                    y0r += ar[q]; y0i += ai[q];
+                }
+                b[2 * d0] = y0r; b[2 * d0 + 1] = y0i;
+                for (int u = 1; u <= H; ++u) {
+                    double Ar = vr[0], Ai = vi[0], Br = 0, Bi = 0;
+                    for (int q = 1; q <= H; ++q) {
+                        const int kk = (q * u) % R;
+                        Ar += ar[q] * cs[2 * kk]; Ai += ai[q] * cs[2 * kk];
+                        Br += br[q] * cs[2 * kk + 1]; Bi += bi[q] * cs[2 * kk + 1];
+                    }
+                    /* y[u] = A + i sign B, y[R-u] = A - i sign B */
+                    const double ibr = -dsg * Bi, ibi = dsg * Br;
+                    b[2 * (d0 + u * ns)] = Ar + ibr; b[2 * (d0 + u * ns) + 1] = Ai + ibi;
+                    b[2 * (d0 + (R - u) * ns)] = Ar - ibr; b[2 * (d0 + (R - u) * ns) + 1] = Ai - ibi;
+                }
+            }
+        }
+        double* t = a; a = b; b = t;
+        ns *= R;
+    }
+    return a;
+}
+
 /* in-place 1-D transform of x[0..n) with stride; sign<0 forward (FFTW_FORWARD) */
 static void fft1(const fft_plan* p, cplx* x, long stride, int sign, cplx* work, cplx* work2) {
     const int n = p->n;
+    if (g_fast_fft && p->nfac > 0) {
+        int ok = 1;
+        for (int s = 0; s < p->nfac; ++s)
+            if (p->fac[s] > 63) ok = 0;
+        if (ok) {
+            double* a = (double*)work;
+            for (int i = 0; i < n; ++i) { a[2 * i] = creal(x[i * stride]); a[2 * i + 1] = cimag(x[i * stride]); }
+            const double* r = fft1_fast_core(p, a, (double*)work2, sign);
+            for (int i = 0; i < n; ++i) x[i * stride] = r[2 * i] + I * r[2 * i + 1];
+            return;
+        }
+    }
     for (int i = 0; i < n; ++i) work[i] = x[i * stride];
     fft_rec(p, sign < 0 ? p->tw_fwd : p->tw_bwd, work2, work, 1, 0, n, 1);
     for (int i = 0; i < n; ++i) x[i * stride] = work2[i];
