@@ -279,9 +279,7 @@ int32_t rdxg_recompute(const rdxg_solver* h);
 int rdxg_profile_kernels(rdxg_solver* h, int32_t reps, double* ms);
 
 /* Launch shapes: threads per block of the kernels that dominate a round.  eval_threads: the
- * fused evaluation (512: k_eval; 576: its warp-specialised form k_eval_ws, 512 transform
- * threads and 64 helper threads, offered where its shared memory fits; 0 on the general
- * path); forward_threads: the general
+ * fused evaluation k_eval (512 or 384; 0 on the general path); forward_threads: the general
  * path's transform kernel k_forward (256 or 512, 512 or 1024 at OTF size 128; 0 on the fused
  * path); adjoint_threads: the analytic gradient k_adjoint (same choices as forward).  No
  * shape changes a result: every element is computed by the same arithmetic. */

@@ -99,7 +99,6 @@ struct rdxg_solver {
     // launch shapes (0 default block size, 1 the alternative) and how they are chosen:
     // tune 1 = measured on the first solve (or taken from the planner's table), 0 = pinned
     int shapeEval = 0, shapeFwd = 0, shapeAdj = 0;
-    bool evalWs = false;   // the warp-specialised evaluation fits this geometry's shared memory
     int tune = 1;
     bool tuned = false;
     // FIT_PLANE: the fitted plane of every (patch, object), slopes along y and x
@@ -755,7 +754,6 @@ int setup_fused(rdxg_solver* h, const rdxg_static* s) {
     size_t fdSmem = 0;
     with_eval(N, [&](auto L) { fdSmem = decltype(L)::fd_smem(h->nH); });
     h->fusedFd = fdSmem + 1024 <= kMaxSmem;   // 1 KB left for static shared memory
-    with_eval(N, [&](auto L) { h->evalWs = decltype(L)::smem_ws(h->nH) <= kMaxSmem; });
     h->evalGrid = h->numSMs * occ;
     h->reduceGrid = h->numSMs * 8;
     h->phaseGrid = h->numSMs * 4;
@@ -1774,10 +1772,9 @@ int time_kernel(rdxg_solver* h, int k, int reps, cudaEvent_t e0, cudaEvent_t e1,
 // Launch-shape planner: the counterpart of the reference's FFTW_MEASURE planning
 // (fouriertransform.cpp:73-90), which times candidate transform plans once per size and
 // keeps the fastest.  The candidates are the block sizes compiled for the kernels that
-// dominate a round -- k_eval (fused path: 512 threads, or its warp-specialised form k_eval_ws
-// with 512 transform and 64 helper threads), k_forward (general path) and k_adjoint (256 or
-// 512 threads, 512 or 1024 at N = 128) -- and no choice changes a result: every element of
-// these kernels is computed by the same arithmetic whatever the form or block size.
+// dominate a round -- k_eval (fused path: 512 or 384 threads), k_forward (general path) and
+// k_adjoint (256 or 512 threads, 512 or 1024 at N = 128) -- and no choice changes a result:
+// every element of these kernels is computed by the same arithmetic whatever the block size.
 // (The radix plan of each size is fixed by its shared-memory tile.)  The first solve of a
 // handle measures the candidates on its loaded batch (the adjoint on a tenth of the patches,
 // the share of a solve round that asks for gradients), unless a handle of the same geometry
@@ -1865,7 +1862,7 @@ int plan_shapes_once(rdxg_solver* h) {
 }
 
 int threads_of(const rdxg_solver* h, int family, int variant) {
-    if (family == 0) return h->fused ? (variant ? (h->evalWs ? kEvalThreadsAlt : 0) : kEvalThreads) : 0;
+    if (family == 0) return h->fused ? (variant ? kEvalThreadsAlt : kEvalThreads) : 0;
     if (family == 1 && h->fused) return 0;
     const int base = h->N >= 128 ? 512 : 256;
     return (variant && !h->fp64) ? 2 * base : base;

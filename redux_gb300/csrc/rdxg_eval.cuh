@@ -267,8 +267,8 @@ __device__ __forceinline__ void stage_phi(T* buf, const T* __restrict__ phi_g) {
 // times the inverse transform in those columns.  afterRows, afterCols1, afterPack run after
 // the row pass, the first column stage and the packing stage (where the caller issues copies
 // into the free parts of the tiles); midColumns runs between the two stages along y.
-template <typename T, int N, int THREADS, typename BAR = BarBlock, typename Pupil, typename Elem, typename HR,
-          typename HC, typename HP, typename HM>
+template <typename T, int N, int THREADS, typename Pupil, typename Elem, typename HR, typename HC, typename HP,
+          typename HM>
 __device__ __forceinline__ void half_plane_core(cx<T>* a, cx<T>* b, const cx<T>* tw, Pupil pupil, Elem elem,
                                                 HR afterRows, HC afterCols1, HP afterPack, HM midColumns) {
     constexpr int LDS = Tile<N>::LDS;
@@ -277,23 +277,23 @@ __device__ __forceinline__ void half_plane_core(cx<T>* a, cx<T>* b, const cx<T>*
     static_assert(R1 % 4 == 0, "the pruned first stage needs a radix divisible by 4");
     T* af = reinterpret_cast<T*>(a);
     // rows [N/4, 3N/4): the pupil field -> b -> a
-    fft_stage_fn<T, N, R1, 1, -1, N / 2, THREADS, LO, HI, BAR>(
+    fft_stage_fn<T, N, R1, 1, -1, N / 2, THREADS, LO, HI>(
         N / 4, tw, [&](int y, int x) { return pupil(y - N / 4, x - N / 4); },
         [&](int y, int e, cx<T> v) { b[y * LDS + e] = v; });
     afterRows();
-    fft_stage_pp<T, N, R2, R1, -1, N / 2, THREADS, 0, R2, BAR>(b, a, N / 4, LDS, 1, tw);
+    fft_stage_pp<T, N, R2, R1, -1, N / 2, THREADS>(b, a, N / 4, LDS, 1, tw);
     // all columns (a -> b), then the last stage into the packed rows of a
-    fft_stage_pp<T, N, R1, 1, -1, N, THREADS, LO, HI, BAR>(a, b, 0, 1, LDS, tw);
+    fft_stage_pp<T, N, R1, 1, -1, N, THREADS, LO, HI>(a, b, 0, 1, LDS, tw);
     afterCols1();
-    fft_stage_fn<T, N, R2, R1, -1, N, THREADS, 0, R2, BAR>(
+    fft_stage_fn<T, N, R2, R1, -1, N, THREADS, 0, R2>(
         0, tw, [&](int x, int e) { return b[e * LDS + x]; },
         [&](int x, int e, cx<T> v) { af[(e >> 1) * 2 * LDS + 2 * x + (e & 1)] = elem(e, x, v); });
     afterPack();
     // inverse along x on the N/2 packed rows (a -> b -> a)
-    fft_stage_pp<T, N, R1, 1, +1, N / 2, THREADS, 0, R1, BAR>(a, b, 0, LDS, 1, tw);
-    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS, 0, R2, BAR>(b, a, 0, LDS, 1, tw);
+    fft_stage_pp<T, N, R1, 1, +1, N / 2, THREADS>(a, b, 0, LDS, 1, tw);
+    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS>(b, a, 0, LDS, 1, tw);
     // inverse along y on the columns [0, N/2), splitting the packed rows as they are loaded
-    fft_stage_fn<T, N, R1, 1, +1, N / 2, THREADS, 0, R1, BAR>(
+    fft_stage_fn<T, N, R1, 1, +1, N / 2, THREADS, 0, R1>(
         0, tw,
         [&](int k, int e) {
             const cx<T> z = a[(e >> 1) * LDS + k];
@@ -303,11 +303,12 @@ __device__ __forceinline__ void half_plane_core(cx<T>* a, cx<T>* b, const cx<T>*
         },
         [&](int k, int e, cx<T> v) { b[e * LDS + k] = v; });
     midColumns();
-    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS, 0, R2, BAR>(b, a, 0, 1, LDS, tw);
+    fft_stage_pp<T, N, R2, R1, +1, N / 2, THREADS>(b, a, 0, 1, LDS, tw);
 }
 
-// Arithmetic shared by k_eval and k_eval_ws, written with explicitly rounded operations so
-// that the compiler has no choice of contraction left and both kernels form the same bits.
+// Arithmetic of the evaluation written with explicitly rounded operations, so that the
+// compiler has no choice of contraction left: every form of the kernel that uses these
+// helpers forms the same bits.
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
@@ -465,193 +466,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
             it = nit;
         }
         jj = nextJj;
-    }
-}
-
-// ----------------------------------------------------------------------------------
-// The same evaluation with the block split into transform warps and helper warps
-// (warp specialisation).  The TT transform threads run only the transforms of
-// half_plane_core, synchronised among themselves by a named barrier.  The HT helper threads
-// meanwhile form the pupil field c PF of the next image (sincos of its phases, read from
-// global memory) and fold the previous image's OTF into the chunk's accumulators (image
-// transform and reference object read from global memory), so neither runs between the
-// transform stages.  The results are the same bits as k_eval: every value is formed by the
-// same expressions, and the images of a chunk are added in the same order.
-//
-// The two groups hand over two shared buffers through named barriers, producer arrive /
-// consumer sync (bar.arrive / bar.sync over all TT + HT threads):
-//   pfb  (c PF of one image):  helpers fill it, FULL; transform warps read it in the first
-//                              row stage, EMPTY;
-//   sbuf (the OTF on the half plane):  transform warps copy it out of the tile after the
-//                              last stage, FULL; helpers accumulate it, EMPTY.
-// Both groups walk the same sequence of images (items blockIdx.x, + gridDim.x, ...), and for
-// every barrier the arrivals of one group and the waits of the other pair up one to one: per
-// image the transform warps wait on pfb FULL and sbuf EMPTY and arrive on pfb EMPTY (all but
-// the last image) and sbuf FULL; the helpers arrive on pfb FULL and sbuf EMPTY once before the
-// first image and then once per image but the last, and wait on pfb EMPTY (all but the last)
-// and sbuf FULL.  A group can only arrive on a barrier again after the other group has passed
-// its previous phase, so no two phases of one barrier are ever open at once.
-// ----------------------------------------------------------------------------------
-enum : int { kBarWsT = 1, kBarWsPfFull = 2, kBarWsPfEmpty = 3, kBarWsSbFull = 4, kBarWsSbEmpty = 5 };
-
-template <int ID, int COUNT>
-__device__ __forceinline__ void named_arrive() {
-    asm volatile("bar.arrive %0, %1;\n" ::"n"(ID), "n"(COUNT) : "memory");
-}
-template <int ID, int COUNT>
-__device__ __forceinline__ void named_sync() {
-    asm volatile("bar.sync %0, %1;\n" ::"n"(ID), "n"(COUNT) : "memory");
-}
-
-// the block's sequence of images: (item, image within the item), advanced in place
-struct WsCursor {
-    int item, jj, nItems, stride;
-    EvalItem it;
-    __device__ bool has_next() const { return jj + 1 < it.count || item + stride < nItems; }
-};
-__device__ __forceinline__ void ws_advance(WsCursor& c, const EvalItem* items) {
-    if (++c.jj >= c.it.count) {
-        c.jj = 0;
-        c.item += c.stride;
-        c.it = items[c.item];
-    }
-}
-
-template <typename T, int N, int TT, int HT>
-__global__ void __launch_bounds__(TT + HT, 1) k_eval_ws(EvalParams<T> e) {
-    constexpr int n = N / 2, n2 = n * n, N2 = N * N, ALL = TT + HT;
-    static_assert(TT % 32 == 0 && HT % 32 == 0, "whole warps per group");
-    using BarT = BarNamed<kBarWsT, TT>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int nH = e.hp.nH;
-    // shared memory: two tiles | twiddles | accumulators (nH records) | OTF on the half plane
-    //                (nH) | c PF of one image (n2) | tile positions (16-bit)
-    cx<T>* a = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* b = a + Tile<N>::ELEMS;
-    cx<T>* tw = b + Tile<N>::ELEMS;
-    Acc4<T>* acc = reinterpret_cast<Acc4<T>*>(tw + N);
-    static_assert((2 * Tile<N>::ELEMS + N) % 2 == 0, "accumulator records 16-byte aligned");
-    cx<T>* sbuf = reinterpret_cast<cx<T>*>(acc + nH);
-    cx<T>* pfb = sbuf + nH;
-    uint16_t* hpos = reinterpret_cast<uint16_t*>(pfb + n2);
-    static_assert(Tile<N>::ELEMS <= 65536, "tile positions are 16-bit");
-    const int nItems = *e.L.nEval;
-    if ((int)blockIdx.x >= nItems) return;    // the whole block, before any barrier
-    WsCursor cur{(int)blockIdx.x, 0, nItems, (int)gridDim.x, e.L.eval[blockIdx.x]};
-    const T inv = (T)1 / (T)N2;
-    if (threadIdx.x < TT) {
-        // ---------------- transform warps ----------------
-        for (int k = threadIdx.x; k < N; k += TT) tw[k] = e.k.tw[k];
-        for (int h = threadIdx.x; h < nH; h += TT) hpos[h] = (uint16_t)e.hPos[h];
-        BarT::sync();
-        while (true) {
-            const bool next = cur.has_next();
-            const size_t g = (size_t)cur.it.p * e.k.I + cur.it.first + cur.jj;
-            const bool keepPX = cur.it.df && !e.k.recompute;
-            const bool keepS = cur.it.df && e.k.S != nullptr;
-            cx<T>* Xg = e.k.X + g * N2;
-            named_sync<kBarWsPfFull, ALL>();
-            half_plane_core<T, N, TT, BarT>(
-                a, b, tw, [&](int y, int x) { return pfb[y * n + x]; },
-                [&](int ee, int x, cx<T> v) {
-                    if (keepPX) Xg[ee * N + x] = v;
-                    return cnorm<T>(v);
-                },
-                [&] {
-                    if (next) named_arrive<kBarWsPfEmpty, ALL>();   // pfb read by the row stage
-                },
-                [] {}, [] {}, [] {});
-            named_sync<kBarWsSbEmpty, ALL>();
-            cx<T>* Sg = e.k.S + g * N2;
-            for (int h = threadIdx.x; h < nH; h += TT) {
-                const cx<T> v = a[hpos[h]];
-                sbuf[h] = v;
-                if (keepS) {
-                    // the full OTF from the half plane (S(-u) = conj S(u)) for the gradient kernels
-                    const cx<T> sv = cscale<T>(v, inv);
-                    const int cidx = e.hp.idx[h];
-                    const int cy = cidx / N, cxx = cidx % N;
-                    Sg[cidx] = sv;
-                    Sg[((N - cy) % N) * N + (N - cxx) % N] = mkc<T>(sv.x, -sv.y);
-                }
-            }
-            named_arrive<kBarWsSbFull, ALL>();
-            if (!next) break;
-            ws_advance(cur, e.L.eval);
-        }
-    } else {
-        // ---------------- helper warps ----------------
-        const int t = threadIdx.x - TT;
-        // c PF of the image at cursor c into pfb (and PF itself for a gradient evaluation)
-        auto pupil = [&](const WsCursor& c) {
-            const size_t g = (size_t)c.it.p * e.k.I + c.it.first + c.jj;
-            const T cn = e.k.otfNorm[e.k.imgCh[c.it.first + c.jj]];
-            const bool keepPX = c.it.df && !e.k.recompute;
-            const T* __restrict__ ph = e.phi + g * n2;
-            const T* __restrict__ A = e.k.A;
-            cx<T>* PFg = e.k.PF + g * n2;
-            constexpr int B = 4;
-            for (int q0 = t; q0 < n2; q0 += HT * B) {
-                T amp[B], phv[B];
-#pragma unroll
-                for (int k = 0; k < B; ++k) {
-                    const int q = q0 + k * HT;
-                    amp[k] = q < n2 ? __ldg(A + q) : (T)0;
-                    phv[k] = q < n2 ? __ldg(ph + q) : (T)0;
-                }
-#pragma unroll
-                for (int k = 0; k < B; ++k) {
-                    const int q = q0 + k * HT;
-                    if (q >= n2) break;
-                    cx<T> pf;
-                    pfb[q] = pupil_field<T>(amp[k], phv[k], cn, &pf);
-                    if (keepPX) PFg[q] = pf;
-                }
-            }
-        };
-        pupil(cur);
-        named_arrive<kBarWsPfFull, ALL>();
-        named_arrive<kBarWsSbEmpty, ALL>();
-        WsCursor nc = cur;
-        while (true) {
-            const bool next = cur.has_next();
-            if (next) {
-                ws_advance(nc, e.L.eval);
-                named_sync<kBarWsPfEmpty, ALL>();
-                pupil(nc);
-                named_arrive<kBarWsPfFull, ALL>();
-            }
-            const EvalItem it = cur.it;
-            const size_t g = (size_t)it.p * e.k.I + it.first + cur.jj;
-            const size_t po = (size_t)it.p * e.k.nObj + it.o;
-            const bool first = cur.jj == 0, last = cur.jj + 1 == it.count;
-            const cx<T>* __restrict__ Dg = e.Dh + g * nH;
-            const cx<T>* __restrict__ Og = e.Oh + po * nH;
-            Acc4<T>* part = e.part + (size_t)(it.p * e.hp.chunksPerPatch + it.chunk) * nH;
-            named_sync<kBarWsSbFull, ALL>();
-            constexpr int B = 4;
-            for (int h0 = t; h0 < nH; h0 += HT * B) {
-                cx<T> dv[B], ov[B];
-#pragma unroll
-                for (int k = 0; k < B; ++k) {
-                    const int h = h0 + k * HT;
-                    dv[k] = h < nH ? Dg[h] : mkc<T>(0, 0);
-                    ov[k] = h < nH ? Og[h] : mkc<T>(0, 0);
-                }
-#pragma unroll
-                for (int k = 0; k < B; ++k) {
-                    const int h = h0 + k * HT;
-                    if (h >= nH) break;
-                    Acc4<T> u = first ? Acc4<T>{0, 0, 0, 0} : acc[h];
-                    acc_point<T>(u, dv[k], ov[k], sbuf[h], inv);
-                    if (last) part[h] = u;
-                    else acc[h] = u;
-                }
-            }
-            if (!next) break;
-            named_arrive<kBarWsSbEmpty, ALL>();
-            ws_advance(cur, e.L.eval);
-        }
     }
 }
 

@@ -169,16 +169,6 @@ template <> struct Plan<128> { static constexpr int R1 = 16, R2 = 8; };
 
 template <int N> struct Tile { static constexpr int LDS = N + 1; static constexpr int ELEMS = N * (N + 1); };
 
-// Barrier of the threads that run a transform: the whole block, or a named barrier of the
-// block's first COUNT threads when its other warps do other work at the same time (k_eval_ws).
-struct BarBlock {
-    __device__ static __forceinline__ void sync() { __syncthreads(); }
-};
-template <int ID, int COUNT> struct BarNamed {
-    static_assert(ID > 0 && ID < 16 && COUNT % 32 == 0, "named barrier id and thread count");
-    __device__ static __forceinline__ void sync() { asm volatile("bar.sync %0, %1;\n" ::"n"(ID), "n"(COUNT) : "memory"); }
-};
-
 // One Stockham stage over LINES lines starting at line0.  Element e of line l is at
 // s[l * lstride + e * estride].
 // Thread index read through volatile asm: kernels that run several transforms inside a
@@ -267,8 +257,7 @@ __device__ __forceinline__ void fft2d(cx<T>* s, const cx<T>* tw) {
 // per stage and one butterfly in registers at a time ----
 // RLO, RHI: only inputs r in [RLO, RHI) of each butterfly can be non-zero (the others are
 // known zeros and are neither loaded nor multiplied)
-template <typename T, int N, int R, int NS, int DIR, int LINES, int THREADS, int RLO = 0, int RHI = R,
-          typename BAR = BarBlock>
+template <typename T, int N, int R, int NS, int DIR, int LINES, int THREADS, int RLO = 0, int RHI = R>
 __device__ __forceinline__ void fft_stage_pp(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst, int line0,
                                              int lstride, int estride, const cx<T>* tw) {
     constexpr int BF = N / R;
@@ -298,14 +287,14 @@ __device__ __forceinline__ void fft_stage_pp(const cx<T>* __restrict__ src, cx<T
 #pragma unroll
         for (int r = 0; r < R; ++r) out[(idxD + r * NS) * estride] = v[r];
     }
-    BAR::sync();
+    __syncthreads();
 }
 
 // The same stage with the element loads and stores supplied by the caller: ld(line, e)
 // returns element e of a line, st(line, e, v) stores output element e.  Used to fold
 // element-wise work into the first or last stage of a pass.
-template <typename T, int N, int R, int NS, int DIR, int LINES, int THREADS, int RLO, int RHI,
-          typename BAR = BarBlock, typename LD, typename ST>
+template <typename T, int N, int R, int NS, int DIR, int LINES, int THREADS, int RLO, int RHI, typename LD,
+          typename ST>
 __device__ __forceinline__ void fft_stage_fn(int line0, const cx<T>* tw, LD ld, ST st) {
     constexpr int BF = N / R;
     constexpr int TOTAL = LINES * BF;
@@ -332,7 +321,7 @@ __device__ __forceinline__ void fft_stage_fn(int line0, const cx<T>* tw, LD ld, 
 #pragma unroll
         for (int r = 0; r < R; ++r) st(line, idxD + r * NS, v[r]);
     }
-    BAR::sync();
+    __syncthreads();
 }
 
 // 2-D transform in tile a (result in a), b is scratch of the same shape.

@@ -179,22 +179,15 @@ size_t EvalLauncher<T, N>::smem(int M, int nH) {
     } while (0)
 
 template <typename T, int N>
-size_t EvalLauncher<T, N>::smem_ws(int nH) {
-    // two tiles | twiddles | accumulators (4 x nH) | OTF on the half plane (nH) | c PF of one
-    // image | tile positions (16-bit)
-    return (size_t)(2 * Tile<N>::ELEMS + N + nH + (N / 2) * (N / 2)) * sizeof(cx<T>) + (size_t)4 * nH * sizeof(T) +
-           (size_t)nH * sizeof(uint16_t) + 16;
-}
-
-template <typename T, int N>
 cudaError_t EvalLauncher<T, N>::setup(int M, int npt, int nH) {
     cudaError_t e = cudaSuccess;
     const int sm = (int)smem(M, nH);
 #define RDXG_SET(NPT) e = raise_smem_limit(k_eval<T, N, kEvalThreads, NPT>, sm)
     RDXG_NPT_SWITCH(npt, RDXG_SET);
 #undef RDXG_SET
-    if (e == cudaSuccess && smem_ws(nH) <= kMaxSmem)
-        e = raise_smem_limit(k_eval_ws<T, N, kEvalWsThreads, kEvalHelpers>, smem_ws(nH));
+#define RDXG_SET(NPT) e = raise_smem_limit(k_eval<T, N, kEvalThreadsAlt, NPT>, sm)
+    if (e == cudaSuccess) RDXG_NPT_SWITCH(npt, RDXG_SET);
+#undef RDXG_SET
     if (e == cudaSuccess)
         e = raise_smem_limit(k_phase<T, N, kPhasePix, kMaxChunk>, (size_t)M * (kPhasePix + kMaxChunk) * sizeof(T));
     if (e == cudaSuccess && fd_smem(nH) + 1024 <= kMaxSmem)
@@ -218,8 +211,9 @@ template <typename T, int N>
 void EvalLauncher<T, N>::eval(const EvalParams<T>& e, int npt, int grid, cudaStream_t st) {
     const size_t sm = smem(e.k.M, e.hp.nH);
     if (e.k.shapeEval == 1) {
-        // warp-specialised form (the host offers it only where its shared memory fits)
-        k_eval_ws<T, N, kEvalWsThreads, kEvalHelpers><<<grid, kEvalThreadsAlt, smem_ws(e.hp.nH), st>>>(e);
+#define RDXG_LAUNCH(NPT) k_eval<T, N, kEvalThreadsAlt, NPT><<<grid, kEvalThreadsAlt, sm, st>>>(e)
+        RDXG_NPT_SWITCH(npt, RDXG_LAUNCH);
+#undef RDXG_LAUNCH
         return;
     }
 #define RDXG_LAUNCH(NPT) k_eval<T, N, kEvalThreads, NPT><<<grid, kEvalThreads, sm, st>>>(e)

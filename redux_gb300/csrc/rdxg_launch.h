@@ -68,18 +68,9 @@ void launch_add_plane(const double* plane, float* objects, int nPo, int ps, cuda
 #endif
 constexpr int kEvalThreads = RDXG_EVAL_THREADS;
 static_assert(kEvalThreads % 32 == 0 && kEvalThreads <= 1024, "block size");
-// the planner's alternative form of k_eval: k_eval_ws, kEvalWsThreads transform threads plus
-// kEvalHelpers helper threads (the same results: every value is formed by the same
-// expressions and every half-plane point is accumulated in image order)
-#ifndef RDXG_WS_THREADS
-#define RDXG_WS_THREADS 512
-#endif
-#ifndef RDXG_WS_HELPERS
-#define RDXG_WS_HELPERS 64
-#endif
-constexpr int kEvalWsThreads = RDXG_WS_THREADS;
-constexpr int kEvalHelpers = RDXG_WS_HELPERS;
-constexpr int kEvalThreadsAlt = kEvalWsThreads + kEvalHelpers;
+// the planner's alternative block size of k_eval (results are the same: each half-plane
+// point is accumulated by one thread, whatever the block size)
+constexpr int kEvalThreadsAlt = kEvalThreads == 384 ? 512 : 384;
 constexpr int kReduceThreads = 256;
 constexpr int kPhasePix = 256;      // pixels per block of the mode expansion
 constexpr int kMaxChunk = 8;        // images per chunk (upper bound)
@@ -95,7 +86,6 @@ template <typename T, int N> struct EvalLauncher {
     static void reduce(const EvalParams<T>& e, int grid, cudaStream_t st);
     static void phase(const EvalParams<T>& e, int grid, cudaStream_t st);
     static size_t smem(int M, int nH);
-    static size_t smem_ws(int nH);                   // shared memory of k_eval_ws (may exceed the limit)
     static int occupancy(int M, int npt, int nH);   // resident blocks per SM
     static int phase_tiles();                        // pixel tiles of the per-patch mode expansion
     static size_t fd_smem(int nH);                   // shared memory of the half-plane FD gradient

@@ -9,8 +9,8 @@ from tests.conftest import workload
 
 pytestmark = pytest.mark.gpu
 
-# k_eval: 512 threads, or the warp-specialised k_eval_ws with 512 transform and 64 helper threads
-EVAL_WS = 576
+# k_eval: 512 or 384 threads
+EVAL_ALT = 384
 
 # (workload, shapes to compare): the fused path (64, 88) tunes k_eval and k_adjoint, the
 # general path (128) k_forward and k_adjoint.  fused88batch gives every block of the
@@ -18,11 +18,11 @@ EVAL_WS = 576
 # evaluations among them.
 CASES = {
     "fused64": (lambda: workload("plain64"), [dict(eval_threads=512, adjoint_threads=256),
-                                      dict(eval_threads=EVAL_WS, adjoint_threads=512)]),
+                                      dict(eval_threads=EVAL_ALT, adjoint_threads=512)]),
     "fused88": (lambda: workload("production88", n_patches=2, frames=4), [dict(eval_threads=512, adjoint_threads=256),
-                                                             dict(eval_threads=EVAL_WS, adjoint_threads=512)]),
+                                                             dict(eval_threads=EVAL_ALT, adjoint_threads=512)]),
     "fused88batch": (lambda: workload("production88", n_patches=64, frames=12),
-                     [dict(eval_threads=512, adjoint_threads=512), dict(eval_threads=EVAL_WS, adjoint_threads=512)]),
+                     [dict(eval_threads=512, adjoint_threads=256), dict(eval_threads=EVAL_ALT, adjoint_threads=512)]),
     "general128": (lambda: workload("large128", n_patches=1, frames=2), [dict(forward_threads=512, adjoint_threads=512),
                                                                 dict(forward_threads=1024, adjoint_threads=1024)]),
 }
