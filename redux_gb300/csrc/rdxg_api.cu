@@ -72,6 +72,12 @@ struct rdxg_solver {
     bool fused = false;
     cudaStream_t side = nullptr;     // capture stream of the graph's conditional bodies
     unsigned long long* dLaunchCount = nullptr;   // kernel launches of a graph-run solve
+    // device loop of a solve graph (on the first handle of a solve): the handles' active
+    // counters, the rounds run and the overrun flag
+    int32_t** dActiveList = nullptr;
+    int activeListCap = 0;
+    long long* dRounds = nullptr;
+    int32_t* dOverrun = nullptr;
     double* dRestore = nullptr;      // restoration scratch (allocated on first use)
     double* dFc = nullptr;           // [nObj] frequency cutoffs of the restoration
     float* dRestoreOut = nullptr;    // [P][nObj][ps][ps] restored objects
@@ -1449,15 +1455,18 @@ int issue_round(const SolvePlan& pl, cudaStream_t st, const ShiftArgs& sar, Opt&
     return 0;
 }
 
-// Runs the rounds of every plan as one CUDA graph of `check` rounds per plan, one branch per
-// handle (forked from the first handle's stream; handles sharing a stream are issued one
-// after the other).  The kernels that are only needed in some rounds (image
-// re-initialisation after a re-shift, the adjoint, the finite-difference gradient) sit in
-// conditional nodes whose conditions k_shift sets from the round's work-list counters.  The
-// host launches the graph until no handle has an active patch.
+// Runs every plan's rounds as one CUDA graph, launched once per solve.  The graph is a WHILE
+// node whose body holds `check` rounds of every handle -- one branch per handle, forked from
+// the first handle's stream (handles sharing a stream are issued one after the other) and
+// joined -- followed by k_loop_cond, which keeps the loop going while any handle has an active
+// patch; the rounds run on the device with no host round trip.  The kernels that are only
+// needed in some rounds (image re-initialisation after a re-shift, the adjoint, the
+// finite-difference gradient) sit in IF nodes inside the body, whose conditions k_shift sets
+// from the round's work-list counters.
 int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
     rdxg_solver* h0 = plans[0].h;
     cudaStream_t origin = h0->stream;
+    const size_t nPlans = plans.size();
     for (SolvePlan& pl : plans) {
         rdxg_solver* h = pl.h;
         if (!h->side) CK(h, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
@@ -1469,22 +1478,52 @@ int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
         // the reset of every handle's state is complete before the graph runs on the origin
         if (h->stream != origin) CK(h, cudaStreamSynchronize(h->stream));
     }
-    const size_t nPlans = plans.size();
+    if (h0->activeListCap < (int)nPlans) {
+        dfree(h0, &h0->dActiveList, (size_t)h0->activeListCap * sizeof(int32_t*));
+        int r = dalloc_t(h0, &h0->dActiveList, nPlans);
+        if (r) return r;
+        h0->activeListCap = (int)nPlans;
+    }
+    if (!h0->dRounds) {
+        int r = dalloc_t(h0, &h0->dRounds, 1);
+        if (!r) r = dalloc_t(h0, &h0->dOverrun, 1);
+        if (r) return r;
+    }
+    {
+        std::vector<int32_t*> act(nPlans);
+        for (size_t k = 0; k < nPlans; ++k) act[k] = plans[k].h->dActive;
+        CK(h0, cudaMemcpyAsync(h0->dActiveList, act.data(), nPlans * sizeof(int32_t*), cudaMemcpyHostToDevice, origin));
+        CK(h0, cudaMemsetAsync(h0->dRounds, 0, sizeof(long long), origin));
+        CK(h0, cudaMemsetAsync(h0->dOverrun, 0, sizeof(int32_t), origin));
+        CK(h0, cudaStreamSynchronize(origin));   // the host vector goes out of scope
+    }
     std::vector<cudaEvent_t> ev(nPlans + 1, nullptr);
     cudaError_t ce = cudaSuccess;
     const char* what = "events";
     for (size_t k = 0; k <= nPlans && ce == cudaSuccess; ++k) ce = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+    // the top-level graph: one WHILE node (its condition starts at 1 on every launch)
+    cudaGraph_t top = nullptr, body = nullptr;
+    cudaGraphConditionalHandle loop = 0;
+    if (ce == cudaSuccess) { what = "graph"; ce = cudaGraphCreate(&top, 0); }
+    if (ce == cudaSuccess) {
+        what = "loop handle";
+        ce = cudaGraphConditionalHandleCreate(&loop, top, 1, cudaGraphCondAssignDefault);
+    }
+    if (ce == cudaSuccess) {
+        what = "loop node";
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = loop;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        if ((ce = cudaGraphAddNode(&node, top, nullptr, nullptr, 0, &np)) == cudaSuccess) body = np.conditional.phGraph_out[0];
+    }
     bool capturing = false;
     if (ce == cudaSuccess) {
         what = "begin capture";
-        ce = cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal);
+        ce = cudaStreamBeginCaptureToGraph(origin, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
         capturing = ce == cudaSuccess;
-    }
-    cudaGraph_t graph = nullptr;
-    if (ce == cudaSuccess) {
-        cudaStreamCaptureStatus status;
-        what = "capture info";
-        ce = cudaStreamGetCaptureInfo(origin, &status, nullptr, &graph, nullptr, nullptr, nullptr);
     }
     // fork: every other stream joins the capture after the origin's start
     if (ce == cudaSuccess && (ce = cudaEventRecord(ev[nPlans], origin)) == cudaSuccess) {
@@ -1496,10 +1535,11 @@ int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
             SolvePlan& pl = plans[k];
             rdxg_solver* h = pl.h;
             cudaStream_t st = h->stream;
-            // a conditional handle belongs to one conditional node: three new ones per round
+            // a conditional handle belongs to one conditional node: three new ones per round,
+            // in the graph that holds the nodes (the loop's body)
             cudaGraphConditionalHandle cond[3] = {};
             what = "conditional handle";
-            for (int c = 0; c < 3 && ce == cudaSuccess; ++c) ce = cudaGraphConditionalHandleCreate(&cond[c], graph, 0, 0);
+            for (int c = 0; c < 3 && ce == cudaSuccess; ++c) ce = cudaGraphConditionalHandleCreate(&cond[c], body, 0, 0);
             if (ce != cudaSuccess) break;
             ShiftArgs sa = pl.sa;
             sa.useConditions = 1;
@@ -1534,58 +1574,73 @@ int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
                                                               cudaStreamSetCaptureDependencies)) != cudaSuccess)
                     return;
                 what = "body capture";
-                cudaGraph_t body = np.conditional.phGraph_out[0];
-                if ((ce = cudaStreamBeginCaptureToGraph(h->side, body, nullptr, nullptr, 0,
+                cudaGraph_t ib = np.conditional.phGraph_out[0];
+                if ((ce = cudaStreamBeginCaptureToGraph(h->side, ib, nullptr, nullptr, 0,
                                                         cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
                     return;
                 issue(h->side);
-                ce = cudaStreamEndCapture(h->side, &body);
+                ce = cudaStreamEndCapture(h->side, &ib);
             };
             if (issue_round(pl, st, sa, optional)) { ce = cudaErrorUnknown; what = "round"; }
             if (ce == cudaSuccess && (ce = cudaGetLastError()) != cudaSuccess) what = "kernel launch";
         }
     }
-    // join: the origin waits for every branch
+    // join: the origin waits for every branch, then decides whether the loop goes on
     for (size_t k = 0; k < nPlans && ce == cudaSuccess; ++k) {
         cudaStream_t st = plans[k].h->stream;
         if (st == origin) continue;
         what = "join";
         if ((ce = cudaEventRecord(ev[k], st)) == cudaSuccess) ce = cudaStreamWaitEvent(origin, ev[k], 0);
     }
-    cudaGraph_t captured = nullptr;
+    if (ce == cudaSuccess) {
+        LoopArgs la;
+        la.loop = loop;
+        la.active = h0->dActiveList;
+        la.nActive = (int32_t)nPlans;
+        la.roundsPerIteration = check;
+        // a round is one evaluation of every active patch, and a CG iteration takes one
+        // gradient and a line search of a few to a few hundred metrics: far more rounds than
+        // that means a state machine that stopped advancing
+        long long maxIter = 0;
+        for (const SolvePlan& pl : plans) maxIter = std::max<long long>(maxIter, pl.prm.max_iterations);
+        la.maxRounds = std::min<long long>(2000000LL, 1000LL * maxIter + 10000LL);
+        la.rounds = h0->dRounds;
+        la.overrun = h0->dOverrun;
+        la.launchCount = h0->dLaunchCount;
+        launch_loop_cond(la, origin);
+        if ((ce = cudaGetLastError()) != cudaSuccess) what = "loop condition";
+    }
     if (capturing) {
+        cudaGraph_t captured = body;
         const cudaError_t ee = cudaStreamEndCapture(origin, &captured);
         if (ce == cudaSuccess && ee != cudaSuccess) { ce = ee; what = "end capture"; }
     }
     cudaGraphExec_t exec = nullptr;
-    if (ce == cudaSuccess && (ce = cudaGraphInstantiate(&exec, captured, 0)) != cudaSuccess) what = "instantiate";
+    if (ce == cudaSuccess && (ce = cudaGraphInstantiate(&exec, top, 0)) != cudaSuccess) what = "instantiate";
     int r = RDXG_OK;
     if (ce != cudaSuccess) {
         cudaGetLastError();
         h0->err = std::string("solver graph (") + what + "): " + cudaGetErrorString(ce);
         r = RDXG_ERR_CUDA;
     }
-    for (long round = 0; r == RDXG_OK; round += check) {
-        bool active = false;
-        if ((ce = cudaGraphLaunch(exec, origin)) == cudaSuccess) {
-            for (SolvePlan& pl : plans) {
-                if ((ce = cudaMemcpyAsync(pl.h->hActive, pl.h->dActive, sizeof(int32_t), cudaMemcpyDeviceToHost,
-                                          origin)) != cudaSuccess)
-                    break;
-            }
+    if (r == RDXG_OK) {
+        int32_t overrun = 0;
+        if ((ce = cudaGraphLaunch(exec, origin)) == cudaSuccess &&
+            (ce = cudaMemcpyAsync(h0->hActive, h0->dOverrun, sizeof(int32_t), cudaMemcpyDeviceToHost, origin)) ==
+                cudaSuccess &&
+            (ce = cudaStreamSynchronize(origin)) == cudaSuccess) {
+            overrun = *h0->hActive;
         }
-        if (ce == cudaSuccess) ce = cudaStreamSynchronize(origin);
         if (ce != cudaSuccess) {
             h0->err = std::string("solver graph launch: ") + cudaGetErrorString(ce);
             r = RDXG_ERR_CUDA;
-            break;
+        } else if (overrun) {
+            h0->err = "solver did not terminate";
+            r = RDXG_ERR_STATE;
         }
-        for (SolvePlan& pl : plans) active = active || *pl.h->hActive != 0;
-        if (!active) break;
-        if (round > 2000000L) { h0->err = "solver did not terminate"; r = RDXG_ERR_STATE; }
     }
     if (exec) cudaGraphExecDestroy(exec);
-    if (captured) cudaGraphDestroy(captured);
+    if (top) cudaGraphDestroy(top);
     for (cudaEvent_t e : ev)
         if (e) cudaEventDestroy(e);
     if (r) return r;

@@ -28,6 +28,23 @@ void launch_add_plane(const double* plane, float* objects, int nPo, int ps, cuda
     k_add_plane<0><<<nPo, 256, 0, st>>>(plane, objects, ps);
 }
 
+// End of one iteration of the solve graph's device loop: the loop (a WHILE node) continues
+// while any handle has an active patch, for at most maxRounds rounds in all.  One thread.
+__global__ void k_loop_cond(LoopArgs a) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int any = 0;
+    for (int k = 0; k < a.nActive; ++k) any |= (*a.active[k] != 0);
+    const long long r = (*a.rounds += a.roundsPerIteration);
+    *a.launchCount += 1ull;
+    if (any && r > a.maxRounds) {
+        *a.overrun = 1;
+        any = 0;
+    }
+    cudaGraphSetConditional(a.loop, any ? 1u : 0u);
+}
+
+void launch_loop_cond(const LoopArgs& a, cudaStream_t st) { k_loop_cond<<<1, 32, 0, st>>>(a); }
+
 // %nsmid: one more than the largest SM identifier %smid can hold (identifiers need not be
 // contiguous), the size of the per-SM slot masks of the recomputing kernels
 __global__ void k_nsmid(int32_t* out) {

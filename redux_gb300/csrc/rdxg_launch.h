@@ -95,6 +95,21 @@ template <typename T> void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st)
 cudaError_t query_nsmid(int32_t* dOut, int32_t* hOut, cudaStream_t st);   // %nsmid of the device
 void launch_shift(const ShiftArgs& a, int P, cudaStream_t st);
 
+// The device loop of a solve graph: a WHILE node whose body runs roundsPerIteration rounds of
+// every handle and then k_loop_cond, which keeps the loop going while a handle has an active
+// patch (bounded by maxRounds; past it, *overrun is set and the loop ends).
+struct LoopArgs {
+    cudaGraphConditionalHandle loop;
+    int32_t* const* active;      // [nActive] each handle's active-patch counter
+    int32_t nActive;
+    int32_t roundsPerIteration;
+    long long maxRounds;
+    long long* rounds;           // rounds run so far (zeroed before the graph launch)
+    int32_t* overrun;
+    unsigned long long* launchCount;
+};
+void launch_loop_cond(const LoopArgs& a, cudaStream_t st);
+
 // mode expansion on the tensor cores (rdxg_phase_tc.cu); parts: 2 (3xBF16) or 3 (6xBF16)
 PhaseTcPlan phase_tc_plan(int I, int M, int n2, int nCh, int parts, int numSMs);
 void launch_tc_pack_modes(const float* Z, const float* phiFixed, int M, int C, int n2, const PhaseTcPlan& p,
