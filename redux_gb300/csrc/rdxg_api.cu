@@ -129,6 +129,9 @@ struct rdxg_solver {
     unsigned* dSlotMask = nullptr;   // [nsmid] slots in use
     int32_t* dRcStatus = nullptr;    // a block of a recomputing kernel found no free slot
     size_t allocBytes = 0;           // device bytes the handle holds
+    // global work tiles of the transform kernels where a tile does not fit shared memory
+    void* dGtile = nullptr;
+    int gtileBlocks = 0;
 };
 
 namespace {
@@ -250,6 +253,8 @@ KParams<T> make_kparams(rdxg_solver* h) {
     k.slotMask = h->dSlotMask;
     k.slotsPerSM = h->slotsPerSM;
     k.rcStatus = h->dRcStatus;
+    k.gtile = (cx<T>*)h->dGtile;
+    k.gtileBlocks = h->gtileBlocks;
     return k;
 }
 
@@ -861,8 +866,6 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
     if (h->N != 2 * h->n) return fail(RDXG_ERR_ARG, "otf_size must be 2 * pupil_pixels");
     if (!supported_N(h->N)) return fail(RDXG_ERR_UNSUPPORTED, "otf_size not compiled (supported: 32, 64, 88, 128)");
     if (h->ps != h->N) return fail(RDXG_ERR_UNSUPPORTED, "patch_size must equal otf_size");
-    if (h->fp64 && (size_t)(Tile<128>::ELEMS + 128) * sizeof(cx<double>) > kMaxSmem && h->N == 128)
-        return fail(RDXG_ERR_UNSUPPORTED, "FP64 at otf_size 128: a double tile of 128 x 129 exceeds the shared memory of a block");
     if (h->cs < h->ps || ((h->cs - h->ps) & 1)) return fail(RDXG_ERR_ARG, "bad cutout_size");
     if (h->M < 1 || h->I < 1 || h->nObj < 1 || h->nObj > 64 || h->C < 1 || h->Pmax < 1 || h->nFree < 1)
         return fail(RDXG_ERR_ARG, "bad geometry");
@@ -921,6 +924,16 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
         if (de != cudaSuccess) { h->err = cudaGetErrorString(de); r = RDXG_ERR_CUDA; }
         h->adjGrid = h->numSMs * 8;
         h->fdGrid = h->numSMs * 8;
+    }
+    if (!r) {
+        // sizes whose work tile does not fit shared memory (FP64 at N = 128): one global tile
+        // per block of the transform kernels, which run one image per block (at most the
+        // batch's images; the finite-difference kernel strides over its items)
+        const size_t cxs = h->fp64 ? 16 : 8, elems = (size_t)h->N * (h->N + 1);   // Tile<N>::ELEMS
+        if ((elems + h->N) * cxs > kMaxSmem) {                                       // GlobalTile<T, N>
+            h->gtileBlocks = h->Pmax * h->I;
+            r = dalloc(h, &h->dGtile, (size_t)h->gtileBlocks * elems * cxs);
+        }
     }
     const char* at = getenv("RDXG_AUTOTUNE");
     if (at && atoi(at) == 0) h->tune = 0;   // default shapes, no measurement

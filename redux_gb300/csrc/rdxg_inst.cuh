@@ -22,8 +22,8 @@ static size_t extra_smem(int M) {
 
 template <typename T, int N>
 static size_t smem_pp(int M) {
-    return (size_t)(PingPong<T, N>::value ? Tile<N>::ELEMS : 0) * sizeof(cx<T>) +
-           (size_t)(Tile<N>::ELEMS + N) * sizeof(cx<T>) + extra_smem<T, N>(M);
+    return (size_t)(PingPong<T, N>::value ? Tile<N>::ELEMS : 0) * sizeof(cx<T>) + Launcher<T, N>::smem_base() +
+           extra_smem<T, N>(M);
 }
 
 // shared memory of the recomputing adjoint: tile [| X tile] | twiddles | PF | projection
@@ -142,6 +142,7 @@ void Launcher<T, N>::fd(const KParams<T>& kp, int grid, int M, cudaStream_t st) 
     }
     const size_t sm = smem_pp<T, N>(kp.M);
     if (!PingPong<T, N>::value) grid = kp.P * kp.I * M;
+    if (GlobalTile<T, N>::value) grid = grid < kp.gtileBlocks ? grid : kp.gtileBlocks;   // one tile per block
     k_fd<T, N, THREADS><<<grid, THREADS, sm, st>>>(kp);
 }
 

@@ -84,7 +84,30 @@ struct KParams {
     unsigned* slotMask;       // [SM] slots in use, for the kernels with one item per block
     int32_t slotsPerSM;
     int32_t* rcStatus;        // non-zero: a block found no free slot
+    // per-block N x N work tiles in global memory, for the sizes whose tile does not fit a
+    // block's shared memory (GlobalTile: FP64 at N = 128); blocks of the tile kernels
+    cx<T>* gtile;
+    int32_t gtileBlocks;
 };
+
+// FP64 at N = 128: a double tile of 128 x 129 (264 KB) exceeds the 227 KB of shared memory
+// of a block, so the general path's transform kernels keep their tile in global memory (one
+// per block, L2-resident) and only the twiddles and small arrays in shared memory.  The
+// transforms are the same code (generic pointers, block barriers order global memory too).
+template <typename T, int N> struct GlobalTile {
+    static constexpr bool value = (size_t)(Tile<N>::ELEMS + N) * sizeof(cx<T>) > 227 * 1024;
+};
+// the block's work tile and the start of its shared-memory arrays (twiddles first)
+template <typename T, int N>
+__device__ __forceinline__ cx<T>* work_tile(const KParams<T>& kp, unsigned char* smem) {
+    if constexpr (GlobalTile<T, N>::value) return kp.gtile + (size_t)blockIdx.x * Tile<N>::ELEMS;
+    else return reinterpret_cast<cx<T>*>(smem);
+}
+template <typename T, int N>
+__device__ __forceinline__ cx<T>* after_tile(unsigned char* smem) {
+    if constexpr (GlobalTile<T, N>::value) return reinterpret_cast<cx<T>*>(smem);
+    else return reinterpret_cast<cx<T>*>(smem) + Tile<N>::ELEMS;
+}
 
 enum GradKind : int32_t { GK_VOGEL = 0, GK_EXACT = 1 };
 
@@ -225,8 +248,8 @@ __global__ void __launch_bounds__(THREADS) k_prep(KParams<T> kp, int full) {
     if (!full && !kp.reinit[g]) return;
     constexpr int LDS = Tile<N>::LDS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* tw = s + Tile<N>::ELEMS;
+    cx<T>* s = work_tile<T, N>(kp, smem_raw);
+    cx<T>* tw = after_tile<T, N>(smem_raw);
     double* red = reinterpret_cast<double*>(tw + N);
     load_twiddles<T, N>(tw, kp.tw);
     const int ps = kp.ps, cs = kp.cs;
@@ -334,8 +357,8 @@ __global__ void __launch_bounds__(THREADS) k_forward(KParams<T> kp) {
     constexpr int LDS = Tile<N>::LDS;
     constexpr int n = N / 2, n2 = n * n;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* tw = s + Tile<N>::ELEMS;
+    cx<T>* s = work_tile<T, N>(kp, smem_raw);
+    cx<T>* tw = after_tile<T, N>(smem_raw);
     T* al = reinterpret_cast<T*>(tw + N);
     load_twiddles<T, N>(tw, kp.tw);
     const int M = kp.M;
@@ -522,9 +545,9 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
     constexpr int n = N / 2, n2 = n * n, N2 = N * N;
     constexpr bool PP = false;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
-    cx<T>* s2 = s + (PP ? Tile<N>::ELEMS : 0);
-    cx<T>* tw = s2 + Tile<N>::ELEMS;
+    cx<T>* s = work_tile<T, N>(kp, smem_raw);
+    cx<T>* s2 = s;
+    cx<T>* tw = after_tile<T, N>(smem_raw);
     T* v = reinterpret_cast<T*>(tw + N);            // [n2]
     __syncthreads();    // previous image's shared memory consumed
     load_twiddles<T, N>(tw, kp.tw);
@@ -747,9 +770,9 @@ __device__ __forceinline__ void fd_image(const KParams<T>& kp, int p, int j, int
         return;
     }
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
+    cx<T>* s = work_tile<T, N>(kp, smem_raw);
     cx<T>* s2 = s + (PP ? Tile<N>::ELEMS : 0);
-    cx<T>* tw = s2 + Tile<N>::ELEMS;
+    cx<T>* tw = GlobalTile<T, N>::value ? after_tile<T, N>(smem_raw) : s2 + Tile<N>::ELEMS;
     double* red = reinterpret_cast<double*>(tw + N);
     __syncthreads();    // previous item's shared memory consumed
     load_twiddles<T, N>(tw, kp.tw);
@@ -815,7 +838,8 @@ __global__ void __launch_bounds__(THREADS) k_fd(KParams<T> kp) {
         const size_t g = (size_t)p * kp.I + j;
         fd_image<T, N, THREADS>(kp, p, j, m, kp.PF + g * (N / 2) * (N / 2), kp.X + g * N * N, (int)threadIdx.x);
     };
-    if constexpr (PingPong<T, N>::value) {
+    if constexpr (PingPong<T, N>::value || GlobalTile<T, N>::value) {
+        // (a global work tile per block: the grid is the number of tiles)
         for (int w = blockIdx.x; w < nWork; w += gridDim.x) item(w);
     } else {
         const int w = blockIdx.x;
@@ -826,7 +850,8 @@ __global__ void __launch_bounds__(THREADS) k_fd(KParams<T> kp) {
 // Shared memory of k_fd (and of k_fd_rc before its own arrays): tiles, twiddles, reduction.
 template <typename T, int N>
 constexpr size_t fd_base_smem() {
-    return (size_t)((PingPong<T, N>::value ? 2 : 1) * Tile<N>::ELEMS + N) * sizeof(cx<T>) + 33 * sizeof(double);
+    return (size_t)((GlobalTile<T, N>::value ? 0 : PingPong<T, N>::value ? 2 : 1) * Tile<N>::ELEMS + N) * sizeof(cx<T>) +
+           33 * sizeof(double);
 }
 
 // The finite-difference gradient with recomputed transforms.  FP32 up to N = 88 (ping-pong

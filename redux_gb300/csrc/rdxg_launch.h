@@ -37,7 +37,10 @@ template <int N> struct ThreadsAlt { static constexpr int value = 2 * Threads<N>
 template <typename T, int N>
 struct Launcher {
     static constexpr int THREADS = Threads<N>::value;
-    static size_t smem_base() { return (size_t)(Tile<N>::ELEMS + N) * sizeof(cx<T>); }
+    // the work tile (unless it lives in global memory, GlobalTile) and the twiddles
+    static size_t smem_base() {
+        return (size_t)((GlobalTile<T, N>::value ? 0 : Tile<N>::ELEMS) + N) * sizeof(cx<T>);
+    }
     static cudaError_t setup(int M);   // opt in to the dynamic shared memory
     static void prep(const KParams<T>& kp, int full, int nImg, cudaStream_t st);
     static void forward(const KParams<T>& kp, int nImg, cudaStream_t st);

@@ -351,3 +351,30 @@ def test_production_geometry_3x12():
         am = a[0].copy(); am[j, m] -= h
         fd = (op.metric(ap) - op.metric(am)) / (2 * h)
         assert abs(ge[0, j, m] - fd) <= 1e-4 * max(abs(fd), 1e-3 * np.abs(ge[0]).max()), (j, m, ge[0, j, m], fd)
+
+
+def test_fp64_n128_matches_oracle():
+    """The FP64 form at N = 128 (its work tiles in global memory, a double tile exceeding a
+    block's shared memory): metric, Vogel and finite-difference gradients against the FP64
+    oracle, and a short solve with the oracle's evaluation sequence."""
+    w = _w4()
+    s = _solver(w, "fp64")
+    op = _oracle(w)
+    for scale in (0.0, 0.5, 1.0):
+        a = w.patches.alpha_true * scale
+        L = s.metric(a)[0]
+        Lo = op.metric(a[0])
+        assert abs(L - Lo) <= 1e-11 * abs(Lo), (scale, L, Lo)
+    a = w.patches.alpha_true * 0.5
+    g, _ = s.gradient(a, "vogel")
+    _, go = op.gradient(a[0], "vogel")
+    assert np.linalg.norm(g[0] - go) / np.linalg.norm(go) < 1e-10
+    gf, _ = s.gradient(a, "fd")
+    _, gfo = op.gradient(a[0], "fd")
+    assert np.linalg.norm(gf[0] - gfo) / np.linalg.norm(gfo) < 1e-9
+    it = 2
+    out = s.run(S.fixed_iterations(w.job.n_modes, it, max_metrics=64))
+    ref = op.solve(oracle.default_cfg(max_iterations=it, n_modes=w.job.n_modes))
+    rep = out["reports"][0]
+    assert rep.n_f_evals == ref["report"].n_f_evals
+    np.testing.assert_allclose(out["metrics"][0, :rep.n_metrics], ref["metrics"], rtol=1e-9)

@@ -25,12 +25,11 @@ def test_library_exports_every_symbol():
     assert L.rdxg_version() >= 100
 
 
-def test_fp64_at_128_is_rejected_before_any_device_call():
-    """A double 128 x 129 tile does not fit the shared memory of a block: rdxg_create answers
-    RDXG_ERR_UNSUPPORTED with a message, before it touches a device (so this runs on a host
-    without a GPU)."""
+def test_unsupported_size_is_rejected_before_any_device_call():
+    """An OTF size without compiled kernels: rdxg_create answers RDXG_ERR_UNSUPPORTED with a
+    message, before it touches a device (so this runs on a host without a GPU)."""
     import pytest
     from redux_gb300 import solver as S, synth
-    job = synth.make_job(128, 8, synth.LAYOUT_1OBJ(2))
-    with pytest.raises(S.SolverError, match=r"status 2: FP64 at otf_size 128"):
+    job = synth.make_job(96, 8, synth.LAYOUT_1OBJ(2))
+    with pytest.raises(S.SolverError, match=r"status 2: otf_size not compiled"):
         S.Solver(job, max_patches=1, precision="fp64")
