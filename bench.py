@@ -460,8 +460,7 @@ def run_large(args):
                 "hbm_gbs": hbm[k] / (kt[k] / 1e3) / 1e9, "hbm_frac": hbm[k] / (kt[k] / 1e3) / 1e9 / peaks["hbm"]}
             for k in ("forward", "accum", "adjoint")}
     # errors against the FP64 restatement (CPU) on one patch: the metric, gradient and restored
-    # object at the same alpha, and a short solve of both (the FP64 GPU form does not take
-    # N = 128: a double tile of 128 x 129 exceeds the shared memory of a block)
+    # object at the same alpha, and a short solve of both
     import oracle
     threads = os.cpu_count() or 1
     check_iters = args.check_iterations
@@ -498,6 +497,74 @@ def run_large(args):
         "short_solve_object_rel_peak": float(np.abs(obj_1s - obj_os).max() / np.abs(obj_os).max()),
     }
     s1.close()
+    # the plain FP64 GPU form at N = 128 (the general path in double, its work tiles in global
+    # memory): the same solve with per-patch launches on a sample of patches, and the FP32
+    # path's errors against it at the same alpha on the same patches
+    nb = max(1, min(args.large_fp64_patches, P))
+    s64 = S.Solver(job, max_patches=1, precision="fp64")
+    t64, fin64 = 0.0, []
+    for p in range(nb):
+        s64.set_patches(cut[p:p + 1])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r64 = s64.run(settings)
+        torch.cuda.synchronize()
+        t64 += time.perf_counter() - t0
+        fin64.append(r64["reports"][0].final_metric)
+    s64.close()
+    plain_v = nb / t64
+    sb32 = S.Solver(job, max_patches=nb)
+    sb32.set_patches(cut[:nb])
+    sb64 = S.Solver(job, max_patches=nb, precision="fp64")
+    sb64.set_patches(cut[:nb])
+    a_same = w.patches.alpha_true[:nb]
+    m32, m64 = sb32.metric(a_same), sb64.metric(a_same)
+    g32, _ = sb32.gradient(a_same)
+    g64, _ = sb64.gradient(a_same)
+    o32, o64 = sb32.restore(a_same, fc), sb64.restore(a_same, fc)
+    errors["fp64_gpu"] = {
+        "reference": f"FP64 GPU form, {nb} patches, at the true alpha",
+        "metric_rel": (np.abs(m32 - m64) / np.abs(m64)).tolist(),
+        "gradient_rel_norm": [float(np.linalg.norm(g32[p] - g64[p]) / np.linalg.norm(g64[p])) for p in range(nb)],
+        "object_rel_peak": [float(np.abs(o32[p] - o64[p]).max() / np.abs(o64[p]).max()) for p in range(nb)],
+        "final_metric_signed_rel_after_solve": [(reps[p].final_metric - fin64[p]) / abs(fin64[p]) for p in range(nb)],
+    }
+    # converged: the whole batch to convergence (FTOL 1e-6 three times in a row, all modes at
+    # once), then FP64 continuations from the FP32 endpoints and from FP64's own on the sample
+    conv = S.SolveSettings(mode_start=M, mode_step=M, max_iterations=args.conv_max_iterations, min_iterations=5,
+                           target_iterations=3, ftol=args.conv_ftol, max_metrics=4096)
+    s.set_patches(cut)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc = s.run(conv)
+    torch.cuda.synchronize()
+    t_conv = time.perf_counter() - t0
+    a32c = rc["alpha"]
+    t0 = time.perf_counter()
+    r64c = sb64.run(conv)
+    torch.cuda.synchronize()
+    t64c = time.perf_counter() - t0
+
+    def continuation(a):
+        sb64.set_start_alpha(a)
+        rr = sb64.run(conv)["reports"]
+        return [(r.initial_metric - r.final_metric) / r.initial_metric for r in rr]
+
+    d32 = continuation(a32c[:nb])
+    d64 = continuation(r64c["alpha"])
+    sb32.close()
+    sb64.close()
+    fin32c = [rc["reports"][p].final_metric for p in range(nb)]
+    fin64c = [r.final_metric for r in r64c["reports"]]
+    its = [r.iterations for r in rc["reports"]]
+    converged = {
+        "settings": f"all modes at once, FTOL {args.conv_ftol} (3 consecutive), MIN_ITER 5, "
+                    f"MAX_ITER {args.conv_max_iterations}",
+        "patches_per_s": P / t_conv, "iterations_median": float(np.median(its)), "iterations_max": int(max(its)),
+        "fp64_batch_patches_per_s": nb / t64c,
+        "continuation_drop_from_fp32": d32, "continuation_drop_from_fp64": d64,
+        "fp32_minus_fp64_final_signed_rel": [(a - b) / abs(b) for a, b in zip(fin32c, fin64c)],
+    }
     line = {"metric": "large-patch patches/s", "value": P / t_solve, "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_solve * 1000.0, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 sums and CG scalars)", "data": "synthetic",
@@ -513,6 +580,9 @@ def run_large(args):
             "gpu_launches": int(launches), "kernels": kern, "peak_hbm_gbs": peaks["hbm"],
             "launch_shapes": s.launch_shape(),
             "errors_vs_fp64": errors,
+            "plain_fp64_gpu": {"value": plain_v, "unit": UNIT, "sample": f"{nb} patches, per-patch launches",
+                               "speedup_chosen_vs_plain": P / t_solve / plain_v},
+            "converged": converged,
             "cpu_baseline": {"value": 1.0 / t_cpu * check_iters / args.iterations, "unit": UNIT, "cores": threads,
                              "kind": "port", "sample": f"1 patch x {check_iters} iterations, FP64 restatement, "
                                                        f"{threads} OpenMP threads over images, scaled to "
@@ -552,6 +622,8 @@ def main():
                     help="convergence: stop restarting once no patch's metric drops by more than this")
     ap.add_argument("--levels", type=int, default=3,
                     help="uneven batch: frames and modes from this many values (0: uniform draws)")
+    ap.add_argument("--large-fp64-patches", type=int, default=4,
+                    help="large patches: patches solved by the plain FP64 GPU form and compared with it")
     ap.add_argument("--check-iterations", type=int, default=10,
                     help="large patches: CG iterations of the solve compared with the FP64 restatement")
     ap.add_argument("--kernels-only", action="store_true",
