@@ -135,6 +135,30 @@ int rdxg_set_patches(rdxg_solver* h, int32_t n_patches, const float* cutouts,
 int rdxg_set_patches_device(rdxg_solver* h, int32_t n_patches, const float* d_cutouts,
                             const double* residual_alpha, const double* fixed_gamma);
 
+/* Ragged batches: patches of one OTF size whose frames per channel and mode counts differ
+ * (redux runs each such patch in the job of its own geometry, momfbdjob.cpp:576-591, with
+ * that job's Constraints, constraints.cpp:536-622).  A shape gives the frames per channel
+ * (each channel's first `frames` images of the handle, in its image order; every channel of
+ * the handle must have the same number), the number of modes (the first n_modes of the
+ * handle's mode set) and that geometry's null-space map, rows indexed image * n_modes + mode
+ * over the shape's own images.  patch_shape[p] picks the shape of patch p; the next
+ * rdxg_set_patches must load n_patches patches, each with its images in the first slots of
+ * its [I] cutouts (the rest are ignored), and alpha arrays keep the [P][I][M] layout with
+ * zeros in the slots and modes a patch does not use.  Each patch is solved exactly as by a
+ * handle of its own geometry (the same evaluations, chunks, sums and maps).  n_shapes = 0
+ * returns to uniform batches.  Not with REG_ALPHA weights or rdxg_metric_noalloc. */
+typedef struct {
+    int32_t frames;
+    int32_t n_modes;
+    int32_t n_free;
+    int64_t ns_nnz;
+    const int32_t* ns_rows;
+    const int32_t* ns_cols;
+    const double* ns_vals;
+} rdxg_patch_shape;
+int rdxg_set_patch_shapes(rdxg_solver* h, int32_t n_shapes, const rdxg_patch_shape* shapes, int32_t n_patches,
+                          const int32_t* patch_shape);
+
 /* Warm start (INIT_FILES): the initial mode coefficients [P][I][M] of the loaded patches,
  * the alpha_offset that Solver::loadInit fills from ObjectData::alpha (solver.cpp:412,
  * 726-733; Object::getInit, object.cpp:446-456), or NULL to start at zero.  As

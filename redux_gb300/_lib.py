@@ -22,7 +22,7 @@ EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "r
             "rdxg_autotune", "rdxg_set_launch_shape", "rdxg_get_launch_shape", "rdxg_set_fit_plane",
             "rdxg_set_initial_alpha", "rdxg_set_reg_alpha", "rdxg_debug_set", "rdxg_set_start_alpha",
             "rdxg_set_recompute", "rdxg_recompute", "rdxg_pupil_size", "rdxg_make_pupil", "rdxg_pupil_support",
-            "rdxg_make_modes", "rdxg_apodization_windows")
+            "rdxg_make_modes", "rdxg_apodization_windows", "rdxg_set_patch_shapes")
 
 
 class Geometry(C.Structure):
@@ -47,6 +47,11 @@ class SolveParams(C.Structure):
                 ("min_iterations", C.c_int32), ("target_iterations", C.c_int32), ("fd_first", C.c_int32),
                 ("max_metrics", C.c_int32), ("check_every", C.c_int32), ("ftol", C.c_double),
                 ("eps", C.c_double)]
+
+
+class PatchShape(C.Structure):
+    _fields_ = [("frames", C.c_int32), ("n_modes", C.c_int32), ("n_free", C.c_int32), ("ns_nnz", C.c_int64),
+                ("ns_rows", C.c_void_p), ("ns_cols", C.c_void_p), ("ns_vals", C.c_void_p)]
 
 
 class ModeParams(C.Structure):
@@ -120,6 +125,7 @@ def load(path: str = LIB_PATH):
     L.rdxg_get_launch_shape.argtypes = [vp, C.POINTER(LaunchShape)]
     L.rdxg_cg_minimize.argtypes = [C.c_int32, C.c_int32, C.POINTER(SolveParams), C.c_double, F_FN, DF_FN,
                                    SHIFT_FN, vp, vp, C.POINTER(PatchReport), vp]
+    L.rdxg_set_patch_shapes.argtypes = [vp, C.c_int32, C.POINTER(PatchShape), C.c_int32, vp]
     L.rdxg_pupil_size.argtypes = [C.c_int32, C.c_double, C.c_double, C.c_double, vp, vp, vp]
     L.rdxg_make_pupil.argtypes = [C.c_int32, C.c_double, C.c_double, vp, vp]
     L.rdxg_pupil_support.argtypes = [vp, C.c_int32, C.c_double, vp, vp, vp, vp, vp, vp]

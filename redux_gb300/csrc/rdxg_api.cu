@@ -132,6 +132,23 @@ struct rdxg_solver {
     // global work tiles of the transform kernels where a tile does not fit shared memory
     void* dGtile = nullptr;
     int gtileBlocks = 0;
+    // patch shapes: shape 0 is the handle's own geometry (every image and mode, the static
+    // null space); rdxg_set_patch_shapes adds those of a ragged batch and gives each patch one.
+    // On the device: every patch's geometry and image/object tables, every shape's maps.
+    struct Shape {
+        int frames = -1, M = 0, nFree = 0, nImg = 0, chunks = 0;
+        std::vector<int32_t> imgObj, imgCh, objFirst, objCount, objChunk0;   // [I] / [nObj]
+        std::vector<int32_t> rowPtr, rowCol, colPtr, colRow;                // rows: slot * M + mode
+        std::vector<double> rowVal, colVal;
+    };
+    std::vector<Shape> shapes;
+    std::vector<int32_t> patchShape;   // [Pmax]
+    bool ragged = false;
+    int raggedPatches = 0;             // patches the shapes were given for
+    PatchGeo* dPGeo = nullptr;
+    int32_t *dPImgObj = nullptr, *dPImgCh = nullptr, *dPObjFirst = nullptr, *dPObjCount = nullptr,
+            *dPObjChunk0 = nullptr;
+    size_t mapRowEntries = 0, mapColEntries = 0, mapNnz = 0;   // sizes of the device maps
 };
 
 namespace {
@@ -232,7 +249,8 @@ KParams<T> make_kparams(rdxg_solver* h) {
     k.ps = h->ps; k.cs = h->cs; k.margin = h->margin; k.nTiles = h->nTiles;
     k.Z = (const T*)h->dZ; k.A = (const T*)h->dA; k.phiFixed = (const T*)h->dPhi;
     k.otfNorm = (const T*)h->dOtfNorm; k.otfMask = h->dMask;
-    k.imgObj = h->dImgObj; k.imgCh = h->dImgCh; k.objFirst = h->dObjFirst; k.objCount = h->dObjCount;
+    k.pgeo = h->dPGeo; k.pImgObj = h->dPImgObj; k.pImgCh = h->dPImgCh;
+    k.pObjFirst = h->dPObjFirst; k.pObjCount = h->dPObjCount;
     k.objWeight = h->dObjW; k.objGradStep = h->dGradStep; k.window = h->dWin; k.noiseWindow = h->dNWin;
     k.tw = (const cx<T>*)h->dTw; k.area = h->area; k.tiltX = h->geo.tilt_x; k.tiltY = h->geo.tilt_y;
     k.cutouts = h->dCutExt ? h->dCutExt : h->dCut;
@@ -274,7 +292,7 @@ EvalParams<T> make_evalparams(rdxg_solver* h) {
     EvalParams<T> e{};
     e.k = make_kparams<T>(h);
     e.hp.nH = h->nH; e.hp.idx = h->dHIdx; e.hp.chunkSize = h->chunk;
-    e.hp.chunksPerPatch = h->chunksPerPatch; e.hp.objChunk0 = h->dObjChunk0;
+    e.hp.chunksPerPatch = h->chunksPerPatch; e.hp.objChunk0 = h->dPObjChunk0;
     e.Dh = (const cx<T>*)h->dDh; e.Oh = (cx<T>*)h->dOh; e.part = (Acc4<T>*)h->dPart;
     e.objMetric = h->dObjMetric; e.L = make_lists(h);
     e.hPos = h->dHPos; e.nTilesH = h->nTilesH; e.phi = (T*)h->dPhiImg;
@@ -362,6 +380,7 @@ CgArgs<T> make_cgargs(rdxg_solver* h, const CgParams& prm) {
     a.P = h->P; a.I = h->I; a.M = h->M; a.nObj = h->nObj; a.nPar = h->nPar; a.nTiles = h->nTiles; a.ps = h->ps;
     a.states = h->dStates; a.vec = h->dVec; a.metrics = h->dMetrics; a.alpha = h->dAlpha; a.alphaOff = h->dAlphaOff;
     a.galpha = h->dGalpha; a.partial = h->dPartial; a.objWeight = h->dObjW;
+    a.pgeo = h->dPGeo;
     a.rowPtr = h->dRowPtr; a.rowCol = h->dRowCol; a.rowVal = h->dRowVal; a.rowVal32 = h->dRowVal32;
     a.colPtr = h->dColPtr; a.colRow = h->dColRow; a.colVal = h->dColVal;
     a.curTilt = h->dCurTilt; a.resAlpha = h->dResAlpha; a.tiltX = h->geo.tilt_x; a.tiltY = h->geo.tilt_y;
@@ -373,8 +392,8 @@ CgArgs<T> make_cgargs(rdxg_solver* h, const CgParams& prm) {
     const char* m64 = getenv("RDXG_MAP64");
     if (m64 && atoi(m64)) a.x1Smem = 0;
     a.objMetric = h->dObjMetric; a.L = make_lists(h); a.nTilesH = h->nTilesH;
-    a.chunkSize = h->chunk; a.chunksPerPatch = h->chunksPerPatch; a.objChunk0 = h->dObjChunk0;
-    a.objFirst = h->dObjFirstC; a.objCount = h->dObjCountC; a.aux = h->dAux;
+    a.chunkSize = h->chunk; a.chunksPerPatch = h->chunksPerPatch; a.objChunk0 = h->dPObjChunk0;
+    a.objFirst = h->dPObjFirst; a.objCount = h->dPObjCount; a.aux = h->dAux;
     a.regW = h->hRegW.empty() ? nullptr : h->dRegW;
     a.phaseList = (!h->fused && h->tcPlan.valid) ? 1 : 0;
     return a;
@@ -493,41 +512,157 @@ int setup_transforms(rdxg_solver* h, bool recompute) {
     return RDXG_OK;
 }
 
-int build_nullspace(rdxg_solver* h, const rdxg_static* s) {
-    const int nPar = h->nPar, nF = h->nFree;
-    std::vector<int32_t> rc(nPar + 1, 0), cc(nF + 1, 0);
-    for (int64_t e = 0; e < s->ns_nnz; ++e) {
-        const int r = s->ns_rows[e], c = s->ns_cols[e];
-        if (r < 0 || r >= nPar || c < 0 || c >= nF) { h->err = "null-space entry out of range"; return RDXG_ERR_ARG; }
-        rc[r + 1]++;
-        cc[c + 1]++;
+// The maps of a shape in the handle's layout (row = image slot * M + mode), both ways, from
+// entries whose rows are in the shape's own layout (packed image k * nMode + mode).
+int shape_maps(rdxg_solver* h, rdxg_solver::Shape& sh, int64_t nnz, const int32_t* rows, const int32_t* cols,
+               const double* vals) {
+    const int nPar = h->nPar, nF = sh.nFree, Ms = sh.M;
+    std::vector<int32_t> hr(nnz);
+    for (int64_t e = 0; e < nnz; ++e) {
+        const int r = rows[e], c = cols[e];
+        if (r < 0 || r >= sh.nImg * Ms || c < 0 || c >= nF) { h->err = "null-space entry out of range"; return RDXG_ERR_ARG; }
+        hr[e] = (r / Ms) * h->M + r % Ms;
+    }
+    std::vector<int32_t>& rc = sh.rowPtr;
+    std::vector<int32_t>& cc = sh.colPtr;
+    rc.assign(nPar + 1, 0);
+    cc.assign(nF + 1, 0);
+    for (int64_t e = 0; e < nnz; ++e) {
+        rc[hr[e] + 1]++;
+        cc[cols[e] + 1]++;
     }
     for (int i = 0; i < nPar; ++i) rc[i + 1] += rc[i];
     for (int i = 0; i < nF; ++i) cc[i + 1] += cc[i];
-    std::vector<int32_t> rcol(s->ns_nnz), crow(s->ns_nnz), rfill(rc.begin(), rc.end() - 1), cfill(cc.begin(), cc.end() - 1);
-    std::vector<double> rval(s->ns_nnz), cval(s->ns_nnz);
-    for (int64_t e = 0; e < s->ns_nnz; ++e) {
-        const int r = s->ns_rows[e], c = s->ns_cols[e];
-        rcol[rfill[r]] = c; rval[rfill[r]++] = s->ns_vals[e];
-        crow[cfill[c]] = r; cval[cfill[c]++] = s->ns_vals[e];
+    sh.rowCol.assign(nnz, 0); sh.colRow.assign(nnz, 0);
+    sh.rowVal.assign(nnz, 0.0); sh.colVal.assign(nnz, 0.0);
+    std::vector<int32_t> rfill(rc.begin(), rc.end() - 1), cfill(cc.begin(), cc.end() - 1);
+    for (int64_t e = 0; e < nnz; ++e) {
+        const int r = hr[e], c = cols[e];
+        sh.rowCol[rfill[r]] = c; sh.rowVal[rfill[r]++] = vals[e];
+        sh.colRow[cfill[c]] = r; sh.colVal[cfill[c]++] = vals[e];
+    }
+    return RDXG_OK;
+}
+
+// The image and object tables of a shape: each channel's first `frames` images (all when
+// frames < 0), in the handle's image order, packed into the first slots.
+int shape_tables(rdxg_solver* h, rdxg_solver::Shape& sh) {
+    std::vector<int> rank(h->C, 0);
+    sh.imgObj.assign(h->I, 0);
+    sh.imgCh.assign(h->I, 0);
+    int k = 0;
+    for (int j = 0; j < h->I; ++j) {
+        const int c = h->imgCh[j];
+        if (sh.frames < 0 || rank[c] < sh.frames) {
+            sh.imgObj[k] = h->imgObj[j];
+            sh.imgCh[k] = c;
+            ++k;
+        }
+        rank[c]++;
+    }
+    sh.nImg = k;
+    sh.objFirst.assign(h->nObj, -1);
+    sh.objCount.assign(h->nObj, 0);
+    for (int j = 0; j < sh.nImg; ++j) {
+        const int o = sh.imgObj[j];
+        if (sh.objFirst[o] < 0) sh.objFirst[o] = j;
+        sh.objCount[o]++;
+    }
+    for (int o = 0; o < h->nObj; ++o)
+        if (sh.objCount[o] == 0) { h->err = "patch shape: an object without images"; return RDXG_ERR_ARG; }
+    sh.objChunk0.assign(h->nObj, 0);
+    int c0 = 0;
+    for (int o = 0; o < h->nObj; ++o) {
+        sh.objChunk0[o] = c0;
+        c0 += (sh.objCount[o] + h->chunk - 1) / h->chunk;
+    }
+    sh.chunks = c0;
+    return RDXG_OK;
+}
+
+int build_nullspace(rdxg_solver* h, const rdxg_static* s) {
+    h->shapes.assign(1, rdxg_solver::Shape{});
+    rdxg_solver::Shape& sh = h->shapes[0];
+    sh.frames = -1; sh.M = h->M; sh.nFree = h->nFree; sh.nImg = h->I;
+    return shape_maps(h, sh, s->ns_nnz, s->ns_rows, s->ns_cols, s->ns_vals);
+}
+
+// Uploads every patch's geometry and tables (patches without a shape take shape 0) and the
+// maps of every shape, one after the other.
+int upload_geometry(rdxg_solver* h) {
+    for (rdxg_solver::Shape& sh : h->shapes) {
+        int r = shape_tables(h, sh);
+        if (r) return r;
+    }
+    const size_t P = h->Pmax;
+    h->patchShape.resize(P, 0);
+    std::vector<int32_t> rowPtr, rowCol, colPtr, colRow;
+    std::vector<double> rowVal, colVal;
+    std::vector<int> rowBase(h->shapes.size()), colBase(h->shapes.size());
+    for (size_t k = 0; k < h->shapes.size(); ++k) {
+        const rdxg_solver::Shape& sh = h->shapes[k];
+        const int32_t off = (int32_t)rowCol.size();
+        rowBase[k] = (int)rowPtr.size();
+        colBase[k] = (int)colPtr.size();
+        for (int32_t v : sh.rowPtr) rowPtr.push_back(v + off);
+        for (int32_t v : sh.colPtr) colPtr.push_back(v + off);
+        rowCol.insert(rowCol.end(), sh.rowCol.begin(), sh.rowCol.end());
+        colRow.insert(colRow.end(), sh.colRow.begin(), sh.colRow.end());
+        rowVal.insert(rowVal.end(), sh.rowVal.begin(), sh.rowVal.end());
+        colVal.insert(colVal.end(), sh.colVal.begin(), sh.colVal.end());
+    }
+    std::vector<PatchGeo> geo(P);
+    std::vector<int32_t> io(P * h->I), ic(P * h->I), of(P * h->nObj), oc(P * h->nObj), ch0(P * h->nObj);
+    for (size_t p = 0; p < P; ++p) {
+        const int k = h->patchShape[p];
+        const rdxg_solver::Shape& sh = h->shapes[k];
+        geo[p] = PatchGeo{sh.nImg, sh.M, sh.nFree, sh.chunks, rowBase[k], colBase[k]};
+        std::copy(sh.imgObj.begin(), sh.imgObj.end(), io.begin() + p * h->I);
+        std::copy(sh.imgCh.begin(), sh.imgCh.end(), ic.begin() + p * h->I);
+        std::copy(sh.objFirst.begin(), sh.objFirst.end(), of.begin() + p * h->nObj);
+        std::copy(sh.objCount.begin(), sh.objCount.end(), oc.begin() + p * h->nObj);
+        std::copy(sh.objChunk0.begin(), sh.objChunk0.end(), ch0.begin() + p * h->nObj);
     }
     int r;
-    void* v;
-    if ((r = upload(h, &v, rc))) return r;
-    h->dRowPtr = (int32_t*)v;
-    if ((r = upload(h, &v, rcol))) return r;
-    h->dRowCol = (int32_t*)v;
-    if ((r = upload(h, &v, rval))) return r;
-    h->dRowVal = (double*)v;
-    std::vector<float> rval32(rval.begin(), rval.end());
-    if ((r = upload(h, &v, rval32))) return r;
-    h->dRowVal32 = (float*)v;
-    if ((r = upload(h, &v, cc))) return r;
-    h->dColPtr = (int32_t*)v;
-    if ((r = upload(h, &v, crow))) return r;
-    h->dColRow = (int32_t*)v;
-    if ((r = upload(h, &v, cval))) return r;
-    h->dColVal = (double*)v;
+    if (!h->dPGeo) {
+        if ((r = dalloc_t(h, &h->dPGeo, P)) || (r = dalloc_t(h, &h->dPImgObj, P * h->I)) ||
+            (r = dalloc_t(h, &h->dPImgCh, P * h->I)) || (r = dalloc_t(h, &h->dPObjFirst, P * h->nObj)) ||
+            (r = dalloc_t(h, &h->dPObjCount, P * h->nObj)) || (r = dalloc_t(h, &h->dPObjChunk0, P * h->nObj)))
+            return r;
+    }
+    CK(h, cudaMemcpy(h->dPGeo, geo.data(), P * sizeof(PatchGeo), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->dPImgObj, io.data(), io.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->dPImgCh, ic.data(), ic.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->dPObjFirst, of.data(), of.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->dPObjCount, oc.data(), oc.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->dPObjChunk0, ch0.data(), ch0.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    // the maps (reallocated when their sizes change)
+    const size_t nnz = rowCol.size();
+    if (rowPtr.size() != h->mapRowEntries || colPtr.size() != h->mapColEntries || nnz != h->mapNnz) {
+        dfree(h, &h->dRowPtr, h->mapRowEntries * sizeof(int32_t));
+        dfree(h, &h->dColPtr, h->mapColEntries * sizeof(int32_t));
+        dfree(h, &h->dRowCol, h->mapNnz * sizeof(int32_t));
+        dfree(h, &h->dColRow, h->mapNnz * sizeof(int32_t));
+        dfree(h, &h->dRowVal, h->mapNnz * sizeof(double));
+        dfree(h, &h->dColVal, h->mapNnz * sizeof(double));
+        dfree(h, &h->dRowVal32, h->mapNnz * sizeof(float));
+        if ((r = dalloc_t(h, &h->dRowPtr, rowPtr.size())) || (r = dalloc_t(h, &h->dColPtr, colPtr.size())) ||
+            (r = dalloc_t(h, &h->dRowCol, nnz)) || (r = dalloc_t(h, &h->dColRow, nnz)) ||
+            (r = dalloc_t(h, &h->dRowVal, nnz)) || (r = dalloc_t(h, &h->dColVal, nnz)) ||
+            (r = dalloc_t(h, &h->dRowVal32, nnz)))
+            return r;
+        h->mapRowEntries = rowPtr.size();
+        h->mapColEntries = colPtr.size();
+        h->mapNnz = nnz;
+    }
+    std::vector<float> rowVal32(rowVal.begin(), rowVal.end());
+    CK(h, cudaMemcpy(h->dRowPtr, rowPtr.data(), rowPtr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->dColPtr, colPtr.data(), colPtr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->dRowCol, rowCol.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->dColRow, colRow.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->dRowVal, rowVal.data(), nnz * sizeof(double), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->dColVal, colVal.data(), nnz * sizeof(double), cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->dRowVal32, rowVal32.data(), nnz * sizeof(float), cudaMemcpyHostToDevice));
     return RDXG_OK;
 }
 
@@ -537,7 +672,7 @@ ShiftArgs make_shift_args(rdxg_solver* h) {
     sa.P = h->P; sa.I = h->I; sa.M = h->M; sa.nObj = h->nObj; sa.ps = h->ps; sa.cs = h->cs; sa.margin = h->margin;
     sa.tiltX = h->haveJ ? h->geo.tilt_x : -1; sa.tiltY = h->haveJ ? h->geo.tilt_y : -1;
     sa.req = h->dReq; sa.alpha = h->dAlpha; sa.tiltOff = h->dCurTilt; sa.shift = h->dShift;
-    sa.reinit = h->dReinit; sa.imgObj = h->dImgObj; sa.aux = h->fused ? h->dAux : nullptr;
+    sa.reinit = h->dReinit; sa.imgObj = h->dPImgObj; sa.pgeo = h->dPGeo; sa.aux = h->fused ? h->dAux : nullptr;
     std::memcpy(sa.J, h->J, sizeof(sa.J));
     std::memcpy(sa.Jinv, h->Jinv, sizeof(sa.Jinv));
     return sa;
@@ -575,9 +710,10 @@ int prepare_patches(rdxg_solver* h) {
     // Object::addRegGamma (object.cpp:465-468): reg_gamma = sum_j 0.1 rg_j / nObjectImages
     std::vector<double> gam((size_t)h->P * h->nObj, 0.0);
     for (int p = 0; p < h->P; ++p) {
-        for (int j = 0; j < h->I; ++j) {
-            const int o = h->imgObj[j];
-            gam[(size_t)p * h->nObj + o] += 0.10 * rg[(size_t)p * h->I + j] / h->objCount[o];
+        const rdxg_solver::Shape& sh = h->shapes[h->patchShape[p]];
+        for (int j = 0; j < sh.nImg; ++j) {
+            const int o = sh.imgObj[j];
+            gam[(size_t)p * h->nObj + o] += 0.10 * rg[(size_t)p * h->I + j] / sh.objCount[o];
         }
     }
     if (h->haveFixedGamma) gam = h->hFixedGamma;
@@ -592,6 +728,11 @@ int prepare_patches(rdxg_solver* h) {
 
 int set_patches_common(rdxg_solver* h, int32_t P, const double* residual_alpha, const double* fixed_gamma) {
     if (P < 1 || P > h->Pmax) { h->err = "n_patches out of range"; return RDXG_ERR_ARG; }
+    if (h->ragged && P != h->raggedPatches) {
+        h->err = "the patch shapes were given for " + std::to_string(h->raggedPatches) + " patches, not " +
+                 std::to_string(P);
+        return RDXG_ERR_ARG;
+    }
     h->P = P;
     h->haveInit = false;     // a new batch starts at zero unless rdxg_set_initial_alpha follows
     const size_t G = (size_t)P * h->I;
@@ -613,7 +754,11 @@ int upload_alpha(rdxg_solver* h, const double* alpha) {
     CK(h, cudaStreamSynchronize(h->stream));
     std::vector<T> ae(G * h->M);
     for (size_t g = 0; g < G; ++g) {
+        // a ragged batch: the image slots and modes a patch does not use stay at zero
+        const rdxg_solver::Shape& sh = h->shapes[h->patchShape[g / h->I]];
+        const bool slotUsed = (int)(g % h->I) < sh.nImg;
         for (int m = 0; m < h->M; ++m) {
+            if (!slotUsed || m >= sh.M) { ae[g * h->M + m] = (T)0; continue; }
             double v = alpha[g * h->M + m];
             if (m == h->geo.tilt_x) v += curTilt[g * 2 + 1] - h->hResAlpha[g * 2 + 1];
             else if (m == h->geo.tilt_y) v += curTilt[g * 2 + 0] - h->hResAlpha[g * 2 + 0];
@@ -671,7 +816,7 @@ void phase_general(rdxg_solver* h, cudaStream_t st) {
     if (h->fused || !h->tcPlan.valid) return;
     PhaseTcArgs a;
     a.Zt = h->dZt; a.alphaEff = (const float*)h->dAlphaEff; a.phiFixed = (const float*)h->dPhi;
-    a.imgCh = h->dImgCh; a.evalP = h->dEvalP; a.nEvalP = h->dCounters + kCounterEvalP;
+    a.imgCh = h->dPImgCh; a.evalP = h->dEvalP; a.nEvalP = h->dCounters + kCounterEvalP;
     a.phi = (float*)h->dPhiImg; a.status = h->dTcStatus;
     a.I = h->I; a.M = h->M; a.n2 = h->n * h->n; a.nCh = h->C;
     a.G = h->tcPlan.G; a.NT = h->tcPlan.NT; a.KP = h->tcPlan.KP; a.parts = h->tcPlan.parts;
@@ -779,14 +924,15 @@ int host_lists(rdxg_solver* h, int req, int mode) {
     std::vector<EvalItem> ev;
     std::vector<PoItem> po;
     for (int p = 0; p < h->P; ++p) {
+        const rdxg_solver::Shape& sh = h->shapes[h->patchShape[p]];
         for (int o = 0; o < h->nObj; ++o) {
-            const int cnt = h->objCount[o];
+            const int cnt = sh.objCount[o];
             const int nc = (cnt + h->chunk - 1) / h->chunk;
             for (int c = 0; c < nc; ++c) {
                 EvalItem it;
-                it.p = p; it.o = o; it.first = h->objFirst[o] + c * h->chunk;
+                it.p = p; it.o = o; it.first = sh.objFirst[o] + c * h->chunk;
                 it.count = std::min(h->chunk, cnt - c * h->chunk);
-                it.chunk = h->objChunk0[o] + c; it.df = req == REQ_DF ? 1 : 0;
+                it.chunk = sh.objChunk0[o] + c; it.df = req == REQ_DF ? 1 : 0;
                 ev.push_back(it);
             }
             PoItem pi;
@@ -939,6 +1085,7 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
     if (at && atoi(at) == 0) h->tune = 0;   // default shapes, no measurement
     const char* nf = getenv("RDXG_NO_FUSED");
     if (!r && !(nf && atoi(nf))) r = setup_fused(h, s);
+    if (!r) r = upload_geometry(h);   // every patch shape 0 (the handle's own geometry)
     if (!r && !h->fused && !h->fp64) {
         // the general FP32 path (OTF size 128, or a support the half-plane evaluation does not
         // take): the mode expansion on the tensor cores ahead of the transform kernel
@@ -1033,6 +1180,10 @@ int rdxg_set_reg_alpha(rdxg_solver* h, const double* weights) {
         const int r = dalloc_t(h, &h->dRegW, (size_t)h->nPar);
         if (r) return r;
     }
+    if (h->ragged) {
+        h->err = "REG_ALPHA weights are per handle geometry; a ragged batch (rdxg_set_patch_shapes) does not take them";
+        return RDXG_ERR_UNSUPPORTED;
+    }
     h->hRegW.assign(weights, weights + h->nPar);
     // on the handle's stream, after any of its work still in flight
     CK(h, cudaMemcpyAsync(h->dRegW, h->hRegW.data(), (size_t)h->nPar * sizeof(double), cudaMemcpyHostToDevice,
@@ -1051,8 +1202,21 @@ int set_start(rdxg_solver* h, const double* alpha, bool recut) {
             const int r = dalloc_t(h, &h->dInitAlpha, (size_t)h->Pmax * h->nPar);
             if (r) return r;
         }
-        CK(h, cudaMemcpyAsync(h->dInitAlpha, alpha, (size_t)h->P * h->nPar * sizeof(double), cudaMemcpyHostToDevice,
-                              h->stream));
+        if (h->ragged) {
+            // the image slots and modes a patch does not use start (and stay) at zero
+            std::vector<double> a(alpha, alpha + (size_t)h->P * h->nPar);
+            for (int p = 0; p < h->P; ++p) {
+                const rdxg_solver::Shape& sh = h->shapes[h->patchShape[p]];
+                for (int i = 0; i < h->nPar; ++i)
+                    if (i / h->M >= sh.nImg || i % h->M >= sh.M) a[(size_t)p * h->nPar + i] = 0.0;
+            }
+            CK(h, cudaMemcpyAsync(h->dInitAlpha, a.data(), a.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                  h->stream));
+            CK(h, cudaStreamSynchronize(h->stream));
+        } else {
+            CK(h, cudaMemcpyAsync(h->dInitAlpha, alpha, (size_t)h->P * h->nPar * sizeof(double),
+                                  cudaMemcpyHostToDevice, h->stream));
+        }
     }
     h->haveInit = alpha != nullptr;
     h->initRecut = recut;
@@ -1062,6 +1226,58 @@ int set_start(rdxg_solver* h, const double* alpha, bool recut) {
 }  // extern "C++"
 
 int rdxg_set_initial_alpha(rdxg_solver* h, const double* alpha) { return set_start(h, alpha, true); }
+
+int rdxg_set_patch_shapes(rdxg_solver* h, int32_t n_shapes, const rdxg_patch_shape* shapes, int32_t n_patches,
+                          const int32_t* patch_shape) {
+    if (!h) return RDXG_ERR_ARG;
+    if (n_shapes <= 0) {
+        // back to a uniform batch: every patch the handle's geometry
+        h->shapes.resize(1);
+        h->patchShape.assign(h->Pmax, 0);
+        h->ragged = false;
+        h->raggedPatches = 0;
+        h->loaded = false;
+        return upload_geometry(h);
+    }
+    if (!shapes || !patch_shape || n_patches < 1 || n_patches > h->Pmax) { h->err = "bad patch shapes"; return RDXG_ERR_ARG; }
+    if (!h->hRegW.empty()) {
+        h->err = "REG_ALPHA weights are per handle geometry; a ragged batch does not take them";
+        return RDXG_ERR_UNSUPPORTED;
+    }
+    // every channel must have the same number of image slots (frames)
+    std::vector<int> perCh(h->C, 0);
+    for (int j = 0; j < h->I; ++j) perCh[h->imgCh[j]]++;
+    const int F = perCh[0];
+    for (int c = 0; c < h->C; ++c)
+        if (perCh[c] != F) { h->err = "ragged batches need the same number of frames in every channel"; return RDXG_ERR_ARG; }
+    const int needModes = std::max(h->geo.tilt_x, h->geo.tilt_y) + 1;
+    std::vector<rdxg_solver::Shape> add(n_shapes);
+    for (int k = 0; k < n_shapes; ++k) {
+        const rdxg_patch_shape& ps = shapes[k];
+        if (ps.frames < 1 || ps.frames > F || ps.n_modes < std::max(1, needModes) || ps.n_modes > h->M ||
+            ps.n_free < 1 || ps.n_free > h->nFree || ps.ns_nnz < 0 || (ps.ns_nnz > 0 && (!ps.ns_rows || !ps.ns_cols || !ps.ns_vals))) {
+            h->err = "patch shape " + std::to_string(k) + ": frames 1.." + std::to_string(F) + ", modes " +
+                     std::to_string(std::max(1, needModes)) + ".." + std::to_string(h->M) + ", n_free 1.." +
+                     std::to_string(h->nFree);
+            return RDXG_ERR_ARG;
+        }
+        rdxg_solver::Shape& sh = add[k];
+        sh.frames = ps.frames; sh.M = ps.n_modes; sh.nFree = ps.n_free;
+        int r = shape_tables(h, sh);
+        if (!r) r = shape_maps(h, sh, ps.ns_nnz, ps.ns_rows, ps.ns_cols, ps.ns_vals);
+        if (r) return r;
+    }
+    for (int p = 0; p < n_patches; ++p)
+        if (patch_shape[p] < 0 || patch_shape[p] >= n_shapes) { h->err = "patch_shape out of range"; return RDXG_ERR_ARG; }
+    h->shapes.resize(1);
+    h->shapes.insert(h->shapes.end(), add.begin(), add.end());
+    h->patchShape.assign(h->Pmax, 0);
+    for (int p = 0; p < n_patches; ++p) h->patchShape[p] = patch_shape[p] + 1;
+    h->ragged = true;
+    h->raggedPatches = n_patches;
+    h->loaded = false;   // the next rdxg_set_patches loads the batch these shapes describe
+    return upload_geometry(h);
+}
 
 int rdxg_set_start_alpha(rdxg_solver* h, const double* alpha) { return set_start(h, alpha, false); }
 
@@ -1140,6 +1356,10 @@ int rdxg_metric_noalloc(rdxg_solver* h, const double* alpha, double* metric) {
     if (!h->fused) {
         h->err = "rdxg_metric_noalloc: needs the FP32 half-plane evaluation (OTF size 32, 64 or 88 with a "
                  "symmetric OTF support)";
+        return RDXG_ERR_UNSUPPORTED;
+    }
+    if (h->ragged) {
+        h->err = "rdxg_metric_noalloc: takes uniform batches only (no rdxg_set_patch_shapes)";
         return RDXG_ERR_UNSUPPORTED;
     }
     int dev = -1;

@@ -75,7 +75,9 @@ struct CgArgs {
     const double* galpha;   // [P][nPar]
     const double* partial;  // [P][nObj][nTiles]
     const double* objWeight;
-    // null-space map, by parameter row and by free column
+    // null-space maps, by parameter row and by free column: every patch shape's, one after the
+    // other (PatchGeo::rowBase, colBase); rows in the handle's layout (image slot * M + mode)
+    const PatchGeo* pgeo;   // [P]
     const int32_t* rowPtr; const int32_t* rowCol; const double* rowVal;
     const float* rowVal32;  // FP32 copy of rowVal
     int32_t x1Smem;         // FP32 metric-request map enabled (dynamic shared memory n_free floats)
@@ -94,9 +96,9 @@ struct CgArgs {
     int32_t nTilesH;
     Lists L;
     int32_t chunkSize, chunksPerPatch;
-    const int32_t* objChunk0;      // [nObj]
-    const int32_t* objFirst;       // [nObj]
-    const int32_t* objCount;       // [nObj]
+    const int32_t* objChunk0;      // [P][nObj]
+    const int32_t* objFirst;       // [P][nObj]
+    const int32_t* objCount;       // [P][nObj]
     int32_t* aux;                  // [P][2]: reference object valid, refresh pending
     const double* regW;            // [nPar] REG_ALPHA weights, or null
     int32_t phaseList;             // general path: list the evaluated patches (tensor-core expansion)
@@ -109,9 +111,10 @@ __device__ void map_point(const CgArgs<T>& a, int p, const double* x1) {
     const double* off = a.alphaOff + (size_t)p * a.nPar;
     double* al = a.alpha + (size_t)p * a.nPar;
     T* ae = a.alphaEff + (size_t)p * a.nPar;
+    const int32_t* rp = a.rowPtr + a.pgeo[p].rowBase;
     for (int r = threadIdx.x; r < a.nPar; r += THREADS) {
         double v = off[r];
-        for (int e = a.rowPtr[r]; e < a.rowPtr[r + 1]; ++e) v += a.rowVal[e] * x1[a.rowCol[e]];
+        for (int e = rp[r]; e < rp[r + 1]; ++e) v += a.rowVal[e] * x1[a.rowCol[e]];
         al[r] = v;
         const int j = r / a.M, m = r % a.M;
         double ve = v;
@@ -129,14 +132,15 @@ __device__ void map_point(const CgArgs<T>& a, int p, const double* x1) {
 // map_point for every gradient, re-shift and final point, where it is used.
 template <typename T, int THREADS>
 __device__ void map_point_f32(const CgArgs<T>& a, int p, const double* x1, float* xs) {
-    const int nF = a.prm.n_free;
+    const int nF = a.pgeo[p].nFree;
     for (int c = threadIdx.x; c < nF; c += THREADS) xs[c] = (float)x1[c];
     __syncthreads();
     const double* off = a.alphaOff + (size_t)p * a.nPar;
     T* ae = a.alphaEff + (size_t)p * a.nPar;
+    const int32_t* rp = a.rowPtr + a.pgeo[p].rowBase;
     for (int r = threadIdx.x; r < a.nPar; r += THREADS) {
         float v = 0.f;
-        for (int e = a.rowPtr[r]; e < a.rowPtr[r + 1]; ++e) v = fmaf(a.rowVal32[e], xs[a.rowCol[e]], v);
+        for (int e = rp[r]; e < rp[r + 1]; ++e) v = fmaf(a.rowVal32[e], xs[a.rowCol[e]], v);
         v += (float)off[r];
         const int j = r / a.M, m = r % a.M;
         const size_t b = ((size_t)p * a.I + j) * 2;
@@ -152,20 +156,21 @@ template <typename T>
 __device__ void enqueue_eval(const CgArgs<T>& a, int p, int rq, int mode) {
     // one reservation per list (the atomics go out together), then the writes
     const int kp = atomicAdd(a.L.nEvalP, 1);
-    const int k0 = atomicAdd(a.L.nEval, a.chunksPerPatch);
+    const int k0 = atomicAdd(a.L.nEval, a.pgeo[p].chunks);
     const int j0 = atomicAdd(a.L.nPo, a.nObj);
     a.L.evalP[kp] = p;
     for (int o = 0; o < a.nObj; ++o) {
-        const int cnt = a.objCount[o];
+        const size_t po = (size_t)p * a.nObj + o;
+        const int cnt = a.objCount[po];
         const int nc = (cnt + a.chunkSize - 1) / a.chunkSize;
         for (int c = 0; c < nc; ++c) {
             EvalItem it;
             it.p = p; it.o = o;
-            it.first = a.objFirst[o] + c * a.chunkSize;
+            it.first = a.objFirst[po] + c * a.chunkSize;
             it.count = min(a.chunkSize, cnt - c * a.chunkSize);
-            it.chunk = a.objChunk0[o] + c;
+            it.chunk = a.objChunk0[po] + c;
             it.df = (rq == REQ_DF) ? 1 : 0;
-            a.L.eval[k0 + a.objChunk0[o] + c] = it;
+            a.L.eval[k0 + a.objChunk0[po] + c] = it;
         }
         PoItem pi;
         pi.p = p; pi.o = o; pi.mode = mode;
@@ -185,12 +190,17 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
     if (threadIdx.x == 0) { pcShared = st.pc; reqShared = st.req; }
     __syncthreads();
     const int pc0 = pcShared, req0 = reqShared;
-    const int nF = a.prm.n_free;
-    double* x = a.vec + (size_t)p * 5 * nF;
-    double* pv = x + nF;
-    double* g = pv + nF;
-    double* g0 = g + nF;
-    double* x1 = g0 + nF;
+    const PatchGeo pg = a.pgeo[p];
+    const int nF = pg.nFree;
+    const int32_t* rp = a.rowPtr + pg.rowBase;
+    const int32_t* cp = a.colPtr + pg.colBase;
+    // the patch's vectors, nF long, at the stride of the handle's largest (prm.n_free)
+    const int stride = a.prm.n_free;
+    double* x = a.vec + (size_t)p * 5 * stride;
+    double* pv = x + stride;
+    double* g = pv + stride;
+    double* g0 = g + stride;
+    double* x1 = g0 + stride;
     if (pc0 == PC_DONE) {
         if (threadIdx.x == 0) a.req[p] = REQ_DONE;
         return;
@@ -239,7 +249,7 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
             double part = 0;
             for (int r = threadIdx.x; r < a.nPar; r += THREADS) {
                 double v = off[r];
-                for (int e = a.rowPtr[r]; e < a.rowPtr[r + 1]; ++e) v += a.rowVal[e] * x1[a.rowCol[e]];
+                for (int e = rp[r]; e < rp[r + 1]; ++e) v += a.rowVal[e] * x1[a.rowCol[e]];
                 part += 0.5 * v * v * a.regW[r];
             }
             f += block_sum<THREADS>(part, red);
@@ -252,7 +262,7 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
         const int mcount = a.modeCount[p];
         for (int c = threadIdx.x; c < nF; c += THREADS) {
             double v = 0;
-            for (int e = a.colPtr[c]; e < a.colPtr[c + 1]; ++e) {
+            for (int e = cp[c]; e < cp[c + 1]; ++e) {
                 const int row = a.colRow[e];
                 const double gr = (a.regW && row % a.M >= mcount) ? al[row] * a.regW[row] : ga[row];
                 v += a.colVal[e] * gr;
@@ -269,7 +279,10 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
     __shared__ int rqShared;
     if (threadIdx.x < 32) {
         WarpVec V{nF};
-        Machine<WarpVec> mc(a.prm, st, V, x, pv, g, g0, x1, a.metrics + (size_t)p * a.prm.max_metrics);
+        CgParams prm = a.prm;       // the patch's own sizes
+        prm.n_free = nF;
+        prm.n_modes = pg.nMode;
+        Machine<WarpVec> mc(prm, st, V, x, pv, g, g0, x1, a.metrics + (size_t)p * a.prm.max_metrics);
         const int r = mc.advance(f);
         if (threadIdx.x == 0) rqShared = r;
     }
@@ -320,7 +333,8 @@ struct ShiftArgs {
     double* tiltOff;         // [P][I][2] currentTiltOffset (y, x)
     int32_t* shift;          // [P][I][2]
     uint8_t* reinit;         // [P][I]
-    const int32_t* imgObj;
+    const int32_t* imgObj;   // [P][I]
+    const PatchGeo* pgeo;     // [P]
     int32_t* aux;            // [P][2] reference object valid flag (cleared on re-initialisation)
     double J[2][2], Jinv[2][2];
     // rounds run as a CUDA graph: the conditions of the graph's optional kernels (image
@@ -350,10 +364,11 @@ __global__ void k_shift(ShiftArgs a) {
         for (int j = threadIdx.x; j < a.I; j += blockDim.x) a.reinit[(size_t)p * a.I + j] = 0;
         return;
     }
+    const int nImg = a.pgeo[p].nImg;
     __shared__ int objShifted[64];
     for (int o = threadIdx.x; o < a.nObj; o += blockDim.x) objShifted[o] = 0;
     __syncthreads();
-    for (int j = threadIdx.x; j < a.I; j += blockDim.x) {
+    for (int j = threadIdx.x; j < nImg; j += blockDim.x) {
         const size_t gi = (size_t)p * a.I + j;
         const double* al = a.alpha + gi * a.M;
         if (a.tiltX < 0 || a.tiltY < 0) continue;
@@ -377,12 +392,12 @@ __global__ void k_shift(ShiftArgs a) {
             a.shift[gi * 2 + 1] += act[1];
             a.tiltOff[gi * 2 + 0] += act[1] * a.Jinv[1][0] + act[0] * a.Jinv[1][1];
             a.tiltOff[gi * 2 + 1] += act[1] * a.Jinv[0][0] + act[0] * a.Jinv[0][1];
-            atomicExch(&objShifted[a.imgObj[j]], 1);
+            atomicExch(&objShifted[a.imgObj[gi]], 1);
         }
     }
     __syncthreads();
     for (int j = threadIdx.x; j < a.I; j += blockDim.x) {
-        const int sh = objShifted[a.imgObj[j]];
+        const int sh = j < nImg ? objShifted[a.imgObj[(size_t)p * a.I + j]] : 0;
         a.reinit[(size_t)p * a.I + j] = sh ? 1 : 0;
         if (sh && a.aux) a.aux[2 * p + 0] = 0;
     }

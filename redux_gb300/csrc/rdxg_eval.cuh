@@ -56,7 +56,7 @@ struct HalfPlane {
     const int32_t* idx;     // [nH] centred index of each half-plane support point
     int32_t chunkSize;      // images per chunk
     int32_t chunksPerPatch; // sum over objects of ceil(count / chunkSize)
-    const int32_t* objChunk0;  // [nObj] first chunk of each object within a patch
+    const int32_t* objChunk0;  // [P][nObj] first chunk of each object within its patch
 };
 
 // Mode expansion on the tensor cores (rdxg_phase_tc.cu): the launch shape chosen per job.
@@ -70,7 +70,7 @@ struct PhaseTcArgs {
     const __nv_bfloat16* Zt;   // [tile][part][128 x KP] split modes in the operand layout
     const float* alphaEff;     // [g][M]
     const float* phiFixed;     // [C][n*n]
-    const int32_t* imgCh;      // [I]
+    const int32_t* imgCh;      // [P][I] channel of each image slot of each patch
     const int32_t* evalP;      // patches with an evaluation this round
     const int32_t* nEvalP;
     float* phi;                // [g][n*n]
@@ -134,8 +134,7 @@ __global__ void __launch_bounds__(PIX) k_phase(EvalParams<T> e) {
             for (int c = 0; c < MAXC; ++c) acc[c] += as[c * M + m] * z;
         }
         for (int c = 0; c < it.count && c < MAXC; ++c) {
-            const int j = it.first + c;
-            e.phi[(g0 + c) * n2 + q] = e.k.phiFixed[(size_t)e.k.imgCh[j] * n2 + q] + acc[c];
+            e.phi[(g0 + c) * n2 + q] = e.k.phiFixed[(size_t)e.k.pImgCh[g0 + c] * n2 + q] + acc[c];
         }
     }
 }
@@ -172,7 +171,7 @@ __global__ void __launch_bounds__(PIX, 4) k_phase_patch(EvalParams<T> e) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* as = reinterpret_cast<T*>(smem_raw);          // [2][MAXI][MAXM]
     T* pfs = as + 2 * MAXI * MAXM;                   // [MAXCH][PIX]
-    int* chs = reinterpret_cast<int*>(pfs + MAXCH * PIX);   // [MAXI]
+    int* chs = reinterpret_cast<int*>(pfs + MAXCH * PIX);   // [2][MAXI]
     const int M = e.k.M, I = e.k.I;
     const int nP = *e.L.nEvalP;
     const int S = gridDim.x / nPix;
@@ -189,7 +188,6 @@ __global__ void __launch_bounds__(PIX, 4) k_phase_patch(EvalParams<T> e) {
         const int qq = q0 + i % PIX;
         pfs[i] = qq < n2 ? e.k.phiFixed[(size_t)(i / PIX) * n2 + qq] : (T)0;
     }
-    for (int i = threadIdx.x; i < MAXI; i += PIX) chs[i] = i < I ? e.k.imgCh[i] : 0;
     __syncthreads();
     const int IM = I * M;
     auto fetch = [&](int k, int buf) {
@@ -197,6 +195,8 @@ __global__ void __launch_bounds__(PIX, 4) k_phase_patch(EvalParams<T> e) {
         const T* src = e.k.alphaEff + (size_t)p * IM;
         T* dst = as + buf * MAXI * MAXM;
         for (int i = threadIdx.x; i < IM; i += PIX) cp_async4(dst + (i / M) * MAXM + i % M, src + i);
+        // the channel of each image slot of the patch (two buffers, like the coefficients)
+        for (int i = threadIdx.x; i < MAXI; i += PIX) chs[buf * MAXI + i] = i < I ? e.k.pImgCh[(size_t)p * I + i] : 0;
     };
     fetch(s0, 0);
     cp_async_commit();
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(PIX, 4) k_phase_patch(EvalParams<T> e) {
                 T* out = e.phi + ((size_t)p * I + i) * n2 + q;
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
-                    if (i + j < I) out[(size_t)j * n2] = pfs[chs[i + j] * PIX + threadIdx.x] + accs[j];
+                    if (i + j < I) out[(size_t)j * n2] = pfs[chs[buf * MAXI + i + j] * PIX + threadIdx.x] + accs[j];
             }
         }
         __syncthreads();    // buffer fully read before the next copy into it
@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
         const T* phiNext = nextItem < nItems ? e.phi + ((size_t)nit.p * e.k.I + nit.first + nextJj) * n2 : nullptr;
         const int j = it.first + jj;
         const size_t g = (size_t)it.p * e.k.I + j;
-        const int ch = e.k.imgCh[j];
+        const int ch = e.k.pImgCh[g];
         // a gradient evaluation keeps PF, X and the full OTF for the gradient kernels, unless
         // they recompute them (the OTF is still kept when a buffer for it is given)
         eval_image<T, N, THREADS>(phiNext, phiBuf, amp, e.k.otfNorm[ch], it.df && !e.k.recompute,
@@ -508,7 +508,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_fd_half(EvalParams<T> e) {
     for (int w = blockIdx.x; w < nWork; w += gridDim.x) {
         const int p = kp.fdP[w / kp.I], j = w % kp.I;
         const size_t g = (size_t)p * kp.I + j;
-        const int o = kp.imgObj[j];
+        if (j >= kp.pgeo[p].nImg) continue;   // an image slot the patch does not use
+        const int o = kp.pImgObj[g];
         const double wgt = kp.objWeight[o];
         const int mc = kp.modeCount[p];
         double* ga = kp.galpha + g * kp.M;
@@ -517,7 +518,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_fd_half(EvalParams<T> e) {
             continue;
         }
         const size_t po = (size_t)p * kp.nObj + o;
-        const T c = kp.otfNorm[kp.imgCh[j]];
+        const T c = kp.otfNorm[kp.pImgCh[g]];
         const double hstep = kp.objGradStep[o];
         __syncthreads();    // previous image's staged factors consumed
         const cx<T>* Xg = kp.X + g * N2;
@@ -621,8 +622,8 @@ __global__ void __launch_bounds__(THREADS) k_reduce(EvalParams<T> e) {
         const int tile = w % e.nTilesH;
         const size_t po = (size_t)it.p * e.k.nObj + it.o;
         const T gam = (T)e.k.gamma[po];
-        const int c0 = e.hp.objChunk0[it.o];
-        const int nc = (e.k.objCount[it.o] + e.hp.chunkSize - 1) / e.hp.chunkSize;
+        const int c0 = e.hp.objChunk0[po];
+        const int nc = (e.k.pObjCount[po] + e.hp.chunkSize - 1) / e.hp.chunkSize;
         const Acc4<T>* base = e.part + (size_t)(it.p * e.hp.chunksPerPatch + c0) * nH;
         double acc = 0;
         const int h = tile * 32 + lane;

@@ -224,7 +224,7 @@ void EvalLauncher<T, N>::eval(const EvalParams<T>& e, int npt, int grid, cudaStr
 
 template <typename T>
 static size_t phase_patch_smem(int maxm) {
-    return ((size_t)2 * kPhaseMaxImg * maxm + kPhaseMaxCh * kPhaseRegPix) * sizeof(T) + kPhaseMaxImg * sizeof(int);
+    return ((size_t)2 * kPhaseMaxImg * maxm + kPhaseMaxCh * kPhaseRegPix) * sizeof(T) + 2 * kPhaseMaxImg * sizeof(int);
 }
 
 template <typename T, int N>
@@ -237,7 +237,7 @@ void EvalLauncher<T, N>::phase(const EvalParams<T>& e, int grid, cudaStream_t st
     if constexpr (std::is_same<T, float>::value) {
         if (e.Zt && e.tc.valid) {
             PhaseTcArgs a;
-            a.Zt = e.Zt; a.alphaEff = e.k.alphaEff; a.phiFixed = e.k.phiFixed; a.imgCh = e.k.imgCh;
+            a.Zt = e.Zt; a.alphaEff = e.k.alphaEff; a.phiFixed = e.k.phiFixed; a.imgCh = e.k.pImgCh;
             a.evalP = e.L.evalP; a.nEvalP = e.L.nEvalP; a.phi = e.phi; a.status = e.tcStatus;
             a.I = e.k.I; a.M = e.k.M; a.n2 = (N / 2) * (N / 2); a.nCh = e.nCh;
             a.G = e.tc.G; a.NT = e.tc.NT; a.KP = e.tc.KP; a.parts = e.tc.parts;

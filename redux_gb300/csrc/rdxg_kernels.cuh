@@ -16,6 +16,19 @@
 
 namespace rdxg {
 
+// Geometry of one patch of the batch.  A uniform batch gives every patch the handle's own;
+// a ragged batch (rdxg_set_patch_shapes) gives each patch its frames per channel and its
+// modes: its images fill the first nImg image slots (each channel's first frames, in the
+// handle's image order) and its modes are the first nMode of the handle's.
+struct PatchGeo {
+    int32_t nImg;       // image slots in use, [0, nImg)
+    int32_t nMode;      // modes in use, [0, nMode)
+    int32_t nFree;      // columns of its null-space map
+    int32_t chunks;     // chunks of its images in the fused evaluation
+    int32_t rowBase;    // its null-space map by row: rowPtr[rowBase + r], r < I*M (handle rows)
+    int32_t colBase;    // by column: colPtr[colBase + c], c <= nFree
+};
+
 template <typename T>
 struct KParams {
     int32_t P, I, M, nObj, N, n, ps, cs, margin, nTiles;
@@ -25,10 +38,11 @@ struct KParams {
     const T* phiFixed;   // [C][n*n]
     const T* otfNorm;    // [C]
     const uint8_t* otfMask;   // [N*N] centred OTF support
-    const int32_t* imgObj;    // [I]
-    const int32_t* imgCh;     // [I]
-    const int32_t* objFirst;  // [nObj]
-    const int32_t* objCount;  // [nObj]
+    const PatchGeo* pgeo;     // [P]
+    const int32_t* pImgObj;   // [P][I] object of each image slot of each patch
+    const int32_t* pImgCh;    // [P][I] channel of each image slot
+    const int32_t* pObjFirst; // [P][nObj] first image slot of each object
+    const int32_t* pObjCount; // [P][nObj]
     const double* objWeight;  // [nObj]
     const double* objGradStep;// [nObj]
     const double* window;     // [ps*ps]
@@ -166,7 +180,7 @@ template <typename T, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_fit_plane(KParams<T> kp, int full) {
     const int po = blockIdx.x;
     const int p = po / kp.nObj, o = po % kp.nObj;
-    const int j0 = kp.objFirst[o], cnt = kp.objCount[o];
+    const int j0 = kp.pObjFirst[po], cnt = kp.pObjCount[po];
     __shared__ double red[33];
     __shared__ int any;
     if (!full) {
@@ -245,6 +259,7 @@ __global__ void k_add_plane(const double* plane, float* objects, int ps) {
 template <typename T, int N, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_prep(KParams<T> kp, int full) {
     const int g = blockIdx.x;
+    if (g % kp.I >= kp.pgeo[g / kp.I].nImg) return;   // an image slot the patch does not use
     if (!full && !kp.reinit[g]) return;
     constexpr int LDS = Tile<N>::LDS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -258,7 +273,7 @@ __global__ void __launch_bounds__(THREADS) k_prep(KParams<T> kp, int full) {
     const float* cut = kp.cutouts + (size_t)g * cs * cs;
     // FIT_PLANE: getWindowedImg subtracts the object's fitted plane inside the window,
     // (img - avg - plane) * window + avg (subimage.cpp:117-123)
-    const double* pl = kp.plane ? kp.plane + 2 * ((size_t)(g / kp.I) * kp.nObj + kp.imgObj[g % kp.I]) : nullptr;
+    const double* pl = kp.plane ? kp.plane + 2 * ((size_t)(g / kp.I) * kp.nObj + kp.pImgObj[g]) : nullptr;
     auto windowed = [&](int y, int x, int i, double avg) {
         const double v = (double)cut[(oy + y) * cs + ox + x] - avg;
         return (pl ? v - plane_value(pl, ps, y, x) : v) * kp.window[i] + avg;
@@ -352,6 +367,7 @@ __global__ void __launch_bounds__(THREADS) k_forward(KParams<T> kp) {
     const int p = g / kp.I, j = g % kp.I;
     const int rq = kp.req[p];
     if (rq != REQ_F && rq != REQ_DF) return;
+    if (j >= kp.pgeo[p].nImg) return;
     // X and PF are kept for the gradient kernels unless they recompute them
     const bool df = (rq == REQ_DF) && !kp.recompute;
     constexpr int LDS = Tile<N>::LDS;
@@ -365,7 +381,7 @@ __global__ void __launch_bounds__(THREADS) k_forward(KParams<T> kp) {
     for (int m = threadIdx.x; m < M; m += THREADS) al[m] = kp.alphaEff[(size_t)g * M + m];
     zero_tile<T, N>(s);
     __syncthreads();
-    const int ch = kp.imgCh[j];
+    const int ch = kp.pImgCh[g];
     const T c = kp.otfNorm[ch];
     const T* phf = kp.phiFixed + (size_t)ch * n2;
     for (int q = threadIdx.x; q < n2; q += THREADS) {
@@ -429,8 +445,8 @@ __global__ void __launch_bounds__(THREADS) k_accum(KParams<T> kp) {
     double term = 0;
     const bool df = (rq == REQ_DF);
     if (u < N2) {
-        const size_t fbase = (size_t)p * kp.I + kp.objFirst[o];
-        const int cnt = kp.objCount[o];
+        const size_t fbase = (size_t)p * kp.I + kp.pObjFirst[po];
+        const int cnt = kp.pObjCount[po];
         const T gam = (T)kp.gamma[po];
         cx<T> O = mkc<T>(0, 0);
         T Qt = (T)1;
@@ -485,7 +501,7 @@ __device__ __forceinline__ void project_modes(const KParams<T>& kp, int kind, in
     constexpr int LDS = Tile<N>::LDS;
     constexpr int n = N / 2, n2 = n * n, N2 = N * N;
     const size_t g = (size_t)p * kp.I + j;
-    const int o = kp.imgObj[j];
+    const int o = kp.pImgObj[g];
 #pragma unroll 4
     for (int q = tid; q < n2; q += THREADS) {
         const int y = q / n, x = q % n;
@@ -500,7 +516,7 @@ __device__ __forceinline__ void project_modes(const KParams<T>& kp, int kind, in
     // projection on the modes: one warp per mode
     const int lane = tid & 31, wid = tid >> 5;
     const int mc = kp.modeCount[p];
-    const int ch = kp.imgCh[j];
+    const int ch = kp.pImgCh[g];
     const double c = (double)kp.otfNorm[ch];
     const double w = kp.objWeight[o];
     double scale;
@@ -551,7 +567,7 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
     T* v = reinterpret_cast<T*>(tw + N);            // [n2]
     __syncthreads();    // previous image's shared memory consumed
     load_twiddles<T, N>(tw, kp.tw);
-    const int o = kp.imgObj[j];
+    const int o = kp.pImgObj[g];
     const size_t po = (size_t)p * kp.nObj + o;
     const cx<T>* Oo = kp.O + po * N2;
     const cx<T>* Dg = kp.D + (size_t)g * N2;
@@ -591,7 +607,9 @@ __global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
     // items the in-place transforms' index arithmetic is hoisted and spills
     const int nWork = *kp.nGradP * kp.I;
     const int w = blockIdx.x;
-    if (w < nWork) adjoint_image<T, N, THREADS>(kp, kind, kp.gradP[w / kp.I], w % kp.I);
+    if (w >= nWork) return;
+    const int p = kp.gradP[w / kp.I], j = w % kp.I;
+    if (j < kp.pgeo[p].nImg) adjoint_image<T, N, THREADS>(kp, kind, p, j);
 }
 
 // ----------------------------------------------------------------------------------
@@ -621,7 +639,8 @@ __device__ __forceinline__ void recompute_pupil(const KParams<T>& kp, size_t g, 
                                                 int tid) {
     constexpr int LDS = Tile<N>::LDS;
     constexpr int n = N / 2, n2 = n * n;
-    const int ch = kp.imgCh[j];
+    (void)j;
+    const int ch = kp.pImgCh[g];
     const T c = kp.otfNorm[ch];
     const T* phf = kp.phiFixed + (size_t)ch * n2;
     for (int i = tid; i < Tile<N>::ELEMS; i += THREADS) s[i] = mkc<T>(0, 0);
@@ -693,6 +712,7 @@ __global__ void __launch_bounds__(THREADS) k_adjoint_rc(KParams<T> kp, int kind)
     const int nWork = *kp.nGradP * kp.I;
     const int w = blockIdx.x;
     if (w >= nWork) return;
+    if (w % kp.I >= kp.pgeo[kp.gradP[w / kp.I]].nImg) return;   // an image slot the patch does not use
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* tw = s + TILES * Tile<N>::ELEMS;
@@ -723,7 +743,7 @@ __global__ void __launch_bounds__(THREADS) k_adjoint_rc(KParams<T> kp, int kind)
     }
     __syncthreads();
     if (SREC) fft2d<T, N, +1, THREADS, false>(s, tw, tid);
-    const size_t po = (size_t)p * kp.nObj + kp.imgObj[j];
+    const size_t po = (size_t)p * kp.nObj + kp.pImgObj[g];
     const cx<T>* Oo = kp.O + po * N2;
     const cx<T>* Dg = kp.D + g * N2;
     for (int i = tid; i < N2; i += THREADS) {
@@ -764,7 +784,8 @@ __device__ __forceinline__ void fd_image(const KParams<T>& kp, int p, int j, int
     constexpr int LDS = Tile<N>::LDS;
     constexpr int n = N / 2, n2 = n * n, N2 = N * N;
     constexpr bool PP = PingPong<T, N>::value;
-    const int o = kp.imgObj[j];
+    if (j >= kp.pgeo[p].nImg) return;   // an image slot the patch does not use
+    const int o = kp.pImgObj[g];
     if (m >= kp.modeCount[p] || kp.objWeight[o] == 0.0) {
         if (tid == 0) kp.galpha[(size_t)g * kp.M + m] = 0.0;
         return;
@@ -778,7 +799,7 @@ __device__ __forceinline__ void fd_image(const KParams<T>& kp, int p, int j, int
     load_twiddles<T, N>(tw, kp.tw);
     for (int i = tid; i < Tile<N>::ELEMS; i += THREADS) s[i] = mkc<T>(0, 0);
     __syncthreads();
-    const int ch = kp.imgCh[j];
+    const int ch = kp.pImgCh[g];
     const T c = kp.otfNorm[ch];
     const double h = kp.objGradStep[o];
     const T* Zm = kp.Z + (size_t)m * n2;
@@ -887,7 +908,8 @@ __global__ void __launch_bounds__(THREADS) k_fd_rc(KParams<T> kp) {
         for (int w = w0; w < w1; ++w) {
             const int p = kp.fdP[w / (kp.M * kp.I)], j = (w / kp.M) % kp.I, m = w % kp.M;
             const size_t g = (size_t)p * kp.I + j;
-            if (m < kp.modeCount[p] && kp.objWeight[kp.imgObj[j]] != 0.0 && (long)g != gPrev) {
+            if (j < kp.pgeo[p].nImg && m < kp.modeCount[p] && kp.objWeight[kp.pImgObj[g]] != 0.0 &&
+                (long)g != gPrev) {
                 prepare(g, j, Xb);
                 gPrev = (long)g;
             }
@@ -898,7 +920,8 @@ __global__ void __launch_bounds__(THREADS) k_fd_rc(KParams<T> kp) {
         if (w >= nWork) return;
         const int p = kp.fdP[w / (kp.M * kp.I)], j = (w / kp.M) % kp.I, m = w % kp.M;
         const size_t g = (size_t)p * kp.I + j;
-        if (m >= kp.modeCount[p] || kp.objWeight[kp.imgObj[j]] == 0.0) {
+        if (j >= kp.pgeo[p].nImg) return;   // an image slot the patch does not use
+        if (m >= kp.modeCount[p] || kp.objWeight[kp.pImgObj[g]] == 0.0) {
             if (threadIdx.x == 0) kp.galpha[g * kp.M + m] = 0.0;
             return;
         }

@@ -1,9 +1,12 @@
 // Mode expansion on the tensor cores: phi = phi_fixed + sum_m alpha_m Z_m
 // (SubImage::calcPhi / addToPhi, subimage.cpp:509-544) for every image of the round's work
 // list as one GEMM  Phi[pixels x images] = Z'[pixels x K] * B[images x K]^T, where the K
-// columns are the M modes followed by the fixed phase of each channel, and B holds each
-// image's coefficients followed by a one-hot entry for its channel (so phi_fixed is added by
-// the tensor core; K is padded to a multiple of 16 anyway).
+// columns are the fixed phase of each channel followed by the M modes, and B holds a one-hot
+// entry for the image's channel followed by its coefficients (so phi_fixed is added by the
+// tensor core; K is padded to a multiple of 16 anyway).  The channels come first so that a
+// patch using only the first modes of a handle (a ragged batch) has its non-zero products in
+// the same K positions as in a handle of its own mode count: the extra modes only add zero
+// products at the end.
 //
 // FP32 operands are split into BF16 parts, x = x0 + x1 (+ x2), each part the BF16 rounding of
 // what the previous parts leave, and the products x_i * y_j with i + j < parts are summed by
@@ -23,8 +26,8 @@ namespace {
 constexpr int kTcRows = 128;     // pixels per tile (MMA M)
 constexpr int kTcThreads = 256;  // eight warps: two per quarter of the accumulator lanes
 
-// Zt[tile][part][kmajor(r, k)] for r < 128 pixels of the tile: k < M the modes, M <= k < M + C
-// the channels' fixed phases, zero elsewhere.
+// Zt[tile][part][kmajor(r, k)] for r < 128 pixels of the tile: k < C the channels' fixed
+// phases, C <= k < C + M the modes, zero elsewhere.
 __global__ void k_tc_pack_modes(const float* __restrict__ Z, const float* __restrict__ phiFixed, int M, int C,
                                 int n2, int KP, int parts, int nTiles, __nv_bfloat16* __restrict__ out) {
     const size_t per = (size_t)kTcRows * KP;
@@ -35,8 +38,8 @@ __global__ void k_tc_pack_modes(const float* __restrict__ Z, const float* __rest
         const int r = e % kTcRows, k = e / kTcRows;
         const int q = tile * kTcRows + r;
         float rest = 0.f;
-        if (q < n2 && k < M) rest = Z[(size_t)k * n2 + q];
-        else if (q < n2 && k < M + C) rest = phiFixed[(size_t)(k - M) * n2 + q];
+        if (q < n2 && k < C) rest = phiFixed[(size_t)k * n2 + q];
+        else if (q < n2 && k < C + M) rest = Z[(size_t)(k - C) * n2 + q];
         __nv_bfloat16* dst = out + (size_t)tile * parts * per + tc::kmajor_off(r, k, kTcRows);
         for (int pt = 0; pt < parts; ++pt) {
             const __nv_bfloat16 b = __float2bfloat16_rn(rest);
@@ -72,7 +75,7 @@ __global__ void __launch_bounds__(kTcThreads) k_phase_tc(PhaseTcArgs a) {
     __shared__ uint32_t tmemBase;
     __shared__ int issued;
 
-    const int KP = a.KP, NT = a.NT, n2 = a.n2, I = a.I, M = a.M, G = a.G, parts = a.parts;
+    const int KP = a.KP, NT = a.NT, n2 = a.n2, I = a.I, M = a.M, C = a.nCh, G = a.G, parts = a.parts;
     const int nTiles = (n2 + kTcRows - 1) / kTcRows;
     const int nP = *a.nEvalP;
     const int nWork = ((nP + G - 1) / G) * nTiles;
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(kTcThreads) k_phase_tc(PhaseTcArgs a) {
             const int s = c / I, j = c - s * I;
             const bool valid = s < nSlots;
             colPtr[c] = valid ? a.phi + ((size_t)a.evalP[grp * G + s] * I + j) * n2 : nullptr;
-            colCh[c] = valid ? a.imgCh[j] : -1;
+            colCh[c] = valid ? a.imgCh[(size_t)a.evalP[grp * G + s] * I + j] : -1;
         }
         cp_async_wait_all();
         __syncthreads();
@@ -143,12 +146,12 @@ __global__ void __launch_bounds__(kTcThreads) k_phase_tc(PhaseTcArgs a) {
             const int s = c / I;
             const float* src = sAl + s * IM + (c - s * I) * M;
             const bool valid = s < nSlots;
-            const int kOne = valid ? M + colCh[c] : -1;
+            const int kOne = valid ? colCh[c] : -1;
             float x[8];
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
                 const int k = k0 + e;
-                x[e] = (valid && k < M) ? src[k] : (k == kOne ? 1.f : 0.f);
+                x[e] = (valid && k >= C && k < C + M) ? src[k - C] : (k == kOne ? 1.f : 0.f);
             }
             split_store8(x, parts, sB + tc::kmajor_off(c, k0, NT), (size_t)bPart);
         }

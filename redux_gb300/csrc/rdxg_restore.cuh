@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(THREADS) k_restore(KParams<T> kp, RestoreArgs 
     int* mask = reinterpret_cast<int*>(tmp + N2);
     __shared__ double noiseVar;
     __shared__ int changed;
-    const int first = kp.objFirst[o], cnt = kp.objCount[o];
+    const int first = kp.pObjFirst[(size_t)p * kp.nObj + o], cnt = kp.pObjCount[(size_t)p * kp.nObj + o];
     const size_t g0 = (size_t)p * kp.I + first;
     // sum_j conj(D_j) S_j and sum_j |S_j|^2 on the support, images in order; conjugate;
     // Array::safeDivide (eps = 0)
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(THREADS) k_restore_objft(KParams<T> kp, Restor
                                     [&](int y, int x, cx<double> v) { F[y * N + x] = v; }, W, s, tw);
         if (!(oa.flags & kRestorePsfAvg)) continue;
         const int p = b / kp.nObj, o = b % kp.nObj;
-        const int first = kp.objFirst[o], cnt = kp.objCount[o];
+        const int first = kp.pObjFirst[b], cnt = kp.pObjCount[b];
         for (int c = threadIdx.x; c < N2; c += THREADS) acc[c] = 0.0;
         for (int j = 0; j < cnt; ++j) {
             const cx<T>* S = kp.S + ((size_t)p * kp.I + first + j) * N2;
@@ -285,7 +285,8 @@ __global__ void __launch_bounds__(THREADS) k_restore_images(KParams<T> kp, Resto
     const int ps = kp.ps, off = (N - ps) / 2;
     auto trimmed = [&](int y, int x) { return y >= off && y < off + ps && x >= off && x < off + ps; };
     for (int g = blockIdx.x; g < kp.P * kp.I; g += gridDim.x) {
-        const int p = g / kp.I, j = g % kp.I, o = kp.imgObj[j];
+        const int p = g / kp.I, j = g % kp.I, o = kp.pImgObj[g];
+        if (j >= kp.pgeo[p].nImg) continue;   // an image slot the patch does not use
         const cx<T>* S = kp.S + (size_t)g * N2;
         auto otfU = [&](int y, int x) {   // the OTF with the zero frequency at (0, 0)
             const cx<T> v = S[((y + N / 2) % N) * N + (x + N / 2) % N];

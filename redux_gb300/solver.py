@@ -129,6 +129,29 @@ class Solver:
                                                         _lib.ptr(fg)), "rdxg_set_patches_device")
         self.P = n_patches
 
+    def set_patch_shapes(self, shapes, patch_shape) -> None:
+        """Ragged batch (rdxg_set_patch_shapes): shapes = [(frames, n_modes, nullspace)] with
+        each geometry's null space (jobsetup.NullSpace, rows image * n_modes + mode over its
+        own images), patch_shape[p] the index of patch p's shape; the next set_patches loads
+        len(patch_shape) patches, each with its images in the first slots.  Empty shapes:
+        uniform batches again."""
+        L = _lib.load()
+        if not shapes:
+            self._check(L.rdxg_set_patch_shapes(self.h, 0, None, 0, None), "rdxg_set_patch_shapes")
+            return
+        keep = []
+        arr = (_lib.PatchShape * len(shapes))()
+        for k, (frames, n_modes, ns) in enumerate(shapes):
+            rows = np.ascontiguousarray(ns.rows, np.int32)
+            cols = np.ascontiguousarray(ns.cols, np.int32)
+            vals = np.ascontiguousarray(ns.vals, np.float64)
+            keep += [rows, cols, vals]
+            arr[k] = _lib.PatchShape(int(frames), int(n_modes), int(ns.n_free), int(vals.size), _lib.ptr(rows),
+                                     _lib.ptr(cols), _lib.ptr(vals))
+        ps = np.ascontiguousarray(patch_shape, np.int32)
+        self._check(L.rdxg_set_patch_shapes(self.h, len(shapes), arr, int(ps.size), _lib.ptr(ps)),
+                    "rdxg_set_patch_shapes")
+
     def set_reg_alpha(self, weights=None) -> None:
         """REG_ALPHA: weights [I][M] of 0.5 sum alpha^2 w added to the metric (None: off);
         jobsetup.reg_alpha_weights gives the reference's."""
