@@ -162,74 +162,107 @@ def run_reference(args, rank):
 
 
 def run_uneven(args):
-    """The uneven batch: patches of sizes {64, 88, 128}, 8-24 frames per
-    channel and 36-60 KL modes, staged modes and per-patch convergence (FTOL 1e-6), one
-    handle per geometry and every handle's rounds in one CUDA graph (rdxg_solve_many), against
-    per-patch launches (each patch its own handle, solved one after the other).  Not the
-    headline line: `python bench.py --workload uneven`."""
+    """The uneven batch: patches of sizes {64, 88, 128}, 8-24 frames per channel and 36-60 KL
+    modes drawn uniformly per patch (the first M modes of one expansion), staged modes and
+    per-patch convergence (FTOL 1e-6).  One ragged handle per OTF size holds every patch of
+    that size, each with its own frames, modes and constraints (rdxg_set_patch_shapes); the
+    three handles' rounds run in one CUDA graph launch (rdxg_solve_many).  Against per-patch
+    launches (each patch in a handle of its own geometry, solved one after the other) on a
+    sample, whose results must be the same bits.  Not the headline line:
+    `python bench.py --workload uneven` (`--levels 3` draws from three levels instead)."""
     import torch
     from redux_gb300 import solver as S, synth
     torch.cuda.set_device(0)
     n = args.patches if args.patches != 225 else 400
     t0 = time.perf_counter()
     ws = synth.uneven_batch(n, levels=args.levels or None)
+    # one handle per OTF size: the largest frames and modes drawn for it, a shape per geometry
+    by_size = {}
+    for w in ws:
+        N = w.job.otf_size
+        by_size.setdefault(N, []).append(w)
+    groups = []
+    for N, wl in sorted(by_size.items()):
+        F_max = max(int(w.job.img_wavefront.max()) + 1 for w in wl)
+        M_max = max(w.job.n_modes for w in wl)
+        big = synth.make_job(N, M_max, synth.LAYOUT_WB_NB(F_max), basis="kl", kl_last=synth.UNEVEN_KL_LAST)
+        shapes, assign, cuts, members = [], [], [], []
+        for k, w in enumerate(wl):
+            F = int(w.job.img_wavefront.max()) + 1
+            shapes.append((F, w.job.n_modes, w.job.nullspace))
+            for i in range(w.patches.cutouts.shape[0]):
+                c = np.zeros((big.n_images, big.cutout_size, big.cutout_size), np.float32)
+                c[:w.job.n_images] = w.patches.cutouts[i]
+                cuts.append(c)
+                assign.append(k)
+                members.append((w, i))
+        groups.append(dict(N=N, big=big, shapes=shapes, assign=assign, cut=np.stack(cuts), members=members))
     t_gen = time.perf_counter() - t0
     st = S.SolveSettings(mode_start=5, mode_step=5, max_iterations=args.iterations if args.iterations != 100 else 30,
                          min_iterations=5, ftol=1e-6, max_metrics=4096)
     hs = []
-    for w in ws:
-        h = S.Solver(w.job, max_patches=w.patches.cutouts.shape[0])
-        h.set_patches(w.patches.cutouts)
+    for g in groups:
+        h = S.Solver(g["big"], max_patches=len(g["assign"]))
+        h.set_patch_shapes(g["shapes"], g["assign"])
+        h.set_patches(g["cut"])
         hs.append(h)
     for _ in range(args.warmup):
         S.solve_many(hs, st)
     torch.cuda.synchronize()
-    times, iters, evals = [], [], []
+    times = []
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
-            for h, w in zip(hs, ws):
-                h.set_patches(w.patches.cutouts)
+            for h, g in zip(hs, groups):
+                h.set_patches(g["cut"])
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             outs = S.solve_many(hs, st)
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t0)
+    iters, evals = [], []
     for out in outs:
         iters += [r.iterations for r in out["reports"]]
         evals += [r.n_f_evals + r.n_df_evals for r in out["reports"]]
     t_many = statistics.median(times)
     launches = sum(h.launch_count() for h in hs)
-    # per-patch launches on one patch of each of 8 geometries spread over the sizes
-    sample = ws[::max(1, len(ws) // 8)][:8]
-    t_single, n_single = 0.0, 0
-    for w in sample:
-        h1 = S.Solver(w.job, max_patches=1)
-        for rep in range(2):     # the first solve of a handle builds its graph: time the second
-            h1.set_patches(w.patches.cutouts[:1])
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            h1.run(st)
-            torch.cuda.synchronize()
-            if rep:
-                t_single += time.perf_counter() - t0
-        n_single += 1
-        h1.close()
-    # the same patches inside the batch: their share of the batch time
+    # per-patch launches on a sample (3 patches of each size), each its own geometry's handle;
+    # their results against the batch's
+    t_single, n_single, identical = 0.0, 0, True
+    for g, out in zip(groups, outs):
+        for pi in range(min(3, len(g["members"]))):
+            w, i = g["members"][pi]
+            h1 = S.Solver(w.job, max_patches=1)
+            for rep in range(2):     # the first solve of a handle plans its launch shapes: time the second
+                h1.set_patches(w.patches.cutouts[i:i + 1])
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                o1 = h1.run(st)
+                torch.cuda.synchronize()
+                if rep:
+                    t_single += time.perf_counter() - t0
+            I, M = w.job.n_images, w.job.n_modes
+            identical &= bool(np.array_equal(out["alpha"][pi][:I, :M], o1["alpha"][0]))
+            r, r1 = out["reports"][pi], o1["reports"][0]
+            identical &= bool(np.array_equal(out["metrics"][pi, :r.n_metrics], o1["metrics"][0, :r1.n_metrics]))
+            n_single += 1
+            h1.close()
     line = {"metric": "uneven-batch converged patches/s", "value": n / t_many, "unit": UNIT,
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_many * 1000.0,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (FP64 sums and CG scalars)", "data": "synthetic",
             "config": {"workload": f"{n} patches, sizes {{64, 88, 128}}, frames 8-24, 36-60 KL modes"
-                                   + (f" ({args.levels} levels)" if args.levels else "")
+                                   + (f" ({args.levels} levels)" if args.levels else " (uniform draws)")
                                    + ", staged modes, FTOL 1e-6, at most "
                                    + f"{st.max_iterations} iterations per stage",
-                       "geometries": len(ws), "iterations_median": float(np.median(iters)),
+                       "geometries": len(ws), "handles": len(hs),
+                       "patches_per_handle": {g["N"]: len(g["assign"]) for g in groups},
+                       "iterations_median": float(np.median(iters)),
                        "evaluations_per_patch": float(np.mean(evals)), "generation_s": t_gen},
             "gpu_launches": int(launches),
-            "launch_shapes": {w.name: h.launch_shape() for w, h in zip(ws, hs)},
+            "launch_shapes": {g["N"]: h.launch_shape() for g, h in zip(groups, hs)},
             "per_patch_launches": {"value": n_single / t_single, "unit": UNIT,
-                                   "sample": f"{n_single} patches, one per geometry, each its own handle: "
-                                             + ", ".join(w.name for w in sample)},
+                                   "sample": f"{n_single} patches (3 per size), each in a handle of its own geometry",
+                                   "results_identical_to_batch": identical},
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     for h in hs:
@@ -620,7 +653,7 @@ def main():
                     help="convergence: restart cycles (continuations from the own endpoint) at most")
     ap.add_argument("--conv-restart-tol", type=float, default=1e-6,
                     help="convergence: stop restarting once no patch's metric drops by more than this")
-    ap.add_argument("--levels", type=int, default=3,
+    ap.add_argument("--levels", type=int, default=0,
                     help="uneven batch: frames and modes from this many values (0: uniform draws)")
     ap.add_argument("--large-fp64-patches", type=int, default=4,
                     help="large patches: patches solved by the plain FP64 GPU form and compared with it")
