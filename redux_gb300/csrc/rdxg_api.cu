@@ -953,6 +953,16 @@ int host_lists(rdxg_solver* h, int req, int mode) {
     return RDXG_OK;
 }
 
+// Single evaluations (metric, gradient, restoration) on the fused path start from a zero
+// reference object, so that their result depends on the point and the loaded patches only,
+// not on what an earlier call left behind (the evaluation is exact for any reference object,
+// but its rounding is not).
+int reset_reference(rdxg_solver* h) {
+    if (h->fused)
+        CK(h, cudaMemsetAsync(h->dOh, 0, (size_t)h->P * h->nObj * h->nH * sizeof(float2), h->stream));
+    return RDXG_OK;
+}
+
 int fused_pass(rdxg_solver* h, int req, int mode) {
     int r;
     if ((r = host_lists(h, req, mode))) return r;
@@ -1328,7 +1338,7 @@ int rdxg_metric(rdxg_solver* h, const double* alpha, double* metric) {
     if (!h->loaded) { h->err = "no patches loaded"; return RDXG_ERR_STATE; }
     int r = h->fp64 ? upload_alpha<double>(h, alpha) : upload_alpha<float>(h, alpha);
     if (r) return r;
-    if ((r = set_requests(h, REQ_F, GM_VOGEL, h->M))) return r;
+    if ((r = set_requests(h, REQ_F, GM_VOGEL, h->M)) || (r = reset_reference(h))) return r;
     if (h->fused) {
         // a first pass sets the reference object to this point, the second evaluates
         if ((r = fused_pass(h, REQ_F, 2))) return r;
@@ -1440,7 +1450,7 @@ int rdxg_metric_with_reference(rdxg_solver* h, const double* alpha_ref, const do
     if (!h->fused) return rdxg_metric(h, alpha, metric);
     int r;
     if ((r = upload_alpha<float>(h, alpha_ref)) || (r = set_requests(h, REQ_F, GM_VOGEL, h->M)) ||
-        (r = fused_pass(h, REQ_F, 2)))
+        (r = reset_reference(h)) || (r = fused_pass(h, REQ_F, 2)))
         return r;
     if ((r = upload_alpha<float>(h, alpha)) || (r = fused_pass(h, REQ_F, 0))) return r;
     if ((r = metric_from_objects(h, metric))) return r;
@@ -1495,7 +1505,7 @@ int restore_impl(rdxg_solver* h, const double* alpha, const double* frequency_cu
     int r = h->fp64 ? upload_alpha<double>(h, alpha) : upload_alpha<float>(h, alpha);
     if (r) return r;
     // the OTFs at alpha on the full plane: a gradient-type evaluation keeps them
-    if ((r = set_requests(h, REQ_DF, GM_VOGEL, h->M))) return r;
+    if ((r = set_requests(h, REQ_DF, GM_VOGEL, h->M)) || (r = reset_reference(h))) return r;
     if (h->fused) {
         if ((r = fused_pass(h, REQ_DF, 1))) return r;
     } else {
@@ -1560,7 +1570,7 @@ int rdxg_gradient(rdxg_solver* h, const double* alpha, const uint8_t* enabled, i
     int r = h->fp64 ? upload_alpha<double>(h, alpha) : upload_alpha<float>(h, alpha);
     if (r) return r;
     const int gm = method == RDXG_GRAD_FD ? GM_FD : GM_VOGEL;
-    if ((r = set_requests(h, REQ_DF, gm, h->M))) return r;
+    if ((r = set_requests(h, REQ_DF, gm, h->M)) || (r = reset_reference(h))) return r;
     if (h->fused) {
         if ((r = fused_pass(h, REQ_DF, 1))) return r;
     }
