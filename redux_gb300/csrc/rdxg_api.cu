@@ -790,7 +790,10 @@ int metric_from_partials(rdxg_solver* h, double* metric) {
 
 int set_requests(rdxg_solver* h, int req, int gm, int mc) {
     std::vector<int32_t> a(h->P, req), b(h->P, gm), c(h->P, mc), all(h->P);
-    for (int p = 0; p < h->P; ++p) all[p] = p;
+    for (int p = 0; p < h->P; ++p) {
+        all[p] = p;
+        c[p] = std::min(mc, h->shapes[h->patchShape[p]].M);   // a ragged batch: the patch's own modes
+    }
     int32_t cnt[2] = {0, 0};
     if (req == REQ_DF) { if (gm == GM_FD) cnt[1] = h->P; else cnt[0] = h->P; }
     CK(h, cudaMemcpyAsync(h->dGradP, all.data(), h->P * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
