@@ -103,5 +103,7 @@ def test_ragged_rejections():
     with pytest.raises(S.SolverError, match="REG_ALPHA"):
         s.set_reg_alpha(np.ones((big.n_images, big.n_modes)))
     s.set_patch_shapes([], [])                                            # uniform again
-    s.set_patches(packed[:3])
+    with pytest.raises(S.SolverError, match="non-finite regularisation"):
+        s.set_patches(packed[:3])         # the unused slots are now images: blank ones
+    s.set_patches(synth.make_patches(big, 3, 12.0, np.random.default_rng(3)).cutouts)
     s.close()
