@@ -2125,10 +2125,16 @@ int plan_shapes(rdxg_solver* h, int reps, double* ms) {
     int r = RDXG_OK;
     for (int f = 0; f < 3 && !r; ++f) {
         if (!used[f]) { *field[f] = 0; continue; }
-        for (int v = 0; v < 2 && !r; ++v) {
-            if (threads_of(h, f, v) == 0) { t[2 * f + v] = 0; continue; }   // not available here
-            *field[f] = v;
-            r = time_kernel(h, which[f], reps, e0, e1, &t[2 * f + v], nGrad[f]);
+        // each candidate timed three times, alternating, the fastest of each kept (a single
+        // measurement of these sub-millisecond launches is at the mercy of the clock ramp)
+        for (int rep = 0; rep < 3 && !r; ++rep) {
+            for (int v = 0; v < 2 && !r; ++v) {
+                if (threads_of(h, f, v) == 0) { t[2 * f + v] = 0; continue; }   // not available here
+                *field[f] = v;
+                double ms = 0;
+                r = time_kernel(h, which[f], reps, e0, e1, &ms, nGrad[f]);
+                if (rep == 0 || ms < t[2 * f + v]) t[2 * f + v] = ms;
+            }
         }
         *field[f] = (threads_of(h, f, 1) != 0 && t[2 * f + 1] < t[2 * f]) ? 1 : 0;
     }
