@@ -311,6 +311,13 @@ typedef struct {
     int32_t eval_threads;
     int32_t forward_threads;
     int32_t adjoint_threads;
+    /* radix plans of the same kernels' transforms: the first radix of the two-stage plan
+     * (32: 8 or 4, 64: 8 or 16, 88: 8, 128: 16 or 8).  Unlike the block size, a plan changes
+     * the rounding of the transforms (not their result beyond it); the planner fixes it once
+     * per device, size and path in a process, so that every handle of a size uses the same. */
+    int32_t eval_radix;
+    int32_t forward_radix;
+    int32_t adjoint_radix;
 } rdxg_launch_shape;
 
 /* The launch-shape planner, in place of the FFTW_MEASURE planning of the reference's

@@ -2100,9 +2100,38 @@ std::map<ShapeKey, ShapeChoice>& wisdom() {
 }
 ShapeKey shape_key(const rdxg_solver* h) { return ShapeKey{h->geo.device, h->N, h->fused ? 1 : 0, h->M, h->I, h->P}; }
 
-// Measures both shapes of every tuned kernel of the handle's path and keeps the faster.
-// ms (or null): [6] eval (default, alternative), forward (...), adjoint (...); 0 where a
-// kernel is not tuned on this path.
+// The radix plans of the FFTs: R1 of plan 0 (Plan<N>) and plan 1 (PlanAlt<N>, 0 where N has none).
+int radix_of(int N, int plan) {
+    switch (N) {
+        case 32: return plan ? PlanAlt<32>::R1 : Plan<32>::R1;
+        case 64: return plan ? PlanAlt<64>::R1 : Plan<64>::R1;
+        case 88: return plan ? 0 : Plan<88>::R1;
+        case 128: return plan ? PlanAlt<128>::R1 : Plan<128>::R1;
+        default: return 0;
+    }
+}
+
+// The radix plan is chosen once per device, size and path in a process (the first handle
+// measures it, every later one takes it), so that handles of one size -- a patch alone, in a
+// batch, in a ragged batch -- give the same bits; the block sizes, which change no result, are
+// chosen per geometry and batch size.
+struct PlanKey {
+    int device, N, fused;
+    bool operator<(const PlanKey& o) const {
+        const int a[3] = {device, N, fused}, b[3] = {o.device, o.N, o.fused};
+        return std::lexicographical_compare(a, a + 3, b, b + 3);
+    }
+};
+std::map<PlanKey, ShapeChoice>& plan_wisdom() {
+    static std::map<PlanKey, ShapeChoice> w;
+    return w;
+}
+PlanKey plan_key(const rdxg_solver* h) { return PlanKey{h->geo.device, h->N, h->fused ? 1 : 0}; }
+
+// Measures the variants of every tuned kernel of the handle's path -- block size (bit 0 of
+// the variant) and radix plan (bit 1), the plan only where none is fixed for this size yet --
+// and keeps the fastest.  ms (or null): [6] eval (default, alternative block size),
+// forward (...), adjoint (...) with the plan kept; 0 where a kernel is not tuned on this path.
 int threads_of(const rdxg_solver* h, int family, int variant);
 
 int plan_shapes(rdxg_solver* h, int reps, double* ms) {
@@ -2111,6 +2140,14 @@ int plan_shapes(rdxg_solver* h, int reps, double* ms) {
         h->shapeEval = h->shapeFwd = h->shapeAdj = 0;
         if (ms) std::memcpy(ms, t, sizeof(t));
         return RDXG_OK;
+    }
+    int fixedPlan[3] = {-1, -1, -1};
+    {
+        std::lock_guard<std::mutex> lock(wisdom_mutex());
+        auto it = plan_wisdom().find(plan_key(h));
+        if (it != plan_wisdom().end()) {
+            fixedPlan[0] = it->second.eval >> 1; fixedPlan[1] = it->second.fwd >> 1; fixedPlan[2] = it->second.adj >> 1;
+        }
     }
     CK(h, cudaMemsetAsync(h->dAlphaEff, 0, (size_t)h->P * h->I * h->M * sizeof(float), h->stream));
     cudaEvent_t e0, e1;
@@ -2122,21 +2159,35 @@ int plan_shapes(rdxg_solver* h, int reps, double* ms) {
     // a solve round evaluates every active patch but takes the gradients of about one in ten
     // (the others are in their line searches): the adjoint is timed on such a list
     const int nGrad[3] = {0, 0, std::max(1, (h->P + 9) / 10)};
+    const bool altPlan = radix_of(h->N, 1) != 0;
     int r = RDXG_OK;
     for (int f = 0; f < 3 && !r; ++f) {
         if (!used[f]) { *field[f] = 0; continue; }
+        double tv[4] = {0, 0, 0, 0};
+        bool avail[4];
+        for (int v = 0; v < 4; ++v) {
+            const int plan = v >> 1;
+            avail[v] = threads_of(h, f, v & 1) != 0 && (plan == 0 || altPlan) &&
+                       (fixedPlan[f] < 0 || plan == fixedPlan[f]);
+        }
         // each candidate timed three times, alternating, the fastest of each kept (a single
         // measurement of these sub-millisecond launches is at the mercy of the clock ramp)
         for (int rep = 0; rep < 3 && !r; ++rep) {
-            for (int v = 0; v < 2 && !r; ++v) {
-                if (threads_of(h, f, v) == 0) { t[2 * f + v] = 0; continue; }   // not available here
+            for (int v = 0; v < 4 && !r; ++v) {
+                if (!avail[v]) continue;
                 *field[f] = v;
-                double ms = 0;
-                r = time_kernel(h, which[f], reps, e0, e1, &ms, nGrad[f]);
-                if (rep == 0 || ms < t[2 * f + v]) t[2 * f + v] = ms;
+                double ms1 = 0;
+                r = time_kernel(h, which[f], reps, e0, e1, &ms1, nGrad[f]);
+                if (rep == 0 || ms1 < tv[v]) tv[v] = ms1;
             }
         }
-        *field[f] = (threads_of(h, f, 1) != 0 && t[2 * f + 1] < t[2 * f]) ? 1 : 0;
+        int best = -1;
+        for (int v = 0; v < 4; ++v)
+            if (avail[v] && (best < 0 || tv[v] < tv[best])) best = v;
+        *field[f] = best < 0 ? 0 : best;
+        const int plan = *field[f] >> 1;
+        t[2 * f] = tv[2 * plan];
+        t[2 * f + 1] = avail[2 * plan + 1] ? tv[2 * plan + 1] : 0.0;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -2145,6 +2196,7 @@ int plan_shapes(rdxg_solver* h, int reps, double* ms) {
     {
         std::lock_guard<std::mutex> lock(wisdom_mutex());
         wisdom()[shape_key(h)] = ShapeChoice{h->shapeEval, h->shapeFwd, h->shapeAdj};
+        plan_wisdom().emplace(plan_key(h), ShapeChoice{h->shapeEval, h->shapeFwd, h->shapeAdj});
     }
     if (getenv("RDXG_VERBOSE"))
         fprintf(stderr, "launch shapes (N %d, P %d): eval %d [%.3f %.3f ms], forward %d [%.3f %.3f], adjoint %d "
@@ -2168,11 +2220,14 @@ int plan_shapes_once(rdxg_solver* h) {
     return plan_shapes(h, 3, nullptr);
 }
 
+// threads per block of a variant (bit 0: the alternative block size), 0 where the kernel is
+// not used on the handle's path
 int threads_of(const rdxg_solver* h, int family, int variant) {
-    if (family == 0) return h->fused ? (variant ? kEvalThreadsAlt : kEvalThreads) : 0;
+    const int alt = variant & 1;
+    if (family == 0) return h->fused ? (alt ? kEvalThreadsAlt : kEvalThreads) : 0;
     if (family == 1 && h->fused) return 0;
     const int base = h->N >= 128 ? 512 : 256;
-    return (variant && !h->fp64) ? 2 * base : base;
+    return (alt && !h->fp64) ? 2 * base : base;
 }
 
 }  // namespace
@@ -2205,19 +2260,32 @@ int rdxg_set_launch_shape(rdxg_solver* h, const rdxg_launch_shape* shape) {
     if (!h || !shape) return RDXG_ERR_ARG;
     int v[3] = {h->shapeEval, h->shapeFwd, h->shapeAdj};
     const int32_t want[3] = {shape->eval_threads, shape->forward_threads, shape->adjoint_threads};
+    const int32_t wantRadix[3] = {shape->eval_radix, shape->forward_radix, shape->adjoint_radix};
     for (int f = 0; f < 3; ++f) {
-        if (want[f] == 0) continue;
+        if (want[f] == 0 && wantRadix[f] == 0) continue;
         if (threads_of(h, f, 0) == 0) {
             h->err = std::string(f == 0 ? "k_eval" : "k_forward") + " is not used on this handle's path";
             return RDXG_ERR_ARG;
         }
-        if (want[f] == threads_of(h, f, 0)) v[f] = 0;
-        else if (want[f] == threads_of(h, f, 1)) v[f] = 1;
-        else {
-            h->err = "launch shape " + std::to_string(want[f]) + " is not compiled for this kernel (" +
-                     std::to_string(threads_of(h, f, 0)) + " or " + std::to_string(threads_of(h, f, 1)) + ")";
-            return RDXG_ERR_ARG;
+        int tv = v[f] & 1, pv = v[f] >> 1;
+        if (want[f] != 0) {
+            if (want[f] == threads_of(h, f, 0)) tv = 0;
+            else if (want[f] == threads_of(h, f, 1)) tv = 1;
+            else {
+                h->err = "launch shape " + std::to_string(want[f]) + " is not compiled for this kernel (" +
+                         std::to_string(threads_of(h, f, 0)) + " or " + std::to_string(threads_of(h, f, 1)) + ")";
+                return RDXG_ERR_ARG;
+            }
         }
+        if (wantRadix[f] != 0) {
+            if (wantRadix[f] == radix_of(h->N, 0)) pv = 0;
+            else if (!h->fp64 && wantRadix[f] == radix_of(h->N, 1)) pv = 1;
+            else {
+                h->err = "radix " + std::to_string(wantRadix[f]) + " is not a plan of size " + std::to_string(h->N);
+                return RDXG_ERR_ARG;
+            }
+        }
+        v[f] = tv | (pv << 1);
     }
     h->shapeEval = v[0]; h->shapeFwd = v[1]; h->shapeAdj = v[2];
     h->tune = 0;
@@ -2229,6 +2297,9 @@ int rdxg_get_launch_shape(const rdxg_solver* h, rdxg_launch_shape* shape) {
     shape->eval_threads = threads_of(h, 0, h->shapeEval);
     shape->forward_threads = threads_of(h, 1, h->shapeFwd);
     shape->adjoint_threads = threads_of(h, 2, h->shapeAdj);
+    shape->eval_radix = shape->eval_threads ? radix_of(h->N, h->shapeEval >> 1) : 0;
+    shape->forward_radix = shape->forward_threads ? radix_of(h->N, h->shapeFwd >> 1) : 0;
+    shape->adjoint_radix = radix_of(h->N, h->shapeAdj >> 1);
     return RDXG_OK;
 }
 

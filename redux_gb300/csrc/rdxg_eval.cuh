@@ -267,12 +267,12 @@ __device__ __forceinline__ void stage_phi(T* buf, const T* __restrict__ phi_g) {
 // times the inverse transform in those columns.  afterRows, afterCols1, afterPack run after
 // the row pass, the first column stage and the packing stage (where the caller issues copies
 // into the free parts of the tiles); midColumns runs between the two stages along y.
-template <typename T, int N, int THREADS, typename Pupil, typename Elem, typename HR, typename HC, typename HP,
-          typename HM>
+template <typename T, int N, int THREADS, typename PL = Plan<N>, typename Pupil, typename Elem, typename HR,
+          typename HC, typename HP, typename HM>
 __device__ __forceinline__ void half_plane_core(cx<T>* a, cx<T>* b, const cx<T>* tw, Pupil pupil, Elem elem,
                                                 HR afterRows, HC afterCols1, HP afterPack, HM midColumns) {
     constexpr int LDS = Tile<N>::LDS;
-    constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
+    constexpr int R1 = PL::R1, R2 = PL::R2;
     constexpr int LO = R1 / 4, HI = 3 * R1 / 4;      // non-zero inputs of the pruned first stage
     static_assert(R1 % 4 == 0, "the pruned first stage needs a radix divisible by 4");
     T* af = reinterpret_cast<T*>(a);
@@ -346,7 +346,7 @@ __device__ __forceinline__ void acc_point(Acc4<T>& u, cx<T> d, cx<T> o, cx<T> s,
 // One image of a chunk: the OTF on the half plane (half_plane_core with elem = |X|^2),
 // folded into the chunk's accumulators.  On entry the phases of this image are in phiBuf;
 // phiNext (or null) is the next image's, fetched into phiBuf once the row pass has read it.
-template <typename T, int N, int THREADS>
+template <typename T, int N, int THREADS, typename PL = Plan<N>>
 __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phiBuf, const T* A, T c, int keepPX,
                                            int keepS,
                                            cx<T>* PF, cx<T>* X, cx<T>* S, const cx<T>* __restrict__ Dg,
@@ -358,7 +358,7 @@ __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phi
     const T inv = (T)1 / (T)N2;
     __syncthreads();    // previous image's tiles fully consumed, staged phases visible
     const int nFirst = nH < St::kPart ? nH : St::kPart;
-    half_plane_core<T, N, THREADS>(
+    half_plane_core<T, N, THREADS, PL>(
         a, b, tw,
         [&](int y, int x) {
             const int q = y * n + x;
@@ -403,7 +403,7 @@ __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phi
 }
 
 // ----------------------------------------------------------------------------------
-template <typename T, int N, int THREADS, int NPT>
+template <typename T, int N, int THREADS, int NPT, typename PL = Plan<N>>
 __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
     constexpr int n = N / 2, n2 = n * n, N2 = N * N;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
         const int ch = e.k.pImgCh[g];
         // a gradient evaluation keeps PF, X and the full OTF for the gradient kernels, unless
         // they recompute them (the OTF is still kept when a buffer for it is given)
-        eval_image<T, N, THREADS>(phiNext, phiBuf, amp, e.k.otfNorm[ch], it.df && !e.k.recompute,
+        eval_image<T, N, THREADS, PL>(phiNext, phiBuf, amp, e.k.otfNorm[ch], it.df && !e.k.recompute,
                                   it.df && e.k.S != nullptr, e.k.PF + g * n2, e.k.X + g * N2,
                                   e.k.S + g * N2, e.Dh + g * nH, s, s2, tw, oh, acc, hpos, e.hp.idx, nH);
         if (nextJj == 0) {

@@ -167,6 +167,18 @@ template <> struct Plan<64> { static constexpr int R1 = 8, R2 = 8; };
 template <> struct Plan<88> { static constexpr int R1 = 8, R2 = 11; };
 template <> struct Plan<128> { static constexpr int R1 = 16, R2 = 8; };
 
+// The launch-shape planner's second radix plan of each size (the first is Plan<N>): the same
+// transform with the stages in the other order (or another split), which rounds differently
+// and runs at a different speed.  N = 88 has none (8 * 11 is the only two-stage plan whose
+// first radix is a multiple of 4, which the pruned half-plane transforms need).
+template <int N> struct PlanAlt : Plan<N> { static constexpr bool exists = false; };
+template <> struct PlanAlt<32> { static constexpr int R1 = 4, R2 = 8; static constexpr bool exists = true; };
+template <> struct PlanAlt<64> { static constexpr int R1 = 16, R2 = 4; static constexpr bool exists = true; };
+template <> struct PlanAlt<128> { static constexpr int R1 = 8, R2 = 16; static constexpr bool exists = true; };
+// plan 0: Plan<N>, plan 1: PlanAlt<N>
+template <int N, int V> struct PlanOf { using type = Plan<N>; };
+template <int N> struct PlanOf<N, 1> { using type = PlanAlt<N>; };
+
 template <int N> struct Tile { static constexpr int LDS = N + 1; static constexpr int ELEMS = N * (N + 1); };
 
 // One Stockham stage over LINES lines starting at line0.  Element e of line l is at
@@ -227,10 +239,10 @@ __device__ __forceinline__ void fft_stage(cx<T>* s, int line0, int lstride, int 
 }
 
 // 1-D transforms of LINES lines (rows when ROWS, else columns).
-template <typename T, int N, int DIR, int LINES, bool ROWS, int THREADS>
+template <typename T, int N, int DIR, int LINES, bool ROWS, int THREADS, typename PL = Plan<N>>
 __device__ __forceinline__ void fft_lines(cx<T>* s, int line0, const cx<T>* tw, int tid) {
     constexpr int LDS = Tile<N>::LDS;
-    constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
+    constexpr int R1 = PL::R1, R2 = PL::R2;
     constexpr int ls = ROWS ? LDS : 1;
     constexpr int es = ROWS ? 1 : LDS;
     fft_stage<T, N, R1, 1, DIR, LINES, THREADS>(s, line0, ls, es, tw, tid);
@@ -239,18 +251,18 @@ __device__ __forceinline__ void fft_lines(cx<T>* s, int line0, const cx<T>* tw, 
 
 // Full 2-D transform.  IN_ROWS_PRUNED: only rows [N/4, 3N/4) of the input are non-zero
 // (an n x n pupil embedded at offset n/2), so only those rows are transformed first.
-template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED>
+template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED, typename PL = Plan<N>>
 __device__ __forceinline__ void fft2d(cx<T>* s, const cx<T>* tw, int tid) {
     if (IN_ROWS_PRUNED) {
-        fft_lines<T, N, DIR, N / 2, true, THREADS>(s, N / 4, tw, tid);
+        fft_lines<T, N, DIR, N / 2, true, THREADS, PL>(s, N / 4, tw, tid);
     } else {
-        fft_lines<T, N, DIR, N, true, THREADS>(s, 0, tw, tid);
+        fft_lines<T, N, DIR, N, true, THREADS, PL>(s, 0, tw, tid);
     }
-    fft_lines<T, N, DIR, N, false, THREADS>(s, 0, tw, tid);
+    fft_lines<T, N, DIR, N, false, THREADS, PL>(s, 0, tw, tid);
 }
-template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED>
+template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED, typename PL = Plan<N>>
 __device__ __forceinline__ void fft2d(cx<T>* s, const cx<T>* tw) {
-    fft2d<T, N, DIR, THREADS, IN_ROWS_PRUNED>(s, tw, (int)threadIdx.x);
+    fft2d<T, N, DIR, THREADS, IN_ROWS_PRUNED, PL>(s, tw, (int)threadIdx.x);
 }
 
 // ---- ping-pong variant: out-of-place stages between two tiles (a -> b -> a), one barrier
@@ -325,10 +337,10 @@ __device__ __forceinline__ void fft_stage_fn(int line0, const cx<T>* tw, LD ld, 
 }
 
 // 2-D transform in tile a (result in a), b is scratch of the same shape.
-template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED>
+template <typename T, int N, int DIR, int THREADS, bool IN_ROWS_PRUNED, typename PL = Plan<N>>
 __device__ __forceinline__ void fft2d_pp(cx<T>* a, cx<T>* b, const cx<T>* tw) {
     constexpr int LDS = Tile<N>::LDS;
-    constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
+    constexpr int R1 = PL::R1, R2 = PL::R2;
     constexpr int RL = IN_ROWS_PRUNED ? N / 2 : N;
     constexpr int r0 = IN_ROWS_PRUNED ? N / 4 : 0;
     fft_stage_pp<T, N, R1, 1, DIR, RL, THREADS>(a, b, r0, LDS, 1, tw);
@@ -338,10 +350,10 @@ __device__ __forceinline__ void fft2d_pp(cx<T>* a, cx<T>* b, const cx<T>* tw) {
 }
 
 // ping-pong transform whose output is only needed on rows [N/4, 3N/4): columns first
-template <typename T, int N, int DIR, int THREADS>
+template <typename T, int N, int DIR, int THREADS, typename PL = Plan<N>>
 __device__ __forceinline__ void fft2d_pp_out_rows_pruned(cx<T>* a, cx<T>* b, const cx<T>* tw) {
     constexpr int LDS = Tile<N>::LDS;
-    constexpr int R1 = Plan<N>::R1, R2 = Plan<N>::R2;
+    constexpr int R1 = PL::R1, R2 = PL::R2;
     fft_stage_pp<T, N, R1, 1, DIR, N, THREADS>(a, b, 0, 1, LDS, tw);
     fft_stage_pp<T, N, R2, R1, DIR, N, THREADS>(b, a, 0, 1, LDS, tw);
     fft_stage_pp<T, N, R1, 1, DIR, N / 2, THREADS>(a, b, N / 4, LDS, 1, tw);
@@ -362,14 +374,14 @@ __device__ __forceinline__ void fft2d_any(cx<T>* a, cx<T>* b, const cx<T>* tw) {
 
 // 2-D transform whose output is only needed on rows [N/4, 3N/4): columns first, then the
 // needed rows.
-template <typename T, int N, int DIR, int THREADS>
+template <typename T, int N, int DIR, int THREADS, typename PL = Plan<N>>
 __device__ __forceinline__ void fft2d_out_rows_pruned(cx<T>* s, const cx<T>* tw, int tid) {
-    fft_lines<T, N, DIR, N, false, THREADS>(s, 0, tw, tid);
-    fft_lines<T, N, DIR, N / 2, true, THREADS>(s, N / 4, tw, tid);
+    fft_lines<T, N, DIR, N, false, THREADS, PL>(s, 0, tw, tid);
+    fft_lines<T, N, DIR, N / 2, true, THREADS, PL>(s, N / 4, tw, tid);
 }
-template <typename T, int N, int DIR, int THREADS>
+template <typename T, int N, int DIR, int THREADS, typename PL = Plan<N>>
 __device__ __forceinline__ void fft2d_out_rows_pruned(cx<T>* s, const cx<T>* tw) {
-    fft2d_out_rows_pruned<T, N, DIR, THREADS>(s, tw, (int)threadIdx.x);
+    fft2d_out_rows_pruned<T, N, DIR, THREADS, PL>(s, tw, (int)threadIdx.x);
 }
 
 }  // namespace rdxg

@@ -57,6 +57,13 @@ cudaError_t Launcher<T, N>::setup(int M) {
         if ((e = raise_smem_limit(k_forward<T, N, ALT>, sm))) return e;
         if ((e = raise_smem_limit(k_adjoint<T, N, ALT>, sm))) return e;
         if (arc <= kMaxSmem && (e = raise_smem_limit(k_adjoint_rc<T, N, ALT, false>, arc))) return e;
+        if constexpr (PlanAlt<N>::exists) {
+            using PA = PlanAlt<N>;
+            if ((e = raise_smem_limit(k_forward<T, N, THREADS, PA>, sm))) return e;
+            if ((e = raise_smem_limit(k_adjoint<T, N, THREADS, PA>, sm))) return e;
+            if ((e = raise_smem_limit(k_forward<T, N, ALT, PA>, sm))) return e;
+            if ((e = raise_smem_limit(k_adjoint<T, N, ALT, PA>, sm))) return e;
+        }
     }
     if constexpr (PingPong<T, N>::value) {
         // the fused path recomputes S too
@@ -88,7 +95,13 @@ template <typename T, int N>
 void Launcher<T, N>::forward(const KParams<T>& kp, int nImg, cudaStream_t st) {
     const size_t sm = smem_base() + extra_smem<T, N>(kp.M);
     if constexpr (HasAlt<T>::value) {
+        // the planner's variant: bit 0 the alternative block size, bit 1 the alternative radix plan
         constexpr int ALT = ThreadsAlt<N>::value;
+        if constexpr (PlanAlt<N>::exists) {
+            using PA = PlanAlt<N>;
+            if (kp.shapeFwd == 2) { k_forward<T, N, THREADS, PA><<<nImg, THREADS, sm, st>>>(kp); return; }
+            if (kp.shapeFwd == 3) { k_forward<T, N, ALT, PA><<<nImg, ALT, sm, st>>>(kp); return; }
+        }
         if (kp.shapeFwd == 1) {
             k_forward<T, N, ALT><<<nImg, ALT, sm, st>>>(kp);
             return;
@@ -104,7 +117,7 @@ void Launcher<T, N>::adjoint(const KParams<T>& kp, int grid, int kind, cudaStrea
         // one image per block; S recomputed where it is not kept (the fused path)
         const size_t sm = adjoint_rc_smem<T, N>(kp.M);
         const int g = kp.P * kp.I;
-        const bool alt = HasAlt<T>::value && kp.shapeAdj == 1;
+        const bool alt = HasAlt<T>::value && (kp.shapeAdj & 1);
         if constexpr (PingPong<T, N>::value) {
             if (!kp.S) {
                 if (alt) k_adjoint_rc<T, N, ThreadsAlt<N>::value, true><<<g, ThreadsAlt<N>::value, sm, st>>>(kp, kind);
@@ -125,6 +138,11 @@ void Launcher<T, N>::adjoint(const KParams<T>& kp, int grid, int kind, cudaStrea
     grid = kp.P * kp.I;
     if constexpr (HasAlt<T>::value) {
         constexpr int ALT = ThreadsAlt<N>::value;
+        if constexpr (PlanAlt<N>::exists) {
+            using PA = PlanAlt<N>;
+            if (kp.shapeAdj == 2) { k_adjoint<T, N, THREADS, PA><<<grid, THREADS, sm, st>>>(kp, kind); return; }
+            if (kp.shapeAdj == 3) { k_adjoint<T, N, ALT, PA><<<grid, ALT, sm, st>>>(kp, kind); return; }
+        }
         if (kp.shapeAdj == 1) {
             k_adjoint<T, N, ALT><<<grid, ALT, sm, st>>>(kp, kind);
             return;
@@ -189,6 +207,10 @@ cudaError_t EvalLauncher<T, N>::setup(int M, int npt, int nH) {
 #define RDXG_SET(NPT) e = raise_smem_limit(k_eval<T, N, kEvalThreadsAlt, NPT>, sm)
     if (e == cudaSuccess) RDXG_NPT_SWITCH(npt, RDXG_SET);
 #undef RDXG_SET
+    if constexpr (PlanAlt<N>::exists) {
+        if (e == cudaSuccess) e = raise_smem_limit(k_eval<T, N, kEvalThreads, 1, PlanAlt<N>>, sm);
+        if (e == cudaSuccess) e = raise_smem_limit(k_eval<T, N, kEvalThreadsAlt, 1, PlanAlt<N>>, sm);
+    }
     if (e == cudaSuccess)
         e = raise_smem_limit(k_phase<T, N, kPhasePix, kMaxChunk>, (size_t)M * (kPhasePix + kMaxChunk) * sizeof(T));
     if (e == cudaSuccess && fd_smem(nH) + 1024 <= kMaxSmem)
@@ -211,6 +233,14 @@ int EvalLauncher<T, N>::occupancy(int M, int npt, int nH) {
 template <typename T, int N>
 void EvalLauncher<T, N>::eval(const EvalParams<T>& e, int npt, int grid, cudaStream_t st) {
     const size_t sm = smem(e.k.M, e.hp.nH);
+    // the planner's variant: bit 0 the alternative block size, bit 1 the alternative radix plan
+    if constexpr (PlanAlt<N>::exists) {
+        if (e.k.shapeEval == 2) { k_eval<T, N, kEvalThreads, 1, PlanAlt<N>><<<grid, kEvalThreads, sm, st>>>(e); return; }
+        if (e.k.shapeEval == 3) {
+            k_eval<T, N, kEvalThreadsAlt, 1, PlanAlt<N>><<<grid, kEvalThreadsAlt, sm, st>>>(e);
+            return;
+        }
+    }
     if (e.k.shapeEval == 1) {
 #define RDXG_LAUNCH(NPT) k_eval<T, N, kEvalThreadsAlt, NPT><<<grid, kEvalThreadsAlt, sm, st>>>(e)
         RDXG_NPT_SWITCH(npt, RDXG_LAUNCH);

@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(THREADS) k_prep(KParams<T> kp, int full) {
 // phi = phi_fixed + sum_m alpha_eff[m] Z_m; PF = A exp(i phi);
 // OTF = fftshift(ifft(|fft(c PF embedded at n/2)|^2) / N^2).
 // ----------------------------------------------------------------------------------
-template <typename T, int N, int THREADS>
+template <typename T, int N, int THREADS, typename PL = Plan<N>>
 __global__ void __launch_bounds__(THREADS) k_forward(KParams<T> kp) {
     const int g = blockIdx.x;
     const int p = g / kp.I, j = g % kp.I;
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(THREADS) k_forward(KParams<T> kp) {
         s[(y + n / 2) * LDS + x + n / 2] = cscale<T>(pf, c);
     }
     __syncthreads();
-    fft2d<T, N, -1, THREADS, true>(s, tw);
+    fft2d<T, N, -1, THREADS, true, PL>(s, tw);
     cx<T>* X = kp.X + (size_t)g * N * N;
     for (int i = threadIdx.x; i < N * N; i += THREADS) {
         const int y = i / N, x = i % N;
@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(THREADS) k_forward(KParams<T> kp) {
         s[y * LDS + x] = mkc<T>(cnorm<T>(v), 0);
     }
     __syncthreads();
-    fft2d<T, N, +1, THREADS, false>(s, tw);
+    fft2d<T, N, +1, THREADS, false, PL>(s, tw);
     const T inv = (T)1 / (T)(N * N);
     cx<T>* S = kp.S + (size_t)g * N * N;
     for (int i = threadIdx.x; i < N * N; i += THREADS) {
@@ -554,7 +554,7 @@ __device__ __forceinline__ void project_modes(const KParams<T>& kp, int kind, in
     }
 }
 
-template <typename T, int N, int THREADS>
+template <typename T, int N, int THREADS, typename PL = Plan<N>>
 __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, int p, int j) {
     const int g = p * kp.I + j;
     constexpr int LDS = Tile<N>::LDS;
@@ -584,7 +584,7 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
         s[y * LDS + x] = (m && !(y == 0 && x == 0)) ? G : mkc<T>(0, 0);
     }
     __syncthreads();
-    fft2d<T, N, -1, THREADS, false>(s, tw);
+    fft2d<T, N, -1, THREADS, false, PL>(s, tw);
     (void)s2;
     const cx<T>* X = kp.X + (size_t)g * N2;
 #pragma unroll 8
@@ -594,14 +594,14 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
     }
     __syncthreads();
     if constexpr (PP) fft2d_pp_out_rows_pruned<T, N, +1, THREADS>(s, s2, tw);
-    else fft2d_out_rows_pruned<T, N, +1, THREADS>(s, tw);
+    else fft2d_out_rows_pruned<T, N, +1, THREADS, PL>(s, tw);
     static_assert(((size_t)(Tile<N>::ELEMS + N) * sizeof(cx<T>)) % 16 == 0, "v is 16-byte aligned");
     const cx<T>* PF = kp.PF + (size_t)g * n2;
     project_modes<T, N, THREADS>(kp, kind, p, j, s, PF, v, (int)threadIdx.x);
 }
 
 
-template <typename T, int N, int THREADS>
+template <typename T, int N, int THREADS, typename PL = Plan<N>>
 __global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
     // one work item per block (the grid covers every image of the batch): in a loop over
     // items the in-place transforms' index arithmetic is hoisted and spills
@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
     const int w = blockIdx.x;
     if (w >= nWork) return;
     const int p = kp.gradP[w / kp.I], j = w % kp.I;
-    if (j < kp.pgeo[p].nImg) adjoint_image<T, N, THREADS>(kp, kind, p, j);
+    if (j < kp.pgeo[p].nImg) adjoint_image<T, N, THREADS, PL>(kp, kind, p, j);
 }
 
 // ----------------------------------------------------------------------------------

@@ -54,14 +54,17 @@ def test_every_shape_gives_identical_results(case):
             assert got[k.replace("_threads", "")] == v, (got, sh)
         if ref is None:
             ref = (L, g, out)
+            ref_radix = {k: got[k + "_radix"] for k in ("eval", "forward", "adjoint")}
             continue
         np.testing.assert_array_equal(L, ref[0])
         np.testing.assert_array_equal(g, ref[1])
         np.testing.assert_array_equal(out["alpha"], ref[2]["alpha"])
         np.testing.assert_array_equal(out["metrics"], ref[2]["metrics"])
-    # the planner on the first solve picks one of them: the results stay the same
+    # the planner on the first solve picks one of them: the results stay the same (unless it
+    # also picked the other radix plan, whose rounding differs; see test_radix_plans)
     L, g, out, got = _run(w, None)
-    np.testing.assert_array_equal(out["alpha"], ref[2]["alpha"])
+    if all(got[k + "_radix"] == ref_radix[k] for k in ("eval", "forward", "adjoint")):
+        np.testing.assert_array_equal(out["alpha"], ref[2]["alpha"])
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
@@ -94,7 +97,40 @@ def test_fp64_has_one_shape():
     s = S.Solver(w.job, max_patches=1, precision="fp64")
     s.set_patches(w.patches.cutouts, None, w.patches.fixed_gamma)
     r = s.autotune(reps=1)
-    assert r["shape"] == dict(eval=0, forward=256, adjoint=256), r
+    assert {k: r["shape"][k] for k in ("eval", "forward", "adjoint")} == dict(eval=0, forward=256, adjoint=256), r
     with pytest.raises(S.SolverError, match="not compiled"):
         s.set_launch_shape(adjoint_threads=512)
+    s.close()
+
+
+# the radix plans of the sizes that have two (32, 64: k_eval and k_adjoint; 128: k_forward and
+# k_adjoint): the same transforms rounded differently
+RADIX = {
+    "fused64": (lambda: workload("plain64"), dict(eval_radix=8, adjoint_radix=8), dict(eval_radix=16, adjoint_radix=16)),
+    "general128": (lambda: workload("large128", n_patches=1, frames=2), dict(forward_radix=16, adjoint_radix=16),
+                   dict(forward_radix=8, adjoint_radix=8)),
+}
+
+
+@pytest.mark.parametrize("case", sorted(RADIX))
+def test_radix_plans(case):
+    make, p0, p1 = RADIX[case]
+    w = make()
+    out = []
+    for plan in (p0, p1):
+        s = S.Solver(w.job, max_patches=w.patches.cutouts.shape[0])
+        s.set_patches(w.patches.cutouts, None, w.patches.fixed_gamma)
+        s.set_launch_shape(**plan)
+        got = s.launch_shape()
+        for k, v in plan.items():
+            assert got[k] == v, (got, plan)
+        a = w.patches.alpha_true * 0.5
+        out.append((s.metric(a), s.gradient(a, "vogel")[0]))
+        s.close()
+    (L0, g0), (L1, g1) = out
+    np.testing.assert_allclose(L1, L0, rtol=1e-6)
+    assert np.linalg.norm(g1 - g0) / np.linalg.norm(g0) < 1e-5
+    s = S.Solver(w.job, max_patches=1)
+    with pytest.raises(S.SolverError, match="not a plan"):
+        s.set_launch_shape(adjoint_radix=11)
     s.close()
