@@ -306,7 +306,7 @@ int rdxg_profile_kernels(rdxg_solver* h, int32_t reps, double* ms);
  * fused evaluation k_eval (512 or 384; 0 on the general path); forward_threads: the general
  * path's transform kernel k_forward (256 or 512, 512 or 1024 at OTF size 128; 0 on the fused
  * path); adjoint_threads: the analytic gradient k_adjoint (same choices as forward).  No
- * shape changes a result: every element is computed by the same arithmetic. */
+ * block size changes a result: every element is computed by the same arithmetic. */
 typedef struct {
     int32_t eval_threads;
     int32_t forward_threads;

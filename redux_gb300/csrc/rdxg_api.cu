@@ -2072,15 +2072,17 @@ int time_kernel(rdxg_solver* h, int k, int reps, cudaEvent_t e0, cudaEvent_t e1,
 // ---------------------------------------------------------------------------------------
 // Launch-shape planner: the counterpart of the reference's FFTW_MEASURE planning
 // (fouriertransform.cpp:73-90), which times candidate transform plans once per size and
-// keeps the fastest.  The candidates are the block sizes compiled for the kernels that
-// dominate a round -- k_eval (fused path: 512 or 384 threads), k_forward (general path) and
-// k_adjoint (256 or 512 threads, 512 or 1024 at N = 128) -- and no choice changes a result:
-// every element of these kernels is computed by the same arithmetic whatever the block size.
-// (The radix plan of each size is fixed by its shared-memory tile.)  The first solve of a
-// handle measures the candidates on its loaded batch (the adjoint on a tenth of the patches,
-// the share of a solve round that asks for gradients), unless a handle of the same geometry
-// on the same device has already done so in this process (the table below, the planner's
-// wisdom).  FP64 handles, the plain baseline form, have one shape.
+// keeps the fastest.  The candidates of the kernels that dominate a round -- k_eval (fused
+// path: 512 or 384 threads), k_forward (general path) and k_adjoint (256 or 512 threads, 512
+// or 1024 at N = 128) -- are their block sizes, which change no result (every element is
+// computed by the same arithmetic whatever the block size), and, for the sizes with two
+// two-stage radix plans (32, 64, 128; see PlanAlt), the plan, which changes the rounding of
+// the transforms as FFTW's plans do.  The first solve of a handle measures the candidates on
+// its loaded batch (the adjoint on a tenth of the patches, the share of a solve round that asks
+// for gradients), unless a handle of the same geometry and batch size on the same device has
+// already done so in this process (the tables below, the planner's wisdom); the plan is
+// measured once per device, size and path, so every handle of a size uses the same.  FP64
+// handles, the plain baseline form, have one shape.
 // ---------------------------------------------------------------------------------------
 struct ShapeKey {
     int device, N, fused, M, I, P;
