@@ -61,8 +61,12 @@ def _dump(job, cutouts, fixed_gamma, st, fc, d, save_mask=0, extras=None):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("cfg", ["plain64", "production88", "plain64+"])
-def test_shim_solve_matches_the_python_harness(tmp_path, cfg):
-    """cfg "plain64+": the plain 64 x 64 workload with FIT_PLANE, REG_ALPHA and a warm start."""
+def test_shim_solve_matches_the_python_harness(tmp_path, cfg, monkeypatch):
+    """cfg "plain64+": the plain 64 x 64 workload with FIT_PLANE, REG_ALPHA and a warm start.
+    The driver runs in a process of its own, whose launch-shape planner could keep the other
+    radix plan (it times the candidates, as FFTW_MEASURE does): both processes keep the default
+    shapes (RDXG_AUTOTUNE=0), so that the bits compare."""
+    monkeypatch.setenv("RDXG_AUTOTUNE", "0")
     extras = None
     if cfg == "plain64+":
         from redux_gb300 import jobsetup as js
