@@ -318,6 +318,11 @@ typedef struct {
     int32_t eval_radix;
     int32_t forward_radix;
     int32_t adjoint_radix;
+    /* the solver kernel's form: 1 staged (the patch's optimiser vectors, object metric sums,
+     * object tables and null-space map copied into shared memory as the kernel starts, taken
+     * whenever they fit in 96 KB), 2 the global-memory form.  Both compute the same bits.
+     * Set: 0 keeps; pinning the form leaves the planner on. */
+    int32_t solver_form;
 } rdxg_launch_shape;
 
 /* The launch-shape planner, in place of the FFTW_MEASURE planning of the reference's

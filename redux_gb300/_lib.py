@@ -62,7 +62,8 @@ class ModeParams(C.Structure):
 
 class LaunchShape(C.Structure):
     _fields_ = [("eval_threads", C.c_int32), ("forward_threads", C.c_int32), ("adjoint_threads", C.c_int32),
-                ("eval_radix", C.c_int32), ("forward_radix", C.c_int32), ("adjoint_radix", C.c_int32)]
+                ("eval_radix", C.c_int32), ("forward_radix", C.c_int32), ("adjoint_radix", C.c_int32),
+                ("solver_form", C.c_int32)]
 
 
 class PatchReport(C.Structure):

@@ -44,6 +44,7 @@ struct rdxg_solver {
     int32_t *dImgObj = nullptr, *dImgCh = nullptr, *dObjFirst = nullptr, *dObjCount = nullptr;
     const int32_t *dObjFirstC = nullptr, *dObjCountC = nullptr;
     double *dObjW = nullptr, *dGradStep = nullptr, *dWin = nullptr, *dNWin = nullptr;
+    double* dGradScale = nullptr;     // [2][nObj][C] the adjoint's factors (Vogel, exact)
     int32_t *dRowPtr = nullptr, *dRowCol = nullptr, *dColPtr = nullptr, *dColRow = nullptr;
     double *dRowVal = nullptr, *dColVal = nullptr;
     float* dRowVal32 = nullptr;   // FP32 copy of the row values (metric requests of the FP32 path)
@@ -149,6 +150,9 @@ struct rdxg_solver {
     int32_t *dPImgObj = nullptr, *dPImgCh = nullptr, *dPObjFirst = nullptr, *dPObjCount = nullptr,
             *dPObjChunk0 = nullptr;
     size_t mapRowEntries = 0, mapColEntries = 0, mapNnz = 0;   // sizes of the device maps
+    int32_t mapMaxNnz = 0;            // the largest row-map entry count of a patch shape
+    int32_t cgStage = 0, cgStageMap = 0;   // the solver kernel's staged form (set per solve)
+    int32_t cgForm = 0;               // pinned solver kernel form (0: staged when it fits)
 };
 
 namespace {
@@ -253,6 +257,7 @@ KParams<T> make_kparams(rdxg_solver* h) {
     k.pObjFirst = h->dPObjFirst; k.pObjCount = h->dPObjCount;
     k.objWeight = h->dObjW; k.objGradStep = h->dGradStep; k.window = h->dWin; k.noiseWindow = h->dNWin;
     k.tw = (const cx<T>*)h->dTw; k.area = h->area; k.tiltX = h->geo.tilt_x; k.tiltY = h->geo.tilt_y;
+    k.gradScale = h->dGradScale; k.nCh = h->C;
     k.cutouts = h->dCutExt ? h->dCutExt : h->dCut;
     k.shift = h->dShift; k.statMean = h->dMean; k.statStd = h->dStd; k.statNoise = h->dNoise; k.rg = h->dRg;
     k.alphaEff = (const T*)h->dAlphaEff;
@@ -373,6 +378,32 @@ void launch_fd(rdxg_solver* h, cudaStream_t st) {
 }
 void launch_fd(rdxg_solver* h) { launch_fd(h, h->stream); }
 
+// FP32 map of metric requests (the point as float in dynamic shared memory, under 44 KB);
+// RDXG_MAP64=1: the FP64 map for metric requests too (precision studies)
+int cg_x1smem(const rdxg_solver* h) {
+    const char* m64 = getenv("RDXG_MAP64");
+    if (m64 && atoi(m64)) return 0;
+    return (!h->fp64 && (size_t)h->nFree * sizeof(float) <= 44 * 1024) ? 1 : 0;
+}
+
+// The solver kernel's form: staged when the patch's data fit in kCgStageBytes (the null-space
+// map too when it fits beside them), unless pinned to the global-memory form
+// (rdxg_set_launch_shape, or RDXG_CG_STAGE=0 in the environment).
+void cg_stage_choice(const rdxg_solver* h, int32_t* stage, int32_t* map, size_t* bytes) {
+    const char* cs = getenv("RDXG_CG_STAGE");
+    const bool allow = h->cgForm != 2 && !(cs && !atoi(cs));
+    const int nT = h->fused ? h->nTilesH : h->nTiles;
+    int m = cg_x1smem(h);
+    size_t b = CgStageLayout(h->nFree, h->nObj, nT, m, h->nPar, h->I, h->mapMaxNnz).total;
+    if (m && b > kCgStageBytes) {
+        m = 0;
+        b = CgStageLayout(h->nFree, h->nObj, nT, 0, h->nPar, h->I, h->mapMaxNnz).total;
+    }
+    *stage = (allow && b <= kCgStageBytes) ? 1 : 0;
+    *map = *stage ? m : 0;
+    *bytes = b;
+}
+
 template <typename T>
 CgArgs<T> make_cgargs(rdxg_solver* h, const CgParams& prm) {
     CgArgs<T> a{};
@@ -386,11 +417,8 @@ CgArgs<T> make_cgargs(rdxg_solver* h, const CgParams& prm) {
     a.curTilt = h->dCurTilt; a.resAlpha = h->dResAlpha; a.tiltX = h->geo.tilt_x; a.tiltY = h->geo.tilt_y;
     a.alphaEff = (T*)h->dAlphaEff; a.req = h->dReq; a.gmethod = h->dGm; a.modeCount = h->dMc; a.active = h->dActive;
     a.fused = h->fused ? 1 : 0;
-    // FP32 map of metric requests: the point as float in dynamic shared memory (under 44 KB)
-    a.x1Smem = (!h->fp64 && (size_t)h->nFree * sizeof(float) <= 44 * 1024) ? 1 : 0;
-    // RDXG_MAP64=1: the FP64 map for metric requests too (precision studies)
-    const char* m64 = getenv("RDXG_MAP64");
-    if (m64 && atoi(m64)) a.x1Smem = 0;
+    a.x1Smem = cg_x1smem(h);
+    a.stage = h->cgStage; a.stageMap = h->cgStageMap; a.maxNnz = h->mapMaxNnz;
     a.objMetric = h->dObjMetric; a.L = make_lists(h); a.nTilesH = h->nTilesH;
     a.chunkSize = h->chunk; a.chunksPerPatch = h->chunksPerPatch; a.objChunk0 = h->dPObjChunk0;
     a.objFirst = h->dPObjFirst; a.objCount = h->dPObjCount; a.aux = h->dAux;
@@ -417,6 +445,17 @@ int create_static(rdxg_solver* h, const rdxg_static* s) {
     // Channel::initPatch: otfNormalization = 1/sqrt(max |OTF(phi = 0)|); the maximum is the
     // zero lag of the pupil autocorrelation, sum A^2 over the pupil support.
     for (int c = 0; c < C; ++c) cn[c] = (T)(1.0 / std::sqrt(a2));
+    // the adjoint's factor per object and channel (project_modes): Vogel -2 area w^2 / N^6 / c
+    // (X carries the factor c: the projection is c N^2 (G (*) PF)), exact gradient
+    // -4 c^2 w / (ps^2 N^2) / c
+    std::vector<double> gs(2 * (size_t)h->nObj * C);
+    const double N2d = (double)N2;
+    for (int o = 0; o < h->nObj; ++o)
+        for (int c = 0; c < C; ++c) {
+            const double cc = (double)cn[c], w = h->objWeight[o];
+            gs[(size_t)o * C + c] = -2.0 * area * w * w / (N2d * N2d * N2d) / cc;
+            gs[((size_t)h->nObj + o) * C + c] = -4.0 * cc * cc * w / ((double)h->ps * h->ps * N2d) / cc;
+        }
     for (size_t i = 0; i < C * n2; ++i) phi[i] = (T)s->phi_fixed[i];
     std::vector<uint8_t> mask(N2, 0);
     for (int k = 0; k < s->n_otf_support; ++k) {
@@ -437,6 +476,8 @@ int create_static(rdxg_solver* h, const rdxg_static* s) {
     void* v;
     if ((r = upload(h, &v, mask))) return r;
     h->dMask = (uint8_t*)v;
+    if ((r = upload(h, &v, gs))) return r;
+    h->dGradScale = (double*)v;
     return RDXG_OK;
 }
 
@@ -636,6 +677,8 @@ int upload_geometry(rdxg_solver* h) {
     CK(h, cudaMemcpy(h->dPObjFirst, of.data(), of.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     CK(h, cudaMemcpy(h->dPObjCount, oc.data(), oc.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     CK(h, cudaMemcpy(h->dPObjChunk0, ch0.data(), ch0.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    h->mapMaxNnz = 0;
+    for (const rdxg_solver::Shape& sh : h->shapes) h->mapMaxNnz = std::max(h->mapMaxNnz, (int32_t)sh.rowCol.size());
     // the maps (reallocated when their sizes change)
     const size_t nnz = rowCol.size();
     if (rowPtr.size() != h->mapRowEntries || colPtr.size() != h->mapColEntries || nnz != h->mapNnz) {
@@ -870,7 +913,7 @@ int setup_fused(rdxg_solver* h, const rdxg_static* s) {
         const int c = h->hIdx[k];
         h->hPos[k] = (((c / N) + N / 2) % N) * (N + 1) + ((c % N) + N / 2) % N;
     }
-    h->nTilesH = (h->nH + 31) / 32;
+    h->nTilesH = (h->nH + kReduceTile - 1) / kReduceTile;
     h->npt = 1;
     if (h->nH > N * (N / 2 + 1)) return RDXG_OK;   // more points than the staging area holds
     const size_t smem = N == 32 ? EvalLauncher<float, 32>::smem(h->M, h->nH)
@@ -1659,6 +1702,10 @@ int prepare_solve(rdxg_solver* h, const rdxg_solve_params* s, SolvePlan& pl) {
         CK(h, cudaMemcpyAsync(h->dAlphaOff, h->dInitAlpha, (size_t)P * h->nPar * sizeof(double),
                               cudaMemcpyDeviceToDevice, h->stream));
     pl.sa = make_shift_args(h);
+    // the solver kernel stages its patch's data in shared memory when it fits
+    size_t bytes = 0;
+    cg_stage_choice(h, &h->cgStage, &h->cgStageMap, &bytes);
+    if (h->cgStage) CK(h, h->fp64 ? setup_cg<double>(bytes) : setup_cg<float>(bytes));
     return RDXG_OK;
 }
 
@@ -1901,29 +1948,46 @@ int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
 }  // namespace
 }  // extern "C++"
 
+// RDXG_NO_GRAPH=1: the rounds issued from a host loop, every kernel launched every round, each
+// handle on its own stream (for profilers that do not take kernels out of graphs with
+// conditional nodes); the host reads the active counters every `check` rounds.
+static bool no_graph() {
+    const char* ng = getenv("RDXG_NO_GRAPH");
+    return ng && atoi(ng);
+}
+
+static int solve_rounds_host(std::vector<SolvePlan>& plans, int check) {
+    for (long round = 0;; ++round) {
+        for (const SolvePlan& pl : plans) {
+            rdxg_solver* h = pl.h;
+            if (issue_round(pl, h->stream, pl.sa, [&](int, auto issue) { issue(h->stream); })) {
+                h->err = "cudaMemsetAsync failed";
+                return RDXG_ERR_CUDA;
+            }
+            h->launches += (h->fused ? 8 : (h->tcPlan.valid ? 8 : 7)) + (h->fitPlane ? 1 : 0);
+            CKL(h);
+        }
+        if ((round + 1) % check == 0) {
+            int32_t active = 0;
+            for (const SolvePlan& pl : plans) {
+                rdxg_solver* h = pl.h;
+                CK(h, cudaMemcpyAsync(h->hActive, h->dActive, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+                CK(h, cudaStreamSynchronize(h->stream));
+                active += *h->hActive;
+            }
+            if (active == 0) break;
+        }
+        if (round > 2000000L) { plans[0].h->err = "solver did not terminate"; return RDXG_ERR_STATE; }
+    }
+    return RDXG_OK;
+}
+
 int rdxg_solve_async(rdxg_solver* h, const rdxg_solve_params* s) {
     std::vector<SolvePlan> plans(1);
     int r = prepare_solve(h, s, plans[0]);
     if (r) return r;
     const int check = s->check_every > 0 ? s->check_every : 8;
-    const char* ng = getenv("RDXG_NO_GRAPH");
-    if (!(ng && atoi(ng))) return solve_rounds_graph(plans, check);
-    const SolvePlan& pl = plans[0];
-    for (long round = 0;; ++round) {
-        if (issue_round(pl, h->stream, pl.sa, [&](int, auto issue) { issue(h->stream); })) {
-            h->err = "cudaMemsetAsync failed";
-            return RDXG_ERR_CUDA;
-        }
-        h->launches += (h->fused ? 8 : (h->tcPlan.valid ? 8 : 7)) + (h->fitPlane ? 1 : 0);
-        CKL(h);
-        if ((round + 1) % check == 0) {
-            CK(h, cudaMemcpyAsync(h->hActive, h->dActive, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
-            CK(h, cudaStreamSynchronize(h->stream));
-            if (*h->hActive == 0) break;
-        }
-        if (round > 2000000L) { h->err = "solver did not terminate"; return RDXG_ERR_STATE; }
-    }
-    return RDXG_OK;
+    return no_graph() ? solve_rounds_host(plans, check) : solve_rounds_graph(plans, check);
 }
 
 int rdxg_solve_many(rdxg_solver* const* handles, int32_t n, const rdxg_solve_params* s) {
@@ -1941,7 +2005,7 @@ int rdxg_solve_many(rdxg_solver* const* handles, int32_t n, const rdxg_solve_par
         if (r) return r;
     }
     const int check = s->check_every > 0 ? s->check_every : 8;
-    return solve_rounds_graph(plans, check);
+    return no_graph() ? solve_rounds_host(plans, check) : solve_rounds_graph(plans, check);
 }
 
 int rdxg_fetch_results(rdxg_solver* h, double* alpha_out, rdxg_patch_report* reports, double* metrics) {
@@ -2289,8 +2353,15 @@ int rdxg_set_launch_shape(rdxg_solver* h, const rdxg_launch_shape* shape) {
         }
         v[f] = tv | (pv << 1);
     }
+    if (shape->solver_form < 0 || shape->solver_form > 2) {
+        h->err = "solver_form is 1 (staged) or 2 (global memory)";
+        return RDXG_ERR_ARG;
+    }
+    if (shape->solver_form) h->cgForm = shape->solver_form;
+    bool pinned = false;
+    for (int f = 0; f < 3; ++f) pinned = pinned || want[f] != 0 || wantRadix[f] != 0;
     h->shapeEval = v[0]; h->shapeFwd = v[1]; h->shapeAdj = v[2];
-    h->tune = 0;
+    if (pinned) h->tune = 0;
     return RDXG_OK;
 }
 
@@ -2302,6 +2373,10 @@ int rdxg_get_launch_shape(const rdxg_solver* h, rdxg_launch_shape* shape) {
     shape->eval_radix = shape->eval_threads ? radix_of(h->N, h->shapeEval >> 1) : 0;
     shape->forward_radix = shape->forward_threads ? radix_of(h->N, h->shapeFwd >> 1) : 0;
     shape->adjoint_radix = radix_of(h->N, h->shapeAdj >> 1);
+    int32_t stage = 0, map = 0;
+    size_t bytes = 0;
+    cg_stage_choice(h, &stage, &map, &bytes);
+    shape->solver_form = stage ? 1 : 2;
     return RDXG_OK;
 }
 

@@ -19,6 +19,14 @@ namespace rdxg {
 // every lane holds the same bits.
 struct WarpVec {
     int n;
+    // with the vectors staged in shared memory: their base and stride, and a bit per vector
+    // written (in every lane), so that only those are copied back
+    double* base = nullptr;
+    int stride = 0;
+    unsigned dirty = 0;
+    __device__ void mark(const double* d) {
+        if (base) dirty |= 1u << (int)((d - base) / stride);
+    }
     __device__ static double wsum(double a) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
@@ -27,10 +35,12 @@ struct WarpVec {
     __device__ static int lane() { return threadIdx.x & 31; }
     __device__ void copy(double* d, const double* s) {
         for (int i = lane(); i < n; i += 32) d[i] = s[i];
+        mark(d);
         __syncwarp();
     }
     __device__ void zero(double* d) {
         for (int i = lane(); i < n; i += 32) d[i] = 0.0;
+        mark(d);
         __syncwarp();
     }
     __device__ double nrm2(const double* v) {
@@ -50,15 +60,18 @@ struct WarpVec {
             a += t * g[i];
             g0[i] = t;
         }
+        mark(g0);
         __syncwarp();
         return wsum(a);
     }
     __device__ void dir_update(double* p, const double* g, double beta) {
         for (int i = lane(); i < n; i += 32) p[i] = g[i] - beta * p[i];
+        mark(p);
         __syncwarp();
     }
     __device__ void step(double* x1, const double* x, const double* p, double s) {
         for (int i = lane(); i < n; i += 32) x1[i] = x[i] + s * p[i];
+        mark(x1);
         __syncwarp();
     }
 };
@@ -81,6 +94,10 @@ struct CgArgs {
     const int32_t* rowPtr; const int32_t* rowCol; const double* rowVal;
     const float* rowVal32;  // FP32 copy of rowVal
     int32_t x1Smem;         // FP32 metric-request map enabled (dynamic shared memory n_free floats)
+    // staged form (CgStageLayout): the patch's vectors, object metric tiles and weights and
+    // object tables copied into shared memory when the kernel starts; stageMap: the entries of
+    // its row map as well (FP32 map, at most kCgRowsPerThread rows per thread)
+    int32_t stage, stageMap, maxNnz;
     const int32_t* colPtr; const int32_t* colRow; const double* colVal;
     const double* curTilt;  // [P][I][2] (y, x): currentTiltOffset of each image
     const double* resAlpha; // [P][I][2] (y, x): channel residual tilt (phi_channel term)
@@ -133,14 +150,17 @@ __device__ void map_point(const CgArgs<T>& a, int p, const double* x1) {
 template <typename T, int THREADS>
 __device__ void map_point_f32(const CgArgs<T>& a, int p, const double* x1, float* xs) {
     const int nF = a.pgeo[p].nFree;
-    for (int c = threadIdx.x; c < nF; c += THREADS) xs[c] = (float)x1[c];
-    __syncthreads();
+    if (xs) {
+        for (int c = threadIdx.x; c < nF; c += THREADS) xs[c] = (float)x1[c];
+        __syncthreads();
+    }
     const double* off = a.alphaOff + (size_t)p * a.nPar;
     T* ae = a.alphaEff + (size_t)p * a.nPar;
     const int32_t* rp = a.rowPtr + a.pgeo[p].rowBase;
     for (int r = threadIdx.x; r < a.nPar; r += THREADS) {
         float v = 0.f;
-        for (int e = rp[r]; e < rp[r + 1]; ++e) v = fmaf(a.rowVal32[e], xs[a.rowCol[e]], v);
+        for (int e = rp[r]; e < rp[r + 1]; ++e)
+            v = fmaf(a.rowVal32[e], xs ? xs[a.rowCol[e]] : (float)x1[a.rowCol[e]], v);
         v += (float)off[r];
         const int j = r / a.M, m = r % a.M;
         const size_t b = ((size_t)p * a.I + j) * 2;
@@ -151,26 +171,72 @@ __device__ void map_point_f32(const CgArgs<T>& a, int p, const double* x1, float
     __syncthreads();
 }
 
-// append the chunks and objects of patch p to the evaluation work lists
+// Shared-memory layout (bytes) of the staged solver kernel: the patch's five vectors, its
+// object metric tiles, the object weights, its reference-object flags and object tables, and
+// (stageMap) its row map (row pointers, entry values and columns), alpha offsets, the tilt
+// terms of its images (currentTiltOffset, channel residual) and the point as float.
+struct CgStageLayout {
+    size_t om, ow, off, tilt, ints, rp, ec, ev, xs, total;
+    __host__ __device__ CgStageLayout(int stride, int nObj, int nT, int stageMap, int nPar, int I, int maxNnz) {
+        const size_t d = sizeof(double), i4 = sizeof(int32_t);
+        om = (size_t)5 * stride * d;
+        ow = om + (size_t)nObj * nT * d;
+        off = ow + (size_t)nObj * d;
+        tilt = off + (stageMap ? (size_t)nPar * d : 0);
+        ints = tilt + (stageMap ? (size_t)4 * I * d : 0);
+        rp = ints + (size_t)(2 + 3 * nObj) * i4;
+        ec = rp + (stageMap ? (size_t)(nPar + 1) * i4 : 0);
+        ev = ec + (stageMap ? (size_t)maxNnz * i4 : 0);
+        xs = ev + (stageMap ? (size_t)maxNnz * sizeof(float) : 0);
+        total = xs + (stageMap ? (size_t)stride * sizeof(float) : 0);
+    }
+};
+
+// The FP32 map of the staged kernel: the same arithmetic as map_point_f32, every operand in
+// shared memory (rps: the patch's row pointers, ec/ev: its entries from entry e0 on, offs: its
+// alpha offsets, tilt: [2][I][2] current tilt offsets and channel residuals, xs: room for the
+// point as float, converted once per free parameter).
+template <typename T, int THREADS>
+__device__ void map_rows_staged(const CgArgs<T>& a, int p, const double* x1, const int32_t* rps, const int32_t* ec,
+                                const float* ev, const double* offs, const double* tilt, float* xs, int nF) {
+    for (int c = threadIdx.x; c < nF; c += THREADS) xs[c] = (float)x1[c];
+    __syncthreads();
+    T* ae = a.alphaEff + (size_t)p * a.nPar;
+    const int e0 = rps[0];
+    const double* cur = tilt;
+    const double* res = tilt + 2 * a.I;
+    for (int r = threadIdx.x; r < a.nPar; r += THREADS) {
+        float v = 0.f;
+        for (int e = rps[r] - e0; e < rps[r + 1] - e0; ++e) v = fmaf(ev[e], xs[ec[e]], v);
+        v += (float)offs[r];
+        const int j = r / a.M, m = r % a.M;
+        if (m == a.tiltX) v += (float)(cur[2 * j + 1] - res[2 * j + 1]);
+        else if (m == a.tiltY) v += (float)(cur[2 * j + 0] - res[2 * j + 0]);
+        ae[r] = (T)v;
+    }
+    __syncthreads();
+}
+
+// append the chunks and objects of patch p to the evaluation work lists; cnt, first, ch0: the
+// patch's object image counts, first images and first chunks
 template <typename T>
-__device__ void enqueue_eval(const CgArgs<T>& a, int p, int rq, int mode) {
+__device__ void enqueue_eval(const CgArgs<T>& a, int p, int rq, int mode, const int32_t* cnt, const int32_t* first,
+                             const int32_t* ch0, int chunks) {
     // one reservation per list (the atomics go out together), then the writes
     const int kp = atomicAdd(a.L.nEvalP, 1);
-    const int k0 = atomicAdd(a.L.nEval, a.pgeo[p].chunks);
+    const int k0 = atomicAdd(a.L.nEval, chunks);
     const int j0 = atomicAdd(a.L.nPo, a.nObj);
     a.L.evalP[kp] = p;
     for (int o = 0; o < a.nObj; ++o) {
-        const size_t po = (size_t)p * a.nObj + o;
-        const int cnt = a.objCount[po];
-        const int nc = (cnt + a.chunkSize - 1) / a.chunkSize;
+        const int nc = (cnt[o] + a.chunkSize - 1) / a.chunkSize;
         for (int c = 0; c < nc; ++c) {
             EvalItem it;
             it.p = p; it.o = o;
-            it.first = a.objFirst[po] + c * a.chunkSize;
-            it.count = min(a.chunkSize, cnt - c * a.chunkSize);
-            it.chunk = a.objChunk0[po] + c;
+            it.first = first[o] + c * a.chunkSize;
+            it.count = min(a.chunkSize, cnt[o] - c * a.chunkSize);
+            it.chunk = ch0[o] + c;
             it.df = (rq == REQ_DF) ? 1 : 0;
-            a.L.eval[k0 + a.objChunk0[po] + c] = it;
+            a.L.eval[k0 + ch0[o] + c] = it;
         }
         PoItem pi;
         pi.p = p; pi.o = o; pi.mode = mode;
@@ -178,65 +244,140 @@ __device__ void enqueue_eval(const CgArgs<T>& a, int p, int rq, int mode) {
     }
 }
 
-template <typename T, int THREADS>
+// One block per patch.  ST (staged): the patch's vectors, object metric tiles, object
+// weights and tables (and, with stageMap, its row map) are copied into shared memory with
+// cp.async as the kernel starts, so that the state machine's vector operations, the object
+// sums, the map and the work-list appends wait on shared memory instead of chains of
+// dependent global loads; the vectors the round wrote are copied back at the end.  The
+// arithmetic and its order are the same in both forms.
+template <typename T, int THREADS, bool ST>
 __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
     const int p = blockIdx.x;
     __shared__ double fsh;
     __shared__ double objSum[64];
     __shared__ int32_t pcShared, reqShared;
+    __shared__ unsigned dirtyShared;
+    extern __shared__ __align__(16) unsigned char cg_smem[];
     // the state is read by the first warp, which runs the machine; the block needs pc and req
     CgState st;
     if (threadIdx.x < 32) st = a.states[p];
-    if (threadIdx.x == 0) { pcShared = st.pc; reqShared = st.req; }
-    __syncthreads();
-    const int pc0 = pcShared, req0 = reqShared;
     const PatchGeo pg = a.pgeo[p];
     const int nF = pg.nFree;
     const int32_t* rp = a.rowPtr + pg.rowBase;
     const int32_t* cp = a.colPtr + pg.colBase;
     // the patch's vectors, nF long, at the stride of the handle's largest (prm.n_free)
     const int stride = a.prm.n_free;
-    double* x = a.vec + (size_t)p * 5 * stride;
+    double* const vg = a.vec + (size_t)p * 5 * stride;
+    const int nT = a.fused ? a.nTilesH : a.nTiles;
+    const double* om = (a.fused ? a.objMetric : a.partial) + (size_t)p * a.nObj * nT;
+    const double* ow = a.objWeight;
+    const int32_t* tabs = nullptr;      // staged: aux flags, object counts, first images, first chunks
+    double* vb = vg;                    // where the machine works on the vectors
+    const CgStageLayout lay(stride, a.nObj, nT, a.stageMap, a.nPar, a.I, a.maxNnz);
+    int32_t* rps = reinterpret_cast<int32_t*>(cg_smem + lay.rp);
+    int32_t* ec = reinterpret_cast<int32_t*>(cg_smem + lay.ec);
+    float* ev = reinterpret_cast<float*>(cg_smem + lay.ev);
+    double* offs = reinterpret_cast<double*>(cg_smem + lay.off);
+    double* tilt = reinterpret_cast<double*>(cg_smem + lay.tilt);
+    int e0 = 0;
+    if (ST) {
+        double* vs = reinterpret_cast<double*>(cg_smem);
+        for (int i = threadIdx.x; i < 5 * nF; i += THREADS) {
+            const int k = i / nF, c = i - k * nF;
+            cp_async8(vs + (size_t)k * stride + c, vg + (size_t)k * stride + c);
+        }
+        double* oms = reinterpret_cast<double*>(cg_smem + lay.om);
+        double* ows = reinterpret_cast<double*>(cg_smem + lay.ow);
+        int32_t* ints = reinterpret_cast<int32_t*>(cg_smem + lay.ints);
+        for (int i = threadIdx.x; i < a.nObj * nT; i += THREADS) cp_async8(oms + i, om + i);
+        for (int i = threadIdx.x; i < a.nObj; i += THREADS) cp_async8(ows + i, a.objWeight + i);
+        if (a.fused) {
+            if (threadIdx.x < 2) cp_async4(ints + threadIdx.x, a.aux + 2 * p + threadIdx.x);
+            for (int i = threadIdx.x; i < a.nObj; i += THREADS) {
+                const size_t po = (size_t)p * a.nObj + i;
+                cp_async4(ints + 2 + i, a.objCount + po);
+                cp_async4(ints + 2 + a.nObj + i, a.objFirst + po);
+                cp_async4(ints + 2 + 2 * a.nObj + i, a.objChunk0 + po);
+            }
+        }
+        cp_async_commit();
+        vb = vs; om = oms; ow = ows; tabs = ints;
+        if (a.stageMap) {
+            // the FP32 map's operands: row pointers, alpha offsets, tilt terms (the entries
+            // follow once their range is known)
+            for (int r = threadIdx.x; r <= a.nPar; r += THREADS) cp_async4(rps + r, rp + r);
+            const double* off = a.alphaOff + (size_t)p * a.nPar;
+            for (int r = threadIdx.x; r < a.nPar; r += THREADS) cp_async8(offs + r, off + r);
+            const size_t b = (size_t)p * a.I * 2;
+            for (int i = threadIdx.x; i < 2 * a.I; i += THREADS) {
+                cp_async8(tilt + i, a.curTilt + b + i);
+                cp_async8(tilt + 2 * a.I + i, a.resAlpha + b + i);
+            }
+            cp_async_commit();
+            e0 = rp[0];
+        }
+    }
+    if (threadIdx.x == 0) { pcShared = st.pc; reqShared = st.req; dirtyShared = 0; }
+    __syncthreads();
+    const int pc0 = pcShared, req0 = reqShared;
+    if (ST && a.stageMap) {
+        const int e1 = rp[a.nPar];
+        for (int e = e0 + (int)threadIdx.x; e < e1; e += THREADS) {
+            cp_async4(ev + (e - e0), a.rowVal32 + e);
+            cp_async4(ec + (e - e0), a.rowCol + e);
+        }
+        cp_async_commit();
+    }
+    double* x = vb;
     double* pv = x + stride;
     double* g = pv + stride;
     double* g0 = g + stride;
     double* x1 = g0 + stride;
     if (pc0 == PC_DONE) {
+        if (ST) cp_async_wait_all();
         if (threadIdx.x == 0) a.req[p] = REQ_DONE;
         return;
     }
     double f = 0;
     if (a.fused && req0 == REQ_F && a.aux[2 * p + 1]) {
         // the last evaluation only refreshed the reference object: repeat the request
+        if (ST) cp_async_wait_all();
         if (threadIdx.x == 0) {
             a.aux[2 * p + 0] = 1;
             a.aux[2 * p + 1] = 0;
             a.req[p] = REQ_F;
             atomicAdd(a.active, 1);
-            enqueue_eval(a, p, REQ_F, 0);
+            const size_t po = (size_t)p * a.nObj;
+            enqueue_eval(a, p, REQ_F, 0, a.objCount + po, a.objFirst + po, a.objChunk0 + po, pg.chunks);
         }
         return;
+    }
+    if (ST) {
+        // the vectors, tiles and tables (the row map's entries may still be in flight)
+        if (a.stageMap) cp_async_wait_one();
+        else cp_async_wait_all();
+        __syncthreads();
     }
     if (req0 == REQ_F) {
         // object sums: one warp per object, each lane adds its tiles in order, then a fixed
         // shuffle tree; the objects are added in order
-        const int nT = a.fused ? a.nTilesH : a.nTiles;
-        const double* src = (a.fused ? a.objMetric : a.partial) + (size_t)p * a.nObj * nT;
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         for (int o = wid; o < a.nObj; o += THREADS / 32) {
             double m = 0;
-            for (int t = lane; t < nT; t += 32) m += src[(size_t)o * nT + t];
+            for (int t = lane; t < nT; t += 32) m += om[(size_t)o * nT + t];
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) m += __shfl_down_sync(0xffffffffu, m, off);
-            if (lane == 0) objSum[o] = m;
+            // each object's weighted term in its own warp (the divisions run side by side)
+            if (lane == 0) {
+                const double w = ow[o];
+                objSum[o] = (w != 0.0) ? w * (m / ((double)a.ps * a.ps)) : 0.0;
+            }
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             double sum = 0;
-            for (int o = 0; o < a.nObj; ++o) {
-                const double w = a.objWeight[o];
-                if (w != 0.0) sum += w * (objSum[o] / ((double)a.ps * a.ps));
-            }
+            for (int o = 0; o < a.nObj; ++o)
+                if (ow[o] != 0.0) sum += objSum[o];
             fsh = sum;
         }
         __syncthreads();
@@ -269,31 +410,52 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
             }
             g[c] = v;
         }
+        if (ST && threadIdx.x == 0) dirtyShared |= 1u << 2;
         __syncthreads();
     } else if (req0 == REQ_SHIFT) {
         double* off = a.alphaOff + (size_t)p * a.nPar;
         const double* al = a.alpha + (size_t)p * a.nPar;
         for (int r = threadIdx.x; r < a.nPar; r += THREADS) off[r] = al[r];
+        if (ST && a.stageMap)
+            for (int r = threadIdx.x; r < a.nPar; r += THREADS) offs[r] = al[r];
         __syncthreads();
     }
     __shared__ int rqShared;
     if (threadIdx.x < 32) {
         WarpVec V{nF};
+        if (ST) { V.base = vb; V.stride = stride; }
         CgParams prm = a.prm;       // the patch's own sizes
         prm.n_free = nF;
         prm.n_modes = pg.nMode;
         Machine<WarpVec> mc(prm, st, V, x, pv, g, g0, x1, a.metrics + (size_t)p * a.prm.max_metrics);
         const int r = mc.advance(f);
-        if (threadIdx.x == 0) rqShared = r;
+        if (threadIdx.x == 0) {
+            rqShared = r;
+            if (ST) dirtyShared |= V.dirty;
+        }
     }
+    if (ST && a.stageMap) cp_async_wait_all();
     __syncthreads();    // the point x1 and the request are visible to the block
     const int rq = rqShared;
     if (sizeof(T) == sizeof(float) && a.x1Smem) {
         extern __shared__ float xs[];
-        if (rq == REQ_F) map_point_f32<T, THREADS>(a, p, x1, xs);
-        else if (rq == REQ_DF || rq == REQ_SHIFT || rq == REQ_DONE) map_point<T, THREADS>(a, p, x1);
+        if (rq == REQ_F) {
+            if (ST && a.stageMap)
+                map_rows_staged<T, THREADS>(a, p, x1, rps, ec, ev, offs, tilt,
+                                            reinterpret_cast<float*>(cg_smem + lay.xs), nF);
+            else map_point_f32<T, THREADS>(a, p, x1, ST ? nullptr : xs);
+        } else if (rq == REQ_DF || rq == REQ_SHIFT || rq == REQ_DONE) {
+            map_point<T, THREADS>(a, p, x1);
+        }
     } else if (rq == REQ_F || rq == REQ_DF || rq == REQ_SHIFT) {
         map_point<T, THREADS>(a, p, x1);
+    }
+    if (ST) {
+        // the vectors written in this round back to global memory
+        const unsigned d = dirtyShared;
+        for (int k = 0; k < 5; ++k)
+            if ((d >> k) & 1u)
+                for (int c = threadIdx.x; c < nF; c += THREADS) vg[(size_t)k * stride + c] = vb[(size_t)k * stride + c];
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -309,14 +471,17 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
         }
         if (a.fused && (rq == REQ_F || rq == REQ_DF)) {
             int mode = 0;
+            const int refValid = ST ? tabs[0] : a.aux[2 * p + 0];
             if (rq == REQ_DF) {
                 mode = 1;
                 a.aux[2 * p + 0] = 1;     // the gradient pass leaves the exact object behind
-            } else if (!a.aux[2 * p + 0]) {
+            } else if (!refValid) {
                 mode = 2;                 // refresh the reference object first
                 a.aux[2 * p + 1] = 1;
             }
-            enqueue_eval(a, p, rq, mode);
+            const size_t po = (size_t)p * a.nObj;
+            if (ST) enqueue_eval(a, p, rq, mode, tabs + 2, tabs + 2 + a.nObj, tabs + 2 + 2 * a.nObj, pg.chunks);
+            else enqueue_eval(a, p, rq, mode, a.objCount + po, a.objFirst + po, a.objChunk0 + po, pg.chunks);
         } else if (a.phaseList && (rq == REQ_F || rq == REQ_DF)) {
             // general path with the tensor-core mode expansion: the patches to expand
             a.L.evalP[atomicAdd(a.L.nEvalP, 1)] = p;

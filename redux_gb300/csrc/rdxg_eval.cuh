@@ -34,6 +34,9 @@ struct PoItem {
     int32_t p, o, mode;   // mode: 0 metric, 1 gradient (write O, Qt), 2 refresh O'
 };
 
+// half-plane points per work item of the object reduction (k_reduce): four per lane
+constexpr int kReduceTile = 128;
+
 // work-list counters (reset every round)
 enum : int32_t { kCounterEval = 0, kCounterPo = 1, kCounterGrad = 2, kCounterFd = 3, kCounterEvalP = 4,
                  kCounterShift = 5 };
@@ -87,7 +90,7 @@ struct EvalParams {
     Acc4<T>* part;      // [P*chunksPerPatch][nH] (R, Q, P're, P'im)
     double* objMetric;  // [po][tiles] object metric summed over tiles of 32 half-plane points
     const int32_t* hPos; // [nH] tile position (row * (N+1) + column) of each half-plane point
-    int32_t nTilesH;    // point tiles (32 points) per object in the reduction
+    int32_t nTilesH;    // point tiles (kReduceTile points) per object in the reduction
     T* phi;             // [g][n*n] phases of the images being evaluated (k_phase)
     int32_t nCh;        // channels (fixed phases)
     Lists L;
@@ -605,15 +608,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_fd_half(EvalParams<T> e) {
 
 // ----------------------------------------------------------------------------------
 // Per-object reduction over the chunks (fixed order) and the object metric: one warp per
-// (object, tile of 32 points); each tile's sum is formed in double by a fixed shuffle tree
-// and the solver adds the tiles in order.  mode 1 (gradient) and 2 (refresh) replace O' by
-// the exact object O of this point; mode 1 also writes O and Q on the full plane for the
-// gradient kernels.
+// (object, tile of kReduceTile points, four per lane); each lane adds its points' terms and
+// the warp adds the lanes' by a fixed shuffle tree, as float-float numbers (about 48 bits, on
+// the FP32 pipe: GB300's FP64 pipe is narrow), and the tile's sum is stored in double; the
+// solver adds the tiles in order.  mode 1 (gradient) and 2 (refresh) replace O' by the exact
+// object O of this point; mode 1 also writes O and Q on the full plane for the gradient
+// kernels.
 // ----------------------------------------------------------------------------------
 template <typename T, int N, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_reduce(EvalParams<T> e) {
     constexpr int WPB = THREADS / 32;
-    static_assert(THREADS % 32 == 0, "tiles are warps");
+    constexpr int PER_LANE = kReduceTile / 32;
+    static_assert(THREADS % 32 == 0 && kReduceTile % 32 == 0, "tiles are warps");
     const int nItems = *e.L.nPo * e.nTilesH;
     const int nH = e.hp.nH;
     const int lane = threadIdx.x & 31;
@@ -625,38 +631,40 @@ __global__ void __launch_bounds__(THREADS) k_reduce(EvalParams<T> e) {
         const int c0 = e.hp.objChunk0[po];
         const int nc = (e.k.pObjCount[po] + e.hp.chunkSize - 1) / e.hp.chunkSize;
         const Acc4<T>* base = e.part + (size_t)(it.p * e.hp.chunksPerPatch + c0) * nH;
-        double acc = 0;
-        const int h = tile * 32 + lane;
-        if (h < nH) {
-            T R = 0, Q = 0, Pr = 0, Pi = 0;
-            for (int c = 0; c < nc; ++c) {
-                const Acc4<T> u = base[(size_t)c * nH + h];
-                R += u.r; Q += u.q; Pr += u.pr; Pi += u.pi;
-            }
-            const cx<T> oh = e.Oh[po * nH + h];
-            const T Qt = gam + Q;
-            // conj(P') - gamma O'
-            const T dPr = Pr - gam * oh.x, dPi = -Pi - gam * oh.y;
-            const T term = R + gam * cnorm<T>(oh) - (dPr * dPr + dPi * dPi) / Qt;
-            const int cidx = e.hp.idx[h];
-            const bool dc = (cidx == (N / 2) * N + N / 2);
-            acc = dc ? (double)term : 2.0 * (double)term;
-            if (it.mode != 0) {
-                const cx<T> O = mkc<T>(oh.x + dPr / Qt, oh.y + dPi / Qt);
-                e.Oh[po * nH + h] = O;
-                if (it.mode == 1) {
-                    const int cy = cidx / N, cxx = cidx % N;
-                    const int partner = ((N - cy) % N) * N + (N - cxx) % N;
-                    e.k.O[po * N * N + cidx] = O;
-                    e.k.Qt[po * N * N + cidx] = Qt;
-                    e.k.O[po * N * N + partner] = mkc<T>(O.x, -O.y);
-                    e.k.Qt[po * N * N + partner] = Qt;
+        float hi = 0.f, lo = 0.f;
+#pragma unroll
+        for (int k = 0; k < PER_LANE; ++k) {
+            const int h = tile * kReduceTile + k * 32 + lane;
+            if (h < nH) {
+                T R = 0, Q = 0, Pr = 0, Pi = 0;
+                for (int c = 0; c < nc; ++c) {
+                    const Acc4<T> u = base[(size_t)c * nH + h];
+                    R += u.r; Q += u.q; Pr += u.pr; Pi += u.pi;
+                }
+                const cx<T> oh = e.Oh[po * nH + h];
+                const T Qt = gam + Q;
+                // conj(P') - gamma O'
+                const T dPr = Pr - gam * oh.x, dPi = -Pi - gam * oh.y;
+                const T term = R + gam * cnorm<T>(oh) - (dPr * dPr + dPi * dPi) / Qt;
+                const int cidx = e.hp.idx[h];
+                const bool dc = (cidx == (N / 2) * N + N / 2);
+                ff_add(hi, lo, dc ? (float)term : 2.f * (float)term, 0.f);
+                if (it.mode != 0) {
+                    const cx<T> O = mkc<T>(oh.x + dPr / Qt, oh.y + dPi / Qt);
+                    e.Oh[po * nH + h] = O;
+                    if (it.mode == 1) {
+                        const int cy = cidx / N, cxx = cidx % N;
+                        const int partner = ((N - cy) % N) * N + (N - cxx) % N;
+                        e.k.O[po * N * N + cidx] = O;
+                        e.k.Qt[po * N * N + cidx] = Qt;
+                        e.k.O[po * N * N + partner] = mkc<T>(O.x, -O.y);
+                        e.k.Qt[po * N * N + partner] = Qt;
+                    }
                 }
             }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if (lane == 0) e.objMetric[po * e.nTilesH + tile] = acc;
+        warp_sum_ff(hi, lo);
+        if (lane == 0) e.objMetric[po * e.nTilesH + tile] = (double)hi + (double)lo;
     }
 }
 

@@ -11,10 +11,12 @@ namespace rdxg {
 // form (the plain baseline) keeps one.
 template <typename T> struct HasAlt { static constexpr bool value = std::is_same<T, float>::value; };
 
+// after the work tile and twiddles: the larger of the alpha staging, the adjoint's projection
+// weights [n2] and mode sums [M] (8 bytes each), a reduction buffer
 template <typename T, int N>
 static size_t extra_smem(int M) {
     size_t a = (size_t)M * sizeof(T);
-    size_t b = (size_t)(N / 2) * (N / 2) * sizeof(T);
+    size_t b = (size_t)(N / 2) * (N / 2) * sizeof(T) + (size_t)M * 8;
     size_t c = 33 * sizeof(double);
     size_t m = a > b ? a : b;
     return (m > c ? m : c) + 16;
@@ -27,12 +29,12 @@ static size_t smem_pp(int M) {
 }
 
 // shared memory of the recomputing adjoint: tile [| X tile] | twiddles | PF | projection
-// weights | alpha
+// weights | alpha, then the mode sums (8 bytes per mode) in its place
 template <typename T, int N>
 static size_t adjoint_rc_smem(int M) {
     constexpr size_t n2 = (size_t)(N / 2) * (N / 2);
     constexpr size_t tiles = PingPong<T, N>::value ? 2 : 1;
-    return (size_t)(tiles * Tile<N>::ELEMS + N + n2) * sizeof(cx<T>) + (n2 + (size_t)M) * sizeof(T) + 16;
+    return (size_t)(tiles * Tile<N>::ELEMS + N + n2) * sizeof(cx<T>) + n2 * sizeof(T) + (size_t)M * 8 + 16;
 }
 // ... of the recomputing finite-difference gradient: k_fd's | PF | alpha
 template <typename T, int N>

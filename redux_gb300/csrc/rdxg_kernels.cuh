@@ -49,6 +49,10 @@ struct KParams {
     const double* noiseWindow;// [ps*ps]
     const cx<T>* tw;          // [N] exp(-2 pi i k/N)
     double area;
+    // the adjoint's factor per object and channel, [2][nObj][nCh]: Vogel, exact gradient
+    // (formed on the host, so that no block spends GB300's narrow FP64 pipe on it)
+    const double* gradScale;
+    int32_t nCh;
     int32_t tiltX, tiltY;
     // per patch
     const float* cutouts;     // [g][cs*cs]
@@ -479,6 +483,32 @@ __global__ void __launch_bounds__(THREADS) k_accum(KParams<T> kp) {
     if (threadIdx.x == 0) kp.partial[(size_t)po * kp.nTiles + blockIdx.x] = tot;
 }
 
+// a + b = s + e exactly (Knuth's TwoSum), in FP32 with explicit roundings
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// (hi, lo) += (h2, l2) as float-float numbers (about 48 significant bits)
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float h2, float l2) {
+    float s, e;
+    two_sum(hi, h2, s, e);
+    e = __fadd_rn(e, __fadd_rn(lo, l2));
+    two_sum(s, e, hi, lo);
+}
+// Float-float sum over the warp by a fixed shuffle tree; lane 0 holds the total.  Sums that the
+// path used to form in FP64 are formed this way on the FP32 pipe (GB300 issues an FP64
+// instruction, conversions included, at a small fraction of the FP32 rate).
+__device__ __forceinline__ void warp_sum_ff(float& hi, float& lo) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float oh = __shfl_down_sync(0xffffffffu, hi, off);
+        const float ol = __shfl_down_sync(0xffffffffu, lo, off);
+        ff_add(hi, lo, oh, ol);
+    }
+}
+
+
 // ----------------------------------------------------------------------------------
 // Adjoint gradient: SubImage::calcVogelWeight + gradientVogel (subimage.cpp:312-390).
 // With G = conj(O) (D - O S) = (PQ D - PS S) / QS on the OTF support, the reference forms
@@ -513,21 +543,15 @@ __device__ __forceinline__ void project_modes(const KParams<T>& kp, int kind, in
         v[q] = (pf.x * U.y - pf.y * U.x) * wq;
     }
     __syncthreads();
-    // projection on the modes: one warp per mode
+    // projection on the modes: one warp per mode, the lanes' partial sums added as float-float
+    // numbers; then one thread per mode scales the total by the factor of the image's object
+    // and channel
     const int lane = tid & 31, wid = tid >> 5;
     const int mc = kp.modeCount[p];
     const int ch = kp.pImgCh[g];
-    const double c = (double)kp.otfNorm[ch];
-    const double w = kp.objWeight[o];
-    double scale;
-    if (kind == GK_VOGEL) {
-        // X carries the factor c: result = c N^2 (G (*) PF); reference: -2 area w^2 / N^6 * sum
-        scale = -2.0 * kp.area * w * w / ((double)N2 * (double)N2 * (double)N2) / c;
-    } else {
-        scale = -4.0 * c * c * w / ((double)kp.ps * kp.ps * (double)N2) / c;
-    }
+    float2* hl = reinterpret_cast<float2*>(v + n2);     // [M] the modes' sums (hi, lo)
     for (int m = wid; m < kp.M; m += THREADS / 32) {
-        double acc = 0;
+        float hi = 0.f, lo = 0.f;
         if (m < mc) {
             const T* Zm = kp.Z + (size_t)m * n2;
             T part = 0;
@@ -546,11 +570,25 @@ __device__ __forceinline__ void project_modes(const KParams<T>& kp, int kind, in
 #pragma unroll 8
                 for (int q = lane; q < n2; q += 32) part += v[q] * Zm[q];
             }
-            acc = (double)part;
+            if constexpr (sizeof(T) == 4) {
+                hi = (float)part;
+                warp_sum_ff(hi, lo);
+            } else {
+                double acc = (double)part;
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+                for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+                if (lane == 0) reinterpret_cast<double*>(hl)[m] = acc;
+            }
         }
-        if (lane == 0) kp.galpha[g * kp.M + m] = (m < mc) ? acc * scale : 0.0;
+        if (sizeof(T) == 4 && lane == 0) hl[m] = make_float2(hi, lo);
+    }
+    __syncthreads();
+    const double scale = kp.gradScale[((size_t)(kind == GK_VOGEL ? 0 : 1) * kp.nObj + o) * kp.nCh + ch];
+    for (int m = tid; m < kp.M; m += THREADS) {
+        double acc;
+        if constexpr (sizeof(T) == 4) acc = (double)hl[m].x + (double)hl[m].y;
+        else acc = reinterpret_cast<const double*>(hl)[m];
+        kp.galpha[g * kp.M + m] = (m < mc) ? acc * scale : 0.0;
     }
 }
 

@@ -95,6 +95,8 @@ template <typename T, int N> struct EvalLauncher {
     static void fd_half(const EvalParams<T>& e, int grid, cudaStream_t st);
 };
 template <typename T> void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st);
+constexpr size_t kCgStageBytes = 96 * 1024;   // shared memory of the staged solver kernel, at most
+template <typename T> cudaError_t setup_cg(size_t stageBytes);   // opt in to it
 cudaError_t query_nsmid(int32_t* dOut, int32_t* hOut, cudaStream_t st);   // %nsmid of the device
 void launch_shift(const ShiftArgs& a, int P, cudaStream_t st);
 

@@ -296,10 +296,13 @@ class Solver:
                                                        adjoint=ms[4:6].tolist()))
 
     def set_launch_shape(self, eval_threads: int = 0, forward_threads: int = 0, adjoint_threads: int = 0,
-                         eval_radix: int = 0, forward_radix: int = 0, adjoint_radix: int = 0) -> None:
+                         eval_radix: int = 0, forward_radix: int = 0, adjoint_radix: int = 0,
+                         solver_form: int = 0) -> None:
         """Pins the threads per block and the radix plans (first radix) of k_eval, k_forward
-        and k_adjoint (0: keep)."""
-        sh = _lib.LaunchShape(eval_threads, forward_threads, adjoint_threads, eval_radix, forward_radix, adjoint_radix)
+        and k_adjoint, and the solver kernel's form (1 staged in shared memory, 2 global
+        memory); 0 keeps."""
+        sh = _lib.LaunchShape(eval_threads, forward_threads, adjoint_threads, eval_radix, forward_radix, adjoint_radix,
+                              solver_form)
         self._check(_lib.load().rdxg_set_launch_shape(self.h, C.byref(sh)), "rdxg_set_launch_shape")
 
     def launch_shape(self) -> dict:
@@ -308,7 +311,8 @@ class Solver:
         sh = _lib.LaunchShape()
         self._check(_lib.load().rdxg_get_launch_shape(self.h, C.byref(sh)), "rdxg_get_launch_shape")
         return dict(eval=sh.eval_threads, forward=sh.forward_threads, adjoint=sh.adjoint_threads,
-                    eval_radix=sh.eval_radix, forward_radix=sh.forward_radix, adjoint_radix=sh.adjoint_radix)
+                    eval_radix=sh.eval_radix, forward_radix=sh.forward_radix, adjoint_radix=sh.adjoint_radix,
+                    solver_form=sh.solver_form)
 
     def launch_count(self) -> int:
         return int(_lib.load().rdxg_last_launch_count(self.h))
