@@ -61,6 +61,7 @@ struct rdxg_solver {
     // solver state
     CgState* dStates = nullptr;
     double *dVec = nullptr, *dMetrics = nullptr, *dAlpha = nullptr, *dAlphaOff = nullptr;
+    float* dAlphaOffF = nullptr;      // [P][nPar] alpha offsets rounded to float
     int32_t* dActive = nullptr;
     int32_t* hActive = nullptr;   // pinned
     int maxMetrics = 0;
@@ -410,6 +411,7 @@ CgArgs<T> make_cgargs(rdxg_solver* h, const CgParams& prm) {
     a.prm = prm;
     a.P = h->P; a.I = h->I; a.M = h->M; a.nObj = h->nObj; a.nPar = h->nPar; a.nTiles = h->nTiles; a.ps = h->ps;
     a.states = h->dStates; a.vec = h->dVec; a.metrics = h->dMetrics; a.alpha = h->dAlpha; a.alphaOff = h->dAlphaOff;
+    a.alphaOffF = h->dAlphaOffF;
     a.galpha = h->dGalpha; a.partial = h->dPartial; a.objWeight = h->dObjW;
     a.pgeo = h->dPGeo;
     a.rowPtr = h->dRowPtr; a.rowCol = h->dRowCol; a.rowVal = h->dRowVal; a.rowVal32 = h->dRowVal32;
@@ -497,9 +499,11 @@ int alloc_patch_buffers(rdxg_solver* h) {
         (r = dalloc_t(h, &h->dCurTilt, G * 2)) || (r = dalloc_t(h, &h->dResAlpha, G * 2)) ||
         (r = dalloc_t(h, &h->dStates, P)) || (r = dalloc_t(h, &h->dVec, P * 5 * h->nFree)) ||
         (r = dalloc_t(h, &h->dAlpha, P * h->nPar)) || (r = dalloc_t(h, &h->dAlphaOff, P * h->nPar)) ||
+        (r = dalloc_t(h, &h->dAlphaOffF, P * h->nPar)) ||
         (r = dalloc_t(h, &h->dActive, 1)) || (r = dalloc_t(h, &h->dGradP, P)) || (r = dalloc_t(h, &h->dFdP, P)) ||
         (r = dalloc_t(h, &h->dEvalP, P)) || (r = dalloc_t(h, &h->dCounters, kNumCounters)))
         return r;
+    CK(h, cudaMemset(h->dCounters, 0, kNumCounters * sizeof(int32_t)));
     CK(h, cudaMallocHost((void**)&h->hActive, sizeof(int32_t)));
     CK(h, cudaMemset(h->dReinit, 0, G));
     return RDXG_OK;
@@ -1701,6 +1705,8 @@ int prepare_solve(rdxg_solver* h, const rdxg_solve_params* s, SolvePlan& pl) {
     if (h->haveInit)   // alpha_offset = the initial coefficients
         CK(h, cudaMemcpyAsync(h->dAlphaOff, h->dInitAlpha, (size_t)P * h->nPar * sizeof(double),
                               cudaMemcpyDeviceToDevice, h->stream));
+    launch_to_float(h->dAlphaOff, h->dAlphaOffF, (size_t)P * h->nPar, h->stream);
+    CKL(h);
     pl.sa = make_shift_args(h);
     // the solver kernel stages its patch's data in shared memory when it fits
     size_t bytes = 0;

@@ -85,6 +85,7 @@ struct CgArgs {
     double* metrics;        // [P][max_metrics]
     double* alpha;          // [P][nPar]
     double* alphaOff;       // [P][nPar]
+    float* alphaOffF;       // [P][nPar] alphaOff rounded to float (the FP32 map's offsets)
     const double* galpha;   // [P][nPar]
     const double* partial;  // [P][nObj][nTiles]
     const double* objWeight;
@@ -124,7 +125,7 @@ struct CgArgs {
 // alpha = offset + N x1; alpha_eff = alpha + currentTiltOffset - residual for the tilt modes
 // (the residual is what Channel::initPatch adds to phi_channel, channel.cpp:916-939)
 template <typename T, int THREADS>
-__device__ void map_point(const CgArgs<T>& a, int p, const double* x1) {
+__device__ void map_point(const CgArgs<T>& a, int p, const double* x1, bool writeEff = true) {
     const double* off = a.alphaOff + (size_t)p * a.nPar;
     double* al = a.alpha + (size_t)p * a.nPar;
     T* ae = a.alphaEff + (size_t)p * a.nPar;
@@ -133,6 +134,7 @@ __device__ void map_point(const CgArgs<T>& a, int p, const double* x1) {
         double v = off[r];
         for (int e = rp[r]; e < rp[r + 1]; ++e) v += a.rowVal[e] * x1[a.rowCol[e]];
         al[r] = v;
+        if (!writeEff) continue;
         const int j = r / a.M, m = r % a.M;
         double ve = v;
         const size_t b = ((size_t)p * a.I + j) * 2;
@@ -143,10 +145,12 @@ __device__ void map_point(const CgArgs<T>& a, int p, const double* x1) {
     __syncthreads();
 }
 
-// The FP32 path's metric requests: alphaEff only, in FP32 arithmetic (it is rounded to FP32
-// for the evaluation anyway), with the point staged in shared memory as float.  GB300's FP64
-// rate makes the FP64 map the largest cost of the solver kernel; the FP64 alpha is formed by
-// map_point for every gradient, re-shift and final point, where it is used.
+// The FP32 path's metric and gradient requests: alphaEff in FP32 arithmetic (it is rounded to
+// FP32 for the evaluation anyway), with the point staged in shared memory as float and the
+// offsets kept as float.  GB300 issues an FP64 instruction in 64 cycles per warp and a
+// double-to-float conversion in about 160, whatever the number of active lanes, which makes
+// the FP64 map the largest cost of the solver kernel; the FP64 alpha is formed by map_point
+// (without alphaEff) for every gradient, re-shift and final point, where it is used.
 template <typename T, int THREADS>
 __device__ void map_point_f32(const CgArgs<T>& a, int p, const double* x1, float* xs) {
     const int nF = a.pgeo[p].nFree;
@@ -154,14 +158,14 @@ __device__ void map_point_f32(const CgArgs<T>& a, int p, const double* x1, float
         for (int c = threadIdx.x; c < nF; c += THREADS) xs[c] = (float)x1[c];
         __syncthreads();
     }
-    const double* off = a.alphaOff + (size_t)p * a.nPar;
+    const float* off = a.alphaOffF + (size_t)p * a.nPar;
     T* ae = a.alphaEff + (size_t)p * a.nPar;
     const int32_t* rp = a.rowPtr + a.pgeo[p].rowBase;
     for (int r = threadIdx.x; r < a.nPar; r += THREADS) {
         float v = 0.f;
         for (int e = rp[r]; e < rp[r + 1]; ++e)
             v = fmaf(a.rowVal32[e], xs ? xs[a.rowCol[e]] : (float)x1[a.rowCol[e]], v);
-        v += (float)off[r];
+        v += off[r];
         const int j = r / a.M, m = r % a.M;
         const size_t b = ((size_t)p * a.I + j) * 2;
         if (m == a.tiltX) v += (float)(a.curTilt[b + 1] - a.resAlpha[b + 1]);
@@ -173,8 +177,8 @@ __device__ void map_point_f32(const CgArgs<T>& a, int p, const double* x1, float
 
 // Shared-memory layout (bytes) of the staged solver kernel: the patch's five vectors, its
 // object metric tiles, the object weights, its reference-object flags and object tables, and
-// (stageMap) its row map (row pointers, entry values and columns), alpha offsets, the tilt
-// terms of its images (currentTiltOffset, channel residual) and the point as float.
+// (stageMap) its row map (row pointers, entry values and columns), alpha offsets (float), the
+// tilt terms of its images (currentTiltOffset, channel residual) and the point as float.
 struct CgStageLayout {
     size_t om, ow, off, tilt, ints, rp, ec, ev, xs, total;
     __host__ __device__ CgStageLayout(int stride, int nObj, int nT, int stageMap, int nPar, int I, int maxNnz) {
@@ -182,7 +186,7 @@ struct CgStageLayout {
         om = (size_t)5 * stride * d;
         ow = om + (size_t)nObj * nT * d;
         off = ow + (size_t)nObj * d;
-        tilt = off + (stageMap ? (size_t)nPar * d : 0);
+        tilt = (off + (stageMap ? (size_t)nPar * sizeof(float) : 0) + 7) & ~(size_t)7;
         ints = tilt + (stageMap ? (size_t)4 * I * d : 0);
         rp = ints + (size_t)(2 + 3 * nObj) * i4;
         ec = rp + (stageMap ? (size_t)(nPar + 1) * i4 : 0);
@@ -198,7 +202,7 @@ struct CgStageLayout {
 // point as float, converted once per free parameter).
 template <typename T, int THREADS>
 __device__ void map_rows_staged(const CgArgs<T>& a, int p, const double* x1, const int32_t* rps, const int32_t* ec,
-                                const float* ev, const double* offs, const double* tilt, float* xs, int nF) {
+                                const float* ev, const float* offs, const double* tilt, float* xs, int nF) {
     for (int c = threadIdx.x; c < nF; c += THREADS) xs[c] = (float)x1[c];
     __syncthreads();
     T* ae = a.alphaEff + (size_t)p * a.nPar;
@@ -208,7 +212,7 @@ __device__ void map_rows_staged(const CgArgs<T>& a, int p, const double* x1, con
     for (int r = threadIdx.x; r < a.nPar; r += THREADS) {
         float v = 0.f;
         for (int e = rps[r] - e0; e < rps[r + 1] - e0; ++e) v = fmaf(ev[e], xs[ec[e]], v);
-        v += (float)offs[r];
+        v += offs[r];
         const int j = r / a.M, m = r % a.M;
         if (m == a.tiltX) v += (float)(cur[2 * j + 1] - res[2 * j + 1]);
         else if (m == a.tiltY) v += (float)(cur[2 * j + 0] - res[2 * j + 0]);
@@ -277,7 +281,7 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
     int32_t* rps = reinterpret_cast<int32_t*>(cg_smem + lay.rp);
     int32_t* ec = reinterpret_cast<int32_t*>(cg_smem + lay.ec);
     float* ev = reinterpret_cast<float*>(cg_smem + lay.ev);
-    double* offs = reinterpret_cast<double*>(cg_smem + lay.off);
+    float* offs = reinterpret_cast<float*>(cg_smem + lay.off);
     double* tilt = reinterpret_cast<double*>(cg_smem + lay.tilt);
     int e0 = 0;
     if (ST) {
@@ -306,8 +310,8 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
             // the FP32 map's operands: row pointers, alpha offsets, tilt terms (the entries
             // follow once their range is known)
             for (int r = threadIdx.x; r <= a.nPar; r += THREADS) cp_async4(rps + r, rp + r);
-            const double* off = a.alphaOff + (size_t)p * a.nPar;
-            for (int r = threadIdx.x; r < a.nPar; r += THREADS) cp_async8(offs + r, off + r);
+            const float* off = a.alphaOffF + (size_t)p * a.nPar;
+            for (int r = threadIdx.x; r < a.nPar; r += THREADS) cp_async4(offs + r, off + r);
             const size_t b = (size_t)p * a.I * 2;
             for (int i = threadIdx.x; i < 2 * a.I; i += THREADS) {
                 cp_async8(tilt + i, a.curTilt + b + i);
@@ -414,10 +418,14 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
         __syncthreads();
     } else if (req0 == REQ_SHIFT) {
         double* off = a.alphaOff + (size_t)p * a.nPar;
+        float* offF = a.alphaOffF + (size_t)p * a.nPar;
         const double* al = a.alpha + (size_t)p * a.nPar;
-        for (int r = threadIdx.x; r < a.nPar; r += THREADS) off[r] = al[r];
-        if (ST && a.stageMap)
-            for (int r = threadIdx.x; r < a.nPar; r += THREADS) offs[r] = al[r];
+        for (int r = threadIdx.x; r < a.nPar; r += THREADS) {
+            const double v = al[r];
+            off[r] = v;
+            offF[r] = (float)v;
+            if (ST && a.stageMap) offs[r] = (float)v;
+        }
         __syncthreads();
     }
     __shared__ int rqShared;
@@ -439,12 +447,16 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
     const int rq = rqShared;
     if (sizeof(T) == sizeof(float) && a.x1Smem) {
         extern __shared__ float xs[];
-        if (rq == REQ_F) {
+        // the FP32 map forms alphaEff of metric and gradient points alike (a gradient point is
+        // evaluated where a metric request at it would be); a gradient point also gets alpha
+        // in FP64, without the conversions to float
+        if (rq == REQ_F || rq == REQ_DF) {
             if (ST && a.stageMap)
                 map_rows_staged<T, THREADS>(a, p, x1, rps, ec, ev, offs, tilt,
                                             reinterpret_cast<float*>(cg_smem + lay.xs), nF);
             else map_point_f32<T, THREADS>(a, p, x1, ST ? nullptr : xs);
-        } else if (rq == REQ_DF || rq == REQ_SHIFT || rq == REQ_DONE) {
+            if (rq == REQ_DF) map_point<T, THREADS>(a, p, x1, false);
+        } else if (rq == REQ_SHIFT || rq == REQ_DONE) {
             map_point<T, THREADS>(a, p, x1);
         }
     } else if (rq == REQ_F || rq == REQ_DF || rq == REQ_SHIFT) {

@@ -37,9 +37,11 @@ struct PoItem {
 // half-plane points per work item of the object reduction (k_reduce): four per lane
 constexpr int kReduceTile = 128;
 
-// work-list counters (reset every round)
+// work-list counters (reset every round); the evaluation's claim and finished-block counters
+// are reset by the evaluation itself (its last block), so that it can be launched again on the
+// same lists
 enum : int32_t { kCounterEval = 0, kCounterPo = 1, kCounterGrad = 2, kCounterFd = 3, kCounterEvalP = 4,
-                 kCounterShift = 5 };
+                 kCounterShift = 5, kCounterEvalClaim = 6, kCounterEvalDone = 7 };
 
 struct Lists {
     EvalItem* eval;  int32_t* nEval;
@@ -424,8 +426,26 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
     uint16_t* hpos = reinterpret_cast<uint16_t*>(phiBuf + n2);
     static_assert(Tile<N>::ELEMS <= 65536, "tile positions are 16-bit");
     const int nItems = *e.L.nEval;
+    // Work items: the block's first two by block index, then claimed from a counter one item
+    // ahead (so the claim's latency is hidden behind a whole item), so that blocks that start
+    // late (the SMs busy with another handle's kernels) take fewer items.  Each item's sums are
+    // the same whichever block forms them.
+    __shared__ int claimSh;
+    auto finish = [&] {
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(e.L.counters + kCounterEvalDone, 1) == (int)gridDim.x - 1) {
+                e.L.counters[kCounterEvalClaim] = 0;
+                e.L.counters[kCounterEvalDone] = 0;
+            }
+        }
+    };
     int item = blockIdx.x;
-    if (item >= nItems) return;
+    if (item >= nItems) {
+        finish();
+        return;
+    }
+    int next = item + (int)gridDim.x;
     load_twiddles<T, N>(tw, e.k.tw);
     for (int h = threadIdx.x; h < nH; h += THREADS) hpos[h] = (uint16_t)e.hPos[h];
     for (int q = threadIdx.x; q < n2; q += THREADS) amp[q] = e.k.A[q];
@@ -434,10 +454,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
     cp_async_commit();
     cp_async_wait_all();
     int jj = 0;
+    int myClaim = 0;    // thread 0: the item claimed while this one runs
     while (true) {
         const size_t po = (size_t)it.p * e.k.nObj + it.o;
         if (jj == 0) {
             __syncthreads();    // previous item's accumulators written out
+            if (threadIdx.x == 0) myClaim = 2 * (int)gridDim.x + atomicAdd(e.L.counters + kCounterEvalClaim, 1);
             for (int h = threadIdx.x; h < nH; h += THREADS) {
                 oh[h] = e.Oh[po * nH + h];
                 acc[h] = Acc4<T>{0, 0, 0, 0};
@@ -447,7 +469,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
         int nextItem = item, nextJj = jj + 1;
         EvalItem nit = it;
         if (nextJj >= it.count) {
-            nextItem = item + gridDim.x;
+            nextItem = next;
             nextJj = 0;
             if (nextItem < nItems) nit = e.L.eval[nextItem];
         }
@@ -461,15 +483,19 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
                                   it.df && e.k.S != nullptr, e.k.PF + g * n2, e.k.X + g * N2,
                                   e.k.S + g * N2, e.Dh + g * nH, s, s2, tw, oh, acc, hpos, e.hp.idx, nH);
         if (nextJj == 0) {
+            if (threadIdx.x == 0) claimSh = myClaim;
             __syncthreads();
+            const int claimed = claimSh;
             Acc4<T>* part = e.part + (size_t)(it.p * e.hp.chunksPerPatch + it.chunk) * nH;
             for (int h = threadIdx.x; h < nH; h += THREADS) part[h] = acc[h];
             if (nextItem >= nItems) break;
             item = nextItem;
             it = nit;
+            next = claimed;
         }
         jj = nextJj;
     }
+    finish();
 }
 
 // ----------------------------------------------------------------------------------

@@ -26,6 +26,15 @@ cudaError_t setup_cg(size_t stageBytes) {
     return raise_smem_limit(k_cg<T, kCgThreads, true>, stageBytes);
 }
 
+__global__ void k_to_float(const double* src, float* dst, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+void launch_to_float(const double* src, float* dst, size_t n, cudaStream_t st) {
+    const size_t blocks = (n + 255) / 256;
+    if (blocks) k_to_float<<<(int)(blocks < 4096 ? blocks : 4096), 256, 0, st>>>(src, dst, n);
+}
+
 void launch_shift(const ShiftArgs& a, int P, cudaStream_t st) {
     k_shift<0><<<P, 128, 0, st>>>(a);
 }

@@ -81,7 +81,7 @@ constexpr int kPhaseRegPix = 128;   // pixels per block of the per-patch mode ex
 constexpr int kPhaseRegModes = 64;  // modes it holds in registers (more: the staged kernel)
 constexpr int kPhaseMaxImg = 64;    // images per patch it stages
 constexpr int kPhaseMaxCh = 16;     // channels whose fixed phases it stages
-constexpr int kNumCounters = 6;     // work-list counters reset every round
+constexpr int kNumCounters = 8;     // work-list counters reset every round (and the evaluation's two)
 constexpr size_t kMaxSmem = 227 * 1024;   // dynamic shared memory per block
 template <typename T, int N> struct EvalLauncher {
     static cudaError_t setup(int M, int npt, int nH);
@@ -99,6 +99,7 @@ constexpr size_t kCgStageBytes = 96 * 1024;   // shared memory of the staged sol
 template <typename T> cudaError_t setup_cg(size_t stageBytes);   // opt in to it
 cudaError_t query_nsmid(int32_t* dOut, int32_t* hOut, cudaStream_t st);   // %nsmid of the device
 void launch_shift(const ShiftArgs& a, int P, cudaStream_t st);
+void launch_to_float(const double* src, float* dst, size_t n, cudaStream_t st);   // dst = (float)src
 
 // The device loop of a solve graph: a WHILE node whose body runs roundsPerIteration rounds of
 // every handle and then k_loop_cond, which keeps the loop going while a handle has an active
