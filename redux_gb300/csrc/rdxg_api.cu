@@ -920,6 +920,10 @@ int setup_fused(rdxg_solver* h, const rdxg_static* s) {
     h->nTilesH = (h->nH + kReduceTile - 1) / kReduceTile;
     h->npt = 1;
     if (h->nH > N * (N / 2 + 1)) return RDXG_OK;   // more points than the staging area holds
+    // more points than the evaluation's register accumulators hold
+    if (h->nH > (N == 32 ? kFusedMaxPoints<32>::value : N == 64 ? kFusedMaxPoints<64>::value
+                                                                 : kFusedMaxPoints<88>::value))
+        return RDXG_OK;
     const size_t smem = N == 32 ? EvalLauncher<float, 32>::smem(h->M, h->nH)
                       : N == 64 ? EvalLauncher<float, 64>::smem(h->M, h->nH)
                                 : EvalLauncher<float, 88>::smem(h->M, h->nH);

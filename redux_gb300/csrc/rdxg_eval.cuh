@@ -34,6 +34,14 @@ struct PoItem {
     int32_t p, o, mode;   // mode: 0 metric, 1 gradient (write O, Qt), 2 refresh O'
 };
 
+// Half-plane points the fused evaluation takes at most: the half plane, capped at 3584 (seven
+// accumulator records per thread of a 512-thread block, in registers).  A circular pupil's
+// OTF support has about 0.42 N^2 of them (3237 at N = 88).
+template <int N> struct kFusedMaxPoints {
+    static constexpr int half = N * (N / 2 + 1);
+    static constexpr int value = half < 3584 ? half : 3584;
+};
+
 // half-plane points per work item of the object reduction (k_reduce): four per lane
 constexpr int kReduceTile = 128;
 
@@ -349,14 +357,15 @@ __device__ __forceinline__ void acc_point(Acc4<T>& u, cx<T> d, cx<T> o, cx<T> s,
 }
 
 // One image of a chunk: the OTF on the half plane (half_plane_core with elem = |X|^2),
-// folded into the chunk's accumulators.  On entry the phases of this image are in phiBuf;
-// phiNext (or null) is the next image's, fetched into phiBuf once the row pass has read it.
-template <typename T, int N, int THREADS, typename PL = Plan<N>>
+// folded into the chunk's accumulators, which live in registers: thread t holds the records of
+// the points t + i * THREADS.  On entry the phases of this image are in phiBuf; phiNext (or
+// null) is the next image's, fetched into phiBuf once the row pass has read it.
+template <typename T, int N, int THREADS, int ACC, typename PL = Plan<N>>
 __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phiBuf, const T* A, T c, int keepPX,
                                            int keepS,
                                            cx<T>* PF, cx<T>* X, cx<T>* S, const cx<T>* __restrict__ Dg,
                                            cx<T>* a, cx<T>* b, const cx<T>* tw, const cx<T>* oh,
-                                           Acc4<T>* acc, const uint16_t* hpos, const int* hidx, int nH) {
+                                           Acc4<T> (&acc)[ACC], const uint16_t* hpos, const int* hidx, int nH) {
     constexpr int n = N / 2, N2 = N * N;
     static_assert(sizeof(cx<T>) == 8, "staging copies 8-byte elements");
     using St = Stage<N>;
@@ -399,11 +408,13 @@ __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phi
             S[((N - cy) % N) * N + (N - cxx) % N] = mkc<T>(v.x, -v.y);
         }
     }
-    for (int h = threadIdx.x; h < nH; h += THREADS) {
-        const cx<T> d = (h < St::kPart ? a : b)[St::dh_slot(h)];
-        Acc4<T> u = acc[h];
-        acc_point<T>(u, d, oh[h], a[hpos[h]], inv);
-        acc[h] = u;
+#pragma unroll
+    for (int i = 0; i < ACC; ++i) {
+        const int h = (int)threadIdx.x + i * THREADS;
+        if (h < nH) {
+            const cx<T> d = (h < St::kPart ? a : b)[St::dh_slot(h)];
+            acc_point<T>(acc[i], d, oh[h], a[hpos[h]], inv);
+        }
     }
 }
 
@@ -413,14 +424,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
     constexpr int n = N / 2, n2 = n * n, N2 = N * N;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nH = e.hp.nH;
-    // shared memory: two tiles | twiddles | accumulators (nH records) | reference object |
-    //                pupil amplitude | phases of the image | tile positions (16-bit)
+    // shared memory: two tiles | twiddles | reference object | pupil amplitude | phases of
+    //                the image | tile positions (16-bit)
     cx<T>* s = reinterpret_cast<cx<T>*>(smem_raw);
     cx<T>* s2 = s + Tile<N>::ELEMS;
     cx<T>* tw = s2 + Tile<N>::ELEMS;
-    Acc4<T>* acc = reinterpret_cast<Acc4<T>*>(tw + N);
-    static_assert((2 * Tile<N>::ELEMS + N) % 2 == 0, "accumulator records 16-byte aligned");
-    cx<T>* oh = reinterpret_cast<cx<T>*>(acc + nH);
+    cx<T>* oh = tw + N;
+    // the chunk's accumulators (R, Q, P') of the points threadIdx.x + i * THREADS
+    constexpr int ACC = (kFusedMaxPoints<N>::value + THREADS - 1) / THREADS;
+    Acc4<T> acc[ACC];
     T* amp = reinterpret_cast<T*>(oh + nH);
     T* phiBuf = amp + n2;
     uint16_t* hpos = reinterpret_cast<uint16_t*>(phiBuf + n2);
@@ -460,10 +472,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
         if (jj == 0) {
             __syncthreads();    // previous item's accumulators written out
             if (threadIdx.x == 0) myClaim = 2 * (int)gridDim.x + atomicAdd(e.L.counters + kCounterEvalClaim, 1);
-            for (int h = threadIdx.x; h < nH; h += THREADS) {
-                oh[h] = e.Oh[po * nH + h];
-                acc[h] = Acc4<T>{0, 0, 0, 0};
-            }
+            for (int h = threadIdx.x; h < nH; h += THREADS) oh[h] = e.Oh[po * nH + h];
+#pragma unroll
+            for (int i = 0; i < ACC; ++i) acc[i] = Acc4<T>{0, 0, 0, 0};
         }
         // the image after this one (same item, or the first of the block's next item)
         int nextItem = item, nextJj = jj + 1;
@@ -479,7 +490,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
         const int ch = e.k.pImgCh[g];
         // a gradient evaluation keeps PF, X and the full OTF for the gradient kernels, unless
         // they recompute them (the OTF is still kept when a buffer for it is given)
-        eval_image<T, N, THREADS, PL>(phiNext, phiBuf, amp, e.k.otfNorm[ch], it.df && !e.k.recompute,
+        eval_image<T, N, THREADS, ACC, PL>(phiNext, phiBuf, amp, e.k.otfNorm[ch], it.df && !e.k.recompute,
                                   it.df && e.k.S != nullptr, e.k.PF + g * n2, e.k.X + g * N2,
                                   e.k.S + g * N2, e.Dh + g * nH, s, s2, tw, oh, acc, hpos, e.hp.idx, nH);
         if (nextJj == 0) {
@@ -487,7 +498,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_eval(EvalParams<T> e) {
             __syncthreads();
             const int claimed = claimSh;
             Acc4<T>* part = e.part + (size_t)(it.p * e.hp.chunksPerPatch + it.chunk) * nH;
-            for (int h = threadIdx.x; h < nH; h += THREADS) part[h] = acc[h];
+#pragma unroll
+            for (int i = 0; i < ACC; ++i) {
+                const int h = (int)threadIdx.x + i * THREADS;
+                if (h < nH) part[h] = acc[i];
+            }
             if (nextItem >= nItems) break;
             item = nextItem;
             it = nit;

@@ -268,14 +268,17 @@ __device__ __forceinline__ void fft2d(cx<T>* s, const cx<T>* tw) {
 // ---- ping-pong variant: out-of-place stages between two tiles (a -> b -> a), one barrier
 // per stage and one butterfly in registers at a time ----
 // RLO, RHI: only inputs r in [RLO, RHI) of each butterfly can be non-zero (the others are
-// known zeros and are neither loaded nor multiplied)
+// known zeros and are neither loaded nor multiplied).  The loop over a thread's butterflies is
+// not unrolled: the fused evaluation keeps its accumulators in registers, and two butterflies
+// in flight would spill them (measured: 0.430 ms per 8100-image evaluation against 0.479 ms
+// unrolled by 2 with spills, 0.452 ms unrolled by 2 with the accumulators in shared memory).
 template <typename T, int N, int R, int NS, int DIR, int LINES, int THREADS, int RLO = 0, int RHI = R>
 __device__ __forceinline__ void fft_stage_pp(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst, int line0,
                                              int lstride, int estride, const cx<T>* tw) {
     constexpr int BF = N / R;
     constexpr int TOTAL = LINES * BF;
     constexpr int TWS = N / (NS * R);
-#pragma unroll 2
+#pragma unroll 1
     for (int b = threadIdx.x; b < TOTAL; b += THREADS) {
         const int line = line0 + b % LINES;
         const int j = b / LINES;
@@ -311,7 +314,7 @@ __device__ __forceinline__ void fft_stage_fn(int line0, const cx<T>* tw, LD ld, 
     constexpr int BF = N / R;
     constexpr int TOTAL = LINES * BF;
     constexpr int TWS = N / (NS * R);
-#pragma unroll 2
+#pragma unroll 1
     for (int b = threadIdx.x; b < TOTAL; b += THREADS) {
         const int line = line0 + b % LINES;
         const int j = b / LINES;

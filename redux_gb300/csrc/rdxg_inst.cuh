@@ -187,10 +187,10 @@ cudaError_t Launcher<T, N>::restore_outputs(const KParams<T>& kp, const RestoreO
 template <typename T, int N>
 size_t EvalLauncher<T, N>::smem(int M, int nH) {
     (void)M;
-    // two tiles | twiddles | accumulators (4 x nH) | reference object | pupil amplitude |
-    // phases of the image | tile positions (16-bit)
-    return (size_t)(2 * Tile<N>::ELEMS + N + nH) * sizeof(cx<T>) + (size_t)4 * nH * sizeof(T) +
-           (size_t)2 * (N / 2) * (N / 2) * sizeof(T) + (size_t)nH * sizeof(uint16_t) + 16;
+    // two tiles | twiddles | reference object | pupil amplitude | phases of the image | tile
+    // positions (16-bit); the accumulators live in registers
+    return (size_t)(2 * Tile<N>::ELEMS + N + nH) * sizeof(cx<T>) + (size_t)2 * (N / 2) * (N / 2) * sizeof(T) +
+           (size_t)nH * sizeof(uint16_t) + 16;
 }
 
 #define RDXG_NPT_SWITCH(npt, CALL) \
