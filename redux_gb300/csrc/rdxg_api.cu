@@ -2237,9 +2237,10 @@ int plan_shapes(rdxg_solver* h, int reps, double* ms) {
     const int nGrad[3] = {0, 0, std::max(1, (h->P + 9) / 10)};
     const bool altPlan = radix_of(h->N, 1) != 0;
     int r = RDXG_OK;
+    double all[3][4] = {};
     for (int f = 0; f < 3 && !r; ++f) {
         if (!used[f]) { *field[f] = 0; continue; }
-        double tv[4] = {0, 0, 0, 0};
+        double* tv = all[f];
         bool avail[4];
         for (int v = 0; v < 4; ++v) {
             const int plan = v >> 1;
@@ -2275,8 +2276,10 @@ int plan_shapes(rdxg_solver* h, int reps, double* ms) {
         plan_wisdom().emplace(plan_key(h), ShapeChoice{h->shapeEval, h->shapeFwd, h->shapeAdj});
     }
     if (getenv("RDXG_VERBOSE"))
-        fprintf(stderr, "launch shapes (N %d, P %d): eval %d [%.3f %.3f ms], forward %d [%.3f %.3f], adjoint %d "
-                "[%.3f %.3f]\n", h->N, h->P, h->shapeEval, t[0], t[1], h->shapeFwd, t[2], t[3], h->shapeAdj, t[4], t[5]);
+        fprintf(stderr, "launch shapes (N %d, P %d): eval %d [%.3f %.3f | %.3f %.3f ms], forward %d [%.3f %.3f | %.3f "
+                "%.3f], adjoint %d [%.3f %.3f | %.3f %.3f] (plan 0: threads, alternative threads | plan 1)\n", h->N,
+                h->P, h->shapeEval, all[0][0], all[0][1], all[0][2], all[0][3], h->shapeFwd, all[1][0], all[1][1],
+                all[1][2], all[1][3], h->shapeAdj, all[2][0], all[2][1], all[2][2], all[2][3]);
     if (ms) std::memcpy(ms, t, sizeof(t));
     return RDXG_OK;
 }

@@ -268,9 +268,9 @@ __device__ __forceinline__ void stage_phi(T* buf, const T* __restrict__ phi_g) {
     for (int p = threadIdx.x; p < pairs; p += THREADS) cp_async8(buf + 2 * p, phi_g + 2 * p);
 }
 
-// Half-plane OTF core.  pupil(y, x) gives the pupil-plane field at pupil pixel (y, x)
-// (embedded at rows and columns [N/4, 3N/4)); it is read by the first stage of the row pass,
-// which loads only those columns.  The column pass loads only those rows in its first stage;
+// Half-plane OTF core.  On entry tile a holds the pupil-plane field at rows and columns
+// [N/4, 3N/4) (the caller embeds it there); the first stage of the row pass loads only those
+// columns of those rows.  The column pass loads only those rows in its first stage;
 // its last stage hands every transform value v at (row e, column x) to elem(e, x, v), which
 // returns a real value (|X|^2 for the OTF) stored as the real (e even) or imaginary (e odd)
 // part of row e/2 of tile a: two real rows packed as one complex row.  The N/2 packed rows are
@@ -280,19 +280,17 @@ __device__ __forceinline__ void stage_phi(T* buf, const T* __restrict__ phi_g) {
 // times the inverse transform in those columns.  afterRows, afterCols1, afterPack run after
 // the row pass, the first column stage and the packing stage (where the caller issues copies
 // into the free parts of the tiles); midColumns runs between the two stages along y.
-template <typename T, int N, int THREADS, typename PL = Plan<N>, typename Pupil, typename Elem, typename HR,
-          typename HC, typename HP, typename HM>
-__device__ __forceinline__ void half_plane_core(cx<T>* a, cx<T>* b, const cx<T>* tw, Pupil pupil, Elem elem,
-                                                HR afterRows, HC afterCols1, HP afterPack, HM midColumns) {
+template <typename T, int N, int THREADS, typename PL = Plan<N>, typename Elem, typename HR, typename HC,
+          typename HP, typename HM>
+__device__ __forceinline__ void half_plane_core(cx<T>* a, cx<T>* b, const cx<T>* tw, Elem elem, HR afterRows,
+                                                HC afterCols1, HP afterPack, HM midColumns) {
     constexpr int LDS = Tile<N>::LDS;
     constexpr int R1 = PL::R1, R2 = PL::R2;
     constexpr int LO = R1 / 4, HI = 3 * R1 / 4;      // non-zero inputs of the pruned first stage
     static_assert(R1 % 4 == 0, "the pruned first stage needs a radix divisible by 4");
     T* af = reinterpret_cast<T*>(a);
     // rows [N/4, 3N/4): the pupil field -> b -> a
-    fft_stage_fn<T, N, R1, 1, -1, N / 2, THREADS, LO, HI>(
-        N / 4, tw, [&](int y, int x) { return pupil(y - N / 4, x - N / 4); },
-        [&](int y, int e, cx<T> v) { b[y * LDS + e] = v; });
+    fft_stage_pp<T, N, R1, 1, -1, N / 2, THREADS, LO, HI>(a, b, N / 4, LDS, 1, tw);
     afterRows();
     fft_stage_pp<T, N, R2, R1, -1, N / 2, THREADS>(b, a, N / 4, LDS, 1, tw);
     // all columns (a -> b), then the last stage into the packed rows of a
@@ -372,32 +370,34 @@ __device__ __forceinline__ void eval_image(const T* __restrict__ phiNext, T* phi
     const T inv = (T)1 / (T)N2;
     __syncthreads();    // previous image's tiles fully consumed, staged phases visible
     const int nFirst = nH < St::kPart ? nH : St::kPart;
-    half_plane_core<T, N, THREADS, PL>(
-        a, b, tw,
-        [&](int y, int x) {
-            const int q = y * n + x;
-            cx<T> pf;
-            const cx<T> v = pupil_field<T>(A[q], phiBuf[q], c, &pf);
-            if (keepPX) PF[q] = pf;
-            return v;
-        },
-        [&](int e, int x, cx<T> v) {
-            if (keepPX) X[e * N + x] = v;
-            return cnorm<T>(v);
-        },
-        [&] {
-            if (phiNext) stage_phi<T, N, THREADS>(phiBuf, phiNext);
-            cp_async_commit();
-        },
-        [&] {
-            for (int h = threadIdx.x; h < nFirst; h += THREADS) cp_async8(a + St::dh_slot(h), Dg + h);
-            cp_async_commit();
-        },
-        [&] {
-            for (int h = nFirst + threadIdx.x; h < nH; h += THREADS) cp_async8(b + St::dh_slot(h), Dg + h);
-            cp_async_commit();
-        },
-        [&] { cp_async_wait_all(); });
+    // c PF of every pupil pixel first, in one balanced pass, into its embedded place in tile a
+    // (rows and columns [N/4, 3N/4), where the first row stage reads it)
+#pragma unroll 1
+    for (int q = threadIdx.x; q < n * n; q += THREADS) {
+        cx<T> pf;
+        const cx<T> v = pupil_field<T>(A[q], phiBuf[q], c, &pf);
+        if (keepPX) PF[q] = pf;
+        a[(q / n + N / 4) * Tile<N>::LDS + q % n + N / 4] = v;
+    }
+    __syncthreads();
+    auto elem = [&](int e, int x, cx<T> v) {
+        if (keepPX) X[e * N + x] = v;
+        return cnorm<T>(v);
+    };
+    auto afterRows = [&] {
+        if (phiNext) stage_phi<T, N, THREADS>(phiBuf, phiNext);
+        cp_async_commit();
+    };
+    auto afterCols1 = [&] {
+        for (int h = threadIdx.x; h < nFirst; h += THREADS) cp_async8(a + St::dh_slot(h), Dg + h);
+        cp_async_commit();
+    };
+    auto afterPack = [&] {
+        for (int h = nFirst + threadIdx.x; h < nH; h += THREADS) cp_async8(b + St::dh_slot(h), Dg + h);
+        cp_async_commit();
+    };
+    auto midColumns = [&] { cp_async_wait_all(); };
+    half_plane_core<T, N, THREADS, PL>(a, b, tw, elem, afterRows, afterCols1, afterPack, midColumns);
     if (keepS) {
         // the full OTF from the half plane (S(-u) = conj S(u)) for the gradient kernels
         for (int h = threadIdx.x; h < nH; h += THREADS) {
@@ -615,16 +615,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_fd_half(EvalParams<T> e) {
             }
             const T* Zm = kp.Z + (size_t)m * n2;
             __syncthreads();    // staged factors visible, previous mode's tiles consumed
+            // c PF (exp(i t) - 1), t = h Z_m, embedded in tile a for the core
+            for (int q = threadIdx.x; q < n2; q += THREADS) {
+                const T t = (T)hstep * Zm[q];
+                T sh, ch2, sn, cs;
+                sincos_t<T>(t * (T)0.5, &sh, &ch2);
+                sincos_t<T>(t, &sn, &cs);
+                a[(q / n + N / 4) * LDS + q % n + N / 4] = cmul<T>(pfs[q], mkc<T>((T)-2 * sh * sh, sn));
+            }
+            __syncthreads();
             half_plane_core<T, N, THREADS>(
                 a, b, tw,
-                [&](int y, int x) {
-                    const int q = y * n + x;
-                    const T t = (T)hstep * Zm[q];
-                    T sh, ch2, sn, cs;
-                    sincos_t<T>(t * (T)0.5, &sh, &ch2);
-                    sincos_t<T>(t, &sn, &cs);
-                    return cmul<T>(pfs[q], mkc<T>((T)-2 * sh * sh, sn));   // c PF (exp(i t) - 1)
-                },
                 [&](int e, int x, cx<T> v) {
                     const cx<T> x0 = Xg[e * N + x];
                     return (T)2 * (x0.x * v.x + x0.y * v.y) + cnorm<T>(v);

@@ -170,7 +170,9 @@ template <> struct Plan<128> { static constexpr int R1 = 16, R2 = 8; };
 // The launch-shape planner's second radix plan of each size (the first is Plan<N>): the same
 // transform with the stages in the other order (or another split), which rounds differently
 // and runs at a different speed.  N = 88 has none (8 * 11 is the only two-stage plan whose
-// first radix is a multiple of 4, which the pruned half-plane transforms need).
+// first radix is a multiple of 4, which the pruned half-plane transforms need; the
+// prime-factor 11 * 8 form, without twiddle factors, was measured slower: 0.493 against
+// 0.424 ms per 8100-image evaluation).
 template <int N> struct PlanAlt : Plan<N> { static constexpr bool exists = false; };
 template <> struct PlanAlt<32> { static constexpr int R1 = 4, R2 = 8; static constexpr bool exists = true; };
 template <> struct PlanAlt<64> { static constexpr int R1 = 16, R2 = 4; static constexpr bool exists = true; };

@@ -132,5 +132,5 @@ def test_radix_plans(case):
     assert np.linalg.norm(g1 - g0) / np.linalg.norm(g0) < 1e-5
     s = S.Solver(w.job, max_patches=1)
     with pytest.raises(S.SolverError, match="not a plan"):
-        s.set_launch_shape(adjoint_radix=11)
+        s.set_launch_shape(adjoint_radix=5)
     s.close()
