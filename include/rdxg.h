@@ -329,7 +329,8 @@ typedef struct {
  * FourierTransform (image/fouriertransform.cpp:73-90, which times candidate plans once per
  * transform size and keeps the fastest): times every compiled shape of each kernel on the
  * loaded batch (reps launches each, CUDA events; the adjoint on the gradient list of a tenth
- * of the patches, the share of a solve round that takes gradients) and keeps the fastest.  The first solve of a
+ * of the patches, the share of a solve round that takes gradients, and of 24 patches at least)
+ * and keeps the fastest.  The first solve of a
  * handle does this by itself (or takes the shapes measured by an earlier handle of the same
  * geometry, device and batch size in this process); RDXG_AUTOTUNE=0 in the environment keeps
  * the default shapes.  FP64 handles have one shape.  chosen (or NULL): the shapes kept;

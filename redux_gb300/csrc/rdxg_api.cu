@@ -2233,8 +2233,10 @@ int plan_shapes(rdxg_solver* h, int reps, double* ms) {
     const bool used[3] = {h->fused, !h->fused, true};
     const int which[3] = {0, 0, 3};
     // a solve round evaluates every active patch but takes the gradients of about one in ten
-    // (the others are in their line searches): the adjoint is timed on such a list
-    const int nGrad[3] = {0, 0, std::max(1, (h->P + 9) / 10)};
+    // (the others are in their line searches): the adjoint is timed on such a list, of at least
+    // 24 patches (on shorter lists the block sizes time alike within the noise, while the
+    // larger one is faster in a solve whose handles run side by side)
+    const int nGrad[3] = {0, 0, std::min(h->P, std::max(24, (h->P + 9) / 10))};
     const bool altPlan = radix_of(h->N, 1) != 0;
     int r = RDXG_OK;
     double all[3][4] = {};
