@@ -148,7 +148,7 @@ __device__ void map_point(const CgArgs<T>& a, int p, const double* x1, bool writ
 // The FP32 path's metric and gradient requests: alphaEff in FP32 arithmetic (it is rounded to
 // FP32 for the evaluation anyway), with the point staged in shared memory as float and the
 // offsets kept as float.  GB300 issues an FP64 instruction in 64 cycles per warp and a
-// double-to-float conversion in about 160, whatever the number of active lanes, which makes
+// double-to-float conversion in about 80, whatever the number of active lanes, which makes
 // the FP64 map the largest cost of the solver kernel; the FP64 alpha is formed by map_point
 // (without alphaEff) for every gradient, re-shift and final point, where it is used.
 template <typename T, int THREADS>
