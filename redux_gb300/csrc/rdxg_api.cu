@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <chrono>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -713,7 +714,8 @@ int upload_geometry(rdxg_solver* h) {
     return RDXG_OK;
 }
 
-// Arguments of the re-shift kernel (SubImage::adjustShifts of patches that request it).
+// Arguments of the re-shifts (SubImage::adjustShifts of patches that request one), done by the
+// solver kernel in the rounds and by k_shift for the initial re-cut of a warm start.
 ShiftArgs make_shift_args(rdxg_solver* h) {
     ShiftArgs sa{};
     sa.P = h->P; sa.I = h->I; sa.M = h->M; sa.nObj = h->nObj; sa.ps = h->ps; sa.cs = h->cs; sa.margin = h->margin;
@@ -1667,7 +1669,7 @@ extern "C++" {
 namespace {
 
 // What a solve of one handle needs once its state is reset: the solver kernel's parameters
-// and the re-shift kernel's arguments.
+// and the re-shifts' arguments.
 struct SolvePlan {
     rdxg_solver* h = nullptr;
     CgParams prm{};
@@ -1719,8 +1721,9 @@ int prepare_solve(rdxg_solver* h, const rdxg_solve_params* s, SolvePlan& pl) {
     return RDXG_OK;
 }
 
-// One round of one handle on stream st: the solver kernel, re-shift, [re-initialisation],
-// evaluation, [adjoint], [finite differences]; optional(k, issue) issues the bracketed kernels.
+// One round of one handle on stream st: the solver kernel (with the re-shifts),
+// [re-initialisation], evaluation, [adjoint], [finite differences]; optional(k, issue) issues
+// the bracketed kernels.
 template <typename Opt>
 int issue_round(const SolvePlan& pl, cudaStream_t st, const ShiftArgs& sar, Opt&& optional) {
     rdxg_solver* h = pl.h;
@@ -1732,8 +1735,7 @@ int issue_round(const SolvePlan& pl, cudaStream_t st, const ShiftArgs& sar, Opt&
         using T = decltype(t);
         KParams<T> kp = make_kparams<T>(h);
         CgArgs<T> ca = make_cgargs<T>(h, pl.prm);
-        launch_cg<T>(ca, P, st);
-        launch_shift(sar, P, st);
+        launch_cg<T>(ca, sar, P, st);    // with the re-shifts of its patches
         optional(0, [&](cudaStream_t s2) {
             // Object::reInitialize: refit the planes of objects with shifted images, then
             // re-initialise their images
@@ -1764,8 +1766,8 @@ int issue_round(const SolvePlan& pl, cudaStream_t st, const ShiftArgs& sar, Opt&
 // joined -- followed by k_loop_cond, which keeps the loop going while any handle has an active
 // patch; the rounds run on the device with no host round trip.  The kernels that are only
 // needed in some rounds (image re-initialisation after a re-shift, the adjoint, the
-// finite-difference gradient) sit in IF nodes inside the body, whose conditions k_shift sets
-// from the round's work-list counters.
+// finite-difference gradient) sit in IF nodes inside the body, whose conditions the last block
+// of the round's solver kernel sets from the round's work-list counters.
 int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
     rdxg_solver* h0 = plans[0].h;
     cudaStream_t origin = h0->stream;
@@ -1803,6 +1805,7 @@ int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
     std::vector<cudaEvent_t> ev(nPlans + 1, nullptr);
     cudaError_t ce = cudaSuccess;
     const char* what = "events";
+    const auto tBuild = std::chrono::steady_clock::now();
     for (size_t k = 0; k <= nPlans && ce == cudaSuccess; ++k) ce = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
     // the top-level graph: one WHILE node (its condition starts at 1 on every launch)
     cudaGraph_t top = nullptr, body = nullptr;
@@ -1847,7 +1850,7 @@ int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
             ShiftArgs sa = pl.sa;
             sa.useConditions = 1;
             sa.counters = h->dCounters;
-            sa.fixedLaunches = (h->fused || h->tcPlan.valid) ? 5 : 4;
+            sa.fixedLaunches = (h->fused || h->tcPlan.valid) ? 4 : 3;
             sa.prepLaunches = h->fitPlane ? 2 : 1;
             sa.launchCount = h->dLaunchCount;
             sa.condPrep = cond[0];
@@ -1926,6 +1929,7 @@ int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
         h0->err = std::string("solver graph (") + what + "): " + cudaGetErrorString(ce);
         r = RDXG_ERR_CUDA;
     }
+    const auto tRun = std::chrono::steady_clock::now();
     if (r == RDXG_OK) {
         int32_t overrun = 0;
         if ((ce = cudaGraphLaunch(exec, origin)) == cudaSuccess &&
@@ -1941,6 +1945,12 @@ int solve_rounds_graph(std::vector<SolvePlan>& plans, int check) {
             h0->err = "solver did not terminate";
             r = RDXG_ERR_STATE;
         }
+    }
+    if (getenv("RDXG_VERBOSE")) {
+        const auto tEnd = std::chrono::steady_clock::now();
+        fprintf(stderr, "solve graph: built and instantiated in %.3f ms, ran in %.3f ms\n",
+                std::chrono::duration<double, std::milli>(tRun - tBuild).count(),
+                std::chrono::duration<double, std::milli>(tEnd - tRun).count());
     }
     if (exec) cudaGraphExecDestroy(exec);
     if (top) cudaGraphDestroy(top);
@@ -1974,7 +1984,7 @@ static int solve_rounds_host(std::vector<SolvePlan>& plans, int check) {
                 h->err = "cudaMemsetAsync failed";
                 return RDXG_ERR_CUDA;
             }
-            h->launches += (h->fused ? 8 : (h->tcPlan.valid ? 8 : 7)) + (h->fitPlane ? 1 : 0);
+            h->launches += (h->fused ? 7 : (h->tcPlan.valid ? 7 : 6)) + (h->fitPlane ? 1 : 0);
             CKL(h);
         }
         if ((round + 1) % check == 0) {

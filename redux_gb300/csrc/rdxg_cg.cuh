@@ -175,6 +175,90 @@ __device__ void map_point_f32(const CgArgs<T>& a, int p, const double* x1, float
     __syncthreads();
 }
 
+// Arguments of the re-shifts (SubImage::adjustShifts of patches that request one).
+struct ShiftArgs {
+    int32_t P, I, M, nObj, ps, cs, margin, tiltX, tiltY;
+    const int32_t* req;
+    const double* alpha;     // [P][I*M]
+    double* tiltOff;         // [P][I][2] currentTiltOffset (y, x)
+    int32_t* shift;          // [P][I][2]
+    uint8_t* reinit;         // [P][I]
+    const int32_t* imgObj;   // [P][I]
+    const PatchGeo* pgeo;     // [P]
+    int32_t* aux;            // [P][2] reference object valid flag (cleared on re-initialisation)
+    double J[2][2], Jinv[2][2];
+    // rounds run as a CUDA graph: the conditions of the graph's optional kernels (image
+    // re-initialisation, adjoint, finite differences), set once per round from the work-list
+    // counters, and the kernel launches of the round added to launchCount
+    int32_t useConditions;
+    cudaGraphConditionalHandle condPrep, condAdjoint, condFd;
+    const int32_t* counters;
+    int32_t fixedLaunches;
+    int32_t prepLaunches;       // kernels of the re-initialisation node (plane fit + preparation)
+    unsigned long long* launchCount;
+};
+
+// adjustShifts of one patch's images (SubImage::adjustShifts, subimage.cpp:444-480) when its
+// request is a re-shift; marks the images of every object that has a shifted image for
+// re-initialisation (Object::reInitialize), and clears the marks otherwise.  All threads of
+// the block.
+__device__ __forceinline__ void shift_patch(const ShiftArgs& a, int p, int req) {
+    if (req != REQ_SHIFT) {
+        for (int j = threadIdx.x; j < a.I; j += blockDim.x) a.reinit[(size_t)p * a.I + j] = 0;
+        return;
+    }
+    const int nImg = a.pgeo[p].nImg;
+    __shared__ int objShifted[64];
+    for (int o = threadIdx.x; o < a.nObj; o += blockDim.x) objShifted[o] = 0;
+    __syncthreads();
+    for (int j = threadIdx.x; j < nImg; j += blockDim.x) {
+        const size_t gi = (size_t)p * a.I + j;
+        const double* al = a.alpha + gi * a.M;
+        if (a.tiltX < 0 || a.tiltY < 0) continue;
+        const double ay = al[a.tiltY] + a.tiltOff[gi * 2 + 0];
+        const double ax = al[a.tiltX] + a.tiltOff[gi * 2 + 1];
+        const double sy = ax * a.J[1][0] + ay * a.J[1][1];
+        const double sx = ax * a.J[0][0] + ay * a.J[0][1];
+        const int want[2] = {-(int)llround(sy), -(int)llround(sx)};
+        int act[2] = {0, 0};
+        for (int d = 0; d < 2; ++d) {
+            int nsh = want[d];
+            if (!nsh) continue;
+            const int first = a.margin + a.shift[gi * 2 + d];
+            const int last = first + a.ps - 1;
+            if (nsh + first < 0) nsh = -first;
+            if (abs(nsh + last) >= a.cs) nsh = a.cs - last - 1;
+            act[d] = nsh;
+        }
+        if (act[0] || act[1]) {
+            a.shift[gi * 2 + 0] += act[0];
+            a.shift[gi * 2 + 1] += act[1];
+            a.tiltOff[gi * 2 + 0] += act[1] * a.Jinv[1][0] + act[0] * a.Jinv[1][1];
+            a.tiltOff[gi * 2 + 1] += act[1] * a.Jinv[0][0] + act[0] * a.Jinv[0][1];
+            atomicExch(&objShifted[a.imgObj[gi]], 1);
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < a.I; j += blockDim.x) {
+        const int sh = j < nImg ? objShifted[a.imgObj[(size_t)p * a.I + j]] : 0;
+        a.reinit[(size_t)p * a.I + j] = sh ? 1 : 0;
+        if (sh && a.aux) a.aux[2 * p + 0] = 0;
+    }
+}
+
+// The conditions of the round's optional graph nodes (image re-initialisation, adjoint,
+// finite differences) from its work-list counters, and the kernel launches of the round
+// added to launchCount.  One thread, once every solver-kernel block of the round is done.
+__device__ __forceinline__ void set_round_conditions(const ShiftArgs& a) {
+    const unsigned prep = atomicAdd(const_cast<int32_t*>(a.counters) + kCounterShift, 0) > 0,
+                   adj = atomicAdd(const_cast<int32_t*>(a.counters) + kCounterGrad, 0) > 0,
+                   fd = atomicAdd(const_cast<int32_t*>(a.counters) + kCounterFd, 0) > 0;
+    cudaGraphSetConditional(a.condPrep, prep);
+    cudaGraphSetConditional(a.condAdjoint, adj);
+    cudaGraphSetConditional(a.condFd, fd);
+    *a.launchCount += (unsigned long long)(a.fixedLaunches + prep * a.prepLaunches + adj + fd);
+}
+
 // Shared-memory layout (bytes) of the staged solver kernel: the patch's five vectors, its
 // object metric tiles, the object weights, its reference-object flags and object tables, and
 // (stageMap) its row map (row pointers, entry values and columns), alpha offsets (float), the
@@ -254,9 +338,25 @@ __device__ void enqueue_eval(const CgArgs<T>& a, int p, int rq, int mode, const 
 // sums, the map and the work-list appends wait on shared memory instead of chains of
 // dependent global loads; the vectors the round wrote are copied back at the end.  The
 // arithmetic and its order are the same in both forms.
+// At the end every block re-shifts its own patch when that is its request (shift_patch) and,
+// in a solve graph, the last block of the round sets the conditions of the round's optional
+// nodes from the work-list counters (set_round_conditions).
 template <typename T, int THREADS, bool ST>
-__global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
+__global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a, ShiftArgs sa) {
     const int p = blockIdx.x;
+    auto finish = [&](int req) {
+        shift_patch(sa, p, req);
+        if (sa.useConditions) {
+            __syncthreads();    // the block's appends to the work lists are done
+            if (threadIdx.x == 0) {
+                __threadfence();
+                if (atomicAdd(a.L.counters + kCounterCgDone, 1) == (int)gridDim.x - 1) {
+                    __threadfence();
+                    set_round_conditions(sa);
+                }
+            }
+        }
+    };
     __shared__ double fsh;
     __shared__ double objSum[64];
     __shared__ int32_t pcShared, reqShared;
@@ -340,6 +440,7 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
     if (pc0 == PC_DONE) {
         if (ST) cp_async_wait_all();
         if (threadIdx.x == 0) a.req[p] = REQ_DONE;
+        finish(REQ_DONE);
         return;
     }
     double f = 0;
@@ -354,6 +455,7 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
             const size_t po = (size_t)p * a.nObj;
             enqueue_eval(a, p, REQ_F, 0, a.objCount + po, a.objFirst + po, a.objChunk0 + po, pg.chunks);
         }
+        finish(REQ_F);
         return;
     }
     if (ST) {
@@ -499,85 +601,15 @@ __global__ void __launch_bounds__(THREADS) k_cg(CgArgs<T> a) {
             a.L.evalP[atomicAdd(a.L.nEvalP, 1)] = p;
         }
     }
+    finish(rq);
 }
 
-// adjustShifts for every image of patches that requested a re-shift; marks the images of
-// every object that has a shifted image for re-initialisation (Object::reInitialize).
-struct ShiftArgs {
-    int32_t P, I, M, nObj, ps, cs, margin, tiltX, tiltY;
-    const int32_t* req;
-    const double* alpha;     // [P][I*M]
-    double* tiltOff;         // [P][I][2] currentTiltOffset (y, x)
-    int32_t* shift;          // [P][I][2]
-    uint8_t* reinit;         // [P][I]
-    const int32_t* imgObj;   // [P][I]
-    const PatchGeo* pgeo;     // [P]
-    int32_t* aux;            // [P][2] reference object valid flag (cleared on re-initialisation)
-    double J[2][2], Jinv[2][2];
-    // rounds run as a CUDA graph: the conditions of the graph's optional kernels (image
-    // re-initialisation, adjoint, finite differences), set once per round from the work-list
-    // counters, and the kernel launches of the round added to launchCount
-    int32_t useConditions;
-    cudaGraphConditionalHandle condPrep, condAdjoint, condFd;
-    const int32_t* counters;
-    int32_t fixedLaunches;
-    int32_t prepLaunches;       // kernels of the re-initialisation node (plane fit + preparation)
-    unsigned long long* launchCount;
-};
-
+// Re-shifts of patches that requested one (the initial re-cut of a warm start); in the solve
+// rounds the solver kernel does the same for its own patch.
 template <int UNUSED = 0>
 __global__ void k_shift(ShiftArgs a) {
-    const int p = blockIdx.x;
-    if (a.useConditions && p == 0 && threadIdx.x == 0) {
-        // written by k_cg, the previous kernel; one thread sets each condition
-        const unsigned prep = a.counters[kCounterShift] > 0, adj = a.counters[kCounterGrad] > 0,
-                       fd = a.counters[kCounterFd] > 0;
-        cudaGraphSetConditional(a.condPrep, prep);
-        cudaGraphSetConditional(a.condAdjoint, adj);
-        cudaGraphSetConditional(a.condFd, fd);
-        *a.launchCount += (unsigned long long)(a.fixedLaunches + prep * a.prepLaunches + adj + fd);
-    }
-    if (a.req[p] != REQ_SHIFT) {
-        for (int j = threadIdx.x; j < a.I; j += blockDim.x) a.reinit[(size_t)p * a.I + j] = 0;
-        return;
-    }
-    const int nImg = a.pgeo[p].nImg;
-    __shared__ int objShifted[64];
-    for (int o = threadIdx.x; o < a.nObj; o += blockDim.x) objShifted[o] = 0;
-    __syncthreads();
-    for (int j = threadIdx.x; j < nImg; j += blockDim.x) {
-        const size_t gi = (size_t)p * a.I + j;
-        const double* al = a.alpha + gi * a.M;
-        if (a.tiltX < 0 || a.tiltY < 0) continue;
-        const double ay = al[a.tiltY] + a.tiltOff[gi * 2 + 0];
-        const double ax = al[a.tiltX] + a.tiltOff[gi * 2 + 1];
-        const double sy = ax * a.J[1][0] + ay * a.J[1][1];
-        const double sx = ax * a.J[0][0] + ay * a.J[0][1];
-        const int want[2] = {-(int)llround(sy), -(int)llround(sx)};
-        int act[2] = {0, 0};
-        for (int d = 0; d < 2; ++d) {
-            int nsh = want[d];
-            if (!nsh) continue;
-            const int first = a.margin + a.shift[gi * 2 + d];
-            const int last = first + a.ps - 1;
-            if (nsh + first < 0) nsh = -first;
-            if (abs(nsh + last) >= a.cs) nsh = a.cs - last - 1;
-            act[d] = nsh;
-        }
-        if (act[0] || act[1]) {
-            a.shift[gi * 2 + 0] += act[0];
-            a.shift[gi * 2 + 1] += act[1];
-            a.tiltOff[gi * 2 + 0] += act[1] * a.Jinv[1][0] + act[0] * a.Jinv[1][1];
-            a.tiltOff[gi * 2 + 1] += act[1] * a.Jinv[0][0] + act[0] * a.Jinv[0][1];
-            atomicExch(&objShifted[a.imgObj[gi]], 1);
-        }
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < a.I; j += blockDim.x) {
-        const int sh = j < nImg ? objShifted[a.imgObj[(size_t)p * a.I + j]] : 0;
-        a.reinit[(size_t)p * a.I + j] = sh ? 1 : 0;
-        if (sh && a.aux) a.aux[2 * p + 0] = 0;
-    }
+    if (a.useConditions && blockIdx.x == 0 && threadIdx.x == 0) set_round_conditions(a);
+    shift_patch(a, blockIdx.x, a.req[blockIdx.x]);
 }
 
 }  // namespace rdxg

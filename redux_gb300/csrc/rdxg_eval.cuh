@@ -49,7 +49,7 @@ constexpr int kReduceTile = 128;
 // are reset by the evaluation itself (its last block), so that it can be launched again on the
 // same lists
 enum : int32_t { kCounterEval = 0, kCounterPo = 1, kCounterGrad = 2, kCounterFd = 3, kCounterEvalP = 4,
-                 kCounterShift = 5, kCounterEvalClaim = 6, kCounterEvalDone = 7 };
+                 kCounterShift = 5, kCounterEvalClaim = 6, kCounterEvalDone = 7, kCounterCgDone = 8 };
 
 struct Lists {
     EvalItem* eval;  int32_t* nEval;

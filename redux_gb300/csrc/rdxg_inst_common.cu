@@ -10,15 +10,15 @@ void launch_accum(const KParams<T>& kp, int nPo, cudaStream_t st) {
 }
 
 template <typename T>
-void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st) {
+void launch_cg(const CgArgs<T>& a, const ShiftArgs& sa, int P, cudaStream_t st) {
     if (a.stage) {
         const int nT = a.fused ? a.nTilesH : a.nTiles;
         const size_t sm = CgStageLayout(a.prm.n_free, a.nObj, nT, a.stageMap, a.nPar, a.I, a.maxNnz).total;
-        k_cg<T, kCgThreads, true><<<P, kCgThreads, sm, st>>>(a);
+        k_cg<T, kCgThreads, true><<<P, kCgThreads, sm, st>>>(a, sa);
         return;
     }
     const size_t sm = a.x1Smem ? (size_t)a.prm.n_free * sizeof(float) : 0;
-    k_cg<T, kCgThreads, false><<<P, kCgThreads, sm, st>>>(a);
+    k_cg<T, kCgThreads, false><<<P, kCgThreads, sm, st>>>(a, sa);
 }
 
 template <typename T>
@@ -85,8 +85,8 @@ template void launch_fit_plane<float>(const KParams<float>&, int, int, cudaStrea
 template void launch_fit_plane<double>(const KParams<double>&, int, int, cudaStream_t);
 template void launch_accum<float>(const KParams<float>&, int, cudaStream_t);
 template void launch_accum<double>(const KParams<double>&, int, cudaStream_t);
-template void launch_cg<float>(const CgArgs<float>&, int, cudaStream_t);
-template void launch_cg<double>(const CgArgs<double>&, int, cudaStream_t);
+template void launch_cg<float>(const CgArgs<float>&, const ShiftArgs&, int, cudaStream_t);
+template void launch_cg<double>(const CgArgs<double>&, const ShiftArgs&, int, cudaStream_t);
 template cudaError_t setup_cg<float>(size_t);
 template cudaError_t setup_cg<double>(size_t);
 

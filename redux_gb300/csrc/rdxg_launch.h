@@ -81,7 +81,7 @@ constexpr int kPhaseRegPix = 128;   // pixels per block of the per-patch mode ex
 constexpr int kPhaseRegModes = 64;  // modes it holds in registers (more: the staged kernel)
 constexpr int kPhaseMaxImg = 64;    // images per patch it stages
 constexpr int kPhaseMaxCh = 16;     // channels whose fixed phases it stages
-constexpr int kNumCounters = 8;     // work-list counters reset every round (and the evaluation's two)
+constexpr int kNumCounters = 9;     // work-list counters reset every round (and the evaluation's two)
 constexpr size_t kMaxSmem = 227 * 1024;   // dynamic shared memory per block
 template <typename T, int N> struct EvalLauncher {
     static cudaError_t setup(int M, int npt, int nH);
@@ -94,7 +94,7 @@ template <typename T, int N> struct EvalLauncher {
     static size_t fd_smem(int nH);                   // shared memory of the half-plane FD gradient
     static void fd_half(const EvalParams<T>& e, int grid, cudaStream_t st);
 };
-template <typename T> void launch_cg(const CgArgs<T>& a, int P, cudaStream_t st);
+template <typename T> void launch_cg(const CgArgs<T>& a, const ShiftArgs& sa, int P, cudaStream_t st);
 constexpr size_t kCgStageBytes = 96 * 1024;   // shared memory of the staged solver kernel, at most
 template <typename T> cudaError_t setup_cg(size_t stageBytes);   // opt in to it
 cudaError_t query_nsmid(int32_t* dOut, int32_t* hOut, cudaStream_t st);   // %nsmid of the device
