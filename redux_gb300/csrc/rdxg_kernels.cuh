@@ -610,16 +610,35 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
     const cx<T>* Oo = kp.O + po * N2;
     const cx<T>* Dg = kp.D + (size_t)g * N2;
     const cx<T>* Sg = kp.S + (size_t)g * N2;
-    // unrolled, and the loads issued before the support test, so that each thread has
-    // several iterations' global loads in flight in one round trip
+    if (sizeof(T) == 4 && kp.Dh) {
+        // fused path: G on the half plane, from the half-plane copy of D, and its mirror
+        // G(-u) = conj G(u) (D, S, O are transforms of real images, so is G); half the loads
+        for (int i = threadIdx.x; i < Tile<N>::ELEMS; i += THREADS) s[i] = mkc<T>(0, 0);
+        __syncthreads();
+        const cx<T>* Dh = kp.Dh + (size_t)g * kp.nH;
+#pragma unroll 4
+        for (int h = threadIdx.x; h < kp.nH; h += THREADS) {
+            const int c = kp.hIdx[h];
+            const int cy = c / N, cxx = c % N;
+            const cx<T> O = Oo[c], D = Dh[h], S = Sg[c];
+            const cx<T> G = cmulc<T>(csub<T>(D, cmul<T>(O, S)), O);   // conj(O) (D - O S)
+            const int y = (cy + N / 2) % N, x = (cxx + N / 2) % N;      // un-centred (lag) position
+            if (y == 0 && x == 0) continue;                                // the DC term is dropped
+            s[y * LDS + x] = G;
+            s[((N - y) % N) * LDS + (N - x) % N] = mkc<T>(G.x, -G.y);
+        }
+    } else {
+        // unrolled, and the loads issued before the support test, so that each thread has
+        // several iterations' global loads in flight in one round trip
 #pragma unroll 8
-    for (int i = threadIdx.x; i < N2; i += THREADS) {
-        const int y = i / N, x = i % N;                 // un-centred (lag) position
-        const int c = ((y + N / 2) % N) * N + (x + N / 2) % N;
-        const uint8_t m = kp.otfMask[c];
-        const cx<T> O = Oo[c], D = Dg[c], S = Sg[c];
-        const cx<T> G = cmulc<T>(csub<T>(D, cmul<T>(O, S)), O);   // conj(O) (D - O S)
-        s[y * LDS + x] = (m && !(y == 0 && x == 0)) ? G : mkc<T>(0, 0);
+        for (int i = threadIdx.x; i < N2; i += THREADS) {
+            const int y = i / N, x = i % N;                 // un-centred (lag) position
+            const int c = ((y + N / 2) % N) * N + (x + N / 2) % N;
+            const uint8_t m = kp.otfMask[c];
+            const cx<T> O = Oo[c], D = Dg[c], S = Sg[c];
+            const cx<T> G = cmulc<T>(csub<T>(D, cmul<T>(O, S)), O);   // conj(O) (D - O S)
+            s[y * LDS + x] = (m && !(y == 0 && x == 0)) ? G : mkc<T>(0, 0);
+        }
     }
     __syncthreads();
     fft2d<T, N, -1, THREADS, false, PL>(s, tw);
