@@ -49,7 +49,7 @@ cudaError_t Launcher<T, N>::setup(int M) {
     cudaError_t e;
     if ((e = raise_smem_limit(k_prep<T, N, THREADS>, sm))) return e;
     if ((e = raise_smem_limit(k_forward<T, N, THREADS>, sm))) return e;
-    if ((e = raise_smem_limit(k_adjoint<T, N, THREADS>, sm))) return e;
+    if ((e = raise_smem_limit(adjoint_kernel<T, N, THREADS>(), sm))) return e;
     if ((e = raise_smem_limit(k_fd<T, N, THREADS>, sm))) return e;
     const size_t arc = adjoint_rc_smem<T, N>(M), frc = fd_rc_smem<T, N>(M);
     if (arc <= kMaxSmem && (e = raise_smem_limit(k_adjoint_rc<T, N, THREADS, false>, arc))) return e;
@@ -57,14 +57,14 @@ cudaError_t Launcher<T, N>::setup(int M) {
     if constexpr (HasAlt<T>::value) {
         constexpr int ALT = ThreadsAlt<N>::value;
         if ((e = raise_smem_limit(k_forward<T, N, ALT>, sm))) return e;
-        if ((e = raise_smem_limit(k_adjoint<T, N, ALT>, sm))) return e;
+        if ((e = raise_smem_limit(adjoint_kernel<T, N, ALT>(), sm))) return e;
         if (arc <= kMaxSmem && (e = raise_smem_limit(k_adjoint_rc<T, N, ALT, false>, arc))) return e;
         if constexpr (PlanAlt<N>::exists) {
             using PA = PlanAlt<N>;
             if ((e = raise_smem_limit(k_forward<T, N, THREADS, PA>, sm))) return e;
-            if ((e = raise_smem_limit(k_adjoint<T, N, THREADS, PA>, sm))) return e;
+            if ((e = raise_smem_limit(adjoint_kernel<T, N, THREADS, PA>(), sm))) return e;
             if ((e = raise_smem_limit(k_forward<T, N, ALT, PA>, sm))) return e;
-            if ((e = raise_smem_limit(k_adjoint<T, N, ALT, PA>, sm))) return e;
+            if ((e = raise_smem_limit(adjoint_kernel<T, N, ALT, PA>(), sm))) return e;
         }
     }
     if constexpr (PingPong<T, N>::value) {
@@ -142,15 +142,15 @@ void Launcher<T, N>::adjoint(const KParams<T>& kp, int grid, int kind, cudaStrea
         constexpr int ALT = ThreadsAlt<N>::value;
         if constexpr (PlanAlt<N>::exists) {
             using PA = PlanAlt<N>;
-            if (kp.shapeAdj == 2) { k_adjoint<T, N, THREADS, PA><<<grid, THREADS, sm, st>>>(kp, kind); return; }
-            if (kp.shapeAdj == 3) { k_adjoint<T, N, ALT, PA><<<grid, ALT, sm, st>>>(kp, kind); return; }
+            if (kp.shapeAdj == 2) { adjoint_kernel<T, N, THREADS, PA>()<<<grid, THREADS, sm, st>>>(kp, kind); return; }
+            if (kp.shapeAdj == 3) { adjoint_kernel<T, N, ALT, PA>()<<<grid, ALT, sm, st>>>(kp, kind); return; }
         }
         if (kp.shapeAdj == 1) {
-            k_adjoint<T, N, ALT><<<grid, ALT, sm, st>>>(kp, kind);
+            adjoint_kernel<T, N, ALT>()<<<grid, ALT, sm, st>>>(kp, kind);
             return;
         }
     }
-    k_adjoint<T, N, THREADS><<<grid, THREADS, sm, st>>>(kp, kind);
+    adjoint_kernel<T, N, THREADS>()<<<grid, THREADS, sm, st>>>(kp, kind);
 }
 
 template <typename T, int N>

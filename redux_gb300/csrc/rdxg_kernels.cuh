@@ -610,7 +610,9 @@ __device__ __forceinline__ void adjoint_image(const KParams<T>& kp, int kind, in
     const cx<T>* Oo = kp.O + po * N2;
     const cx<T>* Dg = kp.D + (size_t)g * N2;
     const cx<T>* Sg = kp.S + (size_t)g * N2;
-    if (sizeof(T) == 4 && kp.Dh) {
+    bool halfG = false;
+    if constexpr (sizeof(T) == 4 && N <= 88) halfG = kp.Dh != nullptr;
+    if (halfG) {
         // fused path: G on the half plane, from the half-plane copy of D, and its mirror
         // G(-u) = conj G(u) (D, S, O are transforms of real images, so is G); half the loads
         for (int i = threadIdx.x; i < Tile<N>::ELEMS; i += THREADS) s[i] = mkc<T>(0, 0);
@@ -667,6 +669,23 @@ __global__ void __launch_bounds__(THREADS) k_adjoint(KParams<T> kp, int kind) {
     if (w >= nWork) return;
     const int p = kp.gradP[w / kp.I], j = w % kp.I;
     if (j < kp.pgeo[p].nImg) adjoint_image<T, N, THREADS, PL>(kp, kind, p, j);
+}
+
+// The same kernel with registers for three 256-thread or two 512-thread blocks per SM, as many
+// as their shared memory allows (FP32 up to N = 88): a round's ~700 gradient images take fewer
+// waves.  (Where the bound would spill, at N = 128 and in FP64, k_adjoint is used.)
+template <typename T, int N, int THREADS, typename PL = Plan<N>>
+__global__ void __launch_bounds__(THREADS, THREADS == 256 ? 3 : 2) k_adjoint_mb(KParams<T> kp, int kind) {
+    const int nWork = *kp.nGradP * kp.I;
+    const int w = blockIdx.x;
+    if (w >= nWork) return;
+    const int p = kp.gradP[w / kp.I], j = w % kp.I;
+    if (j < kp.pgeo[p].nImg) adjoint_image<T, N, THREADS, PL>(kp, kind, p, j);
+}
+template <typename T, int N, int THREADS, typename PL = Plan<N>>
+constexpr auto adjoint_kernel() {
+    if constexpr (sizeof(T) == 4 && N <= 88) return &k_adjoint_mb<T, N, THREADS, PL>;
+    else return &k_adjoint<T, N, THREADS, PL>;
 }
 
 // ----------------------------------------------------------------------------------
