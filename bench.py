@@ -7,9 +7,11 @@ seeded synthetic data.  One step = one complete solve of the batch: image prepar
 (windowing, transforms, noise, regularisation) and 100 iterations of the reference's
 conjugate-gradient/line-search for every patch.
 
-value: patches/s with the cutouts resident in HBM: the batch split over three handles, each
-       on its own stream (rdxg_set_patches_device per handle, then rdxg_solve_many: one CUDA
-       graph, a branch per handle).
+value: patches/s with the cutouts resident in HBM: the batch split over handles of about one
+       object per SM each (three for 225 patches of two objects on 152 SMs), each on its own
+       stream, with evaluation work items of 16 images (eval_chunk)
+       (rdxg_set_patches_device per handle, then rdxg_solve_many: one CUDA graph, a branch per
+       handle).
 e2e:   patches/s through the public API from pinned host memory (cutouts H2D per handle,
        rdxg_solve_many, coefficients/reports/metric histories D2H), per step.
 --impl reference: the reference's CPU path timed on the host cores -- redux itself does not
@@ -635,8 +637,12 @@ def main():
     ap.add_argument("--frames", type=int, default=12)
     ap.add_argument("--iterations", type=int, default=100)
     ap.add_argument("--no-baselines", action="store_true")
-    ap.add_argument("--handles", type=int, default=3,
-                    help="handles (each on its own stream) the batch is split over, solved together")
+    ap.add_argument("--handles", type=int, default=0,
+                    help="handles (each on its own stream) the batch is split over, solved together "
+                         "(0: about one object per SM in each)")
+    ap.add_argument("--chunk", type=int, default=0,
+                    help="images of an object per evaluation work item (eval_chunk; 0: 16 when the batch "
+                         "is split over several handles, else the library's 6)")
     ap.add_argument("--workload", default="production", choices=("production", "uneven", "large", "convergence"),
                     help="production: the headline batch (225 patches 88 x 88); uneven: 400 patches of "
                          "{64, 88, 128} px; large: 256 patches 128 x 128 with 100 modes; convergence: the "
@@ -700,14 +706,21 @@ def main():
         solver.close()
         return
     # the batch split over H handles, each on its own stream, solved together (one CUDA graph,
-    # a branch per handle): one handle's latency-bound kernels of a round overlap the tail of
-    # another's evaluation (measured: 1 handle 780 ms, 2: 765, 3: 758, 4: 766, 6: 795 ms)
-    H = max(1, min(args.handles, P))
+    # a branch per handle): one handle's latency-bound kernels of a round overlap the others'
+    # evaluations.  With about one object per SM in each handle, large evaluation work items
+    # (fewer per-item overheads) pay, as the handles' evaluations fill each other's tails.
+    # Measured on the 225-patch batch (objects of 12 and 24 images), ms per step, by work-item
+    # size: 1 handle 709 (6), 743 (12), 858 (18); 3 handles 688 (6), 678 (12), 668.7 (16),
+    # 669.7 (18), 672 (20), 694 (24); 5 handles 696 (6), 687 (18).
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    H = args.handles or max(1, round(P * job.n_objects / sms))
+    H = max(1, min(H, P))
+    chunk = args.chunk or (16 if H > 1 else 0)
     bounds = [int(round(P * k / H)) for k in range(H + 1)]
     parts = [(bounds[k], bounds[k + 1]) for k in range(H)]
     solvers, streams = [], []
     for b0, b1 in parts:
-        sk = S.Solver(job, max_patches=b1 - b0, device=local)
+        sk = S.Solver(job, max_patches=b1 - b0, device=local, eval_chunk=chunk)
         st = torch.cuda.Stream()
         sk.set_stream(st.cuda_stream)
         solvers.append(sk)
@@ -778,7 +791,8 @@ def main():
     value = world * P / (ms_dev / 1000.0)
     e2e_value = world * P / (e2e_ms / 1000.0)
 
-    # roofline of the dominant kernel, measured on the whole batch in one handle
+    # roofline of the dominant kernel, measured on the whole batch in one handle (6-image
+    # evaluation work items)
     solver = S.Solver(job, max_patches=P, device=local)
     solver.set_patches_device(P, cut_dev.data_ptr())
     solver.autotune(reps=3)
@@ -831,6 +845,7 @@ def main():
                                    f"{args.iterations} CG iterations, all modes at once",
                        "patches_per_gpu": P, "iterations": args.iterations,
                        "handles": H, "handle_patches": [b1 - b0 for b0, b1 in parts],
+                       "eval_chunk": chunk or 6,
                        "l2": "inputs larger than L2 (D, OTF: 2 x 500 MB per batch)",
                        "metric_evals_per_patch": nf, "gradient_evals_per_patch": ndf,
                        "cg_iterations_per_s": world * P * args.iterations / (ms_dev / 1000.0)},
@@ -879,16 +894,31 @@ def main():
         # converged solves with the reference's default settings (MODE_START 5, MODE_STEP 5,
         # MIN_ITER 5, MAX_ITER 500, N_DONE_ITER 3, FTOL 1e-3: staged modes, re-shifts between
         # stages, per-patch stop), the batch against the plain FP64 form on a sample
+        # Patches stop at different rounds, so the late rounds carry few objects: these solves
+        # run on handles of their own with the library's default 6-image evaluation work items
+        # (the same split; 16-image items: 670.6 against 688.8 patches/s)
         conv = S.SolveSettings(max_metrics=4096)
-        load_device()
-        S.solve_many(solvers, conv, fetch=False)           # warm-up (graph capture)
+        conv_solvers = []
+        for (b0, b1), st in zip(parts, streams):
+            sk = S.Solver(job, max_patches=b1 - b0, device=local)
+            sk.set_stream(st.cuda_stream)
+            conv_solvers.append(sk)
+
+        def solve_conv():
+            for sk, (b0, b1) in zip(conv_solvers, parts):
+                sk.set_patches_device(b1 - b0, cut_dev[b0:b1].data_ptr())
+            S.solve_many(conv_solvers, conv, fetch=False)
+
+        solve_conv()                                       # warm-up (graph capture)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        load_device()
-        S.solve_many(solvers, conv, fetch=False)
+        solve_conv()
         torch.cuda.synchronize()
         t_conv = time.perf_counter() - t0
-        rc = fetch_all(conv.max_metrics)
+        outs = [sk.fetch(conv.max_metrics) for sk in conv_solvers]
+        rc = dict(reports=[r for o in outs for r in o["reports"]])
+        for sk in conv_solvers:
+            sk.close()
         s64 = S.Solver(job, max_patches=1, precision="fp64", device=local)
         t64, sr = 0.0, []
         for p in range(nplain):

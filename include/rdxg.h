@@ -56,6 +56,13 @@ typedef struct {
     int32_t max_patches;   /* batch capacity */
     int32_t precision;     /* rdxg_precision (RDXG_FP64 takes otf_size <= 88) */
     int32_t device;        /* CUDA device ordinal */
+    int32_t eval_chunk;    /* images of one object per work item of the fused evaluation, 1..32
+                              (0: 6).  The chunks' sums are added in a fixed order, so a patch's
+                              results depend on this value (at the level of FP32 rounding) and on
+                              nothing else of the batch.  Larger values (fewer, longer work
+                              items) pay when several handles are solved together by
+                              rdxg_solve_many and each handle has about one object per SM; small
+                              ones when one handle holds the batch. */
 } rdxg_geometry;
 
 /* Static inputs (host pointers, copied by rdxg_create). */

@@ -28,7 +28,7 @@ EXPORTED = ("rdxg_version", "rdxg_create", "rdxg_destroy", "rdxg_last_error", "r
 class Geometry(C.Structure):
     _fields_ = [(n, C.c_int32) for n in (
         "otf_size", "pupil_pixels", "patch_size", "n_modes", "n_objects", "n_images", "n_channels",
-        "tilt_x", "tilt_y", "n_free", "cutout_size", "max_patches", "precision", "device")]
+        "tilt_x", "tilt_y", "n_free", "cutout_size", "max_patches", "precision", "device", "eval_chunk")]
 
 
 class Static(C.Structure):

@@ -930,9 +930,7 @@ int setup_fused(rdxg_solver* h, const rdxg_static* s) {
                       : N == 64 ? EvalLauncher<float, 64>::smem(h->M, h->nH)
                                 : EvalLauncher<float, 88>::smem(h->M, h->nH);
     if (smem > 227 * 1024) return RDXG_OK;   // does not fit
-    const char* env = getenv("RDXG_CHUNK");
-    h->chunk = env ? atoi(env) : 6;
-    if (h->chunk < 1 || h->chunk > kMaxChunk) h->chunk = 6;
+    h->chunk = h->geo.eval_chunk > 0 ? h->geo.eval_chunk : 6;
     h->objChunk0.assign(h->nObj, 0);
     int c0 = 0;
     for (int o = 0; o < h->nObj; ++o) {
@@ -1076,6 +1074,7 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
         return code;
     };
     if (h->N != 2 * h->n) return fail(RDXG_ERR_ARG, "otf_size must be 2 * pupil_pixels");
+    if (g->eval_chunk < 0 || g->eval_chunk > kMaxChunk) return fail(RDXG_ERR_ARG, "eval_chunk must be 0..32");
     if (!supported_N(h->N)) return fail(RDXG_ERR_UNSUPPORTED, "otf_size not compiled (supported: 32, 64, 88, 128)");
     if (h->ps != h->N) return fail(RDXG_ERR_UNSUPPORTED, "patch_size must equal otf_size");
     if (h->cs < h->ps || ((h->cs - h->ps) & 1)) return fail(RDXG_ERR_ARG, "bad cutout_size");

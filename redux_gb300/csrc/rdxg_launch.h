@@ -76,7 +76,7 @@ static_assert(kEvalThreads % 32 == 0 && kEvalThreads <= 1024, "block size");
 constexpr int kEvalThreadsAlt = kEvalThreads == 384 ? 512 : 384;
 constexpr int kReduceThreads = 256;
 constexpr int kPhasePix = 256;      // pixels per block of the mode expansion
-constexpr int kMaxChunk = 8;        // images per chunk (upper bound)
+constexpr int kMaxChunk = 32;       // images per chunk (upper bound)
 constexpr int kPhaseRegPix = 128;   // pixels per block of the per-patch mode expansion
 constexpr int kPhaseRegModes = 64;  // modes it holds in registers (more: the staged kernel)
 constexpr int kPhaseMaxImg = 64;    // images per patch it stages

@@ -51,7 +51,7 @@ def fixed_iterations(n_modes: int, iterations: int, **kw) -> SolveSettings:
 class Solver:
     """Batched per-patch MOMFBD solver for one job on one GPU."""
 
-    def __init__(self, job, max_patches: int, precision: str = "fp32", device: int = 0):
+    def __init__(self, job, max_patches: int, precision: str = "fp32", device: int = 0, eval_chunk: int = 0):
         L = _lib.load()
         self.job = job
         self._keep = []
@@ -68,7 +68,7 @@ class Solver:
             n_modes=job.n_modes, n_objects=job.n_objects, n_images=job.n_images, n_channels=job.n_channels,
             tilt_x=job.tilt_x, tilt_y=job.tilt_y, n_free=ns.n_free, cutout_size=job.cutout_size,
             max_patches=max_patches, precision=_lib.RDXG_FP64 if precision == "fp64" else _lib.RDXG_FP32,
-            device=device)
+            device=device, eval_chunk=eval_chunk)
         st = _lib.Static(
             modes=c(job.modes, np.float64), pupil=c(job.pupil, np.float64),
             n_pupil_support=int(sup.pupil_support.size), pupil_support=c(sup.pupil_support, np.int32),

@@ -33,3 +33,14 @@ def test_unsupported_size_is_rejected_before_any_device_call():
     job = synth.make_job(96, 8, synth.LAYOUT_1OBJ(2))
     with pytest.raises(S.SolverError, match=r"status 2: otf_size not compiled"):
         S.Solver(job, max_patches=1, precision="fp64")
+
+
+def test_eval_chunk_out_of_range_is_rejected_before_any_device_call():
+    """rdxg_geometry.eval_chunk takes 0 (the default, 6) to 32 images per work item."""
+    import pytest
+    from redux_gb300 import solver as S
+    from tests.conftest import workload
+    w = workload("production88", n_patches=2, frames=4)
+    for bad in (-1, 33):
+        with pytest.raises(S.SolverError, match=r"eval_chunk must be 0\.\.32"):
+            S.Solver(w.job, max_patches=1, eval_chunk=bad)
