@@ -25,3 +25,11 @@ def test_workload_choices():
                        timeout=120, cwd=ROOT)
     assert r.returncode == 0
     assert "--workload {production,uneven,large,convergence}" in r.stdout
+
+
+def test_split_options():
+    # the handle split and the evaluation work-item size of the headline line
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--help"], capture_output=True, text=True,
+                       timeout=120, cwd=ROOT)
+    assert r.returncode == 0
+    assert "--handles HANDLES" in r.stdout and "--chunk CHUNK" in r.stdout
