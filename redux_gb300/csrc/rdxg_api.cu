@@ -1074,7 +1074,8 @@ int rdxg_create(const rdxg_geometry* g, const rdxg_static* s, rdxg_solver** out)
         return code;
     };
     if (h->N != 2 * h->n) return fail(RDXG_ERR_ARG, "otf_size must be 2 * pupil_pixels");
-    if (g->eval_chunk < 0 || g->eval_chunk > kMaxChunk) return fail(RDXG_ERR_ARG, "eval_chunk must be 0..32");
+    if (g->eval_chunk < 0 || g->eval_chunk > kMaxChunk)
+        return fail(RDXG_ERR_ARG, ("eval_chunk must be 0.." + std::to_string(kMaxChunk)).c_str());
     if (!supported_N(h->N)) return fail(RDXG_ERR_UNSUPPORTED, "otf_size not compiled (supported: 32, 64, 88, 128)");
     if (h->ps != h->N) return fail(RDXG_ERR_UNSUPPORTED, "patch_size must equal otf_size");
     if (h->cs < h->ps || ((h->cs - h->ps) & 1)) return fail(RDXG_ERR_ARG, "bad cutout_size");
