@@ -711,7 +711,7 @@ def main():
     # (fewer per-item overheads) pay, as the handles' evaluations fill each other's tails.
     # Measured on the 225-patch batch (objects of 12 and 24 images), ms per step, by work-item
     # size: 1 handle 709 (6), 743 (12), 858 (18); 3 handles 688 (6), 678 (12), 668.7 (16),
-    # 669.7 (18), 672 (20), 694 (24); 5 handles 696 (6), 687 (18).
+    # 669.7 (18), 672 (20), 694 (24); 4 handles 688 (12, 16); 5 handles 696 (6), 687 (18).
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     H = args.handles or max(1, round(P * job.n_objects / sms))
     H = max(1, min(H, P))
