@@ -66,9 +66,12 @@ typedef struct {
     int fac[40];
     cplx* tw_fwd; /* exp(-2 pi i k / n), k < n */
     cplx* tw_bwd; /* exp(+2 pi i k / n) */
-    /* iterative form (fft1_fast): per stage s, twiddles exp(-+2 pi i r k / (NS R)) for k < NS,
-     * r < R (interleaved cos, sin), NS = product of the earlier radices; cos and sin of
-     * 2 pi q / R for each odd radix */
+    /* iterative form (fft1_fast): its own factorisation (radix 8 first, then 4, 2 and the odd
+     * primes); per stage s, twiddles exp(-+2 pi i r k / (NS R)) for k < NS, r < R
+     * (interleaved cos, sin), NS = product of the earlier radices; cos and sin of 2 pi q / R
+     * for each odd radix */
+    int nffac;
+    int ffac[40];
     double* st_tw[2];
     int st_off[41];
     double* odd_cs;
@@ -76,8 +79,9 @@ typedef struct {
 } fft_plan;
 
 /* Which transform the solver's FFTs use: 0 the recursive one above (the oracle proper), 1 the
- * iterative Stockham form with precomputed tables and real arithmetic (orc_set_fast_fft; used
- * to time the CPU baseline: the same factorisation and the same DFT, rounded differently). */
+ * iterative Stockham form with precomputed tables, real arithmetic and stages specialised per
+ * radix (orc_set_fast_fft; used to time the CPU baseline: the same DFT, factorised with radix 8
+ * first and rounded differently). */
 static int g_fast_fft = 0;
 void orc_set_fast_fft(int on) { g_fast_fft = on ? 1 : 0; }
 static void plan_fast_init(fft_plan* p);
@@ -104,20 +108,28 @@ static void plan_init(fft_plan* p, int n) {
 
 static void plan_fast_init(fft_plan* p) {
     const int n = p->n;
-    int tot = 0, ns = 1, nodd = 0;
-    for (int s = 0; s < p->nfac; ++s) {
-        p->st_off[s] = tot;
-        tot += ns * p->fac[s];
-        ns *= p->fac[s];
-        p->odd_off[s] = nodd;
-        if (p->fac[s] % 2) nodd += p->fac[s];
+    p->nffac = 0;
+    int m = n;
+    while (m % 8 == 0) { p->ffac[p->nffac++] = 8; m /= 8; }
+    while (m % 4 == 0) { p->ffac[p->nffac++] = 4; m /= 4; }
+    while (m % 2 == 0) { p->ffac[p->nffac++] = 2; m /= 2; }
+    for (int f = 3; m > 1; f += 2) {
+        while (m % f == 0) { p->ffac[p->nffac++] = f; m /= f; }
     }
-    p->st_off[p->nfac] = tot;
+    int tot = 0, ns = 1, nodd = 0;
+    for (int s = 0; s < p->nffac; ++s) {
+        p->st_off[s] = tot;
+        tot += ns * p->ffac[s];
+        ns *= p->ffac[s];
+        p->odd_off[s] = nodd;
+        if (p->ffac[s] % 2) nodd += p->ffac[s];
+    }
+    p->st_off[p->nffac] = tot;
     for (int d = 0; d < 2; ++d) p->st_tw[d] = (double*)malloc(sizeof(double) * 2 * (size_t)(tot > 0 ? tot : 1));
     p->odd_cs = (double*)malloc(sizeof(double) * 2 * (size_t)(nodd > 0 ? nodd : 1));
     ns = 1;
-    for (int s = 0; s < p->nfac; ++s) {
-        const int R = p->fac[s];
+    for (int s = 0; s < p->nffac; ++s) {
+        const int R = p->ffac[s];
         for (int k = 0; k < ns; ++k)
             for (int r = 0; r < R; ++r) {
                 const double a = 2.0 * M_PI * (double)r * (double)k / (double)(ns * R);
@@ -189,71 +201,117 @@ static void fft_rec(const fft_plan* p, const cplx* tw, cplx* out, const cplx* in
     if (tt != t) free(tt);
 }
 
+/* One stage of the iterative Stockham transform below: radix R (a compile-time constant at
+ * each call, so that the loops over the butterfly's R values unroll), NS = product of the
+ * earlier radices; a -> b. */
+static inline __attribute__((always_inline)) void fast_stage(const fft_plan* p, int s, const double* a, double* b,
+                                                             int ns, const int R, double dsg, const double* tws) {
+    const int n = p->n;
+    const int bf = n / R;
+    const double* tw = tws + 2 * p->st_off[s];
+    const double* cs = (R % 2) ? p->odd_cs + 2 * p->odd_off[s] : NULL;
+    double vr[64], vi[64];
+    for (int j = 0; j < bf; ++j) {
+        const int k = j % ns;
+        for (int r = 0; r < R; ++r) {
+            vr[r] = a[2 * (j + r * bf)];
+            vi[r] = a[2 * (j + r * bf) + 1];
+        }
+        if (ns > 1) {
+            const double* w = tw + 2 * k * R;
+            for (int r = 1; r < R; ++r) {
+                const double xr = vr[r], xi = vi[r];
+                vr[r] = xr * w[2 * r] - xi * w[2 * r + 1];
+                vi[r] = xr * w[2 * r + 1] + xi * w[2 * r];
+            }
+        }
+        const int d0 = (j / ns) * ns * R + k;
+        if (R == 2) {
+            b[2 * d0] = vr[0] + vr[1]; b[2 * d0 + 1] = vi[0] + vi[1];
+            b[2 * (d0 + ns)] = vr[0] - vr[1]; b[2 * (d0 + ns) + 1] = vi[0] - vi[1];
+        } else if (R == 4) {
+            const double a0r = vr[0] + vr[2], a0i = vi[0] + vi[2], a1r = vr[0] - vr[2], a1i = vi[0] - vi[2];
+            const double b0r = vr[1] + vr[3], b0i = vi[1] + vi[3];
+            /* (v1 - v3) * i sign */
+            const double tr = vr[1] - vr[3], ti = vi[1] - vi[3];
+            const double b1r = -dsg * ti, b1i = dsg * tr;
+            b[2 * d0] = a0r + b0r; b[2 * d0 + 1] = a0i + b0i;
+            b[2 * (d0 + ns)] = a1r + b1r; b[2 * (d0 + ns) + 1] = a1i + b1i;
+            b[2 * (d0 + 2 * ns)] = a0r - b0r; b[2 * (d0 + 2 * ns) + 1] = a0i - b0i;
+            b[2 * (d0 + 3 * ns)] = a1r - b1r; b[2 * (d0 + 3 * ns) + 1] = a1i - b1i;
+        } else if (R == 8) {
+            /* y[u] = E[u mod 4] + w^u O[u mod 4], w = exp(sign 2 pi i / 8): E, O the 4-point
+             * transforms of the even and odd inputs */
+            double er[4], ei[4], orr[4], oi[4];
+            for (int h = 0; h < 2; ++h) {
+                double* xr = h ? orr : er;
+                double* xi = h ? oi : ei;
+                const double a0r = vr[h] + vr[h + 4], a0i = vi[h] + vi[h + 4];
+                const double a1r = vr[h] - vr[h + 4], a1i = vi[h] - vi[h + 4];
+                const double b0r = vr[h + 2] + vr[h + 6], b0i = vi[h + 2] + vi[h + 6];
+                const double tr = vr[h + 2] - vr[h + 6], ti = vi[h + 2] - vi[h + 6];
+                const double b1r = -dsg * ti, b1i = dsg * tr;
+                xr[0] = a0r + b0r; xi[0] = a0i + b0i;
+                xr[1] = a1r + b1r; xi[1] = a1i + b1i;
+                xr[2] = a0r - b0r; xi[2] = a0i - b0i;
+                xr[3] = a1r - b1r; xi[3] = a1i - b1i;
+            }
+            const double hh = 0.70710678118654752440;   /* sqrt(1/2) */
+            const double t1r = hh * (orr[1] - dsg * oi[1]), t1i = hh * (oi[1] + dsg * orr[1]);
+            const double t2r = -dsg * oi[2], t2i = dsg * orr[2];
+            const double t3r = hh * (-orr[3] - dsg * oi[3]), t3i = hh * (-oi[3] + dsg * orr[3]);
+            const double tr_[4] = {orr[0], t1r, t2r, t3r}, ti_[4] = {oi[0], t1i, t2i, t3i};
+            for (int u = 0; u < 4; ++u) {
+                b[2 * (d0 + u * ns)] = er[u] + tr_[u]; b[2 * (d0 + u * ns) + 1] = ei[u] + ti_[u];
+                b[2 * (d0 + (u + 4) * ns)] = er[u] - tr_[u]; b[2 * (d0 + (u + 4) * ns) + 1] = ei[u] - ti_[u];
+            }
+        } else {
+            /* odd radix: pair x[q] with x[R-q] */
+            const int H = (R - 1) / 2;
+            double ar[32], ai[32], br[32], bi[32];
+            double y0r = vr[0], y0i = vi[0];
+            for (int q = 1; q <= H; ++q) {
+                ar[q] = vr[q] + vr[R - q]; ai[q] = vi[q] + vi[R - q];
+                br[q] = vr[q] - vr[R - q]; bi[q] = vi[q] - vi[R - q];
+                y0r += ar[q]; y0i += ai[q];
+            }
+            b[2 * d0] = y0r; b[2 * d0 + 1] = y0i;
+            for (int u = 1; u <= H; ++u) {
+                double Ar = vr[0], Ai = vi[0], Br = 0, Bi = 0;
+                int kk = 0;   /* (q * u) mod R, stepped without a division */
+                for (int q = 1; q <= H; ++q) {
+                    kk += u;
+                    if (kk >= R) kk -= R;
+                    Ar += ar[q] * cs[2 * kk]; Ai += ai[q] * cs[2 * kk];
+                    Br += br[q] * cs[2 * kk + 1]; Bi += bi[q] * cs[2 * kk + 1];
+                }
+                /* y[u] = A + i sign B, y[R-u] = A - i sign B */
+                const double ibr = -dsg * Bi, ibi = dsg * Br;
+                b[2 * (d0 + u * ns)] = Ar + ibr; b[2 * (d0 + u * ns) + 1] = Ai + ibi;
+                b[2 * (d0 + (R - u) * ns)] = Ar - ibr; b[2 * (d0 + (R - u) * ns) + 1] = Ai - ibi;
+            }
+        }
+    }
+}
+
 /* Iterative Stockham transform of the n values in a (interleaved re, im); b is scratch of the
  * same size.  Returns the buffer holding the result. */
 static double* fft1_fast_core(const fft_plan* p, double* a, double* b, int sign) {
-    const int n = p->n;
     const double* tws = p->st_tw[sign < 0 ? 0 : 1];
     const double dsg = sign < 0 ? -1.0 : 1.0;
     int ns = 1;
-    double vr[64], vi[64];
-    for (int s = 0; s < p->nfac; ++s) {
-        const int R = p->fac[s];
-        const int bf = n / R;
-        const double* tw = tws + 2 * p->st_off[s];
-        for (int j = 0; j < bf; ++j) {
-            const int k = j % ns;
-            for (int r = 0; r < R; ++r) {
-                vr[r] = a[2 * (j + r * bf)];
-                vi[r] = a[2 * (j + r * bf) + 1];
-            }
-            if (ns > 1) {
-                const double* w = tw + 2 * k * R;
-                for (int r = 1; r < R; ++r) {
-                    const double xr = vr[r], xi = vi[r];
-                    vr[r] = xr * w[2 * r] - xi * w[2 * r + 1];
-                    vi[r] = xr * w[2 * r + 1] + xi * w[2 * r];
-                }
-            }
-            const int d0 = (j / ns) * ns * R + k;
-            if (R == 2) {
-                b[2 * d0] = vr[0] + vr[1]; b[2 * d0 + 1] = vi[0] + vi[1];
-                b[2 * (d0 + ns)] = vr[0] - vr[1]; b[2 * (d0 + ns) + 1] = vi[0] - vi[1];
-            } else if (R == 4) {
-                const double a0r = vr[0] + vr[2], a0i = vi[0] + vi[2], a1r = vr[0] - vr[2], a1i = vi[0] - vi[2];
-                const double b0r = vr[1] + vr[3], b0i = vi[1] + vi[3];
-                /* (v1 - v3) * i sign */
-                const double tr = vr[1] - vr[3], ti = vi[1] - vi[3];
-                const double b1r = -dsg * ti, b1i = dsg * tr;
-                b[2 * d0] = a0r + b0r; b[2 * d0 + 1] = a0i + b0i;
-                b[2 * (d0 + ns)] = a1r + b1r; b[2 * (d0 + ns) + 1] = a1i + b1i;
-                b[2 * (d0 + 2 * ns)] = a0r - b0r; b[2 * (d0 + 2 * ns) + 1] = a0i - b0i;
-                b[2 * (d0 + 3 * ns)] = a1r - b1r; b[2 * (d0 + 3 * ns) + 1] = a1i - b1i;
-            } else {
-                /* odd radix: pair x[q] with x[R-q] */
-                const double* cs = p->odd_cs + 2 * p->odd_off[s];
-                const int H = (R - 1) / 2;
-                double ar[32], ai[32], br[32], bi[32];
-                double y0r = vr[0], y0i = vi[0];
-                for (int q = 1; q <= H; ++q) {
-                    ar[q] = vr[q] + vr[R - q]; ai[q] = vi[q] + vi[R - q];
-                    br[q] = vr[q] - vr[R - q]; bi[q] = vi[q] - vi[R - q];
-                    y0r += ar[q]; y0i += ai[q];
-                }
-                b[2 * d0] = y0r; b[2 * d0 + 1] = y0i;
-                for (int u = 1; u <= H; ++u) {
-                    double Ar = vr[0], Ai = vi[0], Br = 0, Bi = 0;
-                    for (int q = 1; q <= H; ++q) {
-                        const int kk = (q * u) % R;
-                        Ar += ar[q] * cs[2 * kk]; Ai += ai[q] * cs[2 * kk];
-                        Br += br[q] * cs[2 * kk + 1]; Bi += bi[q] * cs[2 * kk + 1];
-                    }
-                    /* y[u] = A + i sign B, y[R-u] = A - i sign B */
-                    const double ibr = -dsg * Bi, ibi = dsg * Br;
-                    b[2 * (d0 + u * ns)] = Ar + ibr; b[2 * (d0 + u * ns) + 1] = Ai + ibi;
-                    b[2 * (d0 + (R - u) * ns)] = Ar - ibr; b[2 * (d0 + (R - u) * ns) + 1] = Ai - ibi;
-                }
-            }
+    for (int s = 0; s < p->nffac; ++s) {
+        const int R = p->ffac[s];
+        switch (R) {
+            case 2: fast_stage(p, s, a, b, ns, 2, dsg, tws); break;
+            case 3: fast_stage(p, s, a, b, ns, 3, dsg, tws); break;
+            case 4: fast_stage(p, s, a, b, ns, 4, dsg, tws); break;
+            case 8: fast_stage(p, s, a, b, ns, 8, dsg, tws); break;
+            case 5: fast_stage(p, s, a, b, ns, 5, dsg, tws); break;
+            case 7: fast_stage(p, s, a, b, ns, 7, dsg, tws); break;
+            case 11: fast_stage(p, s, a, b, ns, 11, dsg, tws); break;
+            case 13: fast_stage(p, s, a, b, ns, 13, dsg, tws); break;
+            default: fast_stage(p, s, a, b, ns, R, dsg, tws); break;
         }
         double* t = a; a = b; b = t;
         ns *= R;
@@ -264,10 +322,10 @@ static double* fft1_fast_core(const fft_plan* p, double* a, double* b, int sign)
 /* in-place 1-D transform of x[0..n) with stride; sign<0 forward (FFTW_FORWARD) */
 static void fft1(const fft_plan* p, cplx* x, long stride, int sign, cplx* work, cplx* work2) {
     const int n = p->n;
-    if (g_fast_fft && p->nfac > 0) {
+    if (g_fast_fft && p->nffac > 0) {
         int ok = 1;
-        for (int s = 0; s < p->nfac; ++s)
-            if (p->fac[s] > 63) ok = 0;
+        for (int s = 0; s < p->nffac; ++s)
+            if (p->ffac[s] > 63) ok = 0;
         if (ok) {
             double* a = (double*)work;
             for (int i = 0; i < n; ++i) { a[2 * i] = creal(x[i * stride]); a[2 * i + 1] = cimag(x[i * stride]); }
