@@ -117,7 +117,8 @@ def workload(patches, frames, iterations):
 def cpu_port(job, cut, iterations, threads, n_patches=1):
     """FP64 restatement of the reference CPU path on `n_patches` patches, one patch at a time
     with OpenMP over images (redux's thread pool over images), its transforms by the oracle's
-    iterative Stockham FFT with precomputed tables; returns seconds."""
+    iterative Stockham FFT with precomputed tables and stages specialised per radix (radix 8
+    first); returns seconds."""
     import oracle
     t = 0.0
     finals = []
