@@ -327,6 +327,14 @@ static void fft1(const fft_plan* p, cplx* x, long stride, int sign, cplx* work, 
         for (int s = 0; s < p->nffac; ++s)
             if (p->ffac[s] > 63) ok = 0;
         if (ok) {
+            if (stride == 1) {
+                /* a contiguous line is already interleaved (re, im): transform it in place, the
+                 * scratch taking every other stage */
+                double* xa = (double*)x;
+                const double* r = fft1_fast_core(p, xa, (double*)work, sign);
+                if (r != xa) memcpy(xa, r, sizeof(double) * 2 * (size_t)n);
+                return;
+            }
             double* a = (double*)work;
             for (int i = 0; i < n; ++i) { a[2 * i] = creal(x[i * stride]); a[2 * i + 1] = cimag(x[i * stride]); }
             const double* r = fft1_fast_core(p, a, (double*)work2, sign);
